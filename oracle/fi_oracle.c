@@ -1,0 +1,1292 @@
+/*
+ * fi_oracle.c — CPU FP64 restatement of FastIsostasy's LV-ELVA hot path.
+ *
+ * TEST INFRASTRUCTURE, NOT PRODUCT CODE (see fi_oracle.h).  Each function
+ * cites the reference lines it restates (paths relative to the reference
+ * project root).  FFTW, which the reference calls for every transform, is
+ * not available; the transforms here are this file's own mixed-radix
+ * Stockham FFT, so results agree with an FFTW build to rounding (~1e-15
+ * relative), not bit for bit.
+ *
+ * Optional OpenMP (compile with -fopenmp) parallelises rows/columns of the
+ * 2-D transforms and the pointwise loops; the reference itself is serial.
+ */
+#include "fi_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define PI_LIT ((double)3.14159265359f) /* src/isostasy_defs.f90:8: default-real literal */
+#define SP(x) ((double)(float)(x))      /* single-precision literal promoted to double */
+
+void orc_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+/* ======================================================================
+ * 1-D complex FFT: self-sorting Stockham, mixed radix, any length.
+ * Stage with radix R over sub-transform size Ns: butterfly j loads
+ * x[j + r*N/R], twiddles by w^((j mod Ns)*r*N/(Ns*R)), does a radix-R DFT
+ * and stores to ((j/Ns)*Ns*R + j mod Ns) + r*Ns.
+ * ====================================================================== */
+typedef struct {
+    int n, nf, fac[40];
+    double *twr, *twi;      /* exp(-2 pi i t / n), t in [0, n) */
+} cplan;
+
+#define PLAN_CACHE 64
+static cplan *g_plans[PLAN_CACHE];
+static int g_nplans = 0;
+
+static cplan *plan_get(int n)
+{
+    cplan *p;
+    int i, m, f;
+#ifdef _OPENMP
+#pragma omp critical(orc_plan)
+#endif
+    {
+        p = NULL;
+        for (i = 0; i < g_nplans; i++)
+            if (g_plans[i]->n == n) { p = g_plans[i]; break; }
+        if (!p) {
+            p = (cplan *)calloc(1, sizeof(cplan));
+            p->n = n;
+            m = n;
+            while (m % 4 == 0) { p->fac[p->nf++] = 4; m /= 4; }
+            while (m % 2 == 0) { p->fac[p->nf++] = 2; m /= 2; }
+            for (f = 3; m > 1; f += 2)
+                while (m % f == 0) { p->fac[p->nf++] = f; m /= f; }
+            p->twr = (double *)malloc(sizeof(double) * n);
+            p->twi = (double *)malloc(sizeof(double) * n);
+            for (i = 0; i < n; i++) {
+                long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)i / (long double)n;
+                p->twr[i] = (double)cosl(a);
+                p->twi[i] = (double)sinl(a);
+            }
+            if (g_nplans < PLAN_CACHE) g_plans[g_nplans++] = p;
+        }
+    }
+    return p;
+}
+
+/* one Stockham stage; sign -1 forward, +1 backward */
+static void stockham_stage(const cplan *p, int R, int Ns, const double *xr, const double *xi,
+                           double *yr, double *yi, int sign)
+{
+    const int N = p->n, NR = N / R, tstep = N / (Ns * R);
+    double vr[64], vi[64], ur[64], ui[64];
+    double *gr = NULL, *gi = NULL;
+    int j, r, q;
+    if (R > 64) { gr = (double *)malloc(sizeof(double) * 4 * R); gi = gr + 2 * R; }
+    for (j = 0; j < NR; j++) {
+        const int jm = j % Ns;
+        const int out0 = (j / Ns) * Ns * R + jm;
+        double *ar = R > 64 ? gr : vr, *ai = R > 64 ? gi : vi;
+        double *br = R > 64 ? gr + R : ur, *bi = R > 64 ? gi + R : ui;
+        for (r = 0; r < R; r++) {
+            double a = xr[j + r * NR], b = xi[j + r * NR];
+            int t = (jm * r * tstep) % N;
+            double c = p->twr[t], s = -sign * p->twi[t];
+            ar[r] = a * c - b * s;
+            ai[r] = a * s + b * c;
+        }
+        if (R == 2) {
+            br[0] = ar[0] + ar[1]; bi[0] = ai[0] + ai[1];
+            br[1] = ar[0] - ar[1]; bi[1] = ai[0] - ai[1];
+        } else if (R == 4) {
+            double s0r = ar[0] + ar[2], s0i = ai[0] + ai[2];
+            double d0r = ar[0] - ar[2], d0i = ai[0] - ai[2];
+            double s1r = ar[1] + ar[3], s1i = ai[1] + ai[3];
+            double d1r = ar[1] - ar[3], d1i = ai[1] - ai[3];
+            /* multiply d1 by -i*sign... forward (sign=-1): d1 * (-i) */
+            double er = sign < 0 ? d1i : -d1i, ei = sign < 0 ? -d1r : d1r;
+            br[0] = s0r + s1r; bi[0] = s0i + s1i;
+            br[2] = s0r - s1r; bi[2] = s0i - s1i;
+            br[1] = d0r + er;  bi[1] = d0i + ei;
+            br[3] = d0r - er;  bi[3] = d0i - ei;
+        } else {
+            /* generic radix: direct DFT with the root table of n */
+            const int step = N / R;
+            for (q = 0; q < R; q++) {
+                double sr = 0.0, si = 0.0;
+                for (r = 0; r < R; r++) {
+                    int t = ((r * q) % R) * step;
+                    double c = p->twr[t], s = -sign * p->twi[t];
+                    sr += ar[r] * c - ai[r] * s;
+                    si += ar[r] * s + ai[r] * c;
+                }
+                br[q] = sr; bi[q] = si;
+            }
+        }
+        for (r = 0; r < R; r++) {
+            yr[out0 + r * Ns] = br[r];
+            yi[out0 + r * Ns] = bi[r];
+        }
+    }
+    free(gr);
+}
+
+static void cfft_work(const cplan *p, double *re, double *im, int sign, double *wr, double *wi)
+{
+    double *xr = re, *xi = im, *yr = wr, *yi = wi, *t;
+    int s, Ns = 1;
+    if (p->n == 1) return;
+    for (s = 0; s < p->nf; s++) {
+        stockham_stage(p, p->fac[s], Ns, xr, xi, yr, yi, sign);
+        Ns *= p->fac[s];
+        t = xr; xr = yr; yr = t;
+        t = xi; xi = yi; yi = t;
+    }
+    if (xr != re) {
+        memcpy(re, xr, sizeof(double) * p->n);
+        memcpy(im, xi, sizeof(double) * p->n);
+    }
+}
+
+void orc_cfft(int n, double *re, double *im, int sign)
+{
+    const cplan *p = plan_get(n);
+    double *w = (double *)malloc(sizeof(double) * 2 * n);
+    cfft_work(p, re, im, sign < 0 ? -1 : 1, w, w + n);
+    free(w);
+}
+
+/* ======================================================================
+ * 2-D separable DHT (FFTW_DHT along both axes, unnormalised), the
+ * transform planned at src/fastisostasy.f90:140-144 and executed at
+ * src/isos_utils.f90:143-174.  Each 1-D DHT is H[k] = Re F[k] - Im F[k];
+ * two real lines go through one complex FFT (z = a + i b).
+ * ====================================================================== */
+static void dht_lines(int n, int nlines, double *data, int stride_elem, int stride_line)
+{
+    /* data: nlines lines of n samples; element e of line l at data[l*stride_line + e*stride_elem] */
+    const cplan *p = plan_get(n);
+    int l;
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+    {
+        double *zr = (double *)malloc(sizeof(double) * 4 * n);
+        double *zi = zr + n, *wr = zr + 2 * n, *wi = zr + 3 * n;
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (l = 0; l < nlines; l += 2) {
+            const int two = (l + 1 < nlines);
+            double *a = data + (size_t)l * stride_line;
+            double *b = data + (size_t)(l + 1) * stride_line;
+            int k;
+            for (k = 0; k < n; k++) {
+                zr[k] = a[(size_t)k * stride_elem];
+                zi[k] = two ? b[(size_t)k * stride_elem] : 0.0;
+            }
+            cfft_work(p, zr, zi, -1, wr, wi);
+            for (k = 0; k < n; k++) {
+                int mk = k ? n - k : 0;
+                double Ha = 0.5 * (zr[k] + zr[mk] - zi[k] + zi[mk]);
+                double Hb = 0.5 * (zi[k] + zi[mk] + zr[k] - zr[mk]);
+                a[(size_t)k * stride_elem] = Ha;
+                if (two) b[(size_t)k * stride_elem] = Hb;
+            }
+        }
+        free(zr);
+    }
+}
+
+void orc_dht2d(int nx, int ny, const double *in, double *out)
+{
+    if (out != in) memcpy(out, in, sizeof(double) * (size_t)nx * ny);
+    dht_lines(nx, ny, out, 1, nx);   /* along x: lines are rows j */
+    dht_lines(ny, nx, out, nx, 1);   /* along y: lines are columns i */
+}
+
+/* ======================================================================
+ * Real 2-D transforms for the zero-padded convolution
+ * (src/convolutions.f90:59-108; r2c/c2r plans src/fastisostasy.f90:146-150).
+ * Half spectrum along x: spec[l*(M/2+1) + k], k in [0, M/2], l in [0, M).
+ * ====================================================================== */
+static void r2c_2d(int M, const double *real, double *sr, double *si)
+{
+    const int H = M / 2 + 1;
+    const cplan *p = plan_get(M);
+    int j, k;
+    /* rows (pairs) */
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+    {
+        double *zr = (double *)malloc(sizeof(double) * 4 * M);
+        double *zi = zr + M, *wr = zr + 2 * M, *wi = zr + 3 * M;
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (j = 0; j < M; j += 2) {
+            const int two = (j + 1 < M);
+            const double *a = real + (size_t)j * M, *b = real + (size_t)(j + 1) * M;
+            int kk;
+            for (kk = 0; kk < M; kk++) { zr[kk] = a[kk]; zi[kk] = two ? b[kk] : 0.0; }
+            cfft_work(p, zr, zi, -1, wr, wi);
+            for (kk = 0; kk < H; kk++) {
+                int mk = kk ? M - kk : 0;
+                /* Xa = (Z[k] + conj Z[-k]) / 2, Xb = (Z[k] - conj Z[-k]) / 2i */
+                sr[(size_t)j * H + kk] = 0.5 * (zr[kk] + zr[mk]);
+                si[(size_t)j * H + kk] = 0.5 * (zi[kk] - zi[mk]);
+                if (two) {
+                    sr[(size_t)(j + 1) * H + kk] = 0.5 * (zi[kk] + zi[mk]);
+                    si[(size_t)(j + 1) * H + kk] = -0.5 * (zr[kk] - zr[mk]);
+                }
+            }
+        }
+        /* columns: complex FFT of length M for each k */
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (k = 0; k < H; k++) {
+            int l;
+            for (l = 0; l < M; l++) { zr[l] = sr[(size_t)l * H + k]; zi[l] = si[(size_t)l * H + k]; }
+            cfft_work(p, zr, zi, -1, wr, wi);
+            for (l = 0; l < M; l++) { sr[(size_t)l * H + k] = zr[l]; si[(size_t)l * H + k] = zi[l]; }
+        }
+        free(zr);
+    }
+}
+
+static void c2r_2d(int M, double *sr, double *si, double *real)
+{
+    const int H = M / 2 + 1;
+    const cplan *p = plan_get(M);
+    int j, k;
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+    {
+        double *zr = (double *)malloc(sizeof(double) * 4 * M);
+        double *zi = zr + M, *wr = zr + 2 * M, *wi = zr + 3 * M;
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (k = 0; k < H; k++) {
+            int l;
+            for (l = 0; l < M; l++) { zr[l] = sr[(size_t)l * H + k]; zi[l] = si[(size_t)l * H + k]; }
+            cfft_work(p, zr, zi, +1, wr, wi);
+            for (l = 0; l < M; l++) { sr[(size_t)l * H + k] = zr[l]; si[(size_t)l * H + k] = zi[l]; }
+        }
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (j = 0; j < M; j += 2) {
+            const int two = (j + 1 < M);
+            int kk;
+            /* full Hermitian rows Xa, Xb; z = Xa + i Xb; x_a = Re ifft(z), x_b = Im ifft(z) */
+            for (kk = 0; kk < M; kk++) {
+                int src = kk < H ? kk : M - kk;
+                double ar = sr[(size_t)j * H + src], ai = si[(size_t)j * H + src];
+                double br = two ? sr[(size_t)(j + 1) * H + src] : 0.0;
+                double bi = two ? si[(size_t)(j + 1) * H + src] : 0.0;
+                if (kk >= H) { ai = -ai; bi = -bi; }
+                /* FFTW's c2r ignores the imaginary parts of the self-conjugate bins */
+                if (kk == 0 || (M % 2 == 0 && kk == M / 2)) { ai = 0.0; bi = 0.0; }
+                zr[kk] = ar - bi;
+                zi[kk] = ai + br;
+            }
+            cfft_work(p, zr, zi, +1, wr, wi);
+            for (kk = 0; kk < M; kk++) {
+                real[(size_t)j * M + kk] = zr[kk];
+                if (two) real[(size_t)(j + 1) * M + kk] = zi[kk];
+            }
+        }
+        free(zr);
+    }
+}
+
+/* precompute_kernel, src/convolutions.f90:93-108: zero-pad (nx, ny) into
+ * (M, M) at the origin and take the r2c transform. */
+void orc_kernel_spectrum(int nx, int ny, int M, const double *kernel, double *spec_re, double *spec_im)
+{
+    double *ext = (double *)calloc((size_t)M * M, sizeof(double));
+    int i, j;
+    for (j = 0; j < ny; j++)
+        for (i = 0; i < nx; i++) ext[(size_t)j * M + i] = kernel[(size_t)j * nx + i];
+    r2c_2d(M, ext, spec_re, spec_im);
+    free(ext);
+}
+
+/* apply_zerobc_at_corners[_dp], src/isos_utils.f90:104-118 */
+static void zerobc_corners(double *x, int nx, int ny)
+{
+    const double c = 0.25 * (((x[0] + x[(size_t)(ny - 1) * nx + nx - 1]) + x[(size_t)(ny - 1) * nx]) + x[nx - 1]);
+    size_t i, n = (size_t)nx * ny;
+    for (i = 0; i < n; i++) x[i] = x[i] - c;
+}
+
+/* precomputed_fftconvolution, src/convolutions.f90:59-91, with the crop of
+ * calc_convolution_indices (:29-55) for even nx, ny (offset 0). */
+void orc_conv(double *out, int nx, int ny, int M, const double *spec_re, const double *spec_im,
+              const double *in)
+{
+    const int H = M / 2 + 1;
+    double *ext = (double *)calloc((size_t)M * M, sizeof(double));
+    double *sr = (double *)malloc(sizeof(double) * (size_t)M * H);
+    double *si = (double *)malloc(sizeof(double) * (size_t)M * H);
+    const int i1 = nx / 2, j1 = ny / 2;   /* 1-based start of the crop */
+    size_t e;
+    int i, j;
+    for (j = 0; j < ny; j++)
+        for (i = 0; i < nx; i++) ext[(size_t)j * M + i] = in[(size_t)j * nx + i];
+    r2c_2d(M, ext, sr, si);
+    for (e = 0; e < (size_t)M * H; e++) {
+        double a = spec_re[e], b = spec_im[e], c = sr[e], d = si[e];
+        sr[e] = a * c - b * d;
+        si[e] = a * d + b * c;
+    }
+    c2r_2d(M, sr, si, ext);
+    {
+        const double norm = (double)M * (double)M;   /* nx*ny*1._wp, isos_utils.f90:214 */
+        for (e = 0; e < (size_t)M * M; e++) ext[e] = ext[e] / norm;
+    }
+    zerobc_corners(ext, M, M);
+    for (j = 0; j < ny; j++)
+        for (i = 0; i < nx; i++)
+            out[(size_t)j * nx + i] = ext[(size_t)(j1 - 1 + j) * M + (i1 - 1 + i)];
+    free(ext); free(sr); free(si);
+}
+
+void orc_rfft2_conv(int nx, int ny, int M, const double *kspec_re, const double *kspec_im,
+                    const double *in, double *out)
+{
+    orc_conv(out, nx, ny, M, kspec_re, kspec_im, in);
+}
+
+/* ======================================================================
+ * Finite differences, src/finite_differences.f90:17-120.
+ * dx, dy are per-cell matrices (dx*K).  Note the quirk at :91: the last
+ * x row of u_xx divides by dx(1,:)**2.
+ * ====================================================================== */
+#define IX(i, j) ((size_t)(j) * nx + (i))
+
+void orc_derivative_x(double *d, const double *u, const double *dx, int nx, int ny)
+{
+    int i, j;
+    for (j = 0; j < ny; j++) {
+        for (i = 1; i < nx - 1; i++)
+            d[IX(i, j)] = (u[IX(i + 1, j)] - u[IX(i - 1, j)]) / (2 * dx[IX(i, j)]);
+        d[IX(nx - 1, j)] = (u[IX(nx - 1, j)] - u[IX(nx - 2, j)]) / dx[IX(nx - 1, j)];
+        d[IX(0, j)] = (u[IX(1, j)] - u[IX(0, j)]) / dx[IX(0, j)];
+    }
+}
+
+void orc_derivative_y(double *d, const double *u, const double *dy, int nx, int ny)
+{
+    int i, j;
+    for (j = 1; j < ny - 1; j++)
+        for (i = 0; i < nx; i++)
+            d[IX(i, j)] = (u[IX(i, j + 1)] - u[IX(i, j - 1)]) / (2 * dy[IX(i, j)]);
+    for (i = 0; i < nx; i++) {
+        d[IX(i, ny - 1)] = (u[IX(i, ny - 1)] - u[IX(i, ny - 2)]) / dy[IX(i, ny - 1)];
+        d[IX(i, 0)] = (u[IX(i, 1)] - u[IX(i, 0)]) / dy[IX(i, 0)];
+    }
+}
+
+void orc_derivative_xx(double *d, const double *u, const double *dx, int nx, int ny)
+{
+    int i, j;
+    for (j = 0; j < ny; j++) {
+        for (i = 1; i < nx - 1; i++)
+            d[IX(i, j)] = (u[IX(i + 1, j)] - 2 * u[IX(i, j)] + u[IX(i - 1, j)]) / (dx[IX(i, j)] * dx[IX(i, j)]);
+        d[IX(0, j)] = (u[IX(2, j)] - 2 * u[IX(1, j)] + u[IX(0, j)]) / (dx[IX(0, j)] * dx[IX(0, j)]);
+        d[IX(nx - 1, j)] = (u[IX(nx - 1, j)] - 2 * u[IX(nx - 2, j)] + u[IX(nx - 3, j)]) /
+                           (dx[IX(0, j)] * dx[IX(0, j)]);
+    }
+}
+
+void orc_derivative_yy(double *d, const double *u, const double *dy, int nx, int ny)
+{
+    int i, j;
+    for (j = 1; j < ny - 1; j++)
+        for (i = 0; i < nx; i++)
+            d[IX(i, j)] = (u[IX(i, j + 1)] - 2 * u[IX(i, j)] + u[IX(i, j - 1)]) / (dy[IX(i, j)] * dy[IX(i, j)]);
+    for (i = 0; i < nx; i++) {
+        d[IX(i, 0)] = (u[IX(i, 2)] - 2 * u[IX(i, 1)] + u[IX(i, 0)]) / (dy[IX(i, 0)] * dy[IX(i, 0)]);
+        d[IX(i, ny - 1)] = (u[IX(i, ny - 1)] - 2 * u[IX(i, ny - 2)] + u[IX(i, ny - 3)]) /
+                           (dy[IX(i, ny - 1)] * dy[IX(i, ny - 1)]);
+    }
+}
+
+/* calc_kappa, src/lv_elva.f90:442-481: note (n-1)*dx and the (1,1) average */
+void orc_kappa(double *kappa, int nx, int ny, double dx, double dy)
+{
+    const double mu_x = 2.0 * PI_LIT / ((nx - 1) * dx);
+    const double mu_y = 2.0 * PI_LIT / ((ny - 1) * dy);
+    const int ic = (nx - 1) / 2 + 1, jc = (ny - 1) / 2 + 1;
+    int i, j;
+    for (i = 1; i <= nx; i++) {
+        double p = (i <= ic) ? mu_x * (i - 1) : mu_x * (nx - i + 1);
+        for (j = 1; j <= ny; j++) {
+            double q = (j <= jc) ? mu_y * (j - 1) : mu_y * (ny - j + 1);
+            kappa[IX(i - 1, j - 1)] = pow(p * p + q * q, 0.5);
+        }
+    }
+    kappa[IX(0, 0)] = (kappa[IX(0, 1)] + kappa[IX(1, 0)]) / 2.0;
+}
+
+/* calc_lvelva, src/lv_elva.f90:31-126 (maskfield :112, src/isos_utils.f90:580-601) */
+void orc_lvelva(double *dwdt, const double *w, const double *canom_full, const uint8_t *mask,
+                double g, double nu, const double *D, const double *eta, const double *R,
+                const double *kappa, int nx, int ny, const double *dxm, const double *dym,
+                double sec_per_year)
+{
+    const size_t n = (size_t)nx * ny;
+    double *buf = (double *)malloc(sizeof(double) * n * 12);
+    double *w_x = buf, *w_xy = buf + n, *w_xx = buf + 2 * n, *w_yy = buf + 3 * n;
+    double *Mxx = buf + 4 * n, *Myy = buf + 5 * n, *Mxy = buf + 6 * n;
+    double *Mxy_x = buf + 7 * n, *Mxy_xy = buf + 8 * n, *Mx_xx = buf + 9 * n, *My_yy = buf + 10 * n;
+    double *f = buf + 11 * n;
+    size_t e;
+    orc_derivative_x(w_x, w, dxm, nx, ny);
+    orc_derivative_y(w_xy, w_x, dym, nx, ny);
+    orc_derivative_xx(w_xx, w, dxm, nx, ny);
+    orc_derivative_yy(w_yy, w, dym, nx, ny);
+    for (e = 0; e < n; e++) {
+        Mxx[e] = -D[e] * (w_xx[e] + nu * w_yy[e]);
+        Myy[e] = -D[e] * (w_yy[e] + nu * w_xx[e]);
+        Mxy[e] = -D[e] * (1.0 - nu) * w_xy[e];
+    }
+    orc_derivative_x(Mxy_x, Mxy, dxm, nx, ny);
+    orc_derivative_y(Mxy_xy, Mxy_x, dym, nx, ny);
+    orc_derivative_xx(Mx_xx, Mxx, dxm, nx, ny);
+    orc_derivative_yy(My_yy, Myy, dym, nx, ny);
+    for (e = 0; e < n; e++) {
+        double p = mask[e] ? -g * canom_full[e] : 0.0;
+        f[e] = (((p + Mx_xx[e]) + 2.0 * Mxy_xy[e]) + My_yy[e]) / (2.0 * eta[e]);
+    }
+    orc_dht2d(nx, ny, f, f);
+    for (e = 0; e < n; e++) f[e] = f[e] / (kappa[e] * R[e]);
+    orc_dht2d(nx, ny, f, f);
+    {
+        const double norm = (double)(float)(nx * ny);   /* nx*ny*1. (default real), isos_utils.f90:171 */
+        for (e = 0; e < n; e++) f[e] = f[e] / norm;
+    }
+    zerobc_corners(f, nx, ny);
+    for (e = 0; e < n; e++) dwdt[e] = f[e] * sec_per_year;
+    free(buf);
+}
+
+/* ======================================================================
+ * Green's functions, src/green_functions.f90:43-181.
+ * ====================================================================== */
+static const float RN_VALS[42] = {0.0f, 0.011f, 0.111f, 1.112f, 2.224f, 3.336f, 4.448f, 6.672f,
+    8.896f, 11.12f, 17.79f, 22.24f, 27.80f, 33.36f, 44.48f, 55.60f, 66.72f, 88.96f, 111.2f, 133.4f,
+    177.9f, 222.4f, 278.0f, 333.6f, 444.8f, 556.0f, 667.2f, 778.4f, 889.6f, 1001.0f, 1112.0f,
+    1334.0f, 1779.0f, 2224.0f, 2780.0f, 3336.0f, 4448.0f, 5560.0f, 6672.0f, 7784.0f, 8896.0f, 10008.0f};
+static const float GE_VALS[42] = {-33.6488f, -33.64f, -33.56f, -32.75f, -31.86f, -30.98f, -30.12f,
+    -28.44f, -26.87f, -25.41f, -21.80f, -20.02f, -18.36f, -17.18f, -15.71f, -14.91f, -14.41f, -13.69f,
+    -13.01f, -12.31f, -10.95f, -9.757f, -8.519f, -7.533f, -6.131f, -5.237f, -4.660f, -4.272f, -3.999f,
+    -3.798f, -3.640f, -3.392f, -2.999f, -2.619f, -2.103f, -1.530f, -0.292f, 0.848f, 1.676f, 2.083f,
+    2.057f, 1.643f};
+
+static int midindex(int n) { return (n % 2 == 0) ? n / 2 : (n - 1) / 2; }
+
+/* get_ge_value, :131-168; the rn table is multiplied by 1.e3 in single
+ * precision before promotion (:56-60). */
+static double get_ge_value(double r)
+{
+    double rn[42], ge[42];
+    int k;
+    for (k = 0; k < 42; k++) { rn[k] = (double)(RN_VALS[k] * 1.e3f); ge[k] = (double)GE_VALS[k]; }
+    if (r > rn[41]) return 0.0;
+    for (k = 0; k < 41; k++)
+        if (r >= rn[k] && r < rn[k + 1]) break;
+    if (k >= 41) k = 40;   /* r == rn(42) exactly: the reference reads past the table */
+    return ge[k] + (r - rn[k]) / (rn[k + 1] - rn[k]) * (ge[k + 1] - ge[k]);
+}
+
+/* calc_elastic_green, :43-91; called with dy = dx (src/fastisostasy.f90:175).
+ * Both axes are centred on midindex(nx) (:80-81). */
+void orc_elastic_green(double *filt, int nx, int ny, double dx, double dy)
+{
+    const int mx = midindex(nx);
+    int i, j;
+    for (j = 1; j <= ny; j++)
+        for (i = 1; i <= nx; i++) {
+            double x = (i - 1 - mx) * dx, y = (j - 1 - mx) * dy;
+            double r = sqrt(x * x + y * y);
+            filt[IX(i - 1, j - 1)] = get_ge_value(r) * SP(1.e-12) * (dx * dy) /
+                                     (SP(9.81) * (r > dx ? r : dx));
+        }
+}
+
+/* calc_z_ss_green, :94-128, with calc_gn_value :171-181 */
+void orc_zss_green(double *filt, int nx, int ny, double m_earth, double r_earth, double dx, double dy)
+{
+    const int mx = midindex(nx);
+    int i, j;
+    for (j = 1; j <= ny; j++)
+        for (i = 1; i <= nx; i++) {
+            double x = (i - 1 - mx) * dx, y = (j - 1 - mx) * dy;
+            double r = sqrt(x * x + y * y);
+            double rr = (dy / 2 > r) ? dy / 2 : r;
+            filt[IX(i - 1, j - 1)] = r_earth / (2. * m_earth * sin(rr / (2. * r_earth)));
+        }
+}
+
+/* ======================================================================
+ * Model state (src/isostasy_defs.f90:11-209)
+ * ====================================================================== */
+typedef struct {
+    double bsl, V_af, V_den, V_pov, deltaV_bsl, dbsl_total;
+    double *z_bed, *dwdt, *w, *w_eq, *we, *Haf, *Hice, *z_ss, *dz_ss;
+    double *c_ice, *c_sw, *c_litho, *c_mantle, *c_load, *c_full, *mass;
+    uint8_t *m_ocean, *m_grounded, *m_cont;
+} ostate;
+
+struct orc_model {
+    orc_params p;
+    int nx, ny, nx_ice, ny_ice, icrop1, icrop2, jcrop1, jcrop2, M;
+    double dx, dy, sec_per_year, cc, Vden, time_diag, time_prog;
+    int ref_was_set;
+    double *xc, *yc, *K, *dxm, *dym, *A, *kappa, *R, *D, *He, *eta_eff, *GE, *GN;
+    double *FGEr, *FGEi, *FGNr, *FGNi;
+    uint8_t *maskactive;
+    ostate now, ref;
+    /* ode_class */
+    double t, dt;
+    double *x, *k[7], *y, *x1, *x2;
+    long n_rhs, n_accept, n_reject;
+    int fsal_valid;
+};
+
+static double *dalloc(size_t n) { return (double *)calloc(n, sizeof(double)); }
+
+static void state_alloc(ostate *s, size_t n)
+{
+    s->z_bed = dalloc(n); s->dwdt = dalloc(n); s->w = dalloc(n); s->w_eq = dalloc(n);
+    s->we = dalloc(n); s->Haf = dalloc(n); s->Hice = dalloc(n); s->z_ss = dalloc(n);
+    s->dz_ss = dalloc(n); s->c_ice = dalloc(n); s->c_sw = dalloc(n); s->c_litho = dalloc(n);
+    s->c_mantle = dalloc(n); s->c_load = dalloc(n); s->c_full = dalloc(n); s->mass = dalloc(n);
+    s->m_ocean = (uint8_t *)calloc(n, 1); s->m_grounded = (uint8_t *)calloc(n, 1);
+    s->m_cont = (uint8_t *)calloc(n, 1);
+}
+
+static void state_free(ostate *s)
+{
+    free(s->z_bed); free(s->dwdt); free(s->w); free(s->w_eq); free(s->we); free(s->Haf);
+    free(s->Hice); free(s->z_ss); free(s->dz_ss); free(s->c_ice); free(s->c_sw); free(s->c_litho);
+    free(s->c_mantle); free(s->c_load); free(s->c_full); free(s->mass); free(s->m_ocean);
+    free(s->m_grounded); free(s->m_cont);
+}
+
+/* zero_init_state, src/fastisostasy.f90:505-548 */
+static void zero_init_state(ostate *s, size_t n, double z_bed_background)
+{
+    size_t e;
+    for (e = 0; e < n; e++) s->z_bed[e] = z_bed_background;
+    s->bsl = s->deltaV_bsl = s->dbsl_total = s->V_af = s->V_den = s->V_pov = 0.0;
+}
+
+/* calc_gaussian_thickness, src/isos_utils.f90:997-1035 */
+static void gaussian_thickness(double *He, int nx, int ny, double He0, double He1, double sign,
+                               const double *xc, const double *yc)
+{
+    const double xmin = xc[0], xmax = xc[nx - 1], ymin = yc[0], ymax = yc[ny - 1];
+    const double xcntr = (xmax + xmin) / 2.0, ycntr = (ymax + ymin) / 2.0;
+    const double Lx = (xmax - xmin) / 2., Ly = (ymax - ymin) / 2.;
+    const double s11 = (4.0 / Lx) * (4.0 / Lx), s22 = (4.0 / Ly) * (4.0 / Ly);
+    double mx = -1e300;
+    size_t e, n = (size_t)nx * ny;
+    int i, j;
+    for (i = 0; i < nx; i++)
+        for (j = 0; j < ny; j++) {
+            double d1 = xc[i] - xcntr, d2 = yc[j] - ycntr;
+            double v = exp(-0.5 * (d1 * (s11 * d1 + 0.0 * d2) + d2 * (0.0 * d1 + s22 * d2)));
+            He[IX(i, j)] = v;
+        }
+    for (e = 0; e < n; e++) if (He[e] > mx) mx = He[e];
+    for (e = 0; e < n; e++) He[e] = He[e] / mx;
+    for (e = 0; e < n; e++) He[e] = He0 + sign * He1 * He[e];
+}
+
+/* calc_gaussian_viscosity, src/isos_utils.f90:960-995 */
+static void gaussian_viscosity(double *eta, int nx, int ny, double eta0, double sign,
+                               const double *xc, const double *yc)
+{
+    const double xmin = xc[0], xmax = xc[nx - 1], ymin = yc[0], ymax = yc[ny - 1];
+    const double xcntr = (xmax + xmin) / 2.0, ycntr = (ymax + ymin) / 2.0;
+    const double Lx = (xmax - xmin) / 2., Ly = (ymax - ymin) / 2.;
+    const double s11 = (4.0 / Lx) * (4.0 / Lx), s22 = (4.0 / Ly) * (4.0 / Ly);
+    int i, j;
+    for (i = 0; i < nx; i++)
+        for (j = 0; j < ny; j++) {
+            double d1 = xc[i] - xcntr, d2 = yc[j] - ycntr;
+            double f = exp(-0.5 * (d1 * (s11 * d1 + 0.0 * d2) + d2 * (0.0 * d1 + s22 * d2)));
+            eta[IX(i, j)] = eta0 * pow(10.0, sign * f);
+        }
+}
+
+/* calc_heterogeneous_rigidity, src/isos_utils.f90:79-100 */
+static double rigidity(double E, double He, double nu)
+{
+    return E * 1e9 * (He * He * He) / (12.0 * (1.0 - nu * nu));
+}
+
+orc_model *orc_create(const orc_params *p, int nx_ice, int ny_ice, double dx, double dy,
+                      const double *K_or_null)
+{
+    orc_model *m;
+    int nx_tmp, ny_tmp, npx, npy, i, j, k;
+    size_t n, e;
+    if (p->method != 3 || dx != dy || p->min_pad < 0.0 || p->nl < 1 || p->nl > 8) return NULL;
+    m = (orc_model *)calloc(1, sizeof(orc_model));
+    m->p = *p;
+    /* init_domain_size, src/isos_utils.f90:285-354 */
+    m->dx = dx; m->dy = dy; m->nx_ice = nx_ice; m->ny_ice = ny_ice;
+    m->icrop1 = 1; m->jcrop1 = 1;
+    nx_tmp = nx_ice; ny_tmp = ny_ice;
+    if (nx_ice % 2) { m->icrop1++; nx_tmp++; }
+    if (ny_ice % 2) { m->jcrop1++; ny_tmp++; }
+    if (p->nx_target > 0 && p->ny_target > 0) {
+        /* rectangular generalisation: explicit even target sizes, centred */
+        if (p->nx_target < nx_tmp || p->ny_target < ny_tmp || (p->nx_target - nx_tmp) % 2 ||
+            (p->ny_target - ny_tmp) % 2) { free(m); return NULL; }
+        npx = (p->nx_target - nx_tmp) / 2;
+        npy = (p->ny_target - ny_tmp) / 2;
+        m->nx = p->nx_target; m->ny = p->ny_target;
+    } else {
+        int npxy = (int)lround(p->min_pad / dx);
+        npx = npy = npxy;
+        if (nx_tmp < ny_tmp) npx += (ny_tmp - nx_tmp) / 2;
+        else if (nx_tmp > ny_tmp) npy += (nx_tmp - ny_tmp) / 2;
+        m->nx = nx_tmp + 2 * npx;
+        m->ny = ny_tmp + 2 * npy;
+        if (m->nx != m->ny) { free(m); return NULL; }
+    }
+    m->icrop1 += npx; m->icrop2 = m->nx - npx;
+    m->jcrop1 += npy; m->jcrop2 = m->ny - npy;
+    m->M = 2 * (m->nx > m->ny ? m->nx : m->ny) - 1;
+    n = (size_t)m->nx * m->ny;
+    {
+        const int nx = m->nx, ny = m->ny;
+        m->xc = dalloc(nx); m->yc = dalloc(ny);
+        /* init_dims, src/isos_utils.f90:221-240 */
+        for (i = 1; i <= nx; i++) m->xc[i - 1] = (i - nx / 2 - 1) * dx;
+        for (j = 1; j <= ny; j++) m->yc[j - 1] = (j - ny / 2 - 1) * dy;
+        m->K = dalloc(n); m->dxm = dalloc(n); m->dym = dalloc(n); m->A = dalloc(n);
+        m->kappa = dalloc(n); m->R = dalloc(n); m->D = dalloc(n); m->He = dalloc(n);
+        m->eta_eff = dalloc(n); m->GE = dalloc(n); m->GN = dalloc(n);
+        m->maskactive = (uint8_t *)calloc(n, 1);
+        for (e = 0; e < n; e++) { m->R[e] = 1.0; m->K[e] = K_or_null ? K_or_null[e] : 1.0; }
+        /* src/fastisostasy.f90:152-164 */
+        for (e = 0; e < n; e++) {
+            m->dxm[e] = dx * m->K[e];
+            m->dym[e] = dy * m->K[e];
+            m->A[e] = m->dxm[e] * m->dym[e];
+        }
+        m->sec_per_year = (double)(3600.0f * 24.0f * 365.25f);
+        m->cc = p->correct_compression ? 1.5 / (1 + p->nu) : 1.0;
+        m->Vden = p->rho_ice / p->rho_water - p->rho_ice / p->rho_seawater;
+        /* lithosphere, :166-172 */
+        for (e = 0; e < n; e++) { m->He[e] = p->zl[0]; m->D[e] = rigidity(p->E, p->zl[0], p->nu); }
+        /* Green's functions + spectra, :174-183 */
+        orc_elastic_green(m->GE, nx, ny, dx, dx);
+        orc_zss_green(m->GN, nx, ny, p->m_earth, p->r_earth, dx, dx);
+        {
+            const size_t hs = (size_t)m->M * (m->M / 2 + 1);
+            m->FGEr = dalloc(hs); m->FGEi = dalloc(hs); m->FGNr = dalloc(hs); m->FGNi = dalloc(hs);
+            orc_kernel_spectrum(nx, ny, m->M, m->GE, m->FGEr, m->FGEi);
+            orc_kernel_spectrum(nx, ny, m->M, m->GN, m->FGNr, m->FGNi);
+        }
+        /* maskactive, :185-214 (mask files arrive through orc_set_fields) */
+        if (!p->interactive_sealevel) {
+            for (e = 0; e < n; e++) m->maskactive[e] = 1;
+        } else if (p->min_pad > SP(100.e3)) {
+            for (j = m->jcrop1; j <= m->jcrop2; j++)
+                for (i = m->icrop1; i <= m->icrop2; i++) m->maskactive[IX(i - 1, j - 1)] = 1;
+        }
+        /* method 3, :240-443 */
+        orc_kappa(m->kappa, nx, ny, m->dx, m->dy);
+        if (p->lithosphere == 1 || p->lithosphere == 2) {
+            gaussian_thickness(m->He, nx, ny, p->zl[0], SP(100e3), p->lithosphere == 1 ? 1.0 : -1.0,
+                               m->xc, m->yc);
+            for (e = 0; e < n; e++) m->D[e] = rigidity(p->E, m->He[e], p->nu);
+        }
+        {
+            const int nl = p->nl;
+            double *bnd = dalloc(n * nl), *eta = dalloc(n * nl);
+            for (e = 0; e < n; e++) bnd[e] = m->He[e];
+            for (k = 1; k < nl; k++)
+                for (e = 0; e < n; e++)
+                    bnd[k * n + e] = (p->layering == 1) ? bnd[(k - 1) * n + e] + p->dl : p->zl[k];
+            for (k = 0; k < nl; k++)
+                for (e = 0; e < n; e++) eta[k * n + e] = p->viscosities[k];
+            if (p->mantle == 0) {
+                /* calc_effective_viscosity, src/lv_elva.f90:207-237 */
+                for (e = 0; e < n; e++) {
+                    double v = eta[(nl - 1) * n + e], mn = eta[e], mxv = eta[e], s = 0.0, ls = 0.0;
+                    for (k = 0; k < nl; k++) {
+                        double ek = eta[k * n + e];
+                        if (ek < mn) mn = ek;
+                        if (ek > mxv) mxv = ek;
+                        s += ek; ls += log10(ek);
+                    }
+                    switch (p->lumping) {
+                    case 0: m->eta_eff[e] = v; break;
+                    case 1: m->eta_eff[e] = mn; break;
+                    case 2: m->eta_eff[e] = mxv; break;
+                    case 3: m->eta_eff[e] = s / (double)nl; break;
+                    case 4: m->eta_eff[e] = pow(10.0, ls / (double)nl); break;
+                    default: m->eta_eff[e] = v; break;
+                    }
+                }
+                if (p->lumping == 5 && nl > 1) {
+                    /* calc_viscosity_scaling_freqdomain, src/lv_elva.f90:239-306 */
+                    for (k = nl - 1; k >= 1; k--)
+                        for (e = 0; e < n; e++) {
+                            double dz = bnd[k * n + e] - bnd[(k - 1) * n + e];
+                            double er = eta[(k - 1) * n + e] / m->eta_eff[e];
+                            double ir = 1. / er;
+                            double kz = dz * m->kappa[e];
+                            double c = cosh(kz), s = sinh(kz);
+                            m->R[e] = m->R[e] * (2 * er * c * s + (1 - er * er) * (kz * kz) + (er * s) * (er * s) + c * c) /
+                                      ((er + ir) * c * s + (er - ir) * dz * m->kappa[e] + s * s + c * c);
+                        }
+                }
+            } else if (p->mantle == 1 || p->mantle == 2) {
+                /* gaussian_plus passes yc = xc (src/fastisostasy.f90:329-330) */
+                gaussian_viscosity(m->eta_eff, nx, ny, p->viscosities[0], p->mantle == 1 ? 1.0 : -1.0,
+                                   m->xc, p->mantle == 1 ? m->xc : m->yc);
+            } else {
+                for (e = 0; e < n; e++) m->eta_eff[e] = p->viscosities[nl - 1];
+            }
+            free(bnd); free(eta);
+        }
+        /* viscosity scaling, :425-436 */
+        if (p->visc_scaling_method == 2 || p->visc_scaling_method == 3) {
+            double v = m->eta_eff[0];
+            for (e = 0; e < n; e++)
+                v = (p->visc_scaling_method == 2) ? (m->eta_eff[e] < v ? m->eta_eff[e] : v)
+                                                   : (m->eta_eff[e] > v ? m->eta_eff[e] : v);
+            for (e = 0; e < n; e++) m->eta_eff[e] = v;
+        } else if (p->visc_scaling_method == 1) {
+            for (e = 0; e < n; e++) m->eta_eff[e] = m->eta_eff[e] * p->viscosity_scaling;
+        }
+        /* :438-442, including the exp(log10(.)) quirk */
+        for (e = 0; e < n; e++) m->eta_eff[e] = m->eta_eff[e] * m->cc;
+        for (e = 0; e < n; e++) m->eta_eff[e] = exp(log10(p->eta_ref / m->eta_eff[e])) * m->eta_eff[e];
+    }
+    m->time_diag = SP(1e10); m->time_prog = SP(1e10);
+    state_alloc(&m->now, n); state_alloc(&m->ref, n);
+    zero_init_state(&m->now, n, 1e6); zero_init_state(&m->ref, n, 1e6);
+    m->ref_was_set = 0;
+    m->x = dalloc(n); m->y = dalloc(n); m->x1 = dalloc(n); m->x2 = dalloc(n);
+    for (k = 0; k < 7; k++) m->k[k] = dalloc(n);
+    m->t = 0.0; m->dt = 0.0;   /* ode_class is zero before isos_init_state sets it */
+    return m;
+}
+
+void orc_destroy(orc_model *m)
+{
+    int k;
+    if (!m) return;
+    free(m->xc); free(m->yc); free(m->K); free(m->dxm); free(m->dym); free(m->A); free(m->kappa);
+    free(m->R); free(m->D); free(m->He); free(m->eta_eff); free(m->GE); free(m->GN);
+    free(m->FGEr); free(m->FGEi); free(m->FGNr); free(m->FGNi); free(m->maskactive);
+    state_free(&m->now); state_free(&m->ref);
+    free(m->x); free(m->y); free(m->x1); free(m->x2);
+    for (k = 0; k < 7; k++) free(m->k[k]);
+    free(m);
+}
+
+int orc_dims(const orc_model *m, int32_t *o)
+{
+    o[0] = m->nx; o[1] = m->ny; o[2] = m->icrop1; o[3] = m->icrop2; o[4] = m->jcrop1;
+    o[5] = m->jcrop2; o[6] = m->nx_ice; o[7] = m->ny_ice;
+    return 0;
+}
+
+/* Caller-provided fields (rheology-file and mask-file paths of isos_init,
+ * or fields computed by the caller).  eta_eff is taken as final (after the
+ * scaling and compressibility transforms). */
+int orc_set_fields(orc_model *m, const double *D, const double *eta_eff, const double *R,
+                   const uint8_t *maskactive)
+{
+    const size_t n = (size_t)m->nx * m->ny;
+    if (D) memcpy(m->D, D, n * sizeof(double));
+    if (eta_eff) memcpy(m->eta_eff, eta_eff, n * sizeof(double));
+    if (R) memcpy(m->R, R, n * sizeof(double));
+    if (maskactive) memcpy(m->maskactive, maskactive, n);
+    return 0;
+}
+
+/* out2in, src/isos_utils.f90:376-384 */
+static void out2in(const orc_model *m, double *X_in, const double *X_out)
+{
+    int i, j;
+    const int nxi = m->icrop2 - m->icrop1 + 1, nyi = m->jcrop2 - m->jcrop1 + 1;
+    const int nx = m->nx;
+    for (j = 0; j < nyi; j++)
+        for (i = 0; i < nxi; i++)
+            X_in[IX(m->icrop1 - 1 + i, m->jcrop1 - 1 + j)] = X_out[(size_t)j * nxi + i];
+}
+
+int orc_init_ref(orc_model *m, const double *z_bed, const double *H_ice, double bsl,
+                 const double *dz_ss_or_null)
+{
+    /* isos_init_ref, src/fastisostasy.f90:550-575 */
+    const size_t n = (size_t)m->nx * m->ny;
+    size_t e;
+    for (e = 0; e < n; e++) { m->ref.z_bed[e] = 1e6; m->ref.Hice[e] = 0.0; }
+    out2in(m, m->ref.z_bed, z_bed);
+    out2in(m, m->ref.Hice, H_ice);
+    m->ref.bsl = bsl;
+    if (dz_ss_or_null) memcpy(m->ref.dz_ss, dz_ss_or_null, n * sizeof(double));
+    m->ref_was_set = 1;
+    return 0;
+}
+
+/* ---- sea level, src/sealevel.f90 ---- */
+static void calc_z_ss(double *z_ss, double bsl, const double *z_ss_ref, const double *dz_ss, size_t n)
+{
+    size_t e;
+    for (e = 0; e < n; e++) z_ss[e] = (bsl + z_ss_ref[e]) + dz_ss[e];
+}
+
+static void calc_Haf(ostate *s, const orc_params *p, size_t n)
+{
+    size_t e;
+    for (e = 0; e < n; e++) {
+        double h = (s->z_ss[e] - s->z_bed[e]) * (p->rho_seawater / p->rho_ice);
+        if (h < 0.0) h = 0.0;
+        h = s->Hice[e] - h;
+        if (h < 0.0) h = 0.0;
+        s->Haf[e] = h;
+    }
+}
+
+static void calc_masks(ostate *s, size_t n)
+{
+    size_t e;
+    for (e = 0; e < n; e++) {
+        s->m_cont[e] = s->z_bed[e] > s->z_ss[e];
+        s->m_grounded[e] = (s->Hice[e] > 0.0) && (s->Haf[e] > 0.0);
+        s->m_ocean[e] = !(s->m_cont[e] || s->m_grounded[e]);
+    }
+}
+
+static void canom_ice(orc_model *m, size_t n)
+{
+    size_t e;
+    for (e = 0; e < n; e++) m->now.c_ice[e] = 0.0 + m->p.rho_ice * (m->now.Haf[e] - m->ref.Haf[e]);
+}
+
+static void canom_seawater(orc_model *m, size_t n)
+{
+    size_t e;
+    for (e = 0; e < n; e++)
+        m->now.c_sw[e] = 0.0 + (m->now.m_ocean[e] ? m->p.rho_water * (m->now.z_ss[e] - m->ref.z_ss[e]) : 0.0);
+}
+
+static void canom_load(orc_model *m, size_t n)
+{
+    size_t e;
+    for (e = 0; e < n; e++) {
+        double v = m->now.c_ice[e];
+        if (m->p.interactive_sealevel) v = v + m->now.c_sw[e];
+        m->now.c_load[e] = m->maskactive[e] ? v : 0.0;
+    }
+}
+
+static void canom_litho(orc_model *m, size_t n)
+{
+    size_t e;
+    for (e = 0; e < n; e++) m->now.c_litho[e] = 0.0 + m->p.rho_litho * (m->now.we[e] - m->ref.we[e]);
+}
+
+static void canom_mantle(orc_model *m, size_t n)
+{
+    size_t e;
+    for (e = 0; e < n; e++) m->now.c_mantle[e] = 0.0 + m->p.rho_uppermantle * (m->now.w[e] - m->ref.w[e]);
+}
+
+static void canom_full(orc_model *m, size_t n)
+{
+    size_t e;
+    for (e = 0; e < n; e++)
+        m->now.c_full[e] = m->maskactive[e] ? (m->now.c_load[e] + m->now.c_litho[e]) + m->now.c_mantle[e] : 0.0;
+}
+
+static void mass_anom(orc_model *m, size_t n)
+{
+    size_t e;
+    for (e = 0; e < n; e++) m->now.mass[e] = m->maskactive[e] ? m->A[e] * m->now.c_full[e] : 0.0;
+}
+
+/* calc_sl_contributions, src/sealevel.f90:189-205: sequential sums in
+ * column-major order like gfortran's sum() */
+static void sl_contributions(orc_model *m, size_t n)
+{
+    double V_old = (m->now.V_af + m->now.V_den) + m->now.V_pov, s1 = 0.0, s2 = 0.0;
+    size_t e;
+    for (e = 0; e < n; e++) s1 += (m->now.Haf[e] - m->ref.Haf[e]) * m->A[e];
+    for (e = 0; e < n; e++) s2 += ((m->now.Hice[e] - m->ref.Hice[e]) * m->Vden) * m->A[e];
+    m->now.V_af = s1 * (m->p.rho_ice / m->p.rho_seawater);
+    m->now.V_den = s2;
+    m->now.V_pov = 0.0;
+    m->now.deltaV_bsl = ((m->now.V_af + m->now.V_den) + m->now.V_pov) - V_old;
+}
+
+/* ---- RHS: get_dwdt, src/fastisostasy.f90:677-729 ---- */
+static void rhs_eval(orc_model *m, const double *state, double *dwdt)
+{
+    const size_t n = (size_t)m->nx * m->ny;
+    double *cf = m->y == state ? dalloc(n) : m->y;   /* scratch for canom_full */
+    size_t e;
+    if (m->p.stage_mode == 0) {
+        /* reference: canom_full from the frozen anomalies, w = now%w */
+        canom_full(m, n);
+        orc_lvelva(m->now.dwdt, m->now.w, m->now.c_full, m->maskactive, m->p.g, m->p.nu, m->D,
+                   m->eta_eff, m->R, m->kappa, m->nx, m->ny, m->dxm, m->dym, m->sec_per_year);
+        if (dwdt != m->now.dwdt) memcpy(dwdt, m->now.dwdt, n * sizeof(double));
+    } else {
+        /* true stages: mantle anomaly evaluated at the stage state */
+        for (e = 0; e < n; e++)
+            cf[e] = m->maskactive[e]
+                        ? (m->now.c_load[e] + m->now.c_litho[e]) + m->p.rho_uppermantle * (state[e] - m->ref.w[e])
+                        : 0.0;
+        orc_lvelva(dwdt, state, cf, m->maskactive, m->p.g, m->p.nu, m->D, m->eta_eff, m->R,
+                   m->kappa, m->nx, m->ny, m->dxm, m->dym, m->sec_per_year);
+        memcpy(m->now.dwdt, dwdt, n * sizeof(double));
+    }
+    if (cf != m->y) free(cf);
+    m->n_rhs++;
+}
+
+void orc_rhs_now(orc_model *m, double *dwdt) { rhs_eval(m, m->now.w, dwdt); }
+
+static double maxabs(const double *a, size_t n)
+{
+    double v = 0.0;
+    size_t e;
+    for (e = 0; e < n; e++) { double t = fabs(a[e]); if (t > v || t != t) v = t; }
+    return v;
+}
+
+/* ---- integrators, src/integrators.f90 ---- */
+static int step_euler(orc_model *m, double tf)
+{
+    const size_t n = (size_t)m->nx * m->ny;
+    size_t e;
+    while (m->t < tf) {
+        m->dt = fmin(m->dt, tf - m->t);
+        rhs_eval(m, m->p.stage_mode ? m->x : m->now.w, m->k[0]);
+        for (e = 0; e < n; e++) m->x[e] = m->x[e] + m->dt * m->k[0][e];
+        memcpy(m->now.w, m->x, n * sizeof(double));
+        m->t = m->t + m->dt;
+        m->n_accept++;
+    }
+    return 0;
+}
+
+static int step_rk4(orc_model *m, double tf)
+{
+    const size_t n = (size_t)m->nx * m->ny;
+    size_t e;
+    while (m->t < tf) {
+        const double h = fmin(m->dt, tf - m->t);
+        if (m->p.stage_mode == 0) {
+            /* get_dwdt ignores its argument: all four stages see now%w */
+            int s;
+            rhs_eval(m, m->now.w, m->k[0]);
+            for (s = 1; s < 4; s++) { rhs_eval(m, m->now.w, m->k[s]); }
+        } else {
+            double *yy = m->x1;
+            rhs_eval(m, m->x, m->k[0]);
+            for (e = 0; e < n; e++) yy[e] = m->x[e] + (0.5 * h) * m->k[0][e];
+            rhs_eval(m, yy, m->k[1]);
+            for (e = 0; e < n; e++) yy[e] = m->x[e] + (0.5 * h) * m->k[1][e];
+            rhs_eval(m, yy, m->k[2]);
+            for (e = 0; e < n; e++) yy[e] = m->x[e] + h * m->k[2][e];
+            rhs_eval(m, yy, m->k[3]);
+        }
+        for (e = 0; e < n; e++)
+            m->x[e] = m->x[e] + (h / 6) * (((m->k[0][e] + 2 * m->k[1][e]) + 2 * m->k[2][e]) + m->k[3][e]);
+        memcpy(m->now.w, m->x, n * sizeof(double));
+        m->t = m->t + h;
+        m->n_accept++;
+    }
+    return 0;
+}
+
+/* step_tsit54, src/integrators.f90:131-203.  Reference-compatible mode keeps
+ * the transposed tableau (every stage state equals x) and the frozen RHS, so
+ * only one RHS value exists per state; it is evaluated six times as in the
+ * reference.  True-stage mode runs the Dormand-Prince 5(4) pair whose
+ * tableau the reference's truncated coefficients come from, with FSAL. */
+static int step_tsit54(orc_model *m, double tf)
+{
+    const size_t n = (size_t)m->nx * m->ny;
+    size_t e;
+    long rejects = 0;
+    static const double b[6] = {0.0845, 0.0, 0.0, 0.5179, 0.1276, 0.2700};
+    static const double bh[6] = {0.0845, 0.0, 0.0, 0.5179, 0.1276, 0.2700 - 1 / 5.0};
+    while (m->t < tf) {
+        double tol, err, s = 0.0, m1, m2;
+        m->dt = fmin(m->dt, tf - m->t);
+        if (m->p.stage_mode == 0) {
+            int st;
+            for (st = 0; st < 6; st++) rhs_eval(m, m->now.w, m->k[st]);
+            for (e = 0; e < n; e++) {
+                double a1 = m->x[e], a2 = m->x[e];
+                for (st = 0; st < 6; st++) {
+                    a1 = a1 + (m->dt * bh[st]) * m->k[st][e];
+                    a2 = a2 + (m->dt * b[st]) * m->k[st][e];
+                }
+                m->x1[e] = a1; m->x2[e] = a2;
+            }
+        } else {
+            static const double A[7][6] = {
+                {0, 0, 0, 0, 0, 0},
+                {1.0 / 5, 0, 0, 0, 0, 0},
+                {3.0 / 40, 9.0 / 40, 0, 0, 0, 0},
+                {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0, 0},
+                {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0, 0},
+                {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656, 0},
+                {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84}};
+            static const double bs[7] = {5179.0 / 57600, 0, 7571.0 / 16695, 393.0 / 640,
+                                         -92097.0 / 339200, 187.0 / 2100, 1.0 / 40};
+            int st, r;
+            if (!m->fsal_valid) { rhs_eval(m, m->x, m->k[0]); m->fsal_valid = 1; }
+            for (st = 1; st < 7; st++) {
+                double *yy = (st == 6) ? m->x2 : m->y;
+                for (e = 0; e < n; e++) {
+                    double a = 0.0;
+                    for (r = 0; r < st; r++) a += A[st][r] * m->k[r][e];
+                    yy[e] = m->x[e] + m->dt * a;
+                }
+                rhs_eval(m, yy, m->k[st]);
+            }
+            for (e = 0; e < n; e++) {
+                double a = 0.0;
+                for (r = 0; r < 7; r++) a += bs[r] * m->k[r][e];
+                m->x1[e] = m->x[e] + m->dt * a;
+            }
+        }
+        m1 = maxabs(m->x1, n); m2 = maxabs(m->x2, n);
+        tol = m->p.atol + m->p.rtol * fmax(m1, m2);
+        for (e = 0; e < n; e++) { double d = (m->x2[e] - m->x1[e]) / tol; s += d * d; }
+        err = sqrt(s / (double)n);
+        if (err < 1) {
+            memcpy(m->x, m->x2, n * sizeof(double));
+            memcpy(m->now.w, m->x, n * sizeof(double));
+            m->t = m->t + m->dt;
+            m->dt = fmin(m->dt * pow(1 / err, 1 / m->p.q), m->p.dt_max);
+            if (m->p.stage_mode) { double *t = m->k[0]; m->k[0] = m->k[6]; m->k[6] = t; }
+            m->n_accept++;
+        } else {
+            m->dt = m->dt * 0.5;
+            m->n_reject++;
+            if (++rejects > 200) return 3;   /* reference loops forever here (no dt_min floor) */
+        }
+    }
+    return 0;
+}
+
+/* isos_update, src/fastisostasy.f90:731-872 */
+static int update_impl(orc_model *m, const double *H_ice, double time, orc_bsl *bsl, int run_integrator)
+{
+    const size_t n = (size_t)m->nx * m->ny;
+    int diag, rc = 0;
+    size_t e;
+    for (e = 0; e < n; e++) m->now.Hice[e] = 0.0;
+    out2in(m, m->now.Hice, H_ice);
+    calc_Haf(&m->now, &m->p, n);
+    sl_contributions(m, n);
+    if (bsl->method == 2) bsl->bsl_now = bsl->bsl_now - m->now.deltaV_bsl / bsl->A_ocean_now;
+    if (bsl->method == 3) {
+        m->now.dbsl_total = m->now.dbsl_total + m->now.deltaV_bsl / bsl->A_ocean_now;
+        bsl->bsl_now = bsl->bsl_now - m->now.dbsl_total;
+    }
+    m->now.bsl = bsl->bsl_now;
+    calc_z_ss(m->now.z_ss, m->now.bsl, m->ref.z_ss, m->now.dz_ss, n);
+    if (time - m->time_diag >= SP(1e-3)) {
+        diag = 1;
+        m->time_diag = m->time_diag + m->p.dt_diagnostics;
+    } else diag = 0;
+    calc_masks(&m->now, n);
+    canom_ice(m, n);
+    canom_seawater(m, n);
+    canom_load(m, n);
+    if (diag) {
+        if (m->p.include_elastic) {
+            double *in = dalloc(n);
+            for (e = 0; e < n; e++) in[e] = (m->now.c_load[e] * m->p.g) * (m->K[e] * m->K[e]);
+            orc_conv(m->now.we, m->nx, m->ny, m->M, m->FGEr, m->FGEi, in);
+            free(in);
+        } else {
+            for (e = 0; e < n; e++) m->now.we[e] = 0.0;
+        }
+    }
+    canom_litho(m, n);
+    canom_full(m, n);
+    mass_anom(m, n);
+    if (diag) {
+        if (m->p.heterogeneous_ssh) orc_conv(m->now.dz_ss, m->nx, m->ny, m->M, m->FGNr, m->FGNi, m->now.mass);
+        else for (e = 0; e < n; e++) m->now.dz_ss[e] = 0.0;
+    }
+    calc_z_ss(m->now.z_ss, m->now.bsl, m->ref.z_ss, m->now.dz_ss, n);
+    calc_masks(&m->now, n);
+    canom_seawater(m, n);
+    canom_load(m, n);
+    if (run_integrator) {
+        m->fsal_valid = 0;   /* the load changed: FSAL derivative is stale */
+        switch (m->p.dt_method) {
+        case 0: rc = step_euler(m, time); break;
+        case 1: rc = step_rk4(m, time); break;
+        case 2: rc = step_tsit54(m, time); break;
+        default: return 5;
+        }
+    }
+    zerobc_corners(m->now.w, m->nx, m->ny);
+    canom_mantle(m, n);
+    for (e = 0; e < n; e++) m->now.z_bed[e] = (m->ref.z_bed[e] + m->now.w[e]) + m->now.we[e];
+    m->time_prog = time;
+    /* check_isos_instabilities :874-899 and the NaN check :864-869 */
+    if (rc == 0) {
+        double mz = -INFINITY;
+        int nan = 0;
+        if (maxabs(m->now.w, n) > 1e5 || maxabs(m->now.we, n) > 1e5 || maxabs(m->now.w_eq, n) > 1e5 ||
+            maxabs(m->now.dz_ss, n) > 1e3) rc = 2;
+        for (e = 0; e < n; e++) { if (m->now.z_bed[e] != m->now.z_bed[e]) nan = 1; else if (m->now.z_bed[e] > mz) mz = m->now.z_bed[e]; }
+        if (nan) rc = 1;
+    }
+    return rc;
+}
+
+int orc_init_state(orc_model *m, const double *z_bed, const double *H_ice, double time, orc_bsl *bsl)
+{
+    /* isos_init_state, src/fastisostasy.f90:596-660 (no restart path) */
+    const size_t n = (size_t)m->nx * m->ny;
+    int rc;
+    m->now.bsl = bsl->bsl_now;
+    out2in(m, m->now.z_bed, z_bed);
+    out2in(m, m->now.Hice, H_ice);
+    if (!m->ref_was_set) orc_init_ref(m, z_bed, H_ice, m->now.bsl, m->now.dz_ss);
+    {
+        size_t e;
+        for (e = 0; e < n; e++) m->ref.z_ss[e] = 0.0;
+    }
+    calc_z_ss(m->ref.z_ss, m->ref.bsl, m->ref.z_ss, m->ref.dz_ss, n);
+    calc_z_ss(m->now.z_ss, m->now.bsl, m->now.z_ss, m->now.dz_ss, n);
+    calc_Haf(&m->ref, &m->p, n);
+    calc_Haf(&m->now, &m->p, n);
+    calc_masks(&m->ref, n);
+    calc_masks(&m->now, n);
+    m->time_prog = time;
+    m->time_diag = time;
+    /* The nested isos_update runs with the ode clock still zero; for
+     * time <= 0 its integrator loop does not execute.  For time > 0 the
+     * reference would step with dt = 0 (and produce NaN); this restatement
+     * skips the integrator there instead. */
+    rc = update_impl(m, H_ice, time, bsl, time <= m->t);
+    m->dt = m->p.dt_init;
+    m->t = time;
+    memcpy(m->x, m->now.w, n * sizeof(double));
+    return rc;
+}
+
+int orc_update(orc_model *m, const double *H_ice, double time, orc_bsl *bsl)
+{
+    return update_impl(m, H_ice, time, bsl, 1);
+}
+
+/* bsl_update, src/barysealevel.f90:195-252 (file series via the caller's table) */
+static double interp0(const double *x, const double *y, int n, double xo)
+{
+    int j;
+    if (xo < x[0]) return y[0];
+    if (xo > x[n - 1]) return y[n - 1];
+    for (j = 0; j < n; j++) if (x[j] >= xo) break;
+    if (j == 0) return y[0];
+    if (j == n) return y[n - 1];
+    {
+        double alpha = (xo - x[j - 1]) / (x[j] - x[j - 1]);
+        return y[j - 1] + alpha * (y[j] - y[j - 1]);
+    }
+}
+
+void orc_bsl_update(orc_bsl *b, double year_bp)
+{
+    b->time = year_bp;
+    switch (b->method) {
+    case 0: b->bsl_now = b->bsl_init; break;
+    case 1: b->bsl_now = interp0(b->series_t, b->series_v, b->n_series, year_bp); break;
+    case 3: b->bsl_now = interp0(b->series_t, b->series_v, b->n_series, year_bp); /* fall through */
+    case 2:
+        if (b->constant_ocean_surface || b->n_aocean <= 0) b->A_ocean_now = b->A_ocean_pd;
+        else b->A_ocean_now = interp0(b->bsl_vec, b->aocean_vec, b->n_aocean, b->bsl_now);
+        break;
+    default: break;
+    }
+}
+
+int orc_get_field(const orc_model *m, int which, double *out)
+{
+    const size_t n = (size_t)m->nx * m->ny;
+    const double *src = NULL;
+    const uint8_t *msk = NULL;
+    size_t e;
+    switch (which) {
+    case 0: src = m->now.z_bed; break;
+    case 1: src = m->now.dwdt; break;
+    case 2: src = m->now.w; break;
+    case 3: src = m->now.we; break;
+    case 4: src = m->now.Haf; break;
+    case 5: src = m->now.Hice; break;
+    case 6: src = m->now.z_ss; break;
+    case 7: src = m->now.dz_ss; break;
+    case 8: src = m->now.c_load; break;
+    case 9: src = m->now.c_full; break;
+    case 10: src = m->now.mass; break;
+    case 11: msk = m->now.m_ocean; break;
+    case 12: msk = m->now.m_grounded; break;
+    case 13: msk = m->now.m_cont; break;
+    case 14: src = m->now.c_mantle; break;
+    case 15: src = m->now.c_litho; break;
+    case 16: src = m->now.c_sw; break;
+    case 17: src = m->now.c_ice; break;
+    case 18: src = m->x; break;
+    case 19: src = m->kappa; break;
+    case 20: src = m->D; break;
+    case 21: src = m->eta_eff; break;
+    case 22: src = m->R; break;
+    case 23: msk = m->maskactive; break;
+    case 24: src = m->GE; break;
+    case 25: src = m->GN; break;
+    case 26: src = m->ref.w; break;
+    case 27: src = m->ref.z_bed; break;
+    case 28: src = m->ref.Haf; break;
+    case 29: src = m->ref.z_ss; break;
+    case 30: src = m->He; break;
+    default: return -1;
+    }
+    if (src) memcpy(out, src, n * sizeof(double));
+    else for (e = 0; e < n; e++) out[e] = (double)msk[e];
+    return 0;
+}
+
+int orc_get_scalars(const orc_model *m, double *o)
+{
+    o[0] = m->t; o[1] = m->dt; o[2] = m->time_diag; o[3] = m->now.bsl; o[4] = m->now.V_af;
+    o[5] = m->now.V_den; o[6] = m->now.deltaV_bsl; o[7] = m->now.dbsl_total;
+    o[8] = (double)m->n_rhs; o[9] = (double)m->n_accept; o[10] = (double)m->n_reject;
+    o[11] = m->sec_per_year; o[12] = m->cc; o[13] = m->Vden; o[14] = (double)m->M; o[15] = m->ref.bsl;
+    return 0;
+}
