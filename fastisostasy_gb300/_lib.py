@@ -1,0 +1,115 @@
+"""ctypes binding of libfigpu.so (the C ABI of include/fi_gpu.h).
+
+Loading fails loudly when the library is missing or no CUDA device is
+usable: there is no CPU path.
+"""
+import ctypes as C
+import os
+
+from . import build as _build
+
+FI_OK, FI_E_NAN, FI_E_LARGE, FI_E_STEP, FI_E_OOM, FI_E_CONFIG, FI_E_CUDA, FI_E_TIMEOUT, FI_E_ARG, FI_E_STATE = range(10)
+FI_PREC_FP64, FI_PREC_MIXED = 0, 1
+
+ERRORS = {1: "FI_E_NAN", 2: "FI_E_LARGE", 3: "FI_E_STEP", 4: "FI_E_OOM", 5: "FI_E_CONFIG", 6: "FI_E_CUDA",
+          7: "FI_E_TIMEOUT", 8: "FI_E_ARG", 9: "FI_E_STATE"}
+
+FIELDS = {
+    "z_bed": 0, "dwdt": 1, "w": 2, "we": 3, "Haf": 4, "Hice": 5, "z_ss": 6, "dz_ss": 7,
+    "canom_load": 8, "canom_full": 9, "mass_anom": 10, "maskocean": 11, "maskgrounded": 12,
+    "maskcontinent": 13, "canom_mantle": 14, "canom_litho": 15, "canom_seawater": 16,
+    "canom_ice": 17, "x": 18, "kappa": 19, "D_lith": 20, "eta_eff": 21, "R": 22,
+    "maskactive": 23, "GE": 24, "GN": 25,
+}
+
+EXPORTS = ["fi_create", "fi_destroy", "fi_dims", "fi_set_fields", "fi_set_kernels", "fi_init_ref",
+           "fi_init_state", "fi_update", "fi_update_async", "fi_synchronize", "fi_bsl_update",
+           "fi_get_field", "fi_get_scalars", "fi_lvelva", "fi_convolve", "fi_state_size",
+           "fi_state_export", "fi_state_import", "fi_last_error", "fi_version"]
+
+
+class FiParams(C.Structure):
+    _fields_ = [
+        ("method", C.c_int32), ("interactive_sealevel", C.c_int32), ("include_elastic", C.c_int32),
+        ("heterogeneous_ssh", C.c_int32), ("correct_compression", C.c_int32),
+        ("lithosphere", C.c_int32), ("mantle", C.c_int32), ("layering", C.c_int32),
+        ("lumping", C.c_int32), ("visc_scaling_method", C.c_int32), ("nl", C.c_int32),
+        ("dt_method", C.c_int32), ("stage_mode", C.c_int32), ("nx_target", C.c_int32),
+        ("ny_target", C.c_int32), ("precision", C.c_int32),
+        ("dt_diagnostics", C.c_double), ("min_pad", C.c_double), ("viscosity_scaling", C.c_double),
+        ("zl", C.c_double * 8), ("viscosities", C.c_double * 8), ("dl", C.c_double),
+        ("eta_ref", C.c_double), ("E", C.c_double), ("nu", C.c_double), ("rho_water", C.c_double),
+        ("rho_ice", C.c_double), ("rho_seawater", C.c_double), ("rho_uppermantle", C.c_double),
+        ("rho_litho", C.c_double), ("g", C.c_double), ("r_earth", C.c_double),
+        ("m_earth", C.c_double), ("atol", C.c_double), ("rtol", C.c_double),
+        ("dt_min", C.c_double), ("dt_max", C.c_double), ("dt_init", C.c_double), ("q", C.c_double),
+    ]
+
+
+class FiBsl(C.Structure):
+    _fields_ = [
+        ("method", C.c_int32), ("constant_ocean_surface", C.c_int32), ("n_series", C.c_int32),
+        ("n_aocean", C.c_int32), ("bsl_init", C.c_double), ("bsl_now", C.c_double),
+        ("A_ocean_now", C.c_double), ("A_ocean_pd", C.c_double), ("time", C.c_double),
+        ("series_t", C.POINTER(C.c_double)), ("series_v", C.POINTER(C.c_double)),
+        ("bsl_vec", C.POINTER(C.c_double)), ("aocean_vec", C.POINTER(C.c_double)),
+    ]
+
+
+_dp = C.POINTER(C.c_double)
+_u8 = C.POINTER(C.c_uint8)
+
+
+class FiOut(C.Structure):
+    _fields_ = [(k, _dp) for k in ("z_bed", "z_ss", "dz_ss", "w", "we", "dwdt", "canom_full", "Hice")] + \
+               [(k, _u8) for k in ("maskocean", "maskgrounded", "maskcontinent")]
+
+
+_LIB = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libfigpu.so (building it in-tree if needed)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if build_if_missing and not _build.up_to_date():
+        path = _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError("libfigpu.so is not built (run __graft_entry__.build())")
+    L = C.CDLL(path)
+    H = C.c_void_p
+    L.fi_create.argtypes = [C.POINTER(FiParams), C.c_int, C.c_int, C.c_double, C.c_double, _dp, C.POINTER(H)]
+    L.fi_destroy.argtypes = [H]
+    L.fi_dims.argtypes = [H, C.POINTER(C.c_int32)]
+    L.fi_set_fields.argtypes = [H, _dp, _dp, _dp, _u8]
+    L.fi_set_kernels.argtypes = [H, _dp, _dp]
+    L.fi_init_ref.argtypes = [H, _dp, _dp, C.c_double, _dp]
+    L.fi_init_state.argtypes = [H, _dp, _dp, C.c_double, C.POINTER(FiBsl)]
+    L.fi_update.argtypes = [H, _dp, C.c_double, C.POINTER(FiBsl), C.POINTER(FiOut)]
+    L.fi_update_async.argtypes = [H, C.c_void_p, C.c_double, C.POINTER(FiBsl)]
+    L.fi_synchronize.argtypes = [H]
+    L.fi_bsl_update.argtypes = [C.POINTER(FiBsl), C.c_double]
+    L.fi_get_field.argtypes = [H, C.c_int, _dp]
+    L.fi_get_scalars.argtypes = [H, _dp]
+    L.fi_lvelva.argtypes = [H, _dp, _dp, _dp]
+    L.fi_convolve.argtypes = [H, C.c_int, _dp, _dp]
+    L.fi_state_size.argtypes = [H]
+    L.fi_state_size.restype = C.c_size_t
+    L.fi_state_export.argtypes = [H, _dp]
+    L.fi_state_import.argtypes = [H, _dp]
+    L.fi_last_error.argtypes = [H]
+    L.fi_last_error.restype = C.c_char_p
+    _LIB = L
+    return L
+
+
+class FiError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code

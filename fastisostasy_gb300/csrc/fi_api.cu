@@ -1,0 +1,1168 @@
+// fi_api.cu — host side of the C ABI declared in include/fi_gpu.h.
+//
+// One fi_handle = one padded LV-ELVA domain resident on the current CUDA
+// device, with its own stream.  The host code restates the init-time logic
+// of isos_init's method-3 branch (src/fastisostasy.f90:64-473) and drives
+// the device kernels in the order of isos_update
+// (src/fastisostasy.f90:731-872).  There is no CPU compute path: every
+// per-cell operation of init_state/update runs on the device.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fi_gpu.h"
+#include "fi_kernels.h"
+#include "fi_state.h"
+
+using namespace fi;
+
+namespace {
+
+const double PI_LIT = (double)3.14159265359f;   // src/isostasy_defs.f90:8 (default-real literal)
+inline double sp(double x) { return (double)(float)x; }
+
+FftDesc factorize(int n)
+{
+    FftDesc d;
+    memset(&d, 0, sizeof(d));
+    d.n = n;
+    int m = n, e2 = 0;
+    while (m % 2 == 0) { m /= 2; e2++; }
+    int n8 = e2 / 3, r = e2 % 3, n4 = 0, n2 = 0;
+    if (r == 1) { if (n8 > 0) { n8--; n4 = 2; } else n2 = 1; }
+    else if (r == 2) n4 = 1;
+    for (int i = 0; i < n8; ++i) d.fac[d.nf++] = 8;
+    for (int i = 0; i < n4; ++i) d.fac[d.nf++] = 4;
+    for (int i = 0; i < n2; ++i) d.fac[d.nf++] = 2;
+    for (int f = 3; m > 1; f += 2)
+        while (m % f == 0) { d.fac[d.nf++] = f; m /= f; }
+    return d;
+}
+
+bool nice(int n)
+{
+    for (int f : {2, 3, 5, 7})
+        while (n % f == 0) n /= f;
+    return n == 1;
+}
+int nice_even_at_least(int m)
+{
+    int v = m + (m & 1);
+    while (!nice(v)) v += 2;
+    return v;
+}
+
+// get_ge_value (src/green_functions.f90:131-168) with the 42-entry table
+// (:56-66); the radii are multiplied by 1.e3 in single precision.
+const float kRn[42] = {0.0f, 0.011f, 0.111f, 1.112f, 2.224f, 3.336f, 4.448f, 6.672f, 8.896f, 11.12f, 17.79f,
+                       22.24f, 27.80f, 33.36f, 44.48f, 55.60f, 66.72f, 88.96f, 111.2f, 133.4f, 177.9f, 222.4f,
+                       278.0f, 333.6f, 444.8f, 556.0f, 667.2f, 778.4f, 889.6f, 1001.0f, 1112.0f, 1334.0f,
+                       1779.0f, 2224.0f, 2780.0f, 3336.0f, 4448.0f, 5560.0f, 6672.0f, 7784.0f, 8896.0f, 10008.0f};
+const float kGe[42] = {-33.6488f, -33.64f, -33.56f, -32.75f, -31.86f, -30.98f, -30.12f, -28.44f, -26.87f,
+                       -25.41f, -21.80f, -20.02f, -18.36f, -17.18f, -15.71f, -14.91f, -14.41f, -13.69f, -13.01f,
+                       -12.31f, -10.95f, -9.757f, -8.519f, -7.533f, -6.131f, -5.237f, -4.660f, -4.272f, -3.999f,
+                       -3.798f, -3.640f, -3.392f, -2.999f, -2.619f, -2.103f, -1.530f, -0.292f, 0.848f, 1.676f,
+                       2.083f, 2.057f, 1.643f};
+
+double ge_value(double r)
+{
+    static double rn[42], ge[42];
+    static bool ready = false;
+    if (!ready) {
+        for (int k = 0; k < 42; ++k) { rn[k] = (double)(kRn[k] * 1.e3f); ge[k] = (double)kGe[k]; }
+        ready = true;
+    }
+    if (r > rn[41]) return 0.0;
+    int k = 0;
+    while (k < 41 && !(r >= rn[k] && r < rn[k + 1])) ++k;
+    if (k > 40) k = 40;
+    return ge[k] + (r - rn[k]) / (rn[k + 1] - rn[k]) * (ge[k + 1] - ge[k]);
+}
+
+inline int midindex(int n) { return (n % 2 == 0) ? n / 2 : (n - 1) / 2; }
+
+}  // namespace
+
+struct fi_handle {
+    fi_params p;
+    int nx, ny, nx_ice, ny_ice, icrop1, icrop2, jcrop1, jcrop2;
+    size_t n;
+    double dx, dy, spy, cc, Vden;
+    double time_diag, time_prog;
+    int ref_was_set = 0, state_ready = 0;
+    double h_t = 0.0, h_dt = 0.0;       // host mirror of the ode clock (euler/rk4)
+    double ref_bsl = 0.0;
+    int Px = 0, Py = 0;
+    int even = 1, uniform = 1;
+    cudaStream_t s = nullptr;
+    std::vector<void*> allocs;
+    std::string err;
+    // host copies of the static fields
+    std::vector<double> K, kappa, R, D, He, eta_eff, GE, GN, xc, yc;
+    std::vector<uint8_t> mact;
+    // device
+    Dom d;
+    Ctl* ctl = nullptr;
+    Plan2D prhs, pconv;
+    FlexCoef fc;
+    double* y = nullptr;                 // stage state
+    void* q0 = nullptr;                  // RHS load term (T)
+    void* Dt = nullptr;                  // rigidity (T)
+    void* inv2eta = nullptr;             // 1/(2 eta_eff) (T)
+    void* f = nullptr;                   // flexure output (T)
+    void* raw[4] = {nullptr, nullptr, nullptr, nullptr};   // RHS stage outputs (T)
+    void* S = nullptr;                   // RHS half spectrum (T complex)
+    void* mA = nullptr;                  // 1/(kappa R) at (k, l) (T)
+    void* mB = nullptr;                  // 1/(kappa R) at (-k, l) (T)
+    void* S2 = nullptr;                  // convolution spectrum (T complex)
+    void* KS[2] = {nullptr, nullptr};    // elastic / geoid kernel spectra (T complex)
+    void* conv_in = nullptr;             // convolution input (T)
+    double *we_raw = nullptr, *dz_raw = nullptr, *corners = nullptr;
+    int* out_rows = nullptr;
+    double* dH = nullptr;                // ice-grid thickness on the device
+    double* dpack = nullptr;             // packed outputs
+    double* hpin = nullptr;              // pinned staging (max(ice grid, packed outputs))
+    size_t hpin_elems = 0;
+    const double** gsrc = nullptr;
+    const uint8_t** gmsrc = nullptr;
+    double *dxm = nullptr, *dym = nullptr;
+    // reference-state device pointers (non-const views)
+    double *z_bed_ref, *Hice_ref, *Haf_ref, *z_ss_ref, *we_ref, *w_ref, *dz_ss_ref;
+    uint8_t *mo_ref, *mg_ref, *mc_ref;
+};
+
+namespace {
+
+int fail(fi_handle* h, int code, const char* fmt, ...)
+{
+    if (h) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        h->err = buf;
+    }
+    return code;
+}
+
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) return fail(h, FI_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename P> int dalloc(fi_handle* h, P** out, size_t bytes)
+{
+    void* p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return fail(h, e == cudaErrorMemoryAllocation ? FI_E_OOM : FI_E_CUDA, "cudaMalloc(%zu): %s", bytes,
+                    cudaGetErrorString(e));
+    }
+    h->allocs.push_back(p);
+    cudaMemsetAsync(p, 0, bytes, h->s);
+    *out = static_cast<P*>(p);
+    return FI_OK;
+}
+
+bool mixed(const fi_handle* h) { return h->p.precision == FI_PREC_MIXED; }
+size_t tsz(const fi_handle* h) { return mixed(h) ? sizeof(float) : sizeof(double); }
+
+int upload(fi_handle* h, void* dst, const void* src, size_t bytes)
+{
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return FI_OK;
+}
+
+// double host vector -> device buffer of the field type
+int upload_T(fi_handle* h, void* dst, const std::vector<double>& v)
+{
+    if (mixed(h)) {
+        std::vector<float> t(v.size());
+        for (size_t i = 0; i < v.size(); ++i) t[i] = (float)v[i];
+        return upload(h, dst, t.data(), t.size() * sizeof(float));
+    }
+    return upload(h, dst, v.data(), v.size() * sizeof(double));
+}
+
+int make_len(fi_handle* h, int n, FftLen& L)
+{
+    L.d = factorize(n);
+    std::vector<double2> t64(n);
+    std::vector<float2> t32(n);
+    for (int t = 0; t < n; ++t) {
+        long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)t / (long double)n;
+        t64[t] = make_double2((double)cosl(a), (double)sinl(a));
+        t32[t] = make_float2((float)cosl(a), (float)sinl(a));
+    }
+    double2* d64;
+    float2* d32;
+    int rc;
+    if ((rc = dalloc(h, &d64, n * sizeof(double2))) || (rc = dalloc(h, &d32, n * sizeof(float2)))) return rc;
+    if ((rc = upload(h, d64, t64.data(), n * sizeof(double2))) || (rc = upload(h, d32, t32.data(), n * sizeof(float2))))
+        return rc;
+    L.tw64 = d64;
+    L.tw32 = d32;
+    return FI_OK;
+}
+
+int make_plan(fi_handle* h, int nx, int ny, Plan2D& P)
+{
+    P.nx = nx;
+    P.ny = ny;
+    P.h = nx / 2;
+    P.sp = ((P.h + 1) + 7) / 8 * 8;
+    int rc;
+    if ((rc = make_len(h, P.h, P.row)) || (rc = make_len(h, ny, P.col))) return rc;
+    std::vector<double2> r64(P.h + 1);
+    std::vector<float2> r32(P.h + 1);
+    for (int k = 0; k <= P.h; ++k) {
+        long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)k / (long double)nx;
+        r64[k] = make_double2((double)cosl(a), (double)sinl(a));
+        r32[k] = make_float2((float)cosl(a), (float)sinl(a));
+    }
+    double2* d64;
+    float2* d32;
+    if ((rc = dalloc(h, &d64, (P.h + 1) * sizeof(double2))) || (rc = dalloc(h, &d32, (P.h + 1) * sizeof(float2))))
+        return rc;
+    if ((rc = upload(h, d64, r64.data(), (P.h + 1) * sizeof(double2))) ||
+        (rc = upload(h, d32, r32.data(), (P.h + 1) * sizeof(float2))))
+        return rc;
+    P.rtw64 = d64;
+    P.rtw32 = d32;
+    return FI_OK;
+}
+
+// ---- init-time physics (host, double) ---------------------------------------
+// calc_kappa, src/lv_elva.f90:442-481
+void host_kappa(fi_handle* h)
+{
+    const int nx = h->nx, ny = h->ny;
+    const double mu_x = 2.0 * PI_LIT / ((nx - 1) * h->dx), mu_y = 2.0 * PI_LIT / ((ny - 1) * h->dy);
+    const int ic = (nx - 1) / 2 + 1, jc = (ny - 1) / 2 + 1;
+    h->kappa.assign(h->n, 0.0);
+    for (int i = 1; i <= nx; ++i) {
+        const double pp = (i <= ic) ? mu_x * (i - 1) : mu_x * (nx - i + 1);
+        for (int j = 1; j <= ny; ++j) {
+            const double q = (j <= jc) ? mu_y * (j - 1) : mu_y * (ny - j + 1);
+            h->kappa[(size_t)(j - 1) * nx + (i - 1)] = std::pow(pp * pp + q * q, 0.5);
+        }
+    }
+    h->kappa[0] = (h->kappa[nx] + h->kappa[1]) / 2.0;
+}
+
+double rigidity(double E, double He, double nu) { return E * 1e9 * (He * He * He) / (12.0 * (1.0 - nu * nu)); }
+
+// Gaussian bump over the padded domain as in calc_gaussian_thickness /
+// calc_gaussian_viscosity (src/isos_utils.f90:960-1035).
+void gauss_bump(const fi_handle* h, const std::vector<double>& xc, const std::vector<double>& yc,
+                std::vector<double>& out)
+{
+    const int nx = h->nx, ny = h->ny;
+    const double xcntr = (xc[nx - 1] + xc[0]) / 2.0, ycntr = (yc[ny - 1] + yc[0]) / 2.0;
+    const double Lx = (xc[nx - 1] - xc[0]) / 2., Ly = (yc[ny - 1] - yc[0]) / 2.;
+    const double s11 = (4.0 / Lx) * (4.0 / Lx), s22 = (4.0 / Ly) * (4.0 / Ly);
+    out.assign(h->n, 0.0);
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j) {
+            const double d1 = xc[i] - xcntr, d2 = yc[j] - ycntr;
+            out[(size_t)j * nx + i] = std::exp(-0.5 * (d1 * (s11 * d1 + 0.0 * d2) + d2 * (0.0 * d1 + s22 * d2)));
+        }
+}
+
+void host_fields(fi_handle* h)
+{
+    const fi_params& p = h->p;
+    const size_t n = h->n;
+    h->He.assign(n, p.zl[0]);
+    h->D.assign(n, rigidity(p.E, p.zl[0], p.nu));
+    h->R.assign(n, 1.0);
+    h->eta_eff.assign(n, p.viscosities[p.nl - 1]);
+    host_kappa(h);
+    if (p.lithosphere == 1 || p.lithosphere == 2) {
+        std::vector<double> g;
+        gauss_bump(h, h->xc, h->yc, g);
+        double mx = -1e300;
+        for (double v : g) mx = v > mx ? v : mx;
+        const double sgn = p.lithosphere == 1 ? 1.0 : -1.0;
+        for (size_t e = 0; e < n; ++e) {
+            h->He[e] = p.zl[0] + sgn * sp(100e3) * (g[e] / mx);
+            h->D[e] = rigidity(p.E, h->He[e], p.nu);
+        }
+    }
+    const int nl = p.nl;
+    if (p.mantle == 0) {
+        // calc_effective_viscosity, src/lv_elva.f90:207-306
+        std::vector<double> bnd((size_t)nl * n);
+        for (size_t e = 0; e < n; ++e) bnd[e] = h->He[e];
+        for (int k = 1; k < nl; ++k)
+            for (size_t e = 0; e < n; ++e)
+                bnd[(size_t)k * n + e] = (p.layering == 1) ? bnd[(size_t)(k - 1) * n + e] + p.dl : p.zl[k];
+        for (size_t e = 0; e < n; ++e) {
+            double mn = p.viscosities[0], mxv = p.viscosities[0], s = 0.0, ls = 0.0;
+            for (int k = 0; k < nl; ++k) {
+                const double v = p.viscosities[k];
+                mn = v < mn ? v : mn;
+                mxv = v > mxv ? v : mxv;
+                s += v;
+                ls += std::log10(v);
+            }
+            double v = p.viscosities[nl - 1];
+            switch (p.lumping) {
+            case 1: v = mn; break;
+            case 2: v = mxv; break;
+            case 3: v = s / (double)nl; break;
+            case 4: v = std::pow(10.0, ls / (double)nl); break;
+            default: break;
+            }
+            h->eta_eff[e] = v;
+        }
+        if (p.lumping == 5 && nl > 1) {
+            for (int k = nl - 1; k >= 1; --k)
+                for (size_t e = 0; e < n; ++e) {
+                    const double dz = bnd[(size_t)k * n + e] - bnd[(size_t)(k - 1) * n + e];
+                    const double er = p.viscosities[k - 1] / h->eta_eff[e], ir = 1. / er;
+                    const double kz = dz * h->kappa[e];
+                    const double c = std::cosh(kz), s = std::sinh(kz);
+                    h->R[e] = h->R[e] * (2 * er * c * s + (1 - er * er) * (kz * kz) + (er * s) * (er * s) + c * c) /
+                              ((er + ir) * c * s + (er - ir) * dz * h->kappa[e] + s * s + c * c);
+                }
+        }
+    } else if (p.mantle == 1 || p.mantle == 2) {
+        std::vector<double> g;
+        // gaussian_plus passes yc = xc (src/fastisostasy.f90:329-330)
+        gauss_bump(h, h->xc, p.mantle == 1 ? h->xc : h->yc, g);
+        const double sgn = p.mantle == 1 ? 1.0 : -1.0;
+        for (size_t e = 0; e < n; ++e) h->eta_eff[e] = p.viscosities[0] * std::pow(10.0, sgn * g[e]);
+    }
+    // viscosity scaling, src/fastisostasy.f90:425-436
+    if (p.visc_scaling_method == 2 || p.visc_scaling_method == 3) {
+        double v = h->eta_eff[0];
+        for (double e : h->eta_eff) v = (p.visc_scaling_method == 2) ? (e < v ? e : v) : (e > v ? e : v);
+        for (double& e : h->eta_eff) e = v;
+    } else if (p.visc_scaling_method == 1) {
+        for (double& e : h->eta_eff) e = e * p.viscosity_scaling;
+    }
+    for (double& e : h->eta_eff) e = e * h->cc;
+    for (double& e : h->eta_eff) e = std::exp(std::log10(p.eta_ref / e)) * e;   // :441-442
+    // Green's functions, src/green_functions.f90:43-128 (called with dy = dx)
+    const int nx = h->nx, ny = h->ny, mx = midindex(nx);
+    const double dx = h->dx;
+    h->GE.assign(n, 0.0);
+    h->GN.assign(n, 0.0);
+    for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+            const double x = (i - 1 - mx) * dx, y = (j - 1 - mx) * dx;
+            const double r = std::sqrt(x * x + y * y);
+            h->GE[(size_t)(j - 1) * nx + (i - 1)] = ge_value(r) * sp(1.e-12) * (dx * dx) / (sp(9.81) * (r > dx ? r : dx));
+            const double rr = (dx / 2 > r) ? dx / 2 : r;
+            h->GN[(size_t)(j - 1) * nx + (i - 1)] = p.r_earth / (2. * p.m_earth * std::sin(rr / (2. * p.r_earth)));
+        }
+    // maskactive, src/fastisostasy.f90:185-198
+    h->mact.assign(n, 0);
+    if (!p.interactive_sealevel) {
+        for (auto& m : h->mact) m = 1;
+    } else if (p.min_pad > sp(100.e3)) {
+        for (int j = h->jcrop1; j <= h->jcrop2; ++j)
+            for (int i = h->icrop1; i <= h->icrop2; ++i) h->mact[(size_t)(j - 1) * nx + (i - 1)] = 1;
+    }
+}
+
+// Upload the derived static fields: D, 1/(2 eta), 1/(kappa R) in the
+// spectrum layout, maskactive.
+int upload_static(fi_handle* h)
+{
+    const size_t n = h->n;
+    std::vector<double> inv2eta(n);
+    for (size_t e = 0; e < n; ++e) inv2eta[e] = 1.0 / (2.0 * h->eta_eff[e]);
+    int rc;
+    if ((rc = upload_T(h, h->Dt, h->D)) || (rc = upload_T(h, h->inv2eta, inv2eta))) return rc;
+    const int nx = h->nx, ny = h->ny, hh = nx / 2, spitch = h->prhs.sp;
+    std::vector<double> A((size_t)ny * spitch, 0.0), B((size_t)ny * spitch, 0.0);
+    auto m = [&](int k, int l) { return 1.0 / (h->kappa[(size_t)l * nx + k] * h->R[(size_t)l * nx + k]); };
+    h->even = 1;
+    for (int l = 0; l < ny; ++l)
+        for (int k = 0; k <= hh; ++k) {
+            A[(size_t)l * spitch + k] = m(k, l);
+            B[(size_t)l * spitch + k] = m((nx - k) % nx, l);
+        }
+    for (int l = 0; l < ny && h->even; ++l)
+        for (int k = 0; k < nx; ++k)
+            if (m(k, l) != m((nx - k) % nx, l) || m(k, l) != m(k, (ny - l) % ny)) { h->even = 0; break; }
+    if ((rc = upload_T(h, h->mA, A)) || (rc = upload_T(h, h->mB, B))) return rc;
+    if ((rc = upload(h, (void*)h->d.mactive, h->mact.data(), n))) return rc;
+    return FI_OK;
+}
+
+// kernel spectrum: zero-padded r2c of a padded-grid kernel (precompute_kernel,
+// src/convolutions.f90:93-108), computed in double on the device.
+int kernel_spectrum(fi_handle* h, const std::vector<double>& ker, int which)
+{
+    const size_t hs = (size_t)h->pconv.ny * h->pconv.sp;
+    double* tmp;
+    double2* S64;
+    int rc;
+    if ((rc = dalloc(h, &tmp, h->n * sizeof(double))) || (rc = dalloc(h, &S64, hs * sizeof(double2)))) return rc;
+    if ((rc = upload(h, tmp, ker.data(), h->n * sizeof(double)))) return rc;
+    launch_rows_fwd<double>(tmp, h->nx, h->nx, h->ny, S64, h->pconv, h->s);
+    launch_cols_fwd<double>(S64, h->ny, h->pconv, h->s);
+    CK(cudaGetLastError());
+    if (mixed(h)) {
+        std::vector<double2> a(hs);
+        std::vector<float2> b(hs);
+        CK(cudaMemcpyAsync(a.data(), S64, hs * sizeof(double2), cudaMemcpyDeviceToHost, h->s));
+        CK(cudaStreamSynchronize(h->s));
+        for (size_t e = 0; e < hs; ++e) b[e] = make_float2((float)a[e].x, (float)a[e].y);
+        if ((rc = upload(h, h->KS[which], b.data(), hs * sizeof(float2)))) return rc;
+    } else {
+        CK(cudaMemcpyAsync(h->KS[which], S64, hs * sizeof(double2), cudaMemcpyDeviceToDevice, h->s));
+    }
+    CK(cudaStreamSynchronize(h->s));
+    // release the temporaries
+    for (void* p : {(void*)tmp, (void*)S64}) {
+        for (size_t i = 0; i < h->allocs.size(); ++i)
+            if (h->allocs[i] == p) { h->allocs.erase(h->allocs.begin() + i); break; }
+        cudaFree(p);
+    }
+    return FI_OK;
+}
+
+// ---- device pipelines ------------------------------------------------------
+template <typename T> struct TT {
+    typedef typename vec2<T>::type C2;
+};
+
+template <typename T> void rhs(fi_handle* h, const double* y, const double* wref, T* raw_out)
+{
+    typedef typename vec2<T>::type C2;
+    launch_flexure<T>(y, wref, (const T*)h->q0, h->d.mactive, (const T*)h->Dt, (const T*)h->inv2eta, (T*)h->f,
+                      h->nx, h->ny, h->fc, h->s);
+    launch_rows_fwd<T>((const T*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, h->prhs, h->s);
+    launch_cols_hartley<T>((C2*)h->S, (const T*)h->mA, (const T*)h->mB, h->even, h->prhs, h->s);
+    const double norm = (double)(float)((long long)h->nx * h->ny);   // nx*ny*1. (default real)
+    launch_rows_inv<T>((const C2*)h->S, raw_out, h->prhs, 1.0 / norm, h->s);
+}
+
+template <typename T> void conv(fi_handle* h, int which, double* out_raw, double* corners)
+{
+    typedef typename vec2<T>::type C2;
+    launch_rows_fwd<T>((const T*)h->conv_in, h->nx, h->nx, h->ny, (C2*)h->S2, h->pconv, h->s);
+    launch_cols_conv<T>((C2*)h->S2, (const C2*)h->KS[which], h->ny, h->out_rows, h->ny + 2, h->pconv, h->s);
+    launch_conv_rows_inv<T>((const C2*)h->S2, h->ny + 2, out_raw, h->nx, h->ny, h->nx / 2 - 1, corners, 0, 0,
+                            2 * h->nx - 2, h->pconv, 1.0 / ((double)h->Px * (double)h->Py), h->s);
+}
+
+// Integrator loop of one update.  Returns FI status; sets *have_rhs and the
+// raw buffer holding the last RHS evaluated.
+template <typename T> int integrate(fi_handle* h, double tf, int* have_rhs, T** raw_last)
+{
+    const fi_params& p = h->p;
+    const double spy = h->spy;
+    T* r0 = (T*)h->raw[0];
+    *have_rhs = 0;
+    *raw_last = r0;
+    const bool truem = p.stage_mode == 1;
+    const double* wref = truem ? h->w_ref : nullptr;
+    if (p.dt_method == 1 || p.dt_method == 0) {
+        // host mirror of the clock: identical fmin/add sequence as the device
+        while (h->h_t < tf) {
+            double hstep;
+            if (p.dt_method == 1) hstep = fmin(h->h_dt, tf - h->h_t);
+            else { h->h_dt = fmin(h->h_dt, tf - h->h_t); hstep = h->h_dt; }
+            step_begin(h->ctl, tf, p.dt_method == 1 ? 1 : 0, h->s);
+            if (p.dt_method == 1) {
+                if (truem) {
+                    T *r1 = (T*)h->raw[1], *r2 = (T*)h->raw[2], *r3 = (T*)h->raw[3];
+                    rhs<T>(h, h->d.x, wref, r0);
+                    rk_stage<T>(h->ctl, h->y, h->d.x, r0, 0.5, h->nx, h->ny, spy, h->s);
+                    rhs<T>(h, h->y, wref, r1);
+                    rk_stage<T>(h->ctl, h->y, h->d.x, r1, 0.5, h->nx, h->ny, spy, h->s);
+                    rhs<T>(h, h->y, wref, r2);
+                    rk_stage<T>(h->ctl, h->y, h->d.x, r2, 1.0, h->nx, h->ny, spy, h->s);
+                    rhs<T>(h, h->y, wref, r3);
+                    rk4_final<T>(h->ctl, h->d.x, h->d.w, r0, r1, r2, r3, h->nx, h->ny, spy, h->s);
+                    *raw_last = r3;
+                } else {
+                    rhs<T>(h, h->d.w, nullptr, r0);
+                    rk4_final<T>(h->ctl, h->d.x, h->d.w, r0, r0, r0, r0, h->nx, h->ny, spy, h->s);
+                    *raw_last = r0;
+                }
+            } else {
+                rhs<T>(h, truem ? h->d.x : h->d.w, wref, r0);
+                euler_final<T>(h->ctl, h->d.x, h->d.w, r0, h->nx, h->ny, spy, h->s);
+                *raw_last = r0;
+            }
+            step_end(h->ctl, h->s);
+            h->h_t = h->h_t + hstep;
+            *have_rhs = 1;
+        }
+        CK(cudaGetLastError());
+        return FI_OK;
+    }
+    if (p.dt_method == 2) {
+        if (truem) return fail(h, FI_E_CONFIG, "tsit54 with true stages is not available on the device yet");
+        // Reference-compatible Tsit5: one distinct RHS per state; the host
+        // waits for each attempt's accept/reject decision.
+        Ctl hc;
+        CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+        CK(cudaStreamSynchronize(h->s));
+        bool need_rhs = true;
+        int guard = 0;
+        while (hc.t < tf && hc.status == ST_OK) {
+            step_begin(h->ctl, tf, 2, h->s);
+            if (need_rhs) { rhs<T>(h, h->d.w, nullptr, r0); *have_rhs = 1; }
+            ts_max<T>(h->d, r0, p.atol, p.rtol, h->s);
+            ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s);
+            ts_commit<T>(h->d, r0, h->s);
+            CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+            CK(cudaStreamSynchronize(h->s));
+            need_rhs = hc.accepted != 0;
+            if (++guard > 10000000) return fail(h, FI_E_STEP, "tsit54: too many attempts");
+        }
+        *raw_last = r0;
+        return FI_OK;
+    }
+    return fail(h, FI_E_CONFIG, "dt_method %d not supported", p.dt_method);
+}
+
+// The body of isos_update on the device (src/fastisostasy.f90:731-872).
+template <typename T> int update_T(fi_handle* h, const double* dH, double time, bool run_integrator)
+{
+    const fi_params& p = h->p;
+    upd_begin(h->d, dH, h->s);
+    bool diag = false;
+    if (time - h->time_diag >= sp(1e-3)) {   // :782-787
+        diag = true;
+        h->time_diag = h->time_diag + p.dt_diagnostics;
+    }
+    T* cin = (T*)h->conv_in;
+    upd_masks<T>(h->d, (diag && p.include_elastic) ? cin : (T*)nullptr, h->s);
+    int we_mode = 0, dz_mode = 0;
+    if (diag) {
+        if (p.include_elastic) { conv<T>(h, 0, h->we_raw, h->corners); we_mode = 1; }
+        else we_mode = 2;
+    }
+    upd_litho<T>(h->d, h->we_raw, h->corners, we_mode, (diag && p.heterogeneous_ssh) ? cin : (T*)nullptr, h->s);
+    if (diag) {
+        if (p.heterogeneous_ssh) { conv<T>(h, 1, h->dz_raw, h->corners + 4); dz_mode = 1; }
+        else dz_mode = 2;
+    }
+    upd_load<T>(h->d, h->dz_raw, h->corners + 4, dz_mode, (T*)h->q0, p.stage_mode,
+                run_integrator ? time : -INFINITY, h->s);
+    int have_rhs = 0;
+    T* raw_last = (T*)h->raw[0];
+    if (run_integrator) {
+        int rc = integrate<T>(h, time, &have_rhs, &raw_last);
+        if (rc) return rc;
+    }
+    upd_end<T>(h->d, raw_last, have_rhs, h->s);
+    h->time_prog = time;
+    CK(cudaGetLastError());
+    return FI_OK;
+}
+
+int update_any(fi_handle* h, const double* dH, double time, bool run_integrator)
+{
+    return mixed(h) ? update_T<float>(h, dH, time, run_integrator) : update_T<double>(h, dH, time, run_integrator);
+}
+
+int set_bsl_scalars(fi_handle* h, const fi_bsl* b, bool write_bsl)
+{
+    // bsl, A_ocean, bsl_method into the control block
+    struct { double bsl; double A; } v = {b->bsl_now, b->A_ocean_now};
+    if (write_bsl) CK(cudaMemcpyAsync(&h->ctl->bsl, &v.bsl, sizeof(double), cudaMemcpyHostToDevice, h->s));
+    CK(cudaMemcpyAsync(&h->ctl->A_ocean, &v.A, sizeof(double), cudaMemcpyHostToDevice, h->s));
+    int m = b->method;
+    CK(cudaMemcpyAsync(&h->ctl->bsl_method, &m, sizeof(int), cudaMemcpyHostToDevice, h->s));
+    CK(cudaStreamSynchronize(h->s));   // the sources are stack variables
+    return FI_OK;
+}
+
+int read_status(fi_handle* h, Ctl* hc)
+{
+    CK(cudaMemcpyAsync(hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    switch (hc->status) {
+    case ST_OK: return FI_OK;
+    case ST_NAN: return fail(h, FI_E_NAN, "isos_update: NaNs detected");
+    case ST_LARGE: return fail(h, FI_E_LARGE, "large_check: large values detected (|w| %.3g, |we| %.3g, |dz_ss| %.3g)",
+                                hc->red[0], hc->red[1], hc->red[2]);
+    case ST_STEP: return fail(h, FI_E_STEP, "adaptive step rejected too often");
+    default: return fail(h, FI_E_CUDA, "unknown device status %d", hc->status);
+    }
+}
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+int fi_version(void) { return 1; }
+
+const char* fi_last_error(const fi_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy, const double* K_or_null,
+              fi_handle** out)
+{
+    if (!pin || !out) return FI_E_ARG;
+    *out = nullptr;
+    const fi_params& p = *pin;
+    if (p.method != 3 || nx_ice < 3 || ny_ice < 3 || p.nl < 1 || p.nl > 8) return FI_E_CONFIG;
+    if (dx != dy || p.min_pad < 0.0) return FI_E_CONFIG;   // init_domain_size, src/isos_utils.f90:292-300
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return FI_E_CUDA;
+    fi_handle* h = new fi_handle();
+    h->p = p;
+    h->dx = dx;
+    h->dy = dy;
+    h->nx_ice = nx_ice;
+    h->ny_ice = ny_ice;
+    // init_domain_size
+    int nx_tmp = nx_ice, ny_tmp = ny_ice, npx, npy;
+    h->icrop1 = 1;
+    h->jcrop1 = 1;
+    if (nx_ice % 2) { h->icrop1++; nx_tmp++; }
+    if (ny_ice % 2) { h->jcrop1++; ny_tmp++; }
+    if (p.nx_target > 0 && p.ny_target > 0) {
+        if (p.nx_target < nx_tmp || p.ny_target < ny_tmp || (p.nx_target - nx_tmp) % 2 || (p.ny_target - ny_tmp) % 2) {
+            delete h;
+            return FI_E_CONFIG;
+        }
+        npx = (p.nx_target - nx_tmp) / 2;
+        npy = (p.ny_target - ny_tmp) / 2;
+        h->nx = p.nx_target;
+        h->ny = p.ny_target;
+    } else {
+        const int npxy = (int)std::lround(p.min_pad / dx);
+        npx = npy = npxy;
+        if (nx_tmp < ny_tmp) npx += (ny_tmp - nx_tmp) / 2;
+        else if (nx_tmp > ny_tmp) npy += (nx_tmp - ny_tmp) / 2;
+        h->nx = nx_tmp + 2 * npx;
+        h->ny = ny_tmp + 2 * npy;
+    }
+    if (h->nx > 4096 || h->ny > 4096) { delete h; return FI_E_CONFIG; }
+    h->icrop1 += npx;
+    h->icrop2 = h->nx - npx;
+    h->jcrop1 += npy;
+    h->jcrop2 = h->ny - npy;
+    h->n = (size_t)h->nx * h->ny;
+    h->spy = (double)(3600.0f * 24.0f * 365.25f);   // src/fastisostasy.f90:158
+    h->cc = p.correct_compression ? 1.5 / (1 + p.nu) : 1.0;
+    h->Vden = p.rho_ice / p.rho_water - p.rho_ice / p.rho_seawater;
+    h->time_diag = sp(1e10);
+    h->time_prog = sp(1e10);
+    h->xc.resize(h->nx);
+    h->yc.resize(h->ny);
+    for (int i = 1; i <= h->nx; ++i) h->xc[i - 1] = (i - h->nx / 2 - 1) * dx;   // init_dims
+    for (int j = 1; j <= h->ny; ++j) h->yc[j - 1] = (j - h->ny / 2 - 1) * dy;
+    h->K.assign(h->n, 1.0);
+    if (K_or_null) {
+        for (size_t e = 0; e < h->n; ++e) { h->K[e] = K_or_null[e]; if (h->K[e] != 1.0) h->uniform = 0; }
+    }
+    if (cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking) != cudaSuccess) { delete h; return FI_E_CUDA; }
+    *out = h;
+    host_fields(h);
+
+    // ---- device buffers
+    const size_t n = h->n;
+    const size_t nT = n * tsz(h);
+    const size_t nice_ = (size_t)nx_ice * ny_ice;
+    Dom& d = h->d;
+    memset(&d, 0, sizeof(d));
+    d.nx = h->nx;
+    d.ny = h->ny;
+    d.n = n;
+    d.i0 = h->icrop1 - 1;
+    d.j0 = h->jcrop1 - 1;
+    d.nxi = h->icrop2 - h->icrop1 + 1;
+    d.nyi = h->jcrop2 - h->jcrop1 + 1;
+    d.interactive = p.interactive_sealevel;
+    d.rho_ice = p.rho_ice;
+    d.rho_w = p.rho_water;
+    d.rho_m = p.rho_uppermantle;
+    d.rho_l = p.rho_litho;
+    d.g = p.g;
+    d.Vden = h->Vden;
+    d.spy = h->spy;
+    d.rho_sw_over_ice = p.rho_seawater / p.rho_ice;
+    d.rho_ice_over_sw = p.rho_ice / p.rho_seawater;
+    int rc = 0;
+    double *A, *K2;
+    uint8_t* mact;
+#define AL(ptr, bytes) if ((rc = dalloc(h, &(ptr), (bytes)))) return rc
+    AL(A, n * 8); AL(K2, n * 8); AL(mact, n);
+    d.A = A; d.K2 = K2; d.mactive = mact;
+    AL(h->z_bed_ref, n * 8); AL(h->Hice_ref, n * 8); AL(h->Haf_ref, n * 8); AL(h->z_ss_ref, n * 8);
+    AL(h->we_ref, n * 8); AL(h->w_ref, n * 8); AL(h->dz_ss_ref, n * 8);
+    AL(h->mo_ref, n); AL(h->mg_ref, n); AL(h->mc_ref, n);
+    d.z_bed_ref = h->z_bed_ref; d.Hice_ref = h->Hice_ref; d.Haf_ref = h->Haf_ref; d.z_ss_ref = h->z_ss_ref;
+    d.we_ref = h->we_ref; d.w_ref = h->w_ref;
+    AL(d.z_bed, n * 8); AL(d.w, n * 8); AL(d.wout, n * 8); AL(d.we, n * 8); AL(d.Haf, n * 8); AL(d.Hice, n * 8);
+    AL(d.z_ss, n * 8); AL(d.dz_ss, n * 8); AL(d.dwdt, n * 8); AL(d.x, n * 8);
+    AL(d.c_ice, n * 8); AL(d.c_sw, n * 8); AL(d.c_litho, n * 8); AL(d.c_mantle, n * 8); AL(d.c_load, n * 8);
+    AL(d.c_full, n * 8); AL(d.mass, n * 8);
+    AL(d.m_ocean, n); AL(d.m_grounded, n); AL(d.m_cont, n);
+    AL(h->ctl, sizeof(Ctl));
+    d.ctl = h->ctl;
+    AL(d.partials, (size_t)reduce_blocks(n) * 4 * sizeof(double));
+    AL(h->y, n * 8);
+    AL(h->q0, nT); AL(h->Dt, nT); AL(h->inv2eta, nT); AL(h->f, nT);
+    for (int i = 0; i < 4; ++i) AL(h->raw[i], nT);
+    // RHS transform plan
+    if ((rc = make_plan(h, h->nx, h->ny, h->prhs))) return rc;
+    const size_t c2 = 2 * tsz(h);
+    AL(h->S, (size_t)h->ny * h->prhs.sp * c2);
+    AL(h->mA, (size_t)h->ny * h->prhs.sp * tsz(h));
+    AL(h->mB, (size_t)h->ny * h->prhs.sp * tsz(h));
+    // convolution plan: any even size >= 2n-1 gives the reference's linear convolution
+    h->Px = nice_even_at_least(2 * h->nx - 1);
+    h->Py = nice_even_at_least(2 * h->ny - 1);
+    if (h->Px == 2 * h->nx - 2 + 2 && false) {}
+    if ((rc = make_plan(h, h->Px, h->Py, h->pconv))) return rc;
+    AL(h->S2, (size_t)h->Py * h->pconv.sp * c2);
+    AL(h->KS[0], (size_t)h->Py * h->pconv.sp * c2);
+    AL(h->KS[1], (size_t)h->Py * h->pconv.sp * c2);
+    AL(h->conv_in, nT);
+    AL(h->we_raw, n * 8); AL(h->dz_raw, n * 8); AL(h->corners, 8 * sizeof(double));
+    AL(h->out_rows, (h->ny + 2) * sizeof(int));
+    {
+        std::vector<int> rows(h->ny + 2);
+        for (int j = 0; j < h->ny; ++j) rows[j] = h->ny / 2 - 1 + j;   // crop, src/convolutions.f90:29-55
+        rows[h->ny] = 0;
+        rows[h->ny + 1] = 2 * h->ny - 2;
+        if ((rc = upload(h, h->out_rows, rows.data(), rows.size() * sizeof(int)))) return rc;
+    }
+    AL(h->dH, nice_ * 8);
+    const int nout = 11;
+    AL(h->dpack, nice_ * nout * 8);
+    h->hpin_elems = nice_ * nout;
+    if (cudaMallocHost((void**)&h->hpin, h->hpin_elems * sizeof(double)) != cudaSuccess)
+        return fail(h, FI_E_OOM, "cudaMallocHost failed");
+    AL(h->gsrc, 8 * sizeof(double*));
+    AL(h->gmsrc, 3 * sizeof(uint8_t*));
+    {
+        const double* src[8] = {d.z_bed, d.z_ss, d.dz_ss, d.w, d.we, d.dwdt, d.c_full, d.Hice};
+        const uint8_t* msrc[3] = {d.m_ocean, d.m_grounded, d.m_cont};
+        if ((rc = upload(h, (void*)h->gsrc, src, sizeof(src))) || (rc = upload(h, (void*)h->gmsrc, msrc, sizeof(msrc))))
+            return rc;
+    }
+    // static fields
+    {
+        std::vector<double> Av(n), K2v(n), dxm(n), dym(n);
+        for (size_t e = 0; e < n; ++e) {
+            dxm[e] = dx * h->K[e];   // src/fastisostasy.f90:152-155
+            dym[e] = dy * h->K[e];
+            Av[e] = dxm[e] * dym[e];
+            K2v[e] = h->K[e] * h->K[e];
+        }
+        if ((rc = upload(h, A, Av.data(), n * 8)) || (rc = upload(h, K2, K2v.data(), n * 8))) return rc;
+        memset(&h->fc, 0, sizeof(h->fc));
+        h->fc.nu = p.nu;
+        h->fc.one_minus_nu = 1.0 - p.nu;
+        h->fc.coef_mantle = -p.g * p.rho_uppermantle;
+        h->fc.inv_dx = 1.0 / dx;
+        h->fc.inv_2dx = 1.0 / (2 * dx);
+        h->fc.inv_dx2 = 1.0 / (dx * dx);
+        h->fc.inv_dy = 1.0 / dy;
+        h->fc.inv_2dy = 1.0 / (2 * dy);
+        h->fc.inv_dy2 = 1.0 / (dy * dy);
+        if (!h->uniform) {
+            AL(h->dxm, n * 8);
+            AL(h->dym, n * 8);
+            if ((rc = upload(h, h->dxm, dxm.data(), n * 8)) || (rc = upload(h, h->dym, dym.data(), n * 8))) return rc;
+            h->fc.dxm = h->dxm;
+            h->fc.dym = h->dym;
+        }
+    }
+#undef AL
+    if ((rc = upload_static(h))) return rc;
+    if ((rc = kernel_spectrum(h, h->GE, 0)) || (rc = kernel_spectrum(h, h->GN, 1))) return rc;
+    // zero_init_state (src/fastisostasy.f90:505-548): z_bed background 1e6
+    {
+        std::vector<double> bg(n, 1e6);
+        if ((rc = upload(h, d.z_bed, bg.data(), n * 8)) || (rc = upload(h, h->z_bed_ref, bg.data(), n * 8))) return rc;
+        Ctl c0;
+        memset(&c0, 0, sizeof(c0));
+        if ((rc = upload(h, h->ctl, &c0, sizeof(c0)))) return rc;
+    }
+    CK(cudaStreamSynchronize(h->s));
+    return FI_OK;
+}
+
+int fi_destroy(fi_handle* h)
+{
+    if (!h) return FI_OK;
+    if (h->s) cudaStreamSynchronize(h->s);
+    for (void* p : h->allocs) cudaFree(p);
+    if (h->hpin) cudaFreeHost(h->hpin);
+    if (h->s) cudaStreamDestroy(h->s);
+    delete h;
+    return FI_OK;
+}
+
+int fi_dims(const fi_handle* h, int32_t* o)
+{
+    if (!h || !o) return FI_E_ARG;
+    o[0] = h->nx; o[1] = h->ny; o[2] = h->icrop1; o[3] = h->icrop2; o[4] = h->jcrop1; o[5] = h->jcrop2;
+    o[6] = h->nx_ice; o[7] = h->ny_ice;
+    return FI_OK;
+}
+
+int fi_set_fields(fi_handle* h, const double* D_lith, const double* eta_eff, const double* R, const uint8_t* mask)
+{
+    if (!h) return FI_E_ARG;
+    const size_t n = h->n;
+    if (D_lith) h->D.assign(D_lith, D_lith + n);
+    if (eta_eff) h->eta_eff.assign(eta_eff, eta_eff + n);
+    if (R) h->R.assign(R, R + n);
+    if (mask) h->mact.assign(mask, mask + n);
+    return upload_static(h);
+}
+
+int fi_set_kernels(fi_handle* h, const double* GE, const double* GN)
+{
+    if (!h) return FI_E_ARG;
+    int rc;
+    if (GE) { h->GE.assign(GE, GE + h->n); if ((rc = kernel_spectrum(h, h->GE, 0))) return rc; }
+    if (GN) { h->GN.assign(GN, GN + h->n); if ((rc = kernel_spectrum(h, h->GN, 1))) return rc; }
+    return FI_OK;
+}
+
+int fi_init_ref(fi_handle* h, const double* z_bed, const double* H_ice, double bsl, const double* dz_ss)
+{
+    // isos_init_ref, src/fastisostasy.f90:550-575
+    if (!h || !z_bed || !H_ice) return FI_E_ARG;
+    const size_t ni = (size_t)h->nx_ice * h->ny_ice;
+    int rc;
+    if ((rc = upload(h, h->dH, z_bed, ni * 8))) return rc;
+    out2in(h->z_bed_ref, h->dH, h->d, 1e6, 0, h->s);
+    CK(cudaStreamSynchronize(h->s));
+    if ((rc = upload(h, h->dH, H_ice, ni * 8))) return rc;
+    out2in(h->Hice_ref, h->dH, h->d, 0.0, 0, h->s);
+    if (dz_ss) { if ((rc = upload(h, h->dz_ss_ref, dz_ss, h->n * 8))) return rc; }
+    h->ref_bsl = bsl;
+    h->ref_was_set = 1;
+    CK(cudaStreamSynchronize(h->s));
+    return FI_OK;
+}
+
+int fi_init_state(fi_handle* h, const double* z_bed, const double* H_ice, double time, fi_bsl* bsl)
+{
+    // isos_init_state, src/fastisostasy.f90:596-660 (no restart file)
+    if (!h || !z_bed || !H_ice || !bsl) return FI_E_ARG;
+    const size_t ni = (size_t)h->nx_ice * h->ny_ice;
+    const double now_bsl = bsl->bsl_now;
+    int rc;
+    Dom& d = h->d;
+    if ((rc = upload(h, h->dH, z_bed, ni * 8))) return rc;
+    out2in(d.z_bed, h->dH, d, 0.0, 1, h->s);
+    CK(cudaStreamSynchronize(h->s));
+    if ((rc = upload(h, h->dH, H_ice, ni * 8))) return rc;
+    out2in(d.Hice, h->dH, d, 0.0, 1, h->s);
+    CK(cudaStreamSynchronize(h->s));
+    if (!h->ref_was_set) {
+        // isos_init_ref(isos, z_bed, H_ice, now%bsl, now%dz_ss)
+        if ((rc = fi_init_ref(h, z_bed, H_ice, now_bsl, nullptr))) return rc;
+        CK(cudaMemcpyAsync(h->dz_ss_ref, d.dz_ss, h->n * 8, cudaMemcpyDeviceToDevice, h->s));
+    }
+    // ref%z_ss = ref%bsl + 0 + ref%dz_ss ; now%z_ss = now%bsl + now%z_ss + now%dz_ss ; Haf ; masks
+    CK(cudaMemsetAsync(h->z_ss_ref, 0, h->n * 8, h->s));
+    state_diag(h->z_ss_ref, h->z_ss_ref, h->dz_ss_ref, h->ref_bsl, h->z_bed_ref, h->Hice_ref, h->Haf_ref, h->mo_ref,
+               h->mg_ref, h->mc_ref, h->n, d.rho_sw_over_ice, h->s);
+    state_diag(d.z_ss, d.z_ss, d.dz_ss, now_bsl, d.z_bed, d.Hice, d.Haf, d.m_ocean, d.m_grounded, d.m_cont, h->n,
+               d.rho_sw_over_ice, h->s);
+    h->time_prog = time;
+    h->time_diag = time;
+    if ((rc = set_bsl_scalars(h, bsl, true))) return rc;
+    if ((rc = upload(h, h->dH, H_ice, ni * 8))) return rc;
+    // The nested isos_update runs with the ode clock still zero: for time <= 0
+    // its integrator loop does not execute; for time > 0 the reference would
+    // step with dt = 0, which is skipped here.
+    if ((rc = update_any(h, h->dH, time, false))) return rc;
+    // ode%dt = dt_init, ode%t = time, ode%x = now%w
+    CK(cudaMemcpyAsync(d.x, d.w, h->n * 8, cudaMemcpyDeviceToDevice, h->s));
+    Ctl hc;
+    CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    hc.t = time;
+    hc.dt = h->p.dt_init;
+    hc.done = 0;
+    CK(cudaMemcpyAsync(h->ctl, &hc, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    h->h_t = time;
+    h->h_dt = h->p.dt_init;
+    bsl->bsl_now = hc.bsl;
+    h->state_ready = 1;
+    Ctl st;
+    return read_status(h, &st);
+}
+
+int fi_update_async(fi_handle* h, const double* d_H_ice, double time, fi_bsl* bsl)
+{
+    if (!h || !bsl) return FI_E_ARG;
+    if (!h->state_ready) return fail(h, FI_E_STATE, "fi_update before fi_init_state");
+    int rc;
+    if ((rc = set_bsl_scalars(h, bsl, bsl->method == 0 || bsl->method == 1))) return rc;
+    if (d_H_ice) {
+        CK(cudaMemcpyAsync(h->dH, d_H_ice, (size_t)h->nx_ice * h->ny_ice * 8, cudaMemcpyDeviceToDevice, h->s));
+    }
+    return update_any(h, h->dH, time, true);
+}
+
+int fi_synchronize(fi_handle* h)
+{
+    if (!h) return FI_E_ARG;
+    Ctl hc;
+    return read_status(h, &hc);
+}
+
+int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_out* out)
+{
+    if (!h || !H_ice || !bsl) return FI_E_ARG;
+    if (!h->state_ready) return fail(h, FI_E_STATE, "fi_update before fi_init_state");
+    const size_t ni = (size_t)h->nx_ice * h->ny_ice;
+    int rc;
+    memcpy(h->hpin, H_ice, ni * 8);
+    CK(cudaMemcpyAsync(h->dH, h->hpin, ni * 8, cudaMemcpyHostToDevice, h->s));
+    if ((rc = set_bsl_scalars(h, bsl, true))) return rc;
+    if ((rc = update_any(h, h->dH, time, true))) return rc;
+    if (out) {
+        gather(h->gsrc, h->gmsrc, 8, 3, h->d, h->dpack, h->s);
+        CK(cudaMemcpyAsync(h->hpin, h->dpack, ni * 11 * 8, cudaMemcpyDeviceToHost, h->s));
+    }
+    Ctl hc;
+    rc = read_status(h, &hc);
+    bsl->bsl_now = hc.bsl;
+    if (out) {
+        double* dst[8] = {out->z_bed, out->z_ss, out->dz_ss, out->w, out->we, out->dwdt, out->canom_full, out->Hice};
+        for (int f = 0; f < 8; ++f)
+            if (dst[f]) memcpy(dst[f], h->hpin + (size_t)f * ni, ni * 8);
+        uint8_t* mdst[3] = {out->maskocean, out->maskgrounded, out->maskcontinent};
+        for (int f = 0; f < 3; ++f)
+            if (mdst[f]) {
+                const double* src = h->hpin + (size_t)(8 + f) * ni;
+                for (size_t e = 0; e < ni; ++e) mdst[f][e] = src[e] != 0.0;
+            }
+    }
+    return rc;
+}
+
+int fi_bsl_update(fi_bsl* b, double year_bp)
+{
+    // bsl_update, src/barysealevel.f90:195-252 (series from caller tables)
+    if (!b) return FI_E_ARG;
+    auto interp = [](const double* x, const double* y, int n, double xo) {
+        if (xo < x[0]) return y[0];
+        if (xo > x[n - 1]) return y[n - 1];
+        int j = 0;
+        while (j < n && !(x[j] >= xo)) ++j;
+        if (j == 0) return y[0];
+        if (j == n) return y[n - 1];
+        const double a = (xo - x[j - 1]) / (x[j] - x[j - 1]);
+        return y[j - 1] + a * (y[j] - y[j - 1]);
+    };
+    b->time = year_bp;
+    switch (b->method) {
+    case 0: b->bsl_now = b->bsl_init; break;
+    case 1:
+        if (b->n_series < 1) return FI_E_ARG;
+        b->bsl_now = interp(b->series_t, b->series_v, b->n_series, year_bp);
+        break;
+    case 3:
+        if (b->n_series < 1) return FI_E_ARG;
+        b->bsl_now = interp(b->series_t, b->series_v, b->n_series, year_bp);
+        /* fall through */
+    case 2:
+        if (b->constant_ocean_surface || b->n_aocean <= 0) b->A_ocean_now = b->A_ocean_pd;
+        else b->A_ocean_now = interp(b->bsl_vec, b->aocean_vec, b->n_aocean, b->bsl_now);
+        break;
+    default: return FI_E_ARG;
+    }
+    return FI_OK;
+}
+
+int fi_get_field(fi_handle* h, int which, double* out)
+{
+    if (!h || !out) return FI_E_ARG;
+    const size_t n = h->n;
+    const Dom& d = h->d;
+    const double* src = nullptr;
+    const uint8_t* msk = nullptr;
+    const std::vector<double>* hv = nullptr;
+    switch (which) {
+    case FI_FIELD_Z_BED: src = d.z_bed; break;
+    case FI_FIELD_DWDT: src = d.dwdt; break;
+    case FI_FIELD_W: src = d.w; break;
+    case FI_FIELD_WE: src = d.we; break;
+    case FI_FIELD_HAF: src = d.Haf; break;
+    case FI_FIELD_HICE: src = d.Hice; break;
+    case FI_FIELD_Z_SS: src = d.z_ss; break;
+    case FI_FIELD_DZ_SS: src = d.dz_ss; break;
+    case FI_FIELD_CANOM_LOAD: src = d.c_load; break;
+    case FI_FIELD_CANOM_FULL: src = d.c_full; break;
+    case FI_FIELD_MASS_ANOM: src = d.mass; break;
+    case FI_FIELD_MASKOCEAN: msk = d.m_ocean; break;
+    case FI_FIELD_MASKGROUNDED: msk = d.m_grounded; break;
+    case FI_FIELD_MASKCONTINENT: msk = d.m_cont; break;
+    case FI_FIELD_CANOM_MANTLE: src = d.c_mantle; break;
+    case FI_FIELD_CANOM_LITHO: src = d.c_litho; break;
+    case FI_FIELD_CANOM_SEAWATER: src = d.c_sw; break;
+    case FI_FIELD_CANOM_ICE: src = d.c_ice; break;
+    case FI_FIELD_X: src = d.x; break;
+    case FI_FIELD_KAPPA: hv = &h->kappa; break;
+    case FI_FIELD_D_LITH: hv = &h->D; break;
+    case FI_FIELD_ETA_EFF: hv = &h->eta_eff; break;
+    case FI_FIELD_R: hv = &h->R; break;
+    case FI_FIELD_MASKACTIVE: msk = d.mactive; break;
+    case FI_FIELD_GE: hv = &h->GE; break;
+    case FI_FIELD_GN: hv = &h->GN; break;
+    default: return fail(h, FI_E_ARG, "unknown field %d", which);
+    }
+    if (hv) { memcpy(out, hv->data(), n * 8); return FI_OK; }
+    if (src) {
+        CK(cudaMemcpyAsync(out, src, n * 8, cudaMemcpyDeviceToHost, h->s));
+        CK(cudaStreamSynchronize(h->s));
+        return FI_OK;
+    }
+    std::vector<uint8_t> m(n);
+    CK(cudaMemcpyAsync(m.data(), msk, n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    for (size_t e = 0; e < n; ++e) out[e] = m[e];
+    return FI_OK;
+}
+
+int fi_get_scalars(fi_handle* h, double* o)
+{
+    if (!h || !o) return FI_E_ARG;
+    Ctl hc;
+    CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    o[0] = hc.t; o[1] = hc.dt; o[2] = h->time_diag; o[3] = hc.bsl; o[4] = hc.V_af; o[5] = hc.V_den;
+    o[6] = hc.deltaV; o[7] = hc.dbsl_total; o[8] = 0.0; o[9] = (double)hc.n_accept; o[10] = (double)hc.n_reject;
+    o[11] = h->spy; o[12] = h->cc; o[13] = h->Vden; o[14] = (double)h->Px; o[15] = h->ref_bsl;
+    return FI_OK;
+}
+
+int fi_lvelva(fi_handle* h, const double* w, const double* canom_full, double* dwdt)
+{
+    if (!h || !w || !canom_full || !dwdt) return FI_E_ARG;
+    const size_t n = h->n;
+    int rc;
+    double* tmp;
+    if ((rc = dalloc(h, &tmp, n * 8))) return rc;
+    if ((rc = upload(h, h->y, w, n * 8)) || (rc = upload(h, tmp, canom_full, n * 8))) return rc;
+    if (mixed(h)) {
+        q0_from_cf<float>((float*)h->q0, tmp, h->d.mactive, h->p.g, n, h->s);
+        rhs<float>(h, h->y, nullptr, (float*)h->raw[0]);
+        rhs_finish<float>(tmp, (const float*)h->raw[0], h->nx, h->ny, h->spy, h->s);
+    } else {
+        q0_from_cf<double>((double*)h->q0, tmp, h->d.mactive, h->p.g, n, h->s);
+        rhs<double>(h, h->y, nullptr, (double*)h->raw[0]);
+        rhs_finish<double>(tmp, (const double*)h->raw[0], h->nx, h->ny, h->spy, h->s);
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dwdt, tmp, n * 8, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    h->allocs.pop_back();
+    cudaFree(tmp);
+    return FI_OK;
+}
+
+int fi_convolve(fi_handle* h, int kernel, const double* in, double* out)
+{
+    if (!h || !in || !out || kernel < 0 || kernel > 1) return FI_E_ARG;
+    const size_t n = h->n;
+    int rc;
+    if ((rc = upload(h, h->we_raw, in, n * 8))) return rc;
+    if (mixed(h)) {
+        cast_from_double<float>((float*)h->conv_in, h->we_raw, n, h->s);
+        conv<float>(h, kernel, h->dz_raw, h->corners);
+    } else {
+        cast_from_double<double>((double*)h->conv_in, h->we_raw, n, h->s);
+        conv<double>(h, kernel, h->dz_raw, h->corners);
+    }
+    sub_corner(h->we_raw, h->dz_raw, h->corners, n, h->s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, h->we_raw, n * 8, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return FI_OK;
+}
+
+// ---- restart: device state <-> flat double buffer ---------------------------
+namespace {
+struct StateView {
+    std::vector<double*> f;
+    std::vector<uint8_t*> m;
+};
+StateView state_view(fi_handle* h)
+{
+    Dom& d = h->d;
+    StateView v;
+    v.f = {d.z_bed, d.w, d.we, d.Haf, d.Hice, d.z_ss, d.dz_ss, d.dwdt, d.x, d.c_ice, d.c_sw, d.c_litho,
+           d.c_mantle, d.c_load, d.c_full, d.mass, h->z_bed_ref, h->Hice_ref, h->Haf_ref, h->z_ss_ref, h->we_ref,
+           h->w_ref, h->dz_ss_ref};
+    v.m = {d.m_ocean, d.m_grounded, d.m_cont};
+    return v;
+}
+const size_t kScalarSlots = 8 + sizeof(Ctl) / sizeof(double) + 1;
+}  // namespace
+
+size_t fi_state_size(const fi_handle* h)
+{
+    if (!h) return 0;
+    return (23 + 3) * h->n + kScalarSlots;
+}
+
+int fi_state_export(fi_handle* h, double* buf)
+{
+    if (!h || !buf) return FI_E_ARG;
+    StateView v = state_view(h);
+    const size_t n = h->n;
+    size_t off = 0;
+    for (double* p : v.f) { CK(cudaMemcpyAsync(buf + off, p, n * 8, cudaMemcpyDeviceToHost, h->s)); off += n; }
+    std::vector<uint8_t> m(n);
+    for (uint8_t* p : v.m) {
+        CK(cudaMemcpyAsync(m.data(), p, n, cudaMemcpyDeviceToHost, h->s));
+        CK(cudaStreamSynchronize(h->s));
+        for (size_t e = 0; e < n; ++e) buf[off + e] = m[e];
+        off += n;
+    }
+    double* s = buf + off;
+    s[0] = h->time_diag; s[1] = h->time_prog; s[2] = h->h_t; s[3] = h->h_dt; s[4] = h->ref_bsl;
+    s[5] = h->ref_was_set; s[6] = h->state_ready; s[7] = 0.0;
+    CK(cudaMemcpyAsync(s + 8, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return FI_OK;
+}
+
+int fi_state_import(fi_handle* h, const double* buf)
+{
+    if (!h || !buf) return FI_E_ARG;
+    StateView v = state_view(h);
+    const size_t n = h->n;
+    size_t off = 0;
+    for (double* p : v.f) { CK(cudaMemcpyAsync(p, buf + off, n * 8, cudaMemcpyHostToDevice, h->s)); off += n; }
+    CK(cudaStreamSynchronize(h->s));
+    std::vector<uint8_t> m(n);
+    for (uint8_t* p : v.m) {
+        for (size_t e = 0; e < n; ++e) m[e] = buf[off + e] != 0.0;
+        CK(cudaMemcpyAsync(p, m.data(), n, cudaMemcpyHostToDevice, h->s));
+        CK(cudaStreamSynchronize(h->s));
+        off += n;
+    }
+    const double* s = buf + off;
+    h->time_diag = s[0]; h->time_prog = s[1]; h->h_t = s[2]; h->h_dt = s[3]; h->ref_bsl = s[4];
+    h->ref_was_set = (int)s[5]; h->state_ready = (int)s[6];
+    CK(cudaMemcpyAsync(h->ctl, s + 8, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return FI_OK;
+}
+
+}  // extern "C"

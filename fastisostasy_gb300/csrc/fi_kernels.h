@@ -1,0 +1,67 @@
+// fi_kernels.h — host-side launchers of the LV-ELVA device kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fi_common.cuh"
+
+namespace fi {
+
+// Coefficients of the flexure stencil (calc_lvelva, src/lv_elva.f90:95-113).
+struct FlexCoef {
+    double nu, one_minus_nu;
+    double coef_mantle;            // -g*rho_m in true-stage mode (mantle anomaly at the stage state), else 0
+    double inv_dx, inv_2dx, inv_dx2, inv_dy, inv_2dy, inv_dy2;
+    const double* dxm;             // per-cell dx*K, or null for uniform spacing
+    const double* dym;
+};
+
+// One FFT length: factorisation + twiddle tables in both precisions.
+struct FftLen {
+    FftDesc d;
+    const double2* tw64;    // exp(-2 pi i t / n), t < n
+    const float2* tw32;
+};
+
+// A real 2-D transform layout: rows of nx reals -> nx/2+1 complex, pitch sp.
+struct Plan2D {
+    int nx, ny, h, sp;      // h = nx/2, sp = spectrum row pitch (complex elements)
+    FftLen row;             // length h complex
+    FftLen col;             // length ny complex
+    const double2* rtw64;   // exp(-2 pi i k / nx), k <= h
+    const float2* rtw32;
+};
+
+template <typename T>
+void launch_flexure(const double* y, const double* wref, const T* q0, const uint8_t* mask, const T* D,
+                    const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s);
+
+template <typename T>
+void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, typename vec2<T>::type* S,
+                     const Plan2D& p, cudaStream_t s);
+
+template <typename T>
+void launch_cols_hartley(typename vec2<T>::type* S, const T* mA, const T* mB, int even, const Plan2D& p,
+                         cudaStream_t s);
+
+template <typename T>
+void launch_rows_inv(const typename vec2<T>::type* S, T* out, const Plan2D& p, double scale, cudaStream_t s);
+
+// Convolution: columns forward (rows >= nrows_in are zero), multiply by the
+// kernel spectrum K (same layout as S), inverse; only rows listed in
+// out_rows are written back (compacted to rows 0..n_out-1 of S).
+template <typename T>
+void launch_cols_conv(typename vec2<T>::type* S, const typename vec2<T>::type* K, int nrows_in,
+                      const int* out_rows, int n_out, const Plan2D& p, cudaStream_t s);
+
+template <typename T>
+void launch_cols_fwd(typename vec2<T>::type* S, int nrows_in, const Plan2D& p, cudaStream_t s);
+
+// inverse rows of the compacted convolution spectrum, crop + corner values
+template <typename T>
+void launch_conv_rows_inv(const typename vec2<T>::type* S, int n_out, double* out, int nx, int ny, int i_off,
+                          double* corners, int corner_row0, int corner_row1, int corner_col1, const Plan2D& p,
+                          double scale, cudaStream_t s);
+
+}  // namespace fi

@@ -1,0 +1,541 @@
+// fi_rhs.cu — the LV-ELVA viscous-rate pipeline and the FFT convolution
+// passes (calc_lvelva, src/lv_elva.f90:31-126; precomputed_fftconvolution,
+// src/convolutions.f90:59-91).
+//
+// RHS = four kernels:
+//   k_flexure      finite-difference flexure moments and load -> f      (one pass over the grid)
+//   k_rows_fwd     real FFT of every row of f -> half spectrum S
+//   k_cols_hartley column FFT, multiply by 1/(kappa R) in the Hartley basis, inverse column FFT
+//   k_rows_inv     inverse real FFT of the rows, scaled by 1/(nx*ny) -> raw
+// The corner boundary condition and the sec_per_year factor are applied by
+// whichever kernel consumes raw (it reads the four corner values).
+//
+// The reference transforms with FFTW's separable DHT.  The Hartley
+// coefficients are formed from the DFT in the column kernel,
+//   H[k,l] = Re F[k,-l] - Im F[k,l],
+// multiplied by m = 1/(kappa R) at all four (+-k, +-l), and turned back into
+// the DFT of DHT^-1(m H); when m is even in both indices this reduces to
+// F' = m F (flag `even`).
+#include <cstdio>
+
+#include "fi_fft.cuh"
+#include "fi_kernels.h"
+
+namespace fi {
+
+template <typename T> __device__ __forceinline__ const typename vec2<T>::type* twp(const FftLen& L);
+template <> __device__ __forceinline__ const double2* twp<double>(const FftLen& L) { return L.tw64; }
+template <> __device__ __forceinline__ const float2* twp<float>(const FftLen& L) { return L.tw32; }
+template <typename T> __device__ __forceinline__ const typename vec2<T>::type* rtwp(const Plan2D& p);
+template <> __device__ __forceinline__ const double2* rtwp<double>(const Plan2D& p) { return p.rtw64; }
+template <> __device__ __forceinline__ const float2* rtwp<float>(const Plan2D& p) { return p.rtw32; }
+
+static int g_smem_optin = -1;
+static int smem_optin()
+{
+    if (g_smem_optin < 0) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        g_smem_optin = v;
+    }
+    return g_smem_optin;
+}
+
+template <typename K> static void set_smem(K kern, size_t bytes)
+{
+    if (bytes > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+// ---------------------------------------------------------------------------
+// Flexure stencil.  Tile TX x TY outputs with a halo of 2; the first-level
+// differences are taken on the double state, then rounded to T.
+// ---------------------------------------------------------------------------
+constexpr int TX = 32, TY = 8, RX = TX + 4, RY = TY + 4;
+
+template <typename T>
+__global__ void __launch_bounds__(TX* TY)
+k_flexure(const double* __restrict__ y, const double* __restrict__ wref, const T* __restrict__ q0,
+          const uint8_t* __restrict__ mask, const T* __restrict__ D, const T* __restrict__ inv2eta,
+          T* __restrict__ f, int nx, int ny, FlexCoef c)
+{
+    __shared__ double ys[RY][RX];
+    __shared__ T wx[RY][RX];
+    __shared__ T Mxx[RY][RX];
+    __shared__ T Myy[RY][RX];
+    __shared__ T Mxy[RY][RX];
+    __shared__ T Mxyx[RY][RX];
+    const int tid = threadIdx.x + TX * threadIdx.y;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const bool uni = (c.dxm == nullptr);
+
+    // per-cell spacing accessors (uniform fast path)
+    auto idx1 = [&](int i, int j) -> double { return uni ? c.inv_dx : 1.0 / c.dxm[(size_t)j * nx + i]; };
+    auto idx2h = [&](int i, int j) -> double { return uni ? c.inv_2dx : 1.0 / (2 * c.dxm[(size_t)j * nx + i]); };
+    auto idxx = [&](int i, int j) -> double {
+        if (uni) return c.inv_dx2;
+        const double d = c.dxm[(size_t)j * nx + i];
+        return 1.0 / (d * d);
+    };
+    auto idy1 = [&](int i, int j) -> double { return uni ? c.inv_dy : 1.0 / c.dym[(size_t)j * nx + i]; };
+    auto idy2h = [&](int i, int j) -> double { return uni ? c.inv_2dy : 1.0 / (2 * c.dym[(size_t)j * nx + i]); };
+    auto idyy = [&](int i, int j) -> double {
+        if (uni) return c.inv_dy2;
+        const double d = c.dym[(size_t)j * nx + i];
+        return 1.0 / (d * d);
+    };
+
+    for (int e = tid; e < RX * RY; e += TX * TY) {
+        const int lx = e % RX, ly = e / RX;
+        const int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
+        ys[ly][lx] = (gi >= 0 && gi < nx && gj >= 0 && gj < ny) ? y[(size_t)gj * nx + gi] : 0.0;
+    }
+    __syncthreads();
+    // w_x on lx in [1, RX-1), all rows
+    for (int e = tid; e < RX * RY; e += TX * TY) {
+        const int lx = e % RX, ly = e / RX;
+        const int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
+        if (lx < 1 || lx >= RX - 1 || gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
+        double v;
+        if (gi == 0) v = (ys[ly][lx + 1] - ys[ly][lx]) * idx1(gi, gj);
+        else if (gi == nx - 1) v = (ys[ly][lx] - ys[ly][lx - 1]) * idx1(gi, gj);
+        else v = (ys[ly][lx + 1] - ys[ly][lx - 1]) * idx2h(gi, gj);
+        wx[ly][lx] = (T)v;
+    }
+    __syncthreads();
+    // level 1: w_xy, w_xx, w_yy -> moments, on lx, ly in [1, R-1)
+    for (int e = tid; e < RX * RY; e += TX * TY) {
+        const int lx = e % RX, ly = e / RX;
+        const int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
+        if (lx < 1 || lx >= RX - 1 || ly < 1 || ly >= RY - 1 || gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
+        T wxy;
+        if (gj == 0) wxy = (wx[ly + 1][lx] - wx[ly][lx]) * (T)idy1(gi, gj);
+        else if (gj == ny - 1) wxy = (wx[ly][lx] - wx[ly - 1][lx]) * (T)idy1(gi, gj);
+        else wxy = (wx[ly + 1][lx] - wx[ly - 1][lx]) * (T)idy2h(gi, gj);
+        double dxx, dyy;
+        if (gi == 0) dxx = ((ys[ly][lx + 2] - 2 * ys[ly][lx + 1]) + ys[ly][lx]) * idxx(0, gj);
+        else if (gi == nx - 1) dxx = ((ys[ly][lx] - 2 * ys[ly][lx - 1]) + ys[ly][lx - 2]) * idxx(0, gj);
+        else dxx = ((ys[ly][lx + 1] - 2 * ys[ly][lx]) + ys[ly][lx - 1]) * idxx(gi, gj);
+        if (gj == 0) dyy = ((ys[ly + 2][lx] - 2 * ys[ly + 1][lx]) + ys[ly][lx]) * idyy(gi, 0);
+        else if (gj == ny - 1) dyy = ((ys[ly][lx] - 2 * ys[ly - 1][lx]) + ys[ly - 2][lx]) * idyy(gi, gj);
+        else dyy = ((ys[ly + 1][lx] - 2 * ys[ly][lx]) + ys[ly - 1][lx]) * idyy(gi, gj);
+        const T wxx = (T)dxx, wyy = (T)dyy;
+        const T Dl = D[(size_t)gj * nx + gi];
+        const T nu = (T)c.nu;
+        Mxx[ly][lx] = -Dl * (wxx + nu * wyy);
+        Myy[ly][lx] = -Dl * (wyy + nu * wxx);
+        Mxy[ly][lx] = (-Dl * (T)c.one_minus_nu) * wxy;
+    }
+    __syncthreads();
+    // d/dx of Mxy on lx in [2, RX-2), ly in [1, RY-1)
+    for (int e = tid; e < RX * RY; e += TX * TY) {
+        const int lx = e % RX, ly = e / RX;
+        const int gi = i0 - 2 + lx, gj = j0 - 2 + ly;
+        if (lx < 2 || lx >= RX - 2 || ly < 1 || ly >= RY - 1 || gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
+        T v;
+        if (gi == 0) v = (Mxy[ly][lx + 1] - Mxy[ly][lx]) * (T)idx1(gi, gj);
+        else if (gi == nx - 1) v = (Mxy[ly][lx] - Mxy[ly][lx - 1]) * (T)idx1(gi, gj);
+        else v = (Mxy[ly][lx + 1] - Mxy[ly][lx - 1]) * (T)idx2h(gi, gj);
+        Mxyx[ly][lx] = v;
+    }
+    __syncthreads();
+    {
+        const int lx = threadIdx.x + 2, ly = threadIdx.y + 2;
+        const int gi = i0 + threadIdx.x, gj = j0 + threadIdx.y;
+        if (gi < nx && gj < ny) {
+            T mxy_xy, mx_xx, my_yy;
+            if (gj == 0) mxy_xy = (Mxyx[ly + 1][lx] - Mxyx[ly][lx]) * (T)idy1(gi, gj);
+            else if (gj == ny - 1) mxy_xy = (Mxyx[ly][lx] - Mxyx[ly - 1][lx]) * (T)idy1(gi, gj);
+            else mxy_xy = (Mxyx[ly + 1][lx] - Mxyx[ly - 1][lx]) * (T)idy2h(gi, gj);
+            if (gi == 0) mx_xx = ((Mxx[ly][lx + 2] - (T)2 * Mxx[ly][lx + 1]) + Mxx[ly][lx]) * (T)idxx(0, gj);
+            else if (gi == nx - 1) mx_xx = ((Mxx[ly][lx] - (T)2 * Mxx[ly][lx - 1]) + Mxx[ly][lx - 2]) * (T)idxx(0, gj);
+            else mx_xx = ((Mxx[ly][lx + 1] - (T)2 * Mxx[ly][lx]) + Mxx[ly][lx - 1]) * (T)idxx(gi, gj);
+            if (gj == 0) my_yy = ((Myy[ly + 2][lx] - (T)2 * Myy[ly + 1][lx]) + Myy[ly][lx]) * (T)idyy(gi, 0);
+            else if (gj == ny - 1) my_yy = ((Myy[ly][lx] - (T)2 * Myy[ly - 1][lx]) + Myy[ly - 2][lx]) * (T)idyy(gi, gj);
+            else my_yy = ((Myy[ly + 1][lx] - (T)2 * Myy[ly][lx]) + Myy[ly - 1][lx]) * (T)idyy(gi, gj);
+            const size_t e = (size_t)gj * nx + gi;
+            T p = (T)0;
+            if (mask[e]) {
+                double pm = (double)q0[e];
+                if (wref) pm += c.coef_mantle * (ys[ly][lx] - wref[e]);
+                p = (T)pm;
+            }
+            f[e] = (((p + mx_xx) + (T)2 * mxy_xy) + my_yy) * inv2eta[e];
+        }
+    }
+}
+
+template <typename T>
+void launch_flexure(const double* y, const double* wref, const T* q0, const uint8_t* mask, const T* D,
+                    const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s)
+{
+    dim3 b(TX, TY), g((nx + TX - 1) / TX, (ny + TY - 1) / TY);
+    k_flexure<T><<<g, b, 0, s>>>(y, wref, q0, mask, D, inv2eta, f, nx, ny, c);
+}
+
+// ---------------------------------------------------------------------------
+// Row transforms.  A block handles RB rows; nx real samples are packed as
+// h = nx/2 complex samples (z[m] = x[2m] + i x[2m+1]).
+// ---------------------------------------------------------------------------
+static int rows_per_block(int h)
+{
+    int rb = 512 / (h > 0 ? h : 1);
+    if (rb < 1) rb = 1;
+    if (rb > 8) rb = 8;
+    return rb;
+}
+static int threads_for(int work)
+{
+    int t = 32;
+    while (t < work && t < 256) t *= 2;
+    return t;
+}
+
+template <typename T>
+__global__ void k_rows_fwd(const T* __restrict__ in, int in_pitch, int in_width, int nrows_in,
+                           typename vec2<T>::type* __restrict__ S, Plan2D p, int RB)
+{
+    typedef typename vec2<T>::type C2;
+    extern __shared__ unsigned char smem_raw[];
+    C2* b0 = reinterpret_cast<C2*>(smem_raw);
+    C2* b1 = b0 + RB * p.h;
+    const int h = p.h;
+    const int j0 = blockIdx.x * RB;
+    const int nthr = blockDim.x;
+    for (int e = threadIdx.x; e < RB * h; e += nthr) {
+        const int line = e / h, m = e - line * h;
+        const int j = j0 + line;
+        C2 v = mk2<T>((T)0, (T)0);
+        if (j < nrows_in) {
+            const T* row = in + (size_t)j * in_pitch;
+            const int i = 2 * m;
+            if (i + 1 < in_width) {
+                if ((in_pitch & 1) == 0) v = *reinterpret_cast<const C2*>(row + i);
+                else v = mk2<T>(row[i], row[i + 1]);
+            } else if (i < in_width) {
+                v = mk2<T>(row[i], (T)0);
+            }
+        }
+        b0[e] = v;
+    }
+    __syncthreads();
+    C2* r = block_fft<T>(b0, b1, p.row.d, RB, h, twp<T>(p.row), -1);
+    const C2* rtw = rtwp<T>(p);
+    for (int e = threadIdx.x; e < RB * (h + 1); e += nthr) {
+        const int line = e / (h + 1), k = e - line * (h + 1);
+        const int j = j0 + line;
+        if (j >= nrows_in) continue;
+        const C2 Zk = r[line * h + (k == h ? 0 : k)];
+        const C2 Zc = r[line * h + (k == 0 ? 0 : h - k)];
+        C2 E, O;
+        E.x = (T)0.5 * (Zk.x + Zc.x);
+        E.y = (T)0.5 * (Zk.y - Zc.y);
+        O.x = (T)0.5 * (Zk.y + Zc.y);
+        O.y = (T)-0.5 * (Zk.x - Zc.x);
+        S[(size_t)j * p.sp + k] = cadd(E, cmul(__ldg(rtw + k), O));
+    }
+}
+
+template <typename T>
+void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, typename vec2<T>::type* S,
+                     const Plan2D& p, cudaStream_t s)
+{
+    typedef typename vec2<T>::type C2;
+    const int RB = rows_per_block(p.h);
+    const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
+    set_smem(k_rows_fwd<T>, sm);
+    const int nblk = (nrows_in + RB - 1) / RB;
+    k_rows_fwd<T><<<nblk, threads_for(RB * p.h / 4), sm, s>>>(in, in_pitch, in_width, nrows_in, S, p, RB);
+}
+
+template <typename T>
+__global__ void k_rows_inv(const typename vec2<T>::type* __restrict__ S, int nrows, T* __restrict__ out,
+                           int out_pitch, Plan2D p, int RB, T scale)
+{
+    typedef typename vec2<T>::type C2;
+    extern __shared__ unsigned char smem_raw[];
+    C2* b0 = reinterpret_cast<C2*>(smem_raw);
+    C2* b1 = b0 + RB * p.h;
+    const int h = p.h;
+    const int j0 = blockIdx.x * RB;
+    const int nthr = blockDim.x;
+    const C2* rtw = rtwp<T>(p);
+    // Z[k] = (X[k] + conj X[h-k]) + i conj(w^k) (X[k] - conj X[h-k])
+    for (int e = threadIdx.x; e < RB * h; e += nthr) {
+        const int line = e / h, k = e - line * h;
+        const int j = j0 + line;
+        C2 z = mk2<T>((T)0, (T)0);
+        if (j < nrows) {
+            const C2 A = S[(size_t)j * p.sp + k];
+            C2 B = S[(size_t)j * p.sp + (h - k)];
+            B.y = -B.y;
+            const C2 sum = cadd(A, B), dif = csub(A, B);
+            const C2 t = cmulc(dif, __ldg(rtw + k));
+            z.x = sum.x - t.y;
+            z.y = sum.y + t.x;
+        }
+        b0[e] = z;
+    }
+    __syncthreads();
+    C2* r = block_fft<T>(b0, b1, p.row.d, RB, h, twp<T>(p.row), +1);
+    for (int e = threadIdx.x; e < RB * h; e += nthr) {
+        const int line = e / h, m = e - line * h;
+        const int j = j0 + line;
+        if (j >= nrows) continue;
+        C2 v = r[e];
+        v.x *= scale;
+        v.y *= scale;
+        *reinterpret_cast<C2*>(out + (size_t)j * out_pitch + 2 * m) = v;
+    }
+}
+
+template <typename T>
+void launch_rows_inv(const typename vec2<T>::type* S, T* out, const Plan2D& p, double scale, cudaStream_t s)
+{
+    typedef typename vec2<T>::type C2;
+    const int RB = rows_per_block(p.h);
+    const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
+    set_smem(k_rows_inv<T>, sm);
+    const int nblk = (p.ny + RB - 1) / RB;
+    k_rows_inv<T><<<nblk, threads_for(RB * p.h / 4), sm, s>>>(S, p.ny, out, p.nx, p, RB, (T)scale);
+}
+
+// ---------------------------------------------------------------------------
+// Column kernels.  A block loads CB spectrum columns (all ny rows) into
+// shared memory, column-major, and transforms them together.
+// ---------------------------------------------------------------------------
+template <typename T> static int cols_per_block(int ny)
+{
+    typedef typename vec2<T>::type C2;
+    const size_t per_col = 2 * (size_t)ny * sizeof(C2);
+    int cb = (int)((96 * 1024) / per_col);
+    if (cb > 16) cb = 16;
+    if (cb < 1) cb = 1;
+    return cb;
+}
+
+template <typename T>
+__device__ __forceinline__ void load_cols(typename vec2<T>::type* b0, const typename vec2<T>::type* S, int k0,
+                                          int CB, int nrows_in, const Plan2D& p)
+{
+    typedef typename vec2<T>::type C2;
+    const int ny = p.col.d.n;
+    for (int e = threadIdx.x; e < CB * ny; e += blockDim.x) {
+        const int c = e % CB, l = e / CB;
+        const int k = k0 + c;
+        C2 v = mk2<T>((T)0, (T)0);
+        if (k <= p.h && l < nrows_in) v = S[(size_t)l * p.sp + k];
+        b0[c * ny + l] = v;
+    }
+}
+
+template <typename T>
+__global__ void k_cols_hartley(typename vec2<T>::type* __restrict__ S, const T* __restrict__ mA,
+                               const T* __restrict__ mB, int even, Plan2D p, int CB)
+{
+    typedef typename vec2<T>::type C2;
+    extern __shared__ unsigned char smem_raw[];
+    const int ny = p.col.d.n;
+    C2* b0 = reinterpret_cast<C2*>(smem_raw);
+    C2* b1 = b0 + (size_t)CB * ny;
+    const int k0 = blockIdx.x * CB;
+    load_cols<T>(b0, S, k0, CB, ny, p);
+    __syncthreads();
+    C2* r = block_fft<T>(b0, b1, p.col.d, CB, ny, twp<T>(p.col), -1);
+    const int half = ny / 2 + 1;
+    for (int e = threadIdx.x; e < CB * half; e += blockDim.x) {
+        const int c = e % CB, l = e / CB;
+        const int k = k0 + c;
+        if (k > p.h) continue;
+        const int lm = (ny - l) % ny;
+        C2* col = r + (size_t)c * ny;
+        const size_t ia = (size_t)l * p.sp + k, ib = (size_t)lm * p.sp + k;
+        const C2 Fa = col[l], Fb = col[lm];
+        if (even) {
+            const T ma = mA[ia], mb = mA[ib];
+            C2 a = Fa, b = Fb;
+            a.x *= ma; a.y *= ma;
+            b.x *= mb; b.y *= mb;
+            col[l] = a;
+            if (lm != l) col[lm] = b;
+        } else {
+            // Hartley values at (k,l), (-k,-l), (-k,l), (k,-l)
+            const T H_kl = Fb.x - Fa.y, H_mkml = Fb.x + Fa.y;
+            const T H_mkl = Fa.x + Fb.y, H_kml = Fa.x - Fb.y;
+            const T G_kl = mA[ia] * H_kl, G_kml = mA[ib] * H_kml;
+            const T G_mkl = mB[ia] * H_mkl, G_mkml = mB[ib] * H_mkml;
+            C2 a, b;
+            a.x = (T)0.5 * (G_kml + G_mkl);
+            a.y = (T)0.5 * (G_mkml - G_kl);
+            b.x = (T)0.5 * (G_kl + G_mkml);
+            b.y = (T)0.5 * (G_mkl - G_kml);
+            col[l] = a;
+            if (lm != l) col[lm] = b;
+        }
+    }
+    __syncthreads();
+    C2* other = (r == b0) ? b1 : b0;
+    C2* q = block_fft<T>(r, other, p.col.d, CB, ny, twp<T>(p.col), +1);
+    for (int e = threadIdx.x; e < CB * ny; e += blockDim.x) {
+        const int c = e % CB, l = e / CB;
+        const int k = k0 + c;
+        if (k <= p.h) S[(size_t)l * p.sp + k] = q[c * ny + l];
+    }
+}
+
+template <typename T>
+void launch_cols_hartley(typename vec2<T>::type* S, const T* mA, const T* mB, int even, const Plan2D& p,
+                         cudaStream_t s)
+{
+    typedef typename vec2<T>::type C2;
+    const int CB = cols_per_block<T>(p.ny);
+    const size_t sm = 2 * (size_t)CB * p.ny * sizeof(C2);
+    set_smem(k_cols_hartley<T>, sm);
+    const int nblk = (p.h + 1 + CB - 1) / CB;
+    k_cols_hartley<T><<<nblk, threads_for(CB * p.ny / 4), sm, s>>>(S, mA, mB, even, p, CB);
+}
+
+template <typename T>
+__global__ void k_cols_conv(typename vec2<T>::type* __restrict__ S, const typename vec2<T>::type* __restrict__ K,
+                            int nrows_in, const int* __restrict__ out_rows, int n_out, Plan2D p, int CB, int do_inv)
+{
+    typedef typename vec2<T>::type C2;
+    extern __shared__ unsigned char smem_raw[];
+    const int ny = p.col.d.n;
+    C2* b0 = reinterpret_cast<C2*>(smem_raw);
+    C2* b1 = b0 + (size_t)CB * ny;
+    const int k0 = blockIdx.x * CB;
+    load_cols<T>(b0, S, k0, CB, nrows_in, p);
+    __syncthreads();
+    C2* r = block_fft<T>(b0, b1, p.col.d, CB, ny, twp<T>(p.col), -1);
+    if (!do_inv) {
+        for (int e = threadIdx.x; e < CB * ny; e += blockDim.x) {
+            const int c = e % CB, l = e / CB;
+            const int k = k0 + c;
+            if (k <= p.h) S[(size_t)l * p.sp + k] = r[c * ny + l];
+        }
+        return;
+    }
+    for (int e = threadIdx.x; e < CB * ny; e += blockDim.x) {
+        const int c = e % CB, l = e / CB;
+        const int k = k0 + c;
+        if (k > p.h) continue;
+        r[c * ny + l] = cmul(r[c * ny + l], K[(size_t)l * p.sp + k]);
+    }
+    __syncthreads();
+    C2* other = (r == b0) ? b1 : b0;
+    C2* q = block_fft<T>(r, other, p.col.d, CB, ny, twp<T>(p.col), +1);
+    for (int e = threadIdx.x; e < CB * n_out; e += blockDim.x) {
+        const int c = e % CB, o = e / CB;
+        const int k = k0 + c;
+        if (k <= p.h) S[(size_t)o * p.sp + k] = q[c * ny + out_rows[o]];
+    }
+}
+
+template <typename T>
+void launch_cols_conv(typename vec2<T>::type* S, const typename vec2<T>::type* K, int nrows_in, const int* out_rows,
+                      int n_out, const Plan2D& p, cudaStream_t s)
+{
+    typedef typename vec2<T>::type C2;
+    const int CB = cols_per_block<T>(p.ny);
+    const size_t sm = 2 * (size_t)CB * p.ny * sizeof(C2);
+    set_smem(k_cols_conv<T>, sm);
+    const int nblk = (p.h + 1 + CB - 1) / CB;
+    k_cols_conv<T><<<nblk, threads_for(CB * p.ny / 4), sm, s>>>(S, K, nrows_in, out_rows, n_out, p, CB, 1);
+}
+
+template <typename T>
+void launch_cols_fwd(typename vec2<T>::type* S, int nrows_in, const Plan2D& p, cudaStream_t s)
+{
+    typedef typename vec2<T>::type C2;
+    const int CB = cols_per_block<T>(p.ny);
+    const size_t sm = 2 * (size_t)CB * p.ny * sizeof(C2);
+    set_smem(k_cols_conv<T>, sm);
+    const int nblk = (p.h + 1 + CB - 1) / CB;
+    k_cols_conv<T><<<nblk, threads_for(CB * p.ny / 4), sm, s>>>(S, nullptr, nrows_in, nullptr, 0, p, CB, 0);
+}
+
+// Inverse rows of the compacted convolution spectrum.  Rows 0..ny-1 are the
+// cropped output rows; rows ny and ny+1 are the linear-lag rows 0 and
+// 2*ny-2 that hold the corner values of apply_zerobc_at_corners_dp.
+template <typename T>
+__global__ void k_conv_rows_inv(const typename vec2<T>::type* __restrict__ S, int n_out, double* __restrict__ out,
+                                int nx, int ny, int i_off, double* __restrict__ corners, int col1, Plan2D p,
+                                int RB, T scale)
+{
+    typedef typename vec2<T>::type C2;
+    extern __shared__ unsigned char smem_raw[];
+    C2* b0 = reinterpret_cast<C2*>(smem_raw);
+    C2* b1 = b0 + RB * p.h;
+    const int h = p.h;
+    const int j0 = blockIdx.x * RB;
+    const int nthr = blockDim.x;
+    const C2* rtw = rtwp<T>(p);
+    for (int e = threadIdx.x; e < RB * h; e += nthr) {
+        const int line = e / h, k = e - line * h;
+        const int j = j0 + line;
+        C2 z = mk2<T>((T)0, (T)0);
+        if (j < n_out) {
+            const C2 A = S[(size_t)j * p.sp + k];
+            C2 B = S[(size_t)j * p.sp + (h - k)];
+            B.y = -B.y;
+            const C2 sum = cadd(A, B), dif = csub(A, B);
+            const C2 t = cmulc(dif, __ldg(rtw + k));
+            z.x = sum.x - t.y;
+            z.y = sum.y + t.x;
+        }
+        b0[e] = z;
+    }
+    __syncthreads();
+    C2* r = block_fft<T>(b0, b1, p.row.d, RB, h, twp<T>(p.row), +1);
+    const T* rr = reinterpret_cast<const T*>(r);
+    for (int e = threadIdx.x; e < RB * nx; e += nthr) {
+        const int line = e / nx, i = e - line * nx;
+        const int j = j0 + line;
+        if (j < ny) out[(size_t)j * nx + i] = (double)(rr[(size_t)line * 2 * h + i_off + i] * scale);
+    }
+    if (threadIdx.x == 0) {
+        for (int line = 0; line < RB; ++line) {
+            const int j = j0 + line;
+            const T* row = rr + (size_t)line * 2 * h;
+            if (j == ny) {            // linear lag row 0
+                corners[0] = (double)(row[0] * scale);
+                corners[3] = (double)(row[col1] * scale);
+            } else if (j == ny + 1) { // linear lag row 2*ny-2
+                corners[2] = (double)(row[0] * scale);
+                corners[1] = (double)(row[col1] * scale);
+            }
+        }
+    }
+}
+
+template <typename T>
+void launch_conv_rows_inv(const typename vec2<T>::type* S, int n_out, double* out, int nx, int ny, int i_off,
+                          double* corners, int /*corner_row0*/, int /*corner_row1*/, int corner_col1,
+                          const Plan2D& p, double scale, cudaStream_t s)
+{
+    typedef typename vec2<T>::type C2;
+    const int RB = rows_per_block(p.h);
+    const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
+    set_smem(k_conv_rows_inv<T>, sm);
+    const int nblk = (n_out + RB - 1) / RB;
+    k_conv_rows_inv<T><<<nblk, threads_for(RB * p.h / 4), sm, s>>>(S, n_out, out, nx, ny, i_off, corners,
+                                                                   corner_col1, p, RB, (T)scale);
+}
+
+#define FI_INST(T)                                                                                            \
+    template void launch_flexure<T>(const double*, const double*, const T*, const uint8_t*, const T*, const T*, \
+                                    T*, int, int, const FlexCoef&, cudaStream_t);                             \
+    template void launch_rows_fwd<T>(const T*, int, int, int, vec2<T>::type*, const Plan2D&, cudaStream_t);   \
+    template void launch_cols_hartley<T>(vec2<T>::type*, const T*, const T*, int, const Plan2D&, cudaStream_t); \
+    template void launch_rows_inv<T>(const vec2<T>::type*, T*, const Plan2D&, double, cudaStream_t);          \
+    template void launch_cols_conv<T>(vec2<T>::type*, const vec2<T>::type*, int, const int*, int, const Plan2D&, \
+                                      cudaStream_t);                                                          \
+    template void launch_cols_fwd<T>(vec2<T>::type*, int, const Plan2D&, cudaStream_t);                       \
+    template void launch_conv_rows_inv<T>(const vec2<T>::type*, int, double*, int, int, int, double*, int, int,  \
+                                          int, const Plan2D&, double, cudaStream_t);
+
+FI_INST(double)
+FI_INST(float)
+
+}  // namespace fi

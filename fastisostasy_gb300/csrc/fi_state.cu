@@ -1,0 +1,632 @@
+// fi_state.cu — sea level, column anomalies, barystatic sums, integrator
+// stages and the update tail, all in double precision.
+//
+// Restates, per cell and fused into few passes:
+//   calc_Haf, calc_masks, calc_columnanoms_*, calc_mass_anom, calc_z_ss,
+//   calc_sl_contributions                       src/sealevel.f90:25-205
+//   the bsl_now update of isos_update           src/fastisostasy.f90:766-777
+//   step_euler / step_rk4 / step_tsit54 stages  src/integrators.f90:12-203
+//   the update tail + check_isos_instabilities  src/fastisostasy.f90:856-899
+// Grid reductions are deterministic: every block reduces its cells in a
+// fixed tree, writes one partial, and the last block to arrive combines the
+// partials in block order.
+#include <cstdio>
+
+#include "fi_state.h"
+
+namespace fi {
+
+constexpr int NT = 256;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Reduce NV values per thread across the block (sum or max per slot).
+template <int NV>
+__device__ __forceinline__ void block_reduce(double (&v)[NV], const bool (&is_max)[NV], double* sh)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = is_max[q] ? warp_max(v[q]) : warp_sum(v[q]);
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sh[wid * NV + q] = v[q];
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double a = (lane < nw) ? sh[lane * NV + q] : (is_max[q] ? 0.0 : 0.0);
+            v[q] = is_max[q] ? warp_max(a) : warp_sum(a);
+        }
+    }
+}
+
+// Block partials -> last block combines in block order.  Returns true in the
+// thread 0 of the last block, with the totals in `tot`.
+template <int NV>
+__device__ bool grid_finish(double (&v)[NV], const bool (&is_max)[NV], double* partials, unsigned* counter,
+                            double (&tot)[NV])
+{
+    __shared__ double sh[32 * NV];
+    __shared__ bool last;
+    block_reduce<NV>(v, is_max, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) partials[(size_t)blockIdx.x * NV + q] = v[q];
+        __threadfence();
+        const unsigned prev = atomicAdd(counter, 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    if (threadIdx.x == 0) {
+        __threadfence();
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double a = is_max[q] ? 0.0 : 0.0;
+            for (unsigned b = 0; b < gridDim.x; ++b) {
+                const double pb = ((volatile double*)partials)[(size_t)b * NV + q];
+                a = is_max[q] ? fmax(a, pb) : a + pb;
+            }
+            tot[q] = a;
+        }
+        *counter = 0u;
+        return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool in_crop(const Dom& d, int i, int j)
+{
+    return i >= d.i0 && i < d.i0 + d.nxi && j >= d.j0 && j < d.j0 + d.nyi;
+}
+
+// --- 1. Hice <- H_ice, Haf, sea-level contribution sums -------------------
+__global__ void __launch_bounds__(NT) k_upd_begin(Dom d, const double* __restrict__ H_ice)
+{
+    double v[2] = {0.0, 0.0};
+    const bool mx[2] = {false, false};
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        const int i = (int)(e % d.nx), j = (int)(e / d.nx);
+        double H = 0.0;
+        if (H_ice && in_crop(d, i, j)) H = H_ice[(size_t)(j - d.j0) * d.nxi + (i - d.i0)];
+        else if (!H_ice) H = d.Hice[e];
+        d.Hice[e] = H;
+        // calc_Haf, src/sealevel.f90:132-145
+        double h = (d.z_ss[e] - d.z_bed[e]) * d.rho_sw_over_ice;
+        if (h < 0.0) h = 0.0;
+        h = H - h;
+        if (h < 0.0) h = 0.0;
+        d.Haf[e] = h;
+        v[0] += (h - d.Haf_ref[e]) * d.A[e];
+        v[1] += ((H - d.Hice_ref[e]) * d.Vden) * d.A[e];
+    }
+    double tot[2];
+    if (grid_finish<2>(v, mx, d.partials, &d.ctl->counter[0], tot)) {
+        Ctl* c = d.ctl;
+        const double V_old = (c->V_af + c->V_den) + c->V_pov;
+        c->V_af = tot[0] * d.rho_ice_over_sw;
+        c->V_den = tot[1];
+        c->V_pov = 0.0;
+        c->deltaV = ((c->V_af + c->V_den) + c->V_pov) - V_old;
+        // bsl_now update, src/fastisostasy.f90:766-777
+        if (c->bsl_method == 2) c->bsl = c->bsl - c->deltaV / c->A_ocean;
+        if (c->bsl_method == 3) {
+            c->dbsl_total = c->dbsl_total + c->deltaV / c->A_ocean;
+            c->bsl = c->bsl - c->dbsl_total;
+        }
+    }
+}
+
+// --- 2. z_ss, masks, ice/seawater/load anomalies (+ elastic conv input) ---
+template <typename T>
+__global__ void __launch_bounds__(NT) k_upd_masks(Dom d, T* __restrict__ conv_in)
+{
+    const double bsl = d.ctl->bsl;
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        const double zss = (bsl + d.z_ss_ref[e]) + d.dz_ss[e];
+        d.z_ss[e] = zss;
+        const double Haf = d.Haf[e], H = d.Hice[e];
+        const bool cont = d.z_bed[e] > zss;
+        const bool grd = (H > 0.0) && (Haf > 0.0);
+        const bool ocean = !(cont || grd);
+        d.m_cont[e] = cont;
+        d.m_grounded[e] = grd;
+        d.m_ocean[e] = ocean;
+        const double cice = 0.0 + d.rho_ice * (Haf - d.Haf_ref[e]);
+        const double csw = 0.0 + (ocean ? d.rho_w * (zss - d.z_ss_ref[e]) : 0.0);
+        d.c_ice[e] = cice;
+        d.c_sw[e] = csw;
+        double cl = cice;
+        if (d.interactive) cl = cl + csw;
+        cl = d.mactive[e] ? cl : 0.0;
+        d.c_load[e] = cl;
+        if (conv_in) conv_in[e] = (T)((cl * d.g) * d.K2[e]);
+    }
+}
+
+// --- 3. elastic displacement, lithosphere/full anomalies, mass (+ geoid input)
+// we_mode: 0 keep we, 1 we = we_raw - corner mean, 2 we = 0
+template <typename T>
+__global__ void __launch_bounds__(NT)
+k_upd_litho(Dom d, const double* __restrict__ we_raw, const double* __restrict__ corners, int we_mode,
+            T* __restrict__ conv_in)
+{
+    double cm = 0.0;
+    if (we_mode == 1) cm = corner_mean(corners[0], corners[1], corners[2], corners[3]);
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        double we = d.we[e];
+        if (we_mode == 1) we = we_raw[e] - cm;
+        else if (we_mode == 2) we = 0.0;
+        d.we[e] = we;
+        const double cli = 0.0 + d.rho_l * (we - d.we_ref[e]);
+        d.c_litho[e] = cli;
+        const bool act = d.mactive[e];
+        const double cf = act ? (d.c_load[e] + cli) + d.c_mantle[e] : 0.0;
+        d.c_full[e] = cf;
+        const double ma = act ? d.A[e] * cf : 0.0;
+        d.mass[e] = ma;
+        if (conv_in) conv_in[e] = (T)ma;
+    }
+}
+
+// --- 4. sea-surface perturbation, z_ss, masks, load; RHS load term q0 ------
+// dz_mode: 0 keep, 1 dz_ss = raw - corner mean, 2 dz_ss = 0
+// stage_mode 0 (reference): q0 = -g * canom_full (mantle anomaly frozen);
+// stage_mode 1 (true stages): q0 = -g * (canom_load + canom_litho).
+template <typename T>
+__global__ void __launch_bounds__(NT)
+k_upd_load(Dom d, const double* __restrict__ dz_raw, const double* __restrict__ corners, int dz_mode,
+           T* __restrict__ q0, int stage_mode, double tf)
+{
+    double cm = 0.0;
+    if (dz_mode == 1) cm = corner_mean(corners[0], corners[1], corners[2], corners[3]);
+    const double bsl = d.ctl->bsl;
+    const bool will_step = d.ctl->t < tf;   // get_dwdt refreshes canom_full only if a step runs
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        double dz = d.dz_ss[e];
+        if (dz_mode == 1) dz = dz_raw[e] - cm;
+        else if (dz_mode == 2) dz = 0.0;
+        d.dz_ss[e] = dz;
+        const double zss = (bsl + d.z_ss_ref[e]) + dz;
+        d.z_ss[e] = zss;
+        const double Haf = d.Haf[e], H = d.Hice[e];
+        const bool cont = d.z_bed[e] > zss;
+        const bool grd = (H > 0.0) && (Haf > 0.0);
+        const bool ocean = !(cont || grd);
+        d.m_cont[e] = cont;
+        d.m_grounded[e] = grd;
+        d.m_ocean[e] = ocean;
+        const double csw = 0.0 + (ocean ? d.rho_w * (zss - d.z_ss_ref[e]) : 0.0);
+        d.c_sw[e] = csw;
+        double cl = d.c_ice[e];
+        if (d.interactive) cl = cl + csw;
+        const bool act = d.mactive[e];
+        cl = act ? cl : 0.0;
+        d.c_load[e] = cl;
+        if (stage_mode == 0) {
+            const double cf = act ? (cl + d.c_litho[e]) + d.c_mantle[e] : 0.0;
+            if (will_step) d.c_full[e] = cf;
+            q0[e] = (T)(act ? -d.g * cf : 0.0);
+        } else {
+            q0[e] = (T)(act ? -d.g * (cl + d.c_litho[e]) : 0.0);
+        }
+    }
+}
+
+// --- integrator control ------------------------------------------------------
+// kind 0 euler (clips ode%dt), 1 rk4 (local h), 2 tsit54 (clips ode%dt)
+__global__ void k_step_begin(Ctl* c, double tf, int kind)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (c->status != ST_OK || !(c->t < tf)) { c->done = 1; return; }
+    c->done = 0;
+    c->tf = tf;
+    if (kind == 1) c->h = fmin(c->dt, tf - c->t);
+    else { c->dt = fmin(c->dt, tf - c->t); c->h = c->dt; }
+}
+
+// y = x + (a*h) * k,  k = (raw - corner_mean(raw)) * spy
+template <typename T>
+__global__ void __launch_bounds__(NT)
+k_rk_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __restrict__ x, const T* __restrict__ raw,
+           double a, int nx, int ny, double spy)
+{
+    if (c->done) return;
+    const double ah = a * c->h;
+    const double cm = corner_mean_of(raw, nx, ny);
+    const size_t n = (size_t)nx * ny;
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+        const double k = ((double)raw[e] - cm) * spy;
+        y[e] = x[e] + ah * k;
+    }
+}
+
+// RK4 combination x += (h/6)*(k1 + 2k2 + 2k3 + k4), w = x, t += h.
+// Reference mode passes the same raw four times (get_dwdt ignores its state).
+template <typename T>
+__global__ void __launch_bounds__(NT)
+k_rk4_final(Ctl* c, double* __restrict__ x, double* __restrict__ w, const T* __restrict__ r1,
+            const T* __restrict__ r2, const T* __restrict__ r3, const T* __restrict__ r4, int nx, int ny,
+            double spy)
+{
+    if (c->done) return;
+    const double h6 = c->h / 6;
+    const double c1 = corner_mean_of(r1, nx, ny), c2 = corner_mean_of(r2, nx, ny);
+    const double c3 = corner_mean_of(r3, nx, ny), c4 = corner_mean_of(r4, nx, ny);
+    const size_t n = (size_t)nx * ny;
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+        const double k1 = ((double)r1[e] - c1) * spy, k2 = ((double)r2[e] - c2) * spy;
+        const double k3 = ((double)r3[e] - c3) * spy, k4 = ((double)r4[e] - c4) * spy;
+        const double v = x[e] + h6 * (((k1 + 2 * k2) + 2 * k3) + k4);
+        x[e] = v;
+        w[e] = v;
+    }
+}
+
+__global__ void k_step_end(Ctl* c)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0 || c->done) return;
+    c->t = c->t + c->h;
+    c->n_accept++;
+}
+
+// Euler: x += dt*k, w = x
+template <typename T>
+__global__ void __launch_bounds__(NT)
+k_euler_final(const Ctl* __restrict__ c, double* __restrict__ x, double* __restrict__ w, const T* __restrict__ r1,
+              int nx, int ny, double spy)
+{
+    if (c->done) return;
+    const double h = c->h;
+    const double c1 = corner_mean_of(r1, nx, ny);
+    const size_t n = (size_t)nx * ny;
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+        const double v = x[e] + h * (((double)r1[e] - c1) * spy);
+        x[e] = v;
+        w[e] = v;
+    }
+}
+
+// --- Tsitouras 5(4), reference-compatible (single distinct RHS value) --------
+__constant__ double c_ts_b[6] = {0.0845, 0.0, 0.0, 0.5179, 0.1276, 0.2700};
+__constant__ double c_ts_bh[6] = {0.0845, 0.0, 0.0, 0.5179, 0.1276, 0.2700 - 1 / 5.0};
+
+__device__ __forceinline__ void ts_x12(double x, double k, double dt, double& x1, double& x2)
+{
+    double a1 = x, a2 = x;
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
+        a1 = a1 + (dt * c_ts_bh[s]) * k;
+        a2 = a2 + (dt * c_ts_b[s]) * k;
+    }
+    x1 = a1;
+    x2 = a2;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT)
+k_ts_max(Dom d, const T* __restrict__ raw, double atol, double rtol)
+{
+    Ctl* c = d.ctl;
+    if (c->done) return;
+    const double dt = c->h;
+    const double cm = corner_mean_of(raw, d.nx, d.ny);
+    double v[2] = {0.0, 0.0};
+    const bool mx[2] = {true, true};
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        const double k = ((double)raw[e] - cm) * d.spy;
+        double x1, x2;
+        ts_x12(d.x[e], k, dt, x1, x2);
+        v[0] = fmax(v[0], fabs(x1));
+        v[1] = fmax(v[1], fabs(x2));
+    }
+    double tot[2];
+    if (grid_finish<2>(v, mx, d.partials, &c->counter[1], tot)) c->tol = atol + rtol * fmax(tot[0], tot[1]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT)
+k_ts_err(Dom d, const T* __restrict__ raw, double q, double dt_max, int max_reject)
+{
+    Ctl* c = d.ctl;
+    if (c->done) return;
+    const double dt = c->h, tol = c->tol;
+    const double cm = corner_mean_of(raw, d.nx, d.ny);
+    double v[1] = {0.0};
+    const bool mx[1] = {false};
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        const double k = ((double)raw[e] - cm) * d.spy;
+        double x1, x2;
+        ts_x12(d.x[e], k, dt, x1, x2);
+        const double r = (x2 - x1) / tol;
+        v[0] += r * r;
+    }
+    double tot[1];
+    if (grid_finish<1>(v, mx, d.partials, &c->counter[2], tot)) {
+        const double err = sqrt(tot[0] / (double)d.n);
+        c->err = err;
+        c->n_attempt++;
+        if (err < 1) {
+            c->accepted = 1;
+            c->t = c->t + dt;
+            c->dt = fmin(dt * pow(1 / err, 1 / q), dt_max);
+            c->n_accept++;
+        } else {
+            c->accepted = 0;
+            c->dt = dt * 0.5;
+            c->n_reject++;
+            if (c->n_reject > max_reject) { c->status = ST_STEP; c->done = 1; }
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_ts_commit(Dom d, const T* __restrict__ raw)
+{
+    const Ctl* c = d.ctl;
+    if (c->done || !c->accepted) return;
+    const double dt = c->h;
+    const double cm = corner_mean_of(raw, d.nx, d.ny);
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        const double k = ((double)raw[e] - cm) * d.spy;
+        double x1, x2;
+        ts_x12(d.x[e], k, dt, x1, x2);
+        d.x[e] = x2;
+        d.w[e] = x2;
+    }
+}
+
+// --- update tail -----------------------------------------------------------
+// w -= corner mean (apply_zerobc_at_corners), canom_mantle, z_bed, dwdt output,
+// instability and NaN checks (src/fastisostasy.f90:856-869, :874-899).
+template <typename T>
+__global__ void __launch_bounds__(NT) k_upd_end(Dom d, const T* __restrict__ raw_last, int have_rhs)
+{
+    const double cw = corner_mean_of(d.w, d.nx, d.ny);
+    double cr = 0.0;
+    if (have_rhs) cr = corner_mean_of(raw_last, d.nx, d.ny);
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    const bool mx[4] = {true, true, true, true};
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        const double w = d.w[e] - cw;
+        d.wout[e] = w;
+        d.c_mantle[e] = 0.0 + d.rho_m * (w - d.w_ref[e]);
+        const double zb = (d.z_bed_ref[e] + w) + d.we[e];
+        d.z_bed[e] = zb;
+        if (have_rhs) d.dwdt[e] = ((double)raw_last[e] - cr) * d.spy;
+        v[0] = fmax(v[0], fabs(w));
+        v[1] = fmax(v[1], fabs(d.we[e]));
+        v[2] = fmax(v[2], fabs(d.dz_ss[e]));
+        if (zb != zb) v[3] = 1.0;
+    }
+    double tot[4];
+    if (grid_finish<4>(v, mx, d.partials, &d.ctl->counter[3], tot)) {
+        Ctl* c = d.ctl;
+        c->red[0] = tot[0]; c->red[1] = tot[1]; c->red[2] = tot[2];
+        if (c->status == ST_OK) {
+            if (tot[0] > 1e5 || tot[1] > 1e5 || tot[2] > 1e3) c->status = ST_LARGE;
+            if (tot[3] != 0.0) c->status = ST_NAN;
+        }
+    }
+}
+
+// w was written to d.wout (a separate buffer) so that every block read the
+// uncorrected corners; copy it back.
+__global__ void __launch_bounds__(NT) k_copy(double* __restrict__ dst, const double* __restrict__ src, size_t n)
+{
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) dst[e] = src[e];
+}
+
+// Gather cropped outputs (cropstate2out, src/isos_utils.f90:386-405) into a
+// packed buffer: nf fields of nxi*nyi doubles.
+__global__ void __launch_bounds__(NT)
+k_gather(const double* const* __restrict__ src, const uint8_t* const* __restrict__ msrc, int nf, int nm, Dom d,
+         double* __restrict__ out)
+{
+    const size_t nc = (size_t)d.nxi * d.nyi;
+    const size_t tot = nc * (nf + nm);
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < tot; e += (size_t)gridDim.x * NT) {
+        const int f = (int)(e / nc);
+        const size_t r = e - (size_t)f * nc;
+        const int i = (int)(r % d.nxi), j = (int)(r / d.nxi);
+        const size_t g = (size_t)(j + d.j0) * d.nx + (i + d.i0);
+        out[e] = f < nf ? src[f][g] : (double)msrc[f - nf][g];
+    }
+}
+
+// Scatter an ice-grid field into the padded grid: background outside the crop.
+__global__ void __launch_bounds__(NT)
+k_out2in(double* __restrict__ dst, const double* __restrict__ src, Dom d, double background, int keep_outside)
+{
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        const int i = (int)(e % d.nx), j = (int)(e / d.nx);
+        if (in_crop(d, i, j)) dst[e] = src[(size_t)(j - d.j0) * d.nxi + (i - d.i0)];
+        else if (!keep_outside) dst[e] = background;
+    }
+}
+
+// calc_z_ss, calc_Haf and calc_masks of one state (isos_init_state)
+__global__ void __launch_bounds__(NT)
+k_state_diag(double* z_ss, const double* zss_base, const double* dz_ss, double bsl, const double* z_bed,
+             const double* Hice, double* Haf, uint8_t* mo, uint8_t* mg, uint8_t* mc, size_t n, double rho_sw_over_ice)
+{
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+        const double zss = (bsl + zss_base[e]) + dz_ss[e];
+        z_ss[e] = zss;
+        double h = (zss - z_bed[e]) * rho_sw_over_ice;
+        if (h < 0.0) h = 0.0;
+        h = Hice[e] - h;
+        if (h < 0.0) h = 0.0;
+        Haf[e] = h;
+        const bool cont = z_bed[e] > zss;
+        const bool grd = (Hice[e] > 0.0) && (h > 0.0);
+        mc[e] = cont;
+        mg[e] = grd;
+        mo[e] = !(cont || grd);
+    }
+}
+
+// ---------------------------------------------------------------------------
+static int grid_for(size_t n)
+{
+    size_t b = (n + NT - 1) / NT;
+    if (b > 152 * 8) b = 152 * 8;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+int reduce_blocks(size_t n) { return grid_for(n); }
+
+void upd_begin(const Dom& d, const double* H_ice, cudaStream_t s)
+{
+    k_upd_begin<<<grid_for(d.n), NT, 0, s>>>(d, H_ice);
+}
+template <typename T> void upd_masks(const Dom& d, T* conv_in, cudaStream_t s)
+{
+    k_upd_masks<T><<<grid_for(d.n), NT, 0, s>>>(d, conv_in);
+}
+template <typename T>
+void upd_litho(const Dom& d, const double* we_raw, const double* corners, int we_mode, T* conv_in, cudaStream_t s)
+{
+    k_upd_litho<T><<<grid_for(d.n), NT, 0, s>>>(d, we_raw, corners, we_mode, conv_in);
+}
+template <typename T>
+void upd_load(const Dom& d, const double* dz_raw, const double* corners, int dz_mode, T* q0, int stage_mode,
+              double tf, cudaStream_t s)
+{
+    k_upd_load<T><<<grid_for(d.n), NT, 0, s>>>(d, dz_raw, corners, dz_mode, q0, stage_mode, tf);
+}
+void step_begin(Ctl* c, double tf, int kind, cudaStream_t s) { k_step_begin<<<1, 32, 0, s>>>(c, tf, kind); }
+void step_end(Ctl* c, cudaStream_t s) { k_step_end<<<1, 32, 0, s>>>(c); }
+template <typename T>
+void rk_stage(const Ctl* c, double* y, const double* x, const T* raw, double a, int nx, int ny, double spy,
+              cudaStream_t s)
+{
+    k_rk_stage<T><<<grid_for((size_t)nx * ny), NT, 0, s>>>(c, y, x, raw, a, nx, ny, spy);
+}
+template <typename T>
+void rk4_final(Ctl* c, double* x, double* w, const T* r1, const T* r2, const T* r3, const T* r4, int nx, int ny,
+               double spy, cudaStream_t s)
+{
+    k_rk4_final<T><<<grid_for((size_t)nx * ny), NT, 0, s>>>(c, x, w, r1, r2, r3, r4, nx, ny, spy);
+}
+template <typename T>
+void euler_final(const Ctl* c, double* x, double* w, const T* r1, int nx, int ny, double spy, cudaStream_t s)
+{
+    k_euler_final<T><<<grid_for((size_t)nx * ny), NT, 0, s>>>(c, x, w, r1, nx, ny, spy);
+}
+template <typename T> void ts_max(const Dom& d, const T* raw, double atol, double rtol, cudaStream_t s)
+{
+    k_ts_max<T><<<grid_for(d.n), NT, 0, s>>>(d, raw, atol, rtol);
+}
+template <typename T> void ts_err(const Dom& d, const T* raw, double q, double dt_max, int max_reject, cudaStream_t s)
+{
+    k_ts_err<T><<<grid_for(d.n), NT, 0, s>>>(d, raw, q, dt_max, max_reject);
+}
+template <typename T> void ts_commit(const Dom& d, const T* raw, cudaStream_t s)
+{
+    k_ts_commit<T><<<grid_for(d.n), NT, 0, s>>>(d, raw);
+}
+template <typename T> void upd_end(const Dom& d, const T* raw_last, int have_rhs, cudaStream_t s)
+{
+    k_upd_end<T><<<grid_for(d.n), NT, 0, s>>>(d, raw_last, have_rhs);
+    k_copy<<<grid_for(d.n), NT, 0, s>>>(d.w, d.wout, d.n);
+}
+void gather(const double* const* src, const uint8_t* const* msrc, int nf, int nm, const Dom& d, double* out,
+            cudaStream_t s)
+{
+    k_gather<<<grid_for((size_t)d.nxi * d.nyi * (nf + nm)), NT, 0, s>>>(src, msrc, nf, nm, d, out);
+}
+void out2in(double* dst, const double* src, const Dom& d, double background, int keep_outside, cudaStream_t s)
+{
+    k_out2in<<<grid_for(d.n), NT, 0, s>>>(dst, src, d, background, keep_outside);
+}
+void state_diag(double* z_ss, const double* zss_base, const double* dz_ss, double bsl, const double* z_bed,
+                const double* Hice, double* Haf, uint8_t* mo, uint8_t* mg, uint8_t* mc, size_t n,
+                double rho_sw_over_ice, cudaStream_t s)
+{
+    k_state_diag<<<grid_for(n), NT, 0, s>>>(z_ss, zss_base, dz_ss, bsl, z_bed, Hice, Haf, mo, mg, mc, n,
+                                             rho_sw_over_ice);
+}
+
+
+// --- small helpers for the single-function entry points ---------------------
+template <typename T>
+__global__ void __launch_bounds__(NT) k_rhs_finish(double* __restrict__ out, const T* __restrict__ raw, int nx, int ny,
+                                                   double spy)
+{
+    const double cm = corner_mean_of(raw, nx, ny);
+    const size_t n = (size_t)nx * ny;
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
+        out[e] = ((double)raw[e] - cm) * spy;
+}
+
+__global__ void __launch_bounds__(NT) k_sub_corner(double* __restrict__ out, const double* __restrict__ raw,
+                                                   const double* __restrict__ corners, size_t n)
+{
+    const double cm = corner_mean(corners[0], corners[1], corners[2], corners[3]);
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) out[e] = raw[e] - cm;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_cast(T* __restrict__ dst, const double* __restrict__ src, size_t n)
+{
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) dst[e] = (T)src[e];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_q0_from_cf(T* __restrict__ q0, const double* __restrict__ cf,
+                                                   const uint8_t* __restrict__ mask, double g, size_t n)
+{
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
+        q0[e] = (T)(mask[e] ? -g * cf[e] : 0.0);
+}
+
+template <typename T> void rhs_finish(double* out, const T* raw, int nx, int ny, double spy, cudaStream_t s)
+{
+    k_rhs_finish<T><<<grid_for((size_t)nx * ny), NT, 0, s>>>(out, raw, nx, ny, spy);
+}
+void sub_corner(double* out, const double* raw, const double* corners, size_t n, cudaStream_t s)
+{
+    k_sub_corner<<<grid_for(n), NT, 0, s>>>(out, raw, corners, n);
+}
+template <typename T> void cast_from_double(T* dst, const double* src, size_t n, cudaStream_t s)
+{
+    k_cast<T><<<grid_for(n), NT, 0, s>>>(dst, src, n);
+}
+template <typename T> void q0_from_cf(T* q0, const double* cf, const uint8_t* mask, double g, size_t n, cudaStream_t s)
+{
+    k_q0_from_cf<T><<<grid_for(n), NT, 0, s>>>(q0, cf, mask, g, n);
+}
+
+#define FI_STATE_INST(T)                                                                                      \
+    template void upd_masks<T>(const Dom&, T*, cudaStream_t);                                                 \
+    template void upd_litho<T>(const Dom&, const double*, const double*, int, T*, cudaStream_t);              \
+    template void upd_load<T>(const Dom&, const double*, const double*, int, T*, int, double, cudaStream_t);  \
+    template void rk_stage<T>(const Ctl*, double*, const double*, const T*, double, int, int, double, cudaStream_t); \
+    template void rk4_final<T>(Ctl*, double*, double*, const T*, const T*, const T*, const T*, int, int, double,  \
+                               cudaStream_t);                                                                 \
+    template void euler_final<T>(const Ctl*, double*, double*, const T*, int, int, double, cudaStream_t);     \
+    template void ts_max<T>(const Dom&, const T*, double, double, cudaStream_t);                              \
+    template void ts_err<T>(const Dom&, const T*, double, double, int, cudaStream_t);                         \
+    template void ts_commit<T>(const Dom&, const T*, cudaStream_t);                                           \
+    template void upd_end<T>(const Dom&, const T*, int, cudaStream_t);                                       \
+    template void rhs_finish<T>(double*, const T*, int, int, double, cudaStream_t);                          \
+    template void cast_from_double<T>(T*, const double*, size_t, cudaStream_t);                               \
+    template void q0_from_cf<T>(T*, const double*, const uint8_t*, double, size_t, cudaStream_t);
+
+FI_STATE_INST(double)
+FI_STATE_INST(float)
+
+}  // namespace fi

@@ -1,0 +1,67 @@
+// fi_state.h — device pointers and launchers of the sea-level / integrator
+// kernels (double precision state).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fi_common.cuh"
+
+namespace fi {
+
+// Everything the per-cell update kernels touch for one domain.
+struct Dom {
+    int nx, ny;
+    size_t n;
+    int i0, j0, nxi, nyi;              // 0-based crop origin and ice-grid size
+    int interactive;
+    double rho_ice, rho_w, rho_m, rho_l, g, Vden, spy;
+    double rho_sw_over_ice, rho_ice_over_sw;
+    const double* A;
+    const double* K2;                  // K**2
+    const uint8_t* mactive;
+    // reference state
+    const double *z_bed_ref, *Hice_ref, *Haf_ref, *z_ss_ref, *we_ref, *w_ref;
+    // current state
+    double *z_bed, *w, *wout, *we, *Haf, *Hice, *z_ss, *dz_ss, *dwdt, *x;
+    double *c_ice, *c_sw, *c_litho, *c_mantle, *c_load, *c_full, *mass;
+    uint8_t *m_ocean, *m_grounded, *m_cont;
+    Ctl* ctl;
+    double* partials;                  // >= reduce_blocks(n) * 4 doubles
+};
+
+int reduce_blocks(size_t n);
+void upd_begin(const Dom& d, const double* H_ice, cudaStream_t s);
+template <typename T> void upd_masks(const Dom& d, T* conv_in, cudaStream_t s);
+template <typename T>
+void upd_litho(const Dom& d, const double* we_raw, const double* corners, int we_mode, T* conv_in, cudaStream_t s);
+template <typename T>
+void upd_load(const Dom& d, const double* dz_raw, const double* corners, int dz_mode, T* q0, int stage_mode,
+              double tf, cudaStream_t s);
+void step_begin(Ctl* c, double tf, int kind, cudaStream_t s);
+void step_end(Ctl* c, cudaStream_t s);
+template <typename T>
+void rk_stage(const Ctl* c, double* y, const double* x, const T* raw, double a, int nx, int ny, double spy,
+              cudaStream_t s);
+template <typename T>
+void rk4_final(Ctl* c, double* x, double* w, const T* r1, const T* r2, const T* r3, const T* r4, int nx, int ny,
+               double spy, cudaStream_t s);
+template <typename T>
+void euler_final(const Ctl* c, double* x, double* w, const T* r1, int nx, int ny, double spy, cudaStream_t s);
+template <typename T> void ts_max(const Dom& d, const T* raw, double atol, double rtol, cudaStream_t s);
+template <typename T>
+void ts_err(const Dom& d, const T* raw, double q, double dt_max, int max_reject, cudaStream_t s);
+template <typename T> void ts_commit(const Dom& d, const T* raw, cudaStream_t s);
+template <typename T> void upd_end(const Dom& d, const T* raw_last, int have_rhs, cudaStream_t s);
+void gather(const double* const* src, const uint8_t* const* msrc, int nf, int nm, const Dom& d, double* out,
+            cudaStream_t s);
+void out2in(double* dst, const double* src, const Dom& d, double background, int keep_outside, cudaStream_t s);
+void state_diag(double* z_ss, const double* zss_base, const double* dz_ss, double bsl, const double* z_bed,
+                const double* Hice, double* Haf, uint8_t* mo, uint8_t* mg, uint8_t* mc, size_t n,
+                double rho_sw_over_ice, cudaStream_t s);
+template <typename T> void rhs_finish(double* out, const T* raw, int nx, int ny, double spy, cudaStream_t s);
+void sub_corner(double* out, const double* raw, const double* corners, size_t n, cudaStream_t s);
+template <typename T> void cast_from_double(T* dst, const double* src, size_t n, cudaStream_t s);
+template <typename T> void q0_from_cf(T* q0, const double* cf, const uint8_t* mask, double g, size_t n, cudaStream_t s);
+
+}  // namespace fi

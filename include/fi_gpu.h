@@ -1,0 +1,165 @@
+/*
+ * fi_gpu.h — C ABI of the GB300 LV-ELVA library (libfigpu.so).
+ *
+ * Drop-in boundary for FastIsostasy's LV-ELVA path (method = 3).  Each entry
+ * point replaces one reference routine of module `fastisostasy`
+ * (src/fastisostasy.f90) or `barysealevel` (src/barysealevel.f90); the
+ * Fortran caller keeps its isos_class / bsl_class and binds these functions
+ * through iso_c_binding.
+ *
+ * Conventions
+ *   - Arrays are plain host pointers in the reference's Fortran layout:
+ *     a field (nx, ny) is contiguous with x fastest.  "Ice grid" arrays are
+ *     (nx_ice, ny_ice); "padded" arrays are (nx, ny) of the padded domain
+ *     (fi_dims).  Masks are uint8_t 0/1 (Fortran logical on the caller side
+ *     converts with merge(1_c_int8_t, 0_c_int8_t, mask)).
+ *   - Every call returns an int status; the reference `stop`s instead
+ *     (e.g. src/fastisostasy.f90:197, 853, 868, 897).  fi_last_error() gives
+ *     the message.
+ *   - Device buffers are owned by the handle; the caller owns every host
+ *     array.  Each handle has its own CUDA stream; handles are independent
+ *     and may be driven from different host threads.
+ *   - There is no CPU fallback: fi_create fails with FI_E_CUDA when no CUDA
+ *     device is usable.
+ */
+#ifndef FI_GPU_H
+#define FI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    FI_OK = 0,
+    FI_E_NAN = 1,      /* NaN in z_bed (src/fastisostasy.f90:864-869) */
+    FI_E_LARGE = 2,    /* |w|,|we| > 1e5 or |dz_ss| > 1e3 (check_isos_instabilities :874-899) */
+    FI_E_STEP = 3,     /* adaptive step rejected too often (the reference loops forever) */
+    FI_E_OOM = 4,      /* device allocation failed */
+    FI_E_CONFIG = 5,   /* unsupported configuration (the reference's `stop`s in isos_init) */
+    FI_E_CUDA = 6,     /* CUDA runtime error */
+    FI_E_TIMEOUT = 7,  /* a bounded device wait expired */
+    FI_E_ARG = 8,      /* invalid argument */
+    FI_E_STATE = 9     /* call out of order (e.g. update before init_state) */
+};
+
+enum { FI_PREC_FP64 = 0, FI_PREC_MIXED = 1 };
+
+/* isos_param_class (src/isostasy_defs.f90:34-100) after isos_par_load's
+ * unit conversion (src/fastisostasy.f90:925-1015): lengths in m, E in GPa.
+ * String options are integer codes. */
+typedef struct {
+    int32_t method;                 /* must be 3 (LV-ELVA) */
+    int32_t interactive_sealevel;
+    int32_t include_elastic;
+    int32_t heterogeneous_ssh;
+    int32_t correct_compression;
+    int32_t lithosphere;            /* 0 uniform, 1 gaussian_plus, 2 gaussian_minus, 3 caller field */
+    int32_t mantle;                 /* 0 uniform, 1 gaussian_plus, 2 gaussian_minus, 3 caller field */
+    int32_t layering;               /* 0 equalized, 1 parallel */
+    int32_t lumping;                /* 0 bottom, 1 min, 2 max, 3 mean, 4 logmean, 5 freqdomain */
+    int32_t visc_scaling_method;    /* 0 none, 1 scale, 2 min, 3 max */
+    int32_t nl;                     /* viscous layers, 1..8 */
+    int32_t dt_method;              /* 0 euler, 1 rk4, 2 tsit54 */
+    int32_t stage_mode;             /* 0 reference-compatible stages, 1 true stages */
+    int32_t nx_target, ny_target;   /* 0: reference square padding; else explicit even sizes */
+    int32_t precision;              /* FI_PREC_FP64 or FI_PREC_MIXED */
+    double dt_diagnostics, min_pad, viscosity_scaling;
+    double zl[8], viscosities[8], dl, eta_ref;
+    double E, nu, rho_water, rho_ice, rho_seawater, rho_uppermantle, rho_litho, g;
+    double r_earth, m_earth;
+    double atol, rtol, dt_min, dt_max, dt_init, q;
+} fi_params;
+
+/* bsl_class (src/barysealevel.f90:16-29); series arrays are caller-owned
+ * tables replacing the reference's file readers. */
+typedef struct {
+    int32_t method;                 /* 0 const, 1 file, 2 fastiso, 3 mixed */
+    int32_t constant_ocean_surface;
+    int32_t n_series, n_aocean;
+    double bsl_init, bsl_now, A_ocean_now, A_ocean_pd, time;
+    const double *series_t, *series_v;
+    const double *bsl_vec, *aocean_vec;
+} fi_bsl;
+
+/* isos_out_class (src/isostasy_defs.f90:185-200): ice-grid outputs, any
+ * pointer may be NULL. */
+typedef struct {
+    double *z_bed, *z_ss, *dz_ss, *w, *we, *dwdt, *canom_full, *Hice;
+    uint8_t *maskocean, *maskgrounded, *maskcontinent;
+} fi_out;
+
+typedef struct fi_handle fi_handle;
+
+/* Replaces isos_init (src/fastisostasy.f90:64-473), method-3 branch:
+ * domain padding (init_domain_size, src/isos_utils.f90:285-354), kappa,
+ * rigidity, effective viscosity and R, Green's-function spectra, maskactive.
+ * K_or_null is the padded (nx, ny) distortion field or NULL (K = 1). */
+int fi_create(const fi_params* p, int nx_ice, int ny_ice, double dx, double dy, const double* K_or_null,
+              fi_handle** out);
+/* Replaces isos_end (src/fastisostasy.f90:911-923). */
+int fi_destroy(fi_handle* h);
+/* nx, ny, icrop1, icrop2, jcrop1, jcrop2 (1-based like the reference), nx_ice, ny_ice */
+int fi_dims(const fi_handle* h, int32_t* out8);
+/* Caller-computed padded fields (the rheology_file / mask_file branches of
+ * isos_init, src/fastisostasy.f90:185-214, 262-417).  eta_eff is final.
+ * Any pointer may be NULL (kept). */
+int fi_set_fields(fi_handle* h, const double* D_lith, const double* eta_eff, const double* R,
+                  const uint8_t* maskactive);
+/* Replace the elastic (GE) and geoid (GN) Green's functions (padded (nx, ny),
+ * centred like calc_elastic_green, src/green_functions.f90:43-91);
+ * spectra are recomputed.  Either may be NULL. */
+int fi_set_kernels(fi_handle* h, const double* GE, const double* GN);
+/* Replaces isos_init_ref (src/fastisostasy.f90:550-575). */
+int fi_init_ref(fi_handle* h, const double* z_bed, const double* H_ice, double bsl, const double* dz_ss_or_null);
+/* Replaces isos_init_state (src/fastisostasy.f90:596-660), without restart. */
+int fi_init_state(fi_handle* h, const double* z_bed, const double* H_ice, double time, fi_bsl* bsl);
+/* Replaces isos_update (src/fastisostasy.f90:731-872).  H_ice is ice grid;
+ * outputs are copied to `out` (may be NULL).  Synchronous. */
+int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_out* out);
+/* Asynchronous isos_update for device-resident inputs: d_H_ice is a DEVICE
+ * pointer to the ice-grid thickness (NULL keeps the previous one).  Valid for
+ * bsl methods const and file; returns before the work completes. */
+int fi_update_async(fi_handle* h, const double* d_H_ice, double time, fi_bsl* bsl);
+/* Waits for the handle's stream; returns the device status (FI_E_NAN, ...). */
+int fi_synchronize(fi_handle* h);
+/* Replaces bsl_update (src/barysealevel.f90:195-252). */
+int fi_bsl_update(fi_bsl* b, double year_bp);
+
+/* Inspection of padded fields; `which` follows FI_FIELD_*. */
+enum {
+    FI_FIELD_Z_BED = 0, FI_FIELD_DWDT = 1, FI_FIELD_W = 2, FI_FIELD_WE = 3, FI_FIELD_HAF = 4,
+    FI_FIELD_HICE = 5, FI_FIELD_Z_SS = 6, FI_FIELD_DZ_SS = 7, FI_FIELD_CANOM_LOAD = 8,
+    FI_FIELD_CANOM_FULL = 9, FI_FIELD_MASS_ANOM = 10, FI_FIELD_MASKOCEAN = 11, FI_FIELD_MASKGROUNDED = 12,
+    FI_FIELD_MASKCONTINENT = 13, FI_FIELD_CANOM_MANTLE = 14, FI_FIELD_CANOM_LITHO = 15,
+    FI_FIELD_CANOM_SEAWATER = 16, FI_FIELD_CANOM_ICE = 17, FI_FIELD_X = 18, FI_FIELD_KAPPA = 19,
+    FI_FIELD_D_LITH = 20, FI_FIELD_ETA_EFF = 21, FI_FIELD_R = 22, FI_FIELD_MASKACTIVE = 23,
+    FI_FIELD_GE = 24, FI_FIELD_GN = 25
+};
+int fi_get_field(fi_handle* h, int which, double* out_padded);
+/* t, dt, time_diagnostics, bsl, V_af, V_den, deltaV_bsl, dbsl_total, n_rhs,
+ * n_accept, n_reject, sec_per_year, compressibility, Vden_factor, conv size, bsl_ref */
+int fi_get_scalars(fi_handle* h, double* out16);
+
+/* calc_lvelva (src/lv_elva.f90:31-126) on padded host arrays with this
+ * handle's rigidity, viscosity, kappa, R, maskactive and spacing. */
+int fi_lvelva(fi_handle* h, const double* w, const double* canom_full, double* dwdt);
+/* precomputed_fftconvolution (src/convolutions.f90:59-91) with the elastic
+ * (kernel 0) or geoid (kernel 1) spectrum. */
+int fi_convolve(fi_handle* h, int kernel, const double* in_padded, double* out_padded);
+
+/* Restart support: the complete device state (fields + integrator clock) as
+ * doubles; bit-identical round trip. */
+size_t fi_state_size(const fi_handle* h);
+int fi_state_export(fi_handle* h, double* buf);
+int fi_state_import(fi_handle* h, const double* buf);
+
+const char* fi_last_error(const fi_handle* h);
+int fi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

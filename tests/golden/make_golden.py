@@ -1,0 +1,44 @@
+"""Regenerates the golden fixtures in this folder.
+
+1. params_<test>.json: the reference's experiment namelists
+   (par/test_isostasy_<test>.nml of the reference project) parsed with
+   fastisostasy_gb300.params — needs the reference tree, so it only runs
+   where that tree is mounted (pass its path as argv[1]).
+2. oracle_golden.npz: outputs of the cases in tests/make_golden_cases.py.
+
+Usage: python tests/golden/make_golden.py [path/to/reference]
+"""
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [ROOT, os.path.dirname(HERE)]
+
+import numpy as np  # noqa: E402
+
+from fastisostasy_gb300 import params as P  # noqa: E402
+
+TESTS = ["test1d", "test1e", "test2a", "test2b", "test2c", "test3a", "test3b", "test3c", "test3d"]
+
+
+def main():
+    if len(sys.argv) > 1:
+        ref = sys.argv[1]
+        for t in TESTS:
+            path = os.path.join(ref, "par", "test_isostasy_%s.nml" % t)
+            p = P.load(path)
+            with open(os.path.join(HERE, "params_%s.json" % t), "w") as fh:
+                json.dump(p, fh, indent=1, sort_keys=True)
+    import make_golden_cases as MG
+    out = {}
+    for name, fn in MG.CASES.items():
+        for k, v in fn().items():
+            out[name + "__" + k] = v
+    np.savez_compressed(os.path.join(HERE, "oracle_golden.npz"), **out)
+    print("wrote", len(out), "arrays")
+
+
+if __name__ == "__main__":
+    main()

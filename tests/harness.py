@@ -1,0 +1,62 @@
+"""Shared test helpers: paired GPU / oracle runs of one workload."""
+import numpy as np
+
+from fastisostasy_gb300 import _lib
+from fastisostasy_gb300 import workloads as W
+from fastisostasy_gb300.isostasy import Domain
+from oracle import oracle as O
+
+
+def gpu_bsl(method=0, bsl_init=0.0, A_ocean_pd=3.625e14):
+    b = _lib.FiBsl()
+    b.method = method
+    b.constant_ocean_surface = 1
+    b.bsl_init = bsl_init
+    b.bsl_now = bsl_init
+    b.A_ocean_pd = A_ocean_pd
+    b.A_ocean_now = A_ocean_pd
+    return b
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+class Pair:
+    """Runs the same workload through the GPU library and the oracle."""
+
+    def __init__(self, wl: W.Workload, precision=0, gpu=True):
+        self.wl = wl
+        self.orc = O.Model(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
+        self.dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=precision) if gpu else None
+        f = wl.padded_fields(self.orc.nx, self.orc.ny)
+        if f:
+            self.orc.set_fields(**f)
+            if self.dom is not None:
+                self.dom.set_fields(**f)
+        m = wl.bsl.get("method", 0)
+        self.bo = O.make_bsl(m, wl.bsl.get("bsl_init", 0.0), wl.bsl.get("A_ocean_pd", 3.625e14))
+        self.bg = gpu_bsl(m, wl.bsl.get("bsl_init", 0.0), wl.bsl.get("A_ocean_pd", 3.625e14))
+        self.t = 0.0
+
+    def init(self, t0=0.0):
+        self.t = t0
+        rc = self.orc.init_state(self.wl.z_bed, self.wl.H_at(t0), t0, self.bo)
+        assert rc == 0
+        if self.dom is not None:
+            self.dom.init_state(self.wl.z_bed, self.wl.H_at(t0), t0, self.bg)
+
+    def step(self, n=1):
+        for _ in range(n):
+            self.t += self.wl.dtt
+            O.lib().orc_bsl_update(self.bo, self.t)
+            rc = self.orc.update(self.wl.H_at(self.t), self.t, self.bo)
+            assert rc == 0, "oracle update failed with %d at t=%g" % (rc, self.t)
+            if self.dom is not None:
+                _lib.load().fi_bsl_update(self.bg, self.t)
+                self.dom.update(self.wl.H_at(self.t), self.t, self.bg)
+
+    def close(self):
+        if self.dom is not None:
+            self.dom.close()
+        self.orc.close()

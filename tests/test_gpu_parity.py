@@ -1,0 +1,198 @@
+"""GPU parity tests: libfigpu.so (through the C ABI) against the oracle.
+
+Bars: plain FP64 form within 1e-10 of max|value| in every floating field,
+masks bit-exact; mixed FP32/FP64 form within 1e-5 of max|u|.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from fastisostasy_gb300 import _lib
+from fastisostasy_gb300 import workloads as W
+from fastisostasy_gb300.isostasy import Domain
+from harness import Pair, gpu_bsl, rel
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL64 = 1e-10
+TOLMIX = 1e-5
+
+
+def params(name, **over):
+    with open(os.path.join(GOLDEN, "params_%s.json" % name)) as fh:
+        p = json.load(fh)
+    p.update(over)
+    return p
+
+
+def random_case(nx, ny, seed, even_R):
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal((ny, nx)) * 100
+    cf = rng.standard_normal((ny, nx)) * 1e5
+    mask = (rng.random((ny, nx)) > 0.15).astype(np.uint8)
+    D = 1e24 * (1 + rng.random((ny, nx)))
+    eta = 1e21 * (1 + rng.random((ny, nx)))
+    R = np.ones((ny, nx)) if even_R else 1 + 0.2 * rng.random((ny, nx))
+    return w, cf, mask, D, eta, R
+
+
+@pytest.mark.parametrize("nx,ny,even", [(16, 16, True), (32, 32, False), (64, 64, True), (128, 128, False),
+                                        (122, 122, True), (48, 80, False), (256, 256, True), (192, 192, False)])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_lvelva(nx, ny, even, precision):
+    """calc_lvelva (src/lv_elva.f90:31-126) on random fields."""
+    dx = 50e3
+    p = params("test1d", nx_target=nx if nx != ny else 0, ny_target=ny if nx != ny else 0)
+    dom = Domain(p, nx, ny, dx, precision=precision)
+    assert (dom.nx, dom.ny) == (nx, ny)
+    w, cf, mask, D, eta, R = random_case(nx, ny, nx * 7 + ny, even)
+    dom.set_fields(D_lith=D, eta_eff=eta, R=R, maskactive=mask)
+    got = dom.lvelva(w, cf)
+    kap = dom.field("kappa")
+    dxm = np.full((ny, nx), dx)
+    ref = O.lvelva(w, cf, mask, p["g"], p["nu"], D, eta, R, kap, dxm, dxm, dom.scalars()["sec_per_year"])
+    assert rel(got, ref) <= (TOL64 if precision == 0 else TOLMIX)
+    dom.close()
+
+
+@pytest.mark.parametrize("n", [16, 32, 64, 122, 128])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_convolution(n, precision):
+    """precomputed_fftconvolution with the elastic and geoid kernels."""
+    dx = 50e3
+    p = params("test2c", min_pad=0.0)
+    dom = Domain(p, n, n, dx, precision=precision)
+    M = 2 * n - 1
+    x = np.random.default_rng(n).standard_normal((n, n)) * 1e7
+    for k, G in ((0, dom.field("GE")), (1, dom.field("GN"))):
+        ref = O.conv(O.kernel_spectrum(G, M), x, M)
+        got = dom.convolve(k, x)
+        assert rel(got, ref) <= (TOL64 if precision == 0 else TOLMIX), (k, rel(got, ref))
+    # the product's Green's functions equal the oracle's restatement
+    assert np.array_equal(dom.field("GE"), O.elastic_green(n, n, dx))
+    assert np.array_equal(dom.field("GN"), O.zss_green(n, n, p["m_earth"], p["r_earth"], dx))
+    dom.close()
+
+
+FIELDS = ["w", "we", "z_bed", "dz_ss", "dwdt", "canom_full", "z_ss", "Haf", "x"]
+MASKS = ["maskocean", "maskgrounded", "maskcontinent"]
+
+
+def compare(pair, tol, fields=FIELDS, masks=True):
+    worst = {}
+    for f in fields:
+        a, b = pair.dom.field(f), pair.orc.field(f)
+        worst[f] = rel(a, b) if np.abs(b).max() > 0 else float(np.abs(a).max())
+        assert worst[f] <= tol, (f, worst[f])
+    if masks:
+        for m in MASKS:
+            assert np.array_equal(pair.dom.field(m), pair.orc.field(m)), m
+    return worst
+
+
+def ref_disc(name, n=31, dx=200e3, **over):
+    p = params(name, **over)
+    H = W.disc(n, n, dx)
+    return W.Workload(name=name, params=p, nx_ice=n, ny_ice=n, dx=dx, z_bed=np.full((n, n), 1e6), H_final=H)
+
+
+@pytest.mark.parametrize("name,over", [("test1d", {}), ("test1e", {}), ("test2c", {}), ("test3a", {}),
+                                       ("test3c", {}), ("test2c", {"lithosphere": 2})])
+def test_reference_experiments_tsit54(name, over):
+    """Reference experiments (par/*.nml) with the reference's own integrator
+    semantics (frozen RHS, transposed Tsit5 tableau).  test2c with a
+    Gaussian-thinned lithosphere makes R laterally variable (not even in the
+    wavenumbers), which exercises the general Hartley-basis multiply."""
+    pair = Pair(ref_disc(name, **over))
+    pair.init()
+    pair.step(30)
+    compare(pair, TOL64)
+    so, sg = pair.orc.scalars(), pair.dom.scalars()
+    assert so["n_accept"] == sg["n_accept"] and so["n_reject"] == sg["n_reject"]
+    assert so["t"] == sg["t"] and so["dt"] == sg["dt"]
+    pair.close()
+
+
+@pytest.mark.parametrize("dt_method,stage_mode", [(1, 0), (1, 1), (0, 0), (0, 1)])
+def test_config2_rk4_euler(dt_method, stage_mode):
+    wl = W.config2(n=64, L=3000e3 * 64 / 256, dt=1.0, stage_mode=stage_mode)
+    wl.params["dt_method"] = dt_method
+    pair = Pair(wl)
+    pair.init()
+    pair.step(6)
+    compare(pair, TOL64)
+    pair.close()
+
+
+def test_config3_interactive_sealevel_rectangular():
+    """Interactive sea level, masks, elastic + geoid, two-layer freqdomain
+    lumping (non-even R -> general Hartley path), rectangular padding."""
+    wl = W.config3(nx_ice=40, ny_ice=72, dx=20e3, nx_pad=64, ny_pad=96)
+    pair = Pair(wl)
+    pair.init()
+    pair.step(8)
+    compare(pair, TOL64)
+    assert pair.dom.field("R").std() > 0
+    pair.close()
+
+
+def test_mixed_precision_error_bound():
+    wl = W.config2(n=64, L=3000e3 * 64 / 256, dt=1.0, stage_mode=1)
+    a = Pair(wl, precision=0)
+    b = Pair(wl, precision=1, gpu=True)
+    a.init(); b.init()
+    a.step(20); b.step(20)
+    w64, w32 = a.dom.field("w"), b.dom.field("w")
+    assert rel(w32, w64) <= TOLMIX
+    a.close(); b.close()
+
+
+def test_outputs_and_restart_roundtrip():
+    wl = W.config2(n=32, L=3000e3 * 32 / 256, dt=1.0, stage_mode=1)
+    pair = Pair(wl)
+    pair.init()
+    pair.step(3)
+    dom = pair.dom
+    buf = dom.state_export()
+    ni = (wl.ny_ice, wl.nx_ice)
+    out = {k: np.zeros(ni) for k in ("z_bed", "w", "we", "dz_ss")}
+    out["maskocean"] = np.zeros(ni, dtype=np.uint8)
+    t = pair.t + wl.dtt
+    dom.update(wl.H_at(t), t, pair.bg, out=out)
+    assert np.array_equal(out["w"], dom.crop(dom.field("w")))
+    assert np.array_equal(out["z_bed"], dom.crop(dom.field("z_bed")))
+    w1 = dom.field("w")
+    dom.state_import(buf)
+    dom.update(wl.H_at(t), t, pair.bg)
+    assert np.array_equal(dom.field("w"), w1)
+    pair.close()
+
+
+def test_error_status_codes():
+    wl = W.config2(n=32, L=3000e3 * 32 / 256, dt=1.0, stage_mode=1)
+    dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx)
+    bg = gpu_bsl()
+    with pytest.raises(_lib.FiError) as e:
+        dom.update(wl.H_at(10.0), 10.0, bg)
+    assert e.value.code == _lib.FI_E_STATE
+    dom.set_fields(**wl.padded_fields(dom.nx, dom.ny))
+    dom.init_state(wl.z_bed, wl.H_at(0.0), 0.0, bg)
+    H = wl.H_at(10.0).copy()
+    H[3, 3] = np.nan
+    with pytest.raises(_lib.FiError) as e:
+        dom.update(H, 10.0, bg)
+    assert e.value.code == _lib.FI_E_NAN
+    dom.close()
+    # dt = 10 yr on an 11.7 km grid with D ~ 2e25 diverges (lambda*dt ~ -18)
+    wl = W.config2(n=64, L=3000e3 * 64 / 256, dt=10.0, stage_mode=1)
+    dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx)
+    dom.set_fields(**wl.padded_fields(dom.nx, dom.ny))
+    dom.init_state(wl.z_bed, wl.H_at(0.0), 0.0, bg)
+    with pytest.raises(_lib.FiError) as e:
+        for k in range(1, 10):
+            dom.update(wl.H_at(10.0 * k), 10.0 * k, bg)
+    assert e.value.code == _lib.FI_E_LARGE
+    dom.close()

@@ -1,0 +1,113 @@
+"""CPU tests: the oracle against transform definitions, an independent numpy
+restatement, the analytical ELVA disk and the committed golden vectors."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import np_restatement as R
+from oracle import analytical as A
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 8, 12, 61, 64, 73, 122, 243, 256, 511, 1023, 1024])
+def test_fft_matches_numpy(n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    assert np.abs(O.cfft(x, -1) - np.fft.fft(x)).max() <= 2e-15 * np.abs(np.fft.fft(x)).max() * max(1, np.log2(n))
+    assert np.abs(O.cfft(x, +1) - n * np.fft.ifft(x)).max() <= 2e-15 * n * np.abs(np.fft.ifft(x)).max() * max(1, np.log2(n))
+
+
+@pytest.mark.parametrize("shape", [(8, 8), (16, 16), (12, 20), (30, 30)])
+def test_dht_matches_cas_definition(shape):
+    a = np.random.default_rng(1).standard_normal(shape)
+    h = O.dht2d(a)
+    ref = R.dht2d(a)
+    assert np.abs(h - ref).max() <= 1e-13 * np.abs(ref).max()
+    # DHT is its own inverse up to N
+    assert np.abs(O.dht2d(h) / a.size - a).max() <= 1e-13
+
+
+@pytest.mark.parametrize("kind", ["x", "y", "xx", "yy"])
+def test_derivatives_bit_exact(kind):
+    rng = np.random.default_rng(2)
+    u = rng.standard_normal((10, 14))
+    d = 1 + rng.random((10, 14))
+    f = {"x": R.d_x, "y": R.d_y, "xx": R.d_xx, "yy": R.d_yy}[kind]
+    assert np.array_equal(O.derivative(kind, u, d), f(u, d))
+
+
+def test_kappa_within_one_ulp():
+    # the reference takes (p*p + q*q)**0.5 (pow); numpy's sqrt may differ in the last bit
+    for nx, ny in [(20, 12), (64, 64), (122, 122)]:
+        a, b = O.kappa(nx, ny, 1e4, 1e4), R.kappa(nx, ny, 1e4, 1e4)
+        assert np.all(np.abs(a - b) <= 2.3e-16 * np.abs(b))
+
+
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_convolution_is_linear_convolution(n):
+    rng = np.random.default_rng(n)
+    ker, inp = rng.standard_normal((n, n)), rng.standard_normal((n, n))
+    M = 2 * n - 1
+    out = O.conv(O.kernel_spectrum(ker, M), inp, M)
+    ref = R.linear_conv_crop(ker, inp)
+    assert np.abs(out - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("n,even", [(16, True), (32, False), (24, False)])
+def test_lvelva_matches_numpy_restatement(n, even):
+    rng = np.random.default_rng(n)
+    dx = 5e4
+    w = rng.standard_normal((n, n)) * 100
+    cf = rng.standard_normal((n, n)) * 1e5
+    mask = rng.random((n, n)) > 0.2
+    D = 1e24 * (1 + rng.random((n, n)))
+    eta = 1e21 * (1 + rng.random((n, n)))
+    Rr = np.ones((n, n)) if even else 1 + 0.1 * rng.random((n, n))
+    kap = O.kappa(n, n, dx, dx)
+    dxm = np.full((n, n), dx) * (1 + 0.01 * rng.random((n, n)))
+    a = O.lvelva(w, cf, mask, 9.81, 0.28, D, eta, Rr, kap, dxm, dxm.copy(), 31557600.0)
+    b = R.lvelva(w, cf, mask, 9.81, 0.28, D, eta, Rr, kap, dxm, dxm.copy(), 31557600.0)
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+
+
+def test_analytical_disk_pins_oracle():
+    """Reference experiment test1d (par/test_isostasy_test1d.nml) on a 100 km
+    grid against the Bueler et al. (2007) solution the reference itself
+    writes as err_z_bed (src/isostasy_io.f90:382-390)."""
+    with open(os.path.join(GOLDEN, "params_test1d.json")) as fh:
+        p = json.load(fh)
+    dx, n = 100e3, 61
+    xc = -3000e3 + dx * np.arange(n)
+    H = np.where(xc[None, :] ** 2 + xc[:, None] ** 2 <= 1000e3 ** 2, 1000.0, 0.0)
+    m = O.Model(p, n, n, dx, dx)
+    b = O.make_bsl()
+    m.init_state(np.full((n, n), 1e6), np.zeros_like(H), 0.0, b)
+    T = 3000.0
+    for k in range(1, int(T / 10) + 2):
+        t = (k - 1) * 10.0
+        assert m.update(H if t > 0 else np.zeros_like(H), t, b) == 0
+    zb = m.crop(m.field("z_bed")) - 1e6
+    ana = A.elva_disk(n, n, dx, 1000e3, 1000.0, 1e21, m.field("D_lith")[0, 0], 910.0, 3400.0, 9.81, T)
+    centre_err = abs(zb.min() - ana.min()) / abs(ana.min())
+    rms_err = np.sqrt(np.mean((zb - ana) ** 2)) / abs(ana.min())
+    assert centre_err < 0.03, centre_err
+    assert rms_err < 0.05, rms_err
+
+
+def test_golden_vectors():
+    """Regression pin: oracle outputs committed by tests/golden/make_golden.py."""
+    path = os.path.join(GOLDEN, "oracle_golden.npz")
+    g = np.load(path)
+    import make_golden_cases as MG
+    for name, fn in MG.CASES.items():
+        out = fn()
+        for k, v in out.items():
+            key = name + "__" + k
+            assert key in g.files, key
+            ref = g[key]
+            scale = max(np.abs(ref).max(), 1e-300)
+            assert np.abs(v - ref).max() <= 1e-12 * scale, key
