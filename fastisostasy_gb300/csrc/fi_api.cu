@@ -647,7 +647,7 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
         h->nx = nx_tmp + 2 * npx;
         h->ny = ny_tmp + 2 * npy;
     }
-    if (h->nx > 4096 || h->ny > 4096) { delete h; return FI_E_CONFIG; }
+    if (h->nx > 2048 || h->ny > 2048) { delete h; return FI_E_CONFIG; }   // column FFT of 2n must fit in shared memory
     h->icrop1 += npx;
     h->icrop2 = h->nx - npx;
     h->jcrop1 += npy;
