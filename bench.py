@@ -1,0 +1,377 @@
+#!/usr/bin/env python3
+"""LV-ELVA benchmark: simulated kyr/s on a 512 x 512 domain, mixed FP32/FP64
+form against the plain FP64 form on the same GPU.
+
+Workload (one "step" = one coupling step, i.e. one isos_update call):
+  512 x 512 cells at dx = 11.72 km (6000 km square), lithosphere 150 km minus
+  a 100 km Gaussian (sigma 500 km) mapped to rigidity with E = 66 GPa,
+  nu = 0.28, uniform eta = 1e21 Pa s, centred 1000 km / 1000 m ice disc,
+  elastic and geoid convolutions every step (dt_diagnostics = dtt = 10 yr),
+  RK4 with true stages at dt = 1 yr (10 RK4 steps = 40 RHS per coupling
+  step; dt = 10 yr diverges on this grid).  Inputs are seeded synthetic
+  fields; nothing is read from disk.
+
+`value` times fi_update_async with the ice load already resident on the
+device; `e2e` times the public fi_update call with host arrays (ice load in,
+every isos%out field back).  L2 is flushed (256 MiB write) between timed
+steps, outside the timed events.  `--impl reference` times the CPU
+restatement of the reference (reference integrator semantics) on all host
+cores instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "LV-ELVA kyr/s @512² mixed vs FP64, same GPU (err≤1e-5); serve p50/p99 ms"
+N_CELLS = 512
+DX = 11.71875e3
+DT = 1.0
+DTT = 10.0
+WORKLOAD = ("lvelva_512x512_gaussian_lithosphere_disc_rk4_dt1yr_elastic_geoid "
+            "(512^2 at 11.72 km, He 150-100 km Gaussian, eta 1e21, 1000 km/1000 m disc, "
+            "RK4 true stages dt=1 yr, coupling dtt=10 yr, elastic+geoid every step)")
+
+
+def workload(stage_mode=1):
+    from fastisostasy_gb300 import workloads as W
+    return W.config2(n=N_CELLS, L=N_CELLS * DX, dt=DT, dtt=DTT, stage_mode=stage_mode)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(kernel, dom, precision, stage_mode):
+    """Compulsory bytes one launch of `kernel` must move (inputs read once,
+    outputs written once) on the padded domain."""
+    f = 4 if precision == 1 else 8
+    nx, ny = dom.nx, dom.ny
+    n = nx * ny
+    spec = ny * (nx // 2 + 1) * 2 * f
+    px, py = 2 * nx, 2 * ny
+    cspec_in = ny * (px // 2 + 1) * 2 * f
+    cspec_k = py * (px // 2 + 1) * 2 * f
+    cspec_out = (ny + 2) * (px // 2 + 1) * 2 * f
+    table = {
+        "flexure": n * (8 + (8 if stage_mode == 1 else 0) + 3 * f + 1 + f),
+        "rows_fwd": n * f + spec,
+        "cols_hartley": 2 * spec + spec // 2,
+        "rows_inv": spec + n * f,
+        "conv_rows_fwd": n * f + cspec_in,
+        "conv_cols": cspec_in + cspec_k + cspec_out,
+        "conv_rows_inv": cspec_out + n * 8,
+        "rk_stage": n * (8 + f + 8),
+        "rk_final": n * (8 + 4 * f + 16),
+    }
+    return table.get(kernel)
+
+
+def make_domain(precision, stage_mode=1):
+    from fastisostasy_gb300.isostasy import Domain
+    from fastisostasy_gb300 import _lib
+    wl = workload(stage_mode)
+    dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=precision)
+    dom.set_fields(**wl.padded_fields(dom.nx, dom.ny))
+    b = _lib.FiBsl()
+    b.method, b.constant_ocean_surface, b.bsl_init, b.bsl_now = 0, 1, 0.0, 0.0
+    b.A_ocean_pd = b.A_ocean_now = 3.625e14
+    dom.init_state(wl.z_bed, wl.H_at(0.0), 0.0, b)
+    return dom, wl, b
+
+
+def run_resident(dom, wl, b, steps, warmup, flush, t0=0.0, sampler_index=None, profile=False):
+    """Device-resident loop from model time t0: returns (per-step ms list,
+    launches, clocks, per-kernel profile, final time)."""
+    import torch
+    ext = torch.cuda.ExternalStream(dom.L.fi_stream(dom.h))
+    H = torch.from_numpy(np.ascontiguousarray(wl.H_final)).to("cuda")
+    t = t0
+    for _ in range(warmup):
+        t += wl.dtt
+        dom.update_async(H.data_ptr(), t, b)
+    dom.synchronize()
+    if profile:
+        dom.L.fi_profile(dom.h, -1)
+        dom.L.fi_profile(dom.h, 1)
+    l0 = dom.L.fi_launch_count(dom.h)
+    sampler = ClockSampler(sampler_index) if sampler_index is not None else None
+    evs = []
+    for _ in range(steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+        t += wl.dtt
+        dom.update_async(H.data_ptr(), t, b)
+        e1.record(ext)
+        evs.append((e0, e1))
+    dom.synchronize()
+    clocks = sampler.stop() if sampler is not None else None
+    launches = dom.L.fi_launch_count(dom.h) - l0
+    ms = [a.elapsed_time(c) for a, c in evs]
+    prof = None
+    if profile:
+        import ctypes as C
+        from fastisostasy_gb300 import _lib
+        nk = len(_lib.PROFILE_KERNELS)
+        tot = (C.c_double * nk)()
+        cnt = (C.c_longlong * nk)()
+        dom.L.fi_profile_read(dom.h, tot, cnt, nk)
+        dom.L.fi_profile(dom.h, 0)
+        prof = {k: (tot[i], cnt[i]) for i, k in enumerate(_lib.PROFILE_KERNELS) if cnt[i] > 0}
+    return ms, launches, clocks, prof, t
+
+
+def run_e2e(dom, wl, b, steps, warmup, flush, t0):
+    import torch
+    ni = (wl.ny_ice, wl.nx_ice)
+    out = {k: np.zeros(ni) for k in ("z_bed", "z_ss", "dz_ss", "w", "we", "dwdt", "canom_full", "Hice")}
+    out.update({k: np.zeros(ni, dtype=np.uint8) for k in ("maskocean", "maskgrounded", "maskcontinent")})
+    H = np.ascontiguousarray(wl.H_final)
+    t = t0
+    for _ in range(warmup):
+        t += wl.dtt
+        dom.update(H, t, b, out=out)
+    secs = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t += wl.dtt
+        a = time.perf_counter()
+        dom.update(H, t, b, out=out)
+        secs += time.perf_counter() - a
+    h2d = H.nbytes
+    d2h = 11 * H.size * 8   # outputs travel as one packed double buffer
+    return secs, h2d, d2h
+
+
+def cpu_baseline(samples=8, threads=1, stage_mode=1):
+    """The oracle (C restatement) on the same workload, `samples` coupling steps."""
+    from oracle import oracle as O
+    O.set_threads(threads)
+    wl = workload(stage_mode)
+    m = O.Model(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
+    m.set_fields(**wl.padded_fields(m.nx, m.ny))
+    bo = O.make_bsl()
+    m.init_state(wl.z_bed, wl.H_at(0.0), 0.0, bo)
+    t = 0.0
+    t += wl.dtt
+    m.update(wl.H_final, t, bo)   # untimed first step
+    a = time.perf_counter()
+    for _ in range(samples):
+        t += wl.dtt
+        rc = m.update(wl.H_final, t, bo)
+        if rc:
+            raise RuntimeError("oracle update failed %d" % rc)
+    secs = time.perf_counter() - a
+    m.close()
+    return samples * wl.dtt / 1000.0 / secs, secs
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    from oracle import oracle as O
+    O.set_threads(threads)
+    wl = workload(stage_mode=0)
+    m = O.Model(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
+    m.set_fields(**wl.padded_fields(m.nx, m.ny))
+    bo = O.make_bsl()
+    m.init_state(wl.z_bed, wl.H_at(0.0), 0.0, bo)
+    t = 0.0
+    for _ in range(args.warmup):
+        t += wl.dtt
+        m.update(wl.H_final, t, bo)
+    a = time.perf_counter()
+    for _ in range(args.steps):
+        t += wl.dtt
+        m.update(wl.H_final, t, bo)
+    secs = time.perf_counter() - a
+    val = args.steps * wl.dtt / 1000.0 / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "kyr/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "l2": "n/a (CPU)", "integrator": "reference semantics (frozen RHS, 4 RHS/RK4 step)"},
+        "cpu_baseline": {"value": val, "unit": "kyr/s", "cores": threads, "kind": "port",
+                         "sample": "%d coupling steps (%d x 40 RHS + 2 convolutions at 1023^2), OpenMP %d threads"
+                                   % (args.steps, args.steps, threads)},
+        "e2e": {"value": val, "unit": "kyr/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-samples", type=int, default=8)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    import __graft_entry__
+    __graft_entry__.build()
+    from fastisostasy_gb300 import _lib
+    _lib.load()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    results = {}
+    for prec in (0, 1):
+        dom, wl, b = make_domain(prec)
+        barrier()
+        ms, launches, clocks, _, t_end = run_resident(dom, wl, b, args.steps, args.warmup, flush,
+                                                      sampler_index=local if prec == 1 else None)
+        barrier()
+        tot = sum(ms)
+        if ws > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([tot], device="cuda", dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            tot = float(tt.item())
+        results[prec] = {"dom": dom, "wl": wl, "b": b, "ms": tot / args.steps, "launches": launches,
+                         "clocks": clocks, "w": dom.field("w"), "t": t_end}
+    kyr = lambda ms_step: ws * (DTT / 1000.0) / (ms_step / 1000.0)
+    r64, r32 = results[0], results[1]
+    w64, w32 = r64["w"], r32["w"]
+    err_max = float(np.abs(w32 - w64).max() / np.abs(w64).max())
+    err_rms = float(np.sqrt(np.mean((w32 - w64) ** 2)) / np.abs(w64).max())
+
+    # per-kernel CUDA-event timing pass (same workload, same step count) for the roofline
+    dom, wl, b = r32["dom"], r32["wl"], r32["b"]
+    _, _, _, prof, t_now = run_resident(dom, wl, b, args.steps, 0, flush, t0=r32["t"], profile=True)
+    peak, peak_kind = peaks()
+    dominant = max(prof.items(), key=lambda kv: kv[1][0])[0]
+    tot_ms, cnt = prof[dominant]
+    alg = algorithmic_bytes(dominant, dom, 1, 1)
+    achieved = alg / (tot_ms / cnt / 1000.0) / 1e9 if alg else None
+    shares = {k: round(v[0] / sum(x[0] for x in prof.values()), 4) for k, v in prof.items()}
+
+    # end to end through fi_update with host arrays (mixed form)
+    e2e_secs, h2d, d2h = run_e2e(dom, wl, b, args.steps, 1, flush, t_now)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, secs = cpu_baseline(args.cpu_samples, threads=1, stage_mode=1)
+        cpu = {"value": v, "unit": "kyr/s", "cores": 1, "kind": "port",
+               "sample": "%d coupling steps of the same workload (%d x 40 RHS + 2 convolutions at 1023^2), "
+                         "%.1f s, 1 thread (the reference is serial)" % (args.cpu_samples, args.cpu_samples, secs)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": kyr(r32["ms"]), "unit": "kyr/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r32["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": "mixed FP32/FP64", "stage_mode": "true stages",
+                       "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas" if ws > 1 else "1 GPU"},
+            "fp64": {"value": kyr(r64["ms"]), "unit": "kyr/s", "ms_per_step": r64["ms"], "dtype": "f64"},
+            "mixed_over_fp64": r64["ms"] / r32["ms"],
+            "err_vs_fp64": {"max_rel": err_max, "rms_rel": err_rms,
+                            "after_steps": args.warmup + args.steps},
+            "cell_steps_per_s": ws * N_CELLS * N_CELLS * (DTT / DT) / (r32["ms"] / 1000.0),
+            "e2e": {"value": kyr(1000.0 * e2e_secs / args.steps), "unit": "kyr/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,
+                         "avg_launch_us": 1000.0 * tot_ms / cnt, "kernel_time_shares": shares},
+            "cpu_baseline": cpu,
+            "clocks": r32["clocks"],
+            "gpu_launches": r32["launches"],
+        }
+        print(json.dumps(line))
+    for r in results.values():
+        r["dom"].close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -15,7 +15,7 @@ INC = os.path.join(os.path.dirname(HERE), "include")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfigpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INC,
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", CSRC, "-I", INC,
          "--expt-relaxed-constexpr", "-diag-suppress", "177"]
 
 

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -97,6 +98,23 @@ struct fi_handle {
     double ref_bsl = 0.0;
     int Px = 0, Py = 0;
     int even = 1, uniform = 1;
+    long long launches = 0;            // kernels enqueued by this handle
+    // CUDA graphs of whole updates, keyed by (step count, diagnostics, ...)
+    struct GraphEntry {
+        long long key;
+        long long nkernels;
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphEntry> graphs;
+    std::vector<long long> graph_seen;
+    bool use_graphs = true;
+    // optional per-kernel CUDA-event timing (fi_profile)
+    bool prof_on = false;
+    std::vector<cudaEvent_t> prof_ev;
+    std::vector<int> prof_id;
+    size_t prof_used = 0;
+    double prof_ms[32] = {0};
+    long long prof_cnt[32] = {0};
     cudaStream_t s = nullptr;
     std::vector<void*> allocs;
     std::string err;
@@ -153,6 +171,52 @@ int fail(fi_handle* h, int code, const char* fmt, ...)
     do {                                                                                 \
         cudaError_t e_ = (call);                                                         \
         if (e_ != cudaSuccess) return fail(h, FI_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+// Kernel ids of the profiler (fi_profile_read): see include/fi_gpu.h.
+enum { K_FLEX = 0, K_ROWS_FWD, K_COLS_HARTLEY, K_ROWS_INV, K_CONV_ROWS_FWD, K_CONV_COLS, K_CONV_ROWS_INV,
+       K_STAGE, K_RK_FINAL, K_UPD_BEGIN, K_UPD_MASKS, K_UPD_LITHO, K_UPD_LOAD, K_UPD_END, K_CONTROL, K_TS, K_NPROF };
+
+int prof_begin(fi_handle* h, int id)
+{
+    if (!h->prof_on) return -1;
+    if (h->prof_used + 2 > h->prof_ev.size()) {
+        const size_t add = 4096;
+        for (size_t i = 0; i < add; ++i) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            h->prof_ev.push_back(e);
+        }
+        h->prof_id.resize(h->prof_ev.size() / 2 + 1);
+    }
+    const int m = (int)h->prof_used;
+    cudaEventRecord(h->prof_ev[m], h->s);
+    h->prof_id[m / 2] = id;
+    h->prof_used += 2;
+    return m;
+}
+void prof_end(fi_handle* h, int m)
+{
+    if (m >= 0) cudaEventRecord(h->prof_ev[m + 1], h->s);
+}
+void prof_collect(fi_handle* h)
+{
+    if (h->prof_used == 0) return;
+    cudaStreamSynchronize(h->s);
+    for (size_t m = 0; m + 1 < h->prof_used; m += 2) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, h->prof_ev[m], h->prof_ev[m + 1]) == cudaSuccess) {
+            h->prof_ms[h->prof_id[m / 2]] += ms;
+            h->prof_cnt[h->prof_id[m / 2]] += 1;
+        }
+    }
+    h->prof_used = 0;
+}
+#define PROF(h, id, expr)                  \
+    do {                                   \
+        const int pm_ = prof_begin(h, id); \
+        expr;                              \
+        prof_end(h, pm_);                  \
     } while (0)
 
 template <typename P> int dalloc(fi_handle* h, P** out, size_t bytes)
@@ -442,129 +506,205 @@ template <typename T> struct TT {
 template <typename T> void rhs(fi_handle* h, const double* y, const double* wref, T* raw_out)
 {
     typedef typename vec2<T>::type C2;
-    launch_flexure<T>(y, wref, (const T*)h->q0, h->d.mactive, (const T*)h->Dt, (const T*)h->inv2eta, (T*)h->f,
-                      h->nx, h->ny, h->fc, h->s);
-    launch_rows_fwd<T>((const T*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, h->prhs, h->s);
-    launch_cols_hartley<T>((C2*)h->S, (const T*)h->mA, (const T*)h->mB, h->even, h->prhs, h->s);
+    PROF(h, K_FLEX, launch_flexure<T>(y, wref, (const T*)h->q0, h->d.mactive, (const T*)h->Dt, (const T*)h->inv2eta,
+                                      (T*)h->f, h->nx, h->ny, h->fc, h->s));
+    PROF(h, K_ROWS_FWD, launch_rows_fwd<T>((const T*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, h->prhs, h->s));
+    PROF(h, K_COLS_HARTLEY, launch_cols_hartley<T>((C2*)h->S, (const T*)h->mA, (const T*)h->mB, h->even, h->prhs, h->s));
     const double norm = (double)(float)((long long)h->nx * h->ny);   // nx*ny*1. (default real)
-    launch_rows_inv<T>((const C2*)h->S, raw_out, h->prhs, 1.0 / norm, h->s);
+    PROF(h, K_ROWS_INV, launch_rows_inv<T>((const C2*)h->S, raw_out, h->prhs, 1.0 / norm, h->s));
+    h->launches += 4;
 }
 
 template <typename T> void conv(fi_handle* h, int which, double* out_raw, double* corners)
 {
     typedef typename vec2<T>::type C2;
-    launch_rows_fwd<T>((const T*)h->conv_in, h->nx, h->nx, h->ny, (C2*)h->S2, h->pconv, h->s);
-    launch_cols_conv<T>((C2*)h->S2, (const C2*)h->KS[which], h->ny, h->out_rows, h->ny + 2, h->pconv, h->s);
-    launch_conv_rows_inv<T>((const C2*)h->S2, h->ny + 2, out_raw, h->nx, h->ny, h->nx / 2 - 1, corners, 0, 0,
-                            2 * h->nx - 2, h->pconv, 1.0 / ((double)h->Px * (double)h->Py), h->s);
+    PROF(h, K_CONV_ROWS_FWD, launch_rows_fwd<T>((const T*)h->conv_in, h->nx, h->nx, h->ny, (C2*)h->S2, h->pconv, h->s));
+    PROF(h, K_CONV_COLS, launch_cols_conv<T>((C2*)h->S2, (const C2*)h->KS[which], h->ny, h->out_rows, h->ny + 2, h->pconv,
+                                             h->s));
+    PROF(h, K_CONV_ROWS_INV, launch_conv_rows_inv<T>((const C2*)h->S2, h->ny + 2, out_raw, h->nx, h->ny, h->nx / 2 - 1,
+                                                     corners, 0, 0, 2 * h->nx - 2, h->pconv,
+                                                     1.0 / ((double)h->Px * (double)h->Py), h->s));
+    h->launches += 3;
 }
 
-// Integrator loop of one update.  Returns FI status; sets *have_rhs and the
-// raw buffer holding the last RHS evaluated.
-template <typename T> int integrate(fi_handle* h, double tf, int* have_rhs, T** raw_last)
+// Fixed-step integrators (euler, rk4): the step sequence of one update is
+// known on the host from a mirror of the ode clock that repeats the device's
+// fmin/add sequence, so an update has a static kernel sequence.
+int plan_steps(fi_handle* h, double tf)
+{
+    const fi_params& p = h->p;
+    int n = 0;
+    while (h->h_t < tf) {
+        double hstep;
+        if (p.dt_method == 1) hstep = fmin(h->h_dt, tf - h->h_t);
+        else { h->h_dt = fmin(h->h_dt, tf - h->h_t); hstep = h->h_dt; }
+        h->h_t = h->h_t + hstep;
+        ++n;
+    }
+    return n;
+}
+
+// Enqueue `nsteps` euler/rk4 steps; returns the raw buffer of the last RHS.
+template <typename T> T* enqueue_steps(fi_handle* h, int nsteps)
 {
     const fi_params& p = h->p;
     const double spy = h->spy;
+    T *r0 = (T*)h->raw[0], *r1 = (T*)h->raw[1], *r2 = (T*)h->raw[2], *r3 = (T*)h->raw[3];
+    const bool truem = p.stage_mode == 1;
+    const double* wref = truem ? h->w_ref : nullptr;
+    T* last = r0;
+    for (int st = 0; st < nsteps; ++st) {
+        PROF(h, K_CONTROL, step_begin(h->ctl, p.dt_method == 1 ? 1 : 0, h->s));
+        if (p.dt_method == 1 && truem) {
+            rhs<T>(h, h->d.x, wref, r0);
+            PROF(h, K_STAGE, rk_stage<T>(h->ctl, h->y, h->d.x, r0, 0.5, h->nx, h->ny, spy, h->s));
+            rhs<T>(h, h->y, wref, r1);
+            PROF(h, K_STAGE, rk_stage<T>(h->ctl, h->y, h->d.x, r1, 0.5, h->nx, h->ny, spy, h->s));
+            rhs<T>(h, h->y, wref, r2);
+            PROF(h, K_STAGE, rk_stage<T>(h->ctl, h->y, h->d.x, r2, 1.0, h->nx, h->ny, spy, h->s));
+            rhs<T>(h, h->y, wref, r3);
+            PROF(h, K_RK_FINAL, rk4_final<T>(h->ctl, h->d.x, h->d.w, r0, r1, r2, r3, h->nx, h->ny, spy, h->s));
+            h->launches += 4;
+            last = r3;
+        } else if (p.dt_method == 1) {
+            rhs<T>(h, h->d.w, nullptr, r0);
+            PROF(h, K_RK_FINAL, rk4_final<T>(h->ctl, h->d.x, h->d.w, r0, r0, r0, r0, h->nx, h->ny, spy, h->s));
+            h->launches += 1;
+        } else {
+            rhs<T>(h, truem ? h->d.x : h->d.w, wref, r0);
+            PROF(h, K_RK_FINAL, euler_final<T>(h->ctl, h->d.x, h->d.w, r0, h->nx, h->ny, spy, h->s));
+            h->launches += 1;
+        }
+        PROF(h, K_CONTROL, step_end(h->ctl, h->s));
+        h->launches += 2;
+    }
+    return last;
+}
+
+// Reference-compatible Tsit5: one distinct RHS per state; the host waits
+// for each attempt's accept/reject decision.
+template <typename T> int integrate_tsit(fi_handle* h, double tf, int* have_rhs, T** raw_last)
+{
+    const fi_params& p = h->p;
     T* r0 = (T*)h->raw[0];
     *have_rhs = 0;
     *raw_last = r0;
-    const bool truem = p.stage_mode == 1;
-    const double* wref = truem ? h->w_ref : nullptr;
-    if (p.dt_method == 1 || p.dt_method == 0) {
-        // host mirror of the clock: identical fmin/add sequence as the device
-        while (h->h_t < tf) {
-            double hstep;
-            if (p.dt_method == 1) hstep = fmin(h->h_dt, tf - h->h_t);
-            else { h->h_dt = fmin(h->h_dt, tf - h->h_t); hstep = h->h_dt; }
-            step_begin(h->ctl, tf, p.dt_method == 1 ? 1 : 0, h->s);
-            if (p.dt_method == 1) {
-                if (truem) {
-                    T *r1 = (T*)h->raw[1], *r2 = (T*)h->raw[2], *r3 = (T*)h->raw[3];
-                    rhs<T>(h, h->d.x, wref, r0);
-                    rk_stage<T>(h->ctl, h->y, h->d.x, r0, 0.5, h->nx, h->ny, spy, h->s);
-                    rhs<T>(h, h->y, wref, r1);
-                    rk_stage<T>(h->ctl, h->y, h->d.x, r1, 0.5, h->nx, h->ny, spy, h->s);
-                    rhs<T>(h, h->y, wref, r2);
-                    rk_stage<T>(h->ctl, h->y, h->d.x, r2, 1.0, h->nx, h->ny, spy, h->s);
-                    rhs<T>(h, h->y, wref, r3);
-                    rk4_final<T>(h->ctl, h->d.x, h->d.w, r0, r1, r2, r3, h->nx, h->ny, spy, h->s);
-                    *raw_last = r3;
-                } else {
-                    rhs<T>(h, h->d.w, nullptr, r0);
-                    rk4_final<T>(h->ctl, h->d.x, h->d.w, r0, r0, r0, r0, h->nx, h->ny, spy, h->s);
-                    *raw_last = r0;
-                }
-            } else {
-                rhs<T>(h, truem ? h->d.x : h->d.w, wref, r0);
-                euler_final<T>(h->ctl, h->d.x, h->d.w, r0, h->nx, h->ny, spy, h->s);
-                *raw_last = r0;
-            }
-            step_end(h->ctl, h->s);
-            h->h_t = h->h_t + hstep;
-            *have_rhs = 1;
-        }
-        CK(cudaGetLastError());
-        return FI_OK;
-    }
-    if (p.dt_method == 2) {
-        if (truem) return fail(h, FI_E_CONFIG, "tsit54 with true stages is not available on the device yet");
-        // Reference-compatible Tsit5: one distinct RHS per state; the host
-        // waits for each attempt's accept/reject decision.
-        Ctl hc;
+    if (p.stage_mode == 1) return fail(h, FI_E_CONFIG, "tsit54 with true stages is not available on the device yet");
+    Ctl hc;
+    CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    bool need_rhs = true;
+    int guard = 0;
+    while (hc.t < tf && hc.status == ST_OK) {
+        PROF(h, K_CONTROL, step_begin(h->ctl, 2, h->s));
+        if (need_rhs) { rhs<T>(h, h->d.w, nullptr, r0); *have_rhs = 1; }
+        PROF(h, K_TS, ts_max<T>(h->d, r0, p.atol, p.rtol, h->s));
+        PROF(h, K_TS, ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s));
+        PROF(h, K_TS, ts_commit<T>(h->d, r0, h->s));
+        h->launches += 4;
         CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
         CK(cudaStreamSynchronize(h->s));
-        bool need_rhs = true;
-        int guard = 0;
-        while (hc.t < tf && hc.status == ST_OK) {
-            step_begin(h->ctl, tf, 2, h->s);
-            if (need_rhs) { rhs<T>(h, h->d.w, nullptr, r0); *have_rhs = 1; }
-            ts_max<T>(h->d, r0, p.atol, p.rtol, h->s);
-            ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s);
-            ts_commit<T>(h->d, r0, h->s);
-            CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
-            CK(cudaStreamSynchronize(h->s));
-            need_rhs = hc.accepted != 0;
-            if (++guard > 10000000) return fail(h, FI_E_STEP, "tsit54: too many attempts");
-        }
-        *raw_last = r0;
-        return FI_OK;
+        need_rhs = hc.accepted != 0;
+        if (++guard > 10000000) return fail(h, FI_E_STEP, "tsit54: too many attempts");
     }
-    return fail(h, FI_E_CONFIG, "dt_method %d not supported", p.dt_method);
+    return FI_OK;
 }
 
-// The body of isos_update on the device (src/fastisostasy.f90:731-872).
-template <typename T> int update_T(fi_handle* h, const double* dH, double time, bool run_integrator)
+// Kernels of isos_update before the integrator (src/fastisostasy.f90:750-833).
+template <typename T> void enqueue_pre(fi_handle* h, const double* dH, bool diag, bool run_integrator)
 {
     const fi_params& p = h->p;
-    upd_begin(h->d, dH, h->s);
-    bool diag = false;
-    if (time - h->time_diag >= sp(1e-3)) {   // :782-787
-        diag = true;
-        h->time_diag = h->time_diag + p.dt_diagnostics;
-    }
+    PROF(h, K_UPD_BEGIN, upd_begin(h->d, dH, h->s));
     T* cin = (T*)h->conv_in;
-    upd_masks<T>(h->d, (diag && p.include_elastic) ? cin : (T*)nullptr, h->s);
+    PROF(h, K_UPD_MASKS, upd_masks<T>(h->d, (diag && p.include_elastic) ? cin : (T*)nullptr, h->s));
     int we_mode = 0, dz_mode = 0;
     if (diag) {
         if (p.include_elastic) { conv<T>(h, 0, h->we_raw, h->corners); we_mode = 1; }
         else we_mode = 2;
     }
-    upd_litho<T>(h->d, h->we_raw, h->corners, we_mode, (diag && p.heterogeneous_ssh) ? cin : (T*)nullptr, h->s);
+    PROF(h, K_UPD_LITHO,
+         upd_litho<T>(h->d, h->we_raw, h->corners, we_mode, (diag && p.heterogeneous_ssh) ? cin : (T*)nullptr, h->s));
     if (diag) {
         if (p.heterogeneous_ssh) { conv<T>(h, 1, h->dz_raw, h->corners + 4); dz_mode = 1; }
         else dz_mode = 2;
     }
-    upd_load<T>(h->d, h->dz_raw, h->corners + 4, dz_mode, (T*)h->q0, p.stage_mode,
-                run_integrator ? time : -INFINITY, h->s);
-    int have_rhs = 0;
-    T* raw_last = (T*)h->raw[0];
-    if (run_integrator) {
-        int rc = integrate<T>(h, time, &have_rhs, &raw_last);
-        if (rc) return rc;
+    PROF(h, K_UPD_LOAD, upd_load<T>(h->d, h->dz_raw, h->corners + 4, dz_mode, (T*)h->q0, p.stage_mode,
+                                    run_integrator ? 1 : 0, h->s));
+    h->launches += 4;
+}
+
+// The tail: corner BC of w, canom_mantle, z_bed, dwdt, checks (:856-869).
+template <typename T> void enqueue_post(fi_handle* h, T* raw_last, int have_rhs)
+{
+    PROF(h, K_UPD_END, upd_end<T>(h->d, raw_last, have_rhs, h->s));
+    h->launches += 2;
+}
+
+// The body of isos_update on the device (src/fastisostasy.f90:731-872).
+// Euler/RK4 updates are captured once per (diagnostics, step count) into a
+// CUDA graph and replayed; the per-update scalars were written into the
+// control block by enqueue_args just before.
+template <typename T> int update_T(fi_handle* h, const double* dH, double time, bool run_integrator)
+{
+    const fi_params& p = h->p;
+    bool diag = false;
+    if (time - h->time_diag >= sp(1e-3)) {   // :782-787
+        diag = true;
+        h->time_diag = h->time_diag + p.dt_diagnostics;
     }
-    upd_end<T>(h->d, raw_last, have_rhs, h->s);
     h->time_prog = time;
-    CK(cudaGetLastError());
+    if (p.dt_method == 2 && run_integrator) {
+        enqueue_pre<T>(h, dH, diag, true);
+        int have_rhs = 0;
+        T* raw_last = nullptr;
+        int rc = integrate_tsit<T>(h, time, &have_rhs, &raw_last);
+        if (rc) return rc;
+        enqueue_post<T>(h, raw_last, have_rhs);
+        CK(cudaGetLastError());
+        return FI_OK;
+    }
+    const int nsteps = run_integrator ? plan_steps(h, time) : 0;
+    const long long key = ((long long)nsteps << 4) | ((diag ? 1 : 0) << 1) | (run_integrator ? 1 : 0) |
+                          ((long long)(dH == h->dH) << 2);
+    auto enqueue = [&]() {
+        enqueue_pre<T>(h, dH, diag, run_integrator);
+        T* raw_last = enqueue_steps<T>(h, nsteps);
+        enqueue_post<T>(h, raw_last, nsteps > 0 ? 1 : 0);
+    };
+    if (!h->use_graphs || h->prof_on) {
+        enqueue();
+        CK(cudaGetLastError());
+        return FI_OK;
+    }
+    for (auto& g : h->graphs)
+        if (g.key == key) {
+            CK(cudaGraphLaunch(g.exec, h->s));
+            h->launches += g.nkernels;
+            return FI_OK;
+        }
+    bool seen = false;
+    for (long long k : h->graph_seen) seen |= (k == key);
+    if (!seen) {
+        // first occurrence runs eagerly (also sets kernel attributes)
+        h->graph_seen.push_back(key);
+        enqueue();
+        CK(cudaGetLastError());
+        return FI_OK;
+    }
+    const long long l0 = h->launches;
+    CK(cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+    enqueue();
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(h->s, &graph);
+    if (e != cudaSuccess) return fail(h, FI_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    fi_handle::GraphEntry ge;
+    ge.key = key;
+    ge.nkernels = h->launches - l0;
+    e = cudaGraphInstantiate(&ge.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(h, FI_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    h->graphs.push_back(ge);
+    CK(cudaGraphLaunch(ge.exec, h->s));
     return FI_OK;
 }
 
@@ -573,16 +713,12 @@ int update_any(fi_handle* h, const double* dH, double time, bool run_integrator)
     return mixed(h) ? update_T<float>(h, dH, time, run_integrator) : update_T<double>(h, dH, time, run_integrator);
 }
 
-int set_bsl_scalars(fi_handle* h, const fi_bsl* b, bool write_bsl)
+// Per-update scalars (target time, barystatic sea level, ocean area) go to
+// the control block through a kernel argument: no host wait.
+void enqueue_args(fi_handle* h, double tf, const fi_bsl* b, bool write_bsl)
 {
-    // bsl, A_ocean, bsl_method into the control block
-    struct { double bsl; double A; } v = {b->bsl_now, b->A_ocean_now};
-    if (write_bsl) CK(cudaMemcpyAsync(&h->ctl->bsl, &v.bsl, sizeof(double), cudaMemcpyHostToDevice, h->s));
-    CK(cudaMemcpyAsync(&h->ctl->A_ocean, &v.A, sizeof(double), cudaMemcpyHostToDevice, h->s));
-    int m = b->method;
-    CK(cudaMemcpyAsync(&h->ctl->bsl_method, &m, sizeof(int), cudaMemcpyHostToDevice, h->s));
-    CK(cudaStreamSynchronize(h->s));   // the sources are stack variables
-    return FI_OK;
+    set_args(h->ctl, tf, b->bsl_now, b->A_ocean_now, b->method, write_bsl ? 1 : 0, h->s);
+    h->launches += 1;
 }
 
 int read_status(fi_handle* h, Ctl* hc)
@@ -605,6 +741,30 @@ int read_status(fi_handle* h, Ctl* hc)
 extern "C" {
 
 int fi_version(void) { return 1; }
+
+void* fi_stream(fi_handle* h) { return h ? (void*)h->s : nullptr; }
+
+long long fi_launch_count(const fi_handle* h) { return h ? h->launches : -1; }
+
+int fi_profile(fi_handle* h, int enable)
+{
+    if (!h) return FI_E_ARG;
+    prof_collect(h);
+    if (enable < 0) {
+        for (int i = 0; i < 32; ++i) { h->prof_ms[i] = 0.0; h->prof_cnt[i] = 0; }
+    } else {
+        h->prof_on = enable != 0;
+    }
+    return FI_OK;
+}
+
+int fi_profile_read(fi_handle* h, double* ms, long long* counts, int n)
+{
+    if (!h || !ms || !counts) return FI_E_ARG;
+    prof_collect(h);
+    for (int i = 0; i < n && i < 32; ++i) { ms[i] = h->prof_ms[i]; counts[i] = h->prof_cnt[i]; }
+    return FI_OK;
+}
 
 const char* fi_last_error(const fi_handle* h) { return h ? h->err.c_str() : "null handle"; }
 
@@ -667,6 +827,7 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
         for (size_t e = 0; e < h->n; ++e) { h->K[e] = K_or_null[e]; if (h->K[e] != 1.0) h->uniform = 0; }
     }
     if (cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking) != cudaSuccess) { delete h; return FI_E_CUDA; }
+    if (const char* ev = getenv("FI_NO_GRAPHS")) h->use_graphs = !(ev[0] == '1');
     *out = h;
     host_fields(h);
 
@@ -802,6 +963,8 @@ int fi_destroy(fi_handle* h)
     if (h->s) cudaStreamSynchronize(h->s);
     for (void* p : h->allocs) cudaFree(p);
     if (h->hpin) cudaFreeHost(h->hpin);
+    for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
+    for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
     if (h->s) cudaStreamDestroy(h->s);
     delete h;
     return FI_OK;
@@ -880,7 +1043,7 @@ int fi_init_state(fi_handle* h, const double* z_bed, const double* H_ice, double
                d.rho_sw_over_ice, h->s);
     h->time_prog = time;
     h->time_diag = time;
-    if ((rc = set_bsl_scalars(h, bsl, true))) return rc;
+    enqueue_args(h, time, bsl, true);
     if ((rc = upload(h, h->dH, H_ice, ni * 8))) return rc;
     // The nested isos_update runs with the ode clock still zero: for time <= 0
     // its integrator loop does not execute; for time > 0 the reference would
@@ -908,8 +1071,7 @@ int fi_update_async(fi_handle* h, const double* d_H_ice, double time, fi_bsl* bs
 {
     if (!h || !bsl) return FI_E_ARG;
     if (!h->state_ready) return fail(h, FI_E_STATE, "fi_update before fi_init_state");
-    int rc;
-    if ((rc = set_bsl_scalars(h, bsl, bsl->method == 0 || bsl->method == 1))) return rc;
+    enqueue_args(h, time, bsl, bsl->method == 0 || bsl->method == 1);
     if (d_H_ice) {
         CK(cudaMemcpyAsync(h->dH, d_H_ice, (size_t)h->nx_ice * h->ny_ice * 8, cudaMemcpyDeviceToDevice, h->s));
     }
@@ -931,7 +1093,7 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
     int rc;
     memcpy(h->hpin, H_ice, ni * 8);
     CK(cudaMemcpyAsync(h->dH, h->hpin, ni * 8, cudaMemcpyHostToDevice, h->s));
-    if ((rc = set_bsl_scalars(h, bsl, true))) return rc;
+    enqueue_args(h, time, bsl, true);
     if ((rc = update_any(h, h->dH, time, true))) return rc;
     if (out) {
         gather(h->gsrc, h->gmsrc, 8, 3, h->d, h->dpack, h->s);

@@ -42,9 +42,24 @@ static int smem_optin()
     return g_smem_optin;
 }
 
+// Raise a kernel's dynamic shared-memory limit once (never inside a graph
+// capture: every launch shape runs eagerly before it is captured).
 template <typename K> static void set_smem(K kern, size_t bytes)
 {
-    if (bytes > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    static const void* fn[64];
+    static size_t done[64];
+    static int nfn = 0;
+    if (bytes <= 48 * 1024) return;
+    const void* key = (const void*)kern;
+    for (int i = 0; i < nfn; ++i)
+        if (fn[i] == key) {
+            if (done[i] >= bytes) return;
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            done[i] = bytes;
+            return;
+        }
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (nfn < 64) { fn[nfn] = key; done[nfn] = bytes; ++nfn; }
 }
 
 // ---------------------------------------------------------------------------
@@ -165,11 +180,128 @@ k_flexure(const double* __restrict__ y, const double* __restrict__ wref, const T
     }
 }
 
+// Mixed form, uniform spacing.  The only double work per cell is the pair of
+// forward differences of the double state, dX = y[i+1]-y[i] and
+// dY = y[j+1]-y[j] (taken before rounding to float, so the second
+// differences keep the small curvature of a large smooth field), and the
+// mantle term y - w_ref.  Central and second differences are rebuilt
+// exactly from them: y[i+1]-y[i-1] = dX[i]+dX[i-1],
+// y[i+1]-2y[i]+y[i-1] = dX[i]-dX[i-1].
+struct FlexCoefF {
+    float nu, one_minus_nu, coef_mantle, inv_dx, inv_2dx, inv_dx2, inv_dy, inv_2dy, inv_dy2;
+};
+
+__global__ void __launch_bounds__(TX* TY)
+k_flexure_f32(const double* __restrict__ y, const double* __restrict__ wref, const float* __restrict__ q0,
+              const uint8_t* __restrict__ mask, const float* __restrict__ D, const float* __restrict__ inv2eta,
+              float* __restrict__ f, int nx, int ny, FlexCoefF c)
+{
+    __shared__ double ys[RY][RX];
+    __shared__ float dX[RY][RX];
+    __shared__ float dY[RY][RX];
+    __shared__ float Wx[RY][RX];
+    __shared__ float Mxx[RY][RX];
+    __shared__ float Myy[RY][RX];
+    __shared__ float Mxy[RY][RX];
+    __shared__ float Mxyx[RY][RX];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = blockIdx.x * TX - 2, j0 = blockIdx.y * TY - 2;   // global index of lx = ly = 0
+    for (int ly = ty; ly < RY; ly += TY)
+        for (int lx = tx; lx < RX; lx += TX) {
+            const int gi = i0 + lx, gj = j0 + ly;
+            ys[ly][lx] = (gi >= 0 && gi < nx && gj >= 0 && gj < ny) ? y[(size_t)gj * nx + gi] : 0.0;
+        }
+    __syncthreads();
+    for (int ly = ty; ly < RY; ly += TY)
+        for (int lx = tx; lx < RX; lx += TX) {
+            if (lx < RX - 1) dX[ly][lx] = (float)(ys[ly][lx + 1] - ys[ly][lx]);
+            if (ly < RY - 1) dY[ly][lx] = (float)(ys[ly + 1][lx] - ys[ly][lx]);
+        }
+    __syncthreads();
+    for (int ly = ty; ly < RY; ly += TY)
+        for (int lx = tx + 1; lx < RX - 1; lx += TX) {
+            const int gi = i0 + lx, gj = j0 + ly;
+            if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
+            float v;
+            if (gi == 0) v = dX[ly][lx] * c.inv_dx;
+            else if (gi == nx - 1) v = dX[ly][lx - 1] * c.inv_dx;
+            else v = (dX[ly][lx] + dX[ly][lx - 1]) * c.inv_2dx;
+            Wx[ly][lx] = v;
+        }
+    __syncthreads();
+    for (int ly = ty + 1; ly < RY - 1; ly += TY)
+        for (int lx = tx + 1; lx < RX - 1; lx += TX) {
+            const int gi = i0 + lx, gj = j0 + ly;
+            if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
+            float wxy, wxx, wyy;
+            if (gj == 0) wxy = (Wx[ly + 1][lx] - Wx[ly][lx]) * c.inv_dy;
+            else if (gj == ny - 1) wxy = (Wx[ly][lx] - Wx[ly - 1][lx]) * c.inv_dy;
+            else wxy = (Wx[ly + 1][lx] - Wx[ly - 1][lx]) * c.inv_2dy;
+            if (gi == 0) wxx = (dX[ly][lx + 1] - dX[ly][lx]) * c.inv_dx2;
+            else if (gi == nx - 1) wxx = (dX[ly][lx - 1] - dX[ly][lx - 2]) * c.inv_dx2;
+            else wxx = (dX[ly][lx] - dX[ly][lx - 1]) * c.inv_dx2;
+            if (gj == 0) wyy = (dY[ly + 1][lx] - dY[ly][lx]) * c.inv_dy2;
+            else if (gj == ny - 1) wyy = (dY[ly - 1][lx] - dY[ly - 2][lx]) * c.inv_dy2;
+            else wyy = (dY[ly][lx] - dY[ly - 1][lx]) * c.inv_dy2;
+            const float Dl = D[(size_t)gj * nx + gi];
+            Mxx[ly][lx] = -Dl * (wxx + c.nu * wyy);
+            Myy[ly][lx] = -Dl * (wyy + c.nu * wxx);
+            Mxy[ly][lx] = (-Dl * c.one_minus_nu) * wxy;
+        }
+    __syncthreads();
+    for (int ly = ty + 1; ly < RY - 1; ly += TY)
+        for (int lx = tx + 2; lx < RX - 2; lx += TX) {
+            const int gi = i0 + lx, gj = j0 + ly;
+            if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
+            float v;
+            if (gi == 0) v = (Mxy[ly][lx + 1] - Mxy[ly][lx]) * c.inv_dx;
+            else if (gi == nx - 1) v = (Mxy[ly][lx] - Mxy[ly][lx - 1]) * c.inv_dx;
+            else v = (Mxy[ly][lx + 1] - Mxy[ly][lx - 1]) * c.inv_2dx;
+            Mxyx[ly][lx] = v;
+        }
+    __syncthreads();
+    const int lx = tx + 2, ly = ty + 2;
+    const int gi = i0 + lx, gj = j0 + ly;
+    if (gi >= nx || gj >= ny) return;
+    float mxy_xy, mx_xx, my_yy;
+    if (gj == 0) mxy_xy = (Mxyx[ly + 1][lx] - Mxyx[ly][lx]) * c.inv_dy;
+    else if (gj == ny - 1) mxy_xy = (Mxyx[ly][lx] - Mxyx[ly - 1][lx]) * c.inv_dy;
+    else mxy_xy = (Mxyx[ly + 1][lx] - Mxyx[ly - 1][lx]) * c.inv_2dy;
+    if (gi == 0) mx_xx = ((Mxx[ly][lx + 2] - 2.f * Mxx[ly][lx + 1]) + Mxx[ly][lx]) * c.inv_dx2;
+    else if (gi == nx - 1) mx_xx = ((Mxx[ly][lx] - 2.f * Mxx[ly][lx - 1]) + Mxx[ly][lx - 2]) * c.inv_dx2;
+    else mx_xx = ((Mxx[ly][lx + 1] - 2.f * Mxx[ly][lx]) + Mxx[ly][lx - 1]) * c.inv_dx2;
+    if (gj == 0) my_yy = ((Myy[ly + 2][lx] - 2.f * Myy[ly + 1][lx]) + Myy[ly][lx]) * c.inv_dy2;
+    else if (gj == ny - 1) my_yy = ((Myy[ly][lx] - 2.f * Myy[ly - 1][lx]) + Myy[ly - 2][lx]) * c.inv_dy2;
+    else my_yy = ((Myy[ly + 1][lx] - 2.f * Myy[ly][lx]) + Myy[ly - 1][lx]) * c.inv_dy2;
+    const size_t e = (size_t)gj * nx + gi;
+    float p = 0.f;
+    if (mask[e]) {
+        p = q0[e];
+        if (wref) p += c.coef_mantle * (float)(ys[ly][lx] - wref[e]);
+    }
+    f[e] = (((p + mx_xx) + 2.f * mxy_xy) + my_yy) * inv2eta[e];
+}
+
 template <typename T>
 void launch_flexure(const double* y, const double* wref, const T* q0, const uint8_t* mask, const T* D,
                     const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s)
 {
     dim3 b(TX, TY), g((nx + TX - 1) / TX, (ny + TY - 1) / TY);
+    if (sizeof(T) == 4 && c.dxm == nullptr) {
+        FlexCoefF cf;
+        cf.nu = (float)c.nu;
+        cf.one_minus_nu = (float)c.one_minus_nu;
+        cf.coef_mantle = (float)c.coef_mantle;
+        cf.inv_dx = (float)c.inv_dx;
+        cf.inv_2dx = (float)c.inv_2dx;
+        cf.inv_dx2 = (float)c.inv_dx2;
+        cf.inv_dy = (float)c.inv_dy;
+        cf.inv_2dy = (float)c.inv_2dy;
+        cf.inv_dy2 = (float)c.inv_dy2;
+        k_flexure_f32<<<g, b, 0, s>>>(y, wref, (const float*)q0, mask, (const float*)D, (const float*)inv2eta,
+                                      (float*)f, nx, ny, cf);
+        return;
+    }
     k_flexure<T><<<g, b, 0, s>>>(y, wref, q0, mask, D, inv2eta, f, nx, ny, c);
 }
 
@@ -304,13 +436,14 @@ void launch_rows_inv(const typename vec2<T>::type* S, T* out, const Plan2D& p, d
 // Column kernels.  A block loads CB spectrum columns (all ny rows) into
 // shared memory, column-major, and transforms them together.
 // ---------------------------------------------------------------------------
+// Columns per block: two float2 or one double2 column, i.e. 16-byte row
+// segments, which keeps hundreds of blocks in flight at 512^2.
 template <typename T> static int cols_per_block(int ny)
 {
     typedef typename vec2<T>::type C2;
-    const size_t per_col = 2 * (size_t)ny * sizeof(C2);
-    int cb = (int)((96 * 1024) / per_col);
-    if (cb > 16) cb = 16;
+    int cb = (int)(16 / sizeof(C2));
     if (cb < 1) cb = 1;
+    while (cb > 1 && 2 * (size_t)cb * ny * sizeof(C2) > 200 * 1024) cb /= 2;
     return cb;
 }
 

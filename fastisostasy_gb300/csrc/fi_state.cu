@@ -51,8 +51,11 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV], const bool (&is_ma
     }
 }
 
-// Block partials -> last block combines in block order.  Returns true in the
-// thread 0 of the last block, with the totals in `tot`.
+// Block partials -> the last block to arrive combines them: thread t sums
+// partials t, t+NT, ... in order, then the same fixed tree as block_reduce.
+// The combination order depends only on gridDim, so results are
+// run-to-run deterministic.  Returns true in thread 0 of the last block,
+// with the totals in `tot`.
 template <int NV>
 __device__ bool grid_finish(double (&v)[NV], const bool (&is_max)[NV], double* partials, unsigned* counter,
                             double (&tot)[NV])
@@ -69,21 +72,36 @@ __device__ bool grid_finish(double (&v)[NV], const bool (&is_max)[NV], double* p
     }
     __syncthreads();
     if (!last) return false;
-    if (threadIdx.x == 0) {
-        __threadfence();
+    __threadfence();
+    double a[NV];
 #pragma unroll
-        for (int q = 0; q < NV; ++q) {
-            double a = is_max[q] ? 0.0 : 0.0;
-            for (unsigned b = 0; b < gridDim.x; ++b) {
-                const double pb = ((volatile double*)partials)[(size_t)b * NV + q];
-                a = is_max[q] ? fmax(a, pb) : a + pb;
-            }
-            tot[q] = a;
+    for (int q = 0; q < NV; ++q) {
+        a[q] = 0.0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+            const double pb = ((volatile double*)partials)[(size_t)b * NV + q];
+            a[q] = is_max[q] ? fmax(a[q], pb) : a[q] + pb;
         }
+    }
+    __syncthreads();
+    block_reduce<NV>(a, is_max, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) tot[q] = a[q];
         *counter = 0u;
         return true;
     }
     return false;
+}
+
+// Scalar work done once per block (FP64 throughput is low on this part):
+// the corner mean of a field, broadcast through shared memory.
+template <typename T> __device__ __forceinline__ double block_corner_mean(const T* a, int nx, int ny)
+{
+    __shared__ double s_cm;
+    __syncthreads();
+    if (threadIdx.x == 0) s_cm = corner_mean_of(a, nx, ny);
+    __syncthreads();
+    return s_cm;
 }
 
 __device__ __forceinline__ bool in_crop(const Dom& d, int i, int j)
@@ -187,12 +205,13 @@ k_upd_litho(Dom d, const double* __restrict__ we_raw, const double* __restrict__
 template <typename T>
 __global__ void __launch_bounds__(NT)
 k_upd_load(Dom d, const double* __restrict__ dz_raw, const double* __restrict__ corners, int dz_mode,
-           T* __restrict__ q0, int stage_mode, double tf)
+           T* __restrict__ q0, int stage_mode, int run_integrator)
 {
     double cm = 0.0;
     if (dz_mode == 1) cm = corner_mean(corners[0], corners[1], corners[2], corners[3]);
     const double bsl = d.ctl->bsl;
-    const bool will_step = d.ctl->t < tf;   // get_dwdt refreshes canom_full only if a step runs
+    // get_dwdt refreshes canom_full only if a step runs
+    const bool will_step = run_integrator && d.ctl->t < d.ctl->tf;
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
         double dz = d.dz_ss[e];
         if (dz_mode == 1) dz = dz_raw[e] - cm;
@@ -224,35 +243,56 @@ k_upd_load(Dom d, const double* __restrict__ dz_raw, const double* __restrict__ 
     }
 }
 
-// --- integrator control ------------------------------------------------------
-// kind 0 euler (clips ode%dt), 1 rk4 (local h), 2 tsit54 (clips ode%dt)
-__global__ void k_step_begin(Ctl* c, double tf, int kind)
+// --- per-update arguments ----------------------------------------------------
+// Target time and barystatic scalars of one isos_update, written by a kernel
+// so that the host never waits and a captured update graph reads them from
+// the control block.
+__global__ void k_set_args(Ctl* c, double tf, double bsl, double A_ocean, int method, int write_bsl)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    c->tf = tf;
+    if (write_bsl) c->bsl = bsl;
+    c->A_ocean = A_ocean;
+    c->bsl_method = method;
+}
+
+// --- integrator control ------------------------------------------------------
+// kind 0 euler (clips ode%dt), 1 rk4 (local h), 2 tsit54 (clips ode%dt)
+__global__ void k_step_begin(Ctl* c, int kind)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double tf = c->tf;
     if (c->status != ST_OK || !(c->t < tf)) { c->done = 1; return; }
     c->done = 0;
-    c->tf = tf;
     if (kind == 1) c->h = fmin(c->dt, tf - c->t);
     else { c->dt = fmin(c->dt, tf - c->t); c->h = c->dt; }
 }
 
-// y = x + (a*h) * k,  k = (raw - corner_mean(raw)) * spy
+// y = x + (a*h) * k,  k = (raw - corner_mean(raw)) * spy.
+// Plain form: double throughout.  Mixed form: the increment is formed in
+// float and added to the double state (one double add per cell).
 template <typename T>
 __global__ void __launch_bounds__(NT)
 k_rk_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __restrict__ x, const T* __restrict__ raw,
            double a, int nx, int ny, double spy)
 {
     if (c->done) return;
+    const double cm = block_corner_mean(raw, nx, ny);
     const double ah = a * c->h;
-    const double cm = corner_mean_of(raw, nx, ny);
     const size_t n = (size_t)nx * ny;
-    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
-        const double k = ((double)raw[e] - cm) * spy;
-        y[e] = x[e] + ah * k;
+    if (sizeof(T) == 8) {
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+            const double k = ((double)raw[e] - cm) * spy;
+            y[e] = x[e] + ah * k;
+        }
+    } else {
+        const float cmf = (float)cm, sc = (float)(ah * spy);
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
+            y[e] = x[e] + (double)(((float)raw[e] - cmf) * sc);
     }
 }
 
-// RK4 combination x += (h/6)*(k1 + 2k2 + 2k3 + k4), w = x, t += h.
+// RK4 combination x += (h/6)*(k1 + 2k2 + 2k3 + k4), w = x.
 // Reference mode passes the same raw four times (get_dwdt ignores its state).
 template <typename T>
 __global__ void __launch_bounds__(NT)
@@ -261,16 +301,35 @@ k_rk4_final(Ctl* c, double* __restrict__ x, double* __restrict__ w, const T* __r
             double spy)
 {
     if (c->done) return;
-    const double h6 = c->h / 6;
-    const double c1 = corner_mean_of(r1, nx, ny), c2 = corner_mean_of(r2, nx, ny);
-    const double c3 = corner_mean_of(r3, nx, ny), c4 = corner_mean_of(r4, nx, ny);
+    __shared__ double s[5];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s[0] = c->h / 6;
+        s[1] = corner_mean_of(r1, nx, ny);
+        s[2] = corner_mean_of(r2, nx, ny);
+        s[3] = corner_mean_of(r3, nx, ny);
+        s[4] = corner_mean_of(r4, nx, ny);
+    }
+    __syncthreads();
+    const double h6 = s[0], c1 = s[1], c2 = s[2], c3 = s[3], c4 = s[4];
     const size_t n = (size_t)nx * ny;
-    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
-        const double k1 = ((double)r1[e] - c1) * spy, k2 = ((double)r2[e] - c2) * spy;
-        const double k3 = ((double)r3[e] - c3) * spy, k4 = ((double)r4[e] - c4) * spy;
-        const double v = x[e] + h6 * (((k1 + 2 * k2) + 2 * k3) + k4);
-        x[e] = v;
-        w[e] = v;
+    if (sizeof(T) == 8) {
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+            const double k1 = ((double)r1[e] - c1) * spy, k2 = ((double)r2[e] - c2) * spy;
+            const double k3 = ((double)r3[e] - c3) * spy, k4 = ((double)r4[e] - c4) * spy;
+            const double v = x[e] + h6 * (((k1 + 2 * k2) + 2 * k3) + k4);
+            x[e] = v;
+            w[e] = v;
+        }
+    } else {
+        const float f1 = (float)c1, f2 = (float)c2, f3 = (float)c3, f4 = (float)c4, sc = (float)(h6 * spy);
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+            const float k = ((((float)r1[e] - f1) + 2.f * ((float)r2[e] - f2)) + 2.f * ((float)r3[e] - f3)) +
+                            ((float)r4[e] - f4);
+            const double v = x[e] + (double)(k * sc);
+            x[e] = v;
+            w[e] = v;
+        }
     }
 }
 
@@ -288,13 +347,22 @@ k_euler_final(const Ctl* __restrict__ c, double* __restrict__ x, double* __restr
               int nx, int ny, double spy)
 {
     if (c->done) return;
+    const double c1 = block_corner_mean(r1, nx, ny);
     const double h = c->h;
-    const double c1 = corner_mean_of(r1, nx, ny);
     const size_t n = (size_t)nx * ny;
-    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
-        const double v = x[e] + h * (((double)r1[e] - c1) * spy);
-        x[e] = v;
-        w[e] = v;
+    if (sizeof(T) == 8) {
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+            const double v = x[e] + h * (((double)r1[e] - c1) * spy);
+            x[e] = v;
+            w[e] = v;
+        }
+    } else {
+        const float f1 = (float)c1, sc = (float)(h * spy);
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+            const double v = x[e] + (double)(((float)r1[e] - f1) * sc);
+            x[e] = v;
+            w[e] = v;
+        }
     }
 }
 
@@ -321,7 +389,7 @@ k_ts_max(Dom d, const T* __restrict__ raw, double atol, double rtol)
     Ctl* c = d.ctl;
     if (c->done) return;
     const double dt = c->h;
-    const double cm = corner_mean_of(raw, d.nx, d.ny);
+    const double cm = block_corner_mean(raw, d.nx, d.ny);
     double v[2] = {0.0, 0.0};
     const bool mx[2] = {true, true};
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
@@ -342,7 +410,7 @@ k_ts_err(Dom d, const T* __restrict__ raw, double q, double dt_max, int max_reje
     Ctl* c = d.ctl;
     if (c->done) return;
     const double dt = c->h, tol = c->tol;
-    const double cm = corner_mean_of(raw, d.nx, d.ny);
+    const double cm = block_corner_mean(raw, d.nx, d.ny);
     double v[1] = {0.0};
     const bool mx[1] = {false};
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
@@ -377,7 +445,7 @@ __global__ void __launch_bounds__(NT) k_ts_commit(Dom d, const T* __restrict__ r
     const Ctl* c = d.ctl;
     if (c->done || !c->accepted) return;
     const double dt = c->h;
-    const double cm = corner_mean_of(raw, d.nx, d.ny);
+    const double cm = block_corner_mean(raw, d.nx, d.ny);
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
         const double k = ((double)raw[e] - cm) * d.spy;
         double x1, x2;
@@ -393,9 +461,13 @@ __global__ void __launch_bounds__(NT) k_ts_commit(Dom d, const T* __restrict__ r
 template <typename T>
 __global__ void __launch_bounds__(NT) k_upd_end(Dom d, const T* __restrict__ raw_last, int have_rhs)
 {
-    const double cw = corner_mean_of(d.w, d.nx, d.ny);
-    double cr = 0.0;
-    if (have_rhs) cr = corner_mean_of(raw_last, d.nx, d.ny);
+    __shared__ double s_c[2];
+    if (threadIdx.x == 0) {
+        s_c[0] = corner_mean_of(d.w, d.nx, d.ny);
+        s_c[1] = have_rhs ? corner_mean_of(raw_last, d.nx, d.ny) : 0.0;
+    }
+    __syncthreads();
+    const double cw = s_c[0], cr = s_c[1];
     double v[4] = {0.0, 0.0, 0.0, 0.0};
     const bool mx[4] = {true, true, true, true};
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
@@ -503,11 +575,15 @@ void upd_litho(const Dom& d, const double* we_raw, const double* corners, int we
 }
 template <typename T>
 void upd_load(const Dom& d, const double* dz_raw, const double* corners, int dz_mode, T* q0, int stage_mode,
-              double tf, cudaStream_t s)
+              int run_integrator, cudaStream_t s)
 {
-    k_upd_load<T><<<grid_for(d.n), NT, 0, s>>>(d, dz_raw, corners, dz_mode, q0, stage_mode, tf);
+    k_upd_load<T><<<grid_for(d.n), NT, 0, s>>>(d, dz_raw, corners, dz_mode, q0, stage_mode, run_integrator);
 }
-void step_begin(Ctl* c, double tf, int kind, cudaStream_t s) { k_step_begin<<<1, 32, 0, s>>>(c, tf, kind); }
+void set_args(Ctl* c, double tf, double bsl, double A_ocean, int method, int write_bsl, cudaStream_t s)
+{
+    k_set_args<<<1, 32, 0, s>>>(c, tf, bsl, A_ocean, method, write_bsl);
+}
+void step_begin(Ctl* c, int kind, cudaStream_t s) { k_step_begin<<<1, 32, 0, s>>>(c, kind); }
 void step_end(Ctl* c, cudaStream_t s) { k_step_end<<<1, 32, 0, s>>>(c); }
 template <typename T>
 void rk_stage(const Ctl* c, double* y, const double* x, const T* raw, double a, int nx, int ny, double spy,
@@ -566,7 +642,7 @@ template <typename T>
 __global__ void __launch_bounds__(NT) k_rhs_finish(double* __restrict__ out, const T* __restrict__ raw, int nx, int ny,
                                                    double spy)
 {
-    const double cm = corner_mean_of(raw, nx, ny);
+    const double cm = block_corner_mean(raw, nx, ny);
     const size_t n = (size_t)nx * ny;
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
         out[e] = ((double)raw[e] - cm) * spy;
@@ -613,7 +689,7 @@ template <typename T> void q0_from_cf(T* q0, const double* cf, const uint8_t* ma
 #define FI_STATE_INST(T)                                                                                      \
     template void upd_masks<T>(const Dom&, T*, cudaStream_t);                                                 \
     template void upd_litho<T>(const Dom&, const double*, const double*, int, T*, cudaStream_t);              \
-    template void upd_load<T>(const Dom&, const double*, const double*, int, T*, int, double, cudaStream_t);  \
+    template void upd_load<T>(const Dom&, const double*, const double*, int, T*, int, int, cudaStream_t);     \
     template void rk_stage<T>(const Ctl*, double*, const double*, const T*, double, int, int, double, cudaStream_t); \
     template void rk4_final<T>(Ctl*, double*, double*, const T*, const T*, const T*, const T*, int, int, double,  \
                                cudaStream_t);                                                                 \

@@ -37,8 +37,9 @@ template <typename T>
 void upd_litho(const Dom& d, const double* we_raw, const double* corners, int we_mode, T* conv_in, cudaStream_t s);
 template <typename T>
 void upd_load(const Dom& d, const double* dz_raw, const double* corners, int dz_mode, T* q0, int stage_mode,
-              double tf, cudaStream_t s);
-void step_begin(Ctl* c, double tf, int kind, cudaStream_t s);
+              int run_integrator, cudaStream_t s);
+void set_args(Ctl* c, double tf, double bsl, double A_ocean, int method, int write_bsl, cudaStream_t s);
+void step_begin(Ctl* c, int kind, cudaStream_t s);
 void step_end(Ctl* c, cudaStream_t s);
 template <typename T>
 void rk_stage(const Ctl* c, double* y, const double* x, const T* raw, double a, int nx, int ny, double spy,

@@ -156,6 +156,19 @@ size_t fi_state_size(const fi_handle* h);
 int fi_state_export(fi_handle* h, double* buf);
 int fi_state_import(fi_handle* h, const double* buf);
 
+/* The handle's CUDA stream (cudaStream_t) for event timing by the caller. */
+void* fi_stream(fi_handle* h);
+/* Number of kernels this handle has enqueued so far. */
+long long fi_launch_count(const fi_handle* h);
+/* Per-kernel CUDA-event timing of this handle's launches: enable = 1 on,
+ * 0 off, -1 reset the totals.  fi_profile_read returns total milliseconds
+ * and launch counts for kernel ids 0..n-1: 0 flexure, 1 rows_fwd,
+ * 2 cols_hartley, 3 rows_inv, 4 conv_rows_fwd, 5 conv_cols, 6 conv_rows_inv,
+ * 7 rk_stage, 8 rk_final, 9 upd_begin, 10 upd_masks, 11 upd_litho,
+ * 12 upd_load, 13 upd_end. */
+int fi_profile(fi_handle* h, int enable);
+int fi_profile_read(fi_handle* h, double* ms, long long* counts, int n);
+
 const char* fi_last_error(const fi_handle* h);
 int fi_version(void);
 

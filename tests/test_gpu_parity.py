@@ -111,8 +111,10 @@ def test_reference_experiments_tsit54(name, over):
     pair.step(30)
     compare(pair, TOL64)
     so, sg = pair.orc.scalars(), pair.dom.scalars()
+    # identical accept/reject sequence; dt carries the error norm, whose sum
+    # order differs (parallel reduction), so it agrees to rounding only
     assert so["n_accept"] == sg["n_accept"] and so["n_reject"] == sg["n_reject"]
-    assert so["t"] == sg["t"] and so["dt"] == sg["dt"]
+    assert so["t"] == sg["t"] and abs(so["dt"] - sg["dt"]) <= 1e-10 * so["dt"]
     pair.close()
 
 
@@ -186,8 +188,9 @@ def test_error_status_codes():
         dom.update(H, 10.0, bg)
     assert e.value.code == _lib.FI_E_NAN
     dom.close()
-    # dt = 10 yr on an 11.7 km grid with D ~ 2e25 diverges (lambda*dt ~ -18)
-    wl = W.config2(n=64, L=3000e3 * 64 / 256, dt=10.0, stage_mode=1)
+    # dt = 10 yr on an 11.7 km grid with D ~ 2e25 diverges (lambda*dt ~ -18);
+    # the domain must be wider than the disc so that its edge seeds short waves
+    wl = W.config2(n=128, L=3000e3 * 128 / 256, dt=10.0, stage_mode=1)
     dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx)
     dom.set_fields(**wl.padded_fields(dom.nx, dom.ny))
     dom.init_state(wl.z_bed, wl.H_at(0.0), 0.0, bg)
@@ -196,3 +199,20 @@ def test_error_status_codes():
             dom.update(wl.H_at(10.0 * k), 10.0 * k, bg)
     assert e.value.code == _lib.FI_E_LARGE
     dom.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_replay_matches_eager(precision, monkeypatch):
+    """Updates replayed from a captured CUDA graph give bit-identical state to
+    the same updates launched one kernel at a time."""
+    wl = W.config2(n=64, L=3000e3 * 64 / 256, dt=1.0, stage_mode=1)
+    out = []
+    for no_graph in ("1", "0"):
+        monkeypatch.setenv("FI_NO_GRAPHS", no_graph)
+        p = Pair(wl, precision=precision)
+        p.init()
+        p.step(6)
+        out.append((p.dom.field("w"), p.dom.field("z_bed"), p.dom.field("we")))
+        p.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
