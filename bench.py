@@ -277,6 +277,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--lean", action="store_true",
+                    help="mixed form only, no profile / e2e / CPU legs (for ncu captures); prints the timing only")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -302,6 +304,12 @@ def main():
         torch.cuda.synchronize()
 
     results = {}
+    if args.lean:
+        dom, wl, b = make_domain(1)
+        ms, _, _, _, _ = run_resident(dom, wl, b, args.steps, args.warmup, flush)
+        print(json.dumps({"lean": True, "ms_per_step": sum(ms) / len(ms), "steps": args.steps}))
+        dom.close()
+        return 0
     for prec in (0, 1):
         dom, wl, b = make_domain(prec)
         barrier()

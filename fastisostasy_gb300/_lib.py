@@ -26,11 +26,11 @@ EXPORTS = ["fi_create", "fi_destroy", "fi_dims", "fi_set_fields", "fi_set_kernel
            "fi_init_state", "fi_update", "fi_update_async", "fi_synchronize", "fi_bsl_update",
            "fi_get_field", "fi_get_scalars", "fi_lvelva", "fi_convolve", "fi_state_size",
            "fi_state_export", "fi_state_import", "fi_last_error", "fi_version", "fi_stream",
-           "fi_launch_count", "fi_profile", "fi_profile_read"]
+           "fi_launch_count", "fi_profile", "fi_profile_read", "fi_engine_trace"]
 
 PROFILE_KERNELS = ["flexure", "rows_fwd", "cols_hartley", "rows_inv", "conv_rows_fwd", "conv_cols",
                    "conv_rows_inv", "rk_stage", "rk_final", "upd_begin", "upd_masks", "upd_litho",
-                   "upd_load", "upd_end"]
+                   "upd_load", "upd_end", "control", "ts", "engine"]
 
 
 class FiParams(C.Structure):
@@ -112,6 +112,7 @@ def load(build_if_missing: bool = True):
     L.fi_stream.restype = C.c_void_p
     L.fi_launch_count.argtypes = [H]
     L.fi_launch_count.restype = C.c_longlong
+    L.fi_engine_trace.argtypes = [H, C.c_void_p, C.c_int]
     L.fi_profile.argtypes = [H, C.c_int]
     L.fi_profile_read.argtypes = [H, _dp, C.POINTER(C.c_longlong), C.c_int]
     L.fi_last_error.argtypes = [H]

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/fi_gpu.h"
+#include "fi_engine.h"
 #include "fi_kernels.h"
 #include "fi_state.h"
 
@@ -108,6 +109,12 @@ struct fi_handle {
     std::vector<GraphEntry> graphs;
     std::vector<long long> graph_seen;
     bool use_graphs = true;
+    // persistent cooperative RK4 engine (true stages, uniform spacing)
+    bool engine_ok = false;
+    int eng_grid = 0, eng_CB = 1;
+    size_t eng_smem = 0;
+    float *xhi = nullptr, *xlo = nullptr, *wrefhi = nullptr, *wreflo = nullptr;
+    unsigned long long* trace = nullptr;   // engine phase timestamps (fi_engine_trace)
     // optional per-kernel CUDA-event timing (fi_profile)
     bool prof_on = false;
     std::vector<cudaEvent_t> prof_ev;
@@ -175,7 +182,8 @@ int fail(fi_handle* h, int code, const char* fmt, ...)
 
 // Kernel ids of the profiler (fi_profile_read): see include/fi_gpu.h.
 enum { K_FLEX = 0, K_ROWS_FWD, K_COLS_HARTLEY, K_ROWS_INV, K_CONV_ROWS_FWD, K_CONV_COLS, K_CONV_ROWS_INV,
-       K_STAGE, K_RK_FINAL, K_UPD_BEGIN, K_UPD_MASKS, K_UPD_LITHO, K_UPD_LOAD, K_UPD_END, K_CONTROL, K_TS, K_NPROF };
+       K_STAGE, K_RK_FINAL, K_UPD_BEGIN, K_UPD_MASKS, K_UPD_LITHO, K_UPD_LOAD, K_UPD_END, K_CONTROL, K_TS,
+       K_ENGINE, K_NPROF };
 
 int prof_begin(fi_handle* h, int id)
 {
@@ -581,6 +589,44 @@ template <typename T> T* enqueue_steps(fi_handle* h, int nsteps)
     return last;
 }
 
+// All RK4 steps of one update in one cooperative launch (fi_engine.cu).
+template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
+{
+    if (mixed(h)) {
+        PROF(h, K_STAGE, split_hilo(h->d.x, h->xhi, h->xlo, h->n, h->s));
+        h->launches += 1;
+    }
+    EngineArgs g;
+    memset(&g, 0, sizeof(g));
+    g.p = h->prhs;
+    g.fc = h->fc;
+    g.x = h->d.x;
+    g.w = h->d.w;
+    g.xhi = h->xhi;
+    g.xlo = h->xlo;
+    g.wrefhi = h->wrefhi;
+    g.wreflo = h->wreflo;
+    g.wref = h->w_ref;
+    g.q0 = h->q0;
+    g.D = h->Dt;
+    g.inv2eta = h->inv2eta;
+    g.mA = h->mA;
+    g.mB = h->mB;
+    g.even = h->even;
+    g.mask = h->d.mactive;
+    for (int i = 0; i < 4; ++i) g.raw[i] = h->raw[i];
+    g.S = h->S;
+    g.ctl = h->ctl;
+    g.nsteps = nsteps;
+    g.CB = h->eng_CB;
+    g.spy = h->spy;
+    g.norm_scale = 1.0 / (double)(float)((long long)h->nx * h->ny);
+    g.trace = h->trace;
+    PROF(h, K_ENGINE, engine_launch<T>(g, h->eng_grid, h->eng_smem, h->s));
+    h->launches += 1;
+    return (T*)h->raw[3];
+}
+
 // Reference-compatible Tsit5: one distinct RHS per state; the host waits
 // for each attempt's accept/reject decision.
 template <typename T> int integrate_tsit(fi_handle* h, double tf, int* have_rhs, T** raw_last)
@@ -668,7 +714,7 @@ template <typename T> int update_T(fi_handle* h, const double* dH, double time, 
                           ((long long)(dH == h->dH) << 2);
     auto enqueue = [&]() {
         enqueue_pre<T>(h, dH, diag, run_integrator);
-        T* raw_last = enqueue_steps<T>(h, nsteps);
+        T* raw_last = (h->engine_ok && nsteps > 0) ? enqueue_engine<T>(h, nsteps) : enqueue_steps<T>(h, nsteps);
         enqueue_post<T>(h, raw_last, nsteps > 0 ? 1 : 0);
     };
     if (!h->use_graphs || h->prof_on) {
@@ -745,6 +791,21 @@ int fi_version(void) { return 1; }
 void* fi_stream(fi_handle* h) { return h ? (void*)h->s : nullptr; }
 
 long long fi_launch_count(const fi_handle* h) { return h ? h->launches : -1; }
+
+int fi_engine_trace(fi_handle* h, unsigned long long* out, int n)
+{
+    if (!h) return FI_E_ARG;
+    if (!h->trace) {
+        int rc;
+        if ((rc = dalloc(h, &h->trace, 64 * sizeof(unsigned long long)))) return rc;
+        CK(cudaStreamSynchronize(h->s));
+        return FI_OK;
+    }
+    if (!out) return FI_OK;
+    CK(cudaStreamSynchronize(h->s));
+    CK(cudaMemcpy(out, h->trace, (n < 64 ? n : 64) * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    return FI_OK;
+}
 
 int fi_profile(fi_handle* h, int enable)
 {
@@ -945,6 +1006,22 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
 #undef AL
     if ((rc = upload_static(h))) return rc;
     if ((rc = kernel_spectrum(h, h->GE, 0)) || (rc = kernel_spectrum(h, h->GN, 1))) return rc;
+    // cooperative step engine for true-stage RK4 on uniform grids
+    {
+        const char* ev = getenv("FI_NO_ENGINE");
+        const bool want = p.stage_mode == 1 && p.dt_method == 1 && h->uniform && !(ev && ev[0] == '1');
+        if (want) {
+            int ok = mixed(h) ? engine_config<float>(h->prhs, &h->eng_grid, &h->eng_CB, &h->eng_smem)
+                              : engine_config<double>(h->prhs, &h->eng_grid, &h->eng_CB, &h->eng_smem);
+            h->engine_ok = ok != 0;
+            cudaGetLastError();
+            if (h->engine_ok && mixed(h)) {
+#define AL2(ptr, bytes) if ((rc = dalloc(h, &(ptr), (bytes)))) return rc
+                AL2(h->xhi, n * 4); AL2(h->xlo, n * 4); AL2(h->wrefhi, n * 4); AL2(h->wreflo, n * 4);
+#undef AL2
+            }
+        }
+    }
     // zero_init_state (src/fastisostasy.f90:505-548): z_bed background 1e6
     {
         std::vector<double> bg(n, 1e6);
@@ -1043,6 +1120,7 @@ int fi_init_state(fi_handle* h, const double* z_bed, const double* H_ice, double
                d.rho_sw_over_ice, h->s);
     h->time_prog = time;
     h->time_diag = time;
+    if (h->wrefhi) split_hilo(h->w_ref, h->wrefhi, h->wreflo, h->n, h->s);
     enqueue_args(h, time, bsl, true);
     if ((rc = upload(h, h->dH, H_ice, ni * 8))) return rc;
     // The nested isos_update runs with the ode clock still zero: for time <= 0
@@ -1322,6 +1400,7 @@ int fi_state_import(fi_handle* h, const double* buf)
     const double* s = buf + off;
     h->time_diag = s[0]; h->time_prog = s[1]; h->h_t = s[2]; h->h_dt = s[3]; h->ref_bsl = s[4];
     h->ref_was_set = (int)s[5]; h->state_ready = (int)s[6];
+    if (h->wrefhi) split_hilo(h->w_ref, h->wrefhi, h->wreflo, h->n, h->s);
     CK(cudaMemcpyAsync(h->ctl, s + 8, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
     CK(cudaStreamSynchronize(h->s));
     return FI_OK;

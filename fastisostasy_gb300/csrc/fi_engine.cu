@@ -1,0 +1,502 @@
+// fi_engine.cu — persistent cooperative RK4 step engine.
+//
+// One cooperative launch integrates all RK4 steps of an isos_update
+// (step_rk4 with true stages, src/integrators.f90:42-77, evaluating
+// calc_lvelva, src/lv_elva.f90:31-126, at every stage state).  The grid
+// walks through phases separated by grid-wide barriers:
+//
+//   A  stencil + row real-FFT   (work item = 2 grid rows, full width)
+//   B  column FFT, multiply by 1/(kappa R) in the Hartley basis, inverse
+//   C  inverse row real-FFT -> raw_s (stage output before corner BC / sec_per_year)
+//   D  x += h/6 (k1 + 2 k2 + 2 k3 + k4), w = x
+//
+// Stage states y_s = x + a_s h k_{s-1} are never stored: phase A rebuilds the
+// differences it needs from x and raw_{s-1} (the corner mean of raw cancels
+// in every difference and enters only the mantle term).  In the mixed form x
+// also lives as a float hi/lo pair (x = hi + lo), so the forward differences
+// dX = (hi[i+1]-hi[i]) + (lo[i+1]-lo[i]) + s (raw[i+1]-raw[i]) are formed in
+// float without losing the curvature of a large smooth field; the only
+// double arithmetic left is the state update of phase D.
+#include <cooperative_groups.h>
+
+#include <cstdio>
+#include <type_traits>
+
+#include "fi_engine.h"
+#include "fi_fft.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace fi {
+
+template <typename T> __device__ __forceinline__ const typename vec2<T>::type* etw(const FftLen& L);
+template <> __device__ __forceinline__ const double2* etw<double>(const FftLen& L) { return L.tw64; }
+template <> __device__ __forceinline__ const float2* etw<float>(const FftLen& L) { return L.tw32; }
+template <typename T> __device__ __forceinline__ const typename vec2<T>::type* ertw(const Plan2D& p);
+template <> __device__ __forceinline__ const double2* ertw<double>(const Plan2D& p) { return p.rtw64; }
+template <> __device__ __forceinline__ const float2* ertw<float>(const Plan2D& p) { return p.rtw32; }
+
+constexpr int RA = 2;   // rows per phase-A item (must be even: see the y-boundary stencils)
+constexpr int RC = 2;   // rows per phase-C item
+
+// stage coefficients of RK4: y_s = x + a_s h k_{s-1}
+__constant__ double c_rk4_a[4] = {0.0, 0.5, 0.5, 1.0};
+
+template <typename T> struct PhaseAMem {
+    // level-0 differences on RA+4 rows, moments on RA+2 rows, all full width
+    static size_t bytes(int nx, int h)
+    {
+        typedef typename vec2<T>::type C2;
+        const size_t rows = (RA + 4) + (RA + 3) + (RA + 4) + 4 * (RA + 2);
+        return rows * (size_t)nx * sizeof(T) + 2 * (size_t)RA * h * sizeof(C2);
+    }
+};
+
+template <typename T> size_t engine_smem_bytes(const Plan2D& p, int CB)
+{
+    typedef typename vec2<T>::type C2;
+    size_t a = PhaseAMem<T>::bytes(p.nx, p.h);
+    size_t b = 2 * (size_t)CB * p.ny * sizeof(C2);
+    size_t c = 2 * (size_t)RC * p.h * sizeof(C2);
+    size_t m = a > b ? a : b;
+    return (m > c ? m : c) + 64;
+}
+
+template <typename T> __device__ __forceinline__ double corner_mean_dev(const T* a, int nx, int ny)
+{
+    return corner_mean_of(a, nx, ny);
+}
+
+// ---------------------------------------------------------------------------
+// Phase A: one item = output rows j0, j0+1 (full width).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsigned char* smem)
+{
+    typedef typename vec2<T>::type C2;
+    const int nx = g.p.nx, ny = g.p.ny, hh = g.p.h;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    T* dX = reinterpret_cast<T*>(smem);
+    T* dY = dX + (size_t)(RA + 4) * nx;
+    T* Wx = dY + (size_t)(RA + 3) * nx;
+    T* Mxx = Wx + (size_t)(RA + 4) * nx;
+    T* Myy = Mxx + (size_t)(RA + 2) * nx;
+    T* Mxy = Myy + (size_t)(RA + 2) * nx;
+    T* Mxyx = Mxy + (size_t)(RA + 2) * nx;
+    C2* b0 = reinterpret_cast<C2*>(Mxyx + (size_t)(RA + 2) * nx);
+    C2* b1 = b0 + (size_t)RA * hh;
+
+    const T* rprev = stage > 0 ? (const T*)g.raw[stage - 1] : nullptr;
+    __shared__ double s_sc[2];
+    if (tid == 0) {
+        // y = x + a h spy (raw - cm): the scale s and the corner mean cm
+        s_sc[0] = stage > 0 ? c_rk4_a[stage] * h * g.spy : 0.0;
+        s_sc[1] = stage > 0 ? corner_mean_of(rprev, nx, ny) : 0.0;
+    }
+    __syncthreads();
+    const double sd = s_sc[0], cmd = s_sc[1];
+
+    // level 0: forward differences along x (dX) and y (dY)
+    for (int e = tid; e < (RA + 4) * nx; e += nt) {
+        const int r = e / nx, i = e - r * nx;
+        const int gj = j0 - 2 + r;
+        if (gj < 0 || gj >= ny) continue;
+        const size_t c0 = (size_t)gj * nx + i;
+        if (i < nx - 1) {
+            if constexpr (std::is_same<T, float>::value) {
+                float v = (g.xhi[c0 + 1] - g.xhi[c0]) + (g.xlo[c0 + 1] - g.xlo[c0]);
+                if (rprev) v += (float)sd * (rprev[c0 + 1] - rprev[c0]);
+                dX[(size_t)r * nx + i] = v;
+            } else {
+                double y1 = g.x[c0 + 1], y0 = g.x[c0];
+                if (rprev) { y1 += sd * ((double)rprev[c0 + 1] - cmd); y0 += sd * ((double)rprev[c0] - cmd); }
+                dX[(size_t)r * nx + i] = y1 - y0;
+            }
+        }
+        if (r < RA + 3 && gj + 1 < ny) {
+            const size_t c1 = c0 + nx;
+            if constexpr (std::is_same<T, float>::value) {
+                float v = (g.xhi[c1] - g.xhi[c0]) + (g.xlo[c1] - g.xlo[c0]);
+                if (rprev) v += (float)sd * (rprev[c1] - rprev[c0]);
+                dY[(size_t)r * nx + i] = v;
+            } else {
+                double y1 = g.x[c1], y0 = g.x[c0];
+                if (rprev) { y1 += sd * ((double)rprev[c1] - cmd); y0 += sd * ((double)rprev[c0] - cmd); }
+                dY[(size_t)r * nx + i] = y1 - y0;
+            }
+        }
+    }
+    __syncthreads();
+    const T inv_dx = (T)g.fc.inv_dx, inv_2dx = (T)g.fc.inv_2dx, inv_dx2 = (T)g.fc.inv_dx2;
+    const T inv_dy = (T)g.fc.inv_dy, inv_2dy = (T)g.fc.inv_2dy, inv_dy2 = (T)g.fc.inv_dy2;
+    for (int e = tid; e < (RA + 4) * nx; e += nt) {
+        const int r = e / nx, i = e - r * nx;
+        const int gj = j0 - 2 + r;
+        if (gj < 0 || gj >= ny) continue;
+        const T* d = dX + (size_t)r * nx;
+        T v;
+        if (i == 0) v = d[0] * inv_dx;
+        else if (i == nx - 1) v = d[nx - 2] * inv_dx;
+        else v = (d[i] + d[i - 1]) * inv_2dx;
+        Wx[(size_t)r * nx + i] = v;
+    }
+    __syncthreads();
+    const T nu = (T)g.fc.nu, omn = (T)g.fc.one_minus_nu;
+    for (int e = tid; e < (RA + 2) * nx; e += nt) {
+        const int m = e / nx, i = e - m * nx;
+        const int r = m + 1;
+        const int gj = j0 - 2 + r;
+        if (gj < 0 || gj >= ny) continue;
+        const size_t ri = (size_t)r * nx + i;
+        T wxy, wxx, wyy;
+        if (gj == 0) wxy = (Wx[ri + nx] - Wx[ri]) * inv_dy;
+        else if (gj == ny - 1) wxy = (Wx[ri] - Wx[ri - nx]) * inv_dy;
+        else wxy = (Wx[ri + nx] - Wx[ri - nx]) * inv_2dy;
+        const T* d = dX + (size_t)r * nx;
+        if (i == 0) wxx = (d[1] - d[0]) * inv_dx2;
+        else if (i == nx - 1) wxx = (d[nx - 2] - d[nx - 3]) * inv_dx2;
+        else wxx = (d[i] - d[i - 1]) * inv_dx2;
+        if (gj == 0) wyy = (dY[ri + nx] - dY[ri]) * inv_dy2;
+        else if (gj == ny - 1) wyy = (dY[ri - nx] - dY[ri - 2 * nx]) * inv_dy2;
+        else wyy = (dY[ri] - dY[ri - nx]) * inv_dy2;
+        const T Dl = g.D_T<T>()[(size_t)gj * nx + i];
+        const size_t mi = (size_t)m * nx + i;
+        Mxx[mi] = -Dl * (wxx + nu * wyy);
+        Myy[mi] = -Dl * (wyy + nu * wxx);
+        Mxy[mi] = (-Dl * omn) * wxy;
+    }
+    __syncthreads();
+    for (int e = tid; e < (RA + 2) * nx; e += nt) {
+        const int m = e / nx, i = e - m * nx;
+        const int gj = j0 - 1 + m;
+        if (gj < 0 || gj >= ny) continue;
+        const T* M = Mxy + (size_t)m * nx;
+        T v;
+        if (i == 0) v = (M[1] - M[0]) * inv_dx;
+        else if (i == nx - 1) v = (M[nx - 1] - M[nx - 2]) * inv_dx;
+        else v = (M[i + 1] - M[i - 1]) * inv_2dx;
+        Mxyx[(size_t)m * nx + i] = v;
+    }
+    __syncthreads();
+    const T* q0 = g.q0_T<T>();
+    const T* i2e = g.inv2eta_T<T>();
+    for (int e = tid; e < RA * nx; e += nt) {
+        const int o = e / nx, i = e - o * nx;
+        const int gj = j0 + o;
+        T fv = (T)0;
+        if (gj < ny) {
+            const int m = o + 1;
+            const size_t mi = (size_t)m * nx + i;
+            T mxy_xy, mx_xx, my_yy;
+            if (gj == 0) mxy_xy = (Mxyx[mi + nx] - Mxyx[mi]) * inv_dy;
+            else if (gj == ny - 1) mxy_xy = (Mxyx[mi] - Mxyx[mi - nx]) * inv_dy;
+            else mxy_xy = (Mxyx[mi + nx] - Mxyx[mi - nx]) * inv_2dy;
+            const T* M = Mxx + (size_t)m * nx;
+            if (i == 0) mx_xx = ((M[2] - (T)2 * M[1]) + M[0]) * inv_dx2;
+            else if (i == nx - 1) mx_xx = ((M[nx - 1] - (T)2 * M[nx - 2]) + M[nx - 3]) * inv_dx2;
+            else mx_xx = ((M[i + 1] - (T)2 * M[i]) + M[i - 1]) * inv_dx2;
+            if (gj == 0) my_yy = ((Myy[mi + 2 * nx] - (T)2 * Myy[mi + nx]) + Myy[mi]) * inv_dy2;
+            else if (gj == ny - 1) my_yy = ((Myy[mi] - (T)2 * Myy[mi - nx]) + Myy[mi - 2 * nx]) * inv_dy2;
+            else my_yy = ((Myy[mi + nx] - (T)2 * Myy[mi]) + Myy[mi - nx]) * inv_dy2;
+            const size_t c = (size_t)gj * nx + i;
+            T p = (T)0;
+            if (g.mask[c]) {
+                // q0 + (-g rho_m) (y - w_ref) with y the stage state
+                if constexpr (std::is_same<T, float>::value) {
+                    float dy = (g.xhi[c] - g.wrefhi[c]) + (g.xlo[c] - g.wreflo[c]);
+                    if (rprev) dy += (float)sd * (rprev[c] - (float)cmd);
+                    p = q0[c] + (float)g.fc.coef_mantle * dy;
+                } else {
+                    double y = g.x[c];
+                    if (rprev) y += sd * ((double)rprev[c] - cmd);
+                    p = (double)q0[c] + g.fc.coef_mantle * (y - g.wref[c]);
+                }
+            }
+            fv = (((p + mx_xx) + (T)2 * mxy_xy) + my_yy) * i2e[c];
+        }
+        // pack the real row as complex pairs for the half-length FFT
+        T* bz = reinterpret_cast<T*>(b0 + (size_t)o * hh);
+        bz[i] = fv;
+    }
+    __syncthreads();
+    C2* r = block_fft<T>(b0, b1, g.p.row.d, RA, hh, etw<T>(g.p.row), -1);
+    const C2* rtw = ertw<T>(g.p);
+    C2* S = (C2*)g.S;
+    for (int e = tid; e < RA * (hh + 1); e += nt) {
+        const int o = e / (hh + 1), k = e - o * (hh + 1);
+        const int gj = j0 + o;
+        if (gj >= ny) continue;
+        const C2 Zk = r[o * hh + (k == hh ? 0 : k)];
+        const C2 Zc = r[o * hh + (k == 0 ? 0 : hh - k)];
+        C2 E, O;
+        E.x = (T)0.5 * (Zk.x + Zc.x);
+        E.y = (T)0.5 * (Zk.y - Zc.y);
+        O.x = (T)0.5 * (Zk.y + Zc.y);
+        O.y = (T)-0.5 * (Zk.x - Zc.x);
+        S[(size_t)gj * g.p.sp + k] = cadd(E, cmul(__ldg(rtw + k), O));
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Phase B: CB spectrum columns: forward column FFT, Hartley-basis multiply,
+// inverse column FFT.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem)
+{
+    typedef typename vec2<T>::type C2;
+    const int ny = g.p.ny;
+    C2* b0 = reinterpret_cast<C2*>(smem);
+    C2* b1 = b0 + (size_t)CB * ny;
+    C2* S = (C2*)g.S;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int e = tid; e < CB * ny; e += nt) {
+        const int c = e % CB, l = e / CB;
+        const int k = k0 + c;
+        b0[c * ny + l] = (k <= g.p.h) ? S[(size_t)l * g.p.sp + k] : mk2<T>((T)0, (T)0);
+    }
+    __syncthreads();
+    C2* r = block_fft<T>(b0, b1, g.p.col.d, CB, ny, etw<T>(g.p.col), -1);
+    const T* mA = g.mA_T<T>();
+    const T* mB = g.mB_T<T>();
+    const int half = ny / 2 + 1;
+    for (int e = tid; e < CB * half; e += nt) {
+        const int c = e % CB, l = e / CB;
+        const int k = k0 + c;
+        if (k > g.p.h) continue;
+        const int lm = (ny - l) % ny;
+        C2* col = r + (size_t)c * ny;
+        const size_t ia = (size_t)l * g.p.sp + k, ib = (size_t)lm * g.p.sp + k;
+        const C2 Fa = col[l], Fb = col[lm];
+        if (g.even) {
+            const T ma = mA[ia], mb = mA[ib];
+            C2 a = Fa, b = Fb;
+            a.x *= ma; a.y *= ma;
+            b.x *= mb; b.y *= mb;
+            col[l] = a;
+            if (lm != l) col[lm] = b;
+        } else {
+            const T H_kl = Fb.x - Fa.y, H_mkml = Fb.x + Fa.y;
+            const T H_mkl = Fa.x + Fb.y, H_kml = Fa.x - Fb.y;
+            const T G_kl = mA[ia] * H_kl, G_kml = mA[ib] * H_kml;
+            const T G_mkl = mB[ia] * H_mkl, G_mkml = mB[ib] * H_mkml;
+            C2 a, b;
+            a.x = (T)0.5 * (G_kml + G_mkl);
+            a.y = (T)0.5 * (G_mkml - G_kl);
+            b.x = (T)0.5 * (G_kl + G_mkml);
+            b.y = (T)0.5 * (G_mkl - G_kml);
+            col[l] = a;
+            if (lm != l) col[lm] = b;
+        }
+    }
+    __syncthreads();
+    C2* other = (r == b0) ? b1 : b0;
+    C2* q = block_fft<T>(r, other, g.p.col.d, CB, ny, etw<T>(g.p.col), +1);
+    for (int e = tid; e < CB * ny; e += nt) {
+        const int c = e % CB, l = e / CB;
+        const int k = k0 + c;
+        if (k <= g.p.h) S[(size_t)l * g.p.sp + k] = q[c * ny + l];
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Phase C: inverse row real-FFT of rows j0 .. j0+RC-1 -> raw (scaled 1/(nx ny)).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem)
+{
+    typedef typename vec2<T>::type C2;
+    const int hh = g.p.h, ny = g.p.ny, nx = g.p.nx;
+    C2* b0 = reinterpret_cast<C2*>(smem);
+    C2* b1 = b0 + (size_t)RC * hh;
+    const C2* S = (const C2*)g.S;
+    const C2* rtw = ertw<T>(g.p);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int e = tid; e < RC * hh; e += nt) {
+        const int o = e / hh, k = e - o * hh;
+        const int j = j0 + o;
+        C2 z = mk2<T>((T)0, (T)0);
+        if (j < ny) {
+            const C2 A = S[(size_t)j * g.p.sp + k];
+            C2 B = S[(size_t)j * g.p.sp + (hh - k)];
+            B.y = -B.y;
+            const C2 sum = cadd(A, B), dif = csub(A, B);
+            const C2 t = cmulc(dif, __ldg(rtw + k));
+            z.x = sum.x - t.y;
+            z.y = sum.y + t.x;
+        }
+        b0[e] = z;
+    }
+    __syncthreads();
+    C2* r = block_fft<T>(b0, b1, g.p.row.d, RC, hh, etw<T>(g.p.row), +1);
+    const T scale = (T)g.norm_scale;
+    for (int e = tid; e < RC * hh; e += nt) {
+        const int o = e / hh, m = e - o * hh;
+        const int j = j0 + o;
+        if (j >= ny) continue;
+        C2 v = r[e];
+        v.x *= scale;
+        v.y *= scale;
+        *reinterpret_cast<C2*>(out + (size_t)j * nx + 2 * m) = v;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_engine_rk4(EngineArgs g)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    cg::grid_group grid = cg::this_grid();
+    const int nx = g.p.nx, ny = g.p.ny;
+    const size_t n = (size_t)nx * ny;
+    const int na = (ny + RA - 1) / RA, nb = (g.p.h + 1 + g.CB - 1) / g.CB, nc = (ny + RC - 1) / RC;
+    Ctl* ctl = g.ctl;
+    __shared__ double s_h;
+    const bool tr = g.trace && blockIdx.x == 0 && threadIdx.x == 0;
+    int tk = 0;
+#define TRACE() do { if (tr && step == 0 && tk < 64) g.trace[tk++] = gtimer(); } while (0)
+    for (int step = 0; step < g.nsteps; ++step) {
+        TRACE();
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            // step_rk4: h = min(dt, tf - t) (src/integrators.f90:62-63)
+            if (ctl->status == ST_OK && ctl->t < ctl->tf) {
+                ctl->h = fmin(ctl->dt, ctl->tf - ctl->t);
+                ctl->done = 0;
+            } else {
+                ctl->done = 1;
+            }
+        }
+        grid.sync();
+        if (threadIdx.x == 0) s_h = ((volatile Ctl*)ctl)->done ? -1.0 : ((volatile Ctl*)ctl)->h;
+        __syncthreads();
+        const double h = s_h;
+        if (h < 0.0) return;   // uniform over the grid
+        TRACE();
+        for (int stage = 0; stage < 4; ++stage) {
+            for (int it = blockIdx.x; it < na; it += gridDim.x) phase_a<T>(g, it * RA, stage, h, smem);
+            TRACE();
+            grid.sync();
+            TRACE();
+            for (int it = blockIdx.x; it < nb; it += gridDim.x) phase_b<T>(g, it * g.CB, g.CB, smem);
+            TRACE();
+            grid.sync();
+            TRACE();
+            for (int it = blockIdx.x; it < nc; it += gridDim.x) phase_c<T>(g, it * RC, (T*)g.raw[stage], smem);
+            TRACE();
+            grid.sync();
+            TRACE();
+        }
+        // phase D: x += h/6 (k1 + 2 k2 + 2 k3 + k4), w = x (+ hi/lo copy)
+        __shared__ double s_c[5];
+        if (threadIdx.x == 0) {
+            s_c[0] = h / 6;
+            for (int s = 0; s < 4; ++s) s_c[1 + s] = corner_mean_of((const T*)g.raw[s], nx, ny);
+        }
+        __syncthreads();
+        const T* r1 = (const T*)g.raw[0];
+        const T* r2 = (const T*)g.raw[1];
+        const T* r3 = (const T*)g.raw[2];
+        const T* r4 = (const T*)g.raw[3];
+        for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+            if constexpr (std::is_same<T, float>::value) {
+                const float k = ((((float)r1[e] - (float)s_c[1]) + 2.f * ((float)r2[e] - (float)s_c[2])) +
+                                 2.f * ((float)r3[e] - (float)s_c[3])) + ((float)r4[e] - (float)s_c[4]);
+                const double v = g.x[e] + (double)(k * (float)(s_c[0] * g.spy));
+                g.x[e] = v;
+                g.w[e] = v;
+                const float hi = (float)v;
+                g.xhi[e] = hi;
+                g.xlo[e] = (float)(v - (double)hi);
+            } else {
+                const double k1 = ((double)r1[e] - s_c[1]) * g.spy, k2 = ((double)r2[e] - s_c[2]) * g.spy;
+                const double k3 = ((double)r3[e] - s_c[3]) * g.spy, k4 = ((double)r4[e] - s_c[4]) * g.spy;
+                const double v = g.x[e] + s_c[0] * (((k1 + 2 * k2) + 2 * k3) + k4);
+                g.x[e] = v;
+                g.w[e] = v;
+            }
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            ctl->t = ctl->t + h;
+            ctl->n_accept++;
+        }
+        TRACE();
+        grid.sync();
+        TRACE();
+    }
+#undef TRACE
+}
+
+// hi/lo split of the double state (mixed form), used before the first step
+// and after anything outside the engine changed x or w_ref.
+__global__ void k_split(const double* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo, size_t n)
+{
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const double v = x[e];
+        const float a = (float)v;
+        hi[e] = a;
+        lo[e] = (float)(v - (double)a);
+    }
+}
+
+void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s)
+{
+    int b = (int)((n + 255) / 256);
+    if (b > 1216) b = 1216;
+    k_split<<<b, 256, 0, s>>>(x, hi, lo, n);
+}
+
+template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem)
+{
+    typedef typename vec2<T>::type C2;
+    int cb = (int)(16 / sizeof(C2));
+    if (cb < 1) cb = 1;
+    *CB = cb;
+    *smem = engine_smem_bytes<T>(p, cb);
+    int dev = 0, nsm = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (*smem > (size_t)optin) return 0;
+    if (cudaFuncSetAttribute(k_engine_rk4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess)
+        return 0;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T>, 256, *smem) != cudaSuccess || per_sm < 1)
+        return 0;
+    if (per_sm > 2) per_sm = 2;
+    *grid = per_sm * nsm;
+    return 1;
+}
+
+template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, size_t smem, cudaStream_t s)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_engine_rk4<T>, g);
+}
+
+template size_t engine_smem_bytes<float>(const Plan2D&, int);
+template size_t engine_smem_bytes<double>(const Plan2D&, int);
+template int engine_config<float>(const Plan2D&, int*, int*, size_t*);
+template int engine_config<double>(const Plan2D&, int*, int*, size_t*);
+template cudaError_t engine_launch<float>(const EngineArgs&, int, size_t, cudaStream_t);
+template cudaError_t engine_launch<double>(const EngineArgs&, int, size_t, cudaStream_t);
+
+}  // namespace fi

@@ -1,0 +1,51 @@
+// fi_engine.h — the persistent cooperative RK4 step engine (fi_engine.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fi_common.cuh"
+#include "fi_kernels.h"
+
+namespace fi {
+
+struct EngineArgs {
+    Plan2D p;
+    FlexCoef fc;                     // uniform spacing only
+    double* x;                       // integrator state (double)
+    double* w;                       // now%w
+    float* xhi;                      // mixed form: x = xhi + xlo
+    float* xlo;
+    const float* wrefhi;             // mixed form: w_ref = wrefhi + wreflo
+    const float* wreflo;
+    const double* wref;              // plain form
+    const void* q0;                  // RHS load term, field type
+    const void* D;
+    const void* inv2eta;
+    const void* mA;
+    const void* mB;
+    int even;
+    const uint8_t* mask;
+    void* raw[4];                    // stage outputs, field type
+    void* S;                         // half spectrum, field type complex
+    Ctl* ctl;
+    int nsteps;
+    int CB;                          // spectrum columns per phase-B item
+    double spy;
+    double norm_scale;               // 1 / (nx*ny*1.) as the reference normalises
+    unsigned long long* trace;       // optional: %globaltimer at phase boundaries of the first step
+
+    template <typename T> __device__ __forceinline__ const T* q0_T() const { return (const T*)q0; }
+    template <typename T> __device__ __forceinline__ const T* D_T() const { return (const T*)D; }
+    template <typename T> __device__ __forceinline__ const T* inv2eta_T() const { return (const T*)inv2eta; }
+    template <typename T> __device__ __forceinline__ const T* mA_T() const { return (const T*)mA; }
+    template <typename T> __device__ __forceinline__ const T* mB_T() const { return (const T*)mB; }
+};
+
+// Grid size (co-resident blocks), phase-B column count and dynamic shared
+// memory of the engine for this transform plan; 0 if it cannot run.
+template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem);
+template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, size_t smem, cudaStream_t s);
+void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s);
+
+}  // namespace fi

@@ -167,6 +167,10 @@ long long fi_launch_count(const fi_handle* h);
  * 7 rk_stage, 8 rk_final, 9 upd_begin, 10 upd_masks, 11 upd_litho,
  * 12 upd_load, 13 upd_end. */
 int fi_profile(fi_handle* h, int enable);
+/* Step-engine phase timestamps (%globaltimer, ns) of the first RK4 step of
+ * the last update: the first call enables tracing, later calls copy up to n
+ * timestamps into `out`. */
+int fi_engine_trace(fi_handle* h, unsigned long long* out, int n);
 int fi_profile_read(fi_handle* h, double* ms, long long* counts, int n);
 
 const char* fi_last_error(const fi_handle* h);

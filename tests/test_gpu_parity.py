@@ -216,3 +216,21 @@ def test_graph_replay_matches_eager(precision, monkeypatch):
         p.close()
     for a, b in zip(*out):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision,n", [(0, 64), (0, 128), (1, 128), (1, 256)])
+def test_step_engine_matches_kernel_sequence(precision, n, monkeypatch):
+    """The cooperative RK4 step engine against the one-kernel-per-pass path:
+    FP64 to rounding, mixed within the mixed-form bound."""
+    wl = W.config2(n=n, L=3000e3 * n / 256, dt=1.0, stage_mode=1)
+    res = []
+    for no_engine in ("1", "0"):
+        monkeypatch.setenv("FI_NO_ENGINE", no_engine)
+        p = Pair(wl, precision=precision)
+        p.init()
+        p.step(5)
+        res.append(p.dom.field("w"))
+        if no_engine == "0" and precision == 0:
+            compare(p, TOL64)
+        p.close()
+    assert rel(res[1], res[0]) <= (1e-12 if precision == 0 else 1e-6)
