@@ -42,13 +42,20 @@ constexpr int RC = 2;   // rows per phase-C item
 // stage coefficients of RK4: y_s = x + a_s h k_{s-1}
 __constant__ double c_rk4_a[4] = {0.0, 0.5, 0.5, 1.0};
 
+// Shared-memory plan of phase A, in rows of nx field values (T):
+//   R1 (18 rows): prefetched state rows, later Wx (6) + Mxx, Myy, Mxy (4 each)
+//   R2 (17 rows): dX (6), dY (5), load term P (2), Mxyx (4)
+//   R3 (10 rows): D (4), q0 (2), 1/(2 eta) (2), w_ref (2; hi/lo halves in the mixed form)
+//   mask (2 rows of bytes), FFT ping-pong buffers (2 x RA rows of complex half-rows)
+constexpr int A_R1 = 18, A_R2 = 17, A_R3 = 10;
 template <typename T> struct PhaseAMem {
-    // level-0 differences on RA+4 rows, moments on RA+2 rows, all full width
     static size_t bytes(int nx, int h)
     {
         typedef typename vec2<T>::type C2;
-        const size_t rows = (RA + 4) + (RA + 3) + (RA + 4) + 4 * (RA + 2);
-        return rows * (size_t)nx * sizeof(T) + 2 * (size_t)RA * h * sizeof(C2);
+        size_t b = (size_t)(A_R1 + A_R2 + A_R3) * nx * sizeof(T);
+        b += ((size_t)2 * nx + 15) / 16 * 16;
+        b += 2 * (size_t)RA * h * sizeof(C2);
+        return b;
     }
 };
 
@@ -68,23 +75,69 @@ template <typename T> __device__ __forceinline__ double corner_mean_dev(const T*
 }
 
 // ---------------------------------------------------------------------------
-// Phase A: one item = output rows j0, j0+1 (full width).
+// Phase A: one item = output rows j0, j0+1 (full width).  Every global row the
+// item needs is first copied into shared memory with vector loads (all in
+// flight together); the stencil then runs from shared memory only.
 // ---------------------------------------------------------------------------
+template <typename V, typename T>
+__device__ __forceinline__ void rows_to_smem(T* dst, const T* __restrict__ src, int nrows, int gj0, int nx, int ny)
+{
+    // nrows rows starting at global row gj0 (zeros outside the domain); V is
+    // a 16-byte vector of T
+    constexpr int W = sizeof(V) / sizeof(T);
+    const int nv = nx / W;
+    const int tot = nrows * nv;
+    V* d = reinterpret_cast<V*>(dst);
+    for (int e0 = threadIdx.x; e0 < tot; e0 += 4 * blockDim.x) {
+        V v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int e = e0 + u * blockDim.x;
+            if (e < tot) {
+                const int r = e / nv, c = e - r * nv;
+                const int gj = gj0 + r;
+                if (gj >= 0 && gj < ny) v[u] = __ldg(reinterpret_cast<const V*>(src + (size_t)gj * nx) + c);
+                else v[u] = V{};
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int e = e0 + u * blockDim.x;
+            if (e < tot) d[e] = v[u];
+        }
+    }
+}
+
 template <typename T>
 __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsigned char* smem)
 {
     typedef typename vec2<T>::type C2;
+    typedef typename std::conditional<std::is_same<T, float>::value, float4, double2>::type V;
     const int nx = g.p.nx, ny = g.p.ny, hh = g.p.h;
     const int tid = threadIdx.x, nt = blockDim.x;
-    T* dX = reinterpret_cast<T*>(smem);
-    T* dY = dX + (size_t)(RA + 4) * nx;
-    T* Wx = dY + (size_t)(RA + 3) * nx;
-    T* Mxx = Wx + (size_t)(RA + 4) * nx;
-    T* Myy = Mxx + (size_t)(RA + 2) * nx;
-    T* Mxy = Myy + (size_t)(RA + 2) * nx;
-    T* Mxyx = Mxy + (size_t)(RA + 2) * nx;
-    C2* b0 = reinterpret_cast<C2*>(Mxyx + (size_t)(RA + 2) * nx);
+    T* R1 = reinterpret_cast<T*>(smem);
+    T* R2 = R1 + (size_t)A_R1 * nx;
+    T* R3 = R2 + (size_t)A_R2 * nx;
+    uint8_t* MK = reinterpret_cast<uint8_t*>(R3 + (size_t)A_R3 * nx);
+    C2* b0 = reinterpret_cast<C2*>(MK + ((size_t)2 * nx + 15) / 16 * 16);
     C2* b1 = b0 + (size_t)RA * hh;
+    // R1 roles
+    T* XA = R1;                    // 6 rows: xhi (mixed) | x (plain)
+    T* XB = R1 + 6 * (size_t)nx;   // 6 rows: xlo (mixed) | raw_prev (plain)
+    T* XC = R1 + 12 * (size_t)nx;  // 6 rows: raw_prev (mixed) | y (plain)
+    T* Wx = R1;                    // 6 rows   (after level 0)
+    T* Mxx = R1 + 6 * (size_t)nx;  // 4 rows
+    T* Myy = R1 + 10 * (size_t)nx; // 4 rows
+    T* Mxy = R1 + 14 * (size_t)nx; // 4 rows
+    // R2 roles
+    T* dX = R2;
+    T* dY = R2 + 6 * (size_t)nx;
+    T* P = R2 + 11 * (size_t)nx;
+    T* Mxyx = R2 + 13 * (size_t)nx;
+    // R3 roles
+    T* Dr = R3;
+    T* Q0 = R3 + 4 * (size_t)nx;
+    T* I2E = R3 + 6 * (size_t)nx;
 
     const T* rprev = stage > 0 ? (const T*)g.raw[stage - 1] : nullptr;
     __shared__ double s_sc[2];
@@ -93,43 +146,80 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         s_sc[0] = stage > 0 ? c_rk4_a[stage] * h * g.spy : 0.0;
         s_sc[1] = stage > 0 ? corner_mean_of(rprev, nx, ny) : 0.0;
     }
+    // ---- prefetch
+    if constexpr (std::is_same<T, float>::value) {
+        rows_to_smem<V, T>(XA, g.xhi, 6, j0 - 2, nx, ny);
+        rows_to_smem<V, T>(XB, g.xlo, 6, j0 - 2, nx, ny);
+        if (rprev) rows_to_smem<V, T>(XC, rprev, 6, j0 - 2, nx, ny);
+    } else {
+        rows_to_smem<V, T>(XA, g.x, 6, j0 - 2, nx, ny);
+        if (rprev) rows_to_smem<V, T>(XB, rprev, 6, j0 - 2, nx, ny);
+    }
+    rows_to_smem<V, T>(Dr, g.D_T<T>(), 4, j0 - 1, nx, ny);
+    rows_to_smem<V, T>(Q0, g.q0_T<T>(), 2, j0, nx, ny);
+    rows_to_smem<V, T>(I2E, g.inv2eta_T<T>(), 2, j0, nx, ny);
+    for (int e = tid; e < 2 * nx; e += nt) {
+        const int o = e / nx, i = e - o * nx;
+        MK[e] = (j0 + o < ny) ? g.mask[(size_t)(j0 + o) * nx + i] : 0;
+    }
     __syncthreads();
     const double sd = s_sc[0], cmd = s_sc[1];
-
-    // level 0: forward differences along x (dX) and y (dY)
-    for (int e = tid; e < (RA + 4) * nx; e += nt) {
+    // plain form: materialise the stage state y = x + s (raw - cm) in double
+    if constexpr (!std::is_same<T, float>::value) {
+        for (int e = tid; e < 6 * nx; e += nt) {
+            double v = XA[e];
+            if (rprev) v += sd * ((double)XB[e] - cmd);
+            XC[e] = v;
+        }
+        __syncthreads();
+    }
+    // ---- level 0: forward differences and the load term
+    const float sf = (float)sd;
+    for (int e = tid; e < 6 * nx; e += nt) {
         const int r = e / nx, i = e - r * nx;
         const int gj = j0 - 2 + r;
         if (gj < 0 || gj >= ny) continue;
-        const size_t c0 = (size_t)gj * nx + i;
         if (i < nx - 1) {
             if constexpr (std::is_same<T, float>::value) {
-                float v = (g.xhi[c0 + 1] - g.xhi[c0]) + (g.xlo[c0 + 1] - g.xlo[c0]);
-                if (rprev) v += (float)sd * (rprev[c0 + 1] - rprev[c0]);
-                dX[(size_t)r * nx + i] = v;
+                float v = (XA[e + 1] - XA[e]) + (XB[e + 1] - XB[e]);
+                if (rprev) v += sf * (XC[e + 1] - XC[e]);
+                dX[e] = v;
             } else {
-                double y1 = g.x[c0 + 1], y0 = g.x[c0];
-                if (rprev) { y1 += sd * ((double)rprev[c0 + 1] - cmd); y0 += sd * ((double)rprev[c0] - cmd); }
-                dX[(size_t)r * nx + i] = y1 - y0;
+                dX[e] = XC[e + 1] - XC[e];
             }
         }
-        if (r < RA + 3 && gj + 1 < ny) {
-            const size_t c1 = c0 + nx;
+        if (r < 5 && gj + 1 < ny) {
             if constexpr (std::is_same<T, float>::value) {
-                float v = (g.xhi[c1] - g.xhi[c0]) + (g.xlo[c1] - g.xlo[c0]);
-                if (rprev) v += (float)sd * (rprev[c1] - rprev[c0]);
-                dY[(size_t)r * nx + i] = v;
+                float v = (XA[e + nx] - XA[e]) + (XB[e + nx] - XB[e]);
+                if (rprev) v += sf * (XC[e + nx] - XC[e]);
+                dY[e] = v;
             } else {
-                double y1 = g.x[c1], y0 = g.x[c0];
-                if (rprev) { y1 += sd * ((double)rprev[c1] - cmd); y0 += sd * ((double)rprev[c0] - cmd); }
-                dY[(size_t)r * nx + i] = y1 - y0;
+                dY[e] = XC[e + nx] - XC[e];
             }
         }
+    }
+    for (int e = tid; e < 2 * nx; e += nt) {
+        const int o = e / nx, i = e - o * nx;
+        const int gj = j0 + o;
+        T p = (T)0;
+        if (gj < ny && MK[e]) {
+            const size_t c = (size_t)gj * nx + i;
+            const int eo = (o + 2) * nx + i;   // row of the output cell in the 6-row prefetch
+            // q0 + (-g rho_m) (y - w_ref) at the stage state
+            if constexpr (std::is_same<T, float>::value) {
+                float dy = (XA[eo] - g.wrefhi[c]) + (XB[eo] - g.wreflo[c]);
+                if (rprev) dy += sf * (XC[eo] - (float)cmd);
+                p = Q0[e] + (float)g.fc.coef_mantle * dy;
+            } else {
+                p = Q0[e] + g.fc.coef_mantle * (XC[eo] - g.wref[c]);
+            }
+        }
+        P[e] = p;
     }
     __syncthreads();
     const T inv_dx = (T)g.fc.inv_dx, inv_2dx = (T)g.fc.inv_2dx, inv_dx2 = (T)g.fc.inv_dx2;
     const T inv_dy = (T)g.fc.inv_dy, inv_2dy = (T)g.fc.inv_2dy, inv_dy2 = (T)g.fc.inv_dy2;
-    for (int e = tid; e < (RA + 4) * nx; e += nt) {
+    for (int e = tid; e < 6 * nx; e += nt) {
         const int r = e / nx, i = e - r * nx;
         const int gj = j0 - 2 + r;
         if (gj < 0 || gj >= ny) continue;
@@ -138,16 +228,17 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         if (i == 0) v = d[0] * inv_dx;
         else if (i == nx - 1) v = d[nx - 2] * inv_dx;
         else v = (d[i] + d[i - 1]) * inv_2dx;
-        Wx[(size_t)r * nx + i] = v;
+        Wx[e] = v;
     }
     __syncthreads();
+    // ---- level 1: moments on rows j0-1 .. j0+2 (prefetch rows 1..4)
     const T nu = (T)g.fc.nu, omn = (T)g.fc.one_minus_nu;
-    for (int e = tid; e < (RA + 2) * nx; e += nt) {
+    for (int e = tid; e < 4 * nx; e += nt) {
         const int m = e / nx, i = e - m * nx;
         const int r = m + 1;
         const int gj = j0 - 2 + r;
         if (gj < 0 || gj >= ny) continue;
-        const size_t ri = (size_t)r * nx + i;
+        const int ri = r * nx + i;
         T wxy, wxx, wyy;
         if (gj == 0) wxy = (Wx[ri + nx] - Wx[ri]) * inv_dy;
         else if (gj == ny - 1) wxy = (Wx[ri] - Wx[ri - nx]) * inv_dy;
@@ -159,14 +250,13 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         if (gj == 0) wyy = (dY[ri + nx] - dY[ri]) * inv_dy2;
         else if (gj == ny - 1) wyy = (dY[ri - nx] - dY[ri - 2 * nx]) * inv_dy2;
         else wyy = (dY[ri] - dY[ri - nx]) * inv_dy2;
-        const T Dl = g.D_T<T>()[(size_t)gj * nx + i];
-        const size_t mi = (size_t)m * nx + i;
-        Mxx[mi] = -Dl * (wxx + nu * wyy);
-        Myy[mi] = -Dl * (wyy + nu * wxx);
-        Mxy[mi] = (-Dl * omn) * wxy;
+        const T Dl = Dr[e];
+        Mxx[e] = -Dl * (wxx + nu * wyy);
+        Myy[e] = -Dl * (wyy + nu * wxx);
+        Mxy[e] = (-Dl * omn) * wxy;
     }
     __syncthreads();
-    for (int e = tid; e < (RA + 2) * nx; e += nt) {
+    for (int e = tid; e < 4 * nx; e += nt) {
         const int m = e / nx, i = e - m * nx;
         const int gj = j0 - 1 + m;
         if (gj < 0 || gj >= ny) continue;
@@ -175,48 +265,30 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         if (i == 0) v = (M[1] - M[0]) * inv_dx;
         else if (i == nx - 1) v = (M[nx - 1] - M[nx - 2]) * inv_dx;
         else v = (M[i + 1] - M[i - 1]) * inv_2dx;
-        Mxyx[(size_t)m * nx + i] = v;
+        Mxyx[e] = v;
     }
     __syncthreads();
-    const T* q0 = g.q0_T<T>();
-    const T* i2e = g.inv2eta_T<T>();
-    for (int e = tid; e < RA * nx; e += nt) {
+    // ---- level 2 on the two output rows -> packed into the FFT buffer
+    for (int e = tid; e < 2 * nx; e += nt) {
         const int o = e / nx, i = e - o * nx;
         const int gj = j0 + o;
         T fv = (T)0;
         if (gj < ny) {
-            const int m = o + 1;
-            const size_t mi = (size_t)m * nx + i;
+            const int mi = (o + 1) * nx + i;
             T mxy_xy, mx_xx, my_yy;
             if (gj == 0) mxy_xy = (Mxyx[mi + nx] - Mxyx[mi]) * inv_dy;
             else if (gj == ny - 1) mxy_xy = (Mxyx[mi] - Mxyx[mi - nx]) * inv_dy;
             else mxy_xy = (Mxyx[mi + nx] - Mxyx[mi - nx]) * inv_2dy;
-            const T* M = Mxx + (size_t)m * nx;
+            const T* M = Mxx + (size_t)(o + 1) * nx;
             if (i == 0) mx_xx = ((M[2] - (T)2 * M[1]) + M[0]) * inv_dx2;
             else if (i == nx - 1) mx_xx = ((M[nx - 1] - (T)2 * M[nx - 2]) + M[nx - 3]) * inv_dx2;
             else mx_xx = ((M[i + 1] - (T)2 * M[i]) + M[i - 1]) * inv_dx2;
             if (gj == 0) my_yy = ((Myy[mi + 2 * nx] - (T)2 * Myy[mi + nx]) + Myy[mi]) * inv_dy2;
             else if (gj == ny - 1) my_yy = ((Myy[mi] - (T)2 * Myy[mi - nx]) + Myy[mi - 2 * nx]) * inv_dy2;
             else my_yy = ((Myy[mi + nx] - (T)2 * Myy[mi]) + Myy[mi - nx]) * inv_dy2;
-            const size_t c = (size_t)gj * nx + i;
-            T p = (T)0;
-            if (g.mask[c]) {
-                // q0 + (-g rho_m) (y - w_ref) with y the stage state
-                if constexpr (std::is_same<T, float>::value) {
-                    float dy = (g.xhi[c] - g.wrefhi[c]) + (g.xlo[c] - g.wreflo[c]);
-                    if (rprev) dy += (float)sd * (rprev[c] - (float)cmd);
-                    p = q0[c] + (float)g.fc.coef_mantle * dy;
-                } else {
-                    double y = g.x[c];
-                    if (rprev) y += sd * ((double)rprev[c] - cmd);
-                    p = (double)q0[c] + g.fc.coef_mantle * (y - g.wref[c]);
-                }
-            }
-            fv = (((p + mx_xx) + (T)2 * mxy_xy) + my_yy) * i2e[c];
+            fv = (((P[e] + mx_xx) + (T)2 * mxy_xy) + my_yy) * I2E[e];
         }
-        // pack the real row as complex pairs for the half-length FFT
-        T* bz = reinterpret_cast<T*>(b0 + (size_t)o * hh);
-        bz[i] = fv;
+        reinterpret_cast<T*>(b0)[e] = fv;   // row o at b0 + o*hh complex = o*nx reals
     }
     __syncthreads();
     C2* r = block_fft<T>(b0, b1, g.p.row.d, RA, hh, etw<T>(g.p.row), -1);
@@ -251,10 +323,20 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
     C2* b1 = b0 + (size_t)CB * ny;
     C2* S = (C2*)g.S;
     const int tid = threadIdx.x, nt = blockDim.x;
-    for (int e = tid; e < CB * ny; e += nt) {
-        const int c = e % CB, l = e / CB;
-        const int k = k0 + c;
-        b0[c * ny + l] = (k <= g.p.h) ? S[(size_t)l * g.p.sp + k] : mk2<T>((T)0, (T)0);
+    for (int e0 = tid; e0 < CB * ny; e0 += 4 * nt) {
+        C2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int e = e0 + u * nt;
+            const int c = e % CB, l = e / CB;
+            const int k = k0 + c;
+            v[u] = (e < CB * ny && k <= g.p.h) ? S[(size_t)l * g.p.sp + k] : mk2<T>((T)0, (T)0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int e = e0 + u * nt;
+            if (e < CB * ny) b0[(e % CB) * ny + e / CB] = v[u];
+        }
     }
     __syncthreads();
     C2* r = block_fft<T>(b0, b1, g.p.col.d, CB, ny, etw<T>(g.p.col), -1);
@@ -352,8 +434,9 @@ __device__ __forceinline__ unsigned long long gtimer()
     return t;
 }
 
+// mixed form: two blocks per SM (shared memory allows it), so <= 128 registers
 template <typename T>
-__global__ void __launch_bounds__(256) k_engine_rk4(EngineArgs g)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_engine_rk4(EngineArgs g)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     cg::grid_group grid = cg::this_grid();
@@ -407,6 +490,7 @@ __global__ void __launch_bounds__(256) k_engine_rk4(EngineArgs g)
         const T* r2 = (const T*)g.raw[1];
         const T* r3 = (const T*)g.raw[2];
         const T* r4 = (const T*)g.raw[3];
+#pragma unroll 4
         for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
             if constexpr (std::is_same<T, float>::value) {
                 const float k = ((((float)r1[e] - (float)s_c[1]) + 2.f * ((float)r2[e] - (float)s_c[2])) +
@@ -458,6 +542,7 @@ void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s)
 template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem)
 {
     typedef typename vec2<T>::type C2;
+    if (p.nx % 4 != 0) return 0;   // 16-byte row vectors in the phase-A prefetch
     int cb = (int)(16 / sizeof(C2));
     if (cb < 1) cb = 1;
     *CB = cb;
