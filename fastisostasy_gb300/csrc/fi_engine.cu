@@ -20,6 +20,7 @@
 #include <cooperative_groups.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <type_traits>
 
 #include "fi_engine.h"
@@ -79,11 +80,13 @@ template <typename T> __device__ __forceinline__ double corner_mean_dev(const T*
 // item needs is first copied into shared memory with vector loads (all in
 // flight together); the stencil then runs from shared memory only.
 // ---------------------------------------------------------------------------
-template <typename V, typename T>
+template <typename V, bool RO, typename T>
 __device__ __forceinline__ void rows_to_smem(T* dst, const T* __restrict__ src, int nrows, int gj0, int nx, int ny)
 {
     // nrows rows starting at global row gj0 (zeros outside the domain); V is
-    // a 16-byte vector of T
+    // a 16-byte vector of T.  RO: the source is read-only for the whole
+    // kernel (non-coherent cache path allowed); data written by other blocks
+    // during the kernel is read with coherent loads.
     constexpr int W = sizeof(V) / sizeof(T);
     const int nv = nx / W;
     const int tot = nrows * nv;
@@ -96,7 +99,10 @@ __device__ __forceinline__ void rows_to_smem(T* dst, const T* __restrict__ src, 
             if (e < tot) {
                 const int r = e / nv, c = e - r * nv;
                 const int gj = gj0 + r;
-                if (gj >= 0 && gj < ny) v[u] = __ldg(reinterpret_cast<const V*>(src + (size_t)gj * nx) + c);
+                if (gj >= 0 && gj < ny) {
+                    const V* ps = reinterpret_cast<const V*>(src + (size_t)gj * nx) + c;
+                    v[u] = RO ? __ldg(ps) : *ps;
+                }
                 else v[u] = V{};
             }
         }
@@ -148,16 +154,16 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
     }
     // ---- prefetch
     if constexpr (std::is_same<T, float>::value) {
-        rows_to_smem<V, T>(XA, g.xhi, 6, j0 - 2, nx, ny);
-        rows_to_smem<V, T>(XB, g.xlo, 6, j0 - 2, nx, ny);
-        if (rprev) rows_to_smem<V, T>(XC, rprev, 6, j0 - 2, nx, ny);
+        rows_to_smem<V, false>(XA, g.xhi, 6, j0 - 2, nx, ny);
+        rows_to_smem<V, false>(XB, g.xlo, 6, j0 - 2, nx, ny);
+        if (rprev) rows_to_smem<V, false>(XC, rprev, 6, j0 - 2, nx, ny);
     } else {
-        rows_to_smem<V, T>(XA, g.x, 6, j0 - 2, nx, ny);
-        if (rprev) rows_to_smem<V, T>(XB, rprev, 6, j0 - 2, nx, ny);
+        rows_to_smem<V, false>(XA, g.x, 6, j0 - 2, nx, ny);
+        if (rprev) rows_to_smem<V, false>(XB, rprev, 6, j0 - 2, nx, ny);
     }
-    rows_to_smem<V, T>(Dr, g.D_T<T>(), 4, j0 - 1, nx, ny);
-    rows_to_smem<V, T>(Q0, g.q0_T<T>(), 2, j0, nx, ny);
-    rows_to_smem<V, T>(I2E, g.inv2eta_T<T>(), 2, j0, nx, ny);
+    rows_to_smem<V, true>(Dr, g.D_T<T>(), 4, j0 - 1, nx, ny);
+    rows_to_smem<V, true>(Q0, g.q0_T<T>(), 2, j0, nx, ny);
+    rows_to_smem<V, true>(I2E, g.inv2eta_T<T>(), 2, j0, nx, ny);
     for (int e = tid; e < 2 * nx; e += nt) {
         const int o = e / nx, i = e - o * nx;
         MK[e] = (j0 + o < ny) ? g.mask[(size_t)(j0 + o) * nx + i] : 0;
@@ -434,9 +440,9 @@ __device__ __forceinline__ unsigned long long gtimer()
     return t;
 }
 
-// mixed form: two blocks per SM (shared memory allows it), so <= 128 registers
-template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_engine_rk4(EngineArgs g)
+// MINB blocks per SM: 2 caps the registers at 128 per thread
+template <typename T, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_engine_rk4(EngineArgs g)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     cg::grid_group grid = cg::this_grid();
@@ -539,6 +545,12 @@ void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s)
     k_split<<<b, 256, 0, s>>>(x, hi, lo, n);
 }
 
+static int engine_bps()
+{
+    const char* e = getenv("FI_ENGINE_BPS");
+    return (e && e[0] == '2') ? 2 : 1;
+}
+
 template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem)
 {
     typedef typename vec2<T>::type C2;
@@ -552,12 +564,15 @@ template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, siz
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (*smem > (size_t)optin) return 0;
-    if (cudaFuncSetAttribute(k_engine_rk4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess)
-        return 0;
+    const int bps = engine_bps();
+    cudaError_t e1 = bps == 2 ? cudaFuncSetAttribute(k_engine_rk4<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem)
+                              : cudaFuncSetAttribute(k_engine_rk4<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+    if (e1 != cudaSuccess) return 0;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T>, 256, *smem) != cudaSuccess || per_sm < 1)
-        return 0;
-    if (per_sm > 2) per_sm = 2;
+    cudaError_t e2 = bps == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T, 2>, 256, *smem)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T, 1>, 256, *smem);
+    if (e2 != cudaSuccess || per_sm < 1) return 0;
+    if (per_sm > bps) per_sm = bps;
     *grid = per_sm * nsm;
     return 1;
 }
@@ -574,7 +589,8 @@ template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, s
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_engine_rk4<T>, g);
+    if (engine_bps() == 2) return cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 2>, g);
+    return cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 1>, g);
 }
 
 template size_t engine_smem_bytes<float>(const Plan2D&, int);
