@@ -616,6 +616,7 @@ template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
     g.mask = h->d.mactive;
     for (int i = 0; i < 4; ++i) g.raw[i] = h->raw[i];
     g.S = h->S;
+    g.f = h->f;
     g.ctl = h->ctl;
     g.nsteps = nsteps;
     g.CB = h->eng_CB;

@@ -5,12 +5,13 @@
 // calc_lvelva, src/lv_elva.f90:31-126, at every stage state).  The grid
 // walks through phases separated by grid-wide barriers:
 //
-//   A  stencil + row real-FFT   (work item = 2 grid rows, full width)
-//   B  column FFT, multiply by 1/(kappa R) in the Hartley basis, inverse
-//   C  inverse row real-FFT -> raw_s (stage output before corner BC / sec_per_year)
+//   S  flexure stencil on 64 x 16 tiles -> f
+//   R  forward row real-FFT, one warp per row -> half spectrum
+//   C  column FFT, multiply by 1/(kappa R) in the Hartley basis, inverse (one warp per column)
+//   I  inverse row real-FFT, one warp per row -> raw_s (stage output before corner BC / sec_per_year)
 //   D  x += h/6 (k1 + 2 k2 + 2 k3 + k4), w = x
 //
-// Stage states y_s = x + a_s h k_{s-1} are never stored: phase A rebuilds the
+// Stage states y_s = x + a_s h k_{s-1} are never stored: phase S rebuilds the
 // differences it needs from x and raw_{s-1} (the corner mean of raw cancels
 // in every difference and enters only the mantle term).  In the mixed form x
 // also lives as a float hi/lo pair (x = hi + lo), so the forward differences
@@ -24,7 +25,7 @@
 #include <type_traits>
 
 #include "fi_engine.h"
-#include "fi_fft.cuh"
+#include "fi_wfft.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -37,402 +38,342 @@ template <typename T> __device__ __forceinline__ const typename vec2<T>::type* e
 template <> __device__ __forceinline__ const double2* ertw<double>(const Plan2D& p) { return p.rtw64; }
 template <> __device__ __forceinline__ const float2* ertw<float>(const Plan2D& p) { return p.rtw32; }
 
-constexpr int RA = 2;   // rows per phase-A item (must be even: see the y-boundary stencils)
-constexpr int RC = 2;   // rows per phase-C item
-
 // stage coefficients of RK4: y_s = x + a_s h k_{s-1}
 __constant__ double c_rk4_a[4] = {0.0, 0.5, 0.5, 1.0};
 
-// Shared-memory plan of phase A, in rows of nx field values (T):
-//   R1 (18 rows): prefetched state rows, later Wx (6) + Mxx, Myy, Mxy (4 each)
-//   R2 (17 rows): dX (6), dY (5), load term P (2), Mxyx (4)
-//   R3 (10 rows): D (4), q0 (2), 1/(2 eta) (2), w_ref (2; hi/lo halves in the mixed form)
-//   mask (2 rows of bytes), FFT ping-pong buffers (2 x RA rows of complex half-rows)
-constexpr int A_R1 = 18, A_R2 = 17, A_R3 = 10;
-template <typename T> struct PhaseAMem {
-    static size_t bytes(int nx, int h)
-    {
-        typedef typename vec2<T>::type C2;
-        size_t b = (size_t)(A_R1 + A_R2 + A_R3) * nx * sizeof(T);
-        b += ((size_t)2 * nx + 15) / 16 * 16;
-        b += 2 * (size_t)RA * h * sizeof(C2);
-        return b;
-    }
-};
+// ---------------------------------------------------------------------------
+// Stencil tiles: SX x SY outputs per item, halo 2; 256 threads as 64 x 4, each
+// thread owning one column and four output rows.
+// ---------------------------------------------------------------------------
+constexpr int SX = 64, SY = 16, SRX = SX + 4, SRY = SY + 4, SREG = SRX * SRY;
+constexpr int ENGINE_THREADS = 256, ENGINE_WARPS = ENGINE_THREADS / 32;
 
-template <typename T> size_t engine_smem_bytes(const Plan2D& p, int CB)
+template <typename T> size_t engine_smem_bytes(const Plan2D& p, int)
 {
     typedef typename vec2<T>::type C2;
-    size_t a = PhaseAMem<T>::bytes(p.nx, p.h);
-    size_t b = 2 * (size_t)CB * p.ny * sizeof(C2);
-    size_t c = 2 * (size_t)RC * p.h * sizeof(C2);
-    size_t m = a > b ? a : b;
-    return (m > c ? m : c) + 64;
-}
-
-template <typename T> __device__ __forceinline__ double corner_mean_dev(const T* a, int nx, int ny)
-{
-    return corner_mean_of(a, nx, ny);
-}
-
-// ---------------------------------------------------------------------------
-// Phase A: one item = output rows j0, j0+1 (full width).  Every global row the
-// item needs is first copied into shared memory with vector loads (all in
-// flight together); the stencil then runs from shared memory only.
-// ---------------------------------------------------------------------------
-template <typename V, bool RO, typename T>
-__device__ __forceinline__ void rows_to_smem(T* dst, const T* __restrict__ src, int nrows, int gj0, int nx, int ny)
-{
-    // nrows rows starting at global row gj0 (zeros outside the domain); V is
-    // a 16-byte vector of T.  RO: the source is read-only for the whole
-    // kernel (non-coherent cache path allowed); data written by other blocks
-    // during the kernel is read with coherent loads.
-    constexpr int W = sizeof(V) / sizeof(T);
-    const int nv = nx / W;
-    const int tot = nrows * nv;
-    V* d = reinterpret_cast<V*>(dst);
-    for (int e0 = threadIdx.x; e0 < tot; e0 += 4 * blockDim.x) {
-        V v[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int e = e0 + u * blockDim.x;
-            if (e < tot) {
-                const int r = e / nv, c = e - r * nv;
-                const int gj = gj0 + r;
-                if (gj >= 0 && gj < ny) {
-                    const V* ps = reinterpret_cast<const V*>(src + (size_t)gj * nx) + c;
-                    v[u] = RO ? __ldg(ps) : *ps;
-                }
-                else v[u] = V{};
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int e = e0 + u * blockDim.x;
-            if (e < tot) d[e] = v[u];
-        }
-    }
+    const size_t stencil = (size_t)10 * SREG * sizeof(T);
+    const int line = p.h > p.ny ? p.h : p.ny;
+    const size_t warpbuf = (size_t)ENGINE_WARPS * line * sizeof(C2);
+    return (stencil > warpbuf ? stencil : warpbuf) + 64;
 }
 
 template <typename T>
-__device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsigned char* smem)
+__device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h, unsigned char* smem)
 {
-    typedef typename vec2<T>::type C2;
-    typedef typename std::conditional<std::is_same<T, float>::value, float4, double2>::type V;
-    const int nx = g.p.nx, ny = g.p.ny, hh = g.p.h;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    T* R1 = reinterpret_cast<T*>(smem);
-    T* R2 = R1 + (size_t)A_R1 * nx;
-    T* R3 = R2 + (size_t)A_R2 * nx;
-    uint8_t* MK = reinterpret_cast<uint8_t*>(R3 + (size_t)A_R3 * nx);
-    C2* b0 = reinterpret_cast<C2*>(MK + ((size_t)2 * nx + 15) / 16 * 16);
-    C2* b1 = b0 + (size_t)RA * hh;
-    // R1 roles
-    T* XA = R1;                    // 6 rows: xhi (mixed) | x (plain)
-    T* XB = R1 + 6 * (size_t)nx;   // 6 rows: xlo (mixed) | raw_prev (plain)
-    T* XC = R1 + 12 * (size_t)nx;  // 6 rows: raw_prev (mixed) | y (plain)
-    T* Wx = R1;                    // 6 rows   (after level 0)
-    T* Mxx = R1 + 6 * (size_t)nx;  // 4 rows
-    T* Myy = R1 + 10 * (size_t)nx; // 4 rows
-    T* Mxy = R1 + 14 * (size_t)nx; // 4 rows
-    // R2 roles
-    T* dX = R2;
-    T* dY = R2 + 6 * (size_t)nx;
-    T* P = R2 + 11 * (size_t)nx;
-    T* Mxyx = R2 + 13 * (size_t)nx;
-    // R3 roles
-    T* Dr = R3;
-    T* Q0 = R3 + 4 * (size_t)nx;
-    T* I2E = R3 + 6 * (size_t)nx;
-
+    const int nx = g.p.nx, ny = g.p.ny;
+    const int ntx = (nx + SX - 1) / SX;
+    const int i0 = (tile % ntx) * SX - 2, j0 = (tile / ntx) * SY - 2;   // global index of local (0, 0)
+    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
+    T* A0 = reinterpret_cast<T*>(smem);   // mixed: x hi | plain: x
+    T* A1 = A0 + SREG;                    // mixed: x lo | plain: raw_prev
+    T* A2 = A1 + SREG;                    // mixed: raw_prev | plain: y
+    T* dX = A2 + SREG;
+    T* dY = dX + SREG;
+    T* Wx = dY + SREG;
+    T* Mxx = Wx + SREG;
+    T* Myy = Mxx + SREG;
+    T* Mxy = Myy + SREG;
+    T* Mxyx = Mxy + SREG;
     const T* rprev = stage > 0 ? (const T*)g.raw[stage - 1] : nullptr;
     __shared__ double s_sc[2];
-    if (tid == 0) {
-        // y = x + a h spy (raw - cm): the scale s and the corner mean cm
+    __syncthreads();   // previous item's readers are done with the tile buffers
+    if (threadIdx.x == 0) {
         s_sc[0] = stage > 0 ? c_rk4_a[stage] * h * g.spy : 0.0;
         s_sc[1] = stage > 0 ? corner_mean_of(rprev, nx, ny) : 0.0;
     }
-    // ---- prefetch
-    if constexpr (std::is_same<T, float>::value) {
-        rows_to_smem<V, false>(XA, g.xhi, 6, j0 - 2, nx, ny);
-        rows_to_smem<V, false>(XB, g.xlo, 6, j0 - 2, nx, ny);
-        if (rprev) rows_to_smem<V, false>(XC, rprev, 6, j0 - 2, nx, ny);
-    } else {
-        rows_to_smem<V, false>(XA, g.x, 6, j0 - 2, nx, ny);
-        if (rprev) rows_to_smem<V, false>(XB, rprev, 6, j0 - 2, nx, ny);
-    }
-    rows_to_smem<V, true>(Dr, g.D_T<T>(), 4, j0 - 1, nx, ny);
-    rows_to_smem<V, true>(Q0, g.q0_T<T>(), 2, j0, nx, ny);
-    rows_to_smem<V, true>(I2E, g.inv2eta_T<T>(), 2, j0, nx, ny);
-    for (int e = tid; e < 2 * nx; e += nt) {
-        const int o = e / nx, i = e - o * nx;
-        MK[e] = (j0 + o < ny) ? g.mask[(size_t)(j0 + o) * nx + i] : 0;
-    }
+    for (int ly = ty; ly < SRY; ly += 4)
+        for (int lx = tx; lx < SRX; lx += 64) {
+            const int gi = i0 + lx, gj = j0 + ly;
+            const int l = ly * SRX + lx;
+            if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) {
+                const size_t c = (size_t)gj * nx + gi;
+                if constexpr (std::is_same<T, float>::value) {
+                    A0[l] = g.xhi[c];
+                    A1[l] = g.xlo[c];
+                    A2[l] = rprev ? rprev[c] : 0.f;
+                } else {
+                    A0[l] = g.x[c];
+                    A1[l] = rprev ? rprev[c] : 0.0;
+                }
+            } else {
+                A0[l] = (T)0;
+                A1[l] = (T)0;
+                A2[l] = (T)0;
+            }
+        }
     __syncthreads();
     const double sd = s_sc[0], cmd = s_sc[1];
-    // plain form: materialise the stage state y = x + s (raw - cm) in double
+    const float sf = (float)sd;
     if constexpr (!std::is_same<T, float>::value) {
-        for (int e = tid; e < 6 * nx; e += nt) {
-            double v = XA[e];
-            if (rprev) v += sd * ((double)XB[e] - cmd);
-            XC[e] = v;
-        }
+        // plain form: the stage state y = x + s (raw - cm) in double
+        for (int e = threadIdx.x; e < SREG; e += ENGINE_THREADS) A2[e] = rprev ? A0[e] + sd * (A1[e] - cmd) : A0[e];
         __syncthreads();
     }
-    // ---- level 0: forward differences and the load term
-    const float sf = (float)sd;
-    for (int e = tid; e < 6 * nx; e += nt) {
-        const int r = e / nx, i = e - r * nx;
-        const int gj = j0 - 2 + r;
-        if (gj < 0 || gj >= ny) continue;
-        if (i < nx - 1) {
-            if constexpr (std::is_same<T, float>::value) {
-                float v = (XA[e + 1] - XA[e]) + (XB[e + 1] - XB[e]);
-                if (rprev) v += sf * (XC[e + 1] - XC[e]);
-                dX[e] = v;
-            } else {
-                dX[e] = XC[e + 1] - XC[e];
+    for (int ly = ty; ly < SRY; ly += 4)
+        for (int lx = tx; lx < SRX; lx += 64) {
+            const int l = ly * SRX + lx;
+            if (lx < SRX - 1) {
+                if constexpr (std::is_same<T, float>::value)
+                    dX[l] = (A0[l + 1] - A0[l]) + (A1[l + 1] - A1[l]) + sf * (A2[l + 1] - A2[l]);
+                else
+                    dX[l] = A2[l + 1] - A2[l];
+            }
+            if (ly < SRY - 1) {
+                if constexpr (std::is_same<T, float>::value)
+                    dY[l] = (A0[l + SRX] - A0[l]) + (A1[l + SRX] - A1[l]) + sf * (A2[l + SRX] - A2[l]);
+                else
+                    dY[l] = A2[l + SRX] - A2[l];
             }
         }
-        if (r < 5 && gj + 1 < ny) {
-            if constexpr (std::is_same<T, float>::value) {
-                float v = (XA[e + nx] - XA[e]) + (XB[e + nx] - XB[e]);
-                if (rprev) v += sf * (XC[e + nx] - XC[e]);
-                dY[e] = v;
-            } else {
-                dY[e] = XC[e + nx] - XC[e];
-            }
-        }
-    }
-    for (int e = tid; e < 2 * nx; e += nt) {
-        const int o = e / nx, i = e - o * nx;
-        const int gj = j0 + o;
-        T p = (T)0;
-        if (gj < ny && MK[e]) {
-            const size_t c = (size_t)gj * nx + i;
-            const int eo = (o + 2) * nx + i;   // row of the output cell in the 6-row prefetch
-            // q0 + (-g rho_m) (y - w_ref) at the stage state
-            if constexpr (std::is_same<T, float>::value) {
-                float dy = (XA[eo] - g.wrefhi[c]) + (XB[eo] - g.wreflo[c]);
-                if (rprev) dy += sf * (XC[eo] - (float)cmd);
-                p = Q0[e] + (float)g.fc.coef_mantle * dy;
-            } else {
-                p = Q0[e] + g.fc.coef_mantle * (XC[eo] - g.wref[c]);
-            }
-        }
-        P[e] = p;
-    }
     __syncthreads();
     const T inv_dx = (T)g.fc.inv_dx, inv_2dx = (T)g.fc.inv_2dx, inv_dx2 = (T)g.fc.inv_dx2;
     const T inv_dy = (T)g.fc.inv_dy, inv_2dy = (T)g.fc.inv_2dy, inv_dy2 = (T)g.fc.inv_dy2;
-    for (int e = tid; e < 6 * nx; e += nt) {
-        const int r = e / nx, i = e - r * nx;
-        const int gj = j0 - 2 + r;
-        if (gj < 0 || gj >= ny) continue;
-        const T* d = dX + (size_t)r * nx;
-        T v;
-        if (i == 0) v = d[0] * inv_dx;
-        else if (i == nx - 1) v = d[nx - 2] * inv_dx;
-        else v = (d[i] + d[i - 1]) * inv_2dx;
-        Wx[e] = v;
-    }
-    __syncthreads();
-    // ---- level 1: moments on rows j0-1 .. j0+2 (prefetch rows 1..4)
-    const T nu = (T)g.fc.nu, omn = (T)g.fc.one_minus_nu;
-    for (int e = tid; e < 4 * nx; e += nt) {
-        const int m = e / nx, i = e - m * nx;
-        const int r = m + 1;
-        const int gj = j0 - 2 + r;
-        if (gj < 0 || gj >= ny) continue;
-        const int ri = r * nx + i;
-        T wxy, wxx, wyy;
-        if (gj == 0) wxy = (Wx[ri + nx] - Wx[ri]) * inv_dy;
-        else if (gj == ny - 1) wxy = (Wx[ri] - Wx[ri - nx]) * inv_dy;
-        else wxy = (Wx[ri + nx] - Wx[ri - nx]) * inv_2dy;
-        const T* d = dX + (size_t)r * nx;
-        if (i == 0) wxx = (d[1] - d[0]) * inv_dx2;
-        else if (i == nx - 1) wxx = (d[nx - 2] - d[nx - 3]) * inv_dx2;
-        else wxx = (d[i] - d[i - 1]) * inv_dx2;
-        if (gj == 0) wyy = (dY[ri + nx] - dY[ri]) * inv_dy2;
-        else if (gj == ny - 1) wyy = (dY[ri - nx] - dY[ri - 2 * nx]) * inv_dy2;
-        else wyy = (dY[ri] - dY[ri - nx]) * inv_dy2;
-        const T Dl = Dr[e];
-        Mxx[e] = -Dl * (wxx + nu * wyy);
-        Myy[e] = -Dl * (wyy + nu * wxx);
-        Mxy[e] = (-Dl * omn) * wxy;
-    }
-    __syncthreads();
-    for (int e = tid; e < 4 * nx; e += nt) {
-        const int m = e / nx, i = e - m * nx;
-        const int gj = j0 - 1 + m;
-        if (gj < 0 || gj >= ny) continue;
-        const T* M = Mxy + (size_t)m * nx;
-        T v;
-        if (i == 0) v = (M[1] - M[0]) * inv_dx;
-        else if (i == nx - 1) v = (M[nx - 1] - M[nx - 2]) * inv_dx;
-        else v = (M[i + 1] - M[i - 1]) * inv_2dx;
-        Mxyx[e] = v;
-    }
-    __syncthreads();
-    // ---- level 2 on the two output rows -> packed into the FFT buffer
-    for (int e = tid; e < 2 * nx; e += nt) {
-        const int o = e / nx, i = e - o * nx;
-        const int gj = j0 + o;
-        T fv = (T)0;
-        if (gj < ny) {
-            const int mi = (o + 1) * nx + i;
-            T mxy_xy, mx_xx, my_yy;
-            if (gj == 0) mxy_xy = (Mxyx[mi + nx] - Mxyx[mi]) * inv_dy;
-            else if (gj == ny - 1) mxy_xy = (Mxyx[mi] - Mxyx[mi - nx]) * inv_dy;
-            else mxy_xy = (Mxyx[mi + nx] - Mxyx[mi - nx]) * inv_2dy;
-            const T* M = Mxx + (size_t)(o + 1) * nx;
-            if (i == 0) mx_xx = ((M[2] - (T)2 * M[1]) + M[0]) * inv_dx2;
-            else if (i == nx - 1) mx_xx = ((M[nx - 1] - (T)2 * M[nx - 2]) + M[nx - 3]) * inv_dx2;
-            else mx_xx = ((M[i + 1] - (T)2 * M[i]) + M[i - 1]) * inv_dx2;
-            if (gj == 0) my_yy = ((Myy[mi + 2 * nx] - (T)2 * Myy[mi + nx]) + Myy[mi]) * inv_dy2;
-            else if (gj == ny - 1) my_yy = ((Myy[mi] - (T)2 * Myy[mi - nx]) + Myy[mi - 2 * nx]) * inv_dy2;
-            else my_yy = ((Myy[mi + nx] - (T)2 * Myy[mi]) + Myy[mi - nx]) * inv_dy2;
-            fv = (((P[e] + mx_xx) + (T)2 * mxy_xy) + my_yy) * I2E[e];
+    for (int ly = ty; ly < SRY; ly += 4)
+        for (int lx = tx + 1; lx < SRX - 1; lx += 64) {
+            const int gi = i0 + lx;
+            const int l = ly * SRX + lx;
+            T v;
+            if (gi == 0) v = dX[l] * inv_dx;
+            else if (gi == nx - 1) v = dX[l - 1] * inv_dx;
+            else v = (dX[l] + dX[l - 1]) * inv_2dx;
+            Wx[l] = v;
         }
-        reinterpret_cast<T*>(b0)[e] = fv;   // row o at b0 + o*hh complex = o*nx reals
-    }
     __syncthreads();
-    C2* r = block_fft<T>(b0, b1, g.p.row.d, RA, hh, etw<T>(g.p.row), -1);
+    const T nu = (T)g.fc.nu, omn = (T)g.fc.one_minus_nu;
+    const T* Dg = g.D_T<T>();
+    for (int ly = ty + 1; ly < SRY - 1; ly += 4)
+        for (int lx = tx + 1; lx < SRX - 1; lx += 64) {
+            const int gi = i0 + lx, gj = j0 + ly;
+            if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
+            const int l = ly * SRX + lx;
+            T wxy, wxx, wyy;
+            if (gj == 0) wxy = (Wx[l + SRX] - Wx[l]) * inv_dy;
+            else if (gj == ny - 1) wxy = (Wx[l] - Wx[l - SRX]) * inv_dy;
+            else wxy = (Wx[l + SRX] - Wx[l - SRX]) * inv_2dy;
+            if (gi == 0) wxx = (dX[l + 1] - dX[l]) * inv_dx2;
+            else if (gi == nx - 1) wxx = (dX[l - 1] - dX[l - 2]) * inv_dx2;
+            else wxx = (dX[l] - dX[l - 1]) * inv_dx2;
+            if (gj == 0) wyy = (dY[l + SRX] - dY[l]) * inv_dy2;
+            else if (gj == ny - 1) wyy = (dY[l - SRX] - dY[l - 2 * SRX]) * inv_dy2;
+            else wyy = (dY[l] - dY[l - SRX]) * inv_dy2;
+            const T Dl = __ldg(Dg + (size_t)gj * nx + gi);
+            Mxx[l] = -Dl * (wxx + nu * wyy);
+            Myy[l] = -Dl * (wyy + nu * wxx);
+            Mxy[l] = (-Dl * omn) * wxy;
+        }
+    __syncthreads();
+    for (int ly = ty + 1; ly < SRY - 1; ly += 4)
+        for (int lx = tx + 2; lx < SRX - 2; lx += 64) {
+            const int gi = i0 + lx, gj = j0 + ly;
+            if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
+            const int l = ly * SRX + lx;
+            T v;
+            if (gi == 0) v = (Mxy[l + 1] - Mxy[l]) * inv_dx;
+            else if (gi == nx - 1) v = (Mxy[l] - Mxy[l - 1]) * inv_dx;
+            else v = (Mxy[l + 1] - Mxy[l - 1]) * inv_2dx;
+            Mxyx[l] = v;
+        }
+    __syncthreads();
+    const T* q0 = g.q0_T<T>();
+    const T* i2e = g.inv2eta_T<T>();
+    T* f = (T*)g.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int lx = tx + 2, ly = ty + 2 + 4 * q;
+        const int gi = i0 + lx, gj = j0 + ly;
+        if (gi >= nx || gj >= ny) continue;
+        const int l = ly * SRX + lx;
+        T mxy_xy, mx_xx, my_yy;
+        if (gj == 0) mxy_xy = (Mxyx[l + SRX] - Mxyx[l]) * inv_dy;
+        else if (gj == ny - 1) mxy_xy = (Mxyx[l] - Mxyx[l - SRX]) * inv_dy;
+        else mxy_xy = (Mxyx[l + SRX] - Mxyx[l - SRX]) * inv_2dy;
+        if (gi == 0) mx_xx = ((Mxx[l + 2] - (T)2 * Mxx[l + 1]) + Mxx[l]) * inv_dx2;
+        else if (gi == nx - 1) mx_xx = ((Mxx[l] - (T)2 * Mxx[l - 1]) + Mxx[l - 2]) * inv_dx2;
+        else mx_xx = ((Mxx[l + 1] - (T)2 * Mxx[l]) + Mxx[l - 1]) * inv_dx2;
+        if (gj == 0) my_yy = ((Myy[l + 2 * SRX] - (T)2 * Myy[l + SRX]) + Myy[l]) * inv_dy2;
+        else if (gj == ny - 1) my_yy = ((Myy[l] - (T)2 * Myy[l - SRX]) + Myy[l - 2 * SRX]) * inv_dy2;
+        else my_yy = ((Myy[l + SRX] - (T)2 * Myy[l]) + Myy[l - SRX]) * inv_dy2;
+        const size_t c = (size_t)gj * nx + gi;
+        T p = (T)0;
+        if (g.mask[c]) {
+            // q0 + (-g rho_m) (y - w_ref) at the stage state
+            if constexpr (std::is_same<T, float>::value) {
+                float dy = (A0[l] - __ldg(g.wrefhi + c)) + (A1[l] - __ldg(g.wreflo + c));
+                if (rprev) dy += sf * (A2[l] - (float)cmd);
+                p = __ldg(q0 + c) + (float)g.fc.coef_mantle * dy;
+            } else {
+                p = __ldg(q0 + c) + g.fc.coef_mantle * (A2[l] - __ldg(g.wref + c));
+            }
+        }
+        f[c] = (((p + mx_xx) + (T)2 * mxy_xy) + my_yy) * __ldg(i2e + c);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-level transforms: one warp per row or per spectrum column.
+// ---------------------------------------------------------------------------
+// forward real FFT of row j of f -> S row j (h+1 bins)
+template <typename T, int P>
+__device__ void row_fwd_w(const EngineArgs& g, int j, typename vec2<T>::type* wb)
+{
+    typedef typename vec2<T>::type C2;
+    constexpr int hh = 32 * P;
+    const int lane = threadIdx.x & 31;
+    const C2* f2 = reinterpret_cast<const C2*>((const T*)g.f + (size_t)j * g.p.nx);
+    C2 v[P];
+#pragma unroll
+    for (int p = 0; p < P; ++p) v[p] = f2[lane + 32 * p];
+    warp_fft<T, P>(v, lane, etw<T>(g.p.row), -1);
+    const int base = P * brev5(lane);
+#pragma unroll
+    for (int k1 = 0; k1 < P; ++k1) wb[base + k1] = v[k1];
+    __syncwarp();
     const C2* rtw = ertw<T>(g.p);
-    C2* S = (C2*)g.S;
-    for (int e = tid; e < RA * (hh + 1); e += nt) {
-        const int o = e / (hh + 1), k = e - o * (hh + 1);
-        const int gj = j0 + o;
-        if (gj >= ny) continue;
-        const C2 Zk = r[o * hh + (k == hh ? 0 : k)];
-        const C2 Zc = r[o * hh + (k == 0 ? 0 : hh - k)];
+    C2* S = (C2*)g.S + (size_t)j * g.p.sp;
+    for (int k = lane; k <= hh; k += 32) {
+        const C2 Zk = wb[k == hh ? 0 : k];
+        const C2 Zc = wb[k == 0 ? 0 : hh - k];
         C2 E, O;
         E.x = (T)0.5 * (Zk.x + Zc.x);
         E.y = (T)0.5 * (Zk.y - Zc.y);
         O.x = (T)0.5 * (Zk.y + Zc.y);
         O.y = (T)-0.5 * (Zk.x - Zc.x);
-        S[(size_t)gj * g.p.sp + k] = cadd(E, cmul(__ldg(rtw + k), O));
+        S[k] = cadd(E, cmul(__ldg(rtw + k), O));
     }
-    __syncthreads();
+    __syncwarp();
 }
 
-// ---------------------------------------------------------------------------
-// Phase B: CB spectrum columns: forward column FFT, Hartley-basis multiply,
-// inverse column FFT.
-// ---------------------------------------------------------------------------
-template <typename T>
-__device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem)
+// column k of S: forward FFT, Hartley-basis multiply, inverse FFT
+template <typename T, int Q>
+__device__ void col_w(const EngineArgs& g, int k, typename vec2<T>::type* wb)
 {
     typedef typename vec2<T>::type C2;
-    const int ny = g.p.ny;
-    C2* b0 = reinterpret_cast<C2*>(smem);
-    C2* b1 = b0 + (size_t)CB * ny;
+    constexpr int ny = 32 * Q;
+    const int lane = threadIdx.x & 31;
     C2* S = (C2*)g.S;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int e0 = tid; e0 < CB * ny; e0 += 4 * nt) {
-        C2 v[4];
+    const int sp = g.p.sp;
+    C2 v[Q];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int e = e0 + u * nt;
-            const int c = e % CB, l = e / CB;
-            const int k = k0 + c;
-            v[u] = (e < CB * ny && k <= g.p.h) ? S[(size_t)l * g.p.sp + k] : mk2<T>((T)0, (T)0);
-        }
+    for (int q = 0; q < Q; ++q) v[q] = S[(size_t)(lane + 32 * q) * sp + k];
+    warp_fft<T, Q>(v, lane, etw<T>(g.p.col), -1);
+    const int base = Q * brev5(lane);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int e = e0 + u * nt;
-            if (e < CB * ny) b0[(e % CB) * ny + e / CB] = v[u];
-        }
-    }
-    __syncthreads();
-    C2* r = block_fft<T>(b0, b1, g.p.col.d, CB, ny, etw<T>(g.p.col), -1);
+    for (int k1 = 0; k1 < Q; ++k1) wb[base + k1] = v[k1];
+    __syncwarp();
     const T* mA = g.mA_T<T>();
     const T* mB = g.mB_T<T>();
-    const int half = ny / 2 + 1;
-    for (int e = tid; e < CB * half; e += nt) {
-        const int c = e % CB, l = e / CB;
-        const int k = k0 + c;
-        if (k > g.p.h) continue;
-        const int lm = (ny - l) % ny;
-        C2* col = r + (size_t)c * ny;
-        const size_t ia = (size_t)l * g.p.sp + k, ib = (size_t)lm * g.p.sp + k;
-        const C2 Fa = col[l], Fb = col[lm];
+    for (int l = lane; l <= ny / 2; l += 32) {
+        const int lm = (ny - l) & (ny - 1);
+        const size_t ia = (size_t)l * sp + k, ib = (size_t)lm * sp + k;
+        const C2 Fa = wb[l], Fb = wb[lm];
+        C2 a, b;
         if (g.even) {
-            const T ma = mA[ia], mb = mA[ib];
-            C2 a = Fa, b = Fb;
-            a.x *= ma; a.y *= ma;
-            b.x *= mb; b.y *= mb;
-            col[l] = a;
-            if (lm != l) col[lm] = b;
+            const T ma = __ldg(mA + ia), mb = __ldg(mA + ib);
+            a.x = Fa.x * ma; a.y = Fa.y * ma;
+            b.x = Fb.x * mb; b.y = Fb.y * mb;
         } else {
             const T H_kl = Fb.x - Fa.y, H_mkml = Fb.x + Fa.y;
             const T H_mkl = Fa.x + Fb.y, H_kml = Fa.x - Fb.y;
-            const T G_kl = mA[ia] * H_kl, G_kml = mA[ib] * H_kml;
-            const T G_mkl = mB[ia] * H_mkl, G_mkml = mB[ib] * H_mkml;
-            C2 a, b;
+            const T G_kl = __ldg(mA + ia) * H_kl, G_kml = __ldg(mA + ib) * H_kml;
+            const T G_mkl = __ldg(mB + ia) * H_mkl, G_mkml = __ldg(mB + ib) * H_mkml;
             a.x = (T)0.5 * (G_kml + G_mkl);
             a.y = (T)0.5 * (G_mkml - G_kl);
             b.x = (T)0.5 * (G_kl + G_mkml);
             b.y = (T)0.5 * (G_mkl - G_kml);
-            col[l] = a;
-            if (lm != l) col[lm] = b;
         }
+        wb[l] = a;
+        if (lm != l) wb[lm] = b;
     }
-    __syncthreads();
-    C2* other = (r == b0) ? b1 : b0;
-    C2* q = block_fft<T>(r, other, g.p.col.d, CB, ny, etw<T>(g.p.col), +1);
-    for (int e = tid; e < CB * ny; e += nt) {
-        const int c = e % CB, l = e / CB;
-        const int k = k0 + c;
-        if (k <= g.p.h) S[(size_t)l * g.p.sp + k] = q[c * ny + l];
-    }
-    __syncthreads();
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q] = wb[lane + 32 * q];
+    warp_fft<T, Q>(v, lane, etw<T>(g.p.col), +1);
+#pragma unroll
+    for (int k1 = 0; k1 < Q; ++k1) S[(size_t)(base + k1) * sp + k] = v[k1];
+    __syncwarp();
 }
 
-// ---------------------------------------------------------------------------
-// Phase C: inverse row real-FFT of rows j0 .. j0+RC-1 -> raw (scaled 1/(nx ny)).
-// ---------------------------------------------------------------------------
-template <typename T>
-__device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem)
+// inverse real FFT of S row j -> raw row j, scaled
+template <typename T, int P>
+__device__ void row_inv_w(const EngineArgs& g, int j, T* out)
 {
     typedef typename vec2<T>::type C2;
-    const int hh = g.p.h, ny = g.p.ny, nx = g.p.nx;
-    C2* b0 = reinterpret_cast<C2*>(smem);
-    C2* b1 = b0 + (size_t)RC * hh;
-    const C2* S = (const C2*)g.S;
+    constexpr int hh = 32 * P;
+    const int lane = threadIdx.x & 31;
+    const C2* S = (const C2*)g.S + (size_t)j * g.p.sp;
     const C2* rtw = ertw<T>(g.p);
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int e = tid; e < RC * hh; e += nt) {
-        const int o = e / hh, k = e - o * hh;
-        const int j = j0 + o;
-        C2 z = mk2<T>((T)0, (T)0);
-        if (j < ny) {
-            const C2 A = S[(size_t)j * g.p.sp + k];
-            C2 B = S[(size_t)j * g.p.sp + (hh - k)];
-            B.y = -B.y;
-            const C2 sum = cadd(A, B), dif = csub(A, B);
-            const C2 t = cmulc(dif, __ldg(rtw + k));
-            z.x = sum.x - t.y;
-            z.y = sum.y + t.x;
-        }
-        b0[e] = z;
+    C2 v[P];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+        const int k = lane + 32 * p;
+        const C2 A = S[k];
+        C2 B = S[hh - k];
+        B.y = -B.y;
+        const C2 sum = cadd(A, B), dif = csub(A, B);
+        const C2 t = cmulc(dif, __ldg(rtw + k));
+        v[p].x = sum.x - t.y;
+        v[p].y = sum.y + t.x;
     }
-    __syncthreads();
-    C2* r = block_fft<T>(b0, b1, g.p.row.d, RC, hh, etw<T>(g.p.row), +1);
+    warp_fft<T, P>(v, lane, etw<T>(g.p.row), +1);
     const T scale = (T)g.norm_scale;
-    for (int e = tid; e < RC * hh; e += nt) {
-        const int o = e / hh, m = e - o * hh;
-        const int j = j0 + o;
-        if (j >= ny) continue;
-        C2 v = r[e];
-        v.x *= scale;
-        v.y *= scale;
-        *reinterpret_cast<C2*>(out + (size_t)j * nx + 2 * m) = v;
+    C2* o = reinterpret_cast<C2*>(out + (size_t)j * g.p.nx) + P * brev5(lane);
+#pragma unroll
+    for (int k1 = 0; k1 < P; ++k1) {
+        C2 w = v[k1];
+        w.x *= scale;
+        w.y *= scale;
+        o[k1] = w;
     }
-    __syncthreads();
 }
 
-// ---------------------------------------------------------------------------
+template <typename T>
+__device__ void phase_rows_fwd(const EngineArgs& g, unsigned char* smem)
+{
+    typedef typename vec2<T>::type C2;
+    const int warp = threadIdx.x >> 5;
+    const int line = g.p.h > g.p.ny ? g.p.h : g.p.ny;
+    C2* wb = reinterpret_cast<C2*>(smem) + (size_t)warp * line;
+    for (int j = blockIdx.x * ENGINE_WARPS + warp; j < g.p.ny; j += gridDim.x * ENGINE_WARPS) {
+        switch (g.p.h >> 5) {
+        case 2: row_fwd_w<T, 2>(g, j, wb); break;
+        case 4: row_fwd_w<T, 4>(g, j, wb); break;
+        case 8: row_fwd_w<T, 8>(g, j, wb); break;
+        case 16: row_fwd_w<T, 16>(g, j, wb); break;
+        }
+    }
+}
+
+template <typename T>
+__device__ void phase_cols(const EngineArgs& g, unsigned char* smem)
+{
+    typedef typename vec2<T>::type C2;
+    const int warp = threadIdx.x >> 5;
+    const int line = g.p.h > g.p.ny ? g.p.h : g.p.ny;
+    C2* wb = reinterpret_cast<C2*>(smem) + (size_t)warp * line;
+    for (int k = blockIdx.x * ENGINE_WARPS + warp; k <= g.p.h; k += gridDim.x * ENGINE_WARPS) {
+        switch (g.p.ny >> 5) {
+        case 2: col_w<T, 2>(g, k, wb); break;
+        case 4: col_w<T, 4>(g, k, wb); break;
+        case 8: col_w<T, 8>(g, k, wb); break;
+        case 16: col_w<T, 16>(g, k, wb); break;
+        }
+    }
+}
+
+template <typename T>
+__device__ void phase_rows_inv(const EngineArgs& g, T* out)
+{
+    const int warp = threadIdx.x >> 5;
+    for (int j = blockIdx.x * ENGINE_WARPS + warp; j < g.p.ny; j += gridDim.x * ENGINE_WARPS) {
+        switch (g.p.h >> 5) {
+        case 2: row_inv_w<T, 2>(g, j, out); break;
+        case 4: row_inv_w<T, 4>(g, j, out); break;
+        case 8: row_inv_w<T, 8>(g, j, out); break;
+        case 16: row_inv_w<T, 16>(g, j, out); break;
+        }
+    }
+}
+
 __device__ __forceinline__ unsigned long long gtimer()
 {
     unsigned long long t;
@@ -448,7 +389,7 @@ __global__ void __launch_bounds__(256, MINB) k_engine_rk4(EngineArgs g)
     cg::grid_group grid = cg::this_grid();
     const int nx = g.p.nx, ny = g.p.ny;
     const size_t n = (size_t)nx * ny;
-    const int na = (ny + RA - 1) / RA, nb = (g.p.h + 1 + g.CB - 1) / g.CB, nc = (ny + RC - 1) / RC;
+    const int ntiles = ((nx + SX - 1) / SX) * ((ny + SY - 1) / SY);
     Ctl* ctl = g.ctl;
     __shared__ double s_h;
     const bool tr = g.trace && blockIdx.x == 0 && threadIdx.x == 0;
@@ -472,15 +413,19 @@ __global__ void __launch_bounds__(256, MINB) k_engine_rk4(EngineArgs g)
         if (h < 0.0) return;   // uniform over the grid
         TRACE();
         for (int stage = 0; stage < 4; ++stage) {
-            for (int it = blockIdx.x; it < na; it += gridDim.x) phase_a<T>(g, it * RA, stage, h, smem);
+            for (int it = blockIdx.x; it < ntiles; it += gridDim.x) phase_stencil<T>(g, it, stage, h, smem);
             TRACE();
             grid.sync();
             TRACE();
-            for (int it = blockIdx.x; it < nb; it += gridDim.x) phase_b<T>(g, it * g.CB, g.CB, smem);
+            phase_rows_fwd<T>(g, smem);
             TRACE();
             grid.sync();
             TRACE();
-            for (int it = blockIdx.x; it < nc; it += gridDim.x) phase_c<T>(g, it * RC, (T*)g.raw[stage], smem);
+            phase_cols<T>(g, smem);
+            TRACE();
+            grid.sync();
+            TRACE();
+            phase_rows_inv<T>(g, (T*)g.raw[stage]);
             TRACE();
             grid.sync();
             TRACE();
@@ -545,16 +490,19 @@ void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s)
     k_split<<<b, 256, 0, s>>>(x, hi, lo, n);
 }
 
+// blocks per SM of the engine (FI_ENGINE_BPS=1 selects one, with up to 255 registers)
 static int engine_bps()
 {
     const char* e = getenv("FI_ENGINE_BPS");
-    return (e && e[0] == '2') ? 2 : 1;
+    return (e && e[0] == '1') ? 1 : 2;
 }
 
 template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem)
 {
     typedef typename vec2<T>::type C2;
-    if (p.nx % 4 != 0) return 0;   // 16-byte row vectors in the phase-A prefetch
+    // warp transforms: h = nx/2 and ny powers of two with 64 <= len <= 512
+    auto ok_len = [](int L) { return L >= 64 && L <= 512 && (L & (L - 1)) == 0; };
+    if (!ok_len(p.h) || !ok_len(p.ny)) return 0;
     int cb = (int)(16 / sizeof(C2));
     if (cb < 1) cb = 1;
     *CB = cb;

@@ -28,6 +28,7 @@ struct EngineArgs {
     const uint8_t* mask;
     void* raw[4];                    // stage outputs, field type
     void* S;                         // half spectrum, field type complex
+    void* f;                         // stencil output (field type), input of the row transform
     Ctl* ctl;
     int nsteps;
     int CB;                          // spectrum columns per phase-B item

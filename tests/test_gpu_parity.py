@@ -218,7 +218,7 @@ def test_graph_replay_matches_eager(precision, monkeypatch):
         assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("precision,n", [(0, 64), (0, 128), (1, 128), (1, 256)])
+@pytest.mark.parametrize("precision,n", [(0, 128), (0, 256), (1, 128), (1, 256)])
 def test_step_engine_matches_kernel_sequence(precision, n, monkeypatch):
     """The cooperative RK4 step engine against the one-kernel-per-pass path:
     FP64 to rounding, mixed within the mixed-form bound."""
