@@ -81,7 +81,9 @@ __device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h
         s_sc[0] = stage > 0 ? c_rk4_a[stage] * h * g.spy : 0.0;
         s_sc[1] = stage > 0 ? corner_mean_of(rprev, nx, ny) : 0.0;
     }
+#pragma unroll
     for (int ly = ty; ly < SRY; ly += 4)
+#pragma unroll
         for (int lx = tx; lx < SRX; lx += 64) {
             const int gi = i0 + lx, gj = j0 + ly;
             const int l = ly * SRX + lx;
@@ -141,7 +143,9 @@ __device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h
     __syncthreads();
     const T nu = (T)g.fc.nu, omn = (T)g.fc.one_minus_nu;
     const T* Dg = g.D_T<T>();
+#pragma unroll
     for (int ly = ty + 1; ly < SRY - 1; ly += 4)
+#pragma unroll
         for (int lx = tx + 1; lx < SRX - 1; lx += 64) {
             const int gi = i0 + lx, gj = j0 + ly;
             if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
@@ -230,7 +234,10 @@ __device__ void row_fwd_w(const EngineArgs& g, int j, typename vec2<T>::type* wb
     __syncwarp();
     const C2* rtw = ertw<T>(g.p);
     C2* S = (C2*)g.S + (size_t)j * g.p.sp;
-    for (int k = lane; k <= hh; k += 32) {
+#pragma unroll
+    for (int jj = 0; jj <= P; ++jj) {
+        const int k = lane + 32 * jj;
+        if (k > hh) break;
         const C2 Zk = wb[k == hh ? 0 : k];
         const C2 Zc = wb[k == 0 ? 0 : hh - k];
         C2 E, O;
@@ -262,7 +269,10 @@ __device__ void col_w(const EngineArgs& g, int k, typename vec2<T>::type* wb)
     __syncwarp();
     const T* mA = g.mA_T<T>();
     const T* mB = g.mB_T<T>();
-    for (int l = lane; l <= ny / 2; l += 32) {
+#pragma unroll
+    for (int jj = 0; jj <= Q / 2; ++jj) {
+        const int l = lane + 32 * jj;
+        if (l > ny / 2) break;
         const int lm = (ny - l) & (ny - 1);
         const size_t ia = (size_t)l * sp + k, ib = (size_t)lm * sp + k;
         const C2 Fa = wb[l], Fb = wb[lm];
@@ -499,6 +509,9 @@ static int engine_bps()
 
 template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem)
 {
+    // The plain FP64 form is FP64-throughput bound; it runs faster as the
+    // multi-kernel graph (full occupancy) than in the one-grid engine.
+    if (sizeof(T) == 8 && !getenv("FI_ENGINE_FP64")) return 0;
     typedef typename vec2<T>::type C2;
     // warp transforms: h = nx/2 and ny powers of two with 64 <= len <= 512
     auto ok_len = [](int L) { return L >= 64 && L <= 512 && (L & (L - 1)) == 0; };

@@ -142,12 +142,22 @@ __device__ __forceinline__ void warp_fft(typename vec2<T>::type (&v)[P], int lan
 {
     typedef typename vec2<T>::type C2;
     constexpr int n = 32 * P;
+    // all twiddles of this lane first, so their loads overlap
+    C2 w2[P > 1 ? P - 1 : 1], w3[5];
+#pragma unroll
+    for (int k1 = 1; k1 < P; ++k1) w2[k1 - 1] = tw_load<T, C2>(tw, lane * k1, sign);
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+        const int d = 16 >> s;
+        w3[s] = tw_load<T, C2>(tw, (lane & (d - 1)) * (16 / d) * (n / 32), sign);
+    }
     RegDft<T, P>::run(v, sign);
 #pragma unroll
-    for (int k1 = 1; k1 < P; ++k1) v[k1] = cmul(v[k1], tw_load<T, C2>(tw, lane * k1, sign));
+    for (int k1 = 1; k1 < P; ++k1) v[k1] = cmul(v[k1], w2[k1 - 1]);
 #pragma unroll
-    for (int d = 16; d >= 1; d >>= 1) {
-        const C2 w = tw_load<T, C2>(tw, (lane & (d - 1)) * (16 / d) * (n / 32), sign);
+    for (int s = 0; s < 5; ++s) {
+        const int d = 16 >> s;
+        const C2 w = w3[s];
         const bool upper = (lane & d) == 0;
 #pragma unroll
         for (int k1 = 0; k1 < P; ++k1) {
