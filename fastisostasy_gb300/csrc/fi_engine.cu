@@ -48,13 +48,18 @@ __constant__ double c_rk4_a[4] = {0.0, 0.5, 0.5, 1.0};
 constexpr int SX = 64, SY = 16, SRX = SX + 4, SRY = SY + 4, SREG = SRX * SRY;
 constexpr int ENGINE_THREADS = 256, ENGINE_WARPS = ENGINE_THREADS / 32;
 
+constexpr int RB = ENGINE_WARPS;   // rows per row-phase item (one warp per row)
+
 template <typename T> size_t engine_smem_bytes(const Plan2D& p, int)
 {
     typedef typename vec2<T>::type C2;
-    const size_t stencil = (size_t)10 * SREG * sizeof(T);
-    const int line = p.h > p.ny ? p.h : p.ny;
-    const size_t warpbuf = (size_t)ENGINE_WARPS * line * sizeof(C2);
-    return (stencil > warpbuf ? stencil : warpbuf) + 64;
+    const size_t nw = (sizeof(T) == 4) ? 4 : 3;   // interior arrays: q0, 1/(2 eta), w_ref (hi, lo)
+    const size_t stencil = (size_t)11 * SREG * sizeof(T) + nw * SX * SY * sizeof(T) + SX * SY;
+    const size_t rows = (size_t)RB * (p.h + 1) * sizeof(C2) + (size_t)ENGINE_WARPS * p.h * sizeof(C2);
+    const size_t cols = (size_t)ENGINE_WARPS * p.ny * sizeof(C2);
+    size_t m = stencil > rows ? stencil : rows;
+    m = m > cols ? m : cols;
+    return m + 64;
 }
 
 template <typename T>
@@ -74,6 +79,12 @@ __device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h
     T* Myy = Mxx + SREG;
     T* Mxy = Myy + SREG;
     T* Mxyx = Mxy + SREG;
+    T* Ds = Mxyx + SREG;                  // rigidity on the halo region
+    T* Qs = Ds + SREG;                    // interior SX x SY arrays
+    T* Es = Qs + SX * SY;
+    T* W0 = Es + SX * SY;                 // mixed: w_ref hi | plain: w_ref
+    T* W1 = W0 + SX * SY;                 // mixed: w_ref lo
+    uint8_t* Ks = reinterpret_cast<uint8_t*>(W0 + (sizeof(T) == 4 ? 2 : 1) * SX * SY);
     const T* rprev = stage > 0 ? (const T*)g.raw[stage - 1] : nullptr;
     __shared__ double s_sc[2];
     __syncthreads();   // previous item's readers are done with the tile buffers
@@ -81,28 +92,61 @@ __device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h
         s_sc[0] = stage > 0 ? c_rk4_a[stage] * h * g.spy : 0.0;
         s_sc[1] = stage > 0 ? corner_mean_of(rprev, nx, ny) : 0.0;
     }
+    // every global read of the item in one batch
+    const T* Dg = g.D_T<T>();
 #pragma unroll
     for (int ly = ty; ly < SRY; ly += 4)
 #pragma unroll
         for (int lx = tx; lx < SRX; lx += 64) {
             const int gi = i0 + lx, gj = j0 + ly;
             const int l = ly * SRX + lx;
+            T a0 = (T)0, a1 = (T)0, a2 = (T)0, d = (T)0;
             if (gi >= 0 && gi < nx && gj >= 0 && gj < ny) {
                 const size_t c = (size_t)gj * nx + gi;
                 if constexpr (std::is_same<T, float>::value) {
-                    A0[l] = g.xhi[c];
-                    A1[l] = g.xlo[c];
-                    A2[l] = rprev ? rprev[c] : 0.f;
+                    a0 = g.xhi[c];
+                    a1 = g.xlo[c];
+                    if (rprev) a2 = rprev[c];
                 } else {
-                    A0[l] = g.x[c];
-                    A1[l] = rprev ? rprev[c] : 0.0;
+                    a0 = g.x[c];
+                    if (rprev) a1 = rprev[c];
                 }
-            } else {
-                A0[l] = (T)0;
-                A1[l] = (T)0;
-                A2[l] = (T)0;
+                d = __ldg(Dg + c);
             }
+            A0[l] = a0;
+            A1[l] = a1;
+            A2[l] = a2;
+            Ds[l] = d;
         }
+    {
+        const T* q0 = g.q0_T<T>();
+        const T* i2e = g.inv2eta_T<T>();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int oy = ty + 4 * q;
+            const int gi = i0 + 2 + tx, gj = j0 + 2 + oy;
+            const int o = oy * SX + tx;
+            T qv = (T)0, ev = (T)0, w0 = (T)0, w1 = (T)0;
+            uint8_t mk = 0;
+            if (gi < nx && gj < ny) {
+                const size_t c = (size_t)gj * nx + gi;
+                qv = __ldg(q0 + c);
+                ev = __ldg(i2e + c);
+                mk = g.mask[c];
+                if constexpr (std::is_same<T, float>::value) {
+                    w0 = __ldg(g.wrefhi + c);
+                    w1 = __ldg(g.wreflo + c);
+                } else {
+                    w0 = __ldg(g.wref + c);
+                }
+            }
+            Qs[o] = qv;
+            Es[o] = ev;
+            W0[o] = w0;
+            if constexpr (std::is_same<T, float>::value) W1[o] = w1;
+            Ks[o] = mk;
+        }
+    }
     __syncthreads();
     const double sd = s_sc[0], cmd = s_sc[1];
     const float sf = (float)sd;
@@ -111,7 +155,9 @@ __device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h
         for (int e = threadIdx.x; e < SREG; e += ENGINE_THREADS) A2[e] = rprev ? A0[e] + sd * (A1[e] - cmd) : A0[e];
         __syncthreads();
     }
+#pragma unroll
     for (int ly = ty; ly < SRY; ly += 4)
+#pragma unroll
         for (int lx = tx; lx < SRX; lx += 64) {
             const int l = ly * SRX + lx;
             if (lx < SRX - 1) {
@@ -130,7 +176,9 @@ __device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h
     __syncthreads();
     const T inv_dx = (T)g.fc.inv_dx, inv_2dx = (T)g.fc.inv_2dx, inv_dx2 = (T)g.fc.inv_dx2;
     const T inv_dy = (T)g.fc.inv_dy, inv_2dy = (T)g.fc.inv_2dy, inv_dy2 = (T)g.fc.inv_dy2;
+#pragma unroll
     for (int ly = ty; ly < SRY; ly += 4)
+#pragma unroll
         for (int lx = tx + 1; lx < SRX - 1; lx += 64) {
             const int gi = i0 + lx;
             const int l = ly * SRX + lx;
@@ -142,7 +190,6 @@ __device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h
         }
     __syncthreads();
     const T nu = (T)g.fc.nu, omn = (T)g.fc.one_minus_nu;
-    const T* Dg = g.D_T<T>();
 #pragma unroll
     for (int ly = ty + 1; ly < SRY - 1; ly += 4)
 #pragma unroll
@@ -160,13 +207,15 @@ __device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h
             if (gj == 0) wyy = (dY[l + SRX] - dY[l]) * inv_dy2;
             else if (gj == ny - 1) wyy = (dY[l - SRX] - dY[l - 2 * SRX]) * inv_dy2;
             else wyy = (dY[l] - dY[l - SRX]) * inv_dy2;
-            const T Dl = __ldg(Dg + (size_t)gj * nx + gi);
+            const T Dl = Ds[l];
             Mxx[l] = -Dl * (wxx + nu * wyy);
             Myy[l] = -Dl * (wyy + nu * wxx);
             Mxy[l] = (-Dl * omn) * wxy;
         }
     __syncthreads();
+#pragma unroll
     for (int ly = ty + 1; ly < SRY - 1; ly += 4)
+#pragma unroll
         for (int lx = tx + 2; lx < SRX - 2; lx += 64) {
             const int gi = i0 + lx, gj = j0 + ly;
             if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
@@ -178,15 +227,14 @@ __device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h
             Mxyx[l] = v;
         }
     __syncthreads();
-    const T* q0 = g.q0_T<T>();
-    const T* i2e = g.inv2eta_T<T>();
     T* f = (T*)g.f;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const int lx = tx + 2, ly = ty + 2 + 4 * q;
+        const int oy = ty + 4 * q;
+        const int lx = tx + 2, ly = oy + 2;
         const int gi = i0 + lx, gj = j0 + ly;
         if (gi >= nx || gj >= ny) continue;
-        const int l = ly * SRX + lx;
+        const int l = ly * SRX + lx, o = oy * SX + tx;
         T mxy_xy, mx_xx, my_yy;
         if (gj == 0) mxy_xy = (Mxyx[l + SRX] - Mxyx[l]) * inv_dy;
         else if (gj == ny - 1) mxy_xy = (Mxyx[l] - Mxyx[l - SRX]) * inv_dy;
@@ -197,95 +245,123 @@ __device__ void phase_stencil(const EngineArgs& g, int tile, int stage, double h
         if (gj == 0) my_yy = ((Myy[l + 2 * SRX] - (T)2 * Myy[l + SRX]) + Myy[l]) * inv_dy2;
         else if (gj == ny - 1) my_yy = ((Myy[l] - (T)2 * Myy[l - SRX]) + Myy[l - 2 * SRX]) * inv_dy2;
         else my_yy = ((Myy[l + SRX] - (T)2 * Myy[l]) + Myy[l - SRX]) * inv_dy2;
-        const size_t c = (size_t)gj * nx + gi;
         T p = (T)0;
-        if (g.mask[c]) {
+        if (Ks[o]) {
             // q0 + (-g rho_m) (y - w_ref) at the stage state
             if constexpr (std::is_same<T, float>::value) {
-                float dy = (A0[l] - __ldg(g.wrefhi + c)) + (A1[l] - __ldg(g.wreflo + c));
+                float dy = (A0[l] - W0[o]) + (A1[l] - W1[o]);
                 if (rprev) dy += sf * (A2[l] - (float)cmd);
-                p = __ldg(q0 + c) + (float)g.fc.coef_mantle * dy;
+                p = Qs[o] + (float)g.fc.coef_mantle * dy;
             } else {
-                p = __ldg(q0 + c) + g.fc.coef_mantle * (A2[l] - __ldg(g.wref + c));
+                p = Qs[o] + g.fc.coef_mantle * (A2[l] - W0[o]);
             }
         }
-        f[c] = (((p + mx_xx) + (T)2 * mxy_xy) + my_yy) * __ldg(i2e + c);
+        f[(size_t)gj * nx + gi] = (((p + mx_xx) + (T)2 * mxy_xy) + my_yy) * Es[o];
     }
 }
 
 // ---------------------------------------------------------------------------
-// Warp-level transforms: one warp per row or per spectrum column.
+// Warp-level transforms.  The engine keeps the half spectrum transposed,
+// ST[k * ny + l] (k <= h, l < ny), so that every column is contiguous; the
+// row phases move 8-row strips through shared memory (64-byte segments).
 // ---------------------------------------------------------------------------
-// forward real FFT of row j of f -> S row j (h+1 bins)
 template <typename T, int P>
-__device__ void row_fwd_w(const EngineArgs& g, int j, typename vec2<T>::type* wb)
+__device__ void rows_fwd_item(const EngineArgs& g, int j0, unsigned char* smem)
 {
     typedef typename vec2<T>::type C2;
     constexpr int hh = 32 * P;
-    const int lane = threadIdx.x & 31;
-    const C2* f2 = reinterpret_cast<const C2*>((const T*)g.f + (size_t)j * g.p.nx);
-    C2 v[P];
+    const int ny = g.p.ny;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    C2* X = reinterpret_cast<C2*>(smem);            // RB x (hh+1)
+    C2* wb = X + (size_t)RB * (hh + 1) + (size_t)w * hh;
+    const int j = j0 + w;
+    if (j < ny) {
+        const C2* f2 = reinterpret_cast<const C2*>((const T*)g.f + (size_t)j * g.p.nx);
+        C2 v[P];
 #pragma unroll
-    for (int p = 0; p < P; ++p) v[p] = f2[lane + 32 * p];
-    warp_fft<T, P>(v, lane, etw<T>(g.p.row), -1);
-    const int base = P * brev5(lane);
+        for (int p = 0; p < P; ++p) v[p] = f2[lane + 32 * p];
+        const C2* rtw = ertw<T>(g.p);
+        C2 rt[P + 1];
 #pragma unroll
-    for (int k1 = 0; k1 < P; ++k1) wb[base + k1] = v[k1];
-    __syncwarp();
-    const C2* rtw = ertw<T>(g.p);
-    C2* S = (C2*)g.S + (size_t)j * g.p.sp;
+        for (int jj = 0; jj <= P; ++jj) {
+            const int k = lane + 32 * jj;
+            rt[jj] = k <= hh ? __ldg(rtw + k) : mk2<T>((T)0, (T)0);
+        }
+        warp_fft<T, P>(v, lane, etw<T>(g.p.row), -1);
+        const int base = P * brev5(lane);
 #pragma unroll
-    for (int jj = 0; jj <= P; ++jj) {
-        const int k = lane + 32 * jj;
-        if (k > hh) break;
-        const C2 Zk = wb[k == hh ? 0 : k];
-        const C2 Zc = wb[k == 0 ? 0 : hh - k];
-        C2 E, O;
-        E.x = (T)0.5 * (Zk.x + Zc.x);
-        E.y = (T)0.5 * (Zk.y - Zc.y);
-        O.x = (T)0.5 * (Zk.y + Zc.y);
-        O.y = (T)-0.5 * (Zk.x - Zc.x);
-        S[k] = cadd(E, cmul(__ldg(rtw + k), O));
+        for (int k1 = 0; k1 < P; ++k1) wb[base + k1] = v[k1];
+        __syncwarp();
+        C2* Xr = X + (size_t)w * (hh + 1);
+#pragma unroll
+        for (int jj = 0; jj <= P; ++jj) {
+            const int k = lane + 32 * jj;
+            if (k <= hh) {
+                const C2 Zk = wb[k == hh ? 0 : k];
+                const C2 Zc = wb[k == 0 ? 0 : hh - k];
+                C2 E, O;
+                E.x = (T)0.5 * (Zk.x + Zc.x);
+                E.y = (T)0.5 * (Zk.y - Zc.y);
+                O.x = (T)0.5 * (Zk.y + Zc.y);
+                O.y = (T)-0.5 * (Zk.x - Zc.x);
+                Xr[k] = cadd(E, cmul(rt[jj], O));
+            }
+        }
     }
-    __syncwarp();
+    __syncthreads();
+    C2* ST = (C2*)g.ST;
+    for (int e = threadIdx.x; e < RB * (hh + 1); e += ENGINE_THREADS) {
+        const int k = e / RB, o = e - k * RB;
+        if (j0 + o < ny) ST[(size_t)k * ny + j0 + o] = X[(size_t)o * (hh + 1) + k];
+    }
+    __syncthreads();
 }
 
-// column k of S: forward FFT, Hartley-basis multiply, inverse FFT
 template <typename T, int Q>
 __device__ void col_w(const EngineArgs& g, int k, typename vec2<T>::type* wb)
 {
     typedef typename vec2<T>::type C2;
     constexpr int ny = 32 * Q;
     const int lane = threadIdx.x & 31;
-    C2* S = (C2*)g.S;
-    const int sp = g.p.sp;
+    C2* col = (C2*)g.ST + (size_t)k * ny;
+    const T* mA = g.mA_T<T>() + (size_t)k * ny;
+    const T* mB = g.mB_T<T>() + (size_t)k * ny;
     C2 v[Q];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) v[q] = S[(size_t)(lane + 32 * q) * sp + k];
+    for (int q = 0; q < Q; ++q) v[q] = col[lane + 32 * q];
+    // multipliers of this lane's Hartley pairs (l, ny - l), l = lane + 32 jj <= ny/2
+    T ma[Q / 2 + 1], mb[Q / 2 + 1], mc[Q / 2 + 1], md[Q / 2 + 1];
+#pragma unroll
+    for (int jj = 0; jj <= Q / 2; ++jj) {
+        const int l = lane + 32 * jj;
+        const int lm = (ny - l) & (ny - 1);
+        const bool ok = l <= ny / 2;
+        ma[jj] = ok ? __ldg(mA + l) : (T)0;
+        mb[jj] = ok ? __ldg(mA + lm) : (T)0;
+        mc[jj] = (ok && !g.even) ? __ldg(mB + l) : (T)0;
+        md[jj] = (ok && !g.even) ? __ldg(mB + lm) : (T)0;
+    }
     warp_fft<T, Q>(v, lane, etw<T>(g.p.col), -1);
     const int base = Q * brev5(lane);
 #pragma unroll
     for (int k1 = 0; k1 < Q; ++k1) wb[base + k1] = v[k1];
     __syncwarp();
-    const T* mA = g.mA_T<T>();
-    const T* mB = g.mB_T<T>();
 #pragma unroll
     for (int jj = 0; jj <= Q / 2; ++jj) {
         const int l = lane + 32 * jj;
-        if (l > ny / 2) break;
+        if (l > ny / 2) continue;
         const int lm = (ny - l) & (ny - 1);
-        const size_t ia = (size_t)l * sp + k, ib = (size_t)lm * sp + k;
         const C2 Fa = wb[l], Fb = wb[lm];
         C2 a, b;
         if (g.even) {
-            const T ma = __ldg(mA + ia), mb = __ldg(mA + ib);
-            a.x = Fa.x * ma; a.y = Fa.y * ma;
-            b.x = Fb.x * mb; b.y = Fb.y * mb;
+            a.x = Fa.x * ma[jj]; a.y = Fa.y * ma[jj];
+            b.x = Fb.x * mb[jj]; b.y = Fb.y * mb[jj];
         } else {
+            // Hartley values at (k,l), (-k,-l), (-k,l), (k,-l), multiplied, back to the DFT
             const T H_kl = Fb.x - Fa.y, H_mkml = Fb.x + Fa.y;
             const T H_mkl = Fa.x + Fb.y, H_kml = Fa.x - Fb.y;
-            const T G_kl = __ldg(mA + ia) * H_kl, G_kml = __ldg(mA + ib) * H_kml;
-            const T G_mkl = __ldg(mB + ia) * H_mkl, G_mkml = __ldg(mB + ib) * H_mkml;
+            const T G_kl = ma[jj] * H_kl, G_kml = mb[jj] * H_kml;
+            const T G_mkl = mc[jj] * H_mkl, G_mkml = md[jj] * H_mkml;
             a.x = (T)0.5 * (G_kml + G_mkl);
             a.y = (T)0.5 * (G_mkml - G_kl);
             b.x = (T)0.5 * (G_kl + G_mkml);
@@ -299,56 +375,79 @@ __device__ void col_w(const EngineArgs& g, int k, typename vec2<T>::type* wb)
     for (int q = 0; q < Q; ++q) v[q] = wb[lane + 32 * q];
     warp_fft<T, Q>(v, lane, etw<T>(g.p.col), +1);
 #pragma unroll
-    for (int k1 = 0; k1 < Q; ++k1) S[(size_t)(base + k1) * sp + k] = v[k1];
+    for (int k1 = 0; k1 < Q; ++k1) col[base + k1] = v[k1];
     __syncwarp();
 }
 
-// inverse real FFT of S row j -> raw row j, scaled
 template <typename T, int P>
-__device__ void row_inv_w(const EngineArgs& g, int j, T* out)
+__device__ void rows_inv_item(const EngineArgs& g, int j0, T* out, unsigned char* smem)
 {
     typedef typename vec2<T>::type C2;
     constexpr int hh = 32 * P;
-    const int lane = threadIdx.x & 31;
-    const C2* S = (const C2*)g.S + (size_t)j * g.p.sp;
-    const C2* rtw = ertw<T>(g.p);
-    C2 v[P];
+    const int ny = g.p.ny;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    C2* X = reinterpret_cast<C2*>(smem);            // RB x (hh+1)
+    const C2* ST = (const C2*)g.ST;
+    {
+        constexpr int U = 4;
+        const int tot = RB * (hh + 1);
+        for (int e0 = threadIdx.x; e0 < tot; e0 += U * ENGINE_THREADS) {
+            C2 t[U];
 #pragma unroll
-    for (int p = 0; p < P; ++p) {
-        const int k = lane + 32 * p;
-        const C2 A = S[k];
-        C2 B = S[hh - k];
-        B.y = -B.y;
-        const C2 sum = cadd(A, B), dif = csub(A, B);
-        const C2 t = cmulc(dif, __ldg(rtw + k));
-        v[p].x = sum.x - t.y;
-        v[p].y = sum.y + t.x;
-    }
-    warp_fft<T, P>(v, lane, etw<T>(g.p.row), +1);
-    const T scale = (T)g.norm_scale;
-    C2* o = reinterpret_cast<C2*>(out + (size_t)j * g.p.nx) + P * brev5(lane);
+            for (int u = 0; u < U; ++u) {
+                const int e = e0 + u * ENGINE_THREADS;
+                const int k = e / RB, o = e - k * RB;
+                t[u] = (e < tot && j0 + o < ny) ? ST[(size_t)k * ny + j0 + o] : mk2<T>((T)0, (T)0);
+            }
 #pragma unroll
-    for (int k1 = 0; k1 < P; ++k1) {
-        C2 w = v[k1];
-        w.x *= scale;
-        w.y *= scale;
-        o[k1] = w;
+            for (int u = 0; u < U; ++u) {
+                const int e = e0 + u * ENGINE_THREADS;
+                const int k = e / RB, o = e - k * RB;
+                if (e < tot) X[(size_t)o * (hh + 1) + k] = t[u];
+            }
+        }
     }
+    __syncthreads();
+    const int j = j0 + w;
+    if (j < ny) {
+        const C2* Xr = X + (size_t)w * (hh + 1);
+        const C2* rtw = ertw<T>(g.p);
+        C2 v[P];
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+            const int k = lane + 32 * p;
+            const C2 A = Xr[k];
+            C2 B = Xr[hh - k];
+            B.y = -B.y;
+            const C2 sum = cadd(A, B), dif = csub(A, B);
+            const C2 t = cmulc(dif, __ldg(rtw + k));
+            v[p].x = sum.x - t.y;
+            v[p].y = sum.y + t.x;
+        }
+        warp_fft<T, P>(v, lane, etw<T>(g.p.row), +1);
+        const T scale = (T)g.norm_scale;
+        C2* o = reinterpret_cast<C2*>(out + (size_t)j * g.p.nx) + P * brev5(lane);
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) {
+            C2 q = v[k1];
+            q.x *= scale;
+            q.y *= scale;
+            o[k1] = q;
+        }
+    }
+    __syncthreads();
 }
 
 template <typename T>
 __device__ void phase_rows_fwd(const EngineArgs& g, unsigned char* smem)
 {
-    typedef typename vec2<T>::type C2;
-    const int warp = threadIdx.x >> 5;
-    const int line = g.p.h > g.p.ny ? g.p.h : g.p.ny;
-    C2* wb = reinterpret_cast<C2*>(smem) + (size_t)warp * line;
-    for (int j = blockIdx.x * ENGINE_WARPS + warp; j < g.p.ny; j += gridDim.x * ENGINE_WARPS) {
+    const int items = (g.p.ny + RB - 1) / RB;
+    for (int it = blockIdx.x; it < items; it += gridDim.x) {
         switch (g.p.h >> 5) {
-        case 2: row_fwd_w<T, 2>(g, j, wb); break;
-        case 4: row_fwd_w<T, 4>(g, j, wb); break;
-        case 8: row_fwd_w<T, 8>(g, j, wb); break;
-        case 16: row_fwd_w<T, 16>(g, j, wb); break;
+        case 2: rows_fwd_item<T, 2>(g, it * RB, smem); break;
+        case 4: rows_fwd_item<T, 4>(g, it * RB, smem); break;
+        case 8: rows_fwd_item<T, 8>(g, it * RB, smem); break;
+        case 16: rows_fwd_item<T, 16>(g, it * RB, smem); break;
         }
     }
 }
@@ -358,8 +457,7 @@ __device__ void phase_cols(const EngineArgs& g, unsigned char* smem)
 {
     typedef typename vec2<T>::type C2;
     const int warp = threadIdx.x >> 5;
-    const int line = g.p.h > g.p.ny ? g.p.h : g.p.ny;
-    C2* wb = reinterpret_cast<C2*>(smem) + (size_t)warp * line;
+    C2* wb = reinterpret_cast<C2*>(smem) + (size_t)warp * g.p.ny;
     for (int k = blockIdx.x * ENGINE_WARPS + warp; k <= g.p.h; k += gridDim.x * ENGINE_WARPS) {
         switch (g.p.ny >> 5) {
         case 2: col_w<T, 2>(g, k, wb); break;
@@ -371,15 +469,15 @@ __device__ void phase_cols(const EngineArgs& g, unsigned char* smem)
 }
 
 template <typename T>
-__device__ void phase_rows_inv(const EngineArgs& g, T* out)
+__device__ void phase_rows_inv(const EngineArgs& g, T* out, unsigned char* smem)
 {
-    const int warp = threadIdx.x >> 5;
-    for (int j = blockIdx.x * ENGINE_WARPS + warp; j < g.p.ny; j += gridDim.x * ENGINE_WARPS) {
+    const int items = (g.p.ny + RB - 1) / RB;
+    for (int it = blockIdx.x; it < items; it += gridDim.x) {
         switch (g.p.h >> 5) {
-        case 2: row_inv_w<T, 2>(g, j, out); break;
-        case 4: row_inv_w<T, 4>(g, j, out); break;
-        case 8: row_inv_w<T, 8>(g, j, out); break;
-        case 16: row_inv_w<T, 16>(g, j, out); break;
+        case 2: rows_inv_item<T, 2>(g, it * RB, out, smem); break;
+        case 4: rows_inv_item<T, 4>(g, it * RB, out, smem); break;
+        case 8: rows_inv_item<T, 8>(g, it * RB, out, smem); break;
+        case 16: rows_inv_item<T, 16>(g, it * RB, out, smem); break;
         }
     }
 }
@@ -435,7 +533,7 @@ __global__ void __launch_bounds__(256, MINB) k_engine_rk4(EngineArgs g)
             TRACE();
             grid.sync();
             TRACE();
-            phase_rows_inv<T>(g, (T*)g.raw[stage]);
+            phase_rows_inv<T>(g, (T*)g.raw[stage], smem);
             TRACE();
             grid.sync();
             TRACE();
