@@ -48,7 +48,7 @@ __constant__ double c_rk4_a[4] = {0.0, 0.5, 0.5, 1.0};
 constexpr int SX = 64, SY = 16, SRX = SX + 4, SRY = SY + 4, SREG = SRX * SRY;
 constexpr int ENGINE_THREADS = 256, ENGINE_WARPS = ENGINE_THREADS / 32;
 
-constexpr int RB = ENGINE_WARPS;   // rows per row-phase item (one warp per row)
+constexpr int RB = 4;   // rows per row-phase item (one warp per row; 32-byte transpose segments)
 
 template <typename T> size_t engine_smem_bytes(const Plan2D& p, int)
 {
@@ -275,7 +275,7 @@ __device__ void rows_fwd_item(const EngineArgs& g, int j0, unsigned char* smem)
     C2* X = reinterpret_cast<C2*>(smem);            // RB x (hh+1)
     C2* wb = X + (size_t)RB * (hh + 1) + (size_t)w * hh;
     const int j = j0 + w;
-    if (j < ny) {
+    if (w < RB && j < ny) {
         const C2* f2 = reinterpret_cast<const C2*>((const T*)g.f + (size_t)j * g.p.nx);
         C2 v[P];
 #pragma unroll
@@ -409,7 +409,7 @@ __device__ void rows_inv_item(const EngineArgs& g, int j0, T* out, unsigned char
     }
     __syncthreads();
     const int j = j0 + w;
-    if (j < ny) {
+    if (w < RB && j < ny) {
         const C2* Xr = X + (size_t)w * (hh + 1);
         const C2* rtw = ertw<T>(g.p);
         C2 v[P];
@@ -458,7 +458,8 @@ __device__ void phase_cols(const EngineArgs& g, unsigned char* smem)
     typedef typename vec2<T>::type C2;
     const int warp = threadIdx.x >> 5;
     C2* wb = reinterpret_cast<C2*>(smem) + (size_t)warp * g.p.ny;
-    for (int k = blockIdx.x * ENGINE_WARPS + warp; k <= g.p.h; k += gridDim.x * ENGINE_WARPS) {
+    // one column per block first, so that every SM gets work
+    for (int k = blockIdx.x + gridDim.x * warp; k <= g.p.h; k += gridDim.x * ENGINE_WARPS) {
         switch (g.p.ny >> 5) {
         case 2: col_w<T, 2>(g, k, wb); break;
         case 4: col_w<T, 4>(g, k, wb); break;
