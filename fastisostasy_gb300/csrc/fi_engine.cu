@@ -38,6 +38,13 @@ template <typename T> __device__ __forceinline__ const typename vec2<T>::type* e
 template <> __device__ __forceinline__ const double2* ertw<double>(const Plan2D& p) { return p.rtw64; }
 template <> __device__ __forceinline__ const float2* ertw<float>(const Plan2D& p) { return p.rtw32; }
 
+__device__ __forceinline__ unsigned long long gtimer0()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // stage coefficients of RK4: y_s = x + a_s h k_{s-1}
 __constant__ double c_rk4_a[4] = {0.0, 0.5, 0.5, 1.0};
 
@@ -323,6 +330,10 @@ __device__ void col_w(const EngineArgs& g, int k, typename vec2<T>::type* wb)
     typedef typename vec2<T>::type C2;
     constexpr int ny = 32 * Q;
     const int lane = threadIdx.x & 31;
+    const bool tr = g.trace && k == 0 && lane == 0 && g.trace[63] == 0;
+    unsigned long long tt[8];
+    int nt_ = 0;
+    if (tr) tt[nt_++] = gtimer0();
     C2* col = (C2*)g.ST + (size_t)k * ny;
     const T* mA = g.mA_T<T>() + (size_t)k * ny;
     const T* mB = g.mB_T<T>() + (size_t)k * ny;
@@ -341,7 +352,9 @@ __device__ void col_w(const EngineArgs& g, int k, typename vec2<T>::type* wb)
         mc[jj] = (ok && !g.even) ? __ldg(mB + l) : (T)0;
         md[jj] = (ok && !g.even) ? __ldg(mB + lm) : (T)0;
     }
+    if (tr) { volatile float sink = v[0].x + ma[0]; (void)sink; tt[nt_++] = gtimer0(); }
     warp_fft<T, Q>(v, lane, etw<T>(g.p.col), -1);
+    if (tr) { volatile float sink = v[0].x; (void)sink; tt[nt_++] = gtimer0(); }
     const int base = Q * brev5(lane);
 #pragma unroll
     for (int k1 = 0; k1 < Q; ++k1) wb[base + k1] = v[k1];
@@ -373,10 +386,17 @@ __device__ void col_w(const EngineArgs& g, int k, typename vec2<T>::type* wb)
     __syncwarp();
 #pragma unroll
     for (int q = 0; q < Q; ++q) v[q] = wb[lane + 32 * q];
+    if (tr) { volatile float sink = v[0].x; (void)sink; tt[nt_++] = gtimer0(); }
     warp_fft<T, Q>(v, lane, etw<T>(g.p.col), +1);
+    if (tr) { volatile float sink = v[0].x; (void)sink; tt[nt_++] = gtimer0(); }
 #pragma unroll
     for (int k1 = 0; k1 < Q; ++k1) col[base + k1] = v[k1];
     __syncwarp();
+    if (tr) {
+        tt[nt_++] = gtimer0();
+        for (int i = 0; i < nt_; ++i) g.trace[48 + i] = tt[i];
+        g.trace[63] = 1;
+    }
 }
 
 template <typename T, int P>
@@ -438,49 +458,31 @@ __device__ void rows_inv_item(const EngineArgs& g, int j0, T* out, unsigned char
     __syncthreads();
 }
 
-template <typename T>
+// Row/column transform lengths are template parameters (h = 32 P, ny = 32 Q):
+// one engine instantiation carries only the code of its own lengths, which
+// keeps the kernel small enough for the instruction cache.
+template <typename T, int P>
 __device__ void phase_rows_fwd(const EngineArgs& g, unsigned char* smem)
 {
     const int items = (g.p.ny + RB - 1) / RB;
-    for (int it = blockIdx.x; it < items; it += gridDim.x) {
-        switch (g.p.h >> 5) {
-        case 2: rows_fwd_item<T, 2>(g, it * RB, smem); break;
-        case 4: rows_fwd_item<T, 4>(g, it * RB, smem); break;
-        case 8: rows_fwd_item<T, 8>(g, it * RB, smem); break;
-        case 16: rows_fwd_item<T, 16>(g, it * RB, smem); break;
-        }
-    }
+    for (int it = blockIdx.x; it < items; it += gridDim.x) rows_fwd_item<T, P>(g, it * RB, smem);
 }
 
-template <typename T>
+template <typename T, int Q>
 __device__ void phase_cols(const EngineArgs& g, unsigned char* smem)
 {
     typedef typename vec2<T>::type C2;
     const int warp = threadIdx.x >> 5;
     C2* wb = reinterpret_cast<C2*>(smem) + (size_t)warp * g.p.ny;
     // one column per block first, so that every SM gets work
-    for (int k = blockIdx.x + gridDim.x * warp; k <= g.p.h; k += gridDim.x * ENGINE_WARPS) {
-        switch (g.p.ny >> 5) {
-        case 2: col_w<T, 2>(g, k, wb); break;
-        case 4: col_w<T, 4>(g, k, wb); break;
-        case 8: col_w<T, 8>(g, k, wb); break;
-        case 16: col_w<T, 16>(g, k, wb); break;
-        }
-    }
+    for (int k = blockIdx.x + gridDim.x * warp; k <= g.p.h; k += gridDim.x * ENGINE_WARPS) col_w<T, Q>(g, k, wb);
 }
 
-template <typename T>
+template <typename T, int P>
 __device__ void phase_rows_inv(const EngineArgs& g, T* out, unsigned char* smem)
 {
     const int items = (g.p.ny + RB - 1) / RB;
-    for (int it = blockIdx.x; it < items; it += gridDim.x) {
-        switch (g.p.h >> 5) {
-        case 2: rows_inv_item<T, 2>(g, it * RB, out, smem); break;
-        case 4: rows_inv_item<T, 4>(g, it * RB, out, smem); break;
-        case 8: rows_inv_item<T, 8>(g, it * RB, out, smem); break;
-        case 16: rows_inv_item<T, 16>(g, it * RB, out, smem); break;
-        }
-    }
+    for (int it = blockIdx.x; it < items; it += gridDim.x) rows_inv_item<T, P>(g, it * RB, out, smem);
 }
 
 __device__ __forceinline__ unsigned long long gtimer()
@@ -491,8 +493,8 @@ __device__ __forceinline__ unsigned long long gtimer()
 }
 
 // MINB blocks per SM: 2 caps the registers at 128 per thread
-template <typename T, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_engine_rk4(EngineArgs g)
+template <typename T, int P, int Q>
+__global__ void __launch_bounds__(256, 2) k_engine_rk4(EngineArgs g)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     cg::grid_group grid = cg::this_grid();
@@ -526,15 +528,15 @@ __global__ void __launch_bounds__(256, MINB) k_engine_rk4(EngineArgs g)
             TRACE();
             grid.sync();
             TRACE();
-            phase_rows_fwd<T>(g, smem);
+            phase_rows_fwd<T, P>(g, smem);
             TRACE();
             grid.sync();
             TRACE();
-            phase_cols<T>(g, smem);
+            phase_cols<T, Q>(g, smem);
             TRACE();
             grid.sync();
             TRACE();
-            phase_rows_inv<T>(g, (T*)g.raw[stage], smem);
+            phase_rows_inv<T, P>(g, (T*)g.raw[stage], smem);
             TRACE();
             grid.sync();
             TRACE();
@@ -599,46 +601,44 @@ void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s)
     k_split<<<b, 256, 0, s>>>(x, hi, lo, n);
 }
 
-// blocks per SM of the engine (FI_ENGINE_BPS=1 selects one, with up to 255 registers)
-static int engine_bps()
+typedef void (*EngineKernel)(EngineArgs);
+
+// h/32 and ny/32 in {4, 8, 16}
+template <typename T> EngineKernel engine_kernel(int P, int Q)
 {
-    const char* e = getenv("FI_ENGINE_BPS");
-    return (e && e[0] == '1') ? 1 : 2;
+#define EK(p, q) if (P == p && Q == q) return k_engine_rk4<T, p, q>;
+    EK(4, 4) EK(4, 8) EK(4, 16) EK(8, 4) EK(8, 8) EK(8, 16) EK(16, 4) EK(16, 8) EK(16, 16)
+#undef EK
+    return nullptr;
 }
 
 template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem)
 {
     // The plain FP64 form is FP64-throughput bound; it runs faster as the
     // multi-kernel graph (full occupancy) than in the one-grid engine.
-    if (sizeof(T) == 8 && !getenv("FI_ENGINE_FP64")) return 0;
-    typedef typename vec2<T>::type C2;
-    // warp transforms: h = nx/2 and ny powers of two with 64 <= len <= 512
-    auto ok_len = [](int L) { return L >= 64 && L <= 512 && (L & (L - 1)) == 0; };
-    if (!ok_len(p.h) || !ok_len(p.ny)) return 0;
-    int cb = (int)(16 / sizeof(C2));
-    if (cb < 1) cb = 1;
-    *CB = cb;
-    *smem = engine_smem_bytes<T>(p, cb);
+    if (sizeof(T) == 8) return 0;
+    if (p.h % 32 || p.ny % 32) return 0;
+    EngineKernel k = engine_kernel<T>(p.h / 32, p.ny / 32);
+    if (!k) return 0;
+    *CB = 1;
+    *smem = engine_smem_bytes<T>(p, 1);
     int dev = 0, nsm = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (*smem > (size_t)optin) return 0;
-    const int bps = engine_bps();
-    cudaError_t e1 = bps == 2 ? cudaFuncSetAttribute(k_engine_rk4<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem)
-                              : cudaFuncSetAttribute(k_engine_rk4<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
-    if (e1 != cudaSuccess) return 0;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess) return 0;
     int per_sm = 0;
-    cudaError_t e2 = bps == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T, 2>, 256, *smem)
-                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T, 1>, 256, *smem);
-    if (e2 != cudaSuccess || per_sm < 1) return 0;
-    if (per_sm > bps) per_sm = bps;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, *smem) != cudaSuccess || per_sm < 1) return 0;
+    if (per_sm > 2) per_sm = 2;
     *grid = per_sm * nsm;
     return 1;
 }
 
 template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, size_t smem, cudaStream_t s)
 {
+    EngineKernel k = engine_kernel<T>(g.p.h / 32, g.p.ny / 32);
+    if (!k) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(256);
@@ -649,13 +649,13 @@ template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, s
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (engine_bps() == 2) return cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 2>, g);
-    return cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 1>, g);
+    return cudaLaunchKernelEx(&cfg, k, g);
 }
 
 template size_t engine_smem_bytes<float>(const Plan2D&, int);
 template size_t engine_smem_bytes<double>(const Plan2D&, int);
 template int engine_config<float>(const Plan2D&, int*, int*, size_t*);
+template <> EngineKernel engine_kernel<double>(int, int) { return nullptr; }
 template int engine_config<double>(const Plan2D&, int*, int*, size_t*);
 template cudaError_t engine_launch<float>(const EngineArgs&, int, size_t, cudaStream_t);
 template cudaError_t engine_launch<double>(const EngineArgs&, int, size_t, cudaStream_t);
