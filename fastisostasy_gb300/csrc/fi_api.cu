@@ -114,7 +114,6 @@ struct fi_handle {
     int eng_grid = 0, eng_CB = 1;
     size_t eng_smem = 0;
     float *xhi = nullptr, *xlo = nullptr, *wrefhi = nullptr, *wreflo = nullptr;
-    void *ST = nullptr, *mAT = nullptr, *mBT = nullptr;   // engine spectrum / multipliers, column-contiguous
     unsigned long long* trace = nullptr;   // engine phase timestamps (fi_engine_trace)
     // optional per-kernel CUDA-event timing (fi_profile)
     bool prof_on = false;
@@ -470,15 +469,7 @@ int upload_static(fi_handle* h)
         for (int k = 0; k < nx; ++k)
             if (m(k, l) != m((nx - k) % nx, l) || m(k, l) != m(k, (ny - l) % ny)) { h->even = 0; break; }
     if ((rc = upload_T(h, h->mA, A)) || (rc = upload_T(h, h->mB, B))) return rc;
-    if (h->mAT) {
-        std::vector<double> At((size_t)(hh + 1) * ny), Bt((size_t)(hh + 1) * ny);
-        for (int l = 0; l < ny; ++l)
-            for (int k = 0; k <= hh; ++k) {
-                At[(size_t)k * ny + l] = A[(size_t)l * spitch + k];
-                Bt[(size_t)k * ny + l] = B[(size_t)l * spitch + k];
-            }
-        if ((rc = upload_T(h, h->mAT, At)) || (rc = upload_T(h, h->mBT, Bt))) return rc;
-    }
+
     if ((rc = upload(h, (void*)h->d.mactive, h->mact.data(), n))) return rc;
     return FI_OK;
 }
@@ -620,14 +611,12 @@ template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
     g.q0 = h->q0;
     g.D = h->Dt;
     g.inv2eta = h->inv2eta;
-    g.mA = h->mAT;
-    g.mB = h->mBT;
+    g.mA = h->mA;
+    g.mB = h->mB;
     g.even = h->even;
     g.mask = h->d.mactive;
     for (int i = 0; i < 4; ++i) g.raw[i] = h->raw[i];
     g.S = h->S;
-    g.ST = h->ST;
-    g.f = h->f;
     g.ctl = h->ctl;
     g.nsteps = nsteps;
     g.CB = h->eng_CB;
@@ -1029,12 +1018,6 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
 #define AL2(ptr, bytes) if ((rc = dalloc(h, &(ptr), (bytes)))) return rc
                 AL2(h->xhi, n * 4); AL2(h->xlo, n * 4); AL2(h->wrefhi, n * 4); AL2(h->wreflo, n * 4);
 #undef AL2
-            }
-            if (h->engine_ok) {
-                const size_t ns = (size_t)(h->prhs.h + 1) * h->ny;
-                if ((rc = dalloc(h, &h->ST, ns * 2 * tsz(h))) || (rc = dalloc(h, &h->mAT, ns * tsz(h))) ||
-                    (rc = dalloc(h, &h->mBT, ns * tsz(h))))
-                    return rc;
             }
         }
     }

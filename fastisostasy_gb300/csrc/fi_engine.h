@@ -22,14 +22,12 @@ struct EngineArgs {
     const void* q0;                  // RHS load term, field type
     const void* D;
     const void* inv2eta;
-    const void* mA;                  // 1/(kappa R) at (k, l), transposed like ST
-    const void* mB;                  // 1/(kappa R) at (-k, l), transposed like ST
+    const void* mA;
+    const void* mB;
     int even;
     const uint8_t* mask;
     void* raw[4];                    // stage outputs, field type
     void* S;                         // half spectrum, field type complex
-    void* f;                         // stencil output (field type), input of the row transform
-    void* ST;                        // engine spectrum, transposed: ST[k * ny + l]
     Ctl* ctl;
     int nsteps;
     int CB;                          // spectrum columns per phase-B item
