@@ -8,11 +8,13 @@ import os
 
 from . import build as _build
 
-FI_OK, FI_E_NAN, FI_E_LARGE, FI_E_STEP, FI_E_OOM, FI_E_CONFIG, FI_E_CUDA, FI_E_TIMEOUT, FI_E_ARG, FI_E_STATE = range(10)
+FI_OK, FI_E_NAN, FI_E_LARGE, FI_E_STEP, FI_E_OOM, FI_E_CONFIG, FI_E_CUDA, FI_E_TIMEOUT, FI_E_ARG, FI_E_STATE, \
+    FI_E_SIZE = range(11)
+FI_STATIC_MAX_N = 256
 FI_PREC_FP64, FI_PREC_MIXED = 0, 1
 
 ERRORS = {1: "FI_E_NAN", 2: "FI_E_LARGE", 3: "FI_E_STEP", 4: "FI_E_OOM", 5: "FI_E_CONFIG", 6: "FI_E_CUDA",
-          7: "FI_E_TIMEOUT", 8: "FI_E_ARG", 9: "FI_E_STATE"}
+          7: "FI_E_TIMEOUT", 8: "FI_E_ARG", 9: "FI_E_STATE", 10: "FI_E_SIZE"}
 
 FIELDS = {
     "z_bed": 0, "dwdt": 1, "w": 2, "we": 3, "Haf": 4, "Hice": 5, "z_ss": 6, "dz_ss": 7,
@@ -26,7 +28,7 @@ EXPORTS = ["fi_create", "fi_destroy", "fi_dims", "fi_set_fields", "fi_set_kernel
            "fi_init_state", "fi_update", "fi_update_async", "fi_synchronize", "fi_bsl_update",
            "fi_get_field", "fi_get_scalars", "fi_lvelva", "fi_convolve", "fi_state_size",
            "fi_state_export", "fi_state_import", "fi_last_error", "fi_version", "fi_stream",
-           "fi_launch_count", "fi_profile", "fi_profile_read", "fi_engine_trace"]
+           "fi_launch_count", "fi_profile", "fi_profile_read", "fi_engine_trace", "fi_lvelva_static"]
 
 PROFILE_KERNELS = ["flexure", "rows_fwd", "cols_hartley", "rows_inv", "conv_rows_fwd", "conv_cols",
                    "conv_rows_inv", "rk_stage", "rk_final", "upd_begin", "upd_masks", "upd_litho",
@@ -104,6 +106,9 @@ def load(build_if_missing: bool = True):
     L.fi_get_scalars.argtypes = [H, _dp]
     L.fi_lvelva.argtypes = [H, _dp, _dp, _dp]
     L.fi_convolve.argtypes = [H, C.c_int, _dp, _dp]
+    _v = C.c_void_p
+    L.fi_lvelva_static.argtypes = [_v, _v, _v, _v, _v, _v, _v, C.c_int, C.c_int, C.c_double, C.c_double,
+                                   C.c_double, C.c_double, C.c_double, _v, _v]
     L.fi_state_size.argtypes = [H]
     L.fi_state_size.restype = C.c_size_t
     L.fi_state_export.argtypes = [H, _dp]

@@ -42,7 +42,8 @@ enum {
     FI_E_CUDA = 6,     /* CUDA runtime error */
     FI_E_TIMEOUT = 7,  /* a bounded device wait expired */
     FI_E_ARG = 8,      /* invalid argument */
-    FI_E_STATE = 9     /* call out of order (e.g. update before init_state) */
+    FI_E_STATE = 9,    /* call out of order (e.g. update before init_state) */
+    FI_E_SIZE = 10     /* grid larger than fi_lvelva_static's scratch (or odd-sized) */
 };
 
 enum { FI_PREC_FP64 = 0, FI_PREC_MIXED = 1 };
@@ -149,6 +150,24 @@ int fi_lvelva(fi_handle* h, const double* w, const double* canom_full, double* d
 /* precomputed_fftconvolution (src/convolutions.f90:59-91) with the elastic
  * (kernel 0) or geoid (kernel 1) spectrum. */
 int fi_convolve(fi_handle* h, int kernel, const double* in_padded, double* out_padded);
+
+/* fi_lvelva_static has no counterpart in the reference: calc_lvelva
+ * (src/lv_elva.f90:31-126) for callers that may not allocate device memory.
+ * All arrays are DEVICE pointers of the caller, (nx, ny) with x fastest,
+ * double except the 0/1 mask; d_kappa and d_R are the cell-layout fields of
+ * calc_kappa / the viscous response (FI_FIELD_KAPPA, FI_FIELD_R).  The FP64
+ * work is queued on `stream` (a cudaStream_t, NULL = legacy default stream)
+ * and the call returns without waiting.  No device memory is allocated: the
+ * scratch is one static device array sized for nx, ny <= FI_STATIC_MAX_N
+ * (even, >= 4); other sizes return FI_E_SIZE.  The first call on a device
+ * (which must be current) looks up the array's address; make it before
+ * capturing any stream.  Calls that can overlap on one device race on the
+ * shared scratch and must be serialised by the caller. */
+#define FI_STATIC_MAX_N 256
+int fi_lvelva_static(const double* d_w, const double* d_canom_full, const uint8_t* d_maskactive,
+                     const double* d_D_lith, const double* d_eta_eff, const double* d_kappa, const double* d_R,
+                     int nx, int ny, double dx, double dy, double g, double nu, double sec_per_year,
+                     double* d_dwdt, void* stream);
 
 /* Restart support: the complete device state (fields + integrator clock) as
  * doubles; bit-identical round trip. */
