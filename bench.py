@@ -67,7 +67,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + q, "--format=csv,noheader,nounits",
-                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                       "-lms", "20"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
 
@@ -98,9 +98,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_bytes(kernel, dom, precision, stage_mode):
+def algorithmic_bytes(kernel, dom, precision, stage_mode, rk_steps=int(round(DTT / DT))):
     """Compulsory bytes one launch of `kernel` must move (inputs read once,
-    outputs written once) on the padded domain."""
+    outputs written once, intermediate FFT passes excluded) on the padded
+    domain.  Per cell, with s = 8 state bytes and f field bytes (8 plain, 4
+    mixed): one RK4 step with true stages reads the state and the four static
+    RHS fields at each of 4 stages, the previous stage output at 3 of them,
+    writes 4 stage outputs, and the final combination reads x and k1..k4 and
+    writes x: 6s + 27f."""
     f = 4 if precision == 1 else 8
     nx, ny = dom.nx, dom.ny
     n = nx * ny
@@ -119,8 +124,33 @@ def algorithmic_bytes(kernel, dom, precision, stage_mode):
         "conv_rows_inv": cspec_out + n * 8,
         "rk_stage": n * (8 + f + 8),
         "rk_final": n * (8 + 4 * f + 16),
+        "engine": n * rk_steps * (6 * 8 + 27 * f) if stage_mode == 1 else None,
     }
     return table.get(kernel)
+
+
+def update_bytes(dom, precision, rk_steps=int(round(DTT / DT))):
+    """Compulsory bytes of one whole coupling step per cell: rk_steps RK4
+    true-stage steps (6s + 27f), the elastic + geoid convolutions
+    (2 x [in f + kernel spectrum 4f + out f]) and the sea-level / mask pass
+    (about 15f + 3)."""
+    f = 4 if precision == 1 else 8
+    return dom.nx * dom.ny * (rk_steps * (6 * 8 + 27 * f) + 12 * f + 15 * f + 3)
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` (dram__bytes_read.sum +
+    dram__bytes_write.sum) from the committed ncu summaries in profiles/,
+    or None when no capture of it is committed."""
+    import glob
+    import re
+    pat = re.compile(r"traffic_per_launch\[%s\]\s*=\s*([0-9.eE+]+)" % re.escape(kernel))
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        with open(path) as fh:
+            m = pat.search(fh.read())
+        if m:
+            return float(m.group(1))
+    return None
 
 
 def make_domain(precision, stage_mode=1):
@@ -272,7 +302,7 @@ def reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=8)
@@ -338,6 +368,7 @@ def main():
     tot_ms, cnt = prof[dominant]
     alg = algorithmic_bytes(dominant, dom, 1, 1)
     achieved = alg / (tot_ms / cnt / 1000.0) / 1e9 if alg else None
+    upd = update_bytes(dom, 1)
     shares = {k: round(v[0] / sum(x[0] for x in prof.values()), 4) for k, v in prof.items()}
 
     # end to end through fi_update with host arrays (mixed form)
@@ -365,9 +396,12 @@ def main():
             "e2e": {"value": kyr(1000.0 * e2e_secs / args.steps), "unit": "kyr/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "frac": (achieved / peak) if achieved else None, "traffic": ncu_traffic(dominant),
                          "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,
-                         "avg_launch_us": 1000.0 * tot_ms / cnt, "kernel_time_shares": shares},
+                         "avg_launch_us": 1000.0 * tot_ms / cnt, "kernel_time_shares": shares,
+                         "whole_update": {"algorithmic_bytes": upd,
+                                          "achieved": upd / (r32["ms"] / 1000.0) / 1e9,
+                                          "frac": upd / (r32["ms"] / 1000.0) / 1e9 / peak}},
             "cpu_baseline": cpu,
             "clocks": r32["clocks"],
             "gpu_launches": r32["launches"],
