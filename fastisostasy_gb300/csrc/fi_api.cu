@@ -109,6 +109,8 @@ struct fi_handle {
     std::vector<GraphEntry> graphs;
     std::vector<long long> graph_seen;
     bool use_graphs = true;
+    bool tsit_graph_ok = true;         // Tsit5 attempts loop on the device inside captured graphs
+    bool require_tsit_graph = false;   // FI_REQUIRE_TSIT_GRAPH=1: no host-loop fallback (tests)
     // persistent cooperative RK4 engine (true stages, uniform spacing)
     bool engine_ok = false;
     int eng_grid = 0, eng_CB = 1;
@@ -123,6 +125,7 @@ struct fi_handle {
     double prof_ms[32] = {0};
     long long prof_cnt[32] = {0};
     cudaStream_t s = nullptr;
+    cudaStream_t s_body = nullptr;       // captures the body of the device Tsit5 loop
     std::vector<void*> allocs;
     std::string err;
     // host copies of the static fields
@@ -512,15 +515,18 @@ template <typename T> struct TT {
     typedef typename vec2<T>::type C2;
 };
 
-template <typename T> void rhs(fi_handle* h, const double* y, const double* wref, T* raw_out)
+// gate: optional device flag; the four kernels return at once when it is 0
+template <typename T>
+void rhs(fi_handle* h, const double* y, const double* wref, T* raw_out, const int* gate = nullptr)
 {
     typedef typename vec2<T>::type C2;
     PROF(h, K_FLEX, launch_flexure<T>(y, wref, (const T*)h->q0, h->d.mactive, (const T*)h->Dt, (const T*)h->inv2eta,
-                                      (T*)h->f, h->nx, h->ny, h->fc, h->s));
-    PROF(h, K_ROWS_FWD, launch_rows_fwd<T>((const T*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, h->prhs, h->s));
-    PROF(h, K_COLS_HARTLEY, launch_cols_hartley<T>((C2*)h->S, (const T*)h->mA, (const T*)h->mB, h->even, h->prhs, h->s));
+                                      (T*)h->f, h->nx, h->ny, h->fc, h->s, gate));
+    PROF(h, K_ROWS_FWD, launch_rows_fwd<T>((const T*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, h->prhs, h->s, gate));
+    PROF(h, K_COLS_HARTLEY,
+         launch_cols_hartley<T>((C2*)h->S, (const T*)h->mA, (const T*)h->mB, h->even, h->prhs, h->s, gate));
     const double norm = (double)(float)((long long)h->nx * h->ny);   // nx*ny*1. (default real)
-    PROF(h, K_ROWS_INV, launch_rows_inv<T>((const C2*)h->S, raw_out, h->prhs, 1.0 / norm, h->s));
+    PROF(h, K_ROWS_INV, launch_rows_inv<T>((const C2*)h->S, raw_out, h->prhs, 1.0 / norm, h->s, gate));
     h->launches += 4;
 }
 
@@ -657,6 +663,49 @@ template <typename T> int integrate_tsit(fi_handle* h, double tf, int* have_rhs,
     return FI_OK;
 }
 
+// The same attempts as integrate_tsit, enqueued during stream capture as the
+// body of a CUDA graph WHILE node: the accept/reject decisions stay on the
+// device.  Only valid while h->s is capturing.
+const int kMaxAttempts = 10000000;
+template <typename T> int enqueue_tsit_loop(fi_handle* h)
+{
+    const fi_params& p = h->p;
+    if (p.stage_mode == 1) return fail(h, FI_E_CONFIG, "tsit54 with true stages is not available on the device yet");
+    T* r0 = (T*)h->raw[0];
+    ts_loop_begin(h->ctl, h->s);
+    h->launches += 1;
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(h->s, &st, nullptr, &g, &deps, nullptr, &nd));
+    if (st != cudaStreamCaptureStatusActive) return fail(h, FI_E_CUDA, "tsit54 loop: stream is not capturing");
+    cudaGraphConditionalHandle loop;
+    CK(cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CK(cudaStreamUpdateCaptureDependencies(h->s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    CK(cudaStreamBeginCaptureToGraph(h->s_body, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    cudaStream_t s0 = h->s;
+    h->s = h->s_body;
+    ts_attempt_begin(h->ctl, kMaxAttempts, h->s);
+    rhs<T>(h, h->d.w, nullptr, r0, &h->ctl->need_rhs);
+    ts_max<T>(h->d, r0, p.atol, p.rtol, h->s);
+    ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s);
+    ts_commit<T>(h->d, r0, h->s);
+    ts_attempt_end(h->ctl, loop, h->s);
+    h->launches += 5;
+    h->s = s0;
+    cudaGraph_t body_out = nullptr;
+    CK(cudaStreamEndCapture(h->s_body, &body_out));
+    return FI_OK;
+}
+
 // Kernels of isos_update before the integrator (src/fastisostasy.f90:750-833).
 template <typename T> void enqueue_pre(fi_handle* h, const double* dH, bool diag, bool run_integrator)
 {
@@ -700,26 +749,37 @@ template <typename T> int update_T(fi_handle* h, const double* dH, double time, 
         h->time_diag = h->time_diag + p.dt_diagnostics;
     }
     h->time_prog = time;
-    if (p.dt_method == 2 && run_integrator) {
-        enqueue_pre<T>(h, dH, diag, true);
-        int have_rhs = 0;
-        T* raw_last = nullptr;
-        int rc = integrate_tsit<T>(h, time, &have_rhs, &raw_last);
-        if (rc) return rc;
-        enqueue_post<T>(h, raw_last, have_rhs);
-        CK(cudaGetLastError());
-        return FI_OK;
-    }
-    const int nsteps = run_integrator ? plan_steps(h, time) : 0;
-    const long long key = ((long long)nsteps << 4) | ((diag ? 1 : 0) << 1) | (run_integrator ? 1 : 0) |
-                          ((long long)(dH == h->dH) << 2);
-    auto enqueue = [&]() {
+    const bool tsit = p.dt_method == 2 && run_integrator;
+    const int nsteps = (run_integrator && !tsit) ? plan_steps(h, time) : 0;
+    const long long key = ((long long)nsteps << 4) | ((long long)tsit << 3) | ((long long)(dH == h->dH) << 2) |
+                          ((diag ? 1 : 0) << 1) | (run_integrator ? 1 : 0);
+    // eager: Tsit5 attempts are decided on the host (one wait per attempt)
+    auto enqueue = [&]() -> int {
         enqueue_pre<T>(h, dH, diag, run_integrator);
+        if (tsit) {
+            int have_rhs = 0;
+            T* raw_last = nullptr;
+            const int rc = integrate_tsit<T>(h, time, &have_rhs, &raw_last);
+            if (rc) return rc;
+            enqueue_post<T>(h, raw_last, have_rhs);
+            return FI_OK;
+        }
         T* raw_last = (h->engine_ok && nsteps > 0) ? enqueue_engine<T>(h, nsteps) : enqueue_steps<T>(h, nsteps);
         enqueue_post<T>(h, raw_last, nsteps > 0 ? 1 : 0);
+        return FI_OK;
     };
-    if (!h->use_graphs || h->prof_on) {
-        enqueue();
+    // captured: Tsit5 attempts loop on the device (graph WHILE node)
+    auto enqueue_captured = [&]() -> int {
+        if (!tsit) return enqueue();
+        enqueue_pre<T>(h, dH, diag, true);
+        const int rc = enqueue_tsit_loop<T>(h);
+        if (rc) return rc;
+        enqueue_post<T>(h, (T*)h->raw[0], -1);
+        return FI_OK;
+    };
+    if (!h->use_graphs || h->prof_on || (tsit && !h->tsit_graph_ok)) {
+        const int rc = enqueue();
+        if (rc) return rc;
         CK(cudaGetLastError());
         return FI_OK;
     }
@@ -734,16 +794,32 @@ template <typename T> int update_T(fi_handle* h, const double* dH, double time, 
     if (!seen) {
         // first occurrence runs eagerly (also sets kernel attributes)
         h->graph_seen.push_back(key);
-        enqueue();
+        const int rc = enqueue();
+        if (rc) return rc;
         CK(cudaGetLastError());
         return FI_OK;
     }
     const long long l0 = h->launches;
     CK(cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
-    enqueue();
+    const int rc = enqueue_captured();
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(h->s, &graph);
-    if (e != cudaSuccess) return fail(h, FI_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    if (rc || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (tsit && rc != FI_E_CONFIG && !h->require_tsit_graph) {
+            // no conditional graph nodes here: keep deciding Tsit5 attempts on the host
+            h->tsit_graph_ok = false;
+            h->err.clear();
+            h->launches = l0;
+            const int rc2 = enqueue();
+            if (rc2) return rc2;
+            CK(cudaGetLastError());
+            return FI_OK;
+        }
+        if (rc) return rc;
+        return fail(h, FI_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    }
     fi_handle::GraphEntry ge;
     ge.key = key;
     ge.nkernels = h->launches - l0;
@@ -889,7 +965,13 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
         for (size_t e = 0; e < h->n; ++e) { h->K[e] = K_or_null[e]; if (h->K[e] != 1.0) h->uniform = 0; }
     }
     if (cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking) != cudaSuccess) { delete h; return FI_E_CUDA; }
+    if (cudaStreamCreateWithFlags(&h->s_body, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(h->s);
+        delete h;
+        return FI_E_CUDA;
+    }
     if (const char* ev = getenv("FI_NO_GRAPHS")) h->use_graphs = !(ev[0] == '1');
+    if (const char* ev = getenv("FI_REQUIRE_TSIT_GRAPH")) h->require_tsit_graph = (ev[0] == '1');
     *out = h;
     host_fields(h);
 
@@ -1044,6 +1126,7 @@ int fi_destroy(fi_handle* h)
     for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
     if (h->s) cudaStreamDestroy(h->s);
+    if (h->s_body) cudaStreamDestroy(h->s_body);
     delete h;
     return FI_OK;
 }

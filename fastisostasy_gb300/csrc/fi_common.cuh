@@ -57,10 +57,12 @@ struct Ctl {
     double red[8];             // scratch results of grid reductions
     int done;                  // t >= tf for the current update
     int accepted;              // last adaptive attempt accepted
-    int rhs_valid;             // cached RHS matches the current state (reference mode)
+    int rhs_valid;             // device Tsit5 loop: raw[0] holds the RHS of the current state
     int status;                // FI_* error code raised on the device
     int bsl_method;
-    int pad_[3];
+    int need_rhs;              // device Tsit5 loop: gate of the RHS kernels for this attempt
+    int have_rhs;              // device Tsit5 loop: an RHS was evaluated during this update
+    int loop_iter;             // device Tsit5 loop: attempts during this update
     long long n_accept, n_reject, n_rhs, n_attempt;
     unsigned int counter[8];   // last-block arrival counters of grid reductions
 };

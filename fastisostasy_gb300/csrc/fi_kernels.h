@@ -33,20 +33,24 @@ struct Plan2D {
     const float2* rtw32;
 };
 
+// The RHS launchers take an optional device flag: when it points at 0 every
+// block returns at once (device-side skipping inside a graph loop).
 template <typename T>
 void launch_flexure(const double* y, const double* wref, const T* q0, const uint8_t* mask, const T* D,
-                    const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s);
+                    const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s,
+                    const int* gate = nullptr);
 
 template <typename T>
 void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, typename vec2<T>::type* S,
-                     const Plan2D& p, cudaStream_t s);
+                     const Plan2D& p, cudaStream_t s, const int* gate = nullptr);
 
 template <typename T>
 void launch_cols_hartley(typename vec2<T>::type* S, const T* mA, const T* mB, int even, const Plan2D& p,
-                         cudaStream_t s);
+                         cudaStream_t s, const int* gate = nullptr);
 
 template <typename T>
-void launch_rows_inv(const typename vec2<T>::type* S, T* out, const Plan2D& p, double scale, cudaStream_t s);
+void launch_rows_inv(const typename vec2<T>::type* S, T* out, const Plan2D& p, double scale, cudaStream_t s,
+                     const int* gate = nullptr);
 
 // Convolution: columns forward (rows >= nrows_in are zero), multiply by the
 // kernel spectrum K (same layout as S), inverse; only rows listed in

@@ -72,8 +72,9 @@ template <typename T>
 __global__ void __launch_bounds__(TX* TY)
 k_flexure(const double* __restrict__ y, const double* __restrict__ wref, const T* __restrict__ q0,
           const uint8_t* __restrict__ mask, const T* __restrict__ D, const T* __restrict__ inv2eta,
-          T* __restrict__ f, int nx, int ny, FlexCoef c)
+          T* __restrict__ f, int nx, int ny, FlexCoef c, const int* __restrict__ gate)
 {
+    if (gate && *gate == 0) return;
     __shared__ double ys[RY][RX];
     __shared__ T wx[RY][RX];
     __shared__ T Mxx[RY][RX];
@@ -194,8 +195,9 @@ struct FlexCoefF {
 __global__ void __launch_bounds__(TX* TY)
 k_flexure_f32(const double* __restrict__ y, const double* __restrict__ wref, const float* __restrict__ q0,
               const uint8_t* __restrict__ mask, const float* __restrict__ D, const float* __restrict__ inv2eta,
-              float* __restrict__ f, int nx, int ny, FlexCoefF c)
+              float* __restrict__ f, int nx, int ny, FlexCoefF c, const int* __restrict__ gate)
 {
+    if (gate && *gate == 0) return;
     __shared__ double ys[RY][RX];
     __shared__ float dX[RY][RX];
     __shared__ float dY[RY][RX];
@@ -284,7 +286,7 @@ k_flexure_f32(const double* __restrict__ y, const double* __restrict__ wref, con
 
 template <typename T>
 void launch_flexure(const double* y, const double* wref, const T* q0, const uint8_t* mask, const T* D,
-                    const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s)
+                    const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s, const int* gate)
 {
     dim3 b(TX, TY), g((nx + TX - 1) / TX, (ny + TY - 1) / TY);
     if (sizeof(T) == 4 && c.dxm == nullptr) {
@@ -299,10 +301,10 @@ void launch_flexure(const double* y, const double* wref, const T* q0, const uint
         cf.inv_2dy = (float)c.inv_2dy;
         cf.inv_dy2 = (float)c.inv_dy2;
         k_flexure_f32<<<g, b, 0, s>>>(y, wref, (const float*)q0, mask, (const float*)D, (const float*)inv2eta,
-                                      (float*)f, nx, ny, cf);
+                                      (float*)f, nx, ny, cf, gate);
         return;
     }
-    k_flexure<T><<<g, b, 0, s>>>(y, wref, q0, mask, D, inv2eta, f, nx, ny, c);
+    k_flexure<T><<<g, b, 0, s>>>(y, wref, q0, mask, D, inv2eta, f, nx, ny, c, gate);
 }
 
 // ---------------------------------------------------------------------------
@@ -325,8 +327,9 @@ static int threads_for(int work)
 
 template <typename T>
 __global__ void k_rows_fwd(const T* __restrict__ in, int in_pitch, int in_width, int nrows_in,
-                           typename vec2<T>::type* __restrict__ S, Plan2D p, int RB)
+                           typename vec2<T>::type* __restrict__ S, Plan2D p, int RB, const int* __restrict__ gate)
 {
+    if (gate && *gate == 0) return;
     typedef typename vec2<T>::type C2;
     extern __shared__ unsigned char smem_raw[];
     C2* b0 = reinterpret_cast<C2*>(smem_raw);
@@ -370,20 +373,21 @@ __global__ void k_rows_fwd(const T* __restrict__ in, int in_pitch, int in_width,
 
 template <typename T>
 void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, typename vec2<T>::type* S,
-                     const Plan2D& p, cudaStream_t s)
+                     const Plan2D& p, cudaStream_t s, const int* gate)
 {
     typedef typename vec2<T>::type C2;
     const int RB = rows_per_block(p.h);
     const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
     set_smem(k_rows_fwd<T>, sm);
     const int nblk = (nrows_in + RB - 1) / RB;
-    k_rows_fwd<T><<<nblk, threads_for(RB * p.h / 4), sm, s>>>(in, in_pitch, in_width, nrows_in, S, p, RB);
+    k_rows_fwd<T><<<nblk, threads_for(RB * p.h / 4), sm, s>>>(in, in_pitch, in_width, nrows_in, S, p, RB, gate);
 }
 
 template <typename T>
 __global__ void k_rows_inv(const typename vec2<T>::type* __restrict__ S, int nrows, T* __restrict__ out,
-                           int out_pitch, Plan2D p, int RB, T scale)
+                           int out_pitch, Plan2D p, int RB, T scale, const int* __restrict__ gate)
 {
+    if (gate && *gate == 0) return;
     typedef typename vec2<T>::type C2;
     extern __shared__ unsigned char smem_raw[];
     C2* b0 = reinterpret_cast<C2*>(smem_raw);
@@ -422,14 +426,15 @@ __global__ void k_rows_inv(const typename vec2<T>::type* __restrict__ S, int nro
 }
 
 template <typename T>
-void launch_rows_inv(const typename vec2<T>::type* S, T* out, const Plan2D& p, double scale, cudaStream_t s)
+void launch_rows_inv(const typename vec2<T>::type* S, T* out, const Plan2D& p, double scale, cudaStream_t s,
+                     const int* gate)
 {
     typedef typename vec2<T>::type C2;
     const int RB = rows_per_block(p.h);
     const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
     set_smem(k_rows_inv<T>, sm);
     const int nblk = (p.ny + RB - 1) / RB;
-    k_rows_inv<T><<<nblk, threads_for(RB * p.h / 4), sm, s>>>(S, p.ny, out, p.nx, p, RB, (T)scale);
+    k_rows_inv<T><<<nblk, threads_for(RB * p.h / 4), sm, s>>>(S, p.ny, out, p.nx, p, RB, (T)scale, gate);
 }
 
 // ---------------------------------------------------------------------------
@@ -464,8 +469,9 @@ __device__ __forceinline__ void load_cols(typename vec2<T>::type* b0, const type
 
 template <typename T>
 __global__ void k_cols_hartley(typename vec2<T>::type* __restrict__ S, const T* __restrict__ mA,
-                               const T* __restrict__ mB, int even, Plan2D p, int CB)
+                               const T* __restrict__ mB, int even, Plan2D p, int CB, const int* __restrict__ gate)
 {
+    if (gate && *gate == 0) return;
     typedef typename vec2<T>::type C2;
     extern __shared__ unsigned char smem_raw[];
     const int ny = p.col.d.n;
@@ -518,14 +524,14 @@ __global__ void k_cols_hartley(typename vec2<T>::type* __restrict__ S, const T* 
 
 template <typename T>
 void launch_cols_hartley(typename vec2<T>::type* S, const T* mA, const T* mB, int even, const Plan2D& p,
-                         cudaStream_t s)
+                         cudaStream_t s, const int* gate)
 {
     typedef typename vec2<T>::type C2;
     const int CB = cols_per_block<T>(p.ny);
     const size_t sm = 2 * (size_t)CB * p.ny * sizeof(C2);
     set_smem(k_cols_hartley<T>, sm);
     const int nblk = (p.h + 1 + CB - 1) / CB;
-    k_cols_hartley<T><<<nblk, threads_for(CB * p.ny / 4), sm, s>>>(S, mA, mB, even, p, CB);
+    k_cols_hartley<T><<<nblk, threads_for(CB * p.ny / 4), sm, s>>>(S, mA, mB, even, p, CB, gate);
 }
 
 template <typename T>
@@ -658,10 +664,12 @@ void launch_conv_rows_inv(const typename vec2<T>::type* S, int n_out, double* ou
 
 #define FI_INST(T)                                                                                            \
     template void launch_flexure<T>(const double*, const double*, const T*, const uint8_t*, const T*, const T*, \
-                                    T*, int, int, const FlexCoef&, cudaStream_t);                             \
-    template void launch_rows_fwd<T>(const T*, int, int, int, vec2<T>::type*, const Plan2D&, cudaStream_t);   \
-    template void launch_cols_hartley<T>(vec2<T>::type*, const T*, const T*, int, const Plan2D&, cudaStream_t); \
-    template void launch_rows_inv<T>(const vec2<T>::type*, T*, const Plan2D&, double, cudaStream_t);          \
+                                    T*, int, int, const FlexCoef&, cudaStream_t, const int*);                 \
+    template void launch_rows_fwd<T>(const T*, int, int, int, vec2<T>::type*, const Plan2D&, cudaStream_t,    \
+                                     const int*);                                                             \
+    template void launch_cols_hartley<T>(vec2<T>::type*, const T*, const T*, int, const Plan2D&, cudaStream_t, \
+                                         const int*);                                                         \
+    template void launch_rows_inv<T>(const vec2<T>::type*, T*, const Plan2D&, double, cudaStream_t, const int*); \
     template void launch_cols_conv<T>(vec2<T>::type*, const vec2<T>::type*, int, const int*, int, const Plan2D&, \
                                       cudaStream_t);                                                          \
     template void launch_cols_fwd<T>(vec2<T>::type*, int, const Plan2D&, cudaStream_t);                       \

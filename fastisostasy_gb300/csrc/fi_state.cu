@@ -439,6 +439,42 @@ k_ts_err(Dom d, const T* __restrict__ raw, double q, double dt_max, int max_reje
     }
 }
 
+// Device-side attempt loop of the reference-compatible Tsit5: the attempts
+// of one update run as the body of a CUDA graph WHILE node, so the host never
+// waits on an accept/reject decision.  The body is
+//   k_ts_attempt_begin, [RHS kernels gated by need_rhs], ts_max, ts_err,
+//   ts_commit, k_ts_attempt_end
+// and makes the same decisions, in the same order, as the host loop.
+__global__ void k_ts_loop_begin(Ctl* c)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    c->rhs_valid = 0;
+    c->have_rhs = 0;
+    c->loop_iter = 0;
+    c->need_rhs = 0;
+}
+
+__global__ void k_ts_attempt_begin(Ctl* c, int max_iter)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double tf = c->tf;
+    if (c->status != ST_OK || !(c->t < tf)) { c->done = 1; c->need_rhs = 0; return; }
+    if (++c->loop_iter > max_iter) { c->status = ST_STEP; c->done = 1; c->need_rhs = 0; return; }
+    c->done = 0;
+    c->dt = fmin(c->dt, tf - c->t);
+    c->h = c->dt;
+    c->need_rhs = c->rhs_valid ? 0 : 1;
+    if (c->need_rhs) { c->have_rhs = 1; c->rhs_valid = 1; }
+}
+
+__global__ void k_ts_attempt_end(Ctl* c, cudaGraphConditionalHandle loop)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (!c->done && c->accepted) c->rhs_valid = 0;   // the state moved: the next attempt needs a new RHS
+    const unsigned more = (!c->done && c->status == ST_OK && c->t < c->tf) ? 1u : 0u;
+    cudaGraphSetConditional(loop, more);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NT) k_ts_commit(Dom d, const T* __restrict__ raw)
 {
@@ -459,8 +495,10 @@ __global__ void __launch_bounds__(NT) k_ts_commit(Dom d, const T* __restrict__ r
 // w -= corner mean (apply_zerobc_at_corners), canom_mantle, z_bed, dwdt output,
 // instability and NaN checks (src/fastisostasy.f90:856-869, :874-899).
 template <typename T>
-__global__ void __launch_bounds__(NT) k_upd_end(Dom d, const T* __restrict__ raw_last, int have_rhs)
+__global__ void __launch_bounds__(NT) k_upd_end(Dom d, const T* __restrict__ raw_last, int have_rhs_arg)
 {
+    // have_rhs_arg < 0: the update ran the device Tsit5 loop, which recorded it
+    const int have_rhs = have_rhs_arg >= 0 ? have_rhs_arg : d.ctl->have_rhs;
     __shared__ double s_c[2];
     if (threadIdx.x == 0) {
         s_c[0] = corner_mean_of(d.w, d.nx, d.ny);
@@ -585,6 +623,12 @@ void set_args(Ctl* c, double tf, double bsl, double A_ocean, int method, int wri
 }
 void step_begin(Ctl* c, int kind, cudaStream_t s) { k_step_begin<<<1, 32, 0, s>>>(c, kind); }
 void step_end(Ctl* c, cudaStream_t s) { k_step_end<<<1, 32, 0, s>>>(c); }
+void ts_loop_begin(Ctl* c, cudaStream_t s) { k_ts_loop_begin<<<1, 32, 0, s>>>(c); }
+void ts_attempt_begin(Ctl* c, int max_iter, cudaStream_t s) { k_ts_attempt_begin<<<1, 32, 0, s>>>(c, max_iter); }
+void ts_attempt_end(Ctl* c, cudaGraphConditionalHandle loop, cudaStream_t s)
+{
+    k_ts_attempt_end<<<1, 32, 0, s>>>(c, loop);
+}
 template <typename T>
 void rk_stage(const Ctl* c, double* y, const double* x, const T* raw, double a, int nx, int ny, double spy,
               cudaStream_t s)

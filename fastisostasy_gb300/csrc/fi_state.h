@@ -41,6 +41,10 @@ void upd_load(const Dom& d, const double* dz_raw, const double* corners, int dz_
 void set_args(Ctl* c, double tf, double bsl, double A_ocean, int method, int write_bsl, cudaStream_t s);
 void step_begin(Ctl* c, int kind, cudaStream_t s);
 void step_end(Ctl* c, cudaStream_t s);
+// device-side Tsit5 attempt loop (body of a CUDA graph WHILE node)
+void ts_loop_begin(Ctl* c, cudaStream_t s);
+void ts_attempt_begin(Ctl* c, int max_iter, cudaStream_t s);
+void ts_attempt_end(Ctl* c, cudaGraphConditionalHandle loop, cudaStream_t s);
 template <typename T>
 void rk_stage(const Ctl* c, double* y, const double* x, const T* raw, double a, int nx, int ny, double spy,
               cudaStream_t s);
@@ -53,6 +57,7 @@ template <typename T> void ts_max(const Dom& d, const T* raw, double atol, doubl
 template <typename T>
 void ts_err(const Dom& d, const T* raw, double q, double dt_max, int max_reject, cudaStream_t s);
 template <typename T> void ts_commit(const Dom& d, const T* raw, cudaStream_t s);
+// have_rhs < 0: read it from the control block (device Tsit5 loop)
 template <typename T> void upd_end(const Dom& d, const T* raw_last, int have_rhs, cudaStream_t s);
 void gather(const double* const* src, const uint8_t* const* msrc, int nf, int nm, const Dom& d, double* out,
             cudaStream_t s);

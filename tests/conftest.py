@@ -9,5 +9,10 @@ for p in (ROOT, os.path.join(ROOT, "tests")):
         sys.path.insert(0, p)
 
 
+# The device-side Tsit5 attempt loop must be the path the tests exercise:
+# a failed capture of it is an error here, not a silent host-loop run.
+os.environ.setdefault("FI_REQUIRE_TSIT_GRAPH", "1")
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
