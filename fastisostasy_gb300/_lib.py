@@ -28,7 +28,9 @@ EXPORTS = ["fi_create", "fi_destroy", "fi_dims", "fi_set_fields", "fi_set_kernel
            "fi_init_state", "fi_update", "fi_update_async", "fi_synchronize", "fi_bsl_update",
            "fi_get_field", "fi_get_scalars", "fi_lvelva", "fi_convolve", "fi_state_size",
            "fi_state_export", "fi_state_import", "fi_last_error", "fi_version", "fi_stream",
-           "fi_launch_count", "fi_profile", "fi_profile_read", "fi_engine_trace", "fi_lvelva_static"]
+           "fi_launch_count", "fi_profile", "fi_profile_read", "fi_engine_trace", "fi_lvelva_static",
+           "fi_padded_dims", "fi_serve_create", "fi_serve_submit", "fi_serve_info", "fi_serve_wait",
+           "fi_serve_result", "fi_serve_clock", "fi_serve_destroy"]
 
 PROFILE_KERNELS = ["flexure", "rows_fwd", "cols_hartley", "rows_inv", "conv_rows_fwd", "conv_cols",
                    "conv_rows_inv", "rk_stage", "rk_final", "upd_begin", "upd_masks", "upd_litho",
@@ -70,6 +72,18 @@ _u8 = C.POINTER(C.c_uint8)
 class FiOut(C.Structure):
     _fields_ = [(k, _dp) for k in ("z_bed", "z_ss", "dz_ss", "w", "we", "dwdt", "canom_full", "Hice")] + \
                [(k, _u8) for k in ("maskocean", "maskgrounded", "maskcontinent")]
+
+
+class FiRequest(C.Structure):
+    _fields_ = [("p", FiParams), ("nx_ice", C.c_int32), ("ny_ice", C.c_int32), ("dx", C.c_double),
+                ("dy", C.c_double), ("z_bed", _dp), ("H_ref", _dp), ("H_ice", _dp), ("D_lith", _dp), ("eta_eff", _dp),
+                ("R", _dp), ("maskactive", _u8), ("t0", C.c_double), ("t_end", C.c_double),
+                ("dtt", C.c_double), ("bsl", C.c_double)]
+
+
+class FiRequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("updates", C.c_int64), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double), ("error", C.c_char * 128)]
 
 
 _LIB = None
@@ -120,6 +134,16 @@ def load(build_if_missing: bool = True):
     L.fi_engine_trace.argtypes = [H, C.c_void_p, C.c_int]
     L.fi_profile.argtypes = [H, C.c_int]
     L.fi_profile_read.argtypes = [H, _dp, C.POINTER(C.c_longlong), C.c_int]
+    L.fi_padded_dims.argtypes = [C.POINTER(FiParams), C.c_int, C.c_int, C.c_double, C.c_double,
+                                 C.POINTER(C.c_int32)]
+    L.fi_serve_create.argtypes = [C.c_int, C.c_double, C.POINTER(H)]
+    L.fi_serve_submit.argtypes = [H, C.POINTER(FiRequest), C.POINTER(C.c_uint64)]
+    L.fi_serve_info.argtypes = [H, C.c_uint64, C.POINTER(FiRequestInfo)]
+    L.fi_serve_wait.argtypes = [H, C.c_uint64, C.c_double, C.POINTER(FiRequestInfo)]
+    L.fi_serve_result.argtypes = [H, C.c_uint64, _dp, _dp]
+    L.fi_serve_clock.argtypes = [H]
+    L.fi_serve_clock.restype = C.c_double
+    L.fi_serve_destroy.argtypes = [H]
     L.fi_last_error.argtypes = [H]
     L.fi_last_error.restype = C.c_char_p
     _LIB = L

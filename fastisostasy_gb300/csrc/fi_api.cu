@@ -71,12 +71,16 @@ const float kGe[42] = {-33.6488f, -33.64f, -33.56f, -32.75f, -31.86f, -30.98f, -
 
 double ge_value(double r)
 {
-    static double rn[42], ge[42];
-    static bool ready = false;
-    if (!ready) {
-        for (int k = 0; k < 42; ++k) { rn[k] = (double)(kRn[k] * 1.e3f); ge[k] = (double)kGe[k]; }
-        ready = true;
-    }
+    struct Tab {
+        double rn[42], ge[42];
+        Tab()
+        {
+            for (int k = 0; k < 42; ++k) { rn[k] = (double)(kRn[k] * 1.e3f); ge[k] = (double)kGe[k]; }
+        }
+    };
+    static const Tab tab;   // initialised once, thread-safe
+    const double* rn = tab.rn;
+    const double* ge = tab.ge;
     if (r > rn[41]) return 0.0;
     int k = 0;
     while (k < 41 && !(r >= rn[k] && r < rn[k + 1])) ++k;
@@ -906,14 +910,60 @@ int fi_profile_read(fi_handle* h, double* ms, long long* counts, int n)
 
 const char* fi_last_error(const fi_handle* h) { return h ? h->err.c_str() : "null handle"; }
 
+namespace {
+// init_domain_size (src/isos_utils.f90:285-354): padded size and 1-based crop
+// window {nx, ny, icrop1, icrop2, jcrop1, jcrop2}; allocates nothing.
+int padded_domain(const fi_params& p, int nx_ice, int ny_ice, double dx, double dy, int* pd)
+{
+    if (p.method != 3 || nx_ice < 3 || ny_ice < 3 || p.nl < 1 || p.nl > 8) return FI_E_CONFIG;
+    if (dx != dy || p.min_pad < 0.0) return FI_E_CONFIG;   // src/isos_utils.f90:292-300
+    int nx_tmp = nx_ice, ny_tmp = ny_ice, npx, npy, nx, ny;
+    int icrop1 = 1, jcrop1 = 1;
+    if (nx_ice % 2) { icrop1++; nx_tmp++; }
+    if (ny_ice % 2) { jcrop1++; ny_tmp++; }
+    if (p.nx_target > 0 && p.ny_target > 0) {
+        if (p.nx_target < nx_tmp || p.ny_target < ny_tmp || (p.nx_target - nx_tmp) % 2 || (p.ny_target - ny_tmp) % 2)
+            return FI_E_CONFIG;
+        npx = (p.nx_target - nx_tmp) / 2;
+        npy = (p.ny_target - ny_tmp) / 2;
+        nx = p.nx_target;
+        ny = p.ny_target;
+    } else {
+        const int npxy = (int)std::lround(p.min_pad / dx);
+        npx = npy = npxy;
+        if (nx_tmp < ny_tmp) npx += (ny_tmp - nx_tmp) / 2;
+        else if (nx_tmp > ny_tmp) npy += (nx_tmp - ny_tmp) / 2;
+        nx = nx_tmp + 2 * npx;
+        ny = ny_tmp + 2 * npy;
+    }
+    if (nx > 2048 || ny > 2048) return FI_E_CONFIG;   // column FFT of 2n must fit in shared memory
+    pd[0] = nx;
+    pd[1] = ny;
+    pd[2] = icrop1 + npx;
+    pd[3] = nx - npx;
+    pd[4] = jcrop1 + npy;
+    pd[5] = ny - npy;
+    return FI_OK;
+}
+}  // namespace
+
+int fi_padded_dims(const fi_params* p, int nx_ice, int ny_ice, double dx, double dy, int32_t* out6)
+{
+    if (!p || !out6) return FI_E_ARG;
+    int pd[6];
+    if (int rc = padded_domain(*p, nx_ice, ny_ice, dx, dy, pd)) return rc;
+    for (int i = 0; i < 6; ++i) out6[i] = pd[i];
+    return FI_OK;
+}
+
 int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy, const double* K_or_null,
               fi_handle** out)
 {
     if (!pin || !out) return FI_E_ARG;
     *out = nullptr;
     const fi_params& p = *pin;
-    if (p.method != 3 || nx_ice < 3 || ny_ice < 3 || p.nl < 1 || p.nl > 8) return FI_E_CONFIG;
-    if (dx != dy || p.min_pad < 0.0) return FI_E_CONFIG;   // init_domain_size, src/isos_utils.f90:292-300
+    int pd[6];
+    if (int rc = padded_domain(p, nx_ice, ny_ice, dx, dy, pd)) return rc;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return FI_E_CUDA;
     fi_handle* h = new fi_handle();
@@ -922,34 +972,12 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     h->dy = dy;
     h->nx_ice = nx_ice;
     h->ny_ice = ny_ice;
-    // init_domain_size
-    int nx_tmp = nx_ice, ny_tmp = ny_ice, npx, npy;
-    h->icrop1 = 1;
-    h->jcrop1 = 1;
-    if (nx_ice % 2) { h->icrop1++; nx_tmp++; }
-    if (ny_ice % 2) { h->jcrop1++; ny_tmp++; }
-    if (p.nx_target > 0 && p.ny_target > 0) {
-        if (p.nx_target < nx_tmp || p.ny_target < ny_tmp || (p.nx_target - nx_tmp) % 2 || (p.ny_target - ny_tmp) % 2) {
-            delete h;
-            return FI_E_CONFIG;
-        }
-        npx = (p.nx_target - nx_tmp) / 2;
-        npy = (p.ny_target - ny_tmp) / 2;
-        h->nx = p.nx_target;
-        h->ny = p.ny_target;
-    } else {
-        const int npxy = (int)std::lround(p.min_pad / dx);
-        npx = npy = npxy;
-        if (nx_tmp < ny_tmp) npx += (ny_tmp - nx_tmp) / 2;
-        else if (nx_tmp > ny_tmp) npy += (nx_tmp - ny_tmp) / 2;
-        h->nx = nx_tmp + 2 * npx;
-        h->ny = ny_tmp + 2 * npy;
-    }
-    if (h->nx > 2048 || h->ny > 2048) { delete h; return FI_E_CONFIG; }   // column FFT of 2n must fit in shared memory
-    h->icrop1 += npx;
-    h->icrop2 = h->nx - npx;
-    h->jcrop1 += npy;
-    h->jcrop2 = h->ny - npy;
+    h->nx = pd[0];
+    h->ny = pd[1];
+    h->icrop1 = pd[2];
+    h->icrop2 = pd[3];
+    h->jcrop1 = pd[4];
+    h->jcrop2 = pd[5];
     h->n = (size_t)h->nx * h->ny;
     h->spy = (double)(3600.0f * 24.0f * 365.25f);   // src/fastisostasy.f90:158
     h->cc = p.correct_compression ? 1.5 / (1 + p.nu) : 1.0;

@@ -20,6 +20,7 @@
 #include <cooperative_groups.h>
 
 #include <cstdio>
+#include <mutex>
 #include <type_traits>
 
 #include "fi_engine.h"
@@ -470,8 +471,20 @@ template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, siz
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (*smem > (size_t)optin) return 0;
-    if (cudaFuncSetAttribute(k_engine_rk4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess)
-        return 0;
+    {
+        // the limit is a property of the kernel, shared by every handle:
+        // only ever raise it, so a handle of a smaller domain created later
+        // does not lower it under a larger one
+        static std::mutex mu;
+        static size_t cur = 0;
+        std::lock_guard<std::mutex> lk(mu);
+        if (*smem > cur) {
+            if (cudaFuncSetAttribute(k_engine_rk4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) !=
+                cudaSuccess)
+                return 0;
+            cur = *smem;
+        }
+    }
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T>, 256, *smem) != cudaSuccess || per_sm < 1)
         return 0;

@@ -17,8 +17,10 @@
 // the DFT of DHT^-1(m H); when m is even in both indices this reduces to
 // F' = m F (flag `even`).
 #include <cstdio>
+#include <mutex>
 
 #include "fi_fft.cuh"
+
 #include "fi_kernels.h"
 
 namespace fi {
@@ -42,14 +44,17 @@ static int smem_optin()
     return g_smem_optin;
 }
 
-// Raise a kernel's dynamic shared-memory limit once (never inside a graph
-// capture: every launch shape runs eagerly before it is captured).
+// Raise a kernel's dynamic shared-memory limit when a larger launch needs it
+// (the limit belongs to the kernel and is shared by every handle, so it only
+// ever grows).
 template <typename K> static void set_smem(K kern, size_t bytes)
 {
+    static std::mutex mu;
     static const void* fn[64];
     static size_t done[64];
     static int nfn = 0;
     if (bytes <= 48 * 1024) return;
+    std::lock_guard<std::mutex> lk(mu);
     const void* key = (const void*)kern;
     for (int i = 0; i < nfn; ++i)
         if (fn[i] == key) {

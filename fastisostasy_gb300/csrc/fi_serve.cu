@@ -1,0 +1,381 @@
+// fi_serve.cu — continuous-batching solve server and batched ensembles.
+//
+// A request is one LV-ELVA solve: a domain (parameters, ice grid, padded
+// rheology fields), a constant ice load and a horizon, advanced by
+// isos_update calls every dtt.  One scheduler thread owns the device work:
+//
+//   admit     queued requests become handles (fi_create + fields + init) as
+//             long as the in-flight cap and free HBM (cudaMemGetInfo, less a
+//             reserve) allow; the footprint of each padded size is learnt
+//             from the first handle of that size;
+//   step      every running request keeps up to kDepth updates queued on its
+//             own stream (fi_update_async: a captured CUDA graph per update),
+//             so the updates of different requests overlap on the GPU and a
+//             request that arrives while others run joins at the next round;
+//   retire    a request whose last update has completed reports its device
+//             status, hands back w and z_bed on the ice grid, and frees its
+//             handle, which makes room for the next admission.
+//
+// A request's arithmetic does not depend on what else runs: every handle has
+// its own buffers and stream and every reduction is deterministic, so a
+// result is bit-identical alone and in a mix.
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/fi_gpu.h"
+
+namespace {
+
+constexpr int kDepth = 2;   // updates queued ahead per running request
+
+struct Req {
+    uint64_t id = 0;
+    fi_params p;
+    int nxi = 0, nyi = 0;
+    double dx = 0, dy = 0;
+    std::vector<double> z_bed, Href, H, D, eta, R;
+    std::vector<uint8_t> mask;
+    double t0 = 0, t_end = 0, dtt = 0, bsl = 0;
+    // runtime
+    fi_handle* h = nullptr;
+    fi_bsl b;
+    long long k = 0, nsteps = 0;   // updates issued / total
+    double* dH = nullptr;          // the load on the device, handed to the first update
+    int nout = 0, head = 0;
+    cudaEvent_t ev[kDepth] = {nullptr, nullptr};
+    int32_t pd[6] = {0, 0, 0, 0, 0, 0};
+    size_t mem_key = 0;
+    fi_request_info info;
+    std::vector<double> w_out, zb_out;
+};
+
+}  // namespace
+
+struct fi_server {
+    int device = 0;
+    int max_inflight = 1;
+    size_t reserve = 0;
+    std::chrono::steady_clock::time_point t0;
+    std::mutex mu;
+    std::condition_variable cv;        // wakes the scheduler
+    std::condition_variable done_cv;   // wakes waiters
+    std::deque<Req*> queue;
+    std::vector<Req*> active;          // scheduler thread only
+    std::unordered_map<uint64_t, Req*> all;
+    std::map<size_t, size_t> footprint;   // padded cells * 2 + precision -> bytes
+    uint64_t next_id = 1;
+    bool stop = false;
+    std::thread th;
+
+    double now() const
+    {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
+namespace {
+
+void finish(fi_server* s, Req* r, int state, int status)
+{
+    if (state == 3) {
+        const char* m = r->h ? fi_last_error(r->h) : "";
+        snprintf(r->info.error, sizeof(r->info.error), "%s", (m && m[0]) ? m : "solve failed");
+    }
+    if (r->h) {
+        fi_destroy(r->h);
+        r->h = nullptr;
+    }
+    for (auto& e : r->ev)
+        if (e) { cudaEventDestroy(e); e = nullptr; }
+    if (r->dH) {
+        cudaFree(r->dH);
+        r->dH = nullptr;
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    r->info.state = state;
+    r->info.status = status;
+    r->info.t_done = s->now();
+    // the inputs are no longer needed
+    std::vector<double>().swap(r->z_bed);
+    std::vector<double>().swap(r->Href);
+    std::vector<double>().swap(r->H);
+    std::vector<double>().swap(r->D);
+    std::vector<double>().swap(r->eta);
+    std::vector<double>().swap(r->R);
+    std::vector<uint8_t>().swap(r->mask);
+    s->done_cv.notify_all();
+}
+
+// Create, fill and initialise the handle of a request.
+int start(fi_server* s, Req* r)
+{
+    size_t free0 = 0, total = 0;
+    cudaMemGetInfo(&free0, &total);
+    int rc = fi_create(&r->p, r->nxi, r->nyi, r->dx, r->dy, nullptr, &r->h);
+    if (rc) return rc;
+    rc = fi_set_fields(r->h, r->D.empty() ? nullptr : r->D.data(), r->eta.empty() ? nullptr : r->eta.data(),
+                       r->R.empty() ? nullptr : r->R.data(), r->mask.empty() ? nullptr : r->mask.data());
+    if (rc) return rc;
+    memset(&r->b, 0, sizeof(r->b));
+    r->b.method = 0;
+    r->b.constant_ocean_surface = 1;
+    r->b.bsl_init = r->b.bsl_now = r->bsl;
+    r->b.A_ocean_pd = r->b.A_ocean_now = 3.625e14;
+    if ((rc = fi_init_state(r->h, r->z_bed.data(), r->Href.data(), r->t0, &r->b))) return rc;
+    const size_t hb = r->H.size() * sizeof(double);
+    if (cudaMalloc(&r->dH, hb) != cudaSuccess) return FI_E_OOM;
+    if (cudaMemcpy(r->dH, r->H.data(), hb, cudaMemcpyHostToDevice) != cudaSuccess) return FI_E_CUDA;
+    for (auto& e : r->ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return FI_E_CUDA;
+    size_t free1 = 0;
+    cudaMemGetInfo(&free1, &total);
+    if (free0 > free1) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        size_t& f = s->footprint[r->mem_key];
+        if (free0 - free1 > f) f = free0 - free1;
+    }
+    return FI_OK;
+}
+
+size_t estimate(fi_server* s, const Req* r)
+{
+    auto it = s->footprint.find(r->mem_key);
+    if (it != s->footprint.end()) return it->second;
+    // before the first handle of this size: about 100 doubles per padded cell
+    // plus the (2n)^2 convolution spectra
+    const size_t n = (size_t)r->pd[0] * r->pd[1];
+    return n * 800 + 8 * n * 16;
+}
+
+void admit(fi_server* s)
+{
+    for (;;) {
+        Req* r = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            if (s->queue.empty() || (int)s->active.size() >= s->max_inflight) return;
+            r = s->queue.front();
+            if (!s->active.empty()) {
+                size_t free_b = 0, total = 0;
+                cudaMemGetInfo(&free_b, &total);
+                if (free_b < estimate(s, r) + s->reserve) return;   // wait for a running request to retire
+            }
+            s->queue.pop_front();
+            r->info.state = 1;
+            r->info.t_admit = s->now();
+        }
+        const int rc = start(s, r);
+        if (rc) {
+            finish(s, r, 3, rc);
+            continue;
+        }
+        s->active.push_back(r);
+    }
+}
+
+void collect(fi_server* s, Req* r)
+{
+    int st = fi_synchronize(r->h);
+    if (st == FI_OK) {
+        const int nx = r->pd[0];
+        std::vector<double> pad((size_t)r->pd[0] * r->pd[1]);
+        r->w_out.resize((size_t)r->nxi * r->nyi);
+        r->zb_out.resize((size_t)r->nxi * r->nyi);
+        const int i0 = r->pd[2] - 1, j0 = r->pd[4] - 1;
+        int rc = fi_get_field(r->h, FI_FIELD_W, pad.data());
+        for (int j = 0; j < r->nyi && !rc; ++j)
+            memcpy(&r->w_out[(size_t)j * r->nxi], &pad[(size_t)(j + j0) * nx + i0], r->nxi * sizeof(double));
+        if (!rc) rc = fi_get_field(r->h, FI_FIELD_Z_BED, pad.data());
+        for (int j = 0; j < r->nyi && !rc; ++j)
+            memcpy(&r->zb_out[(size_t)j * r->nxi], &pad[(size_t)(j + j0) * nx + i0], r->nxi * sizeof(double));
+        st = rc;
+    }
+    finish(s, r, st == FI_OK ? 2 : 3, st);
+}
+
+void run(fi_server* s)
+{
+    cudaSetDevice(s->device);
+    for (;;) {
+        admit(s);
+        bool work = false;
+        for (size_t a = 0; a < s->active.size();) {
+            Req* r = s->active[a];
+            while (r->nout > 0 && cudaEventQuery(r->ev[r->head]) == cudaSuccess) {
+                r->head = (r->head + 1) % kDepth;
+                r->nout--;
+                work = true;
+            }
+            int rc = FI_OK;
+            while (r->nout < kDepth && r->k < r->nsteps) {
+                // the same time sequence as a caller stepping by dtt, clipped at t_end
+                double tn = r->t0 + (double)(r->k + 1) * r->dtt;
+                if (r->k + 1 == r->nsteps || tn > r->t_end) tn = r->t_end;
+                if ((rc = fi_update_async(r->h, r->k == 0 ? r->dH : nullptr, tn, &r->b))) break;
+                cudaEventRecord(r->ev[(r->head + r->nout) % kDepth], (cudaStream_t)fi_stream(r->h));
+                r->nout++;
+                r->k++;
+                r->info.updates = r->k;
+                work = true;
+            }
+            if (rc) {
+                finish(s, r, 3, rc);
+                s->active.erase(s->active.begin() + a);
+                continue;
+            }
+            if (r->k >= r->nsteps && r->nout == 0) {
+                collect(s, r);
+                s->active.erase(s->active.begin() + a);
+                work = true;
+                continue;
+            }
+            ++a;
+        }
+        if (!work) {
+            std::unique_lock<std::mutex> lk(s->mu);
+            if (s->active.empty()) {
+                if (s->stop && s->queue.empty()) return;
+                if (s->queue.empty()) s->cv.wait(lk, [&] { return s->stop || !s->queue.empty(); });
+            } else {
+                lk.unlock();
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+            }
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int fi_serve_create(int max_inflight, double reserve_gb, fi_server** out)
+{
+    if (!out || max_inflight < 1 || !(reserve_gb >= 0.0)) return FI_E_ARG;
+    *out = nullptr;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FI_E_CUDA;
+    fi_server* s = new fi_server();
+    s->device = dev;
+    s->max_inflight = max_inflight;
+    s->reserve = (size_t)(reserve_gb * 1e9);
+    s->t0 = std::chrono::steady_clock::now();
+    s->th = std::thread(run, s);
+    *out = s;
+    return FI_OK;
+}
+
+int fi_serve_submit(fi_server* s, const fi_request* q, uint64_t* id)
+{
+    if (!s || !q || !id || !q->z_bed || !q->H_ice || !(q->dtt > 0.0) || !(q->t_end >= q->t0)) return FI_E_ARG;
+    Req* r = new Req();
+    r->p = q->p;
+    r->nxi = q->nx_ice;
+    r->nyi = q->ny_ice;
+    r->dx = q->dx;
+    r->dy = q->dy;
+    if (int rc = fi_padded_dims(&q->p, q->nx_ice, q->ny_ice, q->dx, q->dy, r->pd)) {
+        delete r;
+        return rc;
+    }
+    const size_t ni = (size_t)q->nx_ice * q->ny_ice, np = (size_t)r->pd[0] * r->pd[1];
+    r->z_bed.assign(q->z_bed, q->z_bed + ni);
+    r->H.assign(q->H_ice, q->H_ice + ni);
+    if (q->H_ref) r->Href.assign(q->H_ref, q->H_ref + ni);
+    else r->Href.assign(ni, 0.0);
+    if (q->D_lith) r->D.assign(q->D_lith, q->D_lith + np);
+    if (q->eta_eff) r->eta.assign(q->eta_eff, q->eta_eff + np);
+    if (q->R) r->R.assign(q->R, q->R + np);
+    if (q->maskactive) r->mask.assign(q->maskactive, q->maskactive + np);
+    r->t0 = q->t0;
+    r->t_end = q->t_end;
+    r->dtt = q->dtt;
+    r->bsl = q->bsl;
+    long long ns = 0;
+    while (q->t0 + (double)ns * q->dtt < q->t_end) ++ns;
+    r->nsteps = ns;
+    r->mem_key = np * 2 + (size_t)(q->p.precision & 1);
+    memset(&r->info, 0, sizeof(r->info));
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        r->id = s->next_id++;
+        r->info.t_submit = s->now();
+        s->all[r->id] = r;
+        s->queue.push_back(r);
+        *id = r->id;
+    }
+    s->cv.notify_one();
+    return FI_OK;
+}
+
+int fi_serve_info(fi_server* s, uint64_t id, fi_request_info* info)
+{
+    if (!s || !info) return FI_E_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return FI_E_ARG;
+    *info = it->second->info;
+    return FI_OK;
+}
+
+int fi_serve_wait(fi_server* s, uint64_t id, double timeout_s, fi_request_info* info)
+{
+    if (!s) return FI_E_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return FI_E_ARG;
+    Req* r = it->second;
+    const bool ok = s->done_cv.wait_for(lk, std::chrono::duration<double>(timeout_s),
+                                        [&] { return r->info.state >= 2; });
+    if (info) *info = r->info;
+    return ok ? FI_OK : FI_E_TIMEOUT;
+}
+
+int fi_serve_result(fi_server* s, uint64_t id, double* w_ice, double* z_bed_ice)
+{
+    if (!s) return FI_E_ARG;
+    Req* r = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->all.find(id);
+        if (it == s->all.end()) return FI_E_ARG;
+        r = it->second;
+        if (r->info.state < 2) return FI_E_STATE;
+        s->all.erase(it);
+    }
+    int rc = r->info.state == 2 ? FI_OK : (r->info.status ? r->info.status : FI_E_CUDA);
+    if (rc == FI_OK) {
+        if (w_ice) memcpy(w_ice, r->w_out.data(), r->w_out.size() * sizeof(double));
+        if (z_bed_ice) memcpy(z_bed_ice, r->zb_out.data(), r->zb_out.size() * sizeof(double));
+    }
+    delete r;
+    return rc;
+}
+
+double fi_serve_clock(fi_server* s) { return s ? s->now() : 0.0; }
+
+int fi_serve_destroy(fi_server* s)
+{
+    if (!s) return FI_E_ARG;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv.notify_all();
+    if (s->th.joinable()) s->th.join();
+    for (auto& kv : s->all) delete kv.second;
+    delete s;
+    return FI_OK;
+}
+
+}  // extern "C"

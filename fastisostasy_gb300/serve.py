@@ -1,0 +1,121 @@
+"""Host side of the solve server (fi_serve_* in include/fi_gpu.h).
+
+A request is one independent LV-ELVA solve of a Workload: init at t0 with no
+ice (or `H_ref`), then isos_update every `dtt` up to `t_end` under the
+workload's final ice load.  The scheduler, admission and device work live in
+libfigpu.so; this module only packs requests and unpacks results.
+"""
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from .isostasy import FiError, _f64, make_params
+
+STATE = {0: "queued", 1: "running", 2: "done", 3: "failed"}
+
+
+def padded_dims(params: dict, nx_ice: int, ny_ice: int, dx: float, dy: Optional[float] = None, precision=0):
+    """(nx, ny, icrop1, icrop2, jcrop1, jcrop2) of the padded domain."""
+    L = _lib.load()
+    out = (C.c_int32 * 6)()
+    p = make_params(params, precision)
+    rc = L.fi_padded_dims(C.byref(p), int(nx_ice), int(ny_ice), float(dx), float(dx if dy is None else dy), out)
+    if rc:
+        raise FiError(rc, "fi_padded_dims")
+    return tuple(out)
+
+
+class Server:
+    """Continuous-batching server on the current CUDA device."""
+
+    def __init__(self, max_inflight: int = 64, reserve_gb: float = 4.0):
+        self.L = _lib.load()
+        h = C.c_void_p()
+        rc = self.L.fi_serve_create(int(max_inflight), float(reserve_gb), C.byref(h))
+        if rc:
+            raise FiError(rc, "fi_serve_create")
+        self.h = h
+        self._shapes = {}
+
+    def submit(self, wl, t_end: Optional[float] = None, t0: float = 0.0, precision: int = 0,
+               dtt: Optional[float] = None) -> int:
+        p = make_params(wl.params, precision)
+        nx, ny = padded_dims(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=precision)[:2]
+        fields = wl.padded_fields(nx, ny)
+        keep = []
+
+        def arr(a, dtype=np.float64):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dtype)
+            keep.append(a)
+            return a
+
+        q = _lib.FiRequest()
+        q.p = p
+        q.nx_ice, q.ny_ice = wl.nx_ice, wl.ny_ice
+        q.dx = q.dy = wl.dx
+        zb, H = arr(wl.z_bed), arr(wl.H_final)
+        q.z_bed = zb.ctypes.data_as(_lib._dp)
+        q.H_ice = H.ctypes.data_as(_lib._dp)
+        for name in ("D_lith", "eta_eff", "R"):
+            a = arr(fields.get(name))
+            if a is not None:
+                assert a.shape == (ny, nx), (name, a.shape)
+                setattr(q, name, a.ctypes.data_as(_lib._dp))
+        m = arr(fields.get("maskactive"), np.uint8)
+        if m is not None:
+            q.maskactive = m.ctypes.data_as(_lib._u8)
+        q.t0 = t0
+        q.t_end = wl.t_end if t_end is None else t_end
+        q.dtt = wl.dtt if dtt is None else dtt
+        q.bsl = 0.0
+        rid = C.c_uint64()
+        rc = self.L.fi_serve_submit(self.h, C.byref(q), C.byref(rid))   # copies every array
+        if rc:
+            raise FiError(rc, "fi_serve_submit")
+        self._shapes[rid.value] = (wl.ny_ice, wl.nx_ice)
+        return rid.value
+
+    def info(self, rid: int) -> dict:
+        i = _lib.FiRequestInfo()
+        rc = self.L.fi_serve_info(self.h, C.c_uint64(rid), C.byref(i))
+        if rc:
+            raise FiError(rc, "fi_serve_info")
+        return {"state": STATE[i.state], "status": i.status, "updates": i.updates, "t_submit": i.t_submit,
+                "t_admit": i.t_admit, "t_done": i.t_done, "error": i.error.decode(errors="replace")}
+
+    def wait(self, rid: int, timeout: float = 600.0) -> dict:
+        i = _lib.FiRequestInfo()
+        rc = self.L.fi_serve_wait(self.h, C.c_uint64(rid), float(timeout), C.byref(i))
+        if rc:
+            raise FiError(rc, "fi_serve_wait")
+        return {"state": STATE[i.state], "status": i.status, "updates": i.updates, "t_submit": i.t_submit,
+                "t_admit": i.t_admit, "t_done": i.t_done, "error": i.error.decode(errors="replace")}
+
+    def result(self, rid: int):
+        """(w, z_bed) on the ice grid; releases the request."""
+        shape = self._shapes.pop(rid)
+        w = np.empty(shape)
+        zb = np.empty(shape)
+        rc = self.L.fi_serve_result(self.h, C.c_uint64(rid), w.ctypes.data_as(_lib._dp),
+                                    zb.ctypes.data_as(_lib._dp))
+        if rc:
+            raise FiError(rc, "fi_serve_result")
+        return w, zb
+
+    def clock(self) -> float:
+        return self.L.fi_serve_clock(self.h)
+
+    def close(self):
+        if self.h:
+            self.L.fi_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

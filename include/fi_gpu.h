@@ -100,6 +100,10 @@ typedef struct fi_handle fi_handle;
  * K_or_null is the padded (nx, ny) distortion field or NULL (K = 1). */
 int fi_create(const fi_params* p, int nx_ice, int ny_ice, double dx, double dy, const double* K_or_null,
               fi_handle** out);
+/* init_domain_size (src/isos_utils.f90:285-354) without creating anything:
+ * nx, ny, icrop1, icrop2, jcrop1, jcrop2 of the padded domain fi_create
+ * would build.  Callers size padded fields (fi_set_fields, fi_request) with it. */
+int fi_padded_dims(const fi_params* p, int nx_ice, int ny_ice, double dx, double dy, int32_t* out6);
 /* Replaces isos_end (src/fastisostasy.f90:911-923). */
 int fi_destroy(fi_handle* h);
 /* nx, ny, icrop1, icrop2, jcrop1, jcrop2 (1-based like the reference), nx_ice, ny_ice */
@@ -168,6 +172,52 @@ int fi_lvelva_static(const double* d_w, const double* d_canom_full, const uint8_
                      const double* d_D_lith, const double* d_eta_eff, const double* d_kappa, const double* d_R,
                      int nx, int ny, double dx, double dy, double g, double nu, double sec_per_year,
                      double* d_dwdt, void* stream);
+
+/* ---- Solve server: continuous batching of independent solves ----------
+ * No counterpart in the reference (a caller there runs one isos_class at a
+ * time).  A request is one solve: fi_create + fi_set_fields + fi_init_state,
+ * then isos_update every dtt from t0 to t_end with a constant ice load and
+ * barystatic sea level.  One scheduler thread admits queued requests while
+ * the in-flight cap and free device memory (less reserve_gb) allow, keeps
+ * every running request's updates queued on its own stream so that requests
+ * of different sizes overlap on the GPU, and retires finished requests
+ * (their handles are freed).  A result does not depend on the mix it ran in.
+ * An ensemble is a set of requests submitted together. */
+typedef struct fi_server fi_server;
+typedef struct {
+    fi_params p;
+    int32_t nx_ice, ny_ice;
+    double dx, dy;
+    const double* z_bed;          /* ice grid */
+    const double* H_ref;          /* ice grid at t0 (the reference state), NULL = no ice */
+    const double* H_ice;          /* ice grid, the load over the solve */
+    const double* D_lith;         /* padded (fi_padded_dims) or NULL */
+    const double* eta_eff;        /* padded or NULL */
+    const double* R;              /* padded or NULL */
+    const uint8_t* maskactive;    /* padded or NULL */
+    double t0, t_end, dtt;        /* years */
+    double bsl;                   /* barystatic sea level [m] */
+} fi_request;
+typedef struct {
+    int32_t state;                /* 0 queued, 1 running, 2 done, 3 failed */
+    int32_t status;               /* FI_* status of the solve */
+    int64_t updates;              /* isos_update calls issued */
+    double t_submit, t_admit, t_done;   /* seconds on the server clock */
+    char error[128];              /* message of a failed solve */
+} fi_request_info;
+/* The server drives the device that is current when it is created. */
+int fi_serve_create(int max_inflight, double reserve_gb, fi_server** out);
+/* Copies the request's arrays; returns at once. */
+int fi_serve_submit(fi_server* s, const fi_request* r, uint64_t* id);
+int fi_serve_info(fi_server* s, uint64_t id, fi_request_info* info);
+/* Waits up to timeout_s for the request to finish (FI_E_TIMEOUT otherwise). */
+int fi_serve_wait(fi_server* s, uint64_t id, double timeout_s, fi_request_info* info);
+/* w and z_bed on the ice grid of a finished request (either may be NULL);
+ * releases the request's record. */
+int fi_serve_result(fi_server* s, uint64_t id, double* w_ice, double* z_bed_ice);
+double fi_serve_clock(fi_server* s);
+/* Finishes every submitted request, then stops the scheduler. */
+int fi_serve_destroy(fi_server* s);
 
 /* Restart support: the complete device state (fields + integrator clock) as
  * doubles; bit-identical round trip. */

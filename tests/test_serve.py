@@ -1,0 +1,120 @@
+"""Solve server (fi_serve_*): results against directly driven handles, the
+same request alone and in a mix, admission limits, ensembles."""
+import numpy as np
+import pytest
+
+from fastisostasy_gb300 import workloads as W
+from fastisostasy_gb300.isostasy import Domain
+from fastisostasy_gb300.serve import Server, padded_dims
+from harness import gpu_bsl
+from oracle import oracle as O
+
+
+def small_rk4(n=48, seed=0, stage_mode=1):
+    wl = W.config2(n=n, L=3000e3 * n / 256, dt=1.0, stage_mode=stage_mode)
+    wl.t_end = 60.0
+    return wl
+
+
+def small_tsit(n=40):
+    wl = W.config1(n)
+    wl.params["stage_mode"] = 0
+    wl.t_end = 50.0
+    return wl
+
+
+def direct(wl, precision=0):
+    """The same solve through one handle driven by isos_update calls."""
+    dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=precision)
+    f = wl.padded_fields(dom.nx, dom.ny)
+    if f:
+        dom.set_fields(**f)
+    b = gpu_bsl()
+    dom.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+    out = {"w": np.zeros((wl.ny_ice, wl.nx_ice)), "z_bed": np.zeros((wl.ny_ice, wl.nx_ice))}
+    t = 0.0
+    while t < wl.t_end:
+        t = min(t + wl.dtt, wl.t_end)
+        dom.update(wl.H_final, t, b, out=out)
+    dom.close()
+    return out["w"], out["z_bed"]
+
+
+def test_padded_dims_match_oracle():
+    """fi_padded_dims (no device needed) against the oracle's domain."""
+    for wl in (small_rk4(48), small_tsit(40), W.config3(nx_ice=40, ny_ice=72, dx=20e3, nx_pad=64, ny_pad=96)):
+        m = O.Model(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
+        nx, ny = padded_dims(wl.params, wl.nx_ice, wl.ny_ice, wl.dx)[:2]
+        assert (nx, ny) == (m.nx, m.ny)
+        m.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("make,precision", [(small_rk4, 0), (small_rk4, 1), (small_tsit, 0)])
+def test_served_solve_matches_direct_handle(make, precision):
+    wl = make()
+    w_ref, zb_ref = direct(wl, precision)
+    srv = Server(max_inflight=4, reserve_gb=1.0)
+    rid = srv.submit(wl, precision=precision)
+    info = srv.wait(rid, 120.0)
+    assert info["state"] == "done" and info["status"] == 0
+    w, zb = srv.result(rid)
+    srv.close()
+    assert np.array_equal(w, w_ref) and np.array_equal(zb, zb_ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_alone_and_in_a_mix_are_identical(precision):
+    """Continuous batching: a request gives the same bits alone and while
+    requests of other sizes and integrators run beside it."""
+    target = small_rk4(64)
+    srv = Server(max_inflight=16, reserve_gb=1.0)
+    rid = srv.submit(target, precision=precision)
+    srv.wait(rid, 120.0)
+    alone = srv.result(rid)
+    others = []
+    for i, n in enumerate((32, 48, 96, 128, 40, 80)):
+        others.append(srv.submit(small_rk4(n), precision=precision))
+        if i == 2:
+            rid = srv.submit(target, precision=precision)   # arrives while others run
+        others.append(srv.submit(small_tsit(32 + 8 * (i % 3)), precision=0))
+    info = srv.wait(rid, 300.0)
+    assert info["status"] == 0, info
+    mixed = srv.result(rid)
+    for o in others:
+        io = srv.wait(o, 300.0)
+        assert io["status"] == 0, io
+        srv.result(o)
+    srv.close()
+    assert np.array_equal(alone[0], mixed[0]) and np.array_equal(alone[1], mixed[1])
+
+
+@pytest.mark.gpu
+def test_inflight_cap_and_drain():
+    srv = Server(max_inflight=2, reserve_gb=0.5)
+    ids = [srv.submit(small_rk4(48)) for _ in range(5)]
+    infos = [srv.wait(i, 300.0) for i in ids]
+    assert all(i["state"] == "done" for i in infos)
+    for k in range(2, 5):
+        # at most two run at once: the k-th starts after the (k-2)-th ended
+        done = sorted(i["t_done"] for i in infos[:k])
+        assert infos[k]["t_admit"] >= done[k - 2] - 1e-6
+    for i in ids:
+        srv.result(i)
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_unstable_request_fails_alone():
+    """A request whose solve diverges reports FI_E_LARGE; its neighbours finish."""
+    bad = W.config2(n=64, L=3000e3 * 64 / 256 * 2, dt=50.0, stage_mode=1)
+    bad.t_end = 2000.0
+    bad.dtt = 100.0
+    good = small_rk4(48)
+    srv = Server(max_inflight=4, reserve_gb=0.5)
+    rb, rg = srv.submit(bad), srv.submit(good)
+    ib, ig = srv.wait(rb, 120.0), srv.wait(rg, 120.0)
+    srv.close()
+    assert ib["state"] == "failed" and ib["status"] in (1, 2)
+    assert ig["state"] == "done"
