@@ -256,6 +256,154 @@ def cpu_baseline(samples=8, threads=1, stage_mode=1):
     return samples * wl.dtt / 1000.0 / secs, secs
 
 
+def ensemble_leg(n_members=256, n_updates=10):
+    """256-member ensemble: members batched in lockstep (mixed form, every
+    member on its own stream, one fi_batch_update per coupling step) against
+    the same members solved one after another in the plain FP64 form.  Each
+    member runs reference-compatible Tsit5 (the reference's integrator) from
+    t = 20 yr for n_updates coupling steps of 10 yr after two untimed ones
+    (load switch-on and graph capture).  Handle set-up is timed separately."""
+    import torch
+    from fastisostasy_gb300 import workloads as W
+    from fastisostasy_gb300.isostasy import Domain
+    from fastisostasy_gb300.serve import Ensemble
+    from fastisostasy_gb300 import _lib
+    wls = [W.ensemble_member(i, stage_mode=0) for i in range(n_members)]
+    a = time.perf_counter()
+    ens = Ensemble(wls, precision=1)
+    init_s = time.perf_counter() - a
+    ens.first_update(10.0)
+    ens.update(20.0)
+    ens.synchronize()
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    for k in range(n_updates):
+        ens.update(30.0 + 10.0 * k)
+    ens.synchronize()
+    batched_s = time.perf_counter() - a
+    ens.close()
+    seq_s, seq_init = 0.0, 0.0
+    sizes = {}
+    for wl in wls:
+        sizes[wl.nx_ice] = sizes.get(wl.nx_ice, 0) + 1
+        a = time.perf_counter()
+        d = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=0)
+        f = wl.padded_fields(d.nx, d.ny)
+        if f:
+            d.set_fields(**f)
+        b = _lib.FiBsl()
+        b.method, b.constant_ocean_surface = 0, 1
+        b.A_ocean_pd = b.A_ocean_now = 3.625e14
+        d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+        seq_init += time.perf_counter() - a
+        d.update(wl.H_final, 10.0, b)
+        d.update(wl.H_final, 20.0, b)
+        a = time.perf_counter()
+        for k in range(n_updates):
+            d.update(wl.H_final, 30.0 + 10.0 * k, b)
+        seq_s += time.perf_counter() - a
+        d.close()
+    mkyr = n_members * n_updates * 10.0 / 1000.0
+    return {
+        "workload": "ensemble: %d members, n in {128,192,256,384,512} (%s), dx 10-30 km, log10 eta Gaussian random "
+                    "field (mean 21, std 0.5, 500 km), He 50-150 km, disc 300-1200 km / 500-3000 m; "
+                    "reference-compatible Tsit5; %d coupling steps of 10 yr per member (the 10 kyr horizon "
+                    "cut to a bounded sample)" % (n_members, sizes, n_updates),
+        "unit": "member-kyr/s", "batched_mixed": mkyr / batched_s, "sequential_fp64": mkyr / seq_s,
+        "speedup": seq_s / batched_s, "batched_s": batched_s, "sequential_s": seq_s,
+        "setup_s": {"batched_mixed": init_s, "sequential_fp64": seq_init},
+    }
+
+
+def serve_leg(lams=(10, 30, 100, 300, 1000, 2000), n_req=48, reserve_gb=8.0):
+    """Continuous batching: Poisson arrivals at rate lam of n_req solve
+    requests (sizes 64^2..1024^2 weighted 0.3/0.3/0.2/0.15/0.05, random-field
+    rheology, disc or dome load, horizon log-uniform 1-100 kyr scaled by
+    1/100), mixed form, through the solve server; latency = completion -
+    submission on the server clock.  The sequential plain-FP64 comparison
+    replays the same arrivals through one FIFO server whose service times
+    are measured per size (set-up + updates x time per update, FP64)."""
+    from fastisostasy_gb300 import workloads as W
+    from fastisostasy_gb300.isostasy import Domain
+    from fastisostasy_gb300.serve import Server
+    from fastisostasy_gb300 import _lib
+    wls = [W.serve_request(i) for i in range(n_req)]
+    srv = Server(max_inflight=64, reserve_gb=reserve_gb)
+    preps = [srv.prepare(wl, precision=1) for wl in wls]
+    # warm-up: one short request per size (kernel attributes, first captures)
+    seen = {}
+    for wl in wls:
+        if wl.nx_ice not in seen:
+            seen[wl.nx_ice] = srv.submit(wl, t_end=30.0, precision=1)
+    for rid in seen.values():
+        srv.wait(rid, 300.0)
+        srv.result(rid)
+    rng = np.random.default_rng(12345)
+    levels = []
+    for lam in lams:
+        arr = np.cumsum(rng.exponential(1.0 / lam, n_req))
+        t_base = srv.clock() + 0.005
+        ids = []
+        for k, prep in enumerate(preps):
+            while srv.clock() < t_base + arr[k]:
+                pass
+            ids.append(srv.submit_prepared(prep))
+        infos = [srv.wait(i, 600.0) for i in ids]
+        for i in ids:
+            srv.result(i)
+        bad = [f for f in infos if f["state"] != "done"]
+        if bad:
+            raise RuntimeError("serve: %d requests failed: %s" % (len(bad), bad[0]))
+        lat = np.array([f["t_done"] - f["t_submit"] for f in infos]) * 1e3
+        span = max(f["t_done"] for f in infos) - min(f["t_submit"] for f in infos)
+        levels.append({"lambda_per_s": lam, "p50_ms": float(np.percentile(lat, 50)),
+                       "p99_ms": float(np.percentile(lat, 99)), "throughput_req_per_s": n_req / span,
+                       "arrivals": arr})
+    srv.close()
+    # sequential plain FP64: measured service time per size
+    cost = {}
+    for wl in wls:
+        n = wl.nx_ice
+        if n in cost:
+            continue
+        a = time.perf_counter()
+        d = Domain(wl.params, n, n, wl.dx, precision=0)
+        f = wl.padded_fields(d.nx, d.ny)
+        if f:
+            d.set_fields(**f)
+        b = _lib.FiBsl()
+        b.method, b.constant_ocean_surface = 0, 1
+        b.A_ocean_pd = b.A_ocean_now = 3.625e14
+        d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+        setup = time.perf_counter() - a
+        for k in range(2):
+            d.update(wl.H_final, 10.0 * (k + 1), b)
+        a = time.perf_counter()
+        for k in range(4):
+            d.update(wl.H_final, 30.0 + 10.0 * k, b)
+        cost[n] = (setup, (time.perf_counter() - a) / 4)
+        d.close()
+    service = np.array([cost[wl.nx_ice][0] + np.ceil(wl.t_end / wl.dtt) * cost[wl.nx_ice][1] for wl in wls])
+    for lv in levels:
+        arr = lv.pop("arrivals")
+        t_free, lat = 0.0, []
+        for a_k, s_k in zip(arr, service):
+            start = max(a_k, t_free)
+            t_free = start + s_k
+            lat.append(t_free - a_k)
+        lat = np.array(lat) * 1e3
+        lv["sequential_fp64"] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                                 "throughput_req_per_s": n_req / (t_free - arr[0])}
+    sizes = {}
+    for wl in wls:
+        sizes[wl.nx_ice] = sizes.get(wl.nx_ice, 0) + 1
+    return {"workload": "serve stream: %d requests per rate, sizes %s, mixed form, RK4 true stages dt=1 yr, "
+                        "coupling 10 yr, horizon log-uniform 1-100 kyr x 1/100 (mean %.0f yr)"
+                        % (n_req, sizes, float(np.mean([w.t_end for w in wls]))),
+            "levels": levels,
+            "sequential_fp64_service_s": {str(k): {"setup": v[0], "per_update": v[1]} for k, v in cost.items()}}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -307,6 +455,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--ensemble-members", type=int, default=256)
+    ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--lean", action="store_true",
                     help="mixed form only, no profile / e2e / CPU legs (for ncu captures); prints the timing only")
     args = ap.parse_args()
@@ -381,6 +533,12 @@ def main():
                "sample": "%d coupling steps of the same workload (%d x 40 RHS + 2 convolutions at 1023^2), "
                          "%.1f s, 1 thread (the reference is serial)" % (args.cpu_samples, args.cpu_samples, secs)}
 
+    ens = serve = None
+    if not args.no_ensemble:
+        ens = ensemble_leg(args.ensemble_members)
+    if not args.no_serve:
+        serve = serve_leg(n_req=args.serve_requests)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": kyr(r32["ms"]), "unit": "kyr/s", "n_gpus": ws, "steps": args.steps,
@@ -403,6 +561,8 @@ def main():
                                           "achieved": upd / (r32["ms"] / 1000.0) / 1e9,
                                           "frac": upd / (r32["ms"] / 1000.0) / 1e9 / peak}},
             "cpu_baseline": cpu,
+            "ensemble": ens,
+            "serve": serve,
             "clocks": r32["clocks"],
             "gpu_launches": r32["launches"],
         }

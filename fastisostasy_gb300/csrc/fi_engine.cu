@@ -489,7 +489,12 @@ template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, siz
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T>, 256, *smem) != cudaSuccess || per_sm < 1)
         return 0;
     if (per_sm > 2) per_sm = 2;
-    *grid = per_sm * nsm;
+    // no more blocks than the largest phase has work items: a small domain
+    // then leaves SMs free for other handles' work (serving, ensembles)
+    const int na = (p.ny + RA - 1) / RA, nb = (p.h + 1 + cb - 1) / cb, nc = (p.ny + RC - 1) / RC;
+    int items = na > nb ? na : nb;
+    if (nc > items) items = nc;
+    *grid = per_sm * nsm < items ? per_sm * nsm : items;
     return 1;
 }
 

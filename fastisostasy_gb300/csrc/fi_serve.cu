@@ -2,19 +2,21 @@
 //
 // A request is one LV-ELVA solve: a domain (parameters, ice grid, padded
 // rheology fields), a constant ice load and a horizon, advanced by
-// isos_update calls every dtt.  One scheduler thread owns the device work:
+// isos_update calls every dtt.  Two kinds of host threads share the work:
 //
-//   admit     queued requests become handles (fi_create + fields + init) as
-//             long as the in-flight cap and free HBM (cudaMemGetInfo, less a
-//             reserve) allow; the footprint of each padded size is learnt
-//             from the first handle of that size;
-//   step      every running request keeps up to kDepth updates queued on its
-//             own stream (fi_update_async: a captured CUDA graph per update),
-//             so the updates of different requests overlap on the GPU and a
-//             request that arrives while others run joins at the next round;
-//   retire    a request whose last update has completed reports its device
-//             status, hands back w and z_bed on the ice grid, and frees its
-//             handle, which makes room for the next admission.
+//   workers   (kWorkers threads) admit queued requests as long as the
+//             in-flight cap and free HBM (cudaMemGetInfo, less a reserve and
+//             less the estimates of requests still being set up) allow, and
+//             turn them into handles (fi_create + fields + init: host-side
+//             set-up that must not stall the stepping); they also retire
+//             finished requests: device status, w and z_bed on the ice grid,
+//             handle freed, which makes room for the next admission.  The
+//             footprint of each padded size is learnt from its first handle.
+//   scheduler (one thread) steps: every running request keeps up to kDepth
+//             updates queued on its own stream (fi_update_async: one captured
+//             CUDA graph per update), so the updates of different requests
+//             overlap on the GPU, and a request set up while others run joins
+//             at the next round.
 //
 // A request's arithmetic does not depend on what else runs: every handle has
 // its own buffers and stream and every reduction is deterministic, so a
@@ -37,7 +39,8 @@
 
 namespace {
 
-constexpr int kDepth = 2;   // updates queued ahead per running request
+constexpr int kDepth = 2;     // updates queued ahead per running request
+constexpr int kWorkers = 4;   // set-up / retire threads
 
 struct Req {
     uint64_t id = 0;
@@ -53,6 +56,7 @@ struct Req {
     long long k = 0, nsteps = 0;   // updates issued / total
     double* dH = nullptr;          // the load on the device, handed to the first update
     int nout = 0, head = 0;
+    int fail_rc = 0;               // stepping failed with this status
     cudaEvent_t ev[kDepth] = {nullptr, nullptr};
     int32_t pd[6] = {0, 0, 0, 0, 0, 0};
     size_t mem_key = 0;
@@ -69,14 +73,20 @@ struct fi_server {
     std::chrono::steady_clock::time_point t0;
     std::mutex mu;
     std::condition_variable cv;        // wakes the scheduler
+    std::condition_variable work_cv;   // wakes the workers
     std::condition_variable done_cv;   // wakes waiters
-    std::deque<Req*> queue;
+    std::deque<Req*> queue;            // submitted, not admitted
+    std::deque<Req*> ready;            // set up, joining the scheduler
+    std::deque<Req*> retiring;         // stepped to t_end (or failed), to be collected
     std::vector<Req*> active;          // scheduler thread only
+    int inflight = 0;                  // admitted and not yet retired
+    size_t pending_bytes = 0;          // footprint estimates of requests being set up
     std::unordered_map<uint64_t, Req*> all;
     std::map<size_t, size_t> footprint;   // padded cells * 2 + precision -> bytes
     uint64_t next_id = 1;
     bool stop = false;
     std::thread th;
+    std::vector<std::thread> workers;
 
     double now() const
     {
@@ -158,34 +168,23 @@ size_t estimate(fi_server* s, const Req* r)
     return n * 800 + 8 * n * 16;
 }
 
-void admit(fi_server* s)
+// Called with s->mu held.
+bool can_admit(fi_server* s, size_t* est)
 {
-    for (;;) {
-        Req* r = nullptr;
-        {
-            std::lock_guard<std::mutex> lk(s->mu);
-            if (s->queue.empty() || (int)s->active.size() >= s->max_inflight) return;
-            r = s->queue.front();
-            if (!s->active.empty()) {
-                size_t free_b = 0, total = 0;
-                cudaMemGetInfo(&free_b, &total);
-                if (free_b < estimate(s, r) + s->reserve) return;   // wait for a running request to retire
-            }
-            s->queue.pop_front();
-            r->info.state = 1;
-            r->info.t_admit = s->now();
-        }
-        const int rc = start(s, r);
-        if (rc) {
-            finish(s, r, 3, rc);
-            continue;
-        }
-        s->active.push_back(r);
-    }
+    if (s->queue.empty() || s->inflight >= s->max_inflight) return false;
+    *est = estimate(s, s->queue.front());
+    if (s->inflight == 0) return true;   // an idle server always takes one
+    size_t free_b = 0, total = 0;
+    cudaMemGetInfo(&free_b, &total);
+    return free_b >= s->pending_bytes + *est + s->reserve;
 }
 
 void collect(fi_server* s, Req* r)
 {
+    if (r->fail_rc) {
+        finish(s, r, 3, r->fail_rc);
+        return;
+    }
     int st = fi_synchronize(r->h);
     if (st == FI_OK) {
         const int nx = r->pd[0];
@@ -204,12 +203,63 @@ void collect(fi_server* s, Req* r)
     finish(s, r, st == FI_OK ? 2 : 3, st);
 }
 
+void worker(fi_server* s)
+{
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        if (!s->retiring.empty()) {
+            Req* r = s->retiring.front();
+            s->retiring.pop_front();
+            lk.unlock();
+            collect(s, r);
+            lk.lock();
+            s->inflight--;
+            s->work_cv.notify_all();
+            s->cv.notify_one();
+            continue;
+        }
+        size_t est = 0;
+        if (can_admit(s, &est)) {
+            Req* r = s->queue.front();
+            s->queue.pop_front();
+            s->inflight++;
+            s->pending_bytes += est;
+            r->info.state = 1;
+            r->info.t_admit = s->now();
+            lk.unlock();
+            const int rc = start(s, r);
+            if (rc) finish(s, r, 3, rc);
+            lk.lock();
+            s->pending_bytes -= est;
+            if (rc) {
+                s->inflight--;
+                s->work_cv.notify_all();
+            } else {
+                s->ready.push_back(r);
+            }
+            s->cv.notify_one();
+            continue;
+        }
+        if (s->stop && s->queue.empty() && s->retiring.empty() && s->inflight == 0) return;
+        s->work_cv.wait(lk);
+    }
+}
+
 void run(fi_server* s)
 {
     cudaSetDevice(s->device);
     for (;;) {
-        admit(s);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            while (!s->ready.empty()) {
+                s->active.push_back(s->ready.front());
+                s->ready.pop_front();
+            }
+            if (s->active.empty() && s->stop && s->queue.empty() && s->inflight == 0) return;
+        }
         bool work = false;
+        std::vector<Req*> out;
         for (size_t a = 0; a < s->active.size();) {
             Req* r = s->active[a];
             while (r->nout > 0 && cudaEventQuery(r->ev[r->head]) == cudaSuccess) {
@@ -226,31 +276,33 @@ void run(fi_server* s)
                 cudaEventRecord(r->ev[(r->head + r->nout) % kDepth], (cudaStream_t)fi_stream(r->h));
                 r->nout++;
                 r->k++;
-                r->info.updates = r->k;
                 work = true;
             }
-            if (rc) {
-                finish(s, r, 3, rc);
-                s->active.erase(s->active.begin() + a);
-                continue;
-            }
-            if (r->k >= r->nsteps && r->nout == 0) {
-                collect(s, r);
+            if (rc || (r->k >= r->nsteps && r->nout == 0)) {
+                r->fail_rc = rc;
+                out.push_back(r);
                 s->active.erase(s->active.begin() + a);
                 work = true;
                 continue;
             }
             ++a;
         }
-        if (!work) {
-            std::unique_lock<std::mutex> lk(s->mu);
-            if (s->active.empty()) {
-                if (s->stop && s->queue.empty()) return;
-                if (s->queue.empty()) s->cv.wait(lk, [&] { return s->stop || !s->queue.empty(); });
-            } else {
-                lk.unlock();
-                std::this_thread::sleep_for(std::chrono::microseconds(20));
+        std::unique_lock<std::mutex> lk(s->mu);
+        for (Req* r : s->active) r->info.updates = r->k;
+        if (!out.empty()) {
+            for (Req* r : out) {
+                r->info.updates = r->k;
+                s->retiring.push_back(r);
             }
+            s->work_cv.notify_all();
+        }
+        if (!work) {
+            if (s->active.empty())
+                s->cv.wait(lk, [&] {
+                    return !s->ready.empty() || (s->stop && s->queue.empty() && s->inflight == 0);
+                });
+            else
+                s->cv.wait_for(lk, std::chrono::microseconds(30));
         }
     }
 }
@@ -271,6 +323,7 @@ int fi_serve_create(int max_inflight, double reserve_gb, fi_server** out)
     s->reserve = (size_t)(reserve_gb * 1e9);
     s->t0 = std::chrono::steady_clock::now();
     s->th = std::thread(run, s);
+    for (int i = 0; i < kWorkers; ++i) s->workers.emplace_back(worker, s);
     *out = s;
     return FI_OK;
 }
@@ -314,7 +367,7 @@ int fi_serve_submit(fi_server* s, const fi_request* q, uint64_t* id)
         s->queue.push_back(r);
         *id = r->id;
     }
-    s->cv.notify_one();
+    s->work_cv.notify_one();
     return FI_OK;
 }
 
@@ -364,6 +417,28 @@ int fi_serve_result(fi_server* s, uint64_t id, double* w_ice, double* z_bed_ice)
 
 double fi_serve_clock(fi_server* s) { return s ? s->now() : 0.0; }
 
+int fi_batch_update(fi_handle* const* hs, int n, double time, fi_bsl* bsl)
+{
+    if (!hs || n < 0 || !bsl) return FI_E_ARG;
+    for (int i = 0; i < n; ++i) {
+        if (!hs[i]) return FI_E_ARG;
+        if (int rc = fi_update_async(hs[i], nullptr, time, &bsl[i])) return rc;
+    }
+    return FI_OK;
+}
+
+int fi_batch_synchronize(fi_handle* const* hs, int n, int32_t* status)
+{
+    if (!hs || n < 0) return FI_E_ARG;
+    int first = FI_OK;
+    for (int i = 0; i < n; ++i) {
+        const int rc = hs[i] ? fi_synchronize(hs[i]) : FI_E_ARG;
+        if (status) status[i] = rc;
+        if (rc && first == FI_OK) first = rc;
+    }
+    return first;
+}
+
 int fi_serve_destroy(fi_server* s)
 {
     if (!s) return FI_E_ARG;
@@ -372,7 +447,10 @@ int fi_serve_destroy(fi_server* s)
         s->stop = true;
     }
     s->cv.notify_all();
+    s->work_cv.notify_all();
     if (s->th.joinable()) s->th.join();
+    for (auto& w : s->workers)
+        if (w.joinable()) w.join();
     for (auto& kv : s->all) delete kv.second;
     delete s;
     return FI_OK;

@@ -39,8 +39,10 @@ class Server:
         self.h = h
         self._shapes = {}
 
-    def submit(self, wl, t_end: Optional[float] = None, t0: float = 0.0, precision: int = 0,
-               dtt: Optional[float] = None) -> int:
+    def prepare(self, wl, t_end: Optional[float] = None, t0: float = 0.0, precision: int = 0,
+                dtt: Optional[float] = None):
+        """Pack a Workload into a request (padded fields computed here), so
+        that submit_prepared costs only the copy into the server."""
         p = make_params(wl.params, precision)
         nx, ny = padded_dims(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=precision)[:2]
         fields = wl.padded_fields(nx, ny)
@@ -72,12 +74,20 @@ class Server:
         q.t_end = wl.t_end if t_end is None else t_end
         q.dtt = wl.dtt if dtt is None else dtt
         q.bsl = 0.0
+        return (q, keep, (wl.ny_ice, wl.nx_ice))
+
+    def submit_prepared(self, prep) -> int:
+        q, _keep, shape = prep
         rid = C.c_uint64()
         rc = self.L.fi_serve_submit(self.h, C.byref(q), C.byref(rid))   # copies every array
         if rc:
             raise FiError(rc, "fi_serve_submit")
-        self._shapes[rid.value] = (wl.ny_ice, wl.nx_ice)
+        self._shapes[rid.value] = shape
         return rid.value
+
+    def submit(self, wl, t_end: Optional[float] = None, t0: float = 0.0, precision: int = 0,
+               dtt: Optional[float] = None) -> int:
+        return self.submit_prepared(self.prepare(wl, t_end, t0, precision, dtt))
 
     def info(self, rid: int) -> dict:
         i = _lib.FiRequestInfo()
@@ -119,3 +129,52 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+class Ensemble:
+    """Members (independent domains, any sizes) advanced in lockstep with
+    fi_batch_update: each coupling step enqueues one isos_update per member
+    on the member's own stream, so members overlap on the device."""
+
+    def __init__(self, workloads, precision: int = 1):
+        from .isostasy import Domain
+        self.L = _lib.load()
+        self.doms = []
+        self.bsl = (_lib.FiBsl * len(workloads))()
+        for i, wl in enumerate(workloads):
+            d = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=precision)
+            f = wl.padded_fields(d.nx, d.ny)
+            if f:
+                d.set_fields(**f)
+            b = self.bsl[i]
+            b.method, b.constant_ocean_surface = 0, 1
+            b.bsl_init = b.bsl_now = 0.0
+            b.A_ocean_pd = b.A_ocean_now = 3.625e14
+            d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+            self.doms.append(d)
+        self.wls = list(workloads)
+        self.hs = (C.c_void_p * len(self.doms))(*[d.h.value for d in self.doms])
+        self.t = 0.0
+
+    def first_update(self, t: float):
+        """Apply each member's ice load with a synchronous isos_update."""
+        for d, wl, i in zip(self.doms, self.wls, range(len(self.doms))):
+            d.update(wl.H_final, t, self.bsl[i])
+        self.t = t
+
+    def update(self, t: float):
+        rc = self.L.fi_batch_update(self.hs, len(self.doms), float(t), self.bsl)
+        if rc:
+            raise FiError(rc, "fi_batch_update")
+        self.t = t
+
+    def synchronize(self):
+        st = (C.c_int32 * len(self.doms))()
+        rc = self.L.fi_batch_synchronize(self.hs, len(self.doms), st)
+        if rc:
+            raise FiError(rc, "fi_batch_synchronize: member %d" % next(i for i, v in enumerate(st) if v))
+
+    def close(self):
+        for d in self.doms:
+            d.close()
+        self.doms = []

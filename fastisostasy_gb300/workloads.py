@@ -178,3 +178,40 @@ def ensemble_member(i: int, stage_mode=1, t_end=10e3) -> Workload:
         return {"eta_eff": 10.0 ** gaussian_random_field(ny, nx, d, seed=_i)}
     return Workload(name="member_%d" % i, params=p, nx_ice=n, ny_ice=n, dx=dx,
                     z_bed=np.full((n, n), 1e6), H_final=H, t_end=t_end, fields_fn=fields_fn)
+
+
+SERVE_SIZES = (64, 128, 256, 512, 1024)
+SERVE_WEIGHTS = (0.3, 0.3, 0.2, 0.15, 0.05)
+
+
+def serve_request(i: int, horizon_scale: float = 0.01, dx: float = 25e3) -> Workload:
+    """Request i of the serving stream: n drawn from SERVE_SIZES with
+    SERVE_WEIGHTS, seeded random-field mantle viscosity (log10 eta: mean 21,
+    std 0.25, correlation 500 km) and lithosphere thickness (mean 85 km, std
+    15 km, clipped to 50-120 km, mapped to rigidity with E = 66 GPa,
+    nu = 0.28), a disc or a parabolic dome load, horizon log-uniform in
+    1-100 kyr times `horizon_scale`.  RK4 with true stages at dt = 1 yr,
+    coupling every 10 yr; the spacing keeps dt = 1 yr inside RK4's stability
+    region for every draw."""
+    rng = np.random.default_rng(5000 + i)
+    n = int(rng.choice(SERVE_SIZES, p=SERVE_WEIGHTS))
+    horizon = float(np.exp(rng.uniform(np.log(1e3), np.log(1e5)))) * horizon_scale
+    horizon = max(10.0, 10.0 * np.ceil(horizon / 10.0))
+    L = n * dx
+    r0 = float(rng.uniform(0.15, 0.35)) * L
+    h0 = float(rng.uniform(500.0, 3000.0))
+    dome = bool(rng.random() < 0.5)
+    xc = (np.arange(n) - (n - 1) / 2.0) * dx
+    r = np.sqrt(xc[None, :] ** 2 + xc[:, None] ** 2)
+    H = np.where(r <= r0, h0 * (np.sqrt(np.clip(1.0 - (r / r0) ** 2, 0.0, 1.0)) if dome else 1.0), 0.0)
+    p = dict(P.DEFAULTS)
+    p.update(E=66.0, nu=0.28, dt_method=1, dt_init=1.0, dt_max=1.0, stage_mode=1, lithosphere=3, mantle=3)
+    seed = 7000 + i
+
+    def fields_fn(nx, ny, d, _s=seed):
+        He = np.clip(gaussian_random_field(ny, nx, d, mean=85e3, std=15e3, seed=_s), 50e3, 120e3)
+        D = 66.0 * 1e9 * He ** 3 / (12.0 * (1.0 - 0.28 ** 2))
+        eta = 10.0 ** gaussian_random_field(ny, nx, d, mean=21.0, std=0.25, seed=_s + 1)
+        return {"D_lith": D, "eta_eff": eta}
+    return Workload(name="request_%d" % i, params=p, nx_ice=n, ny_ice=n, dx=dx, z_bed=np.full((n, n), 1e6),
+                    H_final=H, dtt=10.0, t_end=horizon, fields_fn=fields_fn)

@@ -219,6 +219,15 @@ double fi_serve_clock(fi_server* s);
 /* Finishes every submitted request, then stops the scheduler. */
 int fi_serve_destroy(fi_server* s);
 
+/* Batched ensembles of handles driven in lockstep: one isos_update to `time`
+ * for each of n handles (bsl[i] is handle i's bsl_class), each enqueued on
+ * its handle's own stream without waiting, so members of different sizes
+ * overlap on the device.  The ice load of each member is the one it already
+ * holds.  fi_batch_synchronize waits for all and returns the first failing
+ * status (per-member statuses in `status` if not NULL). */
+int fi_batch_update(fi_handle* const* hs, int n, double time, fi_bsl* bsl);
+int fi_batch_synchronize(fi_handle* const* hs, int n, int32_t* status);
+
 /* Restart support: the complete device state (fields + integrator clock) as
  * doubles; bit-identical round trip. */
 size_t fi_state_size(const fi_handle* h);
