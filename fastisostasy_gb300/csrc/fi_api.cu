@@ -17,6 +17,7 @@
 #include "../../include/fi_gpu.h"
 #include "fi_engine.h"
 #include "fi_kernels.h"
+#include "fi_batch.h"
 #include "fi_state.h"
 
 using namespace fi;
@@ -520,12 +521,14 @@ template <typename T> struct TT {
 };
 
 // gate: optional device flag; the four kernels return at once when it is 0
+// whi/wlo: the state y as a float pair (mixed Tsit5), else null
 template <typename T>
-void rhs(fi_handle* h, const double* y, const double* wref, T* raw_out, const int* gate = nullptr)
+void rhs(fi_handle* h, const double* y, const double* wref, T* raw_out, const int* gate = nullptr,
+         const float* whi = nullptr, const float* wlo = nullptr)
 {
     typedef typename vec2<T>::type C2;
     PROF(h, K_FLEX, launch_flexure<T>(y, wref, (const T*)h->q0, h->d.mactive, (const T*)h->Dt, (const T*)h->inv2eta,
-                                      (T*)h->f, h->nx, h->ny, h->fc, h->s, gate));
+                                      (T*)h->f, h->nx, h->ny, h->fc, h->s, gate, whi, wlo));
     PROF(h, K_ROWS_FWD, launch_rows_fwd<T>((const T*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, h->prhs, h->s, gate));
     PROF(h, K_COLS_HARTLEY,
          launch_cols_hartley<T>((C2*)h->S, (const T*)h->mA, (const T*)h->mB, h->even, h->prhs, h->s, gate));
@@ -647,6 +650,7 @@ template <typename T> int integrate_tsit(fi_handle* h, double tf, int* have_rhs,
     *have_rhs = 0;
     *raw_last = r0;
     if (p.stage_mode == 1) return fail(h, FI_E_CONFIG, "tsit54 with true stages is not available on the device yet");
+    if (h->d.whi) split_hilo(h->d.w, h->d.whi, h->d.wlo, h->n, h->s);
     Ctl hc;
     CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
@@ -654,7 +658,7 @@ template <typename T> int integrate_tsit(fi_handle* h, double tf, int* have_rhs,
     int guard = 0;
     while (hc.t < tf && hc.status == ST_OK) {
         PROF(h, K_CONTROL, step_begin(h->ctl, 2, h->s));
-        if (need_rhs) { rhs<T>(h, h->d.w, nullptr, r0); *have_rhs = 1; }
+        if (need_rhs) { rhs<T>(h, h->d.w, nullptr, r0, nullptr, h->d.whi, h->d.wlo); *have_rhs = 1; }
         PROF(h, K_TS, ts_max<T>(h->d, r0, p.atol, p.rtol, h->s));
         PROF(h, K_TS, ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s));
         PROF(h, K_TS, ts_commit<T>(h->d, r0, h->s));
@@ -678,6 +682,10 @@ template <typename T> int enqueue_tsit_loop(fi_handle* h)
     T* r0 = (T*)h->raw[0];
     ts_loop_begin(h->ctl, h->s);
     h->launches += 1;
+    if (h->d.whi) {
+        split_hilo(h->d.w, h->d.whi, h->d.wlo, h->n, h->s);
+        h->launches += 1;
+    }
     cudaStreamCaptureStatus st;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t* deps = nullptr;
@@ -698,7 +706,7 @@ template <typename T> int enqueue_tsit_loop(fi_handle* h)
     cudaStream_t s0 = h->s;
     h->s = h->s_body;
     ts_attempt_begin(h->ctl, kMaxAttempts, h->s);
-    rhs<T>(h, h->d.w, nullptr, r0, &h->ctl->need_rhs);
+    rhs<T>(h, h->d.w, nullptr, r0, &h->ctl->need_rhs, h->d.whi, h->d.wlo);
     ts_max<T>(h->d, r0, p.atol, p.rtol, h->s);
     ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s);
     ts_commit<T>(h->d, r0, h->s);
@@ -1045,6 +1053,14 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     AL(h->ctl, sizeof(Ctl));
     d.ctl = h->ctl;
     AL(d.partials, (size_t)reduce_blocks(n) * 4 * sizeof(double));
+    if (p.dt_method == 2) {
+        AL(d.ts_x2, n * sizeof(double));
+        AL(d.ts_dx, n * sizeof(double));
+        if (mixed(h) && h->uniform) {
+            AL(d.whi, n * sizeof(float));
+            AL(d.wlo, n * sizeof(float));
+        }
+    }
     AL(h->y, n * 8);
     AL(h->q0, nT); AL(h->Dt, nT); AL(h->inv2eta, nT); AL(h->f, nT);
     for (int i = 0; i < 4; ++i) AL(h->raw[i], nT);
@@ -1519,3 +1535,345 @@ int fi_state_import(fi_handle* h, const double* buf)
 }
 
 }  // extern "C"
+
+// ---- batched ensembles ------------------------------------------------------
+// One update of every member as a single CUDA graph: the per-member update
+// head (sea level, masks, loads, convolutions) as parallel branches, then
+// one WHILE loop of batched Tsit5 attempts over all members (one launch per
+// pass for the whole ensemble), then the per-member update tails.
+struct fi_batch {
+    std::vector<fi_handle*> hs;
+    bool mixed = false;
+    int nm = 0;
+    cudaStream_t s = nullptr, s_body = nullptr;
+    cudaEvent_t ev_fork = nullptr;
+    std::vector<cudaEvent_t> ev;
+    BMember* dM = nullptr;
+    int* doff = nullptr;                 // 4 x (nm + 1): flexure, rows, columns, reductions
+    int nblk[4] = {0, 0, 0, 0};          // virtual blocks per phase (all members)
+    int grid[4] = {0, 0, 0, 0};          // resident grid per phase
+    int rows_threads = 32, cols_threads = 32;
+    size_t rows_smem = 0, cols_smem = 0;
+    static constexpr int kRing = 4;
+    BArgs* hargs[kRing] = {nullptr, nullptr, nullptr, nullptr};   // pinned
+    BArgs* dargs[kRing] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t args_ev[kRing] = {nullptr, nullptr, nullptr, nullptr};
+    int ring = 0;
+    cudaGraphExec_t g[2] = {nullptr, nullptr};
+    int seen[2] = {0, 0};
+    long long launches = 0;
+    int* dmore = nullptr;                // loop condition of the eager path
+    bool eager = false;
+};
+
+namespace {
+
+// One Tsit5 attempt of every member that still has one, as batched launches.
+template <typename T> void batch_attempt(fi_batch* b, cudaStream_t s, cudaGraphConditionalHandle loop, int* more_out)
+{
+    const int nm = b->nm;
+    const int* off = b->doff;
+    batch_attempt_begin(b->dM, nm, kMaxAttempts, s);
+    batch_flexure<T>(b->dM, off, nm, b->grid[0], s);
+    batch_rows_fwd<T>(b->dM, off + (nm + 1), nm, b->grid[1], b->rows_threads, b->rows_smem, s);
+    batch_cols_hartley<T>(b->dM, off + 2 * (nm + 1), nm, b->grid[2], b->cols_threads, b->cols_smem, s);
+    batch_rows_inv<T>(b->dM, off + (nm + 1), nm, b->grid[1], b->rows_threads, b->rows_smem, s);
+    batch_ts_max<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], s);
+    batch_ts_err<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], 100000, s);
+    batch_ts_commit<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], s);
+    batch_attempt_end(b->dM, nm, loop, s, more_out);
+    b->launches += 10;
+}
+
+// The same update without a graph: the host reads the loop condition after
+// every attempt (profiling; FI_BATCH_EAGER=1).
+template <typename T> int batch_eager(fi_batch* b, bool diag)
+{
+    auto fork_join = [&](auto&& body) -> int {
+        if (cudaEventRecord(b->ev_fork, b->s) != cudaSuccess) return FI_E_CUDA;
+        for (int i = 0; i < b->nm; ++i) {
+            fi_handle* h = b->hs[i];
+            if (cudaStreamWaitEvent(h->s, b->ev_fork, 0) != cudaSuccess) return FI_E_CUDA;
+            body(h);
+            if (cudaEventRecord(b->ev[i], h->s) != cudaSuccess) return FI_E_CUDA;
+            if (cudaStreamWaitEvent(b->s, b->ev[i], 0) != cudaSuccess) return FI_E_CUDA;
+        }
+        return FI_OK;
+    };
+    int rc = fork_join([&](fi_handle* h) {
+        enqueue_pre<T>(h, h->dH, diag, true);
+        if (h->d.whi) split_hilo(h->d.w, h->d.whi, h->d.wlo, h->n, h->s);
+    });
+    if (rc) return rc;
+    batch_loop_begin(b->dM, b->nm, b->s);
+    for (long long it = 0;; ++it) {
+        batch_attempt<T>(b, b->s, 0, b->dmore);
+        int more = 0;
+        if (cudaMemcpyAsync(&more, b->dmore, sizeof(int), cudaMemcpyDeviceToHost, b->s) != cudaSuccess ||
+            cudaStreamSynchronize(b->s) != cudaSuccess)
+            return FI_E_CUDA;
+        if (!more) break;
+        if (it > kMaxAttempts) return FI_E_STEP;
+    }
+    return fork_join([&](fi_handle* h) { enqueue_post<T>(h, (T*)h->raw[0], -1); });
+}
+
+template <typename T> int batch_capture(fi_batch* b, bool diag, cudaGraph_t* out)
+{
+    fi_handle* h0 = b->hs[0];
+    const fi_params& p0 = h0->p;
+    auto ck = [&](cudaError_t e) { return e == cudaSuccess ? FI_OK : FI_E_CUDA; };
+    int rc;
+    if ((rc = ck(cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal)))) return rc;
+    auto join_members = [&](auto&& body) -> int {
+        if (cudaEventRecord(b->ev_fork, b->s) != cudaSuccess) return FI_E_CUDA;
+        for (int i = 0; i < b->nm; ++i) {
+            fi_handle* h = b->hs[i];
+            if (cudaStreamWaitEvent(h->s, b->ev_fork, 0) != cudaSuccess) return FI_E_CUDA;
+            body(h);
+            if (cudaEventRecord(b->ev[i], h->s) != cudaSuccess) return FI_E_CUDA;
+            if (cudaStreamWaitEvent(b->s, b->ev[i], 0) != cudaSuccess) return FI_E_CUDA;
+        }
+        return FI_OK;
+    };
+    rc = join_members([&](fi_handle* h) {
+        enqueue_pre<T>(h, h->dH, diag, true);
+        if (h->d.whi) split_hilo(h->d.w, h->d.whi, h->d.wlo, h->n, h->s);
+    });
+    if (!rc) {
+        batch_loop_begin(b->dM, b->nm, b->s);
+        cudaStreamCaptureStatus st;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        cudaGraphConditionalHandle loop;
+        cudaGraphNode_t node;
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        if (cudaStreamGetCaptureInfo(b->s, &st, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess ||
+            cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+            rc = FI_E_CUDA;
+        } else {
+            cp.conditional.handle = loop;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp) != cudaSuccess ||
+                cudaStreamUpdateCaptureDependencies(b->s, &node, nullptr, 1, cudaStreamSetCaptureDependencies) !=
+                    cudaSuccess ||
+                cudaStreamBeginCaptureToGraph(b->s_body, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                rc = FI_E_CUDA;
+            } else {
+                batch_attempt<T>(b, b->s_body, loop, nullptr);
+                cudaGraph_t body_out = nullptr;
+                if (cudaStreamEndCapture(b->s_body, &body_out) != cudaSuccess) rc = FI_E_CUDA;
+            }
+        }
+    }
+    if (!rc) rc = join_members([&](fi_handle* h) { enqueue_post<T>(h, (T*)h->raw[0], -1); });
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->s, &graph);
+    if (rc || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return rc ? rc : FI_E_CUDA;
+    }
+    (void)p0;
+    *out = graph;
+    return FI_OK;
+}
+
+void batch_free(fi_batch* b)
+{
+    for (auto& g : b->g)
+        if (g) cudaGraphExecDestroy(g);
+    if (b->s) cudaStreamSynchronize(b->s);
+    cudaFree(b->dM);
+    cudaFree(b->doff);
+    cudaFree(b->dmore);
+    for (int i = 0; i < fi_batch::kRing; ++i) {
+        if (b->hargs[i]) cudaFreeHost(b->hargs[i]);
+        cudaFree(b->dargs[i]);
+        if (b->args_ev[i]) cudaEventDestroy(b->args_ev[i]);
+    }
+    for (auto e : b->ev)
+        if (e) cudaEventDestroy(e);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->s) cudaStreamDestroy(b->s);
+    if (b->s_body) cudaStreamDestroy(b->s_body);
+    delete b;
+}
+
+}  // namespace
+
+int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
+{
+    if (!hs || n < 1 || !out) return FI_E_ARG;
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        fi_handle* h = hs[i];
+        if (!h) return FI_E_ARG;
+        if (!h->state_ready) return fail(h, FI_E_STATE, "fi_batch_create before fi_init_state");
+        const fi_handle* h0 = hs[0];
+        if (h->p.dt_method != 2 || h->p.stage_mode != 0 || mixed(h) != mixed(h0) ||
+            h->p.dt_diagnostics != h0->p.dt_diagnostics || h->time_diag != h0->time_diag || !h->tsit_graph_ok)
+            return fail(h, FI_E_CONFIG,
+                        "batched members must run reference-compatible tsit54 in the same precision, in lockstep");
+    }
+    fi_batch* b = new fi_batch();
+    b->hs.assign(hs, hs + n);
+    b->nm = n;
+    b->mixed = mixed(hs[0]);
+    std::vector<BMember> M(n);
+    std::vector<int> off(4 * (n + 1), 0);
+    const size_t c2 = b->mixed ? sizeof(float2) : sizeof(double2);
+    for (int i = 0; i < n; ++i) {
+        fi_handle* h = hs[i];
+        BMember& m = M[i];
+        memset(&m, 0, sizeof(m));
+        m.p = h->prhs;
+        m.fc = h->fc;
+        m.fcf = flex_coef_f32(h->fc);
+        m.y = h->d.w;
+        m.q0 = h->q0;
+        m.mask = h->d.mactive;
+        m.D = h->Dt;
+        m.inv2eta = h->inv2eta;
+        m.f = h->f;
+        m.S = h->S;
+        m.mA = h->mA;
+        m.mB = h->mB;
+        m.raw = h->raw[0];
+        m.even = h->even;
+        m.RB = rhs_rows_per_block(m.p.h);
+        m.CB = b->mixed ? rhs_cols_per_block<float>(m.p.ny) : rhs_cols_per_block<double>(m.p.ny);
+        m.fgx = (m.p.nx + 31) / 32;
+        m.red_nblk = ts_grid(h->n);
+        m.d = h->d;
+        m.atol = h->p.atol;
+        m.rtol = h->p.rtol;
+        m.q = h->p.q;
+        m.dt_max = h->p.dt_max;
+        const int fblk = m.fgx * ((m.p.ny + 7) / 8);
+        const int rblk = (m.p.ny + m.RB - 1) / m.RB;
+        const int cblk = (m.p.h + 1 + m.CB - 1) / m.CB;
+        off[i + 1] = off[i] + fblk;
+        off[(n + 1) + i + 1] = off[(n + 1) + i] + rblk;
+        off[2 * (n + 1) + i + 1] = off[2 * (n + 1) + i] + cblk;
+        off[3 * (n + 1) + i + 1] = off[3 * (n + 1) + i] + m.red_nblk;
+        const int rt = rhs_threads_for(m.RB * m.p.h / 4), ct = rhs_threads_for(m.CB * m.p.ny / 4);
+        if (rt > b->rows_threads) b->rows_threads = rt;
+        if (ct > b->cols_threads) b->cols_threads = ct;
+        const size_t rs = 2 * (size_t)m.RB * m.p.h * c2, cs = 2 * (size_t)m.CB * m.p.ny * c2;
+        if (rs > b->rows_smem) b->rows_smem = rs;
+        if (cs > b->cols_smem) b->cols_smem = cs;
+    }
+    for (int k = 0; k < 4; ++k) b->nblk[k] = off[k * (n + 1) + n];
+    bool ok = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&b->s_body, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaMalloc(&b->dM, n * sizeof(BMember)) == cudaSuccess &&
+              cudaMalloc(&b->doff, off.size() * sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&b->dmore, sizeof(int)) == cudaSuccess;
+    if (const char* e = getenv("FI_BATCH_EAGER")) b->eager = (e[0] == '1');
+    b->ev.assign(n, nullptr);
+    for (int i = 0; ok && i < n; ++i) ok = cudaEventCreateWithFlags(&b->ev[i], cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; ok && i < fi_batch::kRing; ++i)
+        ok = cudaMallocHost(&b->hargs[i], n * sizeof(BArgs)) == cudaSuccess &&
+             cudaMalloc(&b->dargs[i], n * sizeof(BArgs)) == cudaSuccess &&
+             cudaEventCreateWithFlags(&b->args_ev[i], cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaMemcpy(b->dM, M.data(), n * sizeof(BMember), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(b->doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (!ok) {
+        batch_free(b);
+        return FI_E_OOM;
+    }
+    int res[4];
+    if (b->mixed) {
+        batch_prepare<float>(b->rows_smem, b->cols_smem);
+        batch_grids<float>(b->rows_smem, b->cols_smem, b->rows_threads, b->cols_threads, &res[0], &res[1], &res[2],
+                           &res[3]);
+    } else {
+        batch_prepare<double>(b->rows_smem, b->cols_smem);
+        batch_grids<double>(b->rows_smem, b->cols_smem, b->rows_threads, b->cols_threads, &res[0], &res[1], &res[2],
+                            &res[3]);
+    }
+    // resident grid times FI_BATCH_WAVES (default 4) waves, at most one block per virtual block
+    int waves = 4;
+    if (const char* e = getenv("FI_BATCH_WAVES")) waves = atoi(e);
+    for (int k = 0; k < 4; ++k) {
+        const long long g = waves > 0 ? (long long)res[k] * waves : (long long)b->nblk[k];
+        b->grid[k] = (int)(g < b->nblk[k] ? g : b->nblk[k]);
+    }
+    *out = b;
+    return FI_OK;
+}
+
+int fi_batch_step(fi_batch* b, double time, fi_bsl* bsl)
+{
+    if (!b || !bsl) return FI_E_ARG;
+    fi_handle* h0 = b->hs[0];
+    const bool diag = time - h0->time_diag >= sp(1e-3);   // the same for every member (lockstep)
+    const int key = diag ? 1 : 0;
+    if (!b->seen[key]) {
+        // first update of this kind: each member on its own path (sets kernel
+        // attributes and per-handle graphs), then the batch stream joins
+        b->seen[key] = 1;
+        for (int i = 0; i < b->nm; ++i) {
+            if (int rc = fi_update_async(b->hs[i], nullptr, time, &bsl[i])) return rc;
+            if (cudaEventRecord(b->ev[i], b->hs[i]->s) != cudaSuccess ||
+                cudaStreamWaitEvent(b->s, b->ev[i], 0) != cudaSuccess)
+                return FI_E_CUDA;
+        }
+        return FI_OK;
+    }
+    // host side of isos_update for every member (src/fastisostasy.f90:782-787)
+    BArgs* ha = b->hargs[b->ring];
+    if (cudaEventSynchronize(b->args_ev[b->ring]) != cudaSuccess) return FI_E_CUDA;   // ring slot free
+    for (int i = 0; i < b->nm; ++i) {
+        fi_handle* h = b->hs[i];
+        if (diag) h->time_diag = h->time_diag + h->p.dt_diagnostics;
+        h->time_prog = time;
+        ha[i].ctl = h->ctl;
+        ha[i].tf = time;
+        ha[i].bsl = bsl[i].bsl_now;
+        ha[i].A_ocean = bsl[i].A_ocean_now;
+        ha[i].method = bsl[i].method;
+        ha[i].write_bsl = (bsl[i].method == 0 || bsl[i].method == 1) ? 1 : 0;
+    }
+    if (cudaMemcpyAsync(b->dargs[b->ring], ha, b->nm * sizeof(BArgs), cudaMemcpyHostToDevice, b->s) != cudaSuccess)
+        return FI_E_CUDA;
+    batch_set_args(b->dargs[b->ring], b->nm, b->s);
+    if (cudaEventRecord(b->args_ev[b->ring], b->s) != cudaSuccess) return FI_E_CUDA;
+    b->ring = (b->ring + 1) % fi_batch::kRing;
+    if (b->eager) return b->mixed ? batch_eager<float>(b, diag) : batch_eager<double>(b, diag);
+    if (!b->g[key]) {
+        cudaGraph_t graph = nullptr;
+        const int rc = b->mixed ? batch_capture<float>(b, diag, &graph) : batch_capture<double>(b, diag, &graph);
+        if (rc) return rc;
+        const cudaError_t e = cudaGraphInstantiate(&b->g[key], graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return FI_E_CUDA;
+    }
+    if (cudaGraphLaunch(b->g[key], b->s) != cudaSuccess) return FI_E_CUDA;
+    return FI_OK;
+}
+
+int fi_batch_wait(fi_batch* b, int32_t* status)
+{
+    if (!b) return FI_E_ARG;
+    if (cudaStreamSynchronize(b->s) != cudaSuccess) return FI_E_CUDA;
+    int first = FI_OK;
+    for (int i = 0; i < b->nm; ++i) {
+        const int rc = fi_synchronize(b->hs[i]);
+        if (status) status[i] = rc;
+        if (rc && first == FI_OK) first = rc;
+    }
+    return first;
+}
+
+int fi_batch_destroy(fi_batch* b)
+{
+    if (!b) return FI_E_ARG;
+    batch_free(b);
+    return FI_OK;
+}

@@ -1,0 +1,122 @@
+// fi_batch.h — batched launches over the members of an ensemble.
+//
+// A batched launch runs one pass of the reference-compatible Tsit5 attempt
+// (flexure stencil, row rFFT, Hartley column pass, inverse row rFFT, the two
+// error-norm reductions, the state commit) for every member of an ensemble
+// in a single kernel launch: member m owns the blocks [off[m], off[m+1]) and
+// runs exactly the blocks its own single-domain launch would run, so every
+// member gets the bits it gets alone.  Members may differ in size.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fi_common.cuh"
+#include "fi_kernels.h"
+#include "fi_state.h"
+
+namespace fi {
+
+struct BMember {
+    Plan2D p;                 // RHS transform plan
+    FlexCoef fc;              // flexure coefficients
+    FlexCoefF fcf;            // the same in float (mixed form)
+    const double* y;          // the RHS is evaluated at now%w
+    const void* q0;           // load term (T)
+    const uint8_t* mask;
+    const void* D;            // rigidity (T)
+    const void* inv2eta;      // 1/(2 eta) (T)
+    void* f;                  // flexure output (T)
+    void* S;                  // half spectrum (T complex)
+    const void* mA;           // 1/(kappa R) at (k, l), (-k, l) (T)
+    const void* mB;
+    void* raw;                // RHS output (T)
+    int even;
+    int RB, CB;               // rows per row block, columns per column block
+    int fgx;                  // flexure blocks along x
+    int red_nblk;             // blocks of the reduction kernels
+    Dom d;
+    double atol, rtol, q, dt_max;
+};
+
+// per-update scalars of one member (k_set_args)
+struct BArgs {
+    Ctl* ctl;
+    double tf, bsl, A_ocean;
+    int method, write_bsl;
+};
+
+// Block shapes of the single-domain launches (shared with the batched ones).
+int rhs_rows_per_block(int h);
+int rhs_threads_for(int work);
+template <typename T> int rhs_cols_per_block(int ny);
+int reduce_grid(size_t n);
+int ts_grid(size_t n);           // blocks of the Tsit5 attempt reductions
+
+// Raise the shared-memory limits of the batched transform kernels (before
+// any capture).
+template <typename T> void batch_prepare(size_t rows_smem, size_t cols_smem);
+
+// Resident blocks per SM of the batched reduction kernels.
+template <typename T> int batch_red_resident();
+// Resident grid sizes of the batched kernels (blocks per launch).
+template <typename T> void batch_grids(size_t rows_smem, size_t cols_smem, int rows_threads, int cols_threads,
+                                       int* g_flex, int* g_rows, int* g_cols, int* g_red);
+
+// Phase kernels over all members; nblk is the launch's (resident) grid.
+template <typename T> void batch_flexure(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s);
+template <typename T>
+void batch_rows_fwd(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s);
+template <typename T>
+void batch_cols_hartley(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s);
+template <typename T>
+void batch_rows_inv(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s);
+template <typename T> void batch_ts_max(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s);
+template <typename T>
+void batch_ts_err(const BMember* M, const int* off, int nm, int nblk, int max_reject, cudaStream_t s);
+template <typename T> void batch_ts_commit(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s);
+void batch_loop_begin(const BMember* M, int nm, cudaStream_t s);
+void batch_attempt_begin(const BMember* M, int nm, int max_iter, cudaStream_t s);
+// more_out == NULL: sets the WHILE condition `loop`; else writes it there
+void batch_attempt_end(const BMember* M, int nm, cudaGraphConditionalHandle loop, cudaStream_t s,
+                       int* more_out = nullptr);
+void batch_set_args(const BArgs* a, int nm, cudaStream_t s);
+
+// member owning global block b of a batched launch (off has nm + 1 entries)
+__device__ __forceinline__ int batch_member(const int* __restrict__ off, int nm, int b)
+{
+    int lo = 0, hi = nm - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Grid-stride walk over the virtual blocks of a batched launch: member m
+// owns virtual blocks [off[m], off[m+1]); fn(m, local block) runs for the
+// virtual blocks of members with active(m) (uniform over the block), and a
+// member without work is skipped in one jump.  Launches therefore size their
+// grid to what stays resident, not to the members' total block count.
+template <typename Act, typename Fn>
+__device__ __forceinline__ void batch_walk(const int* __restrict__ off, int nm, Act active, Fn fn)
+{
+    const int total = __ldg(off + nm);
+    const int stride = (int)gridDim.x;
+    int vb = (int)blockIdx.x;
+    if (vb >= total) return;
+    int m = batch_member(off, nm, vb);
+    while (vb < total) {
+        while (__ldg(off + m + 1) <= vb) ++m;
+        const int end = __ldg(off + m + 1);
+        if (!active(m)) {
+            vb += ((end - vb + stride - 1) / stride) * stride;
+            continue;
+        }
+        fn(m, vb - __ldg(off + m));
+        vb += stride;
+    }
+}
+
+}  // namespace fi

@@ -17,6 +17,26 @@ struct FlexCoef {
     const double* dym;
 };
 
+// The same coefficients rounded to float (mixed form, uniform spacing).
+struct FlexCoefF {
+    float nu, one_minus_nu, coef_mantle, inv_dx, inv_2dx, inv_dx2, inv_dy, inv_2dy, inv_dy2;
+};
+
+inline FlexCoefF flex_coef_f32(const FlexCoef& c)
+{
+    FlexCoefF f;
+    f.nu = (float)c.nu;
+    f.one_minus_nu = (float)c.one_minus_nu;
+    f.coef_mantle = (float)c.coef_mantle;
+    f.inv_dx = (float)c.inv_dx;
+    f.inv_2dx = (float)c.inv_2dx;
+    f.inv_dx2 = (float)c.inv_dx2;
+    f.inv_dy = (float)c.inv_dy;
+    f.inv_2dy = (float)c.inv_2dy;
+    f.inv_dy2 = (float)c.inv_dy2;
+    return f;
+}
+
 // One FFT length: factorisation + twiddle tables in both precisions.
 struct FftLen {
     FftDesc d;
@@ -34,11 +54,13 @@ struct Plan2D {
 };
 
 // The RHS launchers take an optional device flag: when it points at 0 every
-// block returns at once (device-side skipping inside a graph loop).
+// block returns at once (device-side skipping inside a graph loop).  The
+// mixed-form flexure can take the state as a float pair y = whi + wlo
+// (uniform spacing, no mantle term), which keeps it free of FP64 work.
 template <typename T>
 void launch_flexure(const double* y, const double* wref, const T* q0, const uint8_t* mask, const T* D,
                     const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s,
-                    const int* gate = nullptr);
+                    const int* gate = nullptr, const float* whi = nullptr, const float* wlo = nullptr);
 
 template <typename T>
 void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, typename vec2<T>::type* S,

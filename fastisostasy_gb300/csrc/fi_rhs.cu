@@ -21,6 +21,7 @@
 
 #include "fi_fft.cuh"
 
+#include "fi_batch.h"
 #include "fi_kernels.h"
 
 namespace fi {
@@ -74,12 +75,10 @@ template <typename K> static void set_smem(K kern, size_t bytes)
 constexpr int TX = 32, TY = 8, RX = TX + 4, RY = TY + 4;
 
 template <typename T>
-__global__ void __launch_bounds__(TX* TY)
-k_flexure(const double* __restrict__ y, const double* __restrict__ wref, const T* __restrict__ q0,
+__device__ __forceinline__ void flexure_body(const double* __restrict__ y, const double* __restrict__ wref, const T* __restrict__ q0,
           const uint8_t* __restrict__ mask, const T* __restrict__ D, const T* __restrict__ inv2eta,
-          T* __restrict__ f, int nx, int ny, FlexCoef c, const int* __restrict__ gate)
+          T* __restrict__ f, int nx, int ny, FlexCoef c, int bx, int by)
 {
-    if (gate && *gate == 0) return;
     __shared__ double ys[RY][RX];
     __shared__ T wx[RY][RX];
     __shared__ T Mxx[RY][RX];
@@ -87,7 +86,7 @@ k_flexure(const double* __restrict__ y, const double* __restrict__ wref, const T
     __shared__ T Mxy[RY][RX];
     __shared__ T Mxyx[RY][RX];
     const int tid = threadIdx.x + TX * threadIdx.y;
-    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const int i0 = bx * TX, j0 = by * TY;
     const bool uni = (c.dxm == nullptr);
 
     // per-cell spacing accessors (uniform fast path)
@@ -186,6 +185,16 @@ k_flexure(const double* __restrict__ y, const double* __restrict__ wref, const T
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(TX* TY)
+k_flexure(const double* __restrict__ y, const double* __restrict__ wref, const T* __restrict__ q0,
+          const uint8_t* __restrict__ mask, const T* __restrict__ D, const T* __restrict__ inv2eta,
+          T* __restrict__ f, int nx, int ny, FlexCoef c, const int* __restrict__ gate)
+{
+    if (gate && *gate == 0) return;
+    flexure_body<T>(y, wref, q0, mask, D, inv2eta, f, nx, ny, c, blockIdx.x, blockIdx.y);
+}
+
 // Mixed form, uniform spacing.  The only double work per cell is the pair of
 // forward differences of the double state, dX = y[i+1]-y[i] and
 // dY = y[j+1]-y[j] (taken before rounding to float, so the second
@@ -193,17 +202,20 @@ k_flexure(const double* __restrict__ y, const double* __restrict__ wref, const T
 // mantle term y - w_ref.  Central and second differences are rebuilt
 // exactly from them: y[i+1]-y[i-1] = dX[i]+dX[i-1],
 // y[i+1]-2y[i]+y[i-1] = dX[i]-dX[i-1].
-struct FlexCoefF {
-    float nu, one_minus_nu, coef_mantle, inv_dx, inv_2dx, inv_dx2, inv_dy, inv_2dy, inv_dy2;
-};
-
-__global__ void __launch_bounds__(TX* TY)
-k_flexure_f32(const double* __restrict__ y, const double* __restrict__ wref, const float* __restrict__ q0,
-              const uint8_t* __restrict__ mask, const float* __restrict__ D, const float* __restrict__ inv2eta,
-              float* __restrict__ f, int nx, int ny, FlexCoefF c, const int* __restrict__ gate)
+// HILO: the state arrives as a float pair y = hi + lo (whi, wlo) instead of
+// doubles, and the first differences are (hi[i+1]-hi[i]) + (lo[i+1]-lo[i]),
+// all in float (no mantle term in this form).
+template <bool HILO>
+__device__ __forceinline__ void flexure_f32_body(const double* __restrict__ y, const double* __restrict__ wref,
+                                                 const float* __restrict__ q0, const uint8_t* __restrict__ mask,
+                                                 const float* __restrict__ D, const float* __restrict__ inv2eta,
+                                                 float* __restrict__ f, int nx, int ny, FlexCoefF c, int bx, int by,
+                                                 const float* __restrict__ whi = nullptr,
+                                                 const float* __restrict__ wlo = nullptr)
 {
-    if (gate && *gate == 0) return;
-    __shared__ double ys[RY][RX];
+    __shared__ double ys[HILO ? 1 : RY][HILO ? 1 : RX];
+    __shared__ float yh[HILO ? RY : 1][HILO ? RX : 1];
+    __shared__ float yl[HILO ? RY : 1][HILO ? RX : 1];
     __shared__ float dX[RY][RX];
     __shared__ float dY[RY][RX];
     __shared__ float Wx[RY][RX];
@@ -212,17 +224,28 @@ k_flexure_f32(const double* __restrict__ y, const double* __restrict__ wref, con
     __shared__ float Mxy[RY][RX];
     __shared__ float Mxyx[RY][RX];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int i0 = blockIdx.x * TX - 2, j0 = blockIdx.y * TY - 2;   // global index of lx = ly = 0
+    const int i0 = bx * TX - 2, j0 = by * TY - 2;   // global index of lx = ly = 0
     for (int ly = ty; ly < RY; ly += TY)
         for (int lx = tx; lx < RX; lx += TX) {
             const int gi = i0 + lx, gj = j0 + ly;
-            ys[ly][lx] = (gi >= 0 && gi < nx && gj >= 0 && gj < ny) ? y[(size_t)gj * nx + gi] : 0.0;
+            const bool in = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+            if constexpr (HILO) {
+                yh[ly][lx] = in ? whi[(size_t)gj * nx + gi] : 0.f;
+                yl[ly][lx] = in ? wlo[(size_t)gj * nx + gi] : 0.f;
+            } else {
+                ys[ly][lx] = in ? y[(size_t)gj * nx + gi] : 0.0;
+            }
         }
     __syncthreads();
     for (int ly = ty; ly < RY; ly += TY)
         for (int lx = tx; lx < RX; lx += TX) {
-            if (lx < RX - 1) dX[ly][lx] = (float)(ys[ly][lx + 1] - ys[ly][lx]);
-            if (ly < RY - 1) dY[ly][lx] = (float)(ys[ly + 1][lx] - ys[ly][lx]);
+            if constexpr (HILO) {
+                if (lx < RX - 1) dX[ly][lx] = (yh[ly][lx + 1] - yh[ly][lx]) + (yl[ly][lx + 1] - yl[ly][lx]);
+                if (ly < RY - 1) dY[ly][lx] = (yh[ly + 1][lx] - yh[ly][lx]) + (yl[ly + 1][lx] - yl[ly][lx]);
+            } else {
+                if (lx < RX - 1) dX[ly][lx] = (float)(ys[ly][lx + 1] - ys[ly][lx]);
+                if (ly < RY - 1) dY[ly][lx] = (float)(ys[ly + 1][lx] - ys[ly][lx]);
+            }
         }
     __syncthreads();
     for (int ly = ty; ly < RY; ly += TY)
@@ -284,27 +307,44 @@ k_flexure_f32(const double* __restrict__ y, const double* __restrict__ wref, con
     float p = 0.f;
     if (mask[e]) {
         p = q0[e];
-        if (wref) p += c.coef_mantle * (float)(ys[ly][lx] - wref[e]);
+        if constexpr (!HILO) {
+            if (wref) p += c.coef_mantle * (float)(ys[ly][lx] - wref[e]);
+        }
     }
     f[e] = (((p + mx_xx) + 2.f * mxy_xy) + my_yy) * inv2eta[e];
 }
 
+__global__ void __launch_bounds__(TX* TY)
+k_flexure_f32(const double* __restrict__ y, const double* __restrict__ wref, const float* __restrict__ q0,
+              const uint8_t* __restrict__ mask, const float* __restrict__ D, const float* __restrict__ inv2eta,
+              float* __restrict__ f, int nx, int ny, FlexCoefF c, const int* __restrict__ gate)
+{
+    if (gate && *gate == 0) return;
+    flexure_f32_body<false>(y, wref, q0, mask, D, inv2eta, f, nx, ny, c, blockIdx.x, blockIdx.y);
+}
+
+__global__ void __launch_bounds__(TX* TY)
+k_flexure_f32_hilo(const float* __restrict__ whi, const float* __restrict__ wlo, const float* __restrict__ q0,
+                   const uint8_t* __restrict__ mask, const float* __restrict__ D, const float* __restrict__ inv2eta,
+                   float* __restrict__ f, int nx, int ny, FlexCoefF c, const int* __restrict__ gate)
+{
+    if (gate && *gate == 0) return;
+    flexure_f32_body<true>(nullptr, nullptr, q0, mask, D, inv2eta, f, nx, ny, c, blockIdx.x, blockIdx.y, whi, wlo);
+}
+
 template <typename T>
 void launch_flexure(const double* y, const double* wref, const T* q0, const uint8_t* mask, const T* D,
-                    const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s, const int* gate)
+                    const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s, const int* gate,
+                    const float* whi, const float* wlo)
 {
     dim3 b(TX, TY), g((nx + TX - 1) / TX, (ny + TY - 1) / TY);
     if (sizeof(T) == 4 && c.dxm == nullptr) {
-        FlexCoefF cf;
-        cf.nu = (float)c.nu;
-        cf.one_minus_nu = (float)c.one_minus_nu;
-        cf.coef_mantle = (float)c.coef_mantle;
-        cf.inv_dx = (float)c.inv_dx;
-        cf.inv_2dx = (float)c.inv_2dx;
-        cf.inv_dx2 = (float)c.inv_dx2;
-        cf.inv_dy = (float)c.inv_dy;
-        cf.inv_2dy = (float)c.inv_2dy;
-        cf.inv_dy2 = (float)c.inv_dy2;
+        const FlexCoefF cf = flex_coef_f32(c);
+        if (whi && !wref) {
+            k_flexure_f32_hilo<<<g, b, 0, s>>>(whi, wlo, (const float*)q0, mask, (const float*)D,
+                                               (const float*)inv2eta, (float*)f, nx, ny, cf, gate);
+            return;
+        }
         k_flexure_f32<<<g, b, 0, s>>>(y, wref, (const float*)q0, mask, (const float*)D, (const float*)inv2eta,
                                       (float*)f, nx, ny, cf, gate);
         return;
@@ -331,16 +371,15 @@ static int threads_for(int work)
 }
 
 template <typename T>
-__global__ void k_rows_fwd(const T* __restrict__ in, int in_pitch, int in_width, int nrows_in,
-                           typename vec2<T>::type* __restrict__ S, Plan2D p, int RB, const int* __restrict__ gate)
+__device__ __forceinline__ void rows_fwd_body(const T* __restrict__ in, int in_pitch, int in_width, int nrows_in,
+                           typename vec2<T>::type* __restrict__ S, Plan2D p, int RB, int bx, int by)
 {
-    if (gate && *gate == 0) return;
     typedef typename vec2<T>::type C2;
     extern __shared__ unsigned char smem_raw[];
     C2* b0 = reinterpret_cast<C2*>(smem_raw);
     C2* b1 = b0 + RB * p.h;
     const int h = p.h;
-    const int j0 = blockIdx.x * RB;
+    const int j0 = bx * RB;
     const int nthr = blockDim.x;
     for (int e = threadIdx.x; e < RB * h; e += nthr) {
         const int line = e / h, m = e - line * h;
@@ -377,6 +416,14 @@ __global__ void k_rows_fwd(const T* __restrict__ in, int in_pitch, int in_width,
 }
 
 template <typename T>
+__global__ void k_rows_fwd(const T* __restrict__ in, int in_pitch, int in_width, int nrows_in,
+                           typename vec2<T>::type* __restrict__ S, Plan2D p, int RB, const int* __restrict__ gate)
+{
+    if (gate && *gate == 0) return;
+    rows_fwd_body<T>(in, in_pitch, in_width, nrows_in, S, p, RB, blockIdx.x, 0);
+}
+
+template <typename T>
 void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, typename vec2<T>::type* S,
                      const Plan2D& p, cudaStream_t s, const int* gate)
 {
@@ -389,16 +436,15 @@ void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, type
 }
 
 template <typename T>
-__global__ void k_rows_inv(const typename vec2<T>::type* __restrict__ S, int nrows, T* __restrict__ out,
-                           int out_pitch, Plan2D p, int RB, T scale, const int* __restrict__ gate)
+__device__ __forceinline__ void rows_inv_body(const typename vec2<T>::type* __restrict__ S, int nrows, T* __restrict__ out,
+                           int out_pitch, Plan2D p, int RB, T scale, int bx, int by)
 {
-    if (gate && *gate == 0) return;
     typedef typename vec2<T>::type C2;
     extern __shared__ unsigned char smem_raw[];
     C2* b0 = reinterpret_cast<C2*>(smem_raw);
     C2* b1 = b0 + RB * p.h;
     const int h = p.h;
-    const int j0 = blockIdx.x * RB;
+    const int j0 = bx * RB;
     const int nthr = blockDim.x;
     const C2* rtw = rtwp<T>(p);
     // Z[k] = (X[k] + conj X[h-k]) + i conj(w^k) (X[k] - conj X[h-k])
@@ -428,6 +474,14 @@ __global__ void k_rows_inv(const typename vec2<T>::type* __restrict__ S, int nro
         v.y *= scale;
         *reinterpret_cast<C2*>(out + (size_t)j * out_pitch + 2 * m) = v;
     }
+}
+
+template <typename T>
+__global__ void k_rows_inv(const typename vec2<T>::type* __restrict__ S, int nrows, T* __restrict__ out,
+                           int out_pitch, Plan2D p, int RB, T scale, const int* __restrict__ gate)
+{
+    if (gate && *gate == 0) return;
+    rows_inv_body<T>(S, nrows, out, out_pitch, p, RB, scale, blockIdx.x, 0);
 }
 
 template <typename T>
@@ -473,16 +527,15 @@ __device__ __forceinline__ void load_cols(typename vec2<T>::type* b0, const type
 }
 
 template <typename T>
-__global__ void k_cols_hartley(typename vec2<T>::type* __restrict__ S, const T* __restrict__ mA,
-                               const T* __restrict__ mB, int even, Plan2D p, int CB, const int* __restrict__ gate)
+__device__ __forceinline__ void cols_hartley_body(typename vec2<T>::type* __restrict__ S, const T* __restrict__ mA,
+                               const T* __restrict__ mB, int even, Plan2D p, int CB, int bx, int by)
 {
-    if (gate && *gate == 0) return;
     typedef typename vec2<T>::type C2;
     extern __shared__ unsigned char smem_raw[];
     const int ny = p.col.d.n;
     C2* b0 = reinterpret_cast<C2*>(smem_raw);
     C2* b1 = b0 + (size_t)CB * ny;
-    const int k0 = blockIdx.x * CB;
+    const int k0 = bx * CB;
     load_cols<T>(b0, S, k0, CB, ny, p);
     __syncthreads();
     C2* r = block_fft<T>(b0, b1, p.col.d, CB, ny, twp<T>(p.col), -1);
@@ -525,6 +578,14 @@ __global__ void k_cols_hartley(typename vec2<T>::type* __restrict__ S, const T* 
         const int k = k0 + c;
         if (k <= p.h) S[(size_t)l * p.sp + k] = q[c * ny + l];
     }
+}
+
+template <typename T>
+__global__ void k_cols_hartley(typename vec2<T>::type* __restrict__ S, const T* __restrict__ mA,
+                               const T* __restrict__ mB, int even, Plan2D p, int CB, const int* __restrict__ gate)
+{
+    if (gate && *gate == 0) return;
+    cols_hartley_body<T>(S, mA, mB, even, p, CB, blockIdx.x, 0);
 }
 
 template <typename T>
@@ -667,9 +728,139 @@ void launch_conv_rows_inv(const typename vec2<T>::type* S, int n_out, double* ou
                                                                    corner_col1, p, RB, (T)scale);
 }
 
+// ---------------------------------------------------------------------------
+// Batched launches: the same bodies over every member of an ensemble.  A
+// member whose attempt needs no new RHS (need_rhs == 0) returns at once.
+// ---------------------------------------------------------------------------
+int rhs_rows_per_block(int h) { return rows_per_block(h); }
+int rhs_threads_for(int work) { return threads_for(work); }
+template <typename T> int rhs_cols_per_block(int ny) { return cols_per_block<T>(ny); }
+template int rhs_cols_per_block<float>(int);
+template int rhs_cols_per_block<double>(int);
+
+template <typename T>
+__global__ void __launch_bounds__(TX* TY) k_b_flexure(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+{
+    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+        const BMember& b = M[m];
+        const int bx = local % b.fgx, by = local / b.fgx;
+        if constexpr (sizeof(T) == 4) {
+            if (b.fc.dxm == nullptr) {
+                const FlexCoefF cf = b.fcf;
+                if (b.d.whi)
+                    flexure_f32_body<true>(nullptr, nullptr, (const float*)b.q0, b.mask, (const float*)b.D,
+                                           (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, cf, bx, by,
+                                           b.d.whi, b.d.wlo);
+                else
+                    flexure_f32_body<false>(b.y, nullptr, (const float*)b.q0, b.mask, (const float*)b.D,
+                                            (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, cf, bx, by);
+                __syncthreads();   // the next virtual block reuses the shared tiles
+                return;
+            }
+        }
+        flexure_body<T>(b.y, nullptr, (const T*)b.q0, b.mask, (const T*)b.D, (const T*)b.inv2eta, (T*)b.f, b.p.nx,
+                        b.p.ny, b.fc, bx, by);
+        __syncthreads();
+    });
+}
+
+template <typename T>
+__global__ void k_b_rows_fwd(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+{
+    typedef typename vec2<T>::type C2;
+    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+        const BMember& b = M[m];
+        rows_fwd_body<T>((const T*)b.f, b.p.nx, b.p.nx, b.p.ny, (C2*)b.S, b.p, b.RB, local, 0);
+        __syncthreads();
+    });
+}
+
+template <typename T>
+__global__ void k_b_cols_hartley(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+{
+    typedef typename vec2<T>::type C2;
+    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+        const BMember& b = M[m];
+        cols_hartley_body<T>((C2*)b.S, (const T*)b.mA, (const T*)b.mB, b.even, b.p, b.CB, local, 0);
+        __syncthreads();
+    });
+}
+
+template <typename T>
+__global__ void k_b_rows_inv(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+{
+    typedef typename vec2<T>::type C2;
+    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+        const BMember& b = M[m];
+        const double norm = (double)(float)((long long)b.p.nx * b.p.ny);   // nx*ny*1. (default real)
+        rows_inv_body<T>((const C2*)b.S, b.p.ny, (T*)b.raw, b.p.nx, b.p, b.RB, (T)(1.0 / norm), local, 0);
+        __syncthreads();
+    });
+}
+
+template <typename T> void batch_grids(size_t rows_smem, size_t cols_smem, int rows_threads, int cols_threads,
+                                       int* g_flex, int* g_rows, int* g_cols, int* g_red)
+{
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    auto resident = [&](auto kern, int threads, size_t smem) {
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, smem) != cudaSuccess || per < 1) per = 1;
+        return per * nsm;
+    };
+    *g_flex = resident(k_b_flexure<T>, TX * TY, 0);
+    *g_rows = resident(k_b_rows_fwd<T>, rows_threads, rows_smem);
+    const int gi = resident(k_b_rows_inv<T>, rows_threads, rows_smem);
+    if (gi < *g_rows) *g_rows = gi;
+    *g_cols = resident(k_b_cols_hartley<T>, cols_threads, cols_smem);
+    *g_red = batch_red_resident<T>() * nsm;
+}
+
+template <typename T> void batch_flexure(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s)
+{
+    k_b_flexure<T><<<nblk, dim3(TX, TY), 0, s>>>(M, off, nm);
+}
+template <typename T>
+void batch_rows_fwd(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s)
+{
+    set_smem(k_b_rows_fwd<T>, smem);
+    k_b_rows_fwd<T><<<nblk, threads, smem, s>>>(M, off, nm);
+}
+template <typename T>
+void batch_cols_hartley(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s)
+{
+    set_smem(k_b_cols_hartley<T>, smem);
+    k_b_cols_hartley<T><<<nblk, threads, smem, s>>>(M, off, nm);
+}
+template <typename T>
+void batch_rows_inv(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s)
+{
+    set_smem(k_b_rows_inv<T>, smem);
+    k_b_rows_inv<T><<<nblk, threads, smem, s>>>(M, off, nm);
+}
+
+template <typename T> void batch_prepare(size_t rows_smem, size_t cols_smem)
+{
+    set_smem(k_b_rows_fwd<T>, rows_smem);
+    set_smem(k_b_rows_inv<T>, rows_smem);
+    set_smem(k_b_cols_hartley<T>, cols_smem);
+}
+
+#define FI_BATCH_INST(T)                                                                                   \
+    template void batch_prepare<T>(size_t, size_t);                                                        \
+    template void batch_grids<T>(size_t, size_t, int, int, int*, int*, int*, int*);                        \
+    template void batch_flexure<T>(const BMember*, const int*, int, int, cudaStream_t);                    \
+    template void batch_rows_fwd<T>(const BMember*, const int*, int, int, int, size_t, cudaStream_t);      \
+    template void batch_cols_hartley<T>(const BMember*, const int*, int, int, int, size_t, cudaStream_t);  \
+    template void batch_rows_inv<T>(const BMember*, const int*, int, int, int, size_t, cudaStream_t);
+FI_BATCH_INST(double)
+FI_BATCH_INST(float)
+
 #define FI_INST(T)                                                                                            \
     template void launch_flexure<T>(const double*, const double*, const T*, const uint8_t*, const T*, const T*, \
-                                    T*, int, int, const FlexCoef&, cudaStream_t, const int*);                 \
+                                    T*, int, int, const FlexCoef&, cudaStream_t, const int*, const float*,    \
+                                    const float*);                                                            \
     template void launch_rows_fwd<T>(const T*, int, int, int, vec2<T>::type*, const Plan2D&, cudaStream_t,    \
                                      const int*);                                                             \
     template void launch_cols_hartley<T>(vec2<T>::type*, const T*, const T*, int, const Plan2D&, cudaStream_t, \

@@ -12,6 +12,7 @@
 // partials in block order.
 #include <cstdio>
 
+#include "fi_batch.h"
 #include "fi_state.h"
 
 namespace fi {
@@ -58,17 +59,17 @@ __device__ __forceinline__ void block_reduce(double (&v)[NV], const bool (&is_ma
 // with the totals in `tot`.
 template <int NV>
 __device__ bool grid_finish(double (&v)[NV], const bool (&is_max)[NV], double* partials, unsigned* counter,
-                            double (&tot)[NV])
+                            double (&tot)[NV], int bid, int nblk)
 {
     __shared__ double sh[32 * NV];
     __shared__ bool last;
     block_reduce<NV>(v, is_max, sh);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int q = 0; q < NV; ++q) partials[(size_t)blockIdx.x * NV + q] = v[q];
+        for (int q = 0; q < NV; ++q) partials[(size_t)bid * NV + q] = v[q];
         __threadfence();
         const unsigned prev = atomicAdd(counter, 1u);
-        last = (prev == gridDim.x - 1);
+        last = (prev == (unsigned)nblk - 1);
     }
     __syncthreads();
     if (!last) return false;
@@ -77,7 +78,7 @@ __device__ bool grid_finish(double (&v)[NV], const bool (&is_max)[NV], double* p
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
         a[q] = 0.0;
-        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+        for (unsigned b = threadIdx.x; b < (unsigned)nblk; b += blockDim.x) {
             const double pb = ((volatile double*)partials)[(size_t)b * NV + q];
             a[q] = is_max[q] ? fmax(a[q], pb) : a[q] + pb;
         }
@@ -91,6 +92,14 @@ __device__ bool grid_finish(double (&v)[NV], const bool (&is_max)[NV], double* p
         return true;
     }
     return false;
+}
+
+// The same over this launch's grid.
+template <int NV>
+__device__ __forceinline__ bool grid_finish(double (&v)[NV], const bool (&is_max)[NV], double* partials,
+                                            unsigned* counter, double (&tot)[NV])
+{
+    return grid_finish<NV>(v, is_max, partials, counter, tot, (int)blockIdx.x, (int)gridDim.x);
 }
 
 // Scalar work done once per block (FP64 throughput is low on this part):
@@ -247,13 +256,19 @@ k_upd_load(Dom d, const double* __restrict__ dz_raw, const double* __restrict__ 
 // Target time and barystatic scalars of one isos_update, written by a kernel
 // so that the host never waits and a captured update graph reads them from
 // the control block.
-__global__ void k_set_args(Ctl* c, double tf, double bsl, double A_ocean, int method, int write_bsl)
+__device__ __forceinline__ void set_args_one(Ctl* c, double tf, double bsl, double A_ocean, int method,
+                                             int write_bsl)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
     c->tf = tf;
     if (write_bsl) c->bsl = bsl;
     c->A_ocean = A_ocean;
     c->bsl_method = method;
+}
+
+__global__ void k_set_args(Ctl* c, double tf, double bsl, double A_ocean, int method, int write_bsl)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    set_args_one(c, tf, bsl, A_ocean, method, write_bsl);
 }
 
 // --- integrator control ------------------------------------------------------
@@ -372,19 +387,19 @@ __constant__ double c_ts_bh[6] = {0.0845, 0.0, 0.0, 0.5179, 0.1276, 0.2700 - 1 /
 
 __device__ __forceinline__ void ts_x12(double x, double k, double dt, double& x1, double& x2)
 {
-    double a1 = x, a2 = x;
-#pragma unroll
-    for (int s = 0; s < 6; ++s) {
-        a1 = a1 + (dt * c_ts_bh[s]) * k;
-        a2 = a2 + (dt * c_ts_b[s]) * k;
-    }
-    x1 = a1;
-    x2 = a2;
+    // x1 = x + sum_s (dt bh_s) k and x2 = x + sum_s (dt b_s) k in the
+    // reference's order.  b_1 = b_2 = 0 (those terms add an exact zero) and
+    // bh_s = b_s for s < 5, so both sums share their first three terms.
+    double a = x;
+    a = a + (dt * c_ts_b[0]) * k;
+    a = a + (dt * c_ts_b[3]) * k;
+    a = a + (dt * c_ts_b[4]) * k;
+    x1 = a + (dt * c_ts_bh[5]) * k;
+    x2 = a + (dt * c_ts_b[5]) * k;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NT)
-k_ts_max(Dom d, const T* __restrict__ raw, double atol, double rtol)
+__device__ __forceinline__ void ts_max_body(Dom d, const T* __restrict__ raw, double atol, double rtol, int bid, int nblk)
 {
     Ctl* c = d.ctl;
     if (c->done) return;
@@ -392,36 +407,71 @@ k_ts_max(Dom d, const T* __restrict__ raw, double atol, double rtol)
     const double cm = block_corner_mean(raw, d.nx, d.ny);
     double v[2] = {0.0, 0.0};
     const bool mx[2] = {true, true};
-    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
-        const double k = ((double)raw[e] - cm) * d.spy;
-        double x1, x2;
-        ts_x12(d.x[e], k, dt, x1, x2);
-        v[0] = fmax(v[0], fabs(x1));
-        v[1] = fmax(v[1], fabs(x2));
+    if constexpr (sizeof(T) == 4) {
+        // mixed form: k, the error term x2 - x1 = dt (b_5 - bh_5) k and the
+        // magnitudes for the tolerance in FP32; only the state update
+        // x2 = x + dt (sum_s b_s) k stays in FP64
+        const double cx = ((dt * c_ts_b[0] + dt * c_ts_b[3]) + dt * c_ts_b[4]) + dt * c_ts_b[5];
+        const float ce = (float)(dt * c_ts_b[5] - dt * c_ts_bh[5]);
+        const float cmf = (float)cm, spyf = (float)d.spy;
+        float m1 = 0.f, m2 = 0.f;
+        for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
+            const float k = ((float)raw[e] - cmf) * spyf;
+            const double x2 = d.x[e] + cx * (double)k;
+            const float dx = ce * k;
+            d.ts_x2[e] = x2;
+            ((float*)d.ts_dx)[e] = dx;
+            const float x2f = (float)x2;
+            m1 = fmaxf(m1, fabsf(x2f - dx));
+            m2 = fmaxf(m2, fabsf(x2f));
+        }
+        v[0] = (double)m1;
+        v[1] = (double)m2;
+    } else {
+        for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
+            const double k = ((double)raw[e] - cm) * d.spy;
+            double x1, x2;
+            ts_x12(d.x[e], k, dt, x1, x2);
+            d.ts_x2[e] = x2;         // kept for the error norm and the commit
+            d.ts_dx[e] = x2 - x1;
+            v[0] = fmax(v[0], fabs(x1));
+            v[1] = fmax(v[1], fabs(x2));
+        }
     }
     double tot[2];
-    if (grid_finish<2>(v, mx, d.partials, &c->counter[1], tot)) c->tol = atol + rtol * fmax(tot[0], tot[1]);
+    if (grid_finish<2>(v, mx, d.partials, &c->counter[1], tot, bid, nblk)) c->tol = atol + rtol * fmax(tot[0], tot[1]);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NT)
-k_ts_err(Dom d, const T* __restrict__ raw, double q, double dt_max, int max_reject)
+__global__ void __launch_bounds__(NT) k_ts_max(Dom d, const T* __restrict__ raw, double atol, double rtol)
+{
+    ts_max_body<T>(d, raw, atol, rtol, (int)blockIdx.x, (int)gridDim.x);
+}
+
+template <typename T>
+__device__ __forceinline__ void ts_err_body(Dom d, const T* __restrict__ raw, double q, double dt_max, int max_reject, int bid, int nblk)
 {
     Ctl* c = d.ctl;
     if (c->done) return;
-    const double dt = c->h, tol = c->tol;
-    const double cm = block_corner_mean(raw, d.nx, d.ny);
+    const double dt = c->h, inv_tol = 1.0 / c->tol;
     double v[1] = {0.0};
     const bool mx[1] = {false};
-    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
-        const double k = ((double)raw[e] - cm) * d.spy;
-        double x1, x2;
-        ts_x12(d.x[e], k, dt, x1, x2);
-        const double r = (x2 - x1) / tol;
-        v[0] += r * r;
+    if constexpr (sizeof(T) == 4) {
+        const float it = (float)inv_tol;
+        float acc = 0.f;
+        for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
+            const float r = ((const float*)d.ts_dx)[e] * it;   // (x2 - x1) / tol
+            acc += r * r;
+        }
+        v[0] = (double)acc;
+    } else {
+        for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
+            const double r = d.ts_dx[e] * inv_tol;   // (x2 - x1) / tol
+            v[0] += r * r;
+        }
     }
     double tot[1];
-    if (grid_finish<1>(v, mx, d.partials, &c->counter[2], tot)) {
+    if (grid_finish<1>(v, mx, d.partials, &c->counter[2], tot, bid, nblk)) {
         const double err = sqrt(tot[0] / (double)d.n);
         c->err = err;
         c->n_attempt++;
@@ -439,6 +489,12 @@ k_ts_err(Dom d, const T* __restrict__ raw, double q, double dt_max, int max_reje
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(NT) k_ts_err(Dom d, const T* __restrict__ raw, double q, double dt_max, int max_reject)
+{
+    ts_err_body<T>(d, raw, q, dt_max, max_reject, (int)blockIdx.x, (int)gridDim.x);
+}
+
 // Device-side attempt loop of the reference-compatible Tsit5: the attempts
 // of one update run as the body of a CUDA graph WHILE node, so the host never
 // waits on an accept/reject decision.  The body is
@@ -454,9 +510,8 @@ __global__ void k_ts_loop_begin(Ctl* c)
     c->need_rhs = 0;
 }
 
-__global__ void k_ts_attempt_begin(Ctl* c, int max_iter)
+__device__ __forceinline__ void attempt_begin_one(Ctl* c, int max_iter)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double tf = c->tf;
     if (c->status != ST_OK || !(c->t < tf)) { c->done = 1; c->need_rhs = 0; return; }
     if (++c->loop_iter > max_iter) { c->status = ST_STEP; c->done = 1; c->need_rhs = 0; return; }
@@ -467,28 +522,62 @@ __global__ void k_ts_attempt_begin(Ctl* c, int max_iter)
     if (c->need_rhs) { c->have_rhs = 1; c->rhs_valid = 1; }
 }
 
+__global__ void k_ts_attempt_begin(Ctl* c, int max_iter)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    attempt_begin_one(c, max_iter);
+}
+
+// 1 while the member has attempts left
+__device__ __forceinline__ int attempt_end_one(Ctl* c)
+{
+    if (!c->done && c->accepted) c->rhs_valid = 0;   // the state moved: the next attempt needs a new RHS
+    return (!c->done && c->status == ST_OK && c->t < c->tf) ? 1 : 0;
+}
+
 __global__ void k_ts_attempt_end(Ctl* c, cudaGraphConditionalHandle loop)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    if (!c->done && c->accepted) c->rhs_valid = 0;   // the state moved: the next attempt needs a new RHS
-    const unsigned more = (!c->done && c->status == ST_OK && c->t < c->tf) ? 1u : 0u;
-    cudaGraphSetConditional(loop, more);
+    cudaGraphSetConditional(loop, attempt_end_one(c) ? 1u : 0u);
+}
+
+template <typename T>
+__device__ __forceinline__ void ts_commit_body(Dom d, const T* __restrict__ raw, int bid, int nblk)
+{
+    const Ctl* c = d.ctl;
+    if (c->done || !c->accepted) return;
+    if (sizeof(T) == 4 && d.whi) {
+        // mixed form: now%w's float pair takes the same increment
+        // dt (sum_s b_s) k by an FP32 two-sum (no FP64 work per cell)
+        const double dt = c->h;
+        const float cx = (float)(((dt * c_ts_b[0] + dt * c_ts_b[3]) + dt * c_ts_b[4]) + dt * c_ts_b[5]);
+        const float cmf = (float)block_corner_mean(raw, d.nx, d.ny), spyf = (float)d.spy;
+        for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
+            const double x2 = d.ts_x2[e];
+            d.x[e] = x2;
+            d.w[e] = x2;
+            const float inc = cx * (((float)raw[e] - cmf) * spyf);
+            const float hi = d.whi[e], lo = d.wlo[e];
+            const float sm = hi + inc, bb = sm - hi;
+            const float er = (hi - (sm - bb)) + (inc - bb);
+            const float l2 = lo + er;
+            const float h2 = sm + l2;
+            d.whi[e] = h2;
+            d.wlo[e] = l2 - (h2 - sm);
+        }
+        return;
+    }
+    for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
+        const double x2 = d.ts_x2[e];
+        d.x[e] = x2;
+        d.w[e] = x2;
+    }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(NT) k_ts_commit(Dom d, const T* __restrict__ raw)
 {
-    const Ctl* c = d.ctl;
-    if (c->done || !c->accepted) return;
-    const double dt = c->h;
-    const double cm = block_corner_mean(raw, d.nx, d.ny);
-    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
-        const double k = ((double)raw[e] - cm) * d.spy;
-        double x1, x2;
-        ts_x12(d.x[e], k, dt, x1, x2);
-        d.x[e] = x2;
-        d.w[e] = x2;
-    }
+    ts_commit_body<T>(d, raw, (int)blockIdx.x, (int)gridDim.x);
 }
 
 // --- update tail -----------------------------------------------------------
@@ -596,6 +685,132 @@ static int grid_for(size_t n)
     return (int)b;
 }
 
+int reduce_grid(size_t n) { return grid_for(n); }
+
+// Tsit5 attempt kernels: about 8 cells per thread, so that the per-thread
+// partial sums and maxima of the mixed form stay in FP32 and only block
+// totals pass through FP64.
+int ts_grid(size_t n)
+{
+    size_t b = (n + (size_t)NT * 8 - 1) / ((size_t)NT * 8);
+    if (b > 152 * 8) b = 152 * 8;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// ---- batched Tsit5 attempt over the members of an ensemble -----------------
+template <typename T>
+__global__ void __launch_bounds__(NT) k_b_ts_max(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+{
+    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
+        const BMember& b = M[m];
+        ts_max_body<T>(b.d, (const T*)b.raw, b.atol, b.rtol, local, b.red_nblk);
+        __syncthreads();
+    });
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT)
+k_b_ts_err(const BMember* __restrict__ M, const int* __restrict__ off, int nm, int max_reject)
+{
+    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
+        const BMember& b = M[m];
+        ts_err_body<T>(b.d, (const T*)b.raw, b.q, b.dt_max, max_reject, local, b.red_nblk);
+        __syncthreads();
+    });
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_b_ts_commit(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+{
+    batch_walk(off, nm, [&](int m) { const Ctl* c = M[m].d.ctl; return c->done == 0 && c->accepted != 0; },
+               [&](int m, int local) {
+                   const BMember& b = M[m];
+                   ts_commit_body<T>(b.d, (const T*)b.raw, local, b.red_nblk);
+               });
+}
+
+template <typename T> int batch_red_resident()
+{
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_ts_max<T>, NT, 0) != cudaSuccess || per < 1) per = 1;
+    int p2 = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p2, k_b_ts_err<T>, NT, 0) == cudaSuccess && p2 >= 1 && p2 < per)
+        per = p2;
+    return per;
+}
+template int batch_red_resident<float>();
+template int batch_red_resident<double>();
+
+__global__ void k_b_loop_begin(const BMember* __restrict__ M, int nm)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nm) return;
+    Ctl* c = M[m].d.ctl;
+    c->rhs_valid = 0;
+    c->have_rhs = 0;
+    c->loop_iter = 0;
+    c->need_rhs = 0;
+}
+
+__global__ void k_b_attempt_begin(const BMember* __restrict__ M, int nm, int max_iter)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < nm) attempt_begin_one(M[m].d.ctl, max_iter);
+}
+
+// continue while any member has an attempt left
+__global__ void k_b_attempt_end(const BMember* __restrict__ M, int nm, cudaGraphConditionalHandle loop, int* more_out)
+{
+    __shared__ int any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    int more = 0;
+    for (int m = threadIdx.x; m < nm; m += blockDim.x) more |= attempt_end_one(M[m].d.ctl);
+    if (more) any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (more_out) *more_out = any;
+        else cudaGraphSetConditional(loop, any ? 1u : 0u);
+    }
+}
+
+__global__ void k_b_set_args(const BArgs* __restrict__ a, int nm)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < nm) set_args_one(a[m].ctl, a[m].tf, a[m].bsl, a[m].A_ocean, a[m].method, a[m].write_bsl);
+}
+
+template <typename T> void batch_ts_max(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s)
+{
+    k_b_ts_max<T><<<nblk, NT, 0, s>>>(M, off, nm);
+}
+template <typename T>
+void batch_ts_err(const BMember* M, const int* off, int nm, int nblk, int max_reject, cudaStream_t s)
+{
+    k_b_ts_err<T><<<nblk, NT, 0, s>>>(M, off, nm, max_reject);
+}
+template <typename T> void batch_ts_commit(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s)
+{
+    k_b_ts_commit<T><<<nblk, NT, 0, s>>>(M, off, nm);
+}
+void batch_loop_begin(const BMember* M, int nm, cudaStream_t s) { k_b_loop_begin<<<(nm + 127) / 128, 128, 0, s>>>(M, nm); }
+void batch_attempt_begin(const BMember* M, int nm, int max_iter, cudaStream_t s)
+{
+    k_b_attempt_begin<<<(nm + 127) / 128, 128, 0, s>>>(M, nm, max_iter);
+}
+void batch_attempt_end(const BMember* M, int nm, cudaGraphConditionalHandle loop, cudaStream_t s, int* more_out)
+{
+    k_b_attempt_end<<<1, 256, 0, s>>>(M, nm, loop, more_out);
+}
+void batch_set_args(const BArgs* a, int nm, cudaStream_t s) { k_b_set_args<<<(nm + 127) / 128, 128, 0, s>>>(a, nm); }
+template void batch_ts_max<float>(const BMember*, const int*, int, int, cudaStream_t);
+template void batch_ts_max<double>(const BMember*, const int*, int, int, cudaStream_t);
+template void batch_ts_err<float>(const BMember*, const int*, int, int, int, cudaStream_t);
+template void batch_ts_err<double>(const BMember*, const int*, int, int, int, cudaStream_t);
+template void batch_ts_commit<float>(const BMember*, const int*, int, int, cudaStream_t);
+template void batch_ts_commit<double>(const BMember*, const int*, int, int, cudaStream_t);
+
 int reduce_blocks(size_t n) { return grid_for(n); }
 
 void upd_begin(const Dom& d, const double* H_ice, cudaStream_t s)
@@ -648,15 +863,15 @@ void euler_final(const Ctl* c, double* x, double* w, const T* r1, int nx, int ny
 }
 template <typename T> void ts_max(const Dom& d, const T* raw, double atol, double rtol, cudaStream_t s)
 {
-    k_ts_max<T><<<grid_for(d.n), NT, 0, s>>>(d, raw, atol, rtol);
+    k_ts_max<T><<<ts_grid(d.n), NT, 0, s>>>(d, raw, atol, rtol);
 }
 template <typename T> void ts_err(const Dom& d, const T* raw, double q, double dt_max, int max_reject, cudaStream_t s)
 {
-    k_ts_err<T><<<grid_for(d.n), NT, 0, s>>>(d, raw, q, dt_max, max_reject);
+    k_ts_err<T><<<ts_grid(d.n), NT, 0, s>>>(d, raw, q, dt_max, max_reject);
 }
 template <typename T> void ts_commit(const Dom& d, const T* raw, cudaStream_t s)
 {
-    k_ts_commit<T><<<grid_for(d.n), NT, 0, s>>>(d, raw);
+    k_ts_commit<T><<<ts_grid(d.n), NT, 0, s>>>(d, raw);
 }
 template <typename T> void upd_end(const Dom& d, const T* raw_last, int have_rhs, cudaStream_t s)
 {

@@ -28,6 +28,8 @@ struct Dom {
     uint8_t *m_ocean, *m_grounded, *m_cont;
     Ctl* ctl;
     double* partials;                  // >= reduce_blocks(n) * 4 doubles
+    double *ts_x2, *ts_dx;             // Tsit5 attempt: x2 and x2 - x1 (dt_method 2 only)
+    float *whi, *wlo;                  // mixed Tsit5: now%w as a float pair (w = whi + wlo), else null
 };
 
 int reduce_blocks(size_t n);

@@ -132,13 +132,18 @@ class Server:
 
 
 class Ensemble:
-    """Members (independent domains, any sizes) advanced in lockstep with
-    fi_batch_update: each coupling step enqueues one isos_update per member
-    on the member's own stream, so members overlap on the device."""
+    """Members (independent domains, any sizes) advanced in lockstep.
 
-    def __init__(self, workloads, precision: int = 1):
+    mode "graph": one fi_batch_step per coupling step runs the whole
+    ensemble as one CUDA graph whose Tsit5 attempts are batched launches over
+    all members (members must run reference-compatible Tsit5).
+    mode "streams": fi_batch_update enqueues one isos_update per member on
+    the member's own stream (any integrator)."""
+
+    def __init__(self, workloads, precision: int = 1, mode: str = "graph"):
         from .isostasy import Domain
         self.L = _lib.load()
+        self.mode = mode
         self.doms = []
         self.bsl = (_lib.FiBsl * len(workloads))()
         for i, wl in enumerate(workloads):
@@ -154,27 +159,43 @@ class Ensemble:
             self.doms.append(d)
         self.wls = list(workloads)
         self.hs = (C.c_void_p * len(self.doms))(*[d.h.value for d in self.doms])
+        self.batch = None
+        if mode == "graph":
+            bh = C.c_void_p()
+            rc = self.L.fi_batch_create(self.hs, len(self.doms), C.byref(bh))
+            if rc:
+                raise FiError(rc, "fi_batch_create")
+            self.batch = bh
         self.t = 0.0
 
     def first_update(self, t: float):
         """Apply each member's ice load with a synchronous isos_update."""
-        for d, wl, i in zip(self.doms, self.wls, range(len(self.doms))):
+        for i, (d, wl) in enumerate(zip(self.doms, self.wls)):
             d.update(wl.H_final, t, self.bsl[i])
         self.t = t
 
     def update(self, t: float):
-        rc = self.L.fi_batch_update(self.hs, len(self.doms), float(t), self.bsl)
+        if self.batch is not None:
+            rc = self.L.fi_batch_step(self.batch, float(t), self.bsl)
+        else:
+            rc = self.L.fi_batch_update(self.hs, len(self.doms), float(t), self.bsl)
         if rc:
-            raise FiError(rc, "fi_batch_update")
+            raise FiError(rc, "batched update")
         self.t = t
 
     def synchronize(self):
         st = (C.c_int32 * len(self.doms))()
-        rc = self.L.fi_batch_synchronize(self.hs, len(self.doms), st)
+        if self.batch is not None:
+            rc = self.L.fi_batch_wait(self.batch, st)
+        else:
+            rc = self.L.fi_batch_synchronize(self.hs, len(self.doms), st)
         if rc:
-            raise FiError(rc, "fi_batch_synchronize: member %d" % next(i for i, v in enumerate(st) if v))
+            raise FiError(rc, "ensemble member %d" % next(i for i, v in enumerate(st) if v))
 
     def close(self):
+        if self.batch is not None:
+            self.L.fi_batch_destroy(self.batch)
+            self.batch = None
         for d in self.doms:
             d.close()
         self.doms = []

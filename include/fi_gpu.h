@@ -228,6 +228,22 @@ int fi_serve_destroy(fi_server* s);
 int fi_batch_update(fi_handle* const* hs, int n, double time, fi_bsl* bsl);
 int fi_batch_synchronize(fi_handle* const* hs, int n, int32_t* status);
 
+/* Batched ensembles in shared launches: every member runs reference-
+ * compatible tsit54 (stage_mode 0) in the same precision, initialised to the
+ * same time.  fi_batch_step enqueues one isos_update to `time` for all
+ * members as a single CUDA graph: the members' update heads as parallel
+ * branches, then the adaptive Tsit5 attempts of all members in one loop of
+ * batched launches (each launch covers every member that still has an
+ * attempt left; accept/reject and step sizes stay per member), then the
+ * update tails.  Each member's result is bit-identical to driving it alone.
+ * The members' load is the one they hold.  Do not drive members on their own
+ * while a batch step is in flight (fi_batch_wait first). */
+typedef struct fi_batch fi_batch;
+int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out);
+int fi_batch_step(fi_batch* b, double time, fi_bsl* bsl);
+int fi_batch_wait(fi_batch* b, int32_t* status);
+int fi_batch_destroy(fi_batch* b);
+
 /* Restart support: the complete device state (fields + integrator clock) as
  * doubles; bit-identical round trip. */
 size_t fi_state_size(const fi_handle* h);

@@ -120,14 +120,26 @@ def test_unstable_request_fails_alone():
     assert ig["state"] == "done"
 
 
+def ens_members(mode):
+    if mode == "streams":
+        return [small_rk4(48), small_tsit(40), small_rk4(64), small_tsit(56)]
+    # batched launches: reference-compatible Tsit5 members of different sizes
+    # and rheologies
+    out = [small_tsit(40), small_tsit(56)]
+    for i in (3, 7):
+        wl = W.ensemble_member(i, stage_mode=0)
+        out.append(wl)
+    return out
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", [0, 1])
-def test_ensemble_lockstep_matches_members_alone(precision):
-    """fi_batch_update over members of different sizes and integrators gives
-    each member the bits it gets when driven alone."""
+@pytest.mark.parametrize("precision,mode", [(0, "streams"), (1, "streams"), (0, "graph"), (1, "graph")])
+def test_ensemble_lockstep_matches_members_alone(precision, mode):
+    """Lockstep ensembles (per-member streams, or one graph of batched
+    launches) give each member the bits it gets when driven alone."""
     from fastisostasy_gb300.serve import Ensemble
-    wls = [small_rk4(48), small_tsit(40), small_rk4(64), small_tsit(56)]
-    ens = Ensemble(wls, precision=precision)
+    wls = ens_members(mode)
+    ens = Ensemble(wls, precision=precision, mode=mode)
     ens.first_update(10.0)
     for t in (20.0, 30.0, 40.0, 50.0, 60.0):
         ens.update(t)
@@ -144,5 +156,13 @@ def test_ensemble_lockstep_matches_members_alone(precision):
         dom.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
         for t in (10.0, 20.0, 30.0, 40.0, 50.0, 60.0):
             dom.update(wl.H_final, t, b)
-        assert np.array_equal(dom.field("w"), g)
+        w = dom.field("w")
         dom.close()
+        if mode == "graph" and precision == 1:
+            # the batched launches are other kernels built from the same
+            # code; the compiler may fuse FP32 multiply-adds differently in
+            # them (with contraction off the two agree bit for bit), so the
+            # mixed form agrees to FP32 rounding
+            assert np.abs(w - g).max() <= 1e-6 * np.abs(w).max()
+        else:
+            assert np.array_equal(w, g)
