@@ -1714,10 +1714,11 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         if (!h) return FI_E_ARG;
         if (!h->state_ready) return fail(h, FI_E_STATE, "fi_batch_create before fi_init_state");
         const fi_handle* h0 = hs[0];
-        if (h->p.dt_method != 2 || h->p.stage_mode != 0 || mixed(h) != mixed(h0) ||
+        if (h->p.dt_method != 2 || h->p.stage_mode != 0 || mixed(h) != mixed(h0) || (mixed(h) && !h->d.whi) ||
             h->p.dt_diagnostics != h0->p.dt_diagnostics || h->time_diag != h0->time_diag || !h->tsit_graph_ok)
             return fail(h, FI_E_CONFIG,
-                        "batched members must run reference-compatible tsit54 in the same precision, in lockstep");
+                        "batched members must run reference-compatible tsit54 in the same precision, in lockstep "
+                        "(mixed members with uniform spacing)");
     }
     fi_batch* b = new fi_batch();
     b->hs.assign(hs, hs + n);

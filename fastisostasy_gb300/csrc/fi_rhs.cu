@@ -223,12 +223,22 @@ __device__ __forceinline__ void flexure_f32_body(const double* __restrict__ y, c
     __shared__ float Myy[RY][RX];
     __shared__ float Mxy[RY][RX];
     __shared__ float Mxyx[RY][RX];
+    __shared__ float Ds[RY][RX];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i0 = bx * TX - 2, j0 = by * TY - 2;   // global index of lx = ly = 0
+    // every global input is requested up front, so their latencies overlap:
+    // this thread's output cell ...
+    const int go_i = i0 + tx + 2, go_j = j0 + ty + 2;
+    const bool own = go_i < nx && go_j < ny;
+    const size_t eo = own ? (size_t)go_j * nx + go_i : 0;
+    const uint8_t own_m = own ? mask[eo] : (uint8_t)0;
+    const float own_q = own ? q0[eo] : 0.f, own_ie = own ? inv2eta[eo] : 0.f;
+    // ... and the state and rigidity tiles with their halo
     for (int ly = ty; ly < RY; ly += TY)
         for (int lx = tx; lx < RX; lx += TX) {
             const int gi = i0 + lx, gj = j0 + ly;
             const bool in = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+            Ds[ly][lx] = in ? D[(size_t)gj * nx + gi] : 0.f;
             if constexpr (HILO) {
                 yh[ly][lx] = in ? whi[(size_t)gj * nx + gi] : 0.f;
                 yl[ly][lx] = in ? wlo[(size_t)gj * nx + gi] : 0.f;
@@ -273,7 +283,7 @@ __device__ __forceinline__ void flexure_f32_body(const double* __restrict__ y, c
             if (gj == 0) wyy = (dY[ly + 1][lx] - dY[ly][lx]) * c.inv_dy2;
             else if (gj == ny - 1) wyy = (dY[ly - 1][lx] - dY[ly - 2][lx]) * c.inv_dy2;
             else wyy = (dY[ly][lx] - dY[ly - 1][lx]) * c.inv_dy2;
-            const float Dl = D[(size_t)gj * nx + gi];
+            const float Dl = Ds[ly][lx];
             Mxx[ly][lx] = -Dl * (wxx + c.nu * wyy);
             Myy[ly][lx] = -Dl * (wyy + c.nu * wxx);
             Mxy[ly][lx] = (-Dl * c.one_minus_nu) * wxy;
@@ -303,15 +313,15 @@ __device__ __forceinline__ void flexure_f32_body(const double* __restrict__ y, c
     if (gj == 0) my_yy = ((Myy[ly + 2][lx] - 2.f * Myy[ly + 1][lx]) + Myy[ly][lx]) * c.inv_dy2;
     else if (gj == ny - 1) my_yy = ((Myy[ly][lx] - 2.f * Myy[ly - 1][lx]) + Myy[ly - 2][lx]) * c.inv_dy2;
     else my_yy = ((Myy[ly + 1][lx] - 2.f * Myy[ly][lx]) + Myy[ly - 1][lx]) * c.inv_dy2;
-    const size_t e = (size_t)gj * nx + gi;
+    const size_t e = eo;
     float p = 0.f;
-    if (mask[e]) {
-        p = q0[e];
+    if (own_m) {
+        p = own_q;
         if constexpr (!HILO) {
             if (wref) p += c.coef_mantle * (float)(ys[ly][lx] - wref[e]);
         }
     }
-    f[e] = (((p + mx_xx) + 2.f * mxy_xy) + my_yy) * inv2eta[e];
+    f[e] = (((p + mx_xx) + 2.f * mxy_xy) + my_yy) * own_ie;
 }
 
 __global__ void __launch_bounds__(TX* TY)
@@ -745,22 +755,15 @@ __global__ void __launch_bounds__(TX* TY) k_b_flexure(const BMember* __restrict_
         const BMember& b = M[m];
         const int bx = local % b.fgx, by = local / b.fgx;
         if constexpr (sizeof(T) == 4) {
-            if (b.fc.dxm == nullptr) {
-                const FlexCoefF cf = b.fcf;
-                if (b.d.whi)
-                    flexure_f32_body<true>(nullptr, nullptr, (const float*)b.q0, b.mask, (const float*)b.D,
-                                           (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, cf, bx, by,
-                                           b.d.whi, b.d.wlo);
-                else
-                    flexure_f32_body<false>(b.y, nullptr, (const float*)b.q0, b.mask, (const float*)b.D,
-                                            (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, cf, bx, by);
-                __syncthreads();   // the next virtual block reuses the shared tiles
-                return;
-            }
+            // mixed members have uniform spacing and carry now%w as a float pair
+            flexure_f32_body<true>(nullptr, nullptr, (const float*)b.q0, b.mask, (const float*)b.D,
+                                   (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, b.fcf, bx, by, b.d.whi,
+                                   b.d.wlo);
+        } else {
+            flexure_body<T>(b.y, nullptr, (const T*)b.q0, b.mask, (const T*)b.D, (const T*)b.inv2eta, (T*)b.f,
+                            b.p.nx, b.p.ny, b.fc, bx, by);
         }
-        flexure_body<T>(b.y, nullptr, (const T*)b.q0, b.mask, (const T*)b.D, (const T*)b.inv2eta, (T*)b.f, b.p.nx,
-                        b.p.ny, b.fc, bx, by);
-        __syncthreads();
+        __syncthreads();   // the next virtual block reuses the shared tiles
     });
 }
 

@@ -161,8 +161,8 @@ def test_ensemble_lockstep_matches_members_alone(precision, mode):
         if mode == "graph" and precision == 1:
             # the batched launches are other kernels built from the same
             # code; the compiler may fuse FP32 multiply-adds differently in
-            # them (with contraction off the two agree bit for bit), so the
-            # mixed form agrees to FP32 rounding
-            assert np.abs(w - g).max() <= 1e-6 * np.abs(w).max()
+            # them (with contraction off the two agree bit for bit), and the
+            # adaptive steps carry those roundings on: the mixed form's bound
+            assert np.abs(w - g).max() <= 1e-5 * np.abs(w).max()
         else:
             assert np.array_equal(w, g)
