@@ -467,6 +467,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--ensemble-members", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--only", choices=["ensemble", "serve"],
+                    help="run one secondary leg alone and print its JSON (for profiling), not a bench line")
     ap.add_argument("--lean", action="store_true",
                     help="mixed form only, no profile / e2e / CPU legs (for ncu captures); prints the timing only")
     args = ap.parse_args()
@@ -494,6 +496,12 @@ def main():
         torch.cuda.synchronize()
 
     results = {}
+    if args.only == "ensemble":
+        print(json.dumps({"ensemble": ensemble_leg(args.ensemble_members)}))
+        return 0
+    if args.only == "serve":
+        print(json.dumps({"serve": serve_leg(n_req=args.serve_requests)}))
+        return 0
     if args.lean:
         dom, wl, b = make_domain(1)
         ms, _, _, _, _ = run_resident(dom, wl, b, args.steps, args.warmup, flush)
