@@ -515,11 +515,8 @@ def main():
                                                       sampler_index=local if prec == 1 else None)
         barrier()
         tot = sum(ms)
-        if ws > 1:
-            import torch.distributed as dist
-            tt = torch.tensor([tot], device="cuda", dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            tot = float(tt.item())
+        from fastisostasy_gb300 import replicas
+        tot = replicas.max_over_ranks(tot, device="cuda")   # slowest replica
         results[prec] = {"dom": dom, "wl": wl, "b": b, "ms": tot / args.steps, "launches": launches,
                          "clocks": clocks, "w": dom.field("w"), "t": t_end}
     kyr = lambda ms_step: ws * (DTT / 1000.0) / (ms_step / 1000.0)
