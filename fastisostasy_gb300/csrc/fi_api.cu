@@ -146,7 +146,8 @@ struct fi_handle {
     void* Dt = nullptr;                  // rigidity (T)
     void* inv2eta = nullptr;             // 1/(2 eta_eff) (T)
     void* f = nullptr;                   // flexure output (T)
-    void* raw[4] = {nullptr, nullptr, nullptr, nullptr};   // RHS stage outputs (T)
+    void* raw[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // RHS stage outputs (T)
+    int* dmore = nullptr;                // loop condition of the eager true-stage Tsit5 path
     void* S = nullptr;                   // RHS half spectrum (T complex)
     void* mA = nullptr;                  // 1/(kappa R) at (k, l) (T)
     void* mB = nullptr;                  // 1/(kappa R) at (-k, l) (T)
@@ -641,15 +642,55 @@ template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
     return (T*)h->raw[3];
 }
 
+const int kMaxAttempts = 10000000;
+
+// One attempt of Tsitouras 5(4) with true stages (the Dormand-Prince 5(4)
+// pair, FSAL), decided on the device: k_0 = f(x) unless an accepted attempt
+// left it cached, stage states y_i = x + h sum a_ij k_j with the RHS (mantle
+// term at the stage state) evaluated at each, stage 6 = x2, the embedded x1,
+// the error norm, the commit and the FSAL copy.
+template <typename T> void tsit_true_attempt(fi_handle* h, cudaGraphConditionalHandle loop, int* more_out)
+{
+    const fi_params& p = h->p;
+    DPRaw<T> R;
+    for (int i = 0; i < 7; ++i) R.p[i] = (const T*)h->raw[i];
+    ts_attempt_begin(h->ctl, kMaxAttempts, h->s);
+    rhs<T>(h, h->d.x, h->w_ref, (T*)h->raw[0], &h->ctl->need_rhs);
+    for (int i = 1; i <= 6; ++i) {
+        double* y = i == 6 ? h->d.ts_x2 : h->y;
+        PROF(h, K_STAGE, dp_stage<T>(h->ctl, y, h->d.x, R, i, h->nx, h->ny, h->spy, h->s));
+        rhs<T>(h, y, h->w_ref, (T*)h->raw[i], &h->ctl->active);
+    }
+    PROF(h, K_TS, dp_err<T>(h->d, R, p.atol, p.rtol, h->s));
+    PROF(h, K_TS, ts_err<T>(h->d, (const T*)h->raw[0], p.q, p.dt_max, 100000, h->s));
+    PROF(h, K_TS, ts_commit<T>(h->d, (const T*)h->raw[0], h->s));
+    PROF(h, K_TS, fsal_copy<T>(h->ctl, (T*)h->raw[0], (const T*)h->raw[6], h->n, h->s));
+    ts_attempt_end(h->ctl, loop, h->s, 1, more_out);
+    h->launches += 12;
+}
+
 // Reference-compatible Tsit5: one distinct RHS per state; the host waits
-// for each attempt's accept/reject decision.
+// for each attempt's accept/reject decision.  True stages: the same device
+// attempt as in captured graphs, the host only reads the loop condition.
 template <typename T> int integrate_tsit(fi_handle* h, double tf, int* have_rhs, T** raw_last)
 {
     const fi_params& p = h->p;
     T* r0 = (T*)h->raw[0];
     *have_rhs = 0;
     *raw_last = r0;
-    if (p.stage_mode == 1) return fail(h, FI_E_CONFIG, "tsit54 with true stages is not available on the device yet");
+    if (p.stage_mode == 1) {
+        ts_loop_begin(h->ctl, h->s);
+        for (long long it = 0;; ++it) {
+            tsit_true_attempt<T>(h, 0, h->dmore);
+            int more = 0;
+            CK(cudaMemcpyAsync(&more, h->dmore, sizeof(int), cudaMemcpyDeviceToHost, h->s));
+            CK(cudaStreamSynchronize(h->s));
+            if (!more) break;
+            if (it > kMaxAttempts) return fail(h, FI_E_STEP, "tsit54: too many attempts");
+        }
+        *have_rhs = -1;   // recorded on the device
+        return FI_OK;
+    }
     if (h->d.whi) split_hilo(h->d.w, h->d.whi, h->d.wlo, h->n, h->s);
     Ctl hc;
     CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
@@ -674,11 +715,9 @@ template <typename T> int integrate_tsit(fi_handle* h, double tf, int* have_rhs,
 // The same attempts as integrate_tsit, enqueued during stream capture as the
 // body of a CUDA graph WHILE node: the accept/reject decisions stay on the
 // device.  Only valid while h->s is capturing.
-const int kMaxAttempts = 10000000;
 template <typename T> int enqueue_tsit_loop(fi_handle* h)
 {
     const fi_params& p = h->p;
-    if (p.stage_mode == 1) return fail(h, FI_E_CONFIG, "tsit54 with true stages is not available on the device yet");
     T* r0 = (T*)h->raw[0];
     ts_loop_begin(h->ctl, h->s);
     h->launches += 1;
@@ -705,13 +744,17 @@ template <typename T> int enqueue_tsit_loop(fi_handle* h)
     CK(cudaStreamBeginCaptureToGraph(h->s_body, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     cudaStream_t s0 = h->s;
     h->s = h->s_body;
-    ts_attempt_begin(h->ctl, kMaxAttempts, h->s);
-    rhs<T>(h, h->d.w, nullptr, r0, &h->ctl->need_rhs, h->d.whi, h->d.wlo);
-    ts_max<T>(h->d, r0, p.atol, p.rtol, h->s);
-    ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s);
-    ts_commit<T>(h->d, r0, h->s);
-    ts_attempt_end(h->ctl, loop, h->s);
-    h->launches += 5;
+    if (p.stage_mode == 1) {
+        tsit_true_attempt<T>(h, loop, nullptr);
+    } else {
+        ts_attempt_begin(h->ctl, kMaxAttempts, h->s);
+        rhs<T>(h, h->d.w, nullptr, r0, &h->ctl->need_rhs, h->d.whi, h->d.wlo);
+        ts_max<T>(h->d, r0, p.atol, p.rtol, h->s);
+        ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s);
+        ts_commit<T>(h->d, r0, h->s);
+        ts_attempt_end(h->ctl, loop, h->s);
+        h->launches += 5;
+    }
     h->s = s0;
     cudaGraph_t body_out = nullptr;
     CK(cudaStreamEndCapture(h->s_body, &body_out));
@@ -1056,7 +1099,7 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     if (p.dt_method == 2) {
         AL(d.ts_x2, n * sizeof(double));
         AL(d.ts_dx, n * sizeof(double));
-        if (mixed(h) && h->uniform) {
+        if (mixed(h) && h->uniform && p.stage_mode == 0) {
             AL(d.whi, n * sizeof(float));
             AL(d.wlo, n * sizeof(float));
         }
@@ -1064,6 +1107,10 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     AL(h->y, n * 8);
     AL(h->q0, nT); AL(h->Dt, nT); AL(h->inv2eta, nT); AL(h->f, nT);
     for (int i = 0; i < 4; ++i) AL(h->raw[i], nT);
+    if (p.dt_method == 2 && p.stage_mode == 1) {
+        for (int i = 4; i < 7; ++i) AL(h->raw[i], nT);
+        AL(h->dmore, sizeof(int));
+    }
     // RHS transform plan
     if ((rc = make_plan(h, h->nx, h->ny, h->prhs))) return rc;
     const size_t c2 = 2 * tsz(h);

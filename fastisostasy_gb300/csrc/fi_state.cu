@@ -513,9 +513,16 @@ __global__ void k_ts_loop_begin(Ctl* c)
 __device__ __forceinline__ void attempt_begin_one(Ctl* c, int max_iter)
 {
     const double tf = c->tf;
-    if (c->status != ST_OK || !(c->t < tf)) { c->done = 1; c->need_rhs = 0; return; }
-    if (++c->loop_iter > max_iter) { c->status = ST_STEP; c->done = 1; c->need_rhs = 0; return; }
+    if (c->status != ST_OK || !(c->t < tf)) { c->done = 1; c->need_rhs = 0; c->active = 0; return; }
+    if (++c->loop_iter > max_iter) {
+        c->status = ST_STEP;
+        c->done = 1;
+        c->need_rhs = 0;
+        c->active = 0;
+        return;
+    }
     c->done = 0;
+    c->active = 1;
     c->dt = fmin(c->dt, tf - c->t);
     c->h = c->dt;
     c->need_rhs = c->rhs_valid ? 0 : 1;
@@ -528,17 +535,125 @@ __global__ void k_ts_attempt_begin(Ctl* c, int max_iter)
     attempt_begin_one(c, max_iter);
 }
 
-// 1 while the member has attempts left
-__device__ __forceinline__ int attempt_end_one(Ctl* c)
+// 1 while the member has attempts left.  fsal: the first stage of the next
+// attempt is the last stage of an accepted one (true stages), so the
+// cached RHS stays valid.
+__device__ __forceinline__ int attempt_end_one(Ctl* c, int fsal = 0)
 {
-    if (!c->done && c->accepted) c->rhs_valid = 0;   // the state moved: the next attempt needs a new RHS
+    if (!fsal && !c->done && c->accepted) c->rhs_valid = 0;   // the state moved: the next attempt needs a new RHS
     return (!c->done && c->status == ST_OK && c->t < c->tf) ? 1 : 0;
 }
 
-__global__ void k_ts_attempt_end(Ctl* c, cudaGraphConditionalHandle loop)
+// more_out == NULL: sets the WHILE condition `loop`; else writes it there
+__global__ void k_ts_attempt_end(Ctl* c, cudaGraphConditionalHandle loop, int fsal, int* more_out)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    cudaGraphSetConditional(loop, attempt_end_one(c) ? 1u : 0u);
+    const int more = attempt_end_one(c, fsal);
+    if (more_out) *more_out = more;
+    else cudaGraphSetConditional(loop, more ? 1u : 0u);
+}
+
+// --- Tsitouras 5(4) with true stages: the Dormand-Prince 5(4) pair whose
+// truncated coefficients the reference prints, with FSAL ----------------------
+__constant__ double c_dp_a[7][6] = {
+    {0, 0, 0, 0, 0, 0},
+    {1.0 / 5, 0, 0, 0, 0, 0},
+    {3.0 / 40, 9.0 / 40, 0, 0, 0, 0},
+    {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0, 0},
+    {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0, 0},
+    {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656, 0},
+    {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84}};
+__constant__ double c_dp_bs[7] = {5179.0 / 57600, 0, 7571.0 / 16695, 393.0 / 640, -92097.0 / 339200, 187.0 / 2100,
+                                  1.0 / 40};
+
+// block corner means of the stage outputs 0..ns-1 (shared, one thread each)
+template <typename T>
+__device__ __forceinline__ void dp_corner_means(const DPRaw<T>& r, int ns, int nx, int ny, double* cm)
+{
+    __syncthreads();
+    if (threadIdx.x < (unsigned)ns) cm[threadIdx.x] = corner_mean_of(r.p[threadIdx.x], nx, ny);
+    __syncthreads();
+}
+
+// Stage state y = x + h sum_{r<i} a_{i r} k_r (i = 1..6; stage 6 is x2).
+template <typename T>
+__global__ void __launch_bounds__(NT)
+k_dp_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __restrict__ x, DPRaw<T> r, int i, int nx,
+           int ny, double spy)
+{
+    if (c->done) return;
+    __shared__ double cm[7];
+    dp_corner_means(r, i, nx, ny, cm);
+    const double h = c->h;
+    const size_t n = (size_t)nx * ny;
+    if constexpr (sizeof(T) == 8) {
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+            double a = 0.0;
+            for (int q = 0; q < i; ++q) a += c_dp_a[i][q] * (((double)r.p[q][e] - cm[q]) * spy);
+            y[e] = x[e] + h * a;
+        }
+    } else {
+        float af[6], cmf[6];
+        for (int q = 0; q < i; ++q) { af[q] = (float)(c_dp_a[i][q] * h * spy); cmf[q] = (float)cm[q]; }
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+            float a = 0.f;
+            for (int q = 0; q < i; ++q) a += af[q] * ((float)r.p[q][e] - cmf[q]);
+            y[e] = x[e] + (double)a;
+        }
+    }
+}
+
+// x1 = x + h sum_r bs_r k_r; x2 (stage 6 state) is in ts_x2: store x2 - x1
+// and reduce max|x1|, max|x2| into the tolerance.
+template <typename T>
+__global__ void __launch_bounds__(NT) k_dp_err(Dom d, DPRaw<T> r, double atol, double rtol)
+{
+    Ctl* c = d.ctl;
+    if (c->done) return;
+    __shared__ double cm[7];
+    dp_corner_means(r, 7, d.nx, d.ny, cm);
+    const double h = c->h;
+    double v[2] = {0.0, 0.0};
+    const bool mx[2] = {true, true};
+    if constexpr (sizeof(T) == 8) {
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+            double a = 0.0;
+            for (int q = 0; q < 7; ++q) a += c_dp_bs[q] * (((double)r.p[q][e] - cm[q]) * d.spy);
+            const double x1 = d.x[e] + h * a, x2 = d.ts_x2[e];
+            d.ts_dx[e] = x2 - x1;
+            v[0] = fmax(v[0], fabs(x1));
+            v[1] = fmax(v[1], fabs(x2));
+        }
+    } else {
+        // x2 - x1 = h sum_r (a_{6 r} - bs_r) k_r in FP32
+        float ce[7], cmf[7];
+        for (int q = 0; q < 7; ++q) {
+            ce[q] = (float)(((q < 6 ? c_dp_a[6][q] : 0.0) - c_dp_bs[q]) * h * d.spy);
+            cmf[q] = (float)cm[q];
+        }
+        float m1 = 0.f, m2 = 0.f;
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+            float dx = 0.f;
+            for (int q = 0; q < 7; ++q) dx += ce[q] * ((float)r.p[q][e] - cmf[q]);
+            ((float*)d.ts_dx)[e] = dx;
+            const float x2f = (float)d.ts_x2[e];
+            m1 = fmaxf(m1, fabsf(x2f - dx));
+            m2 = fmaxf(m2, fabsf(x2f));
+        }
+        v[0] = (double)m1;
+        v[1] = (double)m2;
+    }
+    double tot[2];
+    if (grid_finish<2>(v, mx, d.partials, &c->counter[1], tot)) c->tol = atol + rtol * fmax(tot[0], tot[1]);
+}
+
+// accepted: the last stage's RHS becomes the next attempt's first (FSAL)
+template <typename T>
+__global__ void __launch_bounds__(NT) k_fsal_copy(const Ctl* __restrict__ c, T* __restrict__ k0,
+                                                  const T* __restrict__ k6, size_t n)
+{
+    if (c->done || !c->accepted) return;
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) k0[e] = k6[e];
 }
 
 template <typename T>
@@ -840,10 +955,32 @@ void step_begin(Ctl* c, int kind, cudaStream_t s) { k_step_begin<<<1, 32, 0, s>>
 void step_end(Ctl* c, cudaStream_t s) { k_step_end<<<1, 32, 0, s>>>(c); }
 void ts_loop_begin(Ctl* c, cudaStream_t s) { k_ts_loop_begin<<<1, 32, 0, s>>>(c); }
 void ts_attempt_begin(Ctl* c, int max_iter, cudaStream_t s) { k_ts_attempt_begin<<<1, 32, 0, s>>>(c, max_iter); }
-void ts_attempt_end(Ctl* c, cudaGraphConditionalHandle loop, cudaStream_t s)
+void ts_attempt_end(Ctl* c, cudaGraphConditionalHandle loop, cudaStream_t s, int fsal, int* more_out)
 {
-    k_ts_attempt_end<<<1, 32, 0, s>>>(c, loop);
+    k_ts_attempt_end<<<1, 32, 0, s>>>(c, loop, fsal, more_out);
 }
+template <typename T>
+void dp_stage(const Ctl* c, double* y, const double* x, const DPRaw<T>& r, int i, int nx, int ny, double spy,
+              cudaStream_t s)
+{
+    k_dp_stage<T><<<grid_for((size_t)nx * ny), NT, 0, s>>>(c, y, x, r, i, nx, ny, spy);
+}
+template <typename T> void dp_err(const Dom& d, const DPRaw<T>& r, double atol, double rtol, cudaStream_t s)
+{
+    k_dp_err<T><<<ts_grid(d.n), NT, 0, s>>>(d, r, atol, rtol);
+}
+template <typename T> void fsal_copy(const Ctl* c, T* k0, const T* k6, size_t n, cudaStream_t s)
+{
+    k_fsal_copy<T><<<grid_for(n), NT, 0, s>>>(c, k0, k6, n);
+}
+template void dp_stage<float>(const Ctl*, double*, const double*, const DPRaw<float>&, int, int, int, double,
+                              cudaStream_t);
+template void dp_stage<double>(const Ctl*, double*, const double*, const DPRaw<double>&, int, int, int, double,
+                               cudaStream_t);
+template void dp_err<float>(const Dom&, const DPRaw<float>&, double, double, cudaStream_t);
+template void dp_err<double>(const Dom&, const DPRaw<double>&, double, double, cudaStream_t);
+template void fsal_copy<float>(const Ctl*, float*, const float*, size_t, cudaStream_t);
+template void fsal_copy<double>(const Ctl*, double*, const double*, size_t, cudaStream_t);
 template <typename T>
 void rk_stage(const Ctl* c, double* y, const double* x, const T* raw, double a, int nx, int ny, double spy,
               cudaStream_t s)

@@ -46,7 +46,18 @@ void step_end(Ctl* c, cudaStream_t s);
 // device-side Tsit5 attempt loop (body of a CUDA graph WHILE node)
 void ts_loop_begin(Ctl* c, cudaStream_t s);
 void ts_attempt_begin(Ctl* c, int max_iter, cudaStream_t s);
-void ts_attempt_end(Ctl* c, cudaGraphConditionalHandle loop, cudaStream_t s);
+// fsal: true stages (keep the cached first-stage RHS after an accept);
+// more_out != NULL: write the loop condition there instead of `loop`
+void ts_attempt_end(Ctl* c, cudaGraphConditionalHandle loop, cudaStream_t s, int fsal = 0, int* more_out = nullptr);
+// true-stage Tsit5 (Dormand-Prince 5(4), FSAL): stage outputs k_0..k_6
+template <typename T> struct DPRaw {
+    const T* p[7];
+};
+template <typename T>
+void dp_stage(const Ctl* c, double* y, const double* x, const DPRaw<T>& r, int i, int nx, int ny, double spy,
+              cudaStream_t s);
+template <typename T> void dp_err(const Dom& d, const DPRaw<T>& r, double atol, double rtol, cudaStream_t s);
+template <typename T> void fsal_copy(const Ctl* c, T* k0, const T* k6, size_t n, cudaStream_t s);
 template <typename T>
 void rk_stage(const Ctl* c, double* y, const double* x, const T* raw, double a, int nx, int ny, double spy,
               cudaStream_t s);

@@ -118,6 +118,26 @@ def test_reference_experiments_tsit54(name, over):
     pair.close()
 
 
+@pytest.mark.parametrize("name,over", [("test1d", {}), ("test2c", {"lithosphere": 2}), ("test3c", {})])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_true_stage_tsit54(name, over, precision):
+    """Tsitouras 5(4) with true stages (the Dormand-Prince 5(4) pair with
+    FSAL, stage states carrying the mantle term): no reference counterpart,
+    GPU against the oracle's same mode."""
+    pair = Pair(ref_disc(name, stage_mode=1, **over), precision=precision)
+    pair.init()
+    pair.step(20)
+    if precision == 0:
+        compare(pair, TOL64)
+        so, sg = pair.orc.scalars(), pair.dom.scalars()
+        assert so["n_accept"] == sg["n_accept"] and so["n_reject"] == sg["n_reject"]
+        assert so["t"] == sg["t"] and abs(so["dt"] - sg["dt"]) <= 1e-10 * so["dt"]
+    else:
+        w_o, w_g = pair.orc.field("w"), pair.dom.field("w")
+        assert rel(w_g, w_o) <= TOLMIX
+    pair.close()
+
+
 @pytest.mark.parametrize("dt_method,stage_mode", [(1, 0), (1, 1), (0, 0), (0, 1)])
 def test_config2_rk4_euler(dt_method, stage_mode):
     wl = W.config2(n=64, L=3000e3 * 64 / 256, dt=1.0, stage_mode=stage_mode)
@@ -201,7 +221,8 @@ def test_error_status_codes():
     dom.close()
 
 
-@pytest.mark.parametrize("precision,integrator", [(0, "rk4"), (1, "rk4"), (0, "tsit54"), (1, "tsit54")])
+@pytest.mark.parametrize("precision,integrator", [(0, "rk4"), (1, "rk4"), (0, "tsit54"), (1, "tsit54"),
+                                                 (0, "tsit54-true"), (1, "tsit54-true")])
 def test_graph_replay_matches_eager(precision, integrator, monkeypatch):
     """Updates replayed from a captured CUDA graph give bit-identical state to
     the same updates launched one kernel at a time.  For Tsit5 the captured
@@ -209,8 +230,10 @@ def test_graph_replay_matches_eager(precision, integrator, monkeypatch):
     path decides on the host: same attempts, same bits."""
     if integrator == "rk4":
         wl = W.config2(n=64, L=3000e3 * 64 / 256, dt=1.0, stage_mode=1)
-    else:
+    elif integrator == "tsit54":
         wl = ref_disc("test1d")
+    else:
+        wl = ref_disc("test1d", stage_mode=1)
     out = []
     for no_graph in ("1", "0"):
         monkeypatch.setenv("FI_NO_GRAPHS", no_graph)
