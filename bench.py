@@ -412,6 +412,93 @@ def serve_leg(lams=(10, 30, 100, 300, 1000, 2000), n_req=48, reserve_gb=8.0):
             "sequential_fp64_service_s": {str(k): {"setup": v[0], "per_update": v[1]} for k, v in cost.items()}}
 
 
+def configs_leg():
+    """The other configurations as bounded samples: config 1 (128^2 uniform
+    disc, reference-compatible Tsit5), config 2 (256^2 Gaussian lithosphere,
+    RK4 true stages dt = 1 yr) and config 3 (336 x 560 ice grid padded to
+    512 x 1024, interactive sea level, two-layer freqdomain mantle,
+    reference-compatible Tsit5).  Each form runs the same updates; config 3
+    reports the mixed form's error and mask mismatches against the FP64 form
+    (the FP64 form is held to the oracle by the parity tests; the oracle takes
+    minutes per config-3 update on one core)."""
+    import torch
+    from fastisostasy_gb300 import workloads as W
+    from fastisostasy_gb300.isostasy import Domain
+    from fastisostasy_gb300 import _lib
+
+    def run(wl, prec, n_warm, n_timed, stage_mode=None):
+        p = dict(wl.params)
+        if stage_mode is not None:
+            p["stage_mode"] = stage_mode
+        d = Domain(p, wl.nx_ice, wl.ny_ice, wl.dx, precision=prec)
+        f = wl.padded_fields(d.nx, d.ny)
+        if f:
+            d.set_fields(**f)
+        b = _lib.FiBsl()
+        b.method, b.constant_ocean_surface = 0, 1
+        b.A_ocean_pd = b.A_ocean_now = 3.625e14
+        d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+        t = 0.0
+        for _ in range(n_warm):
+            t += wl.dtt
+            d.update(wl.H_final, t, b)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        for _ in range(n_timed):
+            t += wl.dtt
+            d.update_async(0, t, b)
+        d.synchronize()
+        secs = time.perf_counter() - a
+        out = {k: d.field(k) for k in ("w", "maskocean", "maskgrounded", "maskcontinent")}
+        cells = d.nx * d.ny
+        d.close()
+        return n_timed * wl.dtt / 1000.0 / secs, secs, out, cells
+
+    def cpu(wl, n_timed, stage_mode=None):
+        from oracle import oracle as O
+        O.set_threads(1)
+        p = dict(wl.params)
+        if stage_mode is not None:
+            p["stage_mode"] = stage_mode
+        m = O.Model(p, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
+        f = wl.padded_fields(m.nx, m.ny)
+        if f:
+            m.set_fields(**f)
+        bo = O.make_bsl()
+        m.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, bo)
+        t = wl.dtt
+        m.update(wl.H_final, t, bo)
+        a = time.perf_counter()
+        for _ in range(n_timed):
+            t += wl.dtt
+            m.update(wl.H_final, t, bo)
+        secs = time.perf_counter() - a
+        m.close()
+        return n_timed * wl.dtt / 1000.0 / secs
+
+    res = {}
+    cases = [("config1", W.config1(128), 0, 3, 100, 20), ("config2", W.config2(n=256), None, 3, 30, 2)]
+    for name, wl, sm, nw, nt, nc in cases:
+        k64, s64, o64, cells = run(wl, 0, nw, nt, sm)
+        k32, s32, o32, _ = run(wl, 1, nw, nt, sm)
+        err = float(np.abs(o32["w"] - o64["w"]).max() / max(np.abs(o64["w"]).max(), 1e-300))
+        res[name] = {"cells": cells, "updates_timed": nt, "fp64_kyr_s": k64, "mixed_kyr_s": k32,
+                     "mixed_over_fp64": k32 / k64, "err_mixed_vs_fp64": err,
+                     "cpu_oracle_1core_kyr_s": cpu(wl, nc, sm)}
+    wl = W.config3()
+    k64, s64, o64, cells = run(wl, 0, 2, 4)
+    k32, s32, o32, _ = run(wl, 1, 2, 4)
+    wmax = max(np.abs(o64["w"]).max(), 1e-300)
+    res["config3"] = {"cells": cells, "updates_timed": 4, "fp64_kyr_s": k64, "mixed_kyr_s": k32,
+                      "mixed_over_fp64": k32 / k64,
+                      "err_mixed_vs_fp64": {"max_rel": float(np.abs(o32["w"] - o64["w"]).max() / wmax),
+                                            "rms_rel": float(np.sqrt(np.mean((o32["w"] - o64["w"]) ** 2)) / wmax)},
+                      "mask_mismatch": {m: int(np.sum(o32[m] != o64[m]))
+                                        for m in ("maskocean", "maskgrounded", "maskcontinent")},
+                      "cpu_oracle_1core_kyr_s": None}
+    return res
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -465,9 +552,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--ensemble-members", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--only", choices=["ensemble", "serve"],
+    ap.add_argument("--only", choices=["ensemble", "serve", "configs"],
                     help="run one secondary leg alone and print its JSON (for profiling), not a bench line")
     ap.add_argument("--lean", action="store_true",
                     help="mixed form only, no profile / e2e / CPU legs (for ncu captures); prints the timing only")
@@ -501,6 +589,9 @@ def main():
         return 0
     if args.only == "serve":
         print(json.dumps({"serve": serve_leg(n_req=args.serve_requests)}))
+        return 0
+    if args.only == "configs":
+        print(json.dumps({"configs": configs_leg()}))
         return 0
     if args.lean:
         dom, wl, b = make_domain(1)
@@ -546,7 +637,9 @@ def main():
                "sample": "%d coupling steps of the same workload (%d x 40 RHS + 2 convolutions at 1023^2), "
                          "%.1f s, 1 thread (the reference is serial)" % (args.cpu_samples, args.cpu_samples, secs)}
 
-    ens = serve = None
+    ens = serve = cfgs = None
+    if not args.no_configs:
+        cfgs = configs_leg()
     if not args.no_ensemble:
         ens = ensemble_leg(args.ensemble_members)
     if not args.no_serve:
@@ -574,6 +667,7 @@ def main():
                                           "achieved": upd / (r32["ms"] / 1000.0) / 1e9,
                                           "frac": upd / (r32["ms"] / 1000.0) / 1e9 / peak}},
             "cpu_baseline": cpu,
+            "configs": cfgs,
             "ensemble": ens,
             "serve": serve,
             "clocks": r32["clocks"],
