@@ -96,6 +96,9 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
     }
     __syncthreads();
     const double sd = s_sc[0], cmd = s_sc[1];
+    // float copies made once: every FP64 instruction (conversions included)
+    // costs the mixed form 64 FP32 slots on this GPU
+    const float sdf = (float)sd, cmdf = (float)cmd, cmant = (float)g.fc.coef_mantle;
 
     // level 0: forward differences along x (dX) and y (dY)
     for (int e = tid; e < (RA + 4) * nx; e += nt) {
@@ -106,7 +109,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         if (i < nx - 1) {
             if constexpr (std::is_same<T, float>::value) {
                 float v = (g.xhi[c0 + 1] - g.xhi[c0]) + (g.xlo[c0 + 1] - g.xlo[c0]);
-                if (rprev) v += (float)sd * (rprev[c0 + 1] - rprev[c0]);
+                if (rprev) v += sdf * (rprev[c0 + 1] - rprev[c0]);
                 dX[(size_t)r * nx + i] = v;
             } else {
                 double y1 = g.x[c0 + 1], y0 = g.x[c0];
@@ -118,7 +121,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
             const size_t c1 = c0 + nx;
             if constexpr (std::is_same<T, float>::value) {
                 float v = (g.xhi[c1] - g.xhi[c0]) + (g.xlo[c1] - g.xlo[c0]);
-                if (rprev) v += (float)sd * (rprev[c1] - rprev[c0]);
+                if (rprev) v += sdf * (rprev[c1] - rprev[c0]);
                 dY[(size_t)r * nx + i] = v;
             } else {
                 double y1 = g.x[c1], y0 = g.x[c0];
@@ -205,8 +208,8 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
                 // q0 + (-g rho_m) (y - w_ref) with y the stage state
                 if constexpr (std::is_same<T, float>::value) {
                     float dy = (g.xhi[c] - g.wrefhi[c]) + (g.xlo[c] - g.wreflo[c]);
-                    if (rprev) dy += (float)sd * (rprev[c] - (float)cmd);
-                    p = q0[c] + (float)g.fc.coef_mantle * dy;
+                    if (rprev) dy += sdf * (rprev[c] - cmdf);
+                    p = q0[c] + cmant * dy;
                 } else {
                     double y = g.x[c];
                     if (rprev) y += sd * ((double)rprev[c] - cmd);
@@ -404,20 +407,28 @@ __global__ void __launch_bounds__(256) k_engine_rk4(EngineArgs g)
             for (int s = 0; s < 4; ++s) s_c[1 + s] = corner_mean_of((const T*)g.raw[s], nx, ny);
         }
         __syncthreads();
+        const float c1f = (float)s_c[1], c2f = (float)s_c[2], c3f = (float)s_c[3], c4f = (float)s_c[4];
+        const float scf = (float)(s_c[0] * g.spy);
         const T* r1 = (const T*)g.raw[0];
         const T* r2 = (const T*)g.raw[1];
         const T* r3 = (const T*)g.raw[2];
         const T* r4 = (const T*)g.raw[3];
         for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
             if constexpr (std::is_same<T, float>::value) {
-                const float k = ((((float)r1[e] - (float)s_c[1]) + 2.f * ((float)r2[e] - (float)s_c[2])) +
-                                 2.f * ((float)r3[e] - (float)s_c[3])) + ((float)r4[e] - (float)s_c[4]);
-                const double v = g.x[e] + (double)(k * (float)(s_c[0] * g.spy));
+                const float k = ((((float)r1[e] - c1f) + 2.f * ((float)r2[e] - c2f)) + 2.f * ((float)r3[e] - c3f)) +
+                                ((float)r4[e] - c4f);
+                const float inc = k * scf;
+                const double v = g.x[e] + (double)inc;   // the FP64 state update
                 g.x[e] = v;
                 g.w[e] = v;
-                const float hi = (float)v;
-                g.xhi[e] = hi;
-                g.xlo[e] = (float)(v - (double)hi);
+                // the float pair of x takes the same increment by an FP32 two-sum
+                const float hi = g.xhi[e], lo = g.xlo[e];
+                const float sm = hi + inc, bb = sm - hi;
+                const float er = (hi - (sm - bb)) + (inc - bb);
+                const float l2 = lo + er;
+                const float h2 = sm + l2;
+                g.xhi[e] = h2;
+                g.xlo[e] = l2 - (h2 - sm);
             } else {
                 const double k1 = ((double)r1[e] - s_c[1]) * g.spy, k2 = ((double)r2[e] - s_c[2]) * g.spy;
                 const double k3 = ((double)r3[e] - s_c[3]) * g.spy, k4 = ((double)r4[e] - s_c[4]) * g.spy;
