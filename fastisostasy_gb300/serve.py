@@ -134,68 +134,93 @@ class Server:
 class Ensemble:
     """Members (independent domains, any sizes) advanced in lockstep.
 
-    mode "graph": one fi_batch_step per coupling step runs the whole
-    ensemble as one CUDA graph whose Tsit5 attempts are batched launches over
-    all members (members must run reference-compatible Tsit5).
+    mode "graph": one fi_batch_step per coupling step runs a group of
+    members as one CUDA graph whose Tsit5 attempts are batched launches over
+    the group (members must run reference-compatible Tsit5).  With
+    groups > 1 the members are sorted by an estimate of their stiffness
+    (max D / (eta dx^3), which sets how many attempts an update needs) and
+    split into that many groups, each a batch on its own stream, so a stiff
+    member holds back only the members of its own group.
     mode "streams": fi_batch_update enqueues one isos_update per member on
     the member's own stream (any integrator)."""
 
-    def __init__(self, workloads, precision: int = 1, mode: str = "graph"):
+    def __init__(self, workloads, precision: int = 1, mode: str = "graph", groups: int = 1):
         from .isostasy import Domain
         self.L = _lib.load()
         self.mode = mode
         self.doms = []
-        self.bsl = (_lib.FiBsl * len(workloads))()
-        for i, wl in enumerate(workloads):
+        n = len(workloads)
+        stiff = []
+        for wl in workloads:
             d = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=precision)
             f = wl.padded_fields(d.nx, d.ny)
             if f:
                 d.set_fields(**f)
-            b = self.bsl[i]
+            self.doms.append(d)
+            if mode == "graph" and groups > 1:
+                stiff.append(float(np.max(d.field("D_lith") / d.field("eta_eff"))) / wl.dx ** 3)
+        order = sorted(range(n), key=lambda i: -stiff[i]) if stiff else list(range(n))
+        ng = max(1, min(groups if mode == "graph" else 1, n))
+        self.groups = [order[g * n // ng:(g + 1) * n // ng] for g in range(ng)]
+        self.slot = {}
+        self.bsls = []
+        for g, members in enumerate(self.groups):
+            arr = (_lib.FiBsl * len(members))()
+            for j, i in enumerate(members):
+                self.slot[i] = (g, j)
+            self.bsls.append(arr)
+        for i, (d, wl) in enumerate(zip(self.doms, workloads)):
+            b = self.bsl_of(i)
             b.method, b.constant_ocean_surface = 0, 1
             b.bsl_init = b.bsl_now = 0.0
             b.A_ocean_pd = b.A_ocean_now = 3.625e14
             d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
-            self.doms.append(d)
         self.wls = list(workloads)
-        self.hs = (C.c_void_p * len(self.doms))(*[d.h.value for d in self.doms])
-        self.batch = None
+        self.hss = [(C.c_void_p * len(m))(*[self.doms[i].h.value for i in m]) for m in self.groups]
+        self.batches = []
         if mode == "graph":
-            bh = C.c_void_p()
-            rc = self.L.fi_batch_create(self.hs, len(self.doms), C.byref(bh))
-            if rc:
-                raise FiError(rc, "fi_batch_create")
-            self.batch = bh
+            for hs, m in zip(self.hss, self.groups):
+                bh = C.c_void_p()
+                rc = self.L.fi_batch_create(hs, len(m), C.byref(bh))
+                if rc:
+                    raise FiError(rc, "fi_batch_create")
+                self.batches.append(bh)
         self.t = 0.0
+
+    def bsl_of(self, i):
+        g, j = self.slot[i]
+        return self.bsls[g][j]
 
     def first_update(self, t: float):
         """Apply each member's ice load with a synchronous isos_update."""
         for i, (d, wl) in enumerate(zip(self.doms, self.wls)):
-            d.update(wl.H_final, t, self.bsl[i])
+            d.update(wl.H_final, t, self.bsl_of(i))
         self.t = t
 
     def update(self, t: float):
-        if self.batch is not None:
-            rc = self.L.fi_batch_step(self.batch, float(t), self.bsl)
-        else:
-            rc = self.L.fi_batch_update(self.hs, len(self.doms), float(t), self.bsl)
-        if rc:
-            raise FiError(rc, "batched update")
+        for g, m in enumerate(self.groups):
+            if self.batches:
+                rc = self.L.fi_batch_step(self.batches[g], float(t), self.bsls[g])
+            else:
+                rc = self.L.fi_batch_update(self.hss[g], len(m), float(t), self.bsls[g])
+            if rc:
+                raise FiError(rc, "batched update")
         self.t = t
 
     def synchronize(self):
-        st = (C.c_int32 * len(self.doms))()
-        if self.batch is not None:
-            rc = self.L.fi_batch_wait(self.batch, st)
-        else:
-            rc = self.L.fi_batch_synchronize(self.hs, len(self.doms), st)
-        if rc:
-            raise FiError(rc, "ensemble member %d" % next(i for i, v in enumerate(st) if v))
+        for g, m in enumerate(self.groups):
+            st = (C.c_int32 * len(m))()
+            if self.batches:
+                rc = self.L.fi_batch_wait(self.batches[g], st)
+            else:
+                rc = self.L.fi_batch_synchronize(self.hss[g], len(m), st)
+            if rc:
+                raise FiError(rc, "ensemble member %d" % m[next(j for j, v in enumerate(st) if v)])
 
     def close(self):
-        if self.batch is not None:
-            self.L.fi_batch_destroy(self.batch)
-            self.batch = None
+        for b in self.batches:
+            self.L.fi_batch_destroy(b)
+        self.batches = []
         for d in self.doms:
             d.close()
         self.doms = []
