@@ -98,6 +98,8 @@ struct fi_handle {
     int nx, ny, nx_ice, ny_ice, icrop1, icrop2, jcrop1, jcrop2;
     size_t n;
     double dx, dy, spy, cc, Vden;
+    double rate_scale = 1.0;           // stage outputs -> rates: sec/yr (method 3) or 1 (methods 0-2)
+    double L_w = 0.0;                  // flexural length scale (LV-ELRA)
     double time_diag, time_prog;
     int ref_was_set = 0, state_ready = 0;
     double h_t = 0.0, h_dt = 0.0;       // host mirror of the ode clock (euler/rk4)
@@ -134,7 +136,7 @@ struct fi_handle {
     std::vector<void*> allocs;
     std::string err;
     // host copies of the static fields
-    std::vector<double> K, kappa, R, D, He, eta_eff, GE, GN, xc, yc;
+    std::vector<double> K, kappa, R, D, He, eta_eff, GE, GN, GV, xc, yc;
     std::vector<uint8_t> mact;
     // device
     Dom d;
@@ -152,7 +154,9 @@ struct fi_handle {
     void* mA = nullptr;                  // 1/(kappa R) at (k, l) (T)
     void* mB = nullptr;                  // 1/(kappa R) at (-k, l) (T)
     void* S2 = nullptr;                  // convolution spectrum (T complex)
-    void* KS[2] = {nullptr, nullptr};    // elastic / geoid kernel spectra (T complex)
+    void* KS[3] = {nullptr, nullptr, nullptr};   // elastic / geoid / LV-ELRA viscous kernel spectra (T complex)
+    double* weq = nullptr;               // equilibrium displacement (methods 0-2)
+    double* weq_raw = nullptr;           // LV-ELRA convolution output
     void* conv_in = nullptr;             // convolution input (T)
     double *we_raw = nullptr, *dz_raw = nullptr, *corners = nullptr;
     int* out_rows = nullptr;
@@ -358,6 +362,59 @@ void gauss_bump(const fi_handle* h, const std::vector<double>& xc, const std::ve
         }
 }
 
+// Kelvin function kei for LV-ELRA.  The reference interpolates a table of
+// kei(x) at x = 0, 0.01, .., 10 printed with five significant digits and
+// stored as single-precision literals (src/kelvin_function.f90:91-132,
+// 166-1233).  The table is computed here from the function itself,
+// kei(x) = Im K_0(x e^{i pi/4}) = -int_0^inf exp(-a) sin(a) dt with
+// a = x cosh(t) / sqrt(2) (trapezoid rule on an even analytic integrand),
+// then rounded the same way.
+double kelvin_kei(double x)
+{
+    if (x <= 0.0) return -0.78539816339744830962;   // -pi/4
+    const double h = 1.0 / 64.0, r2 = std::sqrt(2.0);
+    double sum = 0.0;
+    for (int k = 0;; ++k) {
+        const double a = x * std::cosh(k * h) / r2;
+        if (a > 60.0) break;
+        sum += (k == 0 ? 0.5 : 1.0) * std::exp(-a) * std::sin(a);
+    }
+    return -h * sum;
+}
+
+struct KeiTable {
+    static constexpr int N = 1001;
+    double rn[N], v[N];
+    KeiTable()
+    {
+        char buf[64];
+        for (int i = 0; i < N; ++i) {
+            const double x = i / 100.0;
+            snprintf(buf, sizeof(buf), "%.4f", x);
+            rn[i] = (double)strtof(buf, nullptr);
+            snprintf(buf, sizeof(buf), "%.4E", kelvin_kei(x));
+            v[i] = (double)strtof(buf, nullptr);
+        }
+    }
+    // get_kei_value: linear interpolation, the last value beyond the table
+    double at(double r, double L_w) const
+    {
+        const double q = r / L_w;
+        if (q > rn[N - 1]) return v[N - 1];
+        int k = (int)(q * 100.0);
+        if (k > N - 2) k = N - 2;
+        while (k > 0 && q < rn[k]) --k;
+        while (k < N - 2 && q >= rn[k + 1]) ++k;
+        return v[k] + (q - rn[k]) / (rn[k + 1] - rn[k]) * (v[k + 1] - v[k]);
+    }
+};
+
+const KeiTable& kei_table()
+{
+    static const KeiTable t;   // built once, thread-safe
+    return t;
+}
+
 void host_fields(fi_handle* h)
 {
     const fi_params& p = h->p;
@@ -367,7 +424,7 @@ void host_fields(fi_handle* h)
     h->R.assign(n, 1.0);
     h->eta_eff.assign(n, p.viscosities[p.nl - 1]);
     host_kappa(h);
-    if (p.lithosphere == 1 || p.lithosphere == 2) {
+    if (p.method == 3 && (p.lithosphere == 1 || p.lithosphere == 2)) {
         std::vector<double> g;
         gauss_bump(h, h->xc, h->yc, g);
         double mx = -1e300;
@@ -379,7 +436,9 @@ void host_fields(fi_handle* h)
         }
     }
     const int nl = p.nl;
-    if (p.mantle == 0) {
+    if (p.method != 3) {
+        // methods 0-2 use no viscosity field
+    } else if (p.mantle == 0) {
         // calc_effective_viscosity, src/lv_elva.f90:207-306
         std::vector<double> bnd((size_t)nl * n);
         for (size_t e = 0; e < n; ++e) bnd[e] = h->He[e];
@@ -446,9 +505,24 @@ void host_fields(fi_handle* h)
             const double rr = (dx / 2 > r) ? dx / 2 : r;
             h->GN[(size_t)(j - 1) * nx + (i - 1)] = p.r_earth / (2. * p.m_earth * std::sin(rr / (2. * p.r_earth)));
         }
-    // maskactive, src/fastisostasy.f90:185-198
+    // LV-ELRA kernel, src/fastisostasy.f90:216-236: kei filter on the padded
+    // domain, GV = -L_w^2 / (2 pi D) kei (dx dy) (src/green_functions.f90:28-41),
+    // L_w = (D / (rho_m g))^(1/4) (src/isos_utils.f90:66-73)
+    if (p.method == 2) {
+        const double Dc = rigidity(p.E, p.zl[0], p.nu);
+        h->L_w = std::pow(Dc / (p.rho_uppermantle * p.g), 0.25);
+        const KeiTable& kt = kei_table();
+        h->GV.assign(n, 0.0);
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const double x = h->xc[i], y = h->yc[j];
+                const double kei = kt.at(std::sqrt(x * x + y * y), h->L_w);
+                h->GV[(size_t)j * nx + i] = -(h->L_w * h->L_w) / (2.0 * PI_LIT * Dc) * kei * (dx * dx);
+            }
+    }
+    // maskactive, src/fastisostasy.f90:185-198; methods 0-2: all active (:444-451)
     h->mact.assign(n, 0);
-    if (!p.interactive_sealevel) {
+    if (p.method != 3 || !p.interactive_sealevel) {
         for (auto& m : h->mact) m = 1;
     } else if (p.min_pad > sp(100.e3)) {
         for (int j = h->jcrop1; j <= h->jcrop2; ++j)
@@ -528,6 +602,12 @@ void rhs(fi_handle* h, const double* y, const double* wref, T* raw_out, const in
          const float* whi = nullptr, const float* wlo = nullptr)
 {
     typedef typename vec2<T>::type C2;
+    if (h->p.method != 3) {
+        // methods 0-2: (w_eq - y) / tau, w_eq computed once per update
+        PROF(h, K_FLEX, relax_rate<T>(raw_out, y, h->weq, h->p.tau, h->n, gate, h->s));
+        h->launches += 1;
+        return;
+    }
     PROF(h, K_FLEX, launch_flexure<T>(y, wref, (const T*)h->q0, h->d.mactive, (const T*)h->Dt, (const T*)h->inv2eta,
                                       (T*)h->f, h->nx, h->ny, h->fc, h->s, gate, whi, wlo));
     PROF(h, K_ROWS_FWD, launch_rows_fwd<T>((const T*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, h->prhs, h->s, gate));
@@ -571,7 +651,7 @@ int plan_steps(fi_handle* h, double tf)
 template <typename T> T* enqueue_steps(fi_handle* h, int nsteps)
 {
     const fi_params& p = h->p;
-    const double spy = h->spy;
+    const double spy = h->rate_scale;
     T *r0 = (T*)h->raw[0], *r1 = (T*)h->raw[1], *r2 = (T*)h->raw[2], *r3 = (T*)h->raw[3];
     const bool truem = p.stage_mode == 1;
     const double* wref = truem ? h->w_ref : nullptr;
@@ -658,7 +738,7 @@ template <typename T> void tsit_true_attempt(fi_handle* h, cudaGraphConditionalH
     rhs<T>(h, h->d.x, h->w_ref, (T*)h->raw[0], &h->ctl->need_rhs);
     for (int i = 1; i <= 6; ++i) {
         double* y = i == 6 ? h->d.ts_x2 : h->y;
-        PROF(h, K_STAGE, dp_stage<T>(h->ctl, y, h->d.x, R, i, h->nx, h->ny, h->spy, h->s));
+        PROF(h, K_STAGE, dp_stage<T>(h->ctl, y, h->d.x, R, i, h->nx, h->ny, h->rate_scale, h->s));
         rhs<T>(h, y, h->w_ref, (T*)h->raw[i], &h->ctl->active);
     }
     PROF(h, K_TS, dp_err<T>(h->d, R, p.atol, p.rtol, h->s));
@@ -782,6 +862,17 @@ template <typename T> void enqueue_pre(fi_handle* h, const double* dH, bool diag
     PROF(h, K_UPD_LOAD, upd_load<T>(h->d, h->dz_raw, h->corners + 4, dz_mode, (T*)h->q0, p.stage_mode,
                                     run_integrator ? 1 : 0, h->s));
     h->launches += 4;
+    if (p.method == 0 || p.method == 1) {
+        // LLRA equilibrium -canom_load / rho_m (zero for method 0)
+        weq_local(h->weq, h->d.c_load, p.rho_uppermantle, p.method == 0 ? 1 : 0, h->n, h->s);
+        h->launches += 1;
+    } else if (p.method == 2) {
+        // LV-ELRA: (-canom_load g K^2) convolved with GV, corner BCs
+        elra_load<T>((T*)h->conv_in, h->d.c_load, h->d.K2, p.g, h->n, h->s);
+        conv<T>(h, 2, h->weq_raw, h->corners + 8);
+        weq_elra(h->weq, h->weq_raw, h->corners + 8, h->nx, h->ny, h->s);
+        h->launches += 2;
+    }
 }
 
 // The tail: corner BC of w, canom_mantle, z_bed, dwdt, checks (:856-869).
@@ -966,7 +1057,7 @@ namespace {
 // window {nx, ny, icrop1, icrop2, jcrop1, jcrop2}; allocates nothing.
 int padded_domain(const fi_params& p, int nx_ice, int ny_ice, double dx, double dy, int* pd)
 {
-    if (p.method != 3 || nx_ice < 3 || ny_ice < 3 || p.nl < 1 || p.nl > 8) return FI_E_CONFIG;
+    if (p.method < 0 || p.method > 3 || nx_ice < 3 || ny_ice < 3 || p.nl < 1 || p.nl > 8) return FI_E_CONFIG;
     if (dx != dy || p.min_pad < 0.0) return FI_E_CONFIG;   // src/isos_utils.f90:292-300
     int nx_tmp = nx_ice, ny_tmp = ny_ice, npx, npy, nx, ny;
     int icrop1 = 1, jcrop1 = 1;
@@ -988,6 +1079,7 @@ int padded_domain(const fi_params& p, int nx_ice, int ny_ice, double dx, double 
         ny = ny_tmp + 2 * npy;
     }
     if (nx > 2048 || ny > 2048) return FI_E_CONFIG;   // column FFT of 2n must fit in shared memory
+    if (p.method == 2 && nx != ny) return FI_E_CONFIG;  // calc_kei_filter_2D needs a square domain
     pd[0] = nx;
     pd[1] = ny;
     pd[2] = icrop1 + npx;
@@ -1031,6 +1123,7 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     h->jcrop2 = pd[5];
     h->n = (size_t)h->nx * h->ny;
     h->spy = (double)(3600.0f * 24.0f * 365.25f);   // src/fastisostasy.f90:158
+    h->rate_scale = p.method == 3 ? h->spy : 1.0;
     h->cc = p.correct_compression ? 1.5 / (1 + p.nu) : 1.0;
     h->Vden = p.rho_ice / p.rho_water - p.rho_ice / p.rho_seawater;
     h->time_diag = sp(1e10);
@@ -1074,7 +1167,7 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     d.rho_l = p.rho_litho;
     d.g = p.g;
     d.Vden = h->Vden;
-    d.spy = h->spy;
+    d.spy = h->rate_scale;
     d.rho_sw_over_ice = p.rho_seawater / p.rho_ice;
     d.rho_ice_over_sw = p.rho_ice / p.rho_seawater;
     int rc = 0;
@@ -1095,6 +1188,13 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     AL(d.m_ocean, n); AL(d.m_grounded, n); AL(d.m_cont, n);
     AL(h->ctl, sizeof(Ctl));
     d.ctl = h->ctl;
+    if (p.method != 3) {
+        // methods 0-2 produce the rate itself: no corner mean, no sec/yr
+        Ctl c0;
+        memset(&c0, 0, sizeof(c0));
+        c0.plain = 1;
+        if ((rc = upload(h, h->ctl, &c0, sizeof(Ctl)))) return rc;
+    }
     AL(d.partials, (size_t)reduce_blocks(n) * 4 * sizeof(double));
     if (p.dt_method == 2) {
         AL(d.ts_x2, n * sizeof(double));
@@ -1125,8 +1225,13 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     AL(h->S2, (size_t)h->Py * h->pconv.sp * c2);
     AL(h->KS[0], (size_t)h->Py * h->pconv.sp * c2);
     AL(h->KS[1], (size_t)h->Py * h->pconv.sp * c2);
+    if (p.method == 2) { AL(h->KS[2], (size_t)h->Py * h->pconv.sp * c2); }
     AL(h->conv_in, nT);
-    AL(h->we_raw, n * 8); AL(h->dz_raw, n * 8); AL(h->corners, 8 * sizeof(double));
+    AL(h->we_raw, n * 8); AL(h->dz_raw, n * 8); AL(h->corners, 12 * sizeof(double));
+    if (p.method != 3) {
+        AL(h->weq, n * 8);
+        if (p.method == 2) { AL(h->weq_raw, n * 8); }
+    }
     AL(h->out_rows, (h->ny + 2) * sizeof(int));
     {
         std::vector<int> rows(h->ny + 2);
@@ -1181,7 +1286,8 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     // cooperative step engine for true-stage RK4 on uniform grids
     {
         const char* ev = getenv("FI_NO_ENGINE");
-        const bool want = p.stage_mode == 1 && p.dt_method == 1 && h->uniform && !(ev && ev[0] == '1');
+        const bool want = p.method == 3 && p.stage_mode == 1 && p.dt_method == 1 && h->uniform &&
+                          !(ev && ev[0] == '1');
         if (want) {
             int ok = mixed(h) ? engine_config<float>(h->prhs, &h->eng_grid, &h->eng_CB, &h->eng_smem)
                               : engine_config<double>(h->prhs, &h->eng_grid, &h->eng_CB, &h->eng_smem);
@@ -1196,6 +1302,7 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     }
     if ((rc = upload_static(h))) return rc;
     if ((rc = kernel_spectrum(h, h->GE, 0)) || (rc = kernel_spectrum(h, h->GN, 1))) return rc;
+    if (p.method == 2 && (rc = kernel_spectrum(h, h->GV, 2))) return rc;
     // zero_init_state (src/fastisostasy.f90:505-548): z_bed background 1e6
     {
         std::vector<double> bg(n, 1e6);
@@ -1761,7 +1868,8 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         if (!h) return FI_E_ARG;
         if (!h->state_ready) return fail(h, FI_E_STATE, "fi_batch_create before fi_init_state");
         const fi_handle* h0 = hs[0];
-        if (h->p.dt_method != 2 || h->p.stage_mode != 0 || mixed(h) != mixed(h0) || (mixed(h) && !h->d.whi) ||
+        if (h->p.method != 3 || h->p.dt_method != 2 || h->p.stage_mode != 0 || mixed(h) != mixed(h0) ||
+            (mixed(h) && !h->d.whi) ||
             h->p.dt_diagnostics != h0->p.dt_diagnostics || h->time_diag != h0->time_diag || !h->tsit_graph_ok)
             return fail(h, FI_E_CONFIG,
                         "batched members must run reference-compatible tsit54 in the same precision, in lockstep "

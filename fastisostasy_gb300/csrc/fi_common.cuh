@@ -64,7 +64,7 @@ struct Ctl {
     int have_rhs;              // device Tsit5 loop: an RHS was evaluated during this update
     int loop_iter;             // device Tsit5 loop: attempts during this update
     int active;                // device Tsit5 loop: this attempt runs (gate of the stage RHS)
-    int pad_;
+    int plain;                 // methods 0-2: stage outputs are the rate itself (no corner mean, no sec/yr)
     long long n_accept, n_reject, n_rhs, n_attempt;
     unsigned int counter[8];   // last-block arrival counters of grid reductions
 };

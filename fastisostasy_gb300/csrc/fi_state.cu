@@ -292,7 +292,7 @@ k_rk_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __re
            double a, int nx, int ny, double spy)
 {
     if (c->done) return;
-    const double cm = block_corner_mean(raw, nx, ny);
+    const double cm = c->plain ? 0.0 : block_corner_mean(raw, nx, ny);
     const double ah = a * c->h;
     const size_t n = (size_t)nx * ny;
     if (sizeof(T) == 8) {
@@ -319,11 +319,12 @@ k_rk4_final(Ctl* c, double* __restrict__ x, double* __restrict__ w, const T* __r
     __shared__ double s[5];
     __syncthreads();
     if (threadIdx.x == 0) {
+        const bool pl = c->plain != 0;
         s[0] = c->h / 6;
-        s[1] = corner_mean_of(r1, nx, ny);
-        s[2] = corner_mean_of(r2, nx, ny);
-        s[3] = corner_mean_of(r3, nx, ny);
-        s[4] = corner_mean_of(r4, nx, ny);
+        s[1] = pl ? 0.0 : corner_mean_of(r1, nx, ny);
+        s[2] = pl ? 0.0 : corner_mean_of(r2, nx, ny);
+        s[3] = pl ? 0.0 : corner_mean_of(r3, nx, ny);
+        s[4] = pl ? 0.0 : corner_mean_of(r4, nx, ny);
     }
     __syncthreads();
     const double h6 = s[0], c1 = s[1], c2 = s[2], c3 = s[3], c4 = s[4];
@@ -362,7 +363,7 @@ k_euler_final(const Ctl* __restrict__ c, double* __restrict__ x, double* __restr
               int nx, int ny, double spy)
 {
     if (c->done) return;
-    const double c1 = block_corner_mean(r1, nx, ny);
+    const double c1 = c->plain ? 0.0 : block_corner_mean(r1, nx, ny);
     const double h = c->h;
     const size_t n = (size_t)nx * ny;
     if (sizeof(T) == 8) {
@@ -404,7 +405,7 @@ __device__ __forceinline__ void ts_max_body(Dom d, const T* __restrict__ raw, do
     Ctl* c = d.ctl;
     if (c->done) return;
     const double dt = c->h;
-    const double cm = block_corner_mean(raw, d.nx, d.ny);
+    const double cm = c->plain ? 0.0 : block_corner_mean(raw, d.nx, d.ny);
     double v[2] = {0.0, 0.0};
     const bool mx[2] = {true, true};
     if constexpr (sizeof(T) == 4) {
@@ -568,10 +569,10 @@ __constant__ double c_dp_bs[7] = {5179.0 / 57600, 0, 7571.0 / 16695, 393.0 / 640
 
 // block corner means of the stage outputs 0..ns-1 (shared, one thread each)
 template <typename T>
-__device__ __forceinline__ void dp_corner_means(const DPRaw<T>& r, int ns, int nx, int ny, double* cm)
+__device__ __forceinline__ void dp_corner_means(const Ctl* c, const DPRaw<T>& r, int ns, int nx, int ny, double* cm)
 {
     __syncthreads();
-    if (threadIdx.x < (unsigned)ns) cm[threadIdx.x] = corner_mean_of(r.p[threadIdx.x], nx, ny);
+    if (threadIdx.x < (unsigned)ns) cm[threadIdx.x] = c->plain ? 0.0 : corner_mean_of(r.p[threadIdx.x], nx, ny);
     __syncthreads();
 }
 
@@ -583,7 +584,7 @@ k_dp_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __re
 {
     if (c->done) return;
     __shared__ double cm[7];
-    dp_corner_means(r, i, nx, ny, cm);
+    dp_corner_means(c, r, i, nx, ny, cm);
     const double h = c->h;
     const size_t n = (size_t)nx * ny;
     if constexpr (sizeof(T) == 8) {
@@ -611,7 +612,7 @@ __global__ void __launch_bounds__(NT) k_dp_err(Dom d, DPRaw<T> r, double atol, d
     Ctl* c = d.ctl;
     if (c->done) return;
     __shared__ double cm[7];
-    dp_corner_means(r, 7, d.nx, d.ny, cm);
+    dp_corner_means(c, r, 7, d.nx, d.ny, cm);
     const double h = c->h;
     double v[2] = {0.0, 0.0};
     const bool mx[2] = {true, true};
@@ -666,7 +667,7 @@ __device__ __forceinline__ void ts_commit_body(Dom d, const T* __restrict__ raw,
         // dt (sum_s b_s) k by an FP32 two-sum (no FP64 work per cell)
         const double dt = c->h;
         const float cx = (float)(((dt * c_ts_b[0] + dt * c_ts_b[3]) + dt * c_ts_b[4]) + dt * c_ts_b[5]);
-        const float cmf = (float)block_corner_mean(raw, d.nx, d.ny), spyf = (float)d.spy;
+        const float cmf = c->plain ? 0.f : (float)block_corner_mean(raw, d.nx, d.ny), spyf = (float)d.spy;
         for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
             const double x2 = d.ts_x2[e];
             d.x[e] = x2;
@@ -706,7 +707,7 @@ __global__ void __launch_bounds__(NT) k_upd_end(Dom d, const T* __restrict__ raw
     __shared__ double s_c[2];
     if (threadIdx.x == 0) {
         s_c[0] = corner_mean_of(d.w, d.nx, d.ny);
-        s_c[1] = have_rhs ? corner_mean_of(raw_last, d.nx, d.ny) : 0.0;
+        s_c[1] = (have_rhs && !d.ctl->plain) ? corner_mean_of(raw_last, d.nx, d.ny) : 0.0;
     }
     __syncthreads();
     const double cw = s_c[0], cr = s_c[1];
@@ -799,6 +800,76 @@ static int grid_for(size_t n)
     if (b < 1) b = 1;
     return (int)b;
 }
+
+// ---- LLRA / LV-ELRA (methods 0-2) ---------------------------------------
+// Equilibrium displacement (src/lv_xlra.f90:30-39, src/fastisostasy.f90:
+// 685-715) and relaxation rate (w_eq - w) / tau (src/lv_xlra.f90:17-27).
+__global__ void __launch_bounds__(NT) k_weq_local(double* __restrict__ weq, const double* __restrict__ c_load,
+                                                  double rho_m, int zero, size_t n)
+{
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
+        weq[e] = zero ? 0.0 : -c_load[e] / rho_m;
+}
+
+// the LV-ELRA load -canom_load g K^2 for the convolution with GV
+template <typename T>
+__global__ void __launch_bounds__(NT) k_elra_load(T* __restrict__ in, const double* __restrict__ c_load,
+                                                  const double* __restrict__ K2, double g, size_t n)
+{
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
+        in[e] = (T)((-c_load[e] * g) * K2[e]);
+}
+
+// w_eq = (conv - mean of the padded buffer's corners), then the domain's own
+// corner BC (apply_zerobc_at_corners on w_equilibrium)
+__global__ void __launch_bounds__(NT) k_weq_elra(double* __restrict__ weq, const double* __restrict__ raw,
+                                                 const double* __restrict__ corners, int nx, int ny)
+{
+    __shared__ double s_c[2];
+    if (threadIdx.x == 0) {
+        const double c1 = corner_mean(corners[0], corners[1], corners[2], corners[3]);
+        const size_t last = (size_t)(ny - 1) * nx;
+        s_c[0] = c1;
+        s_c[1] = corner_mean(raw[0] - c1, raw[last + nx - 1] - c1, raw[last] - c1, raw[nx - 1] - c1);
+    }
+    __syncthreads();
+    const double c1 = s_c[0], c2 = s_c[1];
+    const size_t n = (size_t)nx * ny;
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
+        weq[e] = (raw[e] - c1) - c2;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_relax_rate(T* __restrict__ out, const double* __restrict__ y,
+                                                   const double* __restrict__ weq, double tau, size_t n,
+                                                   const int* __restrict__ gate)
+{
+    if (gate && *gate == 0) return;
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
+        out[e] = (T)((weq[e] - y[e]) / tau);
+}
+
+void weq_local(double* weq, const double* c_load, double rho_m, int zero, size_t n, cudaStream_t s)
+{
+    k_weq_local<<<grid_for(n), NT, 0, s>>>(weq, c_load, rho_m, zero, n);
+}
+template <typename T> void elra_load(T* in, const double* c_load, const double* K2, double g, size_t n, cudaStream_t s)
+{
+    k_elra_load<T><<<grid_for(n), NT, 0, s>>>(in, c_load, K2, g, n);
+}
+void weq_elra(double* weq, const double* raw, const double* corners, int nx, int ny, cudaStream_t s)
+{
+    k_weq_elra<<<grid_for((size_t)nx * ny), NT, 0, s>>>(weq, raw, corners, nx, ny);
+}
+template <typename T>
+void relax_rate(T* out, const double* y, const double* weq, double tau, size_t n, const int* gate, cudaStream_t s)
+{
+    k_relax_rate<T><<<grid_for(n), NT, 0, s>>>(out, y, weq, tau, n, gate);
+}
+template void elra_load<float>(float*, const double*, const double*, double, size_t, cudaStream_t);
+template void elra_load<double>(double*, const double*, const double*, double, size_t, cudaStream_t);
+template void relax_rate<float>(float*, const double*, const double*, double, size_t, const int*, cudaStream_t);
+template void relax_rate<double>(double*, const double*, const double*, double, size_t, const int*, cudaStream_t);
 
 int reduce_grid(size_t n) { return grid_for(n); }
 

@@ -79,6 +79,12 @@ void state_diag(double* z_ss, const double* zss_base, const double* dz_ss, doubl
                 const double* Hice, double* Haf, uint8_t* mo, uint8_t* mg, uint8_t* mc, size_t n,
                 double rho_sw_over_ice, cudaStream_t s);
 template <typename T> void rhs_finish(double* out, const T* raw, int nx, int ny, double spy, cudaStream_t s);
+// LLRA / LV-ELRA (methods 0-2): equilibrium displacement and relaxation rate
+void weq_local(double* weq, const double* c_load, double rho_m, int zero, size_t n, cudaStream_t s);
+template <typename T> void elra_load(T* in, const double* c_load, const double* K2, double g, size_t n, cudaStream_t s);
+void weq_elra(double* weq, const double* raw, const double* corners, int nx, int ny, cudaStream_t s);
+template <typename T>
+void relax_rate(T* out, const double* y, const double* weq, double tau, size_t n, const int* gate, cudaStream_t s);
 void sub_corner(double* out, const double* raw, const double* corners, size_t n, cudaStream_t s);
 template <typename T> void cast_from_double(T* dst, const double* src, size_t n, cudaStream_t s);
 template <typename T> void q0_from_cf(T* q0, const double* cf, const uint8_t* mask, double g, size_t n, cudaStream_t s);

@@ -29,6 +29,7 @@ DEFAULTS = dict(
     E=66.0, nu=0.28, rho_water=1000.0, rho_ice=910.0, rho_seawater=1028.0,
     rho_uppermantle=3400.0, rho_litho=0.0, g=9.81, r_earth=6.378e6, m_earth=5.972e24,
     atol=1e-2, rtol=1e-4, dt_min=1e-10, dt_max=10.0, dt_init=1.0, q=1.0,
+    tau=3000.0,
 )
 
 _CODES = {"lithosphere": LITHOSPHERE, "mantle": MANTLE, "layering": LAYERING, "lumping": LUMPING,

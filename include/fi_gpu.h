@@ -1,7 +1,8 @@
 /*
  * fi_gpu.h — C ABI of the GB300 LV-ELVA library (libfigpu.so).
  *
- * Drop-in boundary for FastIsostasy's LV-ELVA path (method = 3).  Each entry
+ * Drop-in boundary for FastIsostasy's time stepping: LV-ELVA (method 3),
+ * and LLRA / LV-ELRA (methods 0-2) on the same update path.  Each entry
  * point replaces one reference routine of module `fastisostasy`
  * (src/fastisostasy.f90) or `barysealevel` (src/barysealevel.f90); the
  * Fortran caller keeps its isos_class / bsl_class and binds these functions
@@ -52,7 +53,7 @@ enum { FI_PREC_FP64 = 0, FI_PREC_MIXED = 1 };
  * unit conversion (src/fastisostasy.f90:925-1015): lengths in m, E in GPa.
  * String options are integer codes. */
 typedef struct {
-    int32_t method;                 /* must be 3 (LV-ELVA) */
+    int32_t method;                 /* 0 none, 1 LLRA, 2 LV-ELRA, 3 LV-ELVA */
     int32_t interactive_sealevel;
     int32_t include_elastic;
     int32_t heterogeneous_ssh;
@@ -72,6 +73,7 @@ typedef struct {
     double E, nu, rho_water, rho_ice, rho_seawater, rho_uppermantle, rho_litho, g;
     double r_earth, m_earth;
     double atol, rtol, dt_min, dt_max, dt_init, q;
+    double tau;                     /* [yr] asthenosphere relaxation time (methods 0-2) */
 } fi_params;
 
 /* bsl_class (src/barysealevel.f90:16-29); series arrays are caller-owned

@@ -14,6 +14,7 @@
 #include "fi_oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -556,6 +557,7 @@ struct orc_model {
     int ref_was_set;
     double *xc, *yc, *K, *dxm, *dym, *A, *kappa, *R, *D, *He, *eta_eff, *GE, *GN;
     double *FGEr, *FGEi, *FGNr, *FGNi;
+    double *FGVr, *FGVi, *GV, L_w;   /* LV-ELRA (method 2) viscous kernel */
     uint8_t *maskactive;
     ostate now, ref;
     /* ode_class */
@@ -633,6 +635,69 @@ static void gaussian_viscosity(double *eta, int nx, int ny, double eta0, double 
 }
 
 /* calc_heterogeneous_rigidity, src/isos_utils.f90:79-100 */
+/* ---- Kelvin function kei for LV-ELRA (src/kelvin_function.f90) ----
+ * The reference interpolates a 1001-entry table of kei(x), x = 0 .. 10 in
+ * steps of 0.01, printed with five significant digits and written as
+ * default-real literals (load_kei_values, :166-1233).  The table is rebuilt
+ * here from the function itself: kei(x) = Im K_0(x e^{i pi/4}) (A&S 9.9.2)
+ * with K_0(z) = int_0^inf exp(-z cosh t) dt, i.e.
+ *   kei(x) = -int_0^inf exp(-a) sin(a) dt,  a = x cosh(t) / sqrt(2),
+ * by the trapezoid rule (even, analytic integrand: geometric convergence),
+ * then rounded to five significant digits and to single precision. */
+static double kelvin_kei(double x)
+{
+    const double h = 1.0 / 64.0, r2 = sqrt(2.0);
+    double s = 0.0;
+    int k;
+    if (x <= 0.0) return -0.78539816339744830962;   /* -pi/4 */
+    for (k = 0;; k++) {
+        const double a = x * cosh(k * h) / r2;
+        if (a > 60.0) break;
+        s += (k == 0 ? 0.5 : 1.0) * exp(-a) * sin(a);
+    }
+    return -h * s;
+}
+
+#define KEI_N 1001
+static double g_kei_rn[KEI_N], g_kei_v[KEI_N];
+static int g_kei_ready = 0;
+
+static void kei_table(void)
+{
+    char buf[64];
+    int i;
+    if (g_kei_ready) return;
+    for (i = 0; i < KEI_N; i++) {
+        const double x = i / 100.0;
+        snprintf(buf, sizeof(buf), "%.4f", x);
+        g_kei_rn[i] = (double)strtof(buf, NULL);
+        snprintf(buf, sizeof(buf), "%.4E", kelvin_kei(x));
+        g_kei_v[i] = (double)strtof(buf, NULL);
+    }
+    g_kei_ready = 1;
+}
+
+void orc_kei_table(double *rn, double *kv)
+{
+    kei_table();
+    memcpy(rn, g_kei_rn, sizeof(g_kei_rn));
+    memcpy(kv, g_kei_v, sizeof(g_kei_v));
+}
+
+/* get_kei_value, src/kelvin_function.f90:91-132: linear interpolation in
+ * the table, the last value beyond its end */
+static double kei_value(double r, double L_w)
+{
+    const double rn = r / L_w;
+    int k;
+    if (rn > g_kei_rn[KEI_N - 1]) return g_kei_v[KEI_N - 1];
+    k = (int)(rn * 100.0);
+    if (k > KEI_N - 2) k = KEI_N - 2;
+    while (k > 0 && rn < g_kei_rn[k]) k--;
+    while (k < KEI_N - 2 && rn >= g_kei_rn[k + 1]) k++;
+    return g_kei_v[k] + (rn - g_kei_rn[k]) / (g_kei_rn[k + 1] - g_kei_rn[k]) * (g_kei_v[k + 1] - g_kei_v[k]);
+}
+
 static double rigidity(double E, double He, double nu)
 {
     return E * 1e9 * (He * He * He) / (12.0 * (1.0 - nu * nu));
@@ -644,7 +709,7 @@ orc_model *orc_create(const orc_params *p, int nx_ice, int ny_ice, double dx, do
     orc_model *m;
     int nx_tmp, ny_tmp, npx, npy, i, j, k;
     size_t n, e;
-    if (p->method != 3 || dx != dy || p->min_pad < 0.0 || p->nl < 1 || p->nl > 8) return NULL;
+    if (p->method < 0 || p->method > 3 || dx != dy || p->min_pad < 0.0 || p->nl < 1 || p->nl > 8) return NULL;
     m = (orc_model *)calloc(1, sizeof(orc_model));
     m->p = *p;
     /* init_domain_size, src/isos_utils.f90:285-354 */
@@ -704,8 +769,31 @@ orc_model *orc_create(const orc_params *p, int nx_ice, int ny_ice, double dx, do
             orc_kernel_spectrum(nx, ny, m->M, m->GE, m->FGEr, m->FGEi);
             orc_kernel_spectrum(nx, ny, m->M, m->GN, m->FGNr, m->FGNi);
         }
-        /* maskactive, :185-214 (mask files arrive through orc_set_fields) */
-        if (!p->interactive_sealevel) {
+        /* LV-ELRA, :216-236: Kelvin-function filter on the padded domain
+         * (calc_kei_filter_2D needs a square array), the viscous Green's
+         * function GV = -L_w^2 / (2 pi D) kei (dx dy) (src/green_functions.f90:28-41)
+         * with L_w = (D / (rho_m g))^(1/4) (src/isos_utils.f90:66-73) */
+        if (p->method == 2) {
+            const double Dc = rigidity(p->E, p->zl[0], p->nu);
+            const size_t hs = (size_t)m->M * (m->M / 2 + 1);
+            if (nx != ny) { orc_destroy(m); return NULL; }
+            kei_table();
+            m->L_w = pow(Dc / (p->rho_uppermantle * p->g), 0.25);
+            m->GV = dalloc(n);
+            for (j = 0; j < ny; j++)
+                for (i = 0; i < nx; i++) {
+                    const double x = m->xc[i], y = m->yc[j];
+                    const double kei = kei_value(sqrt(x * x + y * y), m->L_w);
+                    m->GV[IX(i, j)] = -(m->L_w * m->L_w) / (2.0 * PI_LIT * Dc) * kei * (dx * dx);
+                }
+            m->FGVr = dalloc(hs); m->FGVi = dalloc(hs);
+            orc_kernel_spectrum(nx, ny, m->M, m->GV, m->FGVr, m->FGVi);
+        }
+        /* maskactive, :185-214 (mask files arrive through orc_set_fields);
+         * methods 0-2 make every cell active (:444-451) */
+        if (p->method != 3) {
+            for (e = 0; e < n; e++) m->maskactive[e] = 1;
+        } else if (!p->interactive_sealevel) {
             for (e = 0; e < n; e++) m->maskactive[e] = 1;
         } else if (p->min_pad > SP(100.e3)) {
             for (j = m->jcrop1; j <= m->jcrop2; j++)
@@ -713,6 +801,7 @@ orc_model *orc_create(const orc_params *p, int nx_ice, int ny_ice, double dx, do
         }
         /* method 3, :240-443 */
         orc_kappa(m->kappa, nx, ny, m->dx, m->dy);
+        if (p->method == 3) {
         if (p->lithosphere == 1 || p->lithosphere == 2) {
             gaussian_thickness(m->He, nx, ny, p->zl[0], SP(100e3), p->lithosphere == 1 ? 1.0 : -1.0,
                                m->xc, m->yc);
@@ -781,6 +870,7 @@ orc_model *orc_create(const orc_params *p, int nx_ice, int ny_ice, double dx, do
         /* :438-442, including the exp(log10(.)) quirk */
         for (e = 0; e < n; e++) m->eta_eff[e] = m->eta_eff[e] * m->cc;
         for (e = 0; e < n; e++) m->eta_eff[e] = exp(log10(p->eta_ref / m->eta_eff[e])) * m->eta_eff[e];
+        }
     }
     m->time_diag = SP(1e10); m->time_prog = SP(1e10);
     state_alloc(&m->now, n); state_alloc(&m->ref, n);
@@ -799,6 +889,7 @@ void orc_destroy(orc_model *m)
     free(m->xc); free(m->yc); free(m->K); free(m->dxm); free(m->dym); free(m->A); free(m->kappa);
     free(m->R); free(m->D); free(m->He); free(m->eta_eff); free(m->GE); free(m->GN);
     free(m->FGEr); free(m->FGEi); free(m->FGNr); free(m->FGNi); free(m->maskactive);
+    free(m->FGVr); free(m->FGVi); free(m->GV);
     state_free(&m->now); state_free(&m->ref);
     free(m->x); free(m->y); free(m->x1); free(m->x2);
     for (k = 0; k < 7; k++) free(m->k[k]);
@@ -944,11 +1035,44 @@ static void sl_contributions(orc_model *m, size_t n)
 }
 
 /* ---- RHS: get_dwdt, src/fastisostasy.f90:677-729 ---- */
+/* get_dwdt for methods 0-2 (src/fastisostasy.f90:685-715): the equilibrium
+ * displacement of LLRA (-canom_load / rho_m, src/lv_xlra.f90:30-39) or of
+ * LV-ELRA (the load -canom_load g K^2 convolved with GV, corner BC), and the
+ * relaxation (w_eq - w) / tau (src/lv_xlra.f90:17-27).  The reference
+ * passes now%w; the true-stage mode passes the stage state. */
+static void rhs_relax(orc_model *m, const double *state, double *dwdt)
+{
+    const size_t n = (size_t)m->nx * m->ny;
+    double *weq = m->now.w_eq;
+    size_t e;
+    if (m->p.method == 0) {
+        for (e = 0; e < n; e++) { weq[e] = 0.0; dwdt[e] = 0.0; }
+    } else {
+        if (m->p.method == 1) {
+            for (e = 0; e < n; e++) weq[e] = -m->now.c_load[e] / m->p.rho_uppermantle;
+        } else {
+            double *in = dalloc(n);
+            for (e = 0; e < n; e++) in[e] = (-m->now.c_load[e] * m->p.g) * (m->K[e] * m->K[e]);
+            orc_conv(weq, m->nx, m->ny, m->M, m->FGVr, m->FGVi, in);
+            free(in);
+            zerobc_corners(weq, m->nx, m->ny);
+        }
+        for (e = 0; e < n; e++) dwdt[e] = (weq[e] - state[e]) / m->p.tau;
+    }
+    if (dwdt != m->now.dwdt) memcpy(m->now.dwdt, dwdt, n * sizeof(double));
+    m->n_rhs++;
+}
+
 static void rhs_eval(orc_model *m, const double *state, double *dwdt)
 {
     const size_t n = (size_t)m->nx * m->ny;
-    double *cf = m->y == state ? dalloc(n) : m->y;   /* scratch for canom_full */
+    double *cf;
     size_t e;
+    if (m->p.method != 3) {
+        rhs_relax(m, m->p.stage_mode == 0 ? m->now.w : state, dwdt);
+        return;
+    }
+    cf = m->y == state ? dalloc(n) : m->y;   /* scratch for canom_full */
     if (m->p.stage_mode == 0) {
         /* reference: canom_full from the frozen anomalies, w = now%w */
         canom_full(m, n);

@@ -32,7 +32,7 @@ extern "C" {
 /* Parameters after isos_par_load's unit conversions
  * (src/fastisostasy.f90:925-1015): lengths in m, E in GPa. */
 typedef struct {
-    int32_t method;                 /* only 3 (LV-ELVA) */
+    int32_t method;                 /* 0 none, 1 LLRA, 2 LV-ELRA, 3 LV-ELVA */
     int32_t interactive_sealevel;
     int32_t include_elastic;
     int32_t heterogeneous_ssh;
@@ -52,6 +52,7 @@ typedef struct {
     double E, nu, rho_water, rho_ice, rho_seawater, rho_uppermantle, rho_litho, g;
     double r_earth, m_earth;
     double atol, rtol, dt_min, dt_max, dt_init, q;
+    double tau;                     /* [yr] asthenosphere relaxation time (methods 0-2) */
 } orc_params;
 
 typedef struct {
@@ -104,6 +105,9 @@ int  orc_get_field(const orc_model *m, int which, double *out);   /* padded grid
 int  orc_get_scalars(const orc_model *m, double *out16);
 void orc_rhs_now(orc_model *m, double *dwdt);   /* get_dwdt at the current state */
 void orc_set_threads(int n);
+
+/* The Kelvin-function table of LV-ELRA (1001 entries each). */
+void orc_kei_table(double *rn, double *kei);
 
 #ifdef __cplusplus
 }

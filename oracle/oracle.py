@@ -38,7 +38,7 @@ class OrcParams(C.Structure):
         ("rho_ice", C.c_double), ("rho_seawater", C.c_double), ("rho_uppermantle", C.c_double),
         ("rho_litho", C.c_double), ("g", C.c_double), ("r_earth", C.c_double),
         ("m_earth", C.c_double), ("atol", C.c_double), ("rtol", C.c_double),
-        ("dt_min", C.c_double), ("dt_max", C.c_double), ("dt_init", C.c_double), ("q", C.c_double),
+        ("dt_min", C.c_double), ("dt_max", C.c_double), ("dt_init", C.c_double), ("q", C.c_double), ("tau", C.c_double),
     ]
 
 

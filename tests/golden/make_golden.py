@@ -2,8 +2,9 @@
 
 1. params_<test>.json: the reference's experiment namelists
    (par/test_isostasy_<test>.nml of the reference project) parsed with
-   fastisostasy_gb300.params — needs the reference tree, so it only runs
-   where that tree is mounted (pass its path as argv[1]).
+   fastisostasy_gb300.params, and kei_reference.npz: the reference's
+   Kelvin-function table — both need the reference tree, so they are only
+   made where that tree is mounted (pass its path as argv[1]).
 2. oracle_golden.npz: outputs of the cases in tests/make_golden_cases.py.
 
 Usage: python tests/golden/make_golden.py [path/to/reference]
@@ -20,7 +21,22 @@ import numpy as np  # noqa: E402
 
 from fastisostasy_gb300 import params as P  # noqa: E402
 
-TESTS = ["test1d", "test1e", "test2a", "test2b", "test2c", "test3a", "test3b", "test3c", "test3d"]
+TESTS = ["test1a", "test1b", "test1c", "test1d", "test1e", "test2a", "test2b", "test2c", "test3a", "test3b",
+         "test3c", "test3d"]
+
+
+def kei_reference(ref):
+    """The reference's tabulated Kelvin function kei (load_kei_values in
+    src/kelvin_function.f90), read from its source: 1001 (x, kei) pairs
+    written as default-real literals, hence rounded to single precision."""
+    import re
+    with open(os.path.join(ref, "src", "kelvin_function.f90")) as fh:
+        src = fh.read()
+    blk = src[src.index("tbl = ["):]
+    blk = blk[:blk.index("]")]
+    nums = [float(x) for x in re.findall(r"[-+]?\d+\.\d+(?:E[-+]\d+)?", blk)]
+    t = np.array(nums, dtype=np.float32).astype(np.float64).reshape(-1, 2)
+    return t[:, 0], t[:, 1]
 
 
 def main():
@@ -31,6 +47,8 @@ def main():
             p = P.load(path)
             with open(os.path.join(HERE, "params_%s.json" % t), "w") as fh:
                 json.dump(p, fh, indent=1, sort_keys=True)
+        rn, kei = kei_reference(ref)
+        np.savez_compressed(os.path.join(HERE, "kei_reference.npz"), rn=rn, kei=kei)
     import make_golden_cases as MG
     out = {}
     for name, fn in MG.CASES.items():

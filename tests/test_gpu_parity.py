@@ -118,6 +118,28 @@ def test_reference_experiments_tsit54(name, over):
     pair.close()
 
 
+@pytest.mark.parametrize("name", ["test1a", "test1b", "test1c"])
+@pytest.mark.parametrize("dt_method", [2, 1, 0])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_relaxation_methods(name, dt_method, precision):
+    """The reference's experiments test1a (method 0, no displacement), test1b
+    (LLRA) and test1c (LV-ELRA: load convolved with the Kelvin-function
+    Green's function, then relaxation over tau) with each integrator, in the
+    reference's integrator semantics."""
+    pair = Pair(ref_disc(name, dt_method=dt_method), precision=precision)
+    pair.init()
+    pair.step(12)
+    if precision == 0:
+        compare(pair, TOL64)
+    else:
+        w_o, w_g = pair.orc.field("w"), pair.dom.field("w")
+        if np.abs(w_o).max() > 0:
+            assert rel(w_g, w_o) <= TOLMIX
+        else:
+            assert np.abs(w_g).max() == 0
+    pair.close()
+
+
 @pytest.mark.parametrize("name,over", [("test1d", {}), ("test2c", {"lithosphere": 2}), ("test3c", {})])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_true_stage_tsit54(name, over, precision):

@@ -1,5 +1,6 @@
 """CPU tests: the oracle against transform definitions, an independent numpy
 restatement, the analytical ELVA disk and the committed golden vectors."""
+import ctypes as C
 import json
 import os
 
@@ -111,3 +112,51 @@ def test_golden_vectors():
             ref = g[key]
             scale = max(np.abs(ref).max(), 1e-300)
             assert np.abs(v - ref).max() <= 1e-12 * scale, key
+
+
+def test_kei_table_matches_reference_table():
+    """The Kelvin-function table of LV-ELRA, rebuilt from kei itself, equals
+    the reference's tabulated values (src/kelvin_function.f90, read into
+    tests/golden/kei_reference.npz by tests/golden/make_golden.py) bit for
+    bit after the same rounding."""
+    ref = np.load(os.path.join(GOLDEN, "kei_reference.npz"))
+    rn, kv = np.zeros(1001), np.zeros(1001)
+    dp = C.POINTER(C.c_double)
+    O.lib().orc_kei_table(rn.ctypes.data_as(dp), kv.ctypes.data_as(dp))
+    assert np.array_equal(rn, ref["rn"]) and np.array_equal(kv, ref["kei"])
+
+
+def _relax_run(name, T, dt_save=None, n=41, dx=100e3):
+    with open(os.path.join(GOLDEN, "params_%s.json" % name)) as fh:
+        p = json.load(fh)
+    xc = -(n // 2) * dx + dx * np.arange(n)
+    H = np.where(xc[None, :] ** 2 + xc[:, None] ** 2 <= 1000e3 ** 2, 1000.0, 0.0)
+    m = O.Model(p, n, n, dx, dx)
+    b = O.make_bsl()
+    m.init_state(np.full((n, n), 1e6), np.zeros_like(H), 0.0, b)
+    for k in range(1, int(T / 10) + 1):
+        assert m.update(H, k * 10.0, b) == 0
+    w = m.crop(m.field("w"))
+    load = m.crop(m.field("canom_load"))
+    m.close()
+    return p, w, load
+
+
+def test_llra_relaxes_exponentially():
+    """LLRA (test1b): w = w_eq (1 - exp(-t / tau)) with w_eq = -canom_load / rho_m
+    under a load switched on at t = 0 (the corner BC subtracts the corner
+    mean, which is zero far from the disc)."""
+    p, w, load = _relax_run("test1b", 3000.0)
+    weq = -load / p["rho_uppermantle"]
+    ana = weq * (1.0 - np.exp(-3000.0 / p["tau"]))
+    assert np.abs(w - ana).max() <= 5e-3 * np.abs(weq).max()
+
+
+def test_elra_equilibrium_matches_local_under_a_broad_load():
+    """LV-ELRA (test1c): under a disc much wider than the flexural length the
+    relaxed deflection at the disc centre approaches the local (LLRA)
+    equilibrium -rho_i H / rho_m."""
+    p, w, load = _relax_run("test1c", 30000.0)
+    weq_local = -load / p["rho_uppermantle"]
+    c = w.shape[0] // 2
+    assert abs(w[c, c] - weq_local[c, c]) <= 0.05 * abs(weq_local[c, c])
