@@ -246,6 +246,13 @@ int fi_batch_step(fi_batch* b, double time, fi_bsl* bsl);
 int fi_batch_wait(fi_batch* b, int32_t* status);
 int fi_batch_destroy(fi_batch* b);
 
+/* The analytical ELVA disc (Bueler et al. 2007, eq. 17) as the reference's
+ * disc benchmark writes it (isosbench_elva_disk,
+ * src/isostasy_benchmarks.f90:74-280), evaluated on the device: a fast
+ * validator for runs of the disc experiments.  out is (nx, ny) on the host. */
+int fi_elva_disk(int nx, int ny, double dx, double r0, double h0, double eta, double D, double rho_ice,
+                 double rho_m, double g, double time_yr, double* out);
+
 /* Restart support: the complete device state (fields + integrator clock) as
  * doubles; bit-identical round trip. */
 size_t fi_state_size(const fi_handle* h);

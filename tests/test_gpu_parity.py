@@ -286,3 +286,34 @@ def test_step_engine_matches_kernel_sequence(precision, n, monkeypatch):
             compare(p, TOL64)
         p.close()
     assert rel(res[1], res[0]) <= (1e-12 if precision == 0 else 1e-6)
+
+
+def test_device_analytical_disk():
+    """fi_elva_disk (the analytical ELVA disc evaluated on the device) against
+    the oracle's evaluation of the same integral, then used as the validator
+    of a GPU run of the reference's disc experiment test1d."""
+    from oracle import analytical as A
+    import ctypes as C
+    L = _lib.load()
+    n, dx, T = 61, 100e3, 3000.0
+    p = params("test1d")
+    D = p["E"] * 1e9 * p["zl"][0] ** 3 / (12.0 * (1.0 - p["nu"] ** 2))
+    got = np.zeros((n, n))
+    rc = L.fi_elva_disk(n, n, dx, 1000e3, 1000.0, 1e21, D, 910.0, 3400.0, 9.81, T,
+                        got.ctypes.data_as(C.POINTER(C.c_double)))
+    assert rc == 0
+    ana = A.elva_disk(n, n, dx, 1000e3, 1000.0, 1e21, D, 910.0, 3400.0, 9.81, T)
+    assert rel(got, ana) <= 1e-9
+    # the GPU solution of test1d against it (the oracle's own physics check)
+    xc = -3000e3 + dx * np.arange(n)
+    H = np.where(xc[None, :] ** 2 + xc[:, None] ** 2 <= 1000e3 ** 2, 1000.0, 0.0)
+    dom = Domain(p, n, n, dx)
+    b = gpu_bsl()
+    dom.init_state(np.full((n, n), 1e6), np.zeros_like(H), 0.0, b)
+    out = {"z_bed": np.zeros((n, n))}
+    for k in range(1, int(T / 10) + 2):
+        t = (k - 1) * 10.0
+        dom.update(H if t > 0 else np.zeros_like(H), t, b, out=out)
+    dom.close()
+    zb = out["z_bed"] - 1e6
+    assert abs(zb.min() - got.min()) <= 0.03 * abs(got.min())
