@@ -16,6 +16,7 @@
 
 #include "../../include/fi_gpu.h"
 #include "fi_engine.h"
+#include "fi_init.h"
 #include "fi_kernels.h"
 #include "fi_batch.h"
 #include "fi_state.h"
@@ -58,8 +59,9 @@ int nice_even_at_least(int m)
     return v;
 }
 
-// get_ge_value (src/green_functions.f90:131-168) with the 42-entry table
-// (:56-66); the radii are multiplied by 1.e3 in single precision.
+// The 42-entry table of get_ge_value (src/green_functions.f90:56-66,
+// 131-168), interpolated on the device; the radii are multiplied by 1.e3 in
+// single precision there.
 const float kRn[42] = {0.0f, 0.011f, 0.111f, 1.112f, 2.224f, 3.336f, 4.448f, 6.672f, 8.896f, 11.12f, 17.79f,
                        22.24f, 27.80f, 33.36f, 44.48f, 55.60f, 66.72f, 88.96f, 111.2f, 133.4f, 177.9f, 222.4f,
                        278.0f, 333.6f, 444.8f, 556.0f, 667.2f, 778.4f, 889.6f, 1001.0f, 1112.0f, 1334.0f,
@@ -70,26 +72,6 @@ const float kGe[42] = {-33.6488f, -33.64f, -33.56f, -32.75f, -31.86f, -30.98f, -
                        -3.798f, -3.640f, -3.392f, -2.999f, -2.619f, -2.103f, -1.530f, -0.292f, 0.848f, 1.676f,
                        2.083f, 2.057f, 1.643f};
 
-double ge_value(double r)
-{
-    struct Tab {
-        double rn[42], ge[42];
-        Tab()
-        {
-            for (int k = 0; k < 42; ++k) { rn[k] = (double)(kRn[k] * 1.e3f); ge[k] = (double)kGe[k]; }
-        }
-    };
-    static const Tab tab;   // initialised once, thread-safe
-    const double* rn = tab.rn;
-    const double* ge = tab.ge;
-    if (r > rn[41]) return 0.0;
-    int k = 0;
-    while (k < 41 && !(r >= rn[k] && r < rn[k + 1])) ++k;
-    if (k > 40) k = 40;
-    return ge[k] + (r - rn[k]) / (rn[k + 1] - rn[k]) * (ge[k + 1] - ge[k]);
-}
-
-inline int midindex(int n) { return (n % 2 == 0) ? n / 2 : (n - 1) / 2; }
 
 }  // namespace
 
@@ -98,6 +80,7 @@ struct fi_handle {
     int nx, ny, nx_ice, ny_ice, icrop1, icrop2, jcrop1, jcrop2;
     size_t n;
     double dx, dy, spy, cc, Vden;
+    int init_rc = 0;                   // device init of kappa, GE, GN
     double rate_scale = 1.0;           // stage outputs -> rates: sec/yr (method 3) or 1 (methods 0-2)
     double L_w = 0.0;                  // flexural length scale (LV-ELRA)
     double time_diag, time_prog;
@@ -326,23 +309,6 @@ int make_plan(fi_handle* h, int nx, int ny, Plan2D& P)
 }
 
 // ---- init-time physics (host, double) ---------------------------------------
-// calc_kappa, src/lv_elva.f90:442-481
-void host_kappa(fi_handle* h)
-{
-    const int nx = h->nx, ny = h->ny;
-    const double mu_x = 2.0 * PI_LIT / ((nx - 1) * h->dx), mu_y = 2.0 * PI_LIT / ((ny - 1) * h->dy);
-    const int ic = (nx - 1) / 2 + 1, jc = (ny - 1) / 2 + 1;
-    h->kappa.assign(h->n, 0.0);
-    for (int i = 1; i <= nx; ++i) {
-        const double pp = (i <= ic) ? mu_x * (i - 1) : mu_x * (nx - i + 1);
-        for (int j = 1; j <= ny; ++j) {
-            const double q = (j <= jc) ? mu_y * (j - 1) : mu_y * (ny - j + 1);
-            h->kappa[(size_t)(j - 1) * nx + (i - 1)] = std::pow(pp * pp + q * q, 0.5);
-        }
-    }
-    h->kappa[0] = (h->kappa[nx] + h->kappa[1]) / 2.0;
-}
-
 double rigidity(double E, double He, double nu) { return E * 1e9 * (He * He * He) / (12.0 * (1.0 - nu * nu)); }
 
 // Gaussian bump over the padded domain as in calc_gaussian_thickness /
@@ -423,7 +389,13 @@ void host_fields(fi_handle* h)
     h->D.assign(n, rigidity(p.E, p.zl[0], p.nu));
     h->R.assign(n, 1.0);
     h->eta_eff.assign(n, p.viscosities[p.nl - 1]);
-    host_kappa(h);
+    // kappa, GE and GN cell by cell on the device (host loops as the fallback
+    // for a failed launch are not kept: a device error is reported)
+    h->kappa.assign(n, 0.0);
+    h->GE.assign(n, 0.0);
+    h->GN.assign(n, 0.0);
+    h->init_rc = init_fields_device(h->nx, h->ny, h->dx, h->dy, PI_LIT, sp(1.e-12), sp(9.81), p.r_earth, p.m_earth,
+                                    kRn, kGe, h->kappa.data(), h->GE.data(), h->GN.data(), h->s);
     if (p.method == 3 && (p.lithosphere == 1 || p.lithosphere == 2)) {
         std::vector<double> g;
         gauss_bump(h, h->xc, h->yc, g);
@@ -445,7 +417,8 @@ void host_fields(fi_handle* h)
         for (int k = 1; k < nl; ++k)
             for (size_t e = 0; e < n; ++e)
                 bnd[(size_t)k * n + e] = (p.layering == 1) ? bnd[(size_t)(k - 1) * n + e] + p.dl : p.zl[k];
-        for (size_t e = 0; e < n; ++e) {
+        {
+            // the layer viscosities are the same in every cell: lump once
             double mn = p.viscosities[0], mxv = p.viscosities[0], s = 0.0, ls = 0.0;
             for (int k = 0; k < nl; ++k) {
                 const double v = p.viscosities[k];
@@ -462,7 +435,7 @@ void host_fields(fi_handle* h)
             case 4: v = std::pow(10.0, ls / (double)nl); break;
             default: break;
             }
-            h->eta_eff[e] = v;
+            h->eta_eff.assign(n, v);
         }
         if (p.lumping == 5 && nl > 1) {
             for (int k = nl - 1; k >= 1; --k)
@@ -491,20 +464,21 @@ void host_fields(fi_handle* h)
         for (double& e : h->eta_eff) e = e * p.viscosity_scaling;
     }
     for (double& e : h->eta_eff) e = e * h->cc;
-    for (double& e : h->eta_eff) e = std::exp(std::log10(p.eta_ref / e)) * e;   // :441-442
-    // Green's functions, src/green_functions.f90:43-128 (called with dy = dx)
-    const int nx = h->nx, ny = h->ny, mx = midindex(nx);
-    const double dx = h->dx;
-    h->GE.assign(n, 0.0);
-    h->GN.assign(n, 0.0);
-    for (int j = 1; j <= ny; ++j)
-        for (int i = 1; i <= nx; ++i) {
-            const double x = (i - 1 - mx) * dx, y = (j - 1 - mx) * dx;
-            const double r = std::sqrt(x * x + y * y);
-            h->GE[(size_t)(j - 1) * nx + (i - 1)] = ge_value(r) * sp(1.e-12) * (dx * dx) / (sp(9.81) * (r > dx ? r : dx));
-            const double rr = (dx / 2 > r) ? dx / 2 : r;
-            h->GN[(size_t)(j - 1) * nx + (i - 1)] = p.r_earth / (2. * p.m_earth * std::sin(rr / (2. * p.r_earth)));
+    {
+        // :441-442, evaluated once per run of equal values (uniform fields are common)
+        double last_in = 0.0, last_out = 0.0;
+        bool have = false;
+        for (double& e : h->eta_eff) {
+            if (!have || e != last_in) {
+                last_in = e;
+                last_out = std::exp(std::log10(p.eta_ref / e)) * e;
+                have = true;
+            }
+            e = last_out;
         }
+    }
+    const int nx = h->nx, ny = h->ny;
+    const double dx = h->dx;
     // LV-ELRA kernel, src/fastisostasy.f90:216-236: kei filter on the padded
     // domain, GV = -L_w^2 / (2 pi D) kei (dx dy) (src/green_functions.f90:28-41),
     // L_w = (D / (rho_m g))^(1/4) (src/isos_utils.f90:66-73)
@@ -571,12 +545,7 @@ int kernel_spectrum(fi_handle* h, const std::vector<double>& ker, int which)
     launch_cols_fwd<double>(S64, h->ny, h->pconv, h->s);
     CK(cudaGetLastError());
     if (mixed(h)) {
-        std::vector<double2> a(hs);
-        std::vector<float2> b(hs);
-        CK(cudaMemcpyAsync(a.data(), S64, hs * sizeof(double2), cudaMemcpyDeviceToHost, h->s));
-        CK(cudaStreamSynchronize(h->s));
-        for (size_t e = 0; e < hs; ++e) b[e] = make_float2((float)a[e].x, (float)a[e].y);
-        if ((rc = upload(h, h->KS[which], b.data(), hs * sizeof(float2)))) return rc;
+        if (narrow_spectrum(S64, (float2*)h->KS[which], hs, h->s)) return fail(h, FI_E_CUDA, "spectrum narrowing");
     } else {
         CK(cudaMemcpyAsync(h->KS[which], S64, hs * sizeof(double2), cudaMemcpyDeviceToDevice, h->s));
     }
@@ -1146,6 +1115,7 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     if (const char* ev = getenv("FI_REQUIRE_TSIT_GRAPH")) h->require_tsit_graph = (ev[0] == '1');
     *out = h;
     host_fields(h);
+    if (h->init_rc) return fail(h, FI_E_CUDA, "device init of kappa and the Green's functions failed");
 
     // ---- device buffers
     const size_t n = h->n;

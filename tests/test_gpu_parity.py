@@ -71,9 +71,11 @@ def test_convolution(n, precision):
         ref = O.conv(O.kernel_spectrum(G, M), x, M)
         got = dom.convolve(k, x)
         assert rel(got, ref) <= (TOL64 if precision == 0 else TOLMIX), (k, rel(got, ref))
-    # the product's Green's functions equal the oracle's restatement
+    # the product's Green's functions equal the oracle's restatement: GE bit
+    # for bit (table interpolation, unfused products), GN to the last place
+    # of the device sine
     assert np.array_equal(dom.field("GE"), O.elastic_green(n, n, dx))
-    assert np.array_equal(dom.field("GN"), O.zss_green(n, n, p["m_earth"], p["r_earth"], dx))
+    assert rel(dom.field("GN"), O.zss_green(n, n, p["m_earth"], p["r_earth"], dx)) <= 4e-16
     dom.close()
 
 
