@@ -20,6 +20,7 @@
 #include <cooperative_groups.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 #include <type_traits>
 
@@ -357,7 +358,7 @@ __device__ __forceinline__ unsigned long long gtimer()
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_engine_rk4(EngineArgs g)
+__global__ void __launch_bounds__(512, 2) k_engine_rk4(EngineArgs g)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     cg::grid_group grid = cg::this_grid();
@@ -467,13 +468,33 @@ void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s)
     k_split<<<b, 256, 0, s>>>(x, hi, lo, n);
 }
 
+// threads per engine block: 512 (two blocks, 1024 threads per SM at 64
+// registers); FI_ENGINE_THREADS=256 for tuning
+int engine_threads()
+{
+    static int t = [] {
+        if (const char* ev = getenv("FI_ENGINE_THREADS")) {
+            const int v = atoi(ev);
+            if (v == 256 || v == 512) return v;
+        }
+        return 512;
+    }();
+    return t;
+}
+
 template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem)
 {
     // The plain FP64 form is FP64-throughput bound; it runs faster as the
     // multi-kernel graph (full occupancy) than in the one-grid engine.
     if (sizeof(T) == 8) return 0;
-    typedef typename vec2<T>::type C2;
-    int cb = (int)(16 / sizeof(C2));
+    // one spectrum column per phase-B item: twice the items of two, so all
+    // resident blocks share phase B (measured faster at 512^2 than 16-byte rows)
+    int cb = 1;
+    // FI_ENGINE_CB: spectrum columns per phase-B item (tuning)
+    if (const char* ev = getenv("FI_ENGINE_CB")) {
+        const int v = atoi(ev);
+        if (v >= 1 && v <= 8) cb = v;
+    }
     if (cb < 1) cb = 1;
     *CB = cb;
     *smem = engine_smem_bytes<T>(p, cb);
@@ -497,9 +518,14 @@ template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, siz
         }
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T>, 256, *smem) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T>, engine_threads(), *smem) != cudaSuccess || per_sm < 1)
         return 0;
-    if (per_sm > 2) per_sm = 2;
+    int cap = 2;   // FI_ENGINE_PER_SM: resident blocks per SM, at most (tuning)
+    if (const char* ev = getenv("FI_ENGINE_PER_SM")) {
+        const int v = atoi(ev);
+        if (v >= 1 && v <= 8) cap = v;
+    }
+    if (per_sm > cap) per_sm = cap;
     // no more blocks than the largest phase has work items: a small domain
     // then leaves SMs free for other handles' work (serving, ensembles)
     const int na = (p.ny + RA - 1) / RA, nb = (p.h + 1 + cb - 1) / cb, nc = (p.ny + RC - 1) / RC;
@@ -513,7 +539,7 @@ template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, s
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(256);
+    cfg.blockDim = dim3(engine_threads());
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
