@@ -749,10 +749,16 @@ template <typename T> int integrate_tsit(fi_handle* h, double tf, int* have_rhs,
     while (hc.t < tf && hc.status == ST_OK) {
         PROF(h, K_CONTROL, step_begin(h->ctl, 2, h->s));
         if (need_rhs) { rhs<T>(h, h->d.w, nullptr, r0, nullptr, h->d.whi, h->d.wlo); *have_rhs = 1; }
-        PROF(h, K_TS, ts_max<T>(h->d, r0, p.atol, p.rtol, h->s));
-        PROF(h, K_TS, ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s));
-        PROF(h, K_TS, ts_commit<T>(h->d, r0, h->s));
-        h->launches += 4;
+        if (sizeof(T) == 4 && h->d.whi) {
+            PROF(h, K_TS, ts_fused(h->d, (const float*)r0, p.atol, p.rtol, p.q, p.dt_max, 100000, h->s));
+            PROF(h, K_TS, ts_commit_pair(h->d, (const float*)r0, h->s));
+            h->launches += 3;
+        } else {
+            PROF(h, K_TS, ts_max<T>(h->d, r0, p.atol, p.rtol, h->s));
+            PROF(h, K_TS, ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s));
+            PROF(h, K_TS, ts_commit<T>(h->d, r0, h->s));
+            h->launches += 4;
+        }
         CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
         CK(cudaStreamSynchronize(h->s));
         need_rhs = hc.accepted != 0;
@@ -798,9 +804,15 @@ template <typename T> int enqueue_tsit_loop(fi_handle* h)
     } else {
         ts_attempt_begin(h->ctl, kMaxAttempts, h->s);
         rhs<T>(h, h->d.w, nullptr, r0, &h->ctl->need_rhs, h->d.whi, h->d.wlo);
-        ts_max<T>(h->d, r0, p.atol, p.rtol, h->s);
-        ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s);
-        ts_commit<T>(h->d, r0, h->s);
+        if (sizeof(T) == 4 && h->d.whi) {
+            ts_fused(h->d, (const float*)r0, p.atol, p.rtol, p.q, p.dt_max, 100000, h->s);
+            ts_commit_pair(h->d, (const float*)r0, h->s);
+            h->launches -= 1;
+        } else {
+            ts_max<T>(h->d, r0, p.atol, p.rtol, h->s);
+            ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s);
+            ts_commit<T>(h->d, r0, h->s);
+        }
         ts_attempt_end(h->ctl, loop, h->s);
         h->launches += 5;
     }
@@ -1702,11 +1714,18 @@ template <typename T> void batch_attempt(fi_batch* b, cudaStream_t s, cudaGraphC
     batch_rows_fwd<T>(b->dM, off + (nm + 1), nm, b->grid[1], b->rows_threads, b->rows_smem, s);
     batch_cols_hartley<T>(b->dM, off + 2 * (nm + 1), nm, b->grid[2], b->cols_threads, b->cols_smem, s);
     batch_rows_inv<T>(b->dM, off + (nm + 1), nm, b->grid[1], b->rows_threads, b->rows_smem, s);
-    batch_ts_max<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], s);
-    batch_ts_err<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], 100000, s);
-    batch_ts_commit<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], s);
+    if (sizeof(T) == 4) {
+        // mixed members always carry now%w's float pair
+        batch_ts_fused(b->dM, off + 3 * (nm + 1), nm, b->grid[3], 100000, s);
+        batch_ts_commit_pair(b->dM, off + 3 * (nm + 1), nm, b->grid[3], s);
+        b->launches += 9;
+    } else {
+        batch_ts_max<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], s);
+        batch_ts_err<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], 100000, s);
+        batch_ts_commit<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], s);
+        b->launches += 10;
+    }
     batch_attempt_end(b->dM, nm, loop, s, more_out);
-    b->launches += 10;
 }
 
 // The same update without a graph: the host reads the loop condition after

@@ -75,6 +75,9 @@ template <typename T> void batch_ts_max(const BMember* M, const int* off, int nm
 template <typename T>
 void batch_ts_err(const BMember* M, const int* off, int nm, int nblk, int max_reject, cudaStream_t s);
 template <typename T> void batch_ts_commit(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s);
+// mixed form with the float pair of now%w: ts_fused / ts_commit_pair per member
+void batch_ts_fused(const BMember* M, const int* off, int nm, int nblk, int max_reject, cudaStream_t s);
+void batch_ts_commit_pair(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s);
 void batch_loop_begin(const BMember* M, int nm, cudaStream_t s);
 void batch_attempt_begin(const BMember* M, int nm, int max_iter, cudaStream_t s);
 // more_out == NULL: sets the WHILE condition `loop`; else writes it there

@@ -399,6 +399,25 @@ __device__ __forceinline__ void ts_x12(double x, double k, double dt, double& x1
     x2 = a + (dt * c_ts_b[5]) * k;
 }
 
+// Accept or reject an attempt from its error norm, adapt dt
+// (src/integrators.f90, tsit54 step control).
+__device__ __forceinline__ void ts_decide(Ctl* c, double err, double dt, double q, double dt_max, int max_reject)
+{
+    c->err = err;
+    c->n_attempt++;
+    if (err < 1) {
+        c->accepted = 1;
+        c->t = c->t + dt;
+        c->dt = fmin(dt * pow(1 / err, 1 / q), dt_max);
+        c->n_accept++;
+    } else {
+        c->accepted = 0;
+        c->dt = dt * 0.5;
+        c->n_reject++;
+        if (c->n_reject > max_reject) { c->status = ST_STEP; c->done = 1; }
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void ts_max_body(Dom d, const T* __restrict__ raw, double atol, double rtol, int bid, int nblk)
 {
@@ -472,28 +491,88 @@ __device__ __forceinline__ void ts_err_body(Dom d, const T* __restrict__ raw, do
         }
     }
     double tot[1];
-    if (grid_finish<1>(v, mx, d.partials, &c->counter[2], tot, bid, nblk)) {
-        const double err = sqrt(tot[0] / (double)d.n);
-        c->err = err;
-        c->n_attempt++;
-        if (err < 1) {
-            c->accepted = 1;
-            c->t = c->t + dt;
-            c->dt = fmin(dt * pow(1 / err, 1 / q), dt_max);
-            c->n_accept++;
-        } else {
-            c->accepted = 0;
-            c->dt = dt * 0.5;
-            c->n_reject++;
-            if (c->n_reject > max_reject) { c->status = ST_STEP; c->done = 1; }
-        }
-    }
+    if (grid_finish<1>(v, mx, d.partials, &c->counter[2], tot, bid, nblk)) ts_decide(c, sqrt(tot[0] / (double)d.n), dt, q, dt_max, max_reject);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(NT) k_ts_err(Dom d, const T* __restrict__ raw, double q, double dt_max, int max_reject)
 {
     ts_err_body<T>(d, raw, q, dt_max, max_reject, (int)blockIdx.x, (int)gridDim.x);
+}
+
+// Mixed form with now%w as a float pair (whi + wlo), one pass per attempt:
+// k, the error term dx = x2 - x1 = dt (b_5 - bh_5) k, x2 in FP32 from the
+// pair for the tolerance magnitudes, and sum dx^2 reduced with them; the
+// last block sets tol = atol + rtol max(|x1|, |x2|) and err = sqrt(sum dx^2
+// / n) / tol, which is the reference's sqrt(sum ((x2 - x1) / tol)^2 / n)
+// with the constant 1/tol taken out of the sum, and decides.  No FP64 work
+// per cell here: the FP64 state update moves to ts_commit_pair_body, which
+// runs for accepted attempts only.
+__device__ __forceinline__ void ts_fused_body(Dom d, const float* __restrict__ raw, double atol, double rtol, double q,
+                                              double dt_max, int max_reject, int bid, int nblk)
+{
+    Ctl* c = d.ctl;
+    if (c->done) return;
+    const double dt = c->h;
+    const double cm = c->plain ? 0.0 : block_corner_mean(raw, d.nx, d.ny);
+    const float cxf = (float)(((dt * c_ts_b[0] + dt * c_ts_b[3]) + dt * c_ts_b[4]) + dt * c_ts_b[5]);
+    const float ce = (float)(dt * c_ts_b[5] - dt * c_ts_bh[5]);
+    const float cmf = (float)cm, spyf = (float)d.spy;
+    float m1 = 0.f, m2 = 0.f, s2 = 0.f;
+    for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
+        const float k = (raw[e] - cmf) * spyf;
+        const float dx = ce * k;
+        const float x2f = d.whi[e] + (d.wlo[e] + cxf * k);
+        m1 = fmaxf(m1, fabsf(x2f - dx));
+        m2 = fmaxf(m2, fabsf(x2f));
+        s2 += dx * dx;
+    }
+    double v[3] = {(double)m1, (double)m2, (double)s2};
+    const bool mx[3] = {true, true, false};
+    double tot[3];
+    if (grid_finish<3>(v, mx, d.partials, &c->counter[1], tot, bid, nblk)) {
+        const double tol = atol + rtol * fmax(tot[0], tot[1]);
+        c->tol = tol;
+        ts_decide(c, sqrt(tot[2] / (double)d.n) / tol, dt, q, dt_max, max_reject);
+    }
+}
+
+// Accepted attempt of the fused mixed form: x = x + dt (sum_s b_s) k in
+// FP64 (k as ts_max_body forms it), now%w = x, and the float pair takes the
+// same increment by an FP32 two-sum.
+__device__ __forceinline__ void ts_commit_pair_body(Dom d, const float* __restrict__ raw, int bid, int nblk)
+{
+    const Ctl* c = d.ctl;
+    if (c->done || !c->accepted) return;
+    const double dt = c->h;
+    const double cx = ((dt * c_ts_b[0] + dt * c_ts_b[3]) + dt * c_ts_b[4]) + dt * c_ts_b[5];
+    const float cxf = (float)cx;
+    const float cmf = c->plain ? 0.f : (float)block_corner_mean(raw, d.nx, d.ny), spyf = (float)d.spy;
+    for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
+        const float k = (raw[e] - cmf) * spyf;
+        const double x2 = d.x[e] + cx * (double)k;
+        d.x[e] = x2;
+        d.w[e] = x2;
+        const float inc = cxf * k;
+        const float hi = d.whi[e], lo = d.wlo[e];
+        const float sm = hi + inc, bb = sm - hi;
+        const float er = (hi - (sm - bb)) + (inc - bb);
+        const float l2 = lo + er;
+        const float h2 = sm + l2;
+        d.whi[e] = h2;
+        d.wlo[e] = l2 - (h2 - sm);
+    }
+}
+
+__global__ void __launch_bounds__(NT) k_ts_fused(Dom d, const float* __restrict__ raw, double atol, double rtol,
+                                                 double q, double dt_max, int max_reject)
+{
+    ts_fused_body(d, raw, atol, rtol, q, dt_max, max_reject, (int)blockIdx.x, (int)gridDim.x);
+}
+
+__global__ void __launch_bounds__(NT) k_ts_commit_pair(Dom d, const float* __restrict__ raw)
+{
+    ts_commit_pair_body(d, raw, (int)blockIdx.x, (int)gridDim.x);
 }
 
 // Device-side attempt loop of the reference-compatible Tsit5: the attempts
@@ -916,12 +995,34 @@ __global__ void __launch_bounds__(NT) k_b_ts_commit(const BMember* __restrict__ 
                });
 }
 
+__global__ void __launch_bounds__(NT)
+k_b_ts_fused(const BMember* __restrict__ M, const int* __restrict__ off, int nm, int max_reject)
+{
+    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
+        const BMember& b = M[m];
+        ts_fused_body(b.d, (const float*)b.raw, b.atol, b.rtol, b.q, b.dt_max, max_reject, local, b.red_nblk);
+        __syncthreads();
+    });
+}
+
+__global__ void __launch_bounds__(NT) k_b_ts_commit_pair(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+{
+    batch_walk(off, nm, [&](int m) { const Ctl* c = M[m].d.ctl; return c->done == 0 && c->accepted != 0; },
+               [&](int m, int local) {
+                   const BMember& b = M[m];
+                   ts_commit_pair_body(b.d, (const float*)b.raw, local, b.red_nblk);
+               });
+}
+
 template <typename T> int batch_red_resident()
 {
     int per = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_ts_max<T>, NT, 0) != cudaSuccess || per < 1) per = 1;
     int p2 = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p2, k_b_ts_err<T>, NT, 0) == cudaSuccess && p2 >= 1 && p2 < per)
+        per = p2;
+    if (sizeof(T) == 4 &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p2, k_b_ts_fused, NT, 0) == cudaSuccess && p2 >= 1 && p2 < per)
         per = p2;
     return per;
 }
@@ -975,6 +1076,14 @@ template <typename T>
 void batch_ts_err(const BMember* M, const int* off, int nm, int nblk, int max_reject, cudaStream_t s)
 {
     k_b_ts_err<T><<<nblk, NT, 0, s>>>(M, off, nm, max_reject);
+}
+void batch_ts_fused(const BMember* M, const int* off, int nm, int nblk, int max_reject, cudaStream_t s)
+{
+    k_b_ts_fused<<<nblk, NT, 0, s>>>(M, off, nm, max_reject);
+}
+void batch_ts_commit_pair(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s)
+{
+    k_b_ts_commit_pair<<<nblk, NT, 0, s>>>(M, off, nm);
 }
 template <typename T> void batch_ts_commit(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s)
 {
@@ -1080,6 +1189,15 @@ template <typename T> void ts_err(const Dom& d, const T* raw, double q, double d
 template <typename T> void ts_commit(const Dom& d, const T* raw, cudaStream_t s)
 {
     k_ts_commit<T><<<ts_grid(d.n), NT, 0, s>>>(d, raw);
+}
+void ts_fused(const Dom& d, const float* raw, double atol, double rtol, double q, double dt_max, int max_reject,
+              cudaStream_t s)
+{
+    k_ts_fused<<<ts_grid(d.n), NT, 0, s>>>(d, raw, atol, rtol, q, dt_max, max_reject);
+}
+void ts_commit_pair(const Dom& d, const float* raw, cudaStream_t s)
+{
+    k_ts_commit_pair<<<ts_grid(d.n), NT, 0, s>>>(d, raw);
 }
 template <typename T> void upd_end(const Dom& d, const T* raw_last, int have_rhs, cudaStream_t s)
 {

@@ -70,6 +70,11 @@ template <typename T> void ts_max(const Dom& d, const T* raw, double atol, doubl
 template <typename T>
 void ts_err(const Dom& d, const T* raw, double q, double dt_max, int max_reject, cudaStream_t s);
 template <typename T> void ts_commit(const Dom& d, const T* raw, cudaStream_t s);
+// Mixed form with now%w's float pair (d.whi/d.wlo): tolerance, error norm
+// and decision in one pass, then the commit of an accepted attempt.
+void ts_fused(const Dom& d, const float* raw, double atol, double rtol, double q, double dt_max, int max_reject,
+              cudaStream_t s);
+void ts_commit_pair(const Dom& d, const float* raw, cudaStream_t s);
 // have_rhs < 0: read it from the control block (device Tsit5 loop)
 template <typename T> void upd_end(const Dom& d, const T* raw_last, int have_rhs, cudaStream_t s);
 void gather(const double* const* src, const uint8_t* const* msrc, int nf, int nm, const Dom& d, double* out,
