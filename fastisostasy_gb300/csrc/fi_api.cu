@@ -1564,7 +1564,16 @@ int fi_lvelva(fi_handle* h, const double* w, const double* canom_full, double* d
     if ((rc = upload(h, h->y, w, n * 8)) || (rc = upload(h, tmp, canom_full, n * 8))) return rc;
     if (mixed(h)) {
         q0_from_cf<float>((float*)h->q0, tmp, h->d.mactive, h->p.g, n, h->s);
-        rhs<float>(h, h->y, nullptr, (float*)h->raw[0]);
+        if (h->p.method == 3 && h->fc.dxm == nullptr) {
+            // uniform spacing: w as a float pair through the column-strip
+            // stencil, as the mixed reference-compatible Tsit5 evaluates it
+            float* pair;
+            if ((rc = dalloc(h, &pair, 2 * n * sizeof(float)))) return rc;
+            split_hilo(h->y, pair, pair + n, n, h->s);
+            rhs<float>(h, h->y, nullptr, (float*)h->raw[0], nullptr, pair, pair + n);
+        } else {
+            rhs<float>(h, h->y, nullptr, (float*)h->raw[0]);
+        }
         rhs_finish<float>(tmp, (const float*)h->raw[0], h->nx, h->ny, h->spy, h->s);
     } else {
         q0_from_cf<double>((double*)h->q0, tmp, h->d.mactive, h->p.g, n, h->s);
@@ -1574,6 +1583,11 @@ int fi_lvelva(fi_handle* h, const double* w, const double* canom_full, double* d
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(dwdt, tmp, n * 8, cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
+    // release the temporaries (tmp, and the float pair when one was made)
+    while (!h->allocs.empty() && h->allocs.back() != (void*)tmp) {
+        cudaFree(h->allocs.back());
+        h->allocs.pop_back();
+    }
     h->allocs.pop_back();
     cudaFree(tmp);
     return FI_OK;
@@ -1686,6 +1700,7 @@ struct fi_batch {
     std::vector<cudaEvent_t> ev;
     BMember* dM = nullptr;
     int* doff = nullptr;                 // 4 x (nm + 1): flexure, rows, columns, reductions
+    int* dcl = nullptr;                  // compacted lists of the current attempt (blist_ints(nm))
     int nblk[4] = {0, 0, 0, 0};          // virtual blocks per phase (all members)
     int grid[4] = {0, 0, 0, 0};          // resident grid per phase
     int rows_threads = 32, cols_threads = 32;
@@ -1709,20 +1724,22 @@ template <typename T> void batch_attempt(fi_batch* b, cudaStream_t s, cudaGraphC
 {
     const int nm = b->nm;
     const int* off = b->doff;
-    batch_attempt_begin(b->dM, nm, kMaxAttempts, s);
-    batch_flexure<T>(b->dM, off, nm, b->grid[0], s);
-    batch_rows_fwd<T>(b->dM, off + (nm + 1), nm, b->grid[1], b->rows_threads, b->rows_smem, s);
-    batch_cols_hartley<T>(b->dM, off + 2 * (nm + 1), nm, b->grid[2], b->cols_threads, b->cols_smem, s);
-    batch_rows_inv<T>(b->dM, off + (nm + 1), nm, b->grid[1], b->rows_threads, b->rows_smem, s);
+    batch_attempt_begin(b->dM, nm, kMaxAttempts, off, b->dcl, s);
+    const BList LF = blist(b->dcl, nm, 0), LR = blist(b->dcl, nm, 1), LC = blist(b->dcl, nm, 2),
+                LT = blist(b->dcl, nm, 3);
+    batch_flexure<T>(b->dM, LF, b->grid[0], s);
+    batch_rows_fwd<T>(b->dM, LR, b->grid[1], b->rows_threads, b->rows_smem, s);
+    batch_cols_hartley<T>(b->dM, LC, b->grid[2], b->cols_threads, b->cols_smem, s);
+    batch_rows_inv<T>(b->dM, LR, b->grid[1], b->rows_threads, b->rows_smem, s);
     if (sizeof(T) == 4) {
         // mixed members always carry now%w's float pair
-        batch_ts_fused(b->dM, off + 3 * (nm + 1), nm, b->grid[3], 100000, s);
-        batch_ts_commit_pair(b->dM, off + 3 * (nm + 1), nm, b->grid[3], s);
+        batch_ts_fused(b->dM, LT, b->grid[3], 100000, s);
+        batch_ts_commit_pair(b->dM, LT, b->grid[3], s);
         b->launches += 9;
     } else {
-        batch_ts_max<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], s);
-        batch_ts_err<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], 100000, s);
-        batch_ts_commit<T>(b->dM, off + 3 * (nm + 1), nm, b->grid[3], s);
+        batch_ts_max<T>(b->dM, LT, b->grid[3], s);
+        batch_ts_err<T>(b->dM, LT, b->grid[3], 100000, s);
+        batch_ts_commit<T>(b->dM, LT, b->grid[3], s);
         b->launches += 10;
     }
     batch_attempt_end(b->dM, nm, loop, s, more_out);
@@ -1832,6 +1849,7 @@ void batch_free(fi_batch* b)
     if (b->s) cudaStreamSynchronize(b->s);
     cudaFree(b->dM);
     cudaFree(b->doff);
+    cudaFree(b->dcl);
     cudaFree(b->dmore);
     for (int i = 0; i < fi_batch::kRing; ++i) {
         if (b->hargs[i]) cudaFreeHost(b->hargs[i]);
@@ -1850,7 +1868,7 @@ void batch_free(fi_batch* b)
 
 int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
 {
-    if (!hs || n < 1 || !out) return FI_E_ARG;
+    if (!hs || n < 1 || n > 2048 || !out) return FI_E_ARG;   // the attempt-begin kernel keeps 5 ints per member in shared memory
     *out = nullptr;
     for (int i = 0; i < n; ++i) {
         fi_handle* h = hs[i];
@@ -1891,6 +1909,16 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         m.even = h->even;
         m.RB = rhs_rows_per_block(m.p.h);
         m.CB = b->mixed ? rhs_cols_per_block<float>(m.p.ny) : rhs_cols_per_block<double>(m.p.ny);
+        if (b->mixed) {
+            // many members share a launch: 8 rows / 8 spectrum columns per
+            // virtual block (64-byte column segments) measured faster than
+            // the single-domain shapes on a 256-member ensemble
+            m.RB = m.RB < 8 ? 8 : m.RB;
+            m.CB = 8;
+        }
+        // FI_BATCH_RB / FI_BATCH_CB: rows / spectrum columns per batched transform block (tuning)
+        if (const char* e = getenv("FI_BATCH_RB")) { const int v = atoi(e); if (v >= 1 && v <= 16) m.RB = v; }
+        if (const char* e = getenv("FI_BATCH_CB")) { const int v = atoi(e); if (v >= 1 && v <= 16) m.CB = v; }
         m.fgx = (m.p.nx + 31) / 32;
         m.red_nblk = ts_grid(h->n);
         m.d = h->d;
@@ -1898,7 +1926,8 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         m.rtol = h->p.rtol;
         m.q = h->p.q;
         m.dt_max = h->p.dt_max;
-        const int fblk = m.fgx * ((m.p.ny + 7) / 8);
+        m.fseg = 16;
+        const int fblk = b->mixed ? batch_flexure_blocks(m.p.nx, m.p.ny, m.fseg) : m.fgx * ((m.p.ny + 7) / 8);
         const int rblk = (m.p.ny + m.RB - 1) / m.RB;
         const int cblk = (m.p.h + 1 + m.CB - 1) / m.CB;
         off[i + 1] = off[i] + fblk;
@@ -1908,7 +1937,7 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         const int rt = rhs_threads_for(m.RB * m.p.h / 4), ct = rhs_threads_for(m.CB * m.p.ny / 4);
         if (rt > b->rows_threads) b->rows_threads = rt;
         if (ct > b->cols_threads) b->cols_threads = ct;
-        const size_t rs = 2 * (size_t)m.RB * m.p.h * c2, cs = 2 * (size_t)m.CB * m.p.ny * c2;
+        const size_t rs = 2 * (size_t)m.RB * m.p.h * c2, cs = 2 * (size_t)m.CB * (m.p.ny + 1) * c2;   // padded columns
         if (rs > b->rows_smem) b->rows_smem = rs;
         if (cs > b->cols_smem) b->cols_smem = cs;
     }
@@ -1918,6 +1947,7 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
               cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
               cudaMalloc(&b->dM, n * sizeof(BMember)) == cudaSuccess &&
               cudaMalloc(&b->doff, off.size() * sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&b->dcl, blist_ints(n) * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&b->dmore, sizeof(int)) == cudaSuccess;
     if (const char* e = getenv("FI_BATCH_EAGER")) b->eager = (e[0] == '1');
     b->ev.assign(n, nullptr);
@@ -1942,14 +1972,32 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         batch_grids<double>(b->rows_smem, b->cols_smem, b->rows_threads, b->cols_threads, &res[0], &res[1], &res[2],
                             &res[3]);
     }
-    // resident grid times FI_BATCH_WAVES (default 4) waves, at most one block per virtual block
-    int waves = 4;
+    // resident grid times FI_BATCH_WAVES (default 8) waves, at most one block per virtual block
+    int waves = 8;
     if (const char* e = getenv("FI_BATCH_WAVES")) waves = atoi(e);
     for (int k = 0; k < 4; ++k) {
         const long long g = waves > 0 ? (long long)res[k] * waves : (long long)b->nblk[k];
         b->grid[k] = (int)(g < b->nblk[k] ? g : b->nblk[k]);
     }
     *out = b;
+    return FI_OK;
+}
+
+int fi_batch_set_priority(fi_batch* b, int level)
+{
+    if (!b || level < 0 || level > 1) return FI_E_ARG;
+    if (b->seen[0] || b->seen[1]) return FI_E_STATE;
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return FI_E_CUDA;
+    cudaStream_t ns = nullptr;
+    if (cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, level ? greatest : least) != cudaSuccess)
+        return FI_E_CUDA;
+    if (cudaStreamSynchronize(b->s) != cudaSuccess) {
+        cudaStreamDestroy(ns);
+        return FI_E_CUDA;
+    }
+    cudaStreamDestroy(b->s);
+    b->s = ns;
     return FI_OK;
 }
 

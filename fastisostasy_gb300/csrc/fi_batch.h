@@ -33,7 +33,8 @@ struct BMember {
     void* raw;                // RHS output (T)
     int even;
     int RB, CB;               // rows per row block, columns per column block
-    int fgx;                  // flexure blocks along x
+    int fgx;                  // flexure blocks along x (FP64 tiles)
+    int fseg;                 // output rows per flexure warp task (mixed column strips)
     int red_nblk;             // blocks of the reduction kernels
     Dom d;
     double atol, rtol, q, dt_max;
@@ -45,6 +46,30 @@ struct BArgs {
     double tf, bsl, A_ocean;
     int method, write_bsl;
 };
+
+// Members with work in the current attempt, compacted by the attempt-begin
+// kernel: ids[j] for j < *cnt, member ids[j] owning the virtual blocks
+// [coff[j], coff[j+1]) of a batched launch.  Four lists share one int buffer
+// of blist_ints(nm) entries: 0 flexure, 1 row transforms, 2 column
+// transforms (members that need a new RHS), 3 attempt kernels (members with
+// an attempt left).
+struct BList {
+    const int* ids;
+    const int* coff;
+    const int* cnt;
+};
+inline size_t blist_ints(int nm) { return 2 + 2 * (size_t)nm + 4 * ((size_t)nm + 1); }
+inline BList blist(const int* base, int nm, int kind)
+{
+    BList L;
+    L.cnt = base + (kind == 3 ? 1 : 0);
+    L.ids = base + 2 + (kind == 3 ? nm : 0);
+    L.coff = base + 2 + 2 * (size_t)nm + (size_t)kind * (nm + 1);
+    return L;
+}
+
+// Virtual blocks of the mixed batched flexure (8 column-strip warp tasks each).
+int batch_flexure_blocks(int nx, int ny, int seg);
 
 // Block shapes of the single-domain launches (shared with the batched ones).
 int rhs_rows_per_block(int h);
@@ -64,22 +89,24 @@ template <typename T> void batch_grids(size_t rows_smem, size_t cols_smem, int r
                                        int* g_flex, int* g_rows, int* g_cols, int* g_red);
 
 // Phase kernels over all members; nblk is the launch's (resident) grid.
-template <typename T> void batch_flexure(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s);
+template <typename T> void batch_flexure(const BMember* M, BList L, int nblk, cudaStream_t s);
 template <typename T>
-void batch_rows_fwd(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s);
+void batch_rows_fwd(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s);
 template <typename T>
-void batch_cols_hartley(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s);
+void batch_cols_hartley(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s);
 template <typename T>
-void batch_rows_inv(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s);
-template <typename T> void batch_ts_max(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s);
+void batch_rows_inv(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s);
+template <typename T> void batch_ts_max(const BMember* M, BList L, int nblk, cudaStream_t s);
 template <typename T>
-void batch_ts_err(const BMember* M, const int* off, int nm, int nblk, int max_reject, cudaStream_t s);
-template <typename T> void batch_ts_commit(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s);
+void batch_ts_err(const BMember* M, BList L, int nblk, int max_reject, cudaStream_t s);
+template <typename T> void batch_ts_commit(const BMember* M, BList L, int nblk, cudaStream_t s);
 // mixed form with the float pair of now%w: ts_fused / ts_commit_pair per member
-void batch_ts_fused(const BMember* M, const int* off, int nm, int nblk, int max_reject, cudaStream_t s);
-void batch_ts_commit_pair(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s);
+void batch_ts_fused(const BMember* M, BList L, int nblk, int max_reject, cudaStream_t s);
+void batch_ts_commit_pair(const BMember* M, BList L, int nblk, cudaStream_t s);
 void batch_loop_begin(const BMember* M, int nm, cudaStream_t s);
-void batch_attempt_begin(const BMember* M, int nm, int max_iter, cudaStream_t s);
+// attempt_begin of every member, then the compacted lists (cl, blist_ints(nm)
+// ints) from the members' static block offsets (off, 4 x (nm + 1)).
+void batch_attempt_begin(const BMember* M, int nm, int max_iter, const int* off, int* cl, cudaStream_t s);
 // more_out == NULL: sets the WHILE condition `loop`; else writes it there
 void batch_attempt_end(const BMember* M, int nm, cudaGraphConditionalHandle loop, cudaStream_t s,
                        int* more_out = nullptr);
@@ -97,27 +124,30 @@ __device__ __forceinline__ int batch_member(const int* __restrict__ off, int nm,
     return lo;
 }
 
-// Grid-stride walk over the virtual blocks of a batched launch: member m
-// owns virtual blocks [off[m], off[m+1]); fn(m, local block) runs for the
-// virtual blocks of members with active(m) (uniform over the block), and a
-// member without work is skipped in one jump.  Launches therefore size their
-// grid to what stays resident, not to the members' total block count.
+// Grid-stride walk over the virtual blocks of the listed members: fn(m,
+// local block) runs for each, skipped where active(m) is false (uniform over
+// the block; a member without work is skipped in one jump).  Launches size
+// their grid to what stays resident, not to the members' total block count,
+// and members without work cost nothing.
 template <typename Act, typename Fn>
-__device__ __forceinline__ void batch_walk(const int* __restrict__ off, int nm, Act active, Fn fn)
+__device__ __forceinline__ void batch_walk(BList L, Act active, Fn fn)
 {
-    const int total = __ldg(off + nm);
+    const int na = __ldg(L.cnt);
+    if (na <= 0) return;
+    const int total = __ldg(L.coff + na);
     const int stride = (int)gridDim.x;
     int vb = (int)blockIdx.x;
     if (vb >= total) return;
-    int m = batch_member(off, nm, vb);
+    int j = batch_member(L.coff, na, vb);
     while (vb < total) {
-        while (__ldg(off + m + 1) <= vb) ++m;
-        const int end = __ldg(off + m + 1);
+        while (__ldg(L.coff + j + 1) <= vb) ++j;
+        const int m = __ldg(L.ids + j);
+        const int end = __ldg(L.coff + j + 1);
         if (!active(m)) {
             vb += ((end - vb + stride - 1) / stride) * stride;
             continue;
         }
-        fn(m, vb - __ldg(off + m));
+        fn(m, vb - __ldg(L.coff + j));
         vb += stride;
     }
 }

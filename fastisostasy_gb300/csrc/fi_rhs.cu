@@ -324,6 +324,164 @@ __device__ __forceinline__ void flexure_f32_body(const double* __restrict__ y, c
     f[e] = (((p + mx_xx) + 2.f * mxy_xy) + my_yy) * own_ie;
 }
 
+// ---------------------------------------------------------------------------
+// Flexure by column strips (mixed form, uniform spacing, the state as a
+// float pair).  One warp task = SW output columns [SW g, SW g + SW) by `seg`
+// output rows [seg s, seg s + seg): lane l holds column SW g - 2 + l and
+// walks down the rows with the vertical stencil window in registers, taking
+// x-neighbours by warp shuffles, so there is no shared memory and no block
+// barrier.  Moments of row m are formed when input row m + 2 has been read,
+// f of row o when moments of row o + 2 exist (the one-sided formulas of the
+// first and last rows reach two rows further than the interior ones); the
+// arithmetic is that of flexure_f32_body<true>, term by term.
+// ---------------------------------------------------------------------------
+constexpr int SW = 28;                     // output columns per warp task
+
+__device__ __forceinline__ int strip_tasks(int nx, int ny, int seg)
+{
+    return ((nx + SW - 1) / SW) * ((ny + seg - 1) / seg);
+}
+
+__device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, const float* __restrict__ wlo,
+                                              const float* __restrict__ q0, const uint8_t* __restrict__ mask,
+                                              const float* __restrict__ D, const float* __restrict__ inv2eta,
+                                              float* __restrict__ f, int nx, int ny, const FlexCoefF& c, int seg,
+                                              int task)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int ncg = (nx + SW - 1) / SW;
+    const int g = task % ncg, sg = task / ncg;
+    const int lane = (int)(threadIdx.x + threadIdx.y * blockDim.x) & 31;   // 1D or 32 x 8 blocks
+    const int col = g * SW - 2 + lane;
+    const bool cin = col >= 0 && col < nx;
+    const bool outl = cin && lane >= 2 && lane < 2 + SW;
+    const bool left = col == 0, right = col == nx - 1;
+    const bool edge = g == 0 || g == ncg - 1;   // warp-uniform: a lane may sit on x = 0 or x = nx - 1
+    const int o0 = sg * seg, o1 = min(o0 + seg, ny);
+    const int cc = cin ? col : 0;
+    float hp = 0.f, lp = 0.f;                           // pair of row r - 1
+    float Wx1 = 0.f, Wx2 = 0.f, Wx3 = 0.f;              // Wx of rows r-1, r-2, r-3
+    float wxx1 = 0.f, wxx2 = 0.f;                       // wxx of rows r-1, r-2
+    float dY1 = 0.f, dY2 = 0.f, dY3 = 0.f, dY4 = 0.f;   // dY of rows r-1 .. r-4 (dY_j = y_{j+1} - y_j)
+    float My0 = 0.f, My1 = 0.f, My2 = 0.f, My3 = 0.f, My4 = 0.f;   // Myy of rows m .. m-4
+    float Mq0 = 0.f, Mq1 = 0.f, Mq2 = 0.f, Mq3 = 0.f;              // Mxyx of rows m .. m-3
+    float mx0 = 0.f, mx1 = 0.f, mx2 = 0.f;                         // mx_xx of rows m .. m-2
+    // the next row's loads are issued one iteration ahead
+    int r = o0 - 4;
+    auto ld_pair = [&](int rr, float& h, float& l) {
+        if (cin && rr >= 0 && rr < ny) {
+            const size_t e = (size_t)rr * nx + cc;
+            h = __ldg(whi + e);
+            l = __ldg(wlo + e);
+        } else {
+            h = 0.f;
+            l = 0.f;
+        }
+    };
+    float hn, ln;
+    ld_pair(r, hn, ln);
+    for (; r < o1 + 4; ++r) {
+        const float h = hn, l = ln;
+        ld_pair(r + 1, hn, ln);
+        const int m = r - 2, o = r - 4;
+        const bool mrow = cin && m >= 0 && m < ny;
+        const float Dm = mrow ? __ldg(D + (size_t)m * nx + cc) : 0.f;
+        const bool orow = outl && o >= o0 && o < o1;
+        const size_t eo = orow ? (size_t)o * nx + cc : 0;
+        const uint8_t om = orow ? __ldg(mask + eo) : (uint8_t)0;
+        const float oq = orow ? __ldg(q0 + eo) : 0.f, oie = orow ? __ldg(inv2eta + eo) : 0.f;
+        // row r: first differences, Wx, wxx
+        const float hr = __shfl_down_sync(FULL, h, 1), lr = __shfl_down_sync(FULL, l, 1);
+        const float dX = (hr - h) + (lr - l);
+        const float dXm = __shfl_up_sync(FULL, dX, 1);
+        float Wx, wxx;
+        if (edge) {
+            const float dXp = __shfl_down_sync(FULL, dX, 1), dXmm = __shfl_up_sync(FULL, dX, 2);
+            Wx = left ? dX * c.inv_dx : right ? dXm * c.inv_dx : (dX + dXm) * c.inv_2dx;
+            wxx = left ? (dXp - dX) * c.inv_dx2 : right ? (dXm - dXmm) * c.inv_dx2 : (dX - dXm) * c.inv_dx2;
+        } else {
+            Wx = (dX + dXm) * c.inv_2dx;
+            wxx = (dX - dXm) * c.inv_dx2;
+        }
+        const float dYn = (h - hp) + (l - lp);   // dY of row r - 1
+        hp = h;
+        lp = l;
+        dY4 = dY3; dY3 = dY2; dY2 = dY1; dY1 = dYn;
+        // moments of row m = r - 2 (Wx1..3 are still those of rows r-1..r-3)
+        float wxy, wyy;
+        if (m == 0) {
+            wxy = (Wx1 - Wx2) * c.inv_dy;
+            wyy = (dY1 - dY2) * c.inv_dy2;
+        } else if (m == ny - 1) {
+            wxy = (Wx2 - Wx3) * c.inv_dy;
+            wyy = (dY3 - dY4) * c.inv_dy2;
+        } else {
+            wxy = (Wx1 - Wx3) * c.inv_2dy;
+            wyy = (dY2 - dY3) * c.inv_dy2;
+        }
+        const float wxm = wxx2;
+        const float Mxx = -Dm * (wxm + c.nu * wyy);
+        const float Myy = -Dm * (wyy + c.nu * wxm);
+        const float Mxy = (-Dm * c.one_minus_nu) * wxy;
+        Wx3 = Wx2; Wx2 = Wx1; Wx1 = Wx;
+        wxx2 = wxx1; wxx1 = wxx;
+        // x-derivatives of the moments of row m
+        const float Mxyp = __shfl_down_sync(FULL, Mxy, 1), Mxym = __shfl_up_sync(FULL, Mxy, 1);
+        const float Mxxp = __shfl_down_sync(FULL, Mxx, 1), Mxxm = __shfl_up_sync(FULL, Mxx, 1);
+        float Mxyx, mxx;
+        if (edge) {
+            const float Mxxp2 = __shfl_down_sync(FULL, Mxx, 2), Mxxm2 = __shfl_up_sync(FULL, Mxx, 2);
+            Mxyx = left ? (Mxyp - Mxy) * c.inv_dx : right ? (Mxy - Mxym) * c.inv_dx : (Mxyp - Mxym) * c.inv_2dx;
+            mxx = left ? ((Mxxp2 - 2.f * Mxxp) + Mxx) * c.inv_dx2
+                : right ? ((Mxx - 2.f * Mxxm) + Mxxm2) * c.inv_dx2
+                : ((Mxxp - 2.f * Mxx) + Mxxm) * c.inv_dx2;
+        } else {
+            Mxyx = (Mxyp - Mxym) * c.inv_2dx;
+            mxx = ((Mxxp - 2.f * Mxx) + Mxxm) * c.inv_dx2;
+        }
+        My4 = My3; My3 = My2; My2 = My1; My1 = My0; My0 = Myy;
+        Mq3 = Mq2; Mq2 = Mq1; Mq1 = Mq0; Mq0 = Mxyx;
+        mx2 = mx1; mx1 = mx0; mx0 = mxx;
+        // f of row o = m - 2
+        if (orow) {
+            float mxy_xy, my_yy;
+            if (o == 0) {
+                mxy_xy = (Mq1 - Mq2) * c.inv_dy;
+                my_yy = ((My0 - 2.f * My1) + My2) * c.inv_dy2;
+            } else if (o == ny - 1) {
+                mxy_xy = (Mq2 - Mq3) * c.inv_dy;
+                my_yy = ((My2 - 2.f * My3) + My4) * c.inv_dy2;
+            } else {
+                mxy_xy = (Mq1 - Mq3) * c.inv_2dy;
+                my_yy = ((My1 - 2.f * My2) + My3) * c.inv_dy2;
+            }
+            const float p = om ? oq : 0.f;
+            f[eo] = (((p + mx2) + 2.f * mxy_xy) + my_yy) * oie;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_flexure_strip(const float* __restrict__ whi, const float* __restrict__ wlo, const float* __restrict__ q0,
+                const uint8_t* __restrict__ mask, const float* __restrict__ D, const float* __restrict__ inv2eta,
+                float* __restrict__ f, int nx, int ny, FlexCoefF c, int seg, const int* __restrict__ gate)
+{
+    if (gate && *gate == 0) return;
+    const int task = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (task >= strip_tasks(nx, ny, seg)) return;   // whole warps
+    flexure_strip(whi, wlo, q0, mask, D, inv2eta, f, nx, ny, c, seg, task);
+}
+
+// rows per warp task for a single domain: enough tasks to fill the GPU
+static int strip_seg_single(int nx, int ny)
+{
+    const long long ncg = (nx + SW - 1) / SW;
+    long long seg = (long long)ny * ncg / (152 * 16);
+    if (seg > 32) seg = 32;
+    if (seg < 8) seg = 8;
+    return (int)seg;
+}
+
 __global__ void __launch_bounds__(TX* TY)
 k_flexure_f32(const double* __restrict__ y, const double* __restrict__ wref, const float* __restrict__ q0,
               const uint8_t* __restrict__ mask, const float* __restrict__ D, const float* __restrict__ inv2eta,
@@ -351,8 +509,10 @@ void launch_flexure(const double* y, const double* wref, const T* q0, const uint
     if (sizeof(T) == 4 && c.dxm == nullptr) {
         const FlexCoefF cf = flex_coef_f32(c);
         if (whi && !wref) {
-            k_flexure_f32_hilo<<<g, b, 0, s>>>(whi, wlo, (const float*)q0, mask, (const float*)D,
-                                               (const float*)inv2eta, (float*)f, nx, ny, cf, gate);
+            const int seg = strip_seg_single(nx, ny);
+            const int tasks = ((nx + SW - 1) / SW) * ((ny + seg - 1) / seg);
+            k_flexure_strip<<<(tasks + 7) / 8, 256, 0, s>>>(whi, wlo, (const float*)q0, mask, (const float*)D,
+                                                            (const float*)inv2eta, (float*)f, nx, ny, cf, seg, gate);
             return;
         }
         k_flexure_f32<<<g, b, 0, s>>>(y, wref, (const float*)q0, mask, (const float*)D, (const float*)inv2eta,
@@ -512,12 +672,17 @@ void launch_rows_inv(const typename vec2<T>::type* S, T* out, const Plan2D& p, d
 // ---------------------------------------------------------------------------
 // Columns per block: two float2 or one double2 column, i.e. 16-byte row
 // segments, which keeps hundreds of blocks in flight at 512^2.
+// Column c of a block lives at c * col_stride(ny) in shared memory: one
+// complex element of padding per column, so the CB columns of a row segment
+// (loaded and stored together) fall in different banks instead of one.
+__host__ __device__ __forceinline__ int col_stride(int ny) { return ny + 1; }
+
 template <typename T> static int cols_per_block(int ny)
 {
     typedef typename vec2<T>::type C2;
     int cb = (int)(16 / sizeof(C2));
     if (cb < 1) cb = 1;
-    while (cb > 1 && 2 * (size_t)cb * ny * sizeof(C2) > 200 * 1024) cb /= 2;
+    while (cb > 1 && 2 * (size_t)cb * col_stride(ny) * sizeof(C2) > 200 * 1024) cb /= 2;
     return cb;
 }
 
@@ -526,13 +691,13 @@ __device__ __forceinline__ void load_cols(typename vec2<T>::type* b0, const type
                                           int CB, int nrows_in, const Plan2D& p)
 {
     typedef typename vec2<T>::type C2;
-    const int ny = p.col.d.n;
+    const int ny = p.col.d.n, ls = col_stride(ny);
     for (int e = threadIdx.x; e < CB * ny; e += blockDim.x) {
         const int c = e % CB, l = e / CB;
         const int k = k0 + c;
         C2 v = mk2<T>((T)0, (T)0);
         if (k <= p.h && l < nrows_in) v = S[(size_t)l * p.sp + k];
-        b0[c * ny + l] = v;
+        b0[c * ls + l] = v;
     }
 }
 
@@ -542,20 +707,20 @@ __device__ __forceinline__ void cols_hartley_body(typename vec2<T>::type* __rest
 {
     typedef typename vec2<T>::type C2;
     extern __shared__ unsigned char smem_raw[];
-    const int ny = p.col.d.n;
+    const int ny = p.col.d.n, ls = col_stride(ny);
     C2* b0 = reinterpret_cast<C2*>(smem_raw);
-    C2* b1 = b0 + (size_t)CB * ny;
+    C2* b1 = b0 + (size_t)CB * ls;
     const int k0 = bx * CB;
     load_cols<T>(b0, S, k0, CB, ny, p);
     __syncthreads();
-    C2* r = block_fft<T>(b0, b1, p.col.d, CB, ny, twp<T>(p.col), -1);
+    C2* r = block_fft<T>(b0, b1, p.col.d, CB, ls, twp<T>(p.col), -1);
     const int half = ny / 2 + 1;
     for (int e = threadIdx.x; e < CB * half; e += blockDim.x) {
         const int c = e % CB, l = e / CB;
         const int k = k0 + c;
         if (k > p.h) continue;
         const int lm = (ny - l) % ny;
-        C2* col = r + (size_t)c * ny;
+        C2* col = r + (size_t)c * ls;
         const size_t ia = (size_t)l * p.sp + k, ib = (size_t)lm * p.sp + k;
         const C2 Fa = col[l], Fb = col[lm];
         if (even) {
@@ -582,11 +747,11 @@ __device__ __forceinline__ void cols_hartley_body(typename vec2<T>::type* __rest
     }
     __syncthreads();
     C2* other = (r == b0) ? b1 : b0;
-    C2* q = block_fft<T>(r, other, p.col.d, CB, ny, twp<T>(p.col), +1);
+    C2* q = block_fft<T>(r, other, p.col.d, CB, ls, twp<T>(p.col), +1);
     for (int e = threadIdx.x; e < CB * ny; e += blockDim.x) {
         const int c = e % CB, l = e / CB;
         const int k = k0 + c;
-        if (k <= p.h) S[(size_t)l * p.sp + k] = q[c * ny + l];
+        if (k <= p.h) S[(size_t)l * p.sp + k] = q[c * ls + l];
     }
 }
 
@@ -604,7 +769,7 @@ void launch_cols_hartley(typename vec2<T>::type* S, const T* mA, const T* mB, in
 {
     typedef typename vec2<T>::type C2;
     const int CB = cols_per_block<T>(p.ny);
-    const size_t sm = 2 * (size_t)CB * p.ny * sizeof(C2);
+    const size_t sm = 2 * (size_t)CB * col_stride(p.ny) * sizeof(C2);
     set_smem(k_cols_hartley<T>, sm);
     const int nblk = (p.h + 1 + CB - 1) / CB;
     k_cols_hartley<T><<<nblk, threads_for(CB * p.ny / 4), sm, s>>>(S, mA, mB, even, p, CB, gate);
@@ -616,18 +781,18 @@ __global__ void k_cols_conv(typename vec2<T>::type* __restrict__ S, const typena
 {
     typedef typename vec2<T>::type C2;
     extern __shared__ unsigned char smem_raw[];
-    const int ny = p.col.d.n;
+    const int ny = p.col.d.n, ls = col_stride(ny);
     C2* b0 = reinterpret_cast<C2*>(smem_raw);
-    C2* b1 = b0 + (size_t)CB * ny;
+    C2* b1 = b0 + (size_t)CB * ls;
     const int k0 = blockIdx.x * CB;
     load_cols<T>(b0, S, k0, CB, nrows_in, p);
     __syncthreads();
-    C2* r = block_fft<T>(b0, b1, p.col.d, CB, ny, twp<T>(p.col), -1);
+    C2* r = block_fft<T>(b0, b1, p.col.d, CB, ls, twp<T>(p.col), -1);
     if (!do_inv) {
         for (int e = threadIdx.x; e < CB * ny; e += blockDim.x) {
             const int c = e % CB, l = e / CB;
             const int k = k0 + c;
-            if (k <= p.h) S[(size_t)l * p.sp + k] = r[c * ny + l];
+            if (k <= p.h) S[(size_t)l * p.sp + k] = r[c * ls + l];
         }
         return;
     }
@@ -635,15 +800,15 @@ __global__ void k_cols_conv(typename vec2<T>::type* __restrict__ S, const typena
         const int c = e % CB, l = e / CB;
         const int k = k0 + c;
         if (k > p.h) continue;
-        r[c * ny + l] = cmul(r[c * ny + l], K[(size_t)l * p.sp + k]);
+        r[c * ls + l] = cmul(r[c * ls + l], K[(size_t)l * p.sp + k]);
     }
     __syncthreads();
     C2* other = (r == b0) ? b1 : b0;
-    C2* q = block_fft<T>(r, other, p.col.d, CB, ny, twp<T>(p.col), +1);
+    C2* q = block_fft<T>(r, other, p.col.d, CB, ls, twp<T>(p.col), +1);
     for (int e = threadIdx.x; e < CB * n_out; e += blockDim.x) {
         const int c = e % CB, o = e / CB;
         const int k = k0 + c;
-        if (k <= p.h) S[(size_t)o * p.sp + k] = q[c * ny + out_rows[o]];
+        if (k <= p.h) S[(size_t)o * p.sp + k] = q[c * ls + out_rows[o]];
     }
 }
 
@@ -653,7 +818,7 @@ void launch_cols_conv(typename vec2<T>::type* S, const typename vec2<T>::type* K
 {
     typedef typename vec2<T>::type C2;
     const int CB = cols_per_block<T>(p.ny);
-    const size_t sm = 2 * (size_t)CB * p.ny * sizeof(C2);
+    const size_t sm = 2 * (size_t)CB * col_stride(p.ny) * sizeof(C2);
     set_smem(k_cols_conv<T>, sm);
     const int nblk = (p.h + 1 + CB - 1) / CB;
     k_cols_conv<T><<<nblk, threads_for(CB * p.ny / 4), sm, s>>>(S, K, nrows_in, out_rows, n_out, p, CB, 1);
@@ -664,7 +829,7 @@ void launch_cols_fwd(typename vec2<T>::type* S, int nrows_in, const Plan2D& p, c
 {
     typedef typename vec2<T>::type C2;
     const int CB = cols_per_block<T>(p.ny);
-    const size_t sm = 2 * (size_t)CB * p.ny * sizeof(C2);
+    const size_t sm = 2 * (size_t)CB * col_stride(p.ny) * sizeof(C2);
     set_smem(k_cols_conv<T>, sm);
     const int nblk = (p.h + 1 + CB - 1) / CB;
     k_cols_conv<T><<<nblk, threads_for(CB * p.ny / 4), sm, s>>>(S, nullptr, nrows_in, nullptr, 0, p, CB, 0);
@@ -749,16 +914,18 @@ template int rhs_cols_per_block<float>(int);
 template int rhs_cols_per_block<double>(int);
 
 template <typename T>
-__global__ void __launch_bounds__(TX* TY) k_b_flexure(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+__global__ void __launch_bounds__(256) k_b_flexure(const BMember* __restrict__ M, BList L)
 {
-    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
         const BMember& b = M[m];
         const int bx = local % b.fgx, by = local / b.fgx;
         if constexpr (sizeof(T) == 4) {
-            // mixed members have uniform spacing and carry now%w as a float pair
-            flexure_f32_body<true>(nullptr, nullptr, (const float*)b.q0, b.mask, (const float*)b.D,
-                                   (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, b.fcf, bx, by, b.d.whi,
-                                   b.d.wlo);
+            // mixed members have uniform spacing and carry now%w as a float
+            // pair: column strips, 8 warp tasks per virtual block
+            const int task = local * 8 + (int)threadIdx.y;   // 32 x 8 block: warp = threadIdx.y
+            if (task < strip_tasks(b.p.nx, b.p.ny, b.fseg))
+                flexure_strip(b.d.whi, b.d.wlo, (const float*)b.q0, b.mask, (const float*)b.D,
+                              (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, b.fcf, b.fseg, task);
         } else {
             flexure_body<T>(b.y, nullptr, (const T*)b.q0, b.mask, (const T*)b.D, (const T*)b.inv2eta, (T*)b.f,
                             b.p.nx, b.p.ny, b.fc, bx, by);
@@ -768,10 +935,10 @@ __global__ void __launch_bounds__(TX* TY) k_b_flexure(const BMember* __restrict_
 }
 
 template <typename T>
-__global__ void k_b_rows_fwd(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+__global__ void k_b_rows_fwd(const BMember* __restrict__ M, BList L)
 {
     typedef typename vec2<T>::type C2;
-    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
         const BMember& b = M[m];
         rows_fwd_body<T>((const T*)b.f, b.p.nx, b.p.nx, b.p.ny, (C2*)b.S, b.p, b.RB, local, 0);
         __syncthreads();
@@ -779,10 +946,10 @@ __global__ void k_b_rows_fwd(const BMember* __restrict__ M, const int* __restric
 }
 
 template <typename T>
-__global__ void k_b_cols_hartley(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+__global__ void k_b_cols_hartley(const BMember* __restrict__ M, BList L)
 {
     typedef typename vec2<T>::type C2;
-    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
         const BMember& b = M[m];
         cols_hartley_body<T>((C2*)b.S, (const T*)b.mA, (const T*)b.mB, b.even, b.p, b.CB, local, 0);
         __syncthreads();
@@ -790,10 +957,10 @@ __global__ void k_b_cols_hartley(const BMember* __restrict__ M, const int* __res
 }
 
 template <typename T>
-__global__ void k_b_rows_inv(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+__global__ void k_b_rows_inv(const BMember* __restrict__ M, BList L)
 {
     typedef typename vec2<T>::type C2;
-    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
         const BMember& b = M[m];
         const double norm = (double)(float)((long long)b.p.nx * b.p.ny);   // nx*ny*1. (default real)
         rows_inv_body<T>((const C2*)b.S, b.p.ny, (T*)b.raw, b.p.nx, b.p, b.RB, (T)(1.0 / norm), local, 0);
@@ -820,27 +987,29 @@ template <typename T> void batch_grids(size_t rows_smem, size_t cols_smem, int r
     *g_red = batch_red_resident<T>() * nsm;
 }
 
-template <typename T> void batch_flexure(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s)
+template <typename T> void batch_flexure(const BMember* M, BList L, int nblk, cudaStream_t s)
 {
-    k_b_flexure<T><<<nblk, dim3(TX, TY), 0, s>>>(M, off, nm);
+    // 256 threads: the tile body reads them as TX x TY, the strip body as 8 warps
+    k_b_flexure<T><<<nblk, dim3(TX, TY), 0, s>>>(M, L);
 }
+int batch_flexure_blocks(int nx, int ny, int seg) { return (((nx + SW - 1) / SW) * ((ny + seg - 1) / seg) + 7) / 8; }
 template <typename T>
-void batch_rows_fwd(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s)
+void batch_rows_fwd(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s)
 {
     set_smem(k_b_rows_fwd<T>, smem);
-    k_b_rows_fwd<T><<<nblk, threads, smem, s>>>(M, off, nm);
+    k_b_rows_fwd<T><<<nblk, threads, smem, s>>>(M, L);
 }
 template <typename T>
-void batch_cols_hartley(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s)
+void batch_cols_hartley(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s)
 {
     set_smem(k_b_cols_hartley<T>, smem);
-    k_b_cols_hartley<T><<<nblk, threads, smem, s>>>(M, off, nm);
+    k_b_cols_hartley<T><<<nblk, threads, smem, s>>>(M, L);
 }
 template <typename T>
-void batch_rows_inv(const BMember* M, const int* off, int nm, int nblk, int threads, size_t smem, cudaStream_t s)
+void batch_rows_inv(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s)
 {
     set_smem(k_b_rows_inv<T>, smem);
-    k_b_rows_inv<T><<<nblk, threads, smem, s>>>(M, off, nm);
+    k_b_rows_inv<T><<<nblk, threads, smem, s>>>(M, L);
 }
 
 template <typename T> void batch_prepare(size_t rows_smem, size_t cols_smem)
@@ -853,10 +1022,10 @@ template <typename T> void batch_prepare(size_t rows_smem, size_t cols_smem)
 #define FI_BATCH_INST(T)                                                                                   \
     template void batch_prepare<T>(size_t, size_t);                                                        \
     template void batch_grids<T>(size_t, size_t, int, int, int*, int*, int*, int*);                        \
-    template void batch_flexure<T>(const BMember*, const int*, int, int, cudaStream_t);                    \
-    template void batch_rows_fwd<T>(const BMember*, const int*, int, int, int, size_t, cudaStream_t);      \
-    template void batch_cols_hartley<T>(const BMember*, const int*, int, int, int, size_t, cudaStream_t);  \
-    template void batch_rows_inv<T>(const BMember*, const int*, int, int, int, size_t, cudaStream_t);
+    template void batch_flexure<T>(const BMember*, BList, int, cudaStream_t);                    \
+    template void batch_rows_fwd<T>(const BMember*, BList, int, int, size_t, cudaStream_t);      \
+    template void batch_cols_hartley<T>(const BMember*, BList, int, int, size_t, cudaStream_t);  \
+    template void batch_rows_inv<T>(const BMember*, BList, int, int, size_t, cudaStream_t);
 FI_BATCH_INST(double)
 FI_BATCH_INST(float)
 

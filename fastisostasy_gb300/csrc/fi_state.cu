@@ -94,6 +94,73 @@ __device__ bool grid_finish(double (&v)[NV], const bool (&is_max)[NV], double* p
     return false;
 }
 
+// grid_finish with the per-block part in FP32 (this GPU runs FP64 at 1/64
+// of the FP32 rate): maxima and sums of the block's threads reduced in
+// float, the block totals passed on as doubles and combined as above.
+__device__ __forceinline__ float warp_sum_f(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_max_f(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+template <int NV>
+__device__ bool grid_finish_f(float (&vf)[NV], const bool (&is_max)[NV], double* partials, unsigned* counter,
+                              double (&tot)[NV], int bid, int nblk)
+{
+    __shared__ float shf[32 * NV];
+    __shared__ double sh[32 * NV];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) vf[q] = is_max[q] ? warp_max_f(vf[q]) : warp_sum_f(vf[q]);
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) shf[wid * NV + q] = vf[q];
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            const float a = (lane < nw) ? shf[lane * NV + q] : 0.f;
+            vf[q] = is_max[q] ? warp_max_f(a) : warp_sum_f(a);
+        }
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) partials[(size_t)bid * NV + q] = (double)vf[q];
+        __threadfence();
+        const unsigned prev = atomicAdd(counter, 1u);
+        last = (prev == (unsigned)nblk - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double a[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        a[q] = 0.0;
+        for (unsigned b = threadIdx.x; b < (unsigned)nblk; b += blockDim.x) {
+            const double pb = ((volatile double*)partials)[(size_t)b * NV + q];
+            a[q] = is_max[q] ? fmax(a[q], pb) : a[q] + pb;
+        }
+    }
+    __syncthreads();
+    block_reduce<NV>(a, is_max, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) tot[q] = a[q];
+        *counter = 0u;
+        return true;
+    }
+    return false;
+}
+
 // The same over this launch's grid.
 template <int NV>
 __device__ __forceinline__ bool grid_finish(double (&v)[NV], const bool (&is_max)[NV], double* partials,
@@ -519,6 +586,8 @@ __device__ __forceinline__ void ts_fused_body(Dom d, const float* __restrict__ r
     const float ce = (float)(dt * c_ts_b[5] - dt * c_ts_bh[5]);
     const float cmf = (float)cm, spyf = (float)d.spy;
     float m1 = 0.f, m2 = 0.f, s2 = 0.f;
+    // unrolled so that several cells' loads are in flight per thread
+#pragma unroll 4
     for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
         const float k = (raw[e] - cmf) * spyf;
         const float dx = ce * k;
@@ -527,10 +596,10 @@ __device__ __forceinline__ void ts_fused_body(Dom d, const float* __restrict__ r
         m2 = fmaxf(m2, fabsf(x2f));
         s2 += dx * dx;
     }
-    double v[3] = {(double)m1, (double)m2, (double)s2};
+    float v[3] = {m1, m2, s2};
     const bool mx[3] = {true, true, false};
     double tot[3];
-    if (grid_finish<3>(v, mx, d.partials, &c->counter[1], tot, bid, nblk)) {
+    if (grid_finish_f<3>(v, mx, d.partials, &c->counter[1], tot, bid, nblk)) {
         const double tol = atol + rtol * fmax(tot[0], tot[1]);
         c->tol = tol;
         ts_decide(c, sqrt(tot[2] / (double)d.n) / tol, dt, q, dt_max, max_reject);
@@ -548,6 +617,7 @@ __device__ __forceinline__ void ts_commit_pair_body(Dom d, const float* __restri
     const double cx = ((dt * c_ts_b[0] + dt * c_ts_b[3]) + dt * c_ts_b[4]) + dt * c_ts_b[5];
     const float cxf = (float)cx;
     const float cmf = c->plain ? 0.f : (float)block_corner_mean(raw, d.nx, d.ny), spyf = (float)d.spy;
+#pragma unroll 4
     for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
         const float k = (raw[e] - cmf) * spyf;
         const double x2 = d.x[e] + cx * (double)k;
@@ -965,9 +1035,9 @@ int ts_grid(size_t n)
 
 // ---- batched Tsit5 attempt over the members of an ensemble -----------------
 template <typename T>
-__global__ void __launch_bounds__(NT) k_b_ts_max(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+__global__ void __launch_bounds__(NT) k_b_ts_max(const BMember* __restrict__ M, BList L)
 {
-    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
         const BMember& b = M[m];
         ts_max_body<T>(b.d, (const T*)b.raw, b.atol, b.rtol, local, b.red_nblk);
         __syncthreads();
@@ -976,9 +1046,9 @@ __global__ void __launch_bounds__(NT) k_b_ts_max(const BMember* __restrict__ M, 
 
 template <typename T>
 __global__ void __launch_bounds__(NT)
-k_b_ts_err(const BMember* __restrict__ M, const int* __restrict__ off, int nm, int max_reject)
+k_b_ts_err(const BMember* __restrict__ M, BList L, int max_reject)
 {
-    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
         const BMember& b = M[m];
         ts_err_body<T>(b.d, (const T*)b.raw, b.q, b.dt_max, max_reject, local, b.red_nblk);
         __syncthreads();
@@ -986,9 +1056,9 @@ k_b_ts_err(const BMember* __restrict__ M, const int* __restrict__ off, int nm, i
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NT) k_b_ts_commit(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+__global__ void __launch_bounds__(NT) k_b_ts_commit(const BMember* __restrict__ M, BList L)
 {
-    batch_walk(off, nm, [&](int m) { const Ctl* c = M[m].d.ctl; return c->done == 0 && c->accepted != 0; },
+    batch_walk(L, [&](int m) { const Ctl* c = M[m].d.ctl; return c->done == 0 && c->accepted != 0; },
                [&](int m, int local) {
                    const BMember& b = M[m];
                    ts_commit_body<T>(b.d, (const T*)b.raw, local, b.red_nblk);
@@ -996,18 +1066,18 @@ __global__ void __launch_bounds__(NT) k_b_ts_commit(const BMember* __restrict__ 
 }
 
 __global__ void __launch_bounds__(NT)
-k_b_ts_fused(const BMember* __restrict__ M, const int* __restrict__ off, int nm, int max_reject)
+k_b_ts_fused(const BMember* __restrict__ M, BList L, int max_reject)
 {
-    batch_walk(off, nm, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
         const BMember& b = M[m];
         ts_fused_body(b.d, (const float*)b.raw, b.atol, b.rtol, b.q, b.dt_max, max_reject, local, b.red_nblk);
         __syncthreads();
     });
 }
 
-__global__ void __launch_bounds__(NT) k_b_ts_commit_pair(const BMember* __restrict__ M, const int* __restrict__ off, int nm)
+__global__ void __launch_bounds__(NT) k_b_ts_commit_pair(const BMember* __restrict__ M, BList L)
 {
-    batch_walk(off, nm, [&](int m) { const Ctl* c = M[m].d.ctl; return c->done == 0 && c->accepted != 0; },
+    batch_walk(L, [&](int m) { const Ctl* c = M[m].d.ctl; return c->done == 0 && c->accepted != 0; },
                [&](int m, int local) {
                    const BMember& b = M[m];
                    ts_commit_pair_body(b.d, (const float*)b.raw, local, b.red_nblk);
@@ -1040,10 +1110,54 @@ __global__ void k_b_loop_begin(const BMember* __restrict__ M, int nm)
     c->need_rhs = 0;
 }
 
-__global__ void k_b_attempt_begin(const BMember* __restrict__ M, int nm, int max_iter)
+// One block: attempt_begin of every member, then the compacted lists of the
+// members that need an RHS (kinds 0-2) and that have an attempt (kind 3),
+// with the prefix sums of their virtual blocks, in member order.
+__global__ void k_b_attempt_begin(const BMember* __restrict__ M, int nm, int max_iter, const int* __restrict__ off,
+                                  int* __restrict__ cl)
 {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m < nm) attempt_begin_one(M[m].d.ctl, max_iter);
+    extern __shared__ int sh_cl[];
+    int* fl = sh_cl;        // bit 0: needs an RHS, bit 1: has an attempt
+    int* cn = sh_cl + nm;   // virtual blocks of member m for kind k at cn[k nm + m]
+    for (int m = threadIdx.x; m < nm; m += blockDim.x) {
+        Ctl* c = M[m].d.ctl;
+        attempt_begin_one(c, max_iter);
+        fl[m] = (c->need_rhs ? 1 : 0) | (c->done == 0 ? 2 : 0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cn[k * nm + m] = off[k * (nm + 1) + m + 1] - off[k * (nm + 1) + m];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int* idsR = cl + 2;
+        int* idsT = cl + 2 + nm;
+        int* co = cl + 2 + 2 * nm;
+        int nR = 0, nT = 0, a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        co[0] = 0;
+        co[nm + 1] = 0;
+        co[2 * (nm + 1)] = 0;
+        co[3 * (nm + 1)] = 0;
+        for (int m = 0; m < nm; ++m) {
+            const int f = fl[m];
+            if (f & 1) {
+                idsR[nR] = m;
+                a0 += cn[m];
+                a1 += cn[nm + m];
+                a2 += cn[2 * nm + m];
+                ++nR;
+                co[nR] = a0;
+                co[(nm + 1) + nR] = a1;
+                co[2 * (nm + 1) + nR] = a2;
+            }
+            if (f & 2) {
+                idsT[nT] = m;
+                a3 += cn[3 * nm + m];
+                ++nT;
+                co[3 * (nm + 1) + nT] = a3;
+            }
+        }
+        cl[0] = nR;
+        cl[1] = nT;
+    }
 }
 
 // continue while any member has an attempt left
@@ -1068,43 +1182,43 @@ __global__ void k_b_set_args(const BArgs* __restrict__ a, int nm)
     if (m < nm) set_args_one(a[m].ctl, a[m].tf, a[m].bsl, a[m].A_ocean, a[m].method, a[m].write_bsl);
 }
 
-template <typename T> void batch_ts_max(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s)
+template <typename T> void batch_ts_max(const BMember* M, BList L, int nblk, cudaStream_t s)
 {
-    k_b_ts_max<T><<<nblk, NT, 0, s>>>(M, off, nm);
+    k_b_ts_max<T><<<nblk, NT, 0, s>>>(M, L);
 }
 template <typename T>
-void batch_ts_err(const BMember* M, const int* off, int nm, int nblk, int max_reject, cudaStream_t s)
+void batch_ts_err(const BMember* M, BList L, int nblk, int max_reject, cudaStream_t s)
 {
-    k_b_ts_err<T><<<nblk, NT, 0, s>>>(M, off, nm, max_reject);
+    k_b_ts_err<T><<<nblk, NT, 0, s>>>(M, L, max_reject);
 }
-void batch_ts_fused(const BMember* M, const int* off, int nm, int nblk, int max_reject, cudaStream_t s)
+void batch_ts_fused(const BMember* M, BList L, int nblk, int max_reject, cudaStream_t s)
 {
-    k_b_ts_fused<<<nblk, NT, 0, s>>>(M, off, nm, max_reject);
+    k_b_ts_fused<<<nblk, NT, 0, s>>>(M, L, max_reject);
 }
-void batch_ts_commit_pair(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s)
+void batch_ts_commit_pair(const BMember* M, BList L, int nblk, cudaStream_t s)
 {
-    k_b_ts_commit_pair<<<nblk, NT, 0, s>>>(M, off, nm);
+    k_b_ts_commit_pair<<<nblk, NT, 0, s>>>(M, L);
 }
-template <typename T> void batch_ts_commit(const BMember* M, const int* off, int nm, int nblk, cudaStream_t s)
+template <typename T> void batch_ts_commit(const BMember* M, BList L, int nblk, cudaStream_t s)
 {
-    k_b_ts_commit<T><<<nblk, NT, 0, s>>>(M, off, nm);
+    k_b_ts_commit<T><<<nblk, NT, 0, s>>>(M, L);
 }
 void batch_loop_begin(const BMember* M, int nm, cudaStream_t s) { k_b_loop_begin<<<(nm + 127) / 128, 128, 0, s>>>(M, nm); }
-void batch_attempt_begin(const BMember* M, int nm, int max_iter, cudaStream_t s)
+void batch_attempt_begin(const BMember* M, int nm, int max_iter, const int* off, int* cl, cudaStream_t s)
 {
-    k_b_attempt_begin<<<(nm + 127) / 128, 128, 0, s>>>(M, nm, max_iter);
+    k_b_attempt_begin<<<1, 256, 5 * (size_t)nm * sizeof(int), s>>>(M, nm, max_iter, off, cl);
 }
 void batch_attempt_end(const BMember* M, int nm, cudaGraphConditionalHandle loop, cudaStream_t s, int* more_out)
 {
     k_b_attempt_end<<<1, 256, 0, s>>>(M, nm, loop, more_out);
 }
 void batch_set_args(const BArgs* a, int nm, cudaStream_t s) { k_b_set_args<<<(nm + 127) / 128, 128, 0, s>>>(a, nm); }
-template void batch_ts_max<float>(const BMember*, const int*, int, int, cudaStream_t);
-template void batch_ts_max<double>(const BMember*, const int*, int, int, cudaStream_t);
-template void batch_ts_err<float>(const BMember*, const int*, int, int, int, cudaStream_t);
-template void batch_ts_err<double>(const BMember*, const int*, int, int, int, cudaStream_t);
-template void batch_ts_commit<float>(const BMember*, const int*, int, int, cudaStream_t);
-template void batch_ts_commit<double>(const BMember*, const int*, int, int, cudaStream_t);
+template void batch_ts_max<float>(const BMember*, BList, int, cudaStream_t);
+template void batch_ts_max<double>(const BMember*, BList, int, cudaStream_t);
+template void batch_ts_err<float>(const BMember*, BList, int, int, cudaStream_t);
+template void batch_ts_err<double>(const BMember*, BList, int, int, cudaStream_t);
+template void batch_ts_commit<float>(const BMember*, BList, int, cudaStream_t);
+template void batch_ts_commit<double>(const BMember*, BList, int, cudaStream_t);
 
 int reduce_blocks(size_t n) { return grid_for(n); }
 

@@ -140,11 +140,13 @@ class Ensemble:
     groups > 1 the members are sorted by an estimate of their stiffness
     (max D / (eta dx^3), which sets how many attempts an update needs) and
     split into that many groups, each a batch on its own stream, so a stiff
-    member holds back only the members of its own group.
+    member holds back only the members of its own group; with `priority`
+    the stiffest group's stream has the device's highest priority.
     mode "streams": fi_batch_update enqueues one isos_update per member on
     the member's own stream (any integrator)."""
 
-    def __init__(self, workloads, precision: int = 1, mode: str = "graph", groups: int = 1):
+    def __init__(self, workloads, precision: int = 1, mode: str = "graph", groups: int = 1,
+                 priority: bool = True):
         from .isostasy import Domain
         self.L = _lib.load()
         self.mode = mode
@@ -179,12 +181,18 @@ class Ensemble:
         self.hss = [(C.c_void_p * len(m))(*[self.doms[i].h.value for i in m]) for m in self.groups]
         self.batches = []
         if mode == "graph":
-            for hs, m in zip(self.hss, self.groups):
+            for g, (hs, m) in enumerate(zip(self.hss, self.groups)):
                 bh = C.c_void_p()
                 rc = self.L.fi_batch_create(hs, len(m), C.byref(bh))
                 if rc:
                     raise FiError(rc, "fi_batch_create")
                 self.batches.append(bh)
+                if g == 0 and len(self.groups) > 1 and priority:
+                    # the stiffest group has the longest chain of attempts:
+                    # its launches go first, the other groups fill idle SMs
+                    rc = self.L.fi_batch_set_priority(bh, 1)
+                    if rc:
+                        raise FiError(rc, "fi_batch_set_priority")
         self.t = 0.0
 
     def bsl_of(self, i):

@@ -237,11 +237,19 @@ int fi_batch_synchronize(fi_handle* const* hs, int n, int32_t* status);
  * branches, then the adaptive Tsit5 attempts of all members in one loop of
  * batched launches (each launch covers every member that still has an
  * attempt left; accept/reject and step sizes stay per member), then the
- * update tails.  Each member's result is bit-identical to driving it alone.
- * The members' load is the one they hold.  Do not drive members on their own
+ * update tails.  Each member's result is bit-identical to driving it alone
+ * in FP64; in the mixed form the batched kernels may contract FP32
+ * multiply-adds differently, so results agree to that rounding.  The
+ * members' load is the one they hold.  Do not drive members on their own
  * while a batch step is in flight (fi_batch_wait first). */
 typedef struct fi_batch fi_batch;
-int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out);
+int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out);   /* 1 <= n <= 2048 */
+/* Scheduling priority of a batch's launches (no reference counterpart):
+ * level 0 normal, 1 high (the device's greatest stream priority).  Several
+ * batches stepping together (an ensemble split into groups) let the group
+ * with the longest chain of attempts go first while the others fill the
+ * SMs it leaves idle.  Only before the batch's first fi_batch_step. */
+int fi_batch_set_priority(fi_batch* b, int level);
 int fi_batch_step(fi_batch* b, double time, fi_bsl* bsl);
 int fi_batch_wait(fi_batch* b, int32_t* status);
 int fi_batch_destroy(fi_batch* b);

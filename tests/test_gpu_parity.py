@@ -319,3 +319,45 @@ def test_device_analytical_disk():
     dom.close()
     zb = out["z_bed"] - 1e6
     assert abs(zb.min() - got.min()) <= 0.03 * abs(got.min())
+
+
+def _tsit_run(wl, precision, eta_scale=1.0, times=(10.0, 20.0, 30.0, 40.0)):
+    dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=precision)
+    f = wl.padded_fields(dom.nx, dom.ny)
+    if "eta_eff" in f:
+        f["eta_eff"] = f["eta_eff"] * eta_scale
+    if f:
+        dom.set_fields(**f)
+    b = gpu_bsl()
+    dom.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+    for t in times:
+        dom.update(wl.H_final, t, b)
+    w = dom.field("w")
+    dom.close()
+    return w
+
+
+@pytest.mark.parametrize("member", [None, 7, 3])
+def test_mixed_reference_tsit54_against_fp64(member):
+    """Reference-compatible Tsit5 in the mixed form (now%w as a float pair,
+    column-strip stencil, one-pass error norm) against the FP64 form over a
+    few coupling steps: within the mixed-form bound."""
+    if member is None:
+        wl = W.config1(56)
+        wl.params["stage_mode"] = 0
+    else:
+        wl = W.ensemble_member(member, stage_mode=0)
+    assert rel(_tsit_run(wl, 1), _tsit_run(wl, 0)) <= TOLMIX
+
+
+def test_reference_tsit54_stability_edge_sensitivity():
+    """The reference's Tsit5 evaluates one RHS per attempt (every stage
+    takes k(x)), so x2 is a forward-Euler step and the error estimate
+    0.2 dt |k| bounds the increment, not the stability of the stiff modes.
+    On a stiff member (384^2, eta down to ~1e20) the accepted steps ride the
+    stability edge and the FP64 form itself moves by far more than 1e-5 of
+    max|w| when eta changes by 1e-12: no precision can be held to the mixed
+    bound there, which is why the bound above is checked on members off
+    that edge."""
+    wl = W.ensemble_member(2, stage_mode=0)
+    assert rel(_tsit_run(wl, 0, eta_scale=1.0 + 1e-12), _tsit_run(wl, 0)) > 1e-3
