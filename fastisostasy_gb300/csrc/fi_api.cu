@@ -311,23 +311,6 @@ int make_plan(fi_handle* h, int nx, int ny, Plan2D& P)
 // ---- init-time physics (host, double) ---------------------------------------
 double rigidity(double E, double He, double nu) { return E * 1e9 * (He * He * He) / (12.0 * (1.0 - nu * nu)); }
 
-// Gaussian bump over the padded domain as in calc_gaussian_thickness /
-// calc_gaussian_viscosity (src/isos_utils.f90:960-1035).
-void gauss_bump(const fi_handle* h, const std::vector<double>& xc, const std::vector<double>& yc,
-                std::vector<double>& out)
-{
-    const int nx = h->nx, ny = h->ny;
-    const double xcntr = (xc[nx - 1] + xc[0]) / 2.0, ycntr = (yc[ny - 1] + yc[0]) / 2.0;
-    const double Lx = (xc[nx - 1] - xc[0]) / 2., Ly = (yc[ny - 1] - yc[0]) / 2.;
-    const double s11 = (4.0 / Lx) * (4.0 / Lx), s22 = (4.0 / Ly) * (4.0 / Ly);
-    out.assign(h->n, 0.0);
-    for (int i = 0; i < nx; ++i)
-        for (int j = 0; j < ny; ++j) {
-            const double d1 = xc[i] - xcntr, d2 = yc[j] - ycntr;
-            out[(size_t)j * nx + i] = std::exp(-0.5 * (d1 * (s11 * d1 + 0.0 * d2) + d2 * (0.0 * d1 + s22 * d2)));
-        }
-}
-
 // Kelvin function kei for LV-ELRA.  The reference interpolates a table of
 // kei(x) at x = 0, 0.01, .., 10 printed with five significant digits and
 // stored as single-precision literals (src/kelvin_function.f90:91-132,
@@ -381,6 +364,28 @@ const KeiTable& kei_table()
     return t;
 }
 
+void fill_rheo_params(const fi_handle* h, RheoParams& P)
+{
+    const fi_params& p = h->p;
+    P.nx = h->nx;
+    P.ny = h->ny;
+    P.method = p.method;
+    P.lithosphere = p.lithosphere;
+    P.mantle = p.mantle;
+    P.layering = p.layering;
+    P.lumping = p.lumping;
+    P.nl = p.nl;
+    P.visc_scaling_method = p.visc_scaling_method;
+    for (int k = 0; k < 8; ++k) { P.zl[k] = p.zl[k]; P.viscosities[k] = p.viscosities[k]; }
+    P.dl = p.dl;
+    P.E = p.E;
+    P.nu = p.nu;
+    P.viscosity_scaling = p.viscosity_scaling;
+    P.cc = h->cc;
+    P.eta_ref = p.eta_ref;
+    P.big_he = sp(100e3);   // calc_gaussian_thickness amplitude (src/fastisostasy.f90:250-260)
+}
+
 void host_fields(fi_handle* h)
 {
     const fi_params& p = h->p;
@@ -396,86 +401,12 @@ void host_fields(fi_handle* h)
     h->GN.assign(n, 0.0);
     h->init_rc = init_fields_device(h->nx, h->ny, h->dx, h->dy, PI_LIT, sp(1.e-12), sp(9.81), p.r_earth, p.m_earth,
                                     kRn, kGe, h->kappa.data(), h->GE.data(), h->GN.data(), h->s);
-    if (p.method == 3 && (p.lithosphere == 1 || p.lithosphere == 2)) {
-        std::vector<double> g;
-        gauss_bump(h, h->xc, h->yc, g);
-        double mx = -1e300;
-        for (double v : g) mx = v > mx ? v : mx;
-        const double sgn = p.lithosphere == 1 ? 1.0 : -1.0;
-        for (size_t e = 0; e < n; ++e) {
-            h->He[e] = p.zl[0] + sgn * sp(100e3) * (g[e] / mx);
-            h->D[e] = rigidity(p.E, h->He[e], p.nu);
-        }
-    }
-    const int nl = p.nl;
-    if (p.method != 3) {
-        // methods 0-2 use no viscosity field
-    } else if (p.mantle == 0) {
-        // calc_effective_viscosity, src/lv_elva.f90:207-306
-        std::vector<double> bnd((size_t)nl * n);
-        for (size_t e = 0; e < n; ++e) bnd[e] = h->He[e];
-        for (int k = 1; k < nl; ++k)
-            for (size_t e = 0; e < n; ++e)
-                bnd[(size_t)k * n + e] = (p.layering == 1) ? bnd[(size_t)(k - 1) * n + e] + p.dl : p.zl[k];
-        {
-            // the layer viscosities are the same in every cell: lump once
-            double mn = p.viscosities[0], mxv = p.viscosities[0], s = 0.0, ls = 0.0;
-            for (int k = 0; k < nl; ++k) {
-                const double v = p.viscosities[k];
-                mn = v < mn ? v : mn;
-                mxv = v > mxv ? v : mxv;
-                s += v;
-                ls += std::log10(v);
-            }
-            double v = p.viscosities[nl - 1];
-            switch (p.lumping) {
-            case 1: v = mn; break;
-            case 2: v = mxv; break;
-            case 3: v = s / (double)nl; break;
-            case 4: v = std::pow(10.0, ls / (double)nl); break;
-            default: break;
-            }
-            h->eta_eff.assign(n, v);
-        }
-        if (p.lumping == 5 && nl > 1) {
-            for (int k = nl - 1; k >= 1; --k)
-                for (size_t e = 0; e < n; ++e) {
-                    const double dz = bnd[(size_t)k * n + e] - bnd[(size_t)(k - 1) * n + e];
-                    const double er = p.viscosities[k - 1] / h->eta_eff[e], ir = 1. / er;
-                    const double kz = dz * h->kappa[e];
-                    const double c = std::cosh(kz), s = std::sinh(kz);
-                    h->R[e] = h->R[e] * (2 * er * c * s + (1 - er * er) * (kz * kz) + (er * s) * (er * s) + c * c) /
-                              ((er + ir) * c * s + (er - ir) * dz * h->kappa[e] + s * s + c * c);
-                }
-        }
-    } else if (p.mantle == 1 || p.mantle == 2) {
-        std::vector<double> g;
-        // gaussian_plus passes yc = xc (src/fastisostasy.f90:329-330)
-        gauss_bump(h, h->xc, p.mantle == 1 ? h->xc : h->yc, g);
-        const double sgn = p.mantle == 1 ? 1.0 : -1.0;
-        for (size_t e = 0; e < n; ++e) h->eta_eff[e] = p.viscosities[0] * std::pow(10.0, sgn * g[e]);
-    }
-    // viscosity scaling, src/fastisostasy.f90:425-436
-    if (p.visc_scaling_method == 2 || p.visc_scaling_method == 3) {
-        double v = h->eta_eff[0];
-        for (double e : h->eta_eff) v = (p.visc_scaling_method == 2) ? (e < v ? e : v) : (e > v ? e : v);
-        for (double& e : h->eta_eff) e = v;
-    } else if (p.visc_scaling_method == 1) {
-        for (double& e : h->eta_eff) e = e * p.viscosity_scaling;
-    }
-    for (double& e : h->eta_eff) e = e * h->cc;
-    {
-        // :441-442, evaluated once per run of equal values (uniform fields are common)
-        double last_in = 0.0, last_out = 0.0;
-        bool have = false;
-        for (double& e : h->eta_eff) {
-            if (!have || e != last_in) {
-                last_in = e;
-                last_out = std::exp(std::log10(p.eta_ref / e)) * e;
-                have = true;
-            }
-            e = last_out;
-        }
+    // He, D and (method 3) eta_eff, R on the device: src/fastisostasy.f90:240-443
+    if (!h->init_rc) {
+        RheoParams P;
+        fill_rheo_params(h, P);
+        h->init_rc = rheology_device(P, h->xc.data(), h->yc.data(), h->dx, h->kappa.data(), nullptr, h->He.data(),
+                                     h->D.data(), h->eta_eff.data(), h->R.data(), h->s);
     }
     const int nx = h->nx, ny = h->ny;
     const double dx = h->dx;
