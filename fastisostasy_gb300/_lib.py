@@ -32,7 +32,7 @@ EXPORTS = ["fi_create", "fi_destroy", "fi_dims", "fi_set_fields", "fi_set_kernel
            "fi_padded_dims", "fi_serve_create", "fi_serve_submit", "fi_serve_info", "fi_serve_wait",
            "fi_serve_result", "fi_serve_clock", "fi_serve_destroy", "fi_batch_update", "fi_batch_synchronize",
            "fi_batch_create", "fi_batch_step", "fi_batch_wait", "fi_batch_destroy", "fi_elva_disk",
-           "fi_batch_set_priority"]
+           "fi_batch_set_priority", "fi_set_rheology"]
 
 PROFILE_KERNELS = ["flexure", "rows_fwd", "cols_hartley", "rows_inv", "conv_rows_fwd", "conv_cols",
                    "conv_rows_inv", "rk_stage", "rk_final", "upd_begin", "upd_masks", "upd_litho",
@@ -55,6 +55,15 @@ class FiParams(C.Structure):
         ("m_earth", C.c_double), ("atol", C.c_double), ("rtol", C.c_double),
         ("dt_min", C.c_double), ("dt_max", C.c_double), ("dt_init", C.c_double), ("q", C.c_double), ("tau", C.c_double),
     ]
+
+
+class FiRheology(C.Structure):
+    """fi_rheology: the arrays of a rheology file (x fastest)."""
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("xc", C.POINTER(C.c_double)), ("yc", C.POINTER(C.c_double)), ("zc", C.POINTER(C.c_double)),
+                ("litho_thickness", C.POINTER(C.c_double)), ("litho_thickness_scaling", C.c_double),
+                ("log10_viscosity", C.POINTER(C.c_double)), ("stddev_log10_viscosity", C.POINTER(C.c_double)),
+                ("stddev_scaling", C.c_int32), ("rheo_smoothing_radius", C.c_double)]
 
 
 class FiBsl(C.Structure):
@@ -111,6 +120,7 @@ def load(build_if_missing: bool = True):
     L.fi_destroy.argtypes = [H]
     L.fi_dims.argtypes = [H, C.POINTER(C.c_int32)]
     L.fi_set_fields.argtypes = [H, _dp, _dp, _dp, _u8]
+    L.fi_set_rheology.argtypes = [H, C.POINTER(FiRheology)]
     L.fi_set_kernels.argtypes = [H, _dp, _dp]
     L.fi_init_ref.argtypes = [H, _dp, _dp, C.c_double, _dp]
     L.fi_init_state.argtypes = [H, _dp, _dp, C.c_double, C.POINTER(FiBsl)]

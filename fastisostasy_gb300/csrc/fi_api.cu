@@ -1261,6 +1261,46 @@ int fi_set_fields(fi_handle* h, const double* D_lith, const double* eta_eff, con
     return upload_static(h);
 }
 
+int fi_set_rheology(fi_handle* h, const fi_rheology* r)
+{
+    if (!h || !r) return FI_E_ARG;
+    if (h->p.method != 3) return fail(h, FI_E_ARG, "fi_set_rheology: LV-ELVA (method 3) only");
+    if (!r->litho_thickness && !r->log10_viscosity) return FI_OK;
+    if (r->nx < 2 || r->ny < 2 || !r->xc || !r->yc || (r->log10_viscosity && (r->nz < 1 || !r->zc)))
+        return fail(h, FI_E_ARG, "fi_set_rheology: file grid");
+    RheoParams P;
+    fill_rheo_params(h, P);
+    RheoFile F;
+    F.nxr = r->nx;
+    F.nyr = r->ny;
+    F.nzr = r->nz;
+    F.xr = r->xc;
+    F.yr = r->yc;
+    F.zr = r->zc;
+    F.thick = r->litho_thickness;
+    F.thick_scale = r->litho_thickness_scaling;
+    F.log10_eta = r->log10_viscosity;
+    F.stddev = r->stddev_log10_viscosity;
+    F.use_stddev = r->stddev_scaling;
+    F.smooth_radius = r->rheo_smoothing_radius;
+    std::vector<double> He(h->He), D(h->D), eta(h->eta_eff), R(h->R);
+    // without a thickness in the file, He (and so the layer boundaries)
+    // follows the lithosphere code as at creation
+    const int rc = rheology_device(P, h->xc.data(), h->yc.data(), h->dx, h->kappa.data(), &F, He.data(), D.data(),
+                                   eta.data(), R.data(), h->s);
+    if (rc == 2) return fail(h, FI_E_ARG, "fi_set_rheology: smoothing window wider than the grid");
+    if (rc) return fail(h, FI_E_CUDA, "fi_set_rheology: device error");
+    if (r->litho_thickness) {
+        h->He.swap(He);
+        h->D.swap(D);
+    }
+    if (r->log10_viscosity) {
+        h->eta_eff.swap(eta);
+        h->R.swap(R);
+    }
+    return upload_static(h);
+}
+
 int fi_set_kernels(fi_handle* h, const double* GE, const double* GN)
 {
     if (!h) return FI_E_ARG;

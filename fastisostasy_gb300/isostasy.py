@@ -113,6 +113,30 @@ class Domain:
             m = mm.ctypes.data_as(C.POINTER(C.c_uint8))
         self._check(self.L.fi_set_fields(self.h, p(D_lith), p(eta_eff), p(R), m))
 
+    def set_rheology(self, xc, yc, zc=None, litho_thickness=None, litho_thickness_scaling=1.0,
+                     log10_viscosity=None, stddev_log10_viscosity=None, stddev_scaling=False,
+                     rheo_smoothing_radius=0.0):
+        """The rheology_file branches of isos_init from a file's arrays:
+        litho_thickness (ny, nx), log10_viscosity / its stddev (nz, ny, nx),
+        coordinates ascending (fi_set_rheology)."""
+        keep = []
+
+        def p(a):
+            if a is None:
+                return None
+            a = _f64(a)
+            keep.append(a)
+            return _dp(a)
+        r = _lib.FiRheology()
+        r.nx, r.ny = len(xc), len(yc)
+        r.nz = 0 if zc is None else len(zc)
+        r.xc, r.yc, r.zc = p(xc), p(yc), p(zc)
+        r.litho_thickness, r.litho_thickness_scaling = p(litho_thickness), float(litho_thickness_scaling)
+        r.log10_viscosity, r.stddev_log10_viscosity = p(log10_viscosity), p(stddev_log10_viscosity)
+        r.stddev_scaling = 1 if stddev_scaling else 0
+        r.rheo_smoothing_radius = float(rheo_smoothing_radius)
+        self._check(self.L.fi_set_rheology(self.h, C.byref(r)))
+
     def set_kernels(self, GE=None, GN=None):
         a = _f64(GE) if GE is not None else None
         b = _f64(GN) if GN is not None else None

@@ -115,6 +115,31 @@ int fi_dims(const fi_handle* h, int32_t* out8);
  * Any pointer may be NULL (kept). */
 int fi_set_fields(fi_handle* h, const double* D_lith, const double* eta_eff, const double* R,
                   const uint8_t* maskactive);
+/* The rheology_file branches of isos_init (lithosphere and/or mantle =
+ * "rheology_file", src/fastisostasy.f90:262-290, 340-420), from the arrays
+ * its NetCDF reader returns (coordinates and fields as nc_read_and_scale_*
+ * leaves them; fields x fastest, then y, then z).  On the device:
+ * bilinear_interpolation onto the padded grid (single precision, flat
+ * beyond the file's grid; src/isos_utils.f90:495-575), smooth_gauss_2D when
+ * rheo_smoothing_radius > 0 (src/isos_utils.f90:696-819), the rigidity; per
+ * file level the interpolated log10 viscosity (+ viscosity_scaling x its
+ * stddev when stddev_scaling), clamped to [16, 23], interpolated in depth to
+ * the layer boundaries (interp_0d), 10**, lumped (freqdomain R), smoothed;
+ * then the viscosity scaling, compressibility and eta_ref transform.
+ * Replaces the handle's lithosphere thickness and D_lith (thickness given)
+ * and eta_eff and R (viscosity given).  Method 3 only.  FI_E_ARG for a
+ * smoothing window wider than the grid (the reference stops there). */
+typedef struct {
+    int32_t nx, ny, nz;                   /* file grid */
+    const double *xc, *yc, *zc;           /* ascending */
+    const double* litho_thickness;        /* nx*ny, or NULL */
+    double litho_thickness_scaling;
+    const double* log10_viscosity;        /* nx*ny*nz, or NULL */
+    const double* stddev_log10_viscosity; /* nx*ny*nz, or NULL */
+    int32_t stddev_scaling;               /* viscosity_scaling_method = "stddev" */
+    double rheo_smoothing_radius;         /* [m]; 0: none */
+} fi_rheology;
+int fi_set_rheology(fi_handle* h, const fi_rheology* r);
 /* Replace the elastic (GE) and geoid (GN) Green's functions (padded (nx, ny),
  * centred like calc_elastic_green, src/green_functions.f90:43-91);
  * spectra are recomputed.  Either may be NULL. */

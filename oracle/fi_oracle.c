@@ -1414,3 +1414,147 @@ int orc_get_scalars(const orc_model *m, double *o)
     o[11] = m->sec_per_year; o[12] = m->cc; o[13] = m->Vden; o[14] = (double)m->M; o[15] = m->ref.bsl;
     return 0;
 }
+
+/* ---- rheology_file branch (src/fastisostasy.f90:262-420) ------------------ */
+
+/* bilinear_interpolation (src/isos_utils.f90:495-559): its arguments are
+ * declared `real`, so the arithmetic is single precision; the grid cell is
+ * found by the routine's linear scan. */
+static float orc_bilinear_one(const float *x, int nxr, const float *y, int nyr, const float *z, float xo, float yo)
+{
+    const float tol = 1.0f;
+    int i = 0, j = 0, flat = 0;
+    float tx = 0.f, ty = 0.f;
+    if (xo <= x[0] + tol) { i = 0; flat = 1; }
+    else if (xo >= x[nxr - 1] - tol) { i = nxr - 1; flat = 1; }
+    else {
+        for (i = 0; i < nxr - 1; i++)
+            if (xo > x[i] && xo <= x[i + 1]) break;
+        tx = (xo - x[i]) / (x[i + 1] - x[i]);
+    }
+    if (yo <= y[0] + tol) { j = 0; flat = 1; }
+    else if (yo >= y[nyr - 1] - tol) { j = nyr - 1; flat = 1; }
+    else {
+        for (j = 0; j < nyr - 1; j++)
+            if (yo > y[j] && yo <= y[j + 1]) break;
+        ty = (yo - y[j]) / (y[j + 1] - y[j]);
+    }
+    if (flat) return z[(size_t)j * nxr + i];
+    {
+        const float z11 = z[(size_t)j * nxr + i], z21 = z[(size_t)j * nxr + i + 1];
+        const float z12 = z[(size_t)(j + 1) * nxr + i], z22 = z[(size_t)(j + 1) * nxr + i + 1];
+        return z11 * (1.0f - tx) * (1.0f - ty) + z21 * tx * (1.0f - ty) + z12 * (1.0f - tx) * ty + z22 * tx * ty;
+    }
+}
+
+/* bilinear_interpolation_array (src/isos_utils.f90:561-575) */
+void orc_bilinear_array(const double *x, int nxr, const double *y, int nyr, const double *z,
+                        const double *xo, int nx, const double *yo, int ny, double *out)
+{
+    float *fx = (float *)malloc(sizeof(float) * nxr), *fy = (float *)malloc(sizeof(float) * nyr);
+    float *fz = (float *)malloc(sizeof(float) * (size_t)nxr * nyr);
+    size_t q;
+    int i, j;
+    for (i = 0; i < nxr; i++) fx[i] = (float)x[i];
+    for (j = 0; j < nyr; j++) fy[j] = (float)y[j];
+    for (q = 0; q < (size_t)nxr * nyr; q++) fz[q] = (float)z[q];
+    for (j = 0; j < ny; j++)
+        for (i = 0; i < nx; i++)
+            out[(size_t)j * nx + i] = (double)orc_bilinear_one(fx, nxr, fy, nyr, fz, (float)xo[i], (float)yo[j]);
+    free(fx); free(fy); free(fz);
+}
+
+/* interp_0d (src/isos_utils.f90:423-457) */
+double orc_interp_0d(const double *x, const double *y, int n, double xout)
+{
+    int j;
+    if (xout < x[0]) return y[0];
+    if (xout > x[n - 1]) return y[n - 1];
+    for (j = 0; j < n; j++)
+        if (x[j] >= xout) break;
+    if (j == 0) return y[0];
+    if (j == n) return y[n - 1];
+    {
+        const double alpha = (xout - x[j - 1]) / (x[j] - x[j - 1]);
+        return y[j - 1] + alpha * (y[j] - y[j - 1]);
+    }
+}
+
+/* smooth_gauss_2D (src/isos_utils.f90:696-819) with gauss_values
+ * (:918-958): the window of half-width ceiling(2 sigma / dx), mirror
+ * extension, the filter normalised in gauss_values and again before use,
+ * sums in column-major order.  Returns 1 where the reference stops
+ * ("Missing points!": the window reaches beyond the mirrored band). */
+int orc_smooth_gauss_2d(double *var, int nx, int ny, double dx, double sigma)
+{
+    const int n2 = (int)ceil(2.0 * sigma / dx), n = 2 * n2 + 1;
+    double *filt, *out, s = 0.0;
+    int a, b, i, j;
+    if (n2 >= nx || n2 >= ny) return 1;
+    filt = (double *)malloc(sizeof(double) * (size_t)n * n);
+    out = (double *)malloc(sizeof(double) * (size_t)nx * ny);
+    for (b = -n2; b <= n2; b++)
+        for (a = -n2; a <= n2; a++) {
+            const double x = a * dx, y = b * dx;
+            filt[(size_t)(b + n2) * n + (a + n2)] =
+                1.0 / (2.0 * PI_LIT * sigma * sigma) * exp(-(x * x + y * y) / (2 * sigma * sigma));
+        }
+    for (a = 0; a < n * n; a++) s += filt[a];
+    for (a = 0; a < n * n; a++) filt[a] /= s;
+    s = 0.0;
+    for (a = 0; a < n * n; a++) s += filt[a];
+    for (a = 0; a < n * n; a++) filt[a] /= s;
+    for (j = 0; j < ny; j++)
+        for (i = 0; i < nx; i++) {
+            double acc = 0.0;
+            for (b = -n2; b <= n2; b++) {
+                int jj = j + b;
+                jj = jj < 0 ? -1 - jj : (jj >= ny ? 2 * ny - 1 - jj : jj);
+                for (a = -n2; a <= n2; a++) {
+                    int ii = i + a;
+                    ii = ii < 0 ? -1 - ii : (ii >= nx ? 2 * nx - 1 - ii : ii);
+                    acc += var[(size_t)jj * nx + ii] * filt[(size_t)(b + n2) * n + (a + n2)];
+                }
+            }
+            out[(size_t)j * nx + i] = acc;
+        }
+    memcpy(var, out, sizeof(double) * (size_t)nx * ny);
+    free(filt); free(out);
+    return 0;
+}
+
+/* calc_effective_viscosity with per-cell layer viscosities eta3 (nl x n)
+ * and layer boundaries bnd (nl x n) (src/lv_elva.f90:207-306); R starts at 1. */
+void orc_lump3(const double *eta3, const double *bnd, const double *kappa, int n, int nl, int lumping,
+               double *eta_eff, double *R)
+{
+    int e, k;
+    for (e = 0; e < n; e++) {
+        double mn = eta3[e], mx = eta3[e], sm = 0.0, ls = 0.0, v, r = 1.0;
+        for (k = 0; k < nl; k++) {
+            const double q = eta3[(size_t)k * n + e];
+            mn = q < mn ? q : mn;
+            mx = q > mx ? q : mx;
+            sm += q;
+            ls += log10(q);
+        }
+        v = eta3[(size_t)(nl - 1) * n + e];
+        switch (lumping) {
+        case 1: v = mn; break;
+        case 2: v = mx; break;
+        case 3: v = sm / (double)nl; break;
+        case 4: v = pow(10.0, ls / (double)nl); break;
+        default: break;
+        }
+        if (lumping == 5 && nl > 1)
+            for (k = nl - 1; k >= 1; k--) {
+                const double dz = bnd[(size_t)k * n + e] - bnd[(size_t)(k - 1) * n + e];
+                const double er = eta3[(size_t)(k - 1) * n + e] / v, ir = 1. / er;
+                const double kz = dz * kappa[e], c = cosh(kz), sn = sinh(kz);
+                r = r * (2 * er * c * sn + (1 - er * er) * (kz * kz) + (er * sn) * (er * sn) + c * c) /
+                    ((er + ir) * c * sn + (er - ir) * dz * kappa[e] + sn * sn + c * c);
+            }
+        eta_eff[e] = v;
+        R[e] = r;
+    }
+}

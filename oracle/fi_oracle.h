@@ -109,6 +109,14 @@ void orc_set_threads(int n);
 /* The Kelvin-function table of LV-ELRA (1001 entries each). */
 void orc_kei_table(double *rn, double *kei);
 
+/* rheology_file branch helpers (src/fastisostasy.f90:262-420) */
+void orc_bilinear_array(const double *x, int nxr, const double *y, int nyr, const double *z,
+                        const double *xo, int nx, const double *yo, int ny, double *out);
+double orc_interp_0d(const double *x, const double *y, int n, double xout);
+int orc_smooth_gauss_2d(double *var, int nx, int ny, double dx, double sigma);
+void orc_lump3(const double *eta3, const double *bnd, const double *kappa, int n, int nl, int lumping,
+               double *eta_eff, double *R);
+
 #ifdef __cplusplus
 }
 #endif

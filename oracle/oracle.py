@@ -84,6 +84,12 @@ def lib():
         L.orc_get_scalars.argtypes = [C.c_void_p, dp]
         L.orc_rhs_now.argtypes = [C.c_void_p, dp]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_bilinear_array.argtypes = [dp, C.c_int, dp, C.c_int, dp, dp, C.c_int, dp, C.c_int, dp]
+        L.orc_interp_0d.argtypes = [dp, dp, C.c_int, C.c_double]
+        L.orc_interp_0d.restype = C.c_double
+        L.orc_smooth_gauss_2d.argtypes = [dp, C.c_int, C.c_int, C.c_double, C.c_double]
+        L.orc_smooth_gauss_2d.restype = C.c_int
+        L.orc_lump3.argtypes = [dp, dp, dp, C.c_int, C.c_int, C.c_int, dp, dp]
         _lib = L
     return _lib
 
@@ -273,3 +279,79 @@ def make_bsl(method=0, bsl_init=0.0, A_ocean_pd=3.625e14) -> OrcBsl:
     b.A_ocean_pd = A_ocean_pd
     b.A_ocean_now = A_ocean_pd
     return b
+
+
+# ---- rheology_file branch of isos_init (src/fastisostasy.f90:262-443) -------
+
+def bilinear_array(xr, yr, z, xo, yo):
+    """bilinear_interpolation_array (src/isos_utils.f90:561-575) of z (nyr,
+    nxr) at the points xo x yo, in the routine's single precision."""
+    xr, yr, z, xo, yo = _f64(xr), _f64(yr), _f64(z), _f64(xo), _f64(yo)
+    out = np.zeros((len(yo), len(xo)))
+    lib().orc_bilinear_array(_p(xr), len(xr), _p(yr), len(yr), _p(z), _p(xo), len(xo), _p(yo), len(yo), _p(out))
+    return out
+
+
+def smooth_gauss_2d(var, dx, sigma):
+    """smooth_gauss_2D (src/isos_utils.f90:696-819); None where the
+    reference stops (window wider than the grid)."""
+    v = _f64(var).copy()
+    if lib().orc_smooth_gauss_2d(_p(v), v.shape[1], v.shape[0], float(dx), float(sigma)):
+        return None
+    return v
+
+
+def rheology_file(p: dict, xc, yc, dx, kappa, He, xr, yr, zr=None, thick=None, thick_scale=1.0,
+                  log10_eta=None, stddev=None, stddev_scaling=False, radius=0.0, cc=1.0):
+    """He, D, eta_eff, R of the padded grid from a rheology file's arrays,
+    step by step as isos_init does it: thickness (nyr, nxr), log10 eta and
+    stddev (nzr, nyr, nxr).  He: the thickness used without a file
+    thickness."""
+    ny, nx = len(yc), len(xc)
+    n = nx * ny
+    He = np.array(He, dtype=np.float64).reshape(ny, nx)
+    if thick is not None:
+        He = bilinear_array(xr, yr, _f64(thick) * thick_scale, xc, yc)
+        if radius > 0:
+            He = smooth_gauss_2d(He, dx, radius)
+    D = p["E"] * 1e9 * (He * He * He) / (12.0 * (1.0 - p["nu"] * p["nu"]))
+    if log10_eta is None:
+        return He, D, None, None
+    nz = len(zr)
+    nl = int(p["nl"])
+    depth = np.array([zr[nz - 1] - zr[nz - 1 - q] for q in range(nz)])
+    prof = np.stack([bilinear_array(xr, yr, log10_eta[nz - 1 - q], xc, yc) for q in range(nz)])
+    if stddev_scaling and stddev is not None:
+        sd = np.stack([bilinear_array(xr, yr, stddev[nz - 1 - q], xc, yc) for q in range(nz)])
+        prof = prof + p["viscosity_scaling"] * sd
+    prof = np.where(prof < 16, 16.0, prof)
+    prof = np.where(prof > 23, 23.0, prof)
+    bnd = np.zeros((nl, ny, nx))
+    bnd[0] = He
+    for k in range(1, nl):
+        bnd[k] = bnd[k - 1] + p["dl"] if int(p["layering"]) == 1 else p["zl"][k]
+    eta3 = np.zeros((nl, ny, nx))
+    L = lib()
+    dep = _f64(depth)
+    col = np.zeros(nz)
+    for j in range(ny):
+        for i in range(nx):
+            col[:] = prof[:, j, i]
+            for k in range(nl):
+                eta3[k, j, i] = 10.0 ** L.orc_interp_0d(_p(dep), _p(col), nz, float(bnd[k, j, i]))
+    eta_eff = np.zeros((ny, nx))
+    R = np.zeros((ny, nx))
+    e3, b3, kap = _f64(eta3), _f64(bnd), _f64(kappa)
+    L.orc_lump3(_p(e3), _p(b3), _p(kap), n, nl, int(p["lumping"]), _p(eta_eff), _p(R))
+    if radius > 0:
+        eta_eff = smooth_gauss_2d(eta_eff, dx, radius)
+    mode = 0 if stddev_scaling else int(p["visc_scaling_method"])
+    if mode == 2:
+        eta_eff = np.full_like(eta_eff, eta_eff.min())
+    elif mode == 3:
+        eta_eff = np.full_like(eta_eff, eta_eff.max())
+    elif mode == 1:
+        eta_eff = eta_eff * p["viscosity_scaling"]
+    eta_eff = eta_eff * cc
+    eta_eff = np.exp(np.log10(p["eta_ref"] / eta_eff)) * eta_eff
+    return He, D, eta_eff, R

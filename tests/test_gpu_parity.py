@@ -361,3 +361,67 @@ def test_reference_tsit54_stability_edge_sensitivity():
     that edge."""
     wl = W.ensemble_member(2, stage_mode=0)
     assert rel(_tsit_run(wl, 0, eta_scale=1.0 + 1e-12), _tsit_run(wl, 0)) > 1e-3
+
+
+def _rheo_file(nx_dom, dx, seed, nz=5):
+    """A synthetic rheology file: a coarser grid than the domain (its edges
+    inside the domain, so the flat extension is exercised), thickness in km,
+    log10 eta with values beyond the [16, 23] clamp, a stddev field."""
+    rng = np.random.default_rng(seed)
+    L = nx_dom * dx / 2
+    xr = np.linspace(-0.9 * L, 0.9 * L, 23)
+    yr = np.linspace(-0.85 * L, 0.95 * L, 19)
+    X, Y = np.meshgrid(xr, yr)
+    thick = 90.0 + 30.0 * np.sin(X / 4e5) * np.cos(Y / 5e5) + rng.random(X.shape)
+    zr = np.array([-660e3, -410e3, -250e3, -120e3, 0.0])
+    lg = np.stack([20.5 + 0.3 * k + 0.8 * np.sin((X + k * 1e5) / 3e5) * np.cos(Y / 4e5) for k in range(nz)])
+    lg[0, :3, :3] = 24.0
+    lg[-1, -2:, -2:] = 15.0
+    sd = 0.1 + 0.05 * rng.random(lg.shape)
+    return xr, yr, zr, thick, lg, sd
+
+
+@pytest.mark.parametrize("radius,stddev,lumping,layering", [(0.0, False, 5, 1), (120e3, True, 5, 0),
+                                                             (120e3, False, 4, 1), (0.0, True, 0, 1)])
+def test_rheology_file(radius, stddev, lumping, layering):
+    """The rheology_file branches of isos_init on the device (fi_set_rheology:
+    bilinear onto the grid, smooth_gauss_2D, clamp, depth interpolation,
+    lumping, scaling) against the oracle's step-by-step restatement, then a
+    few updates with those fields against the oracle."""
+    wl = W.config1(48)
+    wl.t_end = 30.0
+    wl.params.update(nl=3, zl=[100e3, 250e3, 500e3], viscosities=[1e21, 1e21, 1e21], lumping=lumping,
+                     layering=layering, dl=120e3, mantle=3, lithosphere=3, correct_compression=1,
+                     visc_scaling_method=0 if stddev else 1, viscosity_scaling=1.5)
+    pair = Pair(wl)
+    dom, orc = pair.dom, pair.orc
+    nx, ny, dx = dom.nx, dom.ny, wl.dx
+    xc = (np.arange(1, nx + 1) - nx // 2 - 1) * dx
+    yc = (np.arange(1, ny + 1) - ny // 2 - 1) * dx
+    xr, yr, zr, thick, lg, sd = _rheo_file(nx, dx, 5)
+    dom.set_rheology(xr, yr, zr, litho_thickness=thick, litho_thickness_scaling=1e3, log10_viscosity=lg,
+                     stddev_log10_viscosity=sd, stddev_scaling=stddev, rheo_smoothing_radius=radius)
+    cc = 1.5 / (1 + wl.params["nu"])
+    He, D, eta, R = O.rheology_file(wl.params, xc, yc, dx, dom.field("kappa"), np.full((ny, nx), 100e3), xr, yr,
+                                    zr, thick, 1e3, lg, sd, stddev, radius, cc)
+    assert rel(dom.field("D_lith"), D) <= 1e-12
+    assert rel(dom.field("eta_eff"), eta) <= 1e-12
+    assert rel(dom.field("R"), R) <= 1e-12
+    if lumping == 5:
+        assert R.std() > 0
+    orc.set_fields(D_lith=D, eta_eff=eta, R=R)
+    pair.init()
+    pair.step(3)
+    compare(pair, TOL64)
+    pair.close()
+
+
+def test_rheology_file_rejects_a_window_wider_than_the_grid():
+    wl = W.config1(32)
+    wl.params.update(mantle=3, lithosphere=3)
+    dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=0)
+    xr, yr, zr, thick, lg, sd = _rheo_file(dom.nx, wl.dx, 1)
+    with pytest.raises(Exception):
+        dom.set_rheology(xr, yr, zr, litho_thickness=thick, litho_thickness_scaling=1e3,
+                         rheo_smoothing_radius=40 * wl.dx)
+    dom.close()

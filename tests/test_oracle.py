@@ -160,3 +160,25 @@ def test_elra_equilibrium_matches_local_under_a_broad_load():
     weq_local = -load / p["rho_uppermantle"]
     c = w.shape[0] // 2
     assert abs(w[c, c] - weq_local[c, c]) <= 0.05 * abs(weq_local[c, c])
+
+
+def test_smooth_gauss_2d_keeps_constants_and_rejects_wide_windows():
+    """smooth_gauss_2D's normalised window leaves a constant field unchanged
+    (mirror extension included) and the reference stops when the window
+    reaches past the mirrored band."""
+    v = np.full((20, 24), 3.25)
+    s = O.smooth_gauss_2d(v, 10e3, 35e3)
+    assert np.allclose(s, 3.25, rtol=0, atol=1e-14)
+    assert O.smooth_gauss_2d(v, 10e3, 120e3) is None
+
+
+def test_bilinear_array_nodes_and_flat_extension():
+    """bilinear_interpolation reproduces the grid values at interior nodes
+    (to single precision) and holds the edge values beyond the grid."""
+    xr = np.linspace(-1e6, 1e6, 21)
+    yr = np.linspace(-8e5, 8e5, 17)
+    z = np.random.default_rng(3).random((17, 21))
+    got = O.bilinear_array(xr, yr, z, xr[3:-3], yr[3:-3])
+    assert np.allclose(got, z[3:-3, 3:-3].astype(np.float32), rtol=0, atol=2e-6)
+    far = O.bilinear_array(xr, yr, z, np.array([-2e6, 2e6]), np.array([-2e6, 2e6]))
+    assert far[0, 0] == np.float32(z[0, 0]) and far[1, 1] == np.float32(z[-1, -1])
