@@ -166,6 +166,41 @@ def make_domain(precision, stage_mode=1):
     return dom, wl, b
 
 
+def output_leg(dom, wl, b, steps, t0):
+    """ms per update of device-resident updates with and without an
+    asynchronous output snapshot (fi_output_async into page-locked memory)
+    after every update; the snapshot's copy overlaps the next update."""
+    import torch
+    H = torch.from_numpy(np.ascontiguousarray(wl.H_final)).to("cuda")
+    buf = torch.empty(dom.output_bytes() // 8, dtype=torch.float64).pin_memory()
+    ext = torch.cuda.ExternalStream(dom.L.fi_stream(dom.h))
+    t = t0
+    res = {}
+    for with_out in (False, True):
+        for _ in range(2):   # warm-up
+            t += wl.dtt
+            dom.update_async(H.data_ptr(), t, b)
+            if with_out:
+                dom.output_async(buf.data_ptr())
+        dom.output_wait()
+        dom.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for _ in range(steps):
+            t += wl.dtt
+            dom.update_async(H.data_ptr(), t, b)
+            if with_out:
+                dom.output_async(buf.data_ptr())
+        dom.output_wait()
+        e1.record(ext)
+        dom.synchronize()
+        res["with" if with_out else "without"] = e0.elapsed_time(e1) / steps
+    return {"ms_per_step_without": res["without"], "ms_per_step_with": res["with"],
+            "bytes_per_snapshot": dom.output_bytes(),
+            "note": "e1 is recorded after fi_output_wait, so the last copy is inside the timed region"}
+
+
 def run_resident(dom, wl, b, steps, warmup, flush, t0=0.0, sampler_index=None, profile=False):
     """Device-resident loop from model time t0: returns (per-step ms list,
     launches, clocks, per-kernel profile, final time)."""
@@ -668,6 +703,10 @@ def main():
 
     # end to end through fi_update with host arrays (mixed form)
     e2e_secs, h2d, d2h = run_e2e(dom, wl, b, args.steps, 1, flush, t_now)
+    t_now += wl.dtt * (args.steps + 1)
+    # device-resident updates with an asynchronous isos%out snapshot after
+    # every update (fi_output_async) against the same updates without
+    outp = output_leg(dom, wl, b, args.steps, t_now)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -705,6 +744,7 @@ def main():
                          "whole_update": {"algorithmic_bytes": upd,
                                           "achieved": upd / (r32["ms"] / 1000.0) / 1e9,
                                           "frac": upd / (r32["ms"] / 1000.0) / 1e9 / peak}},
+            "output_async": outp,
             "cpu_baseline": cpu,
             "configs": cfgs,
             "ensemble": ens,

@@ -32,7 +32,8 @@ EXPORTS = ["fi_create", "fi_destroy", "fi_dims", "fi_set_fields", "fi_set_kernel
            "fi_padded_dims", "fi_serve_create", "fi_serve_submit", "fi_serve_info", "fi_serve_wait",
            "fi_serve_result", "fi_serve_clock", "fi_serve_destroy", "fi_batch_update", "fi_batch_synchronize",
            "fi_batch_create", "fi_batch_step", "fi_batch_wait", "fi_batch_destroy", "fi_elva_disk",
-           "fi_batch_set_priority", "fi_set_rheology"]
+           "fi_batch_set_priority", "fi_set_rheology", "fi_output_bytes", "fi_output_async",
+           "fi_output_wait"]
 
 PROFILE_KERNELS = ["flexure", "rows_fwd", "cols_hartley", "rows_inv", "conv_rows_fwd", "conv_cols",
                    "conv_rows_inv", "rk_stage", "rk_final", "upd_begin", "upd_masks", "upd_litho",
@@ -121,6 +122,10 @@ def load(build_if_missing: bool = True):
     L.fi_dims.argtypes = [H, C.POINTER(C.c_int32)]
     L.fi_set_fields.argtypes = [H, _dp, _dp, _dp, _u8]
     L.fi_set_rheology.argtypes = [H, C.POINTER(FiRheology)]
+    L.fi_output_bytes.argtypes = [H]
+    L.fi_output_bytes.restype = C.c_int64
+    L.fi_output_async.argtypes = [H, C.c_void_p]
+    L.fi_output_wait.argtypes = [H]
     L.fi_set_kernels.argtypes = [H, _dp, _dp]
     L.fi_init_ref.argtypes = [H, _dp, _dp, C.c_double, _dp]
     L.fi_init_state.argtypes = [H, _dp, _dp, C.c_double, C.POINTER(FiBsl)]

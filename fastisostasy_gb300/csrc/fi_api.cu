@@ -145,6 +145,10 @@ struct fi_handle {
     int* out_rows = nullptr;
     double* dH = nullptr;                // ice-grid thickness on the device
     double* dpack = nullptr;             // packed outputs
+    double* dsnap = nullptr;             // asynchronous output: device snapshot (11 x ice grid)
+    cudaStream_t s_out = nullptr;        // asynchronous output: copy stream
+    cudaEvent_t ev_snap = nullptr, ev_out = nullptr;
+    bool out_pending = false;
     double* hpin = nullptr;              // pinned staging (max(ice grid, packed outputs))
     size_t hpin_elems = 0;
     const double** gsrc = nullptr;
@@ -1236,9 +1240,55 @@ int fi_destroy(fi_handle* h)
     if (h->hpin) cudaFreeHost(h->hpin);
     for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
+    if (h->s_out) {
+        cudaStreamSynchronize(h->s_out);
+        cudaStreamDestroy(h->s_out);
+    }
+    if (h->ev_snap) cudaEventDestroy(h->ev_snap);
+    if (h->ev_out) cudaEventDestroy(h->ev_out);
     if (h->s) cudaStreamDestroy(h->s);
     if (h->s_body) cudaStreamDestroy(h->s_body);
     delete h;
+    return FI_OK;
+}
+
+int64_t fi_output_bytes(const fi_handle* h)
+{
+    if (!h) return -1;
+    return (int64_t)h->nx_ice * h->ny_ice * 11 * 8;
+}
+
+int fi_output_async(fi_handle* h, double* dst)
+{
+    if (!h || !dst) return FI_E_ARG;
+    if (!h->state_ready) return fail(h, FI_E_STATE, "fi_output_async before fi_init_state");
+    const size_t ni = (size_t)h->nx_ice * h->ny_ice;
+    if (!h->s_out) {
+        int rc;
+        if ((rc = dalloc(h, &h->dsnap, ni * 11 * 8))) return rc;
+        CK(cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->ev_snap, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming));
+    }
+    // the previous snapshot's copy must have left the staging buffer
+    if (h->out_pending) CK(cudaStreamWaitEvent(h->s, h->ev_out, 0));
+    gather(h->gsrc, h->gmsrc, 8, 3, h->d, h->dsnap, h->s);
+    CK(cudaGetLastError());
+    h->launches += 1;
+    CK(cudaEventRecord(h->ev_snap, h->s));
+    CK(cudaStreamWaitEvent(h->s_out, h->ev_snap, 0));
+    CK(cudaMemcpyAsync(dst, h->dsnap, ni * 11 * 8, cudaMemcpyDeviceToHost, h->s_out));
+    CK(cudaEventRecord(h->ev_out, h->s_out));
+    h->out_pending = true;
+    return FI_OK;
+}
+
+int fi_output_wait(fi_handle* h)
+{
+    if (!h) return FI_E_ARG;
+    if (!h->out_pending) return FI_OK;
+    CK(cudaEventSynchronize(h->ev_out));
+    h->out_pending = false;
     return FI_OK;
 }
 

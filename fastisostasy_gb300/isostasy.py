@@ -137,6 +137,29 @@ class Domain:
         r.rheo_smoothing_radius = float(rheo_smoothing_radius)
         self._check(self.L.fi_set_rheology(self.h, C.byref(r)))
 
+    OUTPUT_FIELDS = ("z_bed", "z_ss", "dz_ss", "w", "we", "dwdt", "canom_full", "Hice",
+                     "maskocean", "maskgrounded", "maskcontinent")
+
+    def output_async(self, dst_ptr: int):
+        """Snapshot isos%out after the updates enqueued so far and copy it to
+        host memory at dst_ptr (output_bytes() bytes) while later updates
+        run (fi_output_async)."""
+        self._check(self.L.fi_output_async(self.h, C.c_void_p(dst_ptr)))
+
+    def output_wait(self):
+        self._check(self.L.fi_output_wait(self.h))
+
+    def output_bytes(self) -> int:
+        return int(self.L.fi_output_bytes(self.h))
+
+    def unpack_output(self, buf: np.ndarray) -> dict:
+        """The fields of an output snapshot (buf: float64, output_bytes()/8)."""
+        a = np.asarray(buf, dtype=np.float64).reshape(11, self.ny_ice, self.nx_ice)
+        out = {k: a[i] for i, k in enumerate(self.OUTPUT_FIELDS)}
+        for k in ("maskocean", "maskgrounded", "maskcontinent"):
+            out[k] = out[k] != 0.0
+        return out
+
     def set_kernels(self, GE=None, GN=None):
         a = _f64(GE) if GE is not None else None
         b = _f64(GN) if GN is not None else None

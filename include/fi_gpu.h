@@ -160,6 +160,21 @@ int fi_synchronize(fi_handle* h);
 /* Replaces bsl_update (src/barysealevel.f90:195-252). */
 int fi_bsl_update(fi_bsl* b, double year_bp);
 
+/* Asynchronous output (no reference counterpart; the step loop's write of
+ * isos%out every dt_out, src/isostasy_io.f90:56-465, without a stall):
+ * fi_output_async snapshots the isos%out fields on the device in stream
+ * order, after the updates enqueued so far, and copies them to dst on a
+ * side stream while later updates run.  dst holds fi_output_bytes(h) bytes
+ * (page-locked memory lets the copy overlap): 11 ice-grid fields of doubles,
+ * x fastest, in the order z_bed, z_ss, dz_ss, w, we, dwdt, canom_full,
+ * Hice, maskocean, maskgrounded, maskcontinent (masks as 0.0 / 1.0).  One
+ * snapshot is staged at a time: the next fi_output_async orders itself
+ * after the previous copy on the device.  fi_output_wait returns when the
+ * last copy has landed. */
+int64_t fi_output_bytes(const fi_handle* h);
+int fi_output_async(fi_handle* h, double* dst);
+int fi_output_wait(fi_handle* h);
+
 /* Inspection of padded fields; `which` follows FI_FIELD_*. */
 enum {
     FI_FIELD_Z_BED = 0, FI_FIELD_DWDT = 1, FI_FIELD_W = 2, FI_FIELD_WE = 3, FI_FIELD_HAF = 4,

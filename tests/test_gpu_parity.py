@@ -425,3 +425,49 @@ def test_rheology_file_rejects_a_window_wider_than_the_grid():
         dom.set_rheology(xr, yr, zr, litho_thickness=thick, litho_thickness_scaling=1e3,
                          rheo_smoothing_radius=40 * wl.dx)
     dom.close()
+
+
+def test_async_output_snapshots_match_synchronous_outputs():
+    """fi_output_async snapshots taken between asynchronous updates (copied
+    on a side stream while the next updates run) equal the isos%out fields
+    that synchronous fi_update calls return at the same times."""
+    import torch
+    from fastisostasy_gb300.isostasy import OUT_FIELDS, OUT_MASKS
+    wl = W.config2(n=64, L=3000e3 * 64 / 256, dt=1.0, stage_mode=1)
+    times = [wl.dtt * (k + 1) for k in range(6)]
+    # synchronous: outputs of fi_update every second update
+    a = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=1)
+    ba = gpu_bsl()
+    a.init_state(wl.z_bed, wl.H_at(0.0), 0.0, ba)
+    want = []
+    for k, t in enumerate(times):
+        out = None
+        if k % 2 == 1:
+            out = {f: np.zeros((wl.ny_ice, wl.nx_ice)) for f in OUT_FIELDS}
+            out.update({m: np.zeros((wl.ny_ice, wl.nx_ice), dtype=np.uint8) for m in OUT_MASKS})
+        a.update(wl.H_final, t, ba, out)
+        if out is not None:
+            want.append(out)
+    a.close()
+    # asynchronous: device-resident updates, a snapshot after every second one
+    b = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=1)
+    bb = gpu_bsl()
+    b.init_state(wl.z_bed, wl.H_at(0.0), 0.0, bb)
+    H = torch.from_numpy(np.ascontiguousarray(wl.H_final)).to("cuda")
+    nb = b.output_bytes() // 8
+    bufs = [torch.empty(nb, dtype=torch.float64).pin_memory() for _ in range(len(want))]
+    j = 0
+    for k, t in enumerate(times):
+        b.update_async(H.data_ptr(), t, bb)
+        if k % 2 == 1:
+            b.output_async(bufs[j].data_ptr())
+            j += 1
+    b.output_wait()
+    b.synchronize()
+    for w_out, buf in zip(want, bufs):
+        got = b.unpack_output(buf.numpy())
+        for f in OUT_FIELDS:
+            assert np.array_equal(got[f], w_out[f]), f
+        for m in OUT_MASKS:
+            assert np.array_equal(got[m], w_out[m].astype(bool)), m
+    b.close()
