@@ -1736,6 +1736,7 @@ struct fi_batch {
     long long launches = 0;
     int* dmore = nullptr;                // loop condition of the eager path
     bool eager = false;
+    bool true_stages = false;            // members run Tsit5 with true stages (stage_mode 1)
 };
 
 namespace {
@@ -1748,6 +1749,30 @@ template <typename T> void batch_attempt(fi_batch* b, cudaStream_t s, cudaGraphC
     batch_attempt_begin(b->dM, nm, kMaxAttempts, off, b->dcl, s);
     const BList LF = blist(b->dcl, nm, 0), LR = blist(b->dcl, nm, 1), LC = blist(b->dcl, nm, 2),
                 LT = blist(b->dcl, nm, 3);
+    if (b->true_stages) {
+        // Dormand-Prince 5(4) with FSAL (tsit_true_attempt per member): k_0
+        // where no accepted attempt left it cached, then stages 1-6 for every
+        // member with an attempt, the embedded error, decision, commit, FSAL
+        const BList LF6 = blist(b->dcl, nm, 4), LR6 = blist(b->dcl, nm, 5), LC6 = blist(b->dcl, nm, 6);
+        batch_flexure_y<T>(b->dM, LF, b->grid[0], 0, s);
+        batch_rows_fwd<T>(b->dM, LR, b->grid[1], b->rows_threads, b->rows_smem, s);
+        batch_cols_hartley<T>(b->dM, LC, b->grid[2], b->cols_threads, b->cols_smem, s);
+        batch_rows_inv<T>(b->dM, LR, b->grid[1], b->rows_threads, b->rows_smem, s, 0);
+        for (int i = 1; i <= 6; ++i) {
+            batch_dp_stage<T>(b->dM, LT, b->grid[3], i, s);
+            batch_flexure_y<T>(b->dM, LF6, b->grid[0], i, s);
+            batch_rows_fwd<T>(b->dM, LR6, b->grid[1], b->rows_threads, b->rows_smem, s);
+            batch_cols_hartley<T>(b->dM, LC6, b->grid[2], b->cols_threads, b->cols_smem, s);
+            batch_rows_inv<T>(b->dM, LR6, b->grid[1], b->rows_threads, b->rows_smem, s, i);
+        }
+        batch_dp_err<T>(b->dM, LT, b->grid[3], s);
+        batch_ts_err<T>(b->dM, LT, b->grid[3], 100000, s);
+        batch_ts_commit<T>(b->dM, LT, b->grid[3], s);
+        batch_fsal<T>(b->dM, LT, b->grid[3], s);
+        batch_attempt_end(b->dM, nm, loop, s, more_out, 1);
+        b->launches += 40;
+        return;
+    }
     batch_flexure<T>(b->dM, LF, b->grid[0], s);
     batch_rows_fwd<T>(b->dM, LR, b->grid[1], b->rows_threads, b->rows_smem, s);
     batch_cols_hartley<T>(b->dM, LC, b->grid[2], b->cols_threads, b->cols_smem, s);
@@ -1896,17 +1921,18 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         if (!h) return FI_E_ARG;
         if (!h->state_ready) return fail(h, FI_E_STATE, "fi_batch_create before fi_init_state");
         const fi_handle* h0 = hs[0];
-        if (h->p.method != 3 || h->p.dt_method != 2 || h->p.stage_mode != 0 || mixed(h) != mixed(h0) ||
-            (mixed(h) && !h->d.whi) ||
+        if (h->p.method != 3 || h->p.dt_method != 2 || h->p.stage_mode != h0->p.stage_mode || mixed(h) != mixed(h0) ||
+            (mixed(h) && h->p.stage_mode == 0 && !h->d.whi) || (mixed(h) && h->fc.dxm != nullptr) ||
             h->p.dt_diagnostics != h0->p.dt_diagnostics || h->time_diag != h0->time_diag || !h->tsit_graph_ok)
             return fail(h, FI_E_CONFIG,
-                        "batched members must run reference-compatible tsit54 in the same precision, in lockstep "
+                        "batched members must run tsit54 with the same stage mode and precision, in lockstep "
                         "(mixed members with uniform spacing)");
     }
     fi_batch* b = new fi_batch();
     b->hs.assign(hs, hs + n);
     b->nm = n;
     b->mixed = mixed(hs[0]);
+    b->true_stages = hs[0]->p.stage_mode == 1;
     std::vector<BMember> M(n);
     std::vector<int> off(4 * (n + 1), 0);
     const size_t c2 = b->mixed ? sizeof(float2) : sizeof(double2);
@@ -1927,6 +1953,9 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         m.mA = h->mA;
         m.mB = h->mB;
         m.raw = h->raw[0];
+        for (int q = 0; q < 7; ++q) m.raw7[q] = h->raw[q];
+        m.yst = h->y;
+        m.wref = h->w_ref;
         m.even = h->even;
         m.RB = rhs_rows_per_block(m.p.h);
         m.CB = b->mixed ? rhs_cols_per_block<float>(m.p.ny) : rhs_cols_per_block<double>(m.p.ny);
@@ -1948,7 +1977,8 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         m.q = h->p.q;
         m.dt_max = h->p.dt_max;
         m.fseg = 16;
-        const int fblk = b->mixed ? batch_flexure_blocks(m.p.nx, m.p.ny, m.fseg) : m.fgx * ((m.p.ny + 7) / 8);
+        const int fblk = (b->mixed && !b->true_stages) ? batch_flexure_blocks(m.p.nx, m.p.ny, m.fseg)
+                                                       : m.fgx * ((m.p.ny + 7) / 8);
         const int rblk = (m.p.ny + m.RB - 1) / m.RB;
         const int cblk = (m.p.h + 1 + m.CB - 1) / m.CB;
         off[i + 1] = off[i] + fblk;

@@ -31,6 +31,9 @@ struct BMember {
     const void* mA;           // 1/(kappa R) at (k, l), (-k, l) (T)
     const void* mB;
     void* raw;                // RHS output (T)
+    void* raw7[7];            // true stages: the seven stage outputs (T); raw7[0] = raw
+    double* yst;              // true stages: stage state buffer (stages 1-5; stage 6 is d.ts_x2)
+    const double* wref;       // true stages: w_ref of the mantle term
     int even;
     int RB, CB;               // rows per row block, columns per column block
     int fgx;                  // flexure blocks along x (FP64 tiles)
@@ -49,21 +52,22 @@ struct BArgs {
 
 // Members with work in the current attempt, compacted by the attempt-begin
 // kernel: ids[j] for j < *cnt, member ids[j] owning the virtual blocks
-// [coff[j], coff[j+1]) of a batched launch.  Four lists share one int buffer
-// of blist_ints(nm) entries: 0 flexure, 1 row transforms, 2 column
-// transforms (members that need a new RHS), 3 attempt kernels (members with
-// an attempt left).
+// [coff[j], coff[j+1]) of a batched launch.  Seven lists share one int
+// buffer of blist_ints(nm) entries: 0 flexure, 1 row transforms, 2 column
+// transforms (members that need a new RHS), 3 attempt kernels, 4 flexure,
+// 5 row transforms, 6 column transforms (members with an attempt left; the
+// RHS of true stages 1-6).
 struct BList {
     const int* ids;
     const int* coff;
     const int* cnt;
 };
-inline size_t blist_ints(int nm) { return 2 + 2 * (size_t)nm + 4 * ((size_t)nm + 1); }
+inline size_t blist_ints(int nm) { return 2 + 2 * (size_t)nm + 7 * ((size_t)nm + 1); }
 inline BList blist(const int* base, int nm, int kind)
 {
     BList L;
-    L.cnt = base + (kind == 3 ? 1 : 0);
-    L.ids = base + 2 + (kind == 3 ? nm : 0);
+    L.cnt = base + (kind >= 3 ? 1 : 0);
+    L.ids = base + 2 + (kind >= 3 ? nm : 0);
     L.coff = base + 2 + 2 * (size_t)nm + (size_t)kind * (nm + 1);
     return L;
 }
@@ -95,11 +99,16 @@ void batch_rows_fwd(const BMember* M, BList L, int nblk, int threads, size_t sme
 template <typename T>
 void batch_cols_hartley(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s);
 template <typename T>
-void batch_rows_inv(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s);
+void batch_rows_inv(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s, int stage = 0);
 template <typename T> void batch_ts_max(const BMember* M, BList L, int nblk, cudaStream_t s);
 template <typename T>
 void batch_ts_err(const BMember* M, BList L, int nblk, int max_reject, cudaStream_t s);
 template <typename T> void batch_ts_commit(const BMember* M, BList L, int nblk, cudaStream_t s);
+// true stages (Dormand-Prince 5(4) with FSAL) per member
+template <typename T> void batch_dp_stage(const BMember* M, BList L, int nblk, int i, cudaStream_t s);
+template <typename T> void batch_dp_err(const BMember* M, BList L, int nblk, cudaStream_t s);
+template <typename T> void batch_fsal(const BMember* M, BList L, int nblk, cudaStream_t s);
+template <typename T> void batch_flexure_y(const BMember* M, BList L, int nblk, int stage, cudaStream_t s);
 // mixed form with the float pair of now%w: ts_fused / ts_commit_pair per member
 void batch_ts_fused(const BMember* M, BList L, int nblk, int max_reject, cudaStream_t s);
 void batch_ts_commit_pair(const BMember* M, BList L, int nblk, cudaStream_t s);
@@ -109,7 +118,7 @@ void batch_loop_begin(const BMember* M, int nm, cudaStream_t s);
 void batch_attempt_begin(const BMember* M, int nm, int max_iter, const int* off, int* cl, cudaStream_t s);
 // more_out == NULL: sets the WHILE condition `loop`; else writes it there
 void batch_attempt_end(const BMember* M, int nm, cudaGraphConditionalHandle loop, cudaStream_t s,
-                       int* more_out = nullptr);
+                       int* more_out = nullptr, int fsal = 0);
 void batch_set_args(const BArgs* a, int nm, cudaStream_t s);
 
 // member owning global block b of a batched launch (off has nm + 1 entries)

@@ -916,7 +916,7 @@ template int rhs_cols_per_block<double>(int);
 template <typename T>
 __global__ void __launch_bounds__(256) k_b_flexure(const BMember* __restrict__ M, BList L)
 {
-    batch_walk(L, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return true; }, [&](int m, int local) {   // the list holds the members with work
         const BMember& b = M[m];
         const int bx = local % b.fgx, by = local / b.fgx;
         if constexpr (sizeof(T) == 4) {
@@ -938,7 +938,7 @@ template <typename T>
 __global__ void k_b_rows_fwd(const BMember* __restrict__ M, BList L)
 {
     typedef typename vec2<T>::type C2;
-    batch_walk(L, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return true; }, [&](int m, int local) {   // the list holds the members with work
         const BMember& b = M[m];
         rows_fwd_body<T>((const T*)b.f, b.p.nx, b.p.nx, b.p.ny, (C2*)b.S, b.p, b.RB, local, 0);
         __syncthreads();
@@ -949,7 +949,7 @@ template <typename T>
 __global__ void k_b_cols_hartley(const BMember* __restrict__ M, BList L)
 {
     typedef typename vec2<T>::type C2;
-    batch_walk(L, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return true; }, [&](int m, int local) {   // the list holds the members with work
         const BMember& b = M[m];
         cols_hartley_body<T>((C2*)b.S, (const T*)b.mA, (const T*)b.mB, b.even, b.p, b.CB, local, 0);
         __syncthreads();
@@ -957,13 +957,13 @@ __global__ void k_b_cols_hartley(const BMember* __restrict__ M, BList L)
 }
 
 template <typename T>
-__global__ void k_b_rows_inv(const BMember* __restrict__ M, BList L)
+__global__ void k_b_rows_inv(const BMember* __restrict__ M, BList L, int stage)
 {
     typedef typename vec2<T>::type C2;
-    batch_walk(L, [&](int m) { return M[m].d.ctl->need_rhs != 0; }, [&](int m, int local) {
+    batch_walk(L, [&](int m) { return true; }, [&](int m, int local) {
         const BMember& b = M[m];
         const double norm = (double)(float)((long long)b.p.nx * b.p.ny);   // nx*ny*1. (default real)
-        rows_inv_body<T>((const C2*)b.S, b.p.ny, (T*)b.raw, b.p.nx, b.p, b.RB, (T)(1.0 / norm), local, 0);
+        rows_inv_body<T>((const C2*)b.S, b.p.ny, (T*)b.raw7[stage], b.p.nx, b.p, b.RB, (T)(1.0 / norm), local, 0);
         __syncthreads();
     });
 }
@@ -1006,10 +1006,34 @@ void batch_cols_hartley(const BMember* M, BList L, int nblk, int threads, size_t
     k_b_cols_hartley<T><<<nblk, threads, smem, s>>>(M, L);
 }
 template <typename T>
-void batch_rows_inv(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s)
+void batch_rows_inv(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s, int stage)
 {
     set_smem(k_b_rows_inv<T>, smem);
-    k_b_rows_inv<T><<<nblk, threads, smem, s>>>(M, L);
+    k_b_rows_inv<T><<<nblk, threads, smem, s>>>(M, L, stage);
+}
+
+// True stages: the RHS at stage state y (stage 0: x, 1-5: the stage buffer,
+// 6: x2) with the mantle term at that state, by shared-memory tiles.
+template <typename T>
+__global__ void __launch_bounds__(256) k_b_flexure_y(const BMember* __restrict__ M, BList L, int stage)
+{
+    batch_walk(L, [&](int m) { return true; }, [&](int m, int local) {
+        const BMember& b = M[m];
+        const int bx = local % b.fgx, by = local / b.fgx;
+        const double* y = stage == 0 ? b.d.x : (stage == 6 ? b.d.ts_x2 : b.yst);
+        if constexpr (sizeof(T) == 4) {
+            flexure_f32_body<false>(y, b.wref, (const float*)b.q0, b.mask, (const float*)b.D,
+                                    (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, b.fcf, bx, by);
+        } else {
+            flexure_body<T>(y, b.wref, (const T*)b.q0, b.mask, (const T*)b.D, (const T*)b.inv2eta, (T*)b.f, b.p.nx,
+                            b.p.ny, b.fc, bx, by);
+        }
+        __syncthreads();
+    });
+}
+template <typename T> void batch_flexure_y(const BMember* M, BList L, int nblk, int stage, cudaStream_t s)
+{
+    k_b_flexure_y<T><<<nblk, dim3(TX, TY), 0, s>>>(M, L, stage);
 }
 
 template <typename T> void batch_prepare(size_t rows_smem, size_t cols_smem)
@@ -1025,7 +1049,8 @@ template <typename T> void batch_prepare(size_t rows_smem, size_t cols_smem)
     template void batch_flexure<T>(const BMember*, BList, int, cudaStream_t);                    \
     template void batch_rows_fwd<T>(const BMember*, BList, int, int, size_t, cudaStream_t);      \
     template void batch_cols_hartley<T>(const BMember*, BList, int, int, size_t, cudaStream_t);  \
-    template void batch_rows_inv<T>(const BMember*, BList, int, int, size_t, cudaStream_t);
+    template void batch_rows_inv<T>(const BMember*, BList, int, int, size_t, cudaStream_t, int);      \
+    template void batch_flexure_y<T>(const BMember*, BList, int, int, cudaStream_t);
 FI_BATCH_INST(double)
 FI_BATCH_INST(float)
 

@@ -727,9 +727,9 @@ __device__ __forceinline__ void dp_corner_means(const Ctl* c, const DPRaw<T>& r,
 
 // Stage state y = x + h sum_{r<i} a_{i r} k_r (i = 1..6; stage 6 is x2).
 template <typename T>
-__global__ void __launch_bounds__(NT)
-k_dp_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __restrict__ x, DPRaw<T> r, int i, int nx,
-           int ny, double spy)
+__device__ __forceinline__ void dp_stage_body(const Ctl* __restrict__ c, double* __restrict__ y,
+                                              const double* __restrict__ x, const DPRaw<T>& r, int i, int nx, int ny,
+                                              double spy, int bid, int nblk)
 {
     if (c->done) return;
     __shared__ double cm[7];
@@ -737,7 +737,7 @@ k_dp_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __re
     const double h = c->h;
     const size_t n = (size_t)nx * ny;
     if constexpr (sizeof(T) == 8) {
-        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+        for (size_t e = (size_t)bid * NT + threadIdx.x; e < n; e += (size_t)nblk * NT) {
             double a = 0.0;
             for (int q = 0; q < i; ++q) a += c_dp_a[i][q] * (((double)r.p[q][e] - cm[q]) * spy);
             y[e] = x[e] + h * a;
@@ -745,7 +745,7 @@ k_dp_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __re
     } else {
         float af[6], cmf[6];
         for (int q = 0; q < i; ++q) { af[q] = (float)(c_dp_a[i][q] * h * spy); cmf[q] = (float)cm[q]; }
-        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+        for (size_t e = (size_t)bid * NT + threadIdx.x; e < n; e += (size_t)nblk * NT) {
             float a = 0.f;
             for (int q = 0; q < i; ++q) a += af[q] * ((float)r.p[q][e] - cmf[q]);
             y[e] = x[e] + (double)a;
@@ -753,10 +753,18 @@ k_dp_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __re
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(NT)
+k_dp_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __restrict__ x, DPRaw<T> r, int i, int nx,
+           int ny, double spy)
+{
+    dp_stage_body<T>(c, y, x, r, i, nx, ny, spy, (int)blockIdx.x, (int)gridDim.x);
+}
+
 // x1 = x + h sum_r bs_r k_r; x2 (stage 6 state) is in ts_x2: store x2 - x1
 // and reduce max|x1|, max|x2| into the tolerance.
 template <typename T>
-__global__ void __launch_bounds__(NT) k_dp_err(Dom d, DPRaw<T> r, double atol, double rtol)
+__device__ __forceinline__ void dp_err_body(Dom d, const DPRaw<T>& r, double atol, double rtol, int bid, int nblk)
 {
     Ctl* c = d.ctl;
     if (c->done) return;
@@ -766,7 +774,7 @@ __global__ void __launch_bounds__(NT) k_dp_err(Dom d, DPRaw<T> r, double atol, d
     double v[2] = {0.0, 0.0};
     const bool mx[2] = {true, true};
     if constexpr (sizeof(T) == 8) {
-        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
             double a = 0.0;
             for (int q = 0; q < 7; ++q) a += c_dp_bs[q] * (((double)r.p[q][e] - cm[q]) * d.spy);
             const double x1 = d.x[e] + h * a, x2 = d.ts_x2[e];
@@ -782,7 +790,7 @@ __global__ void __launch_bounds__(NT) k_dp_err(Dom d, DPRaw<T> r, double atol, d
             cmf[q] = (float)cm[q];
         }
         float m1 = 0.f, m2 = 0.f;
-        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
+        for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
             float dx = 0.f;
             for (int q = 0; q < 7; ++q) dx += ce[q] * ((float)r.p[q][e] - cmf[q]);
             ((float*)d.ts_dx)[e] = dx;
@@ -794,7 +802,13 @@ __global__ void __launch_bounds__(NT) k_dp_err(Dom d, DPRaw<T> r, double atol, d
         v[1] = (double)m2;
     }
     double tot[2];
-    if (grid_finish<2>(v, mx, d.partials, &c->counter[1], tot)) c->tol = atol + rtol * fmax(tot[0], tot[1]);
+    if (grid_finish<2>(v, mx, d.partials, &c->counter[1], tot, bid, nblk)) c->tol = atol + rtol * fmax(tot[0], tot[1]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_dp_err(Dom d, DPRaw<T> r, double atol, double rtol)
+{
+    dp_err_body<T>(d, r, atol, rtol, (int)blockIdx.x, (int)gridDim.x);
 }
 
 // accepted: the last stage's RHS becomes the next attempt's first (FSAL)
@@ -1084,6 +1098,68 @@ __global__ void __launch_bounds__(NT) k_b_ts_commit_pair(const BMember* __restri
                });
 }
 
+template <typename T> __device__ __forceinline__ DPRaw<T> member_raw(const BMember& b)
+{
+    DPRaw<T> r;
+#pragma unroll
+    for (int q = 0; q < 7; ++q) r.p[q] = (const T*)b.raw7[q];
+    return r;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_b_dp_stage(const BMember* __restrict__ M, BList L, int i)
+{
+    batch_walk(L, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
+        const BMember& b = M[m];
+        dp_stage_body<T>(b.d.ctl, i == 6 ? b.d.ts_x2 : b.yst, b.d.x, member_raw<T>(b), i, b.p.nx, b.p.ny, b.d.spy,
+                         local, b.red_nblk);
+        __syncthreads();
+    });
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_b_dp_err(const BMember* __restrict__ M, BList L)
+{
+    batch_walk(L, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
+        const BMember& b = M[m];
+        dp_err_body<T>(b.d, member_raw<T>(b), b.atol, b.rtol, local, b.red_nblk);
+        __syncthreads();
+    });
+}
+
+// accepted: the last stage's RHS becomes the next attempt's first (FSAL)
+template <typename T>
+__global__ void __launch_bounds__(NT) k_b_fsal(const BMember* __restrict__ M, BList L)
+{
+    batch_walk(L, [&](int m) { const Ctl* c = M[m].d.ctl; return c->done == 0 && c->accepted != 0; },
+               [&](int m, int local) {
+                   const BMember& b = M[m];
+                   T* k0 = (T*)b.raw7[0];
+                   const T* k6 = (const T*)b.raw7[6];
+                   for (size_t e = (size_t)local * NT + threadIdx.x; e < b.d.n; e += (size_t)b.red_nblk * NT)
+                       k0[e] = k6[e];
+               });
+}
+
+template <typename T> void batch_dp_stage(const BMember* M, BList L, int nblk, int i, cudaStream_t s)
+{
+    k_b_dp_stage<T><<<nblk, NT, 0, s>>>(M, L, i);
+}
+template <typename T> void batch_dp_err(const BMember* M, BList L, int nblk, cudaStream_t s)
+{
+    k_b_dp_err<T><<<nblk, NT, 0, s>>>(M, L);
+}
+template <typename T> void batch_fsal(const BMember* M, BList L, int nblk, cudaStream_t s)
+{
+    k_b_fsal<T><<<nblk, NT, 0, s>>>(M, L);
+}
+template void batch_dp_stage<float>(const BMember*, BList, int, int, cudaStream_t);
+template void batch_dp_stage<double>(const BMember*, BList, int, int, cudaStream_t);
+template void batch_dp_err<float>(const BMember*, BList, int, cudaStream_t);
+template void batch_dp_err<double>(const BMember*, BList, int, cudaStream_t);
+template void batch_fsal<float>(const BMember*, BList, int, cudaStream_t);
+template void batch_fsal<double>(const BMember*, BList, int, cudaStream_t);
+
 template <typename T> int batch_red_resident()
 {
     int per = 0;
@@ -1131,11 +1207,8 @@ __global__ void k_b_attempt_begin(const BMember* __restrict__ M, int nm, int max
         int* idsR = cl + 2;
         int* idsT = cl + 2 + nm;
         int* co = cl + 2 + 2 * nm;
-        int nR = 0, nT = 0, a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-        co[0] = 0;
-        co[nm + 1] = 0;
-        co[2 * (nm + 1)] = 0;
-        co[3 * (nm + 1)] = 0;
+        int nR = 0, nT = 0, a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, a6 = 0;
+        for (int k = 0; k < 7; ++k) co[k * (nm + 1)] = 0;
         for (int m = 0; m < nm; ++m) {
             const int f = fl[m];
             if (f & 1) {
@@ -1151,8 +1224,14 @@ __global__ void k_b_attempt_begin(const BMember* __restrict__ M, int nm, int max
             if (f & 2) {
                 idsT[nT] = m;
                 a3 += cn[3 * nm + m];
+                a4 += cn[m];
+                a5 += cn[nm + m];
+                a6 += cn[2 * nm + m];
                 ++nT;
                 co[3 * (nm + 1) + nT] = a3;
+                co[4 * (nm + 1) + nT] = a4;
+                co[5 * (nm + 1) + nT] = a5;
+                co[6 * (nm + 1) + nT] = a6;
             }
         }
         cl[0] = nR;
@@ -1161,13 +1240,14 @@ __global__ void k_b_attempt_begin(const BMember* __restrict__ M, int nm, int max
 }
 
 // continue while any member has an attempt left
-__global__ void k_b_attempt_end(const BMember* __restrict__ M, int nm, cudaGraphConditionalHandle loop, int* more_out)
+__global__ void k_b_attempt_end(const BMember* __restrict__ M, int nm, cudaGraphConditionalHandle loop, int* more_out,
+                                int fsal)
 {
     __shared__ int any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
     int more = 0;
-    for (int m = threadIdx.x; m < nm; m += blockDim.x) more |= attempt_end_one(M[m].d.ctl);
+    for (int m = threadIdx.x; m < nm; m += blockDim.x) more |= attempt_end_one(M[m].d.ctl, fsal);
     if (more) any = 1;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1208,9 +1288,10 @@ void batch_attempt_begin(const BMember* M, int nm, int max_iter, const int* off,
 {
     k_b_attempt_begin<<<1, 256, 5 * (size_t)nm * sizeof(int), s>>>(M, nm, max_iter, off, cl);
 }
-void batch_attempt_end(const BMember* M, int nm, cudaGraphConditionalHandle loop, cudaStream_t s, int* more_out)
+void batch_attempt_end(const BMember* M, int nm, cudaGraphConditionalHandle loop, cudaStream_t s, int* more_out,
+                       int fsal)
 {
-    k_b_attempt_end<<<1, 256, 0, s>>>(M, nm, loop, more_out);
+    k_b_attempt_end<<<1, 256, 0, s>>>(M, nm, loop, more_out, fsal);
 }
 void batch_set_args(const BArgs* a, int nm, cudaStream_t s) { k_b_set_args<<<(nm + 127) / 128, 128, 0, s>>>(a, nm); }
 template void batch_ts_max<float>(const BMember*, BList, int, cudaStream_t);

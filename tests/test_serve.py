@@ -166,3 +166,38 @@ def test_ensemble_lockstep_matches_members_alone(precision, mode):
             assert np.abs(w - g).max() <= 1e-5 * np.abs(w).max()
         else:
             assert np.array_equal(w, g)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_true_stage_ensemble_matches_members_alone(precision):
+    """Batched Tsit5 with true stages (Dormand-Prince 5(4), FSAL) over
+    members of different sizes: each member's result equals driving it
+    alone (FP64 bit for bit; mixed to the mixed-form bound)."""
+    from fastisostasy_gb300.serve import Ensemble
+    wls = []
+    for wl in (small_tsit(40), small_tsit(56), W.ensemble_member(3, stage_mode=1), W.ensemble_member(7, stage_mode=1)):
+        wl.params["stage_mode"] = 1
+        wls.append(wl)
+    ens = Ensemble(wls, precision=precision, mode="graph")
+    ens.first_update(10.0)
+    for t in (20.0, 30.0, 40.0, 50.0):
+        ens.update(t)
+    ens.synchronize()
+    got = [d.field("w") for d in ens.doms]
+    ens.close()
+    for wl, g in zip(wls, got):
+        dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=precision)
+        f = wl.padded_fields(dom.nx, dom.ny)
+        if f:
+            dom.set_fields(**f)
+        b = gpu_bsl()
+        dom.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+        for t in (10.0, 20.0, 30.0, 40.0, 50.0):
+            dom.update(wl.H_final, t, b)
+        w = dom.field("w")
+        dom.close()
+        if precision == 1:
+            assert np.abs(w - g).max() <= 1e-5 * np.abs(w).max()
+        else:
+            assert np.array_equal(w, g)
