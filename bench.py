@@ -628,6 +628,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--ensemble-members", type=int, default=256)
+    ap.add_argument("--ensemble-updates", type=int, default=10)
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--only", choices=["ensemble", "serve", "configs"],
                     help="run one secondary leg alone and print its JSON (for profiling), not a bench line")
@@ -659,7 +660,7 @@ def main():
 
     results = {}
     if args.only == "ensemble":
-        print(json.dumps({"ensemble": ensemble_leg(args.ensemble_members)}))
+        print(json.dumps({"ensemble": ensemble_leg(args.ensemble_members, args.ensemble_updates)}))
         return 0
     if args.only == "serve":
         print(json.dumps({"serve": serve_leg(n_req=args.serve_requests)}))
@@ -719,7 +720,7 @@ def main():
     if not args.no_configs:
         cfgs = configs_leg()
     if not args.no_ensemble:
-        ens = ensemble_leg(args.ensemble_members)
+        ens = ensemble_leg(args.ensemble_members, args.ensemble_updates)
     if not args.no_serve:
         serve = serve_leg(n_req=args.serve_requests)
 
