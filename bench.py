@@ -311,6 +311,8 @@ def ensemble_leg(n_members=256, n_updates=10):
         a = time.perf_counter()
         ens = Ensemble(wls, precision=1, mode=mode, groups=2 if mode == "graph" else 1)
         init_s = time.perf_counter() - a
+        if mode == "graph":
+            shapes = list(ens.shapes)
         ens.first_update(10.0)
         ens.update(20.0)
         ens.update(30.0)   # the first batched update of a kind is captured
@@ -382,6 +384,8 @@ def ensemble_leg(n_members=256, n_updates=10):
         "speedup": seq_s / batched_s, "batched_s": batched_s, "sequential_s": seq_s,
         "streams_mixed": mkyr / timed["streams"][0],
         "setup_s": {"batched_mixed": init_s, "sequential_fp64": seq_init},
+        "autotuned_shapes": [{"rows_per_block": a_[0], "columns_per_block": a_[1], "strip_rows": a_[2],
+                              "waves": a_[3]} for a_ in shapes],
         "err_vs_fp64": {
             "max_rel": float(errs.max()), "median_rel": float(np.median(errs)),
             "rms_rel": float(np.sqrt(np.mean(errs ** 2))),

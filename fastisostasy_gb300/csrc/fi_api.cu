@@ -1737,7 +1737,69 @@ struct fi_batch {
     int* dmore = nullptr;                // loop condition of the eager path
     bool eager = false;
     bool true_stages = false;            // members run Tsit5 with true stages (stage_mode 1)
+    std::vector<BMember> hM;             // host copy of the member descriptors
+    std::vector<int> hoff;               // host copy of the virtual-block offsets (4 x (nm + 1))
+    int shape[4] = {0, 0, 16, 8};        // rows / columns per transform block (0: single-domain shape), strip rows, waves
 };
+
+// Per-member transform and stencil shapes, the virtual-block offsets and
+// the resident grids of the batched launches; uploads the descriptors.
+// RB / CB <= 0: the single-domain shapes.
+int batch_shape(fi_batch* b, int RB, int CB, int fseg, int waves)
+{
+    const int n = b->nm;
+    std::vector<int> off(4 * (n + 1), 0);
+    const size_t c2 = b->mixed ? sizeof(float2) : sizeof(double2);
+    b->rows_threads = b->cols_threads = 0;
+    b->rows_smem = b->cols_smem = 0;
+    for (int i = 0; i < n; ++i) {
+        BMember& m = b->hM[i];
+        m.RB = RB > 0 ? RB : rhs_rows_per_block(m.p.h);
+        m.CB = CB > 0 ? CB : (b->mixed ? rhs_cols_per_block<float>(m.p.ny) : rhs_cols_per_block<double>(m.p.ny));
+        m.fseg = fseg;
+        const int fblk = (b->mixed && !b->true_stages) ? batch_flexure_blocks(m.p.nx, m.p.ny, m.fseg)
+                                                       : m.fgx * ((m.p.ny + 7) / 8);
+        const int rblk = (m.p.ny + m.RB - 1) / m.RB;
+        const int cblk = (m.p.h + 1 + m.CB - 1) / m.CB;
+        off[i + 1] = off[i] + fblk;
+        off[(n + 1) + i + 1] = off[(n + 1) + i] + rblk;
+        off[2 * (n + 1) + i + 1] = off[2 * (n + 1) + i] + cblk;
+        off[3 * (n + 1) + i + 1] = off[3 * (n + 1) + i] + m.red_nblk;
+        const int rt = rhs_threads_for(m.RB * m.p.h / 4), ct = rhs_threads_for(m.CB * m.p.ny / 4);
+        if (rt > b->rows_threads) b->rows_threads = rt;
+        if (ct > b->cols_threads) b->cols_threads = ct;
+        const size_t rs = 2 * (size_t)m.RB * m.p.h * c2, cs = 2 * (size_t)m.CB * (m.p.ny + 1) * c2;   // padded columns
+        if (rs > b->rows_smem) b->rows_smem = rs;
+        if (cs > b->cols_smem) b->cols_smem = cs;
+    }
+    if (b->rows_smem > 200 * 1024 || b->cols_smem > 200 * 1024) return 2;   // shape does not fit
+    for (int k = 0; k < 4; ++k) b->nblk[k] = off[k * (n + 1) + n];
+    b->hoff = off;
+    if (cudaMemcpy(b->dM, b->hM.data(), n * sizeof(BMember), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b->doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+        return 1;
+    int res[4];
+    if (b->mixed) {
+        batch_prepare<float>(b->rows_smem, b->cols_smem);
+        batch_grids<float>(b->rows_smem, b->cols_smem, b->rows_threads, b->cols_threads, &res[0], &res[1], &res[2],
+                           &res[3]);
+    } else {
+        batch_prepare<double>(b->rows_smem, b->cols_smem);
+        batch_grids<double>(b->rows_smem, b->cols_smem, b->rows_threads, b->cols_threads, &res[0], &res[1], &res[2],
+                            &res[3]);
+    }
+    // resident grid times `waves`, at most one block per virtual block
+    for (int k = 0; k < 4; ++k) {
+        const long long g = waves > 0 ? (long long)res[k] * waves : (long long)b->nblk[k];
+        b->grid[k] = (int)(g < b->nblk[k] ? g : b->nblk[k]);
+        if (b->grid[k] < 1) b->grid[k] = 1;
+    }
+    b->shape[0] = RB;
+    b->shape[1] = CB;
+    b->shape[2] = fseg;
+    b->shape[3] = waves;
+    return 0;
+}
 
 namespace {
 
@@ -1934,8 +1996,6 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
     b->mixed = mixed(hs[0]);
     b->true_stages = hs[0]->p.stage_mode == 1;
     std::vector<BMember> M(n);
-    std::vector<int> off(4 * (n + 1), 0);
-    const size_t c2 = b->mixed ? sizeof(float2) : sizeof(double2);
     for (int i = 0; i < n; ++i) {
         fi_handle* h = hs[i];
         BMember& m = M[i];
@@ -1957,18 +2017,6 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         m.yst = h->y;
         m.wref = h->w_ref;
         m.even = h->even;
-        m.RB = rhs_rows_per_block(m.p.h);
-        m.CB = b->mixed ? rhs_cols_per_block<float>(m.p.ny) : rhs_cols_per_block<double>(m.p.ny);
-        if (b->mixed) {
-            // many members share a launch: 8 rows / 8 spectrum columns per
-            // virtual block (64-byte column segments) measured faster than
-            // the single-domain shapes on a 256-member ensemble
-            m.RB = m.RB < 8 ? 8 : m.RB;
-            m.CB = 8;
-        }
-        // FI_BATCH_RB / FI_BATCH_CB: rows / spectrum columns per batched transform block (tuning)
-        if (const char* e = getenv("FI_BATCH_RB")) { const int v = atoi(e); if (v >= 1 && v <= 16) m.RB = v; }
-        if (const char* e = getenv("FI_BATCH_CB")) { const int v = atoi(e); if (v >= 1 && v <= 16) m.CB = v; }
         m.fgx = (m.p.nx + 31) / 32;
         m.red_nblk = ts_grid(h->n);
         m.d = h->d;
@@ -1976,28 +2024,12 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         m.rtol = h->p.rtol;
         m.q = h->p.q;
         m.dt_max = h->p.dt_max;
-        m.fseg = 16;
-        const int fblk = (b->mixed && !b->true_stages) ? batch_flexure_blocks(m.p.nx, m.p.ny, m.fseg)
-                                                       : m.fgx * ((m.p.ny + 7) / 8);
-        const int rblk = (m.p.ny + m.RB - 1) / m.RB;
-        const int cblk = (m.p.h + 1 + m.CB - 1) / m.CB;
-        off[i + 1] = off[i] + fblk;
-        off[(n + 1) + i + 1] = off[(n + 1) + i] + rblk;
-        off[2 * (n + 1) + i + 1] = off[2 * (n + 1) + i] + cblk;
-        off[3 * (n + 1) + i + 1] = off[3 * (n + 1) + i] + m.red_nblk;
-        const int rt = rhs_threads_for(m.RB * m.p.h / 4), ct = rhs_threads_for(m.CB * m.p.ny / 4);
-        if (rt > b->rows_threads) b->rows_threads = rt;
-        if (ct > b->cols_threads) b->cols_threads = ct;
-        const size_t rs = 2 * (size_t)m.RB * m.p.h * c2, cs = 2 * (size_t)m.CB * (m.p.ny + 1) * c2;   // padded columns
-        if (rs > b->rows_smem) b->rows_smem = rs;
-        if (cs > b->cols_smem) b->cols_smem = cs;
     }
-    for (int k = 0; k < 4; ++k) b->nblk[k] = off[k * (n + 1) + n];
     bool ok = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&b->s_body, cudaStreamNonBlocking) == cudaSuccess &&
               cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
               cudaMalloc(&b->dM, n * sizeof(BMember)) == cudaSuccess &&
-              cudaMalloc(&b->doff, off.size() * sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&b->doff, 4 * (size_t)(n + 1) * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&b->dcl, blist_ints(n) * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&b->dmore, sizeof(int)) == cudaSuccess;
     if (const char* e = getenv("FI_BATCH_EAGER")) b->eager = (e[0] == '1');
@@ -2007,30 +2039,115 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         ok = cudaMallocHost(&b->hargs[i], n * sizeof(BArgs)) == cudaSuccess &&
              cudaMalloc(&b->dargs[i], n * sizeof(BArgs)) == cudaSuccess &&
              cudaEventCreateWithFlags(&b->args_ev[i], cudaEventDisableTiming) == cudaSuccess;
-    ok = ok && cudaMemcpy(b->dM, M.data(), n * sizeof(BMember), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(b->doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
     if (!ok) {
         batch_free(b);
         return FI_E_OOM;
     }
-    int res[4];
-    if (b->mixed) {
-        batch_prepare<float>(b->rows_smem, b->cols_smem);
-        batch_grids<float>(b->rows_smem, b->cols_smem, b->rows_threads, b->cols_threads, &res[0], &res[1], &res[2],
-                           &res[3]);
-    } else {
-        batch_prepare<double>(b->rows_smem, b->cols_smem);
-        batch_grids<double>(b->rows_smem, b->cols_smem, b->rows_threads, b->cols_threads, &res[0], &res[1], &res[2],
-                            &res[3]);
-    }
-    // resident grid times FI_BATCH_WAVES (default 8) waves, at most one block per virtual block
-    int waves = 8;
+    b->hM.swap(M);
+    // default shapes: 8 rows / 8 spectrum columns per transform block for
+    // mixed batches (64-byte column segments), 16-row strip tasks, 8 waves;
+    // FI_BATCH_RB / FI_BATCH_CB / FI_BATCH_WAVES override (tuning)
+    int RB = b->mixed ? 8 : 0, CB = b->mixed ? 8 : 0, waves = 8;
+    if (const char* e = getenv("FI_BATCH_RB")) { const int v = atoi(e); if (v >= 1 && v <= 16) RB = v; }
+    if (const char* e = getenv("FI_BATCH_CB")) { const int v = atoi(e); if (v >= 1 && v <= 16) CB = v; }
     if (const char* e = getenv("FI_BATCH_WAVES")) waves = atoi(e);
-    for (int k = 0; k < 4; ++k) {
-        const long long g = waves > 0 ? (long long)res[k] * waves : (long long)b->nblk[k];
-        b->grid[k] = (int)(g < b->nblk[k] ? g : b->nblk[k]);
+    if (batch_shape(b, RB, CB, 16, waves)) {
+        batch_free(b);
+        return FI_E_CUDA;
     }
     *out = b;
+    return FI_OK;
+}
+
+namespace {
+
+// Lists of all members (every list kind) for timing the batched passes.
+int batch_all_lists(fi_batch* b)
+{
+    const int n = b->nm;
+    std::vector<int> cl(blist_ints(n), 0);
+    cl[0] = cl[1] = n;
+    for (int i = 0; i < n; ++i) cl[2 + i] = cl[2 + n + i] = i;
+    for (int k = 0; k < 7; ++k) {
+        const int src = k < 3 ? k : (k == 3 ? 3 : k - 4);
+        for (int i = 0; i <= n; ++i) cl[2 + 2 * n + k * (n + 1) + i] = b->hoff[src * (n + 1) + i];
+    }
+    return cudaMemcpy(b->dcl, cl.data(), cl.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess ? 0 : 1;
+}
+
+// Device time [ms] of the first RHS of an attempt over all members: part 1
+// the stencil, 2 the row transforms, 3 the column transform, 0 all; best of
+// `reps` after one warm-up.
+template <typename T> float batch_time_rhs(fi_batch* b, int part, int reps)
+{
+    const int nm = b->nm;
+    const BList LF = blist(b->dcl, nm, 0), LR = blist(b->dcl, nm, 1), LC = blist(b->dcl, nm, 2);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int r = 0; r <= reps; ++r) {
+        cudaEventRecord(e0, b->s);
+        if (part == 0 || part == 1) {
+            if (b->true_stages) batch_flexure_y<T>(b->dM, LF, b->grid[0], 0, b->s);
+            else batch_flexure<T>(b->dM, LF, b->grid[0], b->s);
+        }
+        if (part == 0 || part == 2) batch_rows_fwd<T>(b->dM, LR, b->grid[1], b->rows_threads, b->rows_smem, b->s);
+        if (part == 0 || part == 3) batch_cols_hartley<T>(b->dM, LC, b->grid[2], b->cols_threads, b->cols_smem, b->s);
+        if (part == 0 || part == 2) batch_rows_inv<T>(b->dM, LR, b->grid[1], b->rows_threads, b->rows_smem, b->s, 0);
+        cudaEventRecord(e1, b->s);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return cudaGetLastError() == cudaSuccess ? best : -1.f;
+}
+
+}  // namespace
+
+int fi_batch_autotune(fi_batch* b, int32_t* chosen4)
+{
+    if (!b) return FI_E_ARG;
+    if (b->seen[0] || b->seen[1]) return FI_E_STATE;
+    for (fi_handle* h : b->hs)
+        if (cudaStreamSynchronize(h->s) != cudaSuccess) return FI_E_CUDA;
+    // the stencil of the reference stages reads now%w's float pair
+    for (fi_handle* h : b->hs)
+        if (h->d.whi) split_hilo(h->d.w, h->d.whi, h->d.wlo, h->n, b->s);
+    auto time_of = [&](int part) { return b->mixed ? batch_time_rhs<float>(b, part, 3) : batch_time_rhs<double>(b, part, 3); };
+    int sh[4] = {b->shape[0], b->shape[1], b->shape[2], b->shape[3]};
+    auto try_shape = [&](const int* c, int part, float* t) -> int {
+        const int rc = batch_shape(b, c[0], c[1], c[2], c[3]);
+        if (rc == 2) { *t = 1e30f; return 0; }   // does not fit
+        if (rc || batch_all_lists(b)) return 1;
+        *t = time_of(part);
+        return *t < 0 ? 1 : 0;
+    };
+    // coordinate descent: stencil rows per task, transform rows, transform
+    // columns, then waves over the whole RHS
+    const int seg_c[3] = {8, 16, 32}, rb_c[4] = {2, 4, 8, 16}, cb_c[5] = {1, 2, 4, 8, 16}, wv_c[4] = {2, 4, 8, 16};
+    struct Axis { int idx, part, nc; const int* c; };
+    const Axis axes[4] = {{2, 1, 3, seg_c}, {0, 2, 4, rb_c}, {1, 3, 5, cb_c}, {3, 0, 4, wv_c}};
+    for (const Axis& ax : axes) {
+        if (ax.idx == 2 && (!b->mixed || b->true_stages)) continue;   // column strips: mixed reference stages only
+        int best_v = sh[ax.idx];
+        float best_t = 1e30f;
+        for (int k = 0; k < ax.nc; ++k) {
+            int c[4] = {sh[0], sh[1], sh[2], sh[3]};
+            c[ax.idx] = ax.c[k];
+            float t;
+            if (try_shape(c, ax.part, &t)) return FI_E_CUDA;
+            if (t < best_t) { best_t = t; best_v = ax.c[k]; }
+        }
+        sh[ax.idx] = best_v;
+    }
+    if (batch_shape(b, sh[0], sh[1], sh[2], sh[3])) return FI_E_CUDA;
+    if (cudaStreamSynchronize(b->s) != cudaSuccess) return FI_E_CUDA;
+    if (chosen4)
+        for (int k = 0; k < 4; ++k) chosen4[k] = sh[k];
     return FI_OK;
 }
 

@@ -141,12 +141,14 @@ class Ensemble:
     (max D / (eta dx^3), which sets how many attempts an update needs) and
     split into that many groups, each a batch on its own stream, so a stiff
     member holds back only the members of its own group; with `priority`
-    the stiffest group's stream has the device's highest priority.
+    the stiffest group's stream has the device's highest priority; with
+    `autotune` each batch's transform and stencil shapes are chosen by
+    timing candidates on its own members (fi_batch_autotune).
     mode "streams": fi_batch_update enqueues one isos_update per member on
     the member's own stream (any integrator)."""
 
     def __init__(self, workloads, precision: int = 1, mode: str = "graph", groups: int = 1,
-                 priority: bool = True):
+                 priority: bool = True, autotune: bool = True):
         from .isostasy import Domain
         self.L = _lib.load()
         self.mode = mode
@@ -180,6 +182,7 @@ class Ensemble:
         self.wls = list(workloads)
         self.hss = [(C.c_void_p * len(m))(*[self.doms[i].h.value for i in m]) for m in self.groups]
         self.batches = []
+        self.shapes = []   # autotuned (rows, columns, strip rows, waves) per batch
         if mode == "graph":
             for g, (hs, m) in enumerate(zip(self.hss, self.groups)):
                 bh = C.c_void_p()
@@ -187,6 +190,12 @@ class Ensemble:
                 if rc:
                     raise FiError(rc, "fi_batch_create")
                 self.batches.append(bh)
+                if autotune:
+                    shape = (C.c_int32 * 4)()
+                    rc = self.L.fi_batch_autotune(bh, shape)
+                    if rc:
+                        raise FiError(rc, "fi_batch_autotune")
+                    self.shapes.append(tuple(shape))
                 if g == 0 and len(self.groups) > 1 and priority:
                     # the stiffest group has the longest chain of attempts:
                     # its launches go first, the other groups fill idle SMs

@@ -290,6 +290,15 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out);   /* 1 <= n <=
  * with the longest chain of attempts go first while the others fill the
  * SMs it leaves idle.  Only before the batch's first fi_batch_step. */
 int fi_batch_set_priority(fi_batch* b, int level);
+/* Autotuner of the batched passes (no reference counterpart): times the
+ * first RHS of an attempt over all members on the device for candidate
+ * shapes — stencil rows per column-strip task (8/16/32), rows per row-
+ * transform block (2/4/8/16), spectrum columns per column-transform block
+ * (1/2/4/8/16), resident-grid waves (2/4/8/16) — by coordinate descent,
+ * and keeps the fastest.  Overwrites the members' RHS scratch (dead between
+ * updates).  Only before the batch's first fi_batch_step.  chosen4 (or
+ * NULL): rows, columns, strip rows, waves. */
+int fi_batch_autotune(fi_batch* b, int32_t* chosen4);
 int fi_batch_step(fi_batch* b, double time, fi_bsl* bsl);
 int fi_batch_wait(fi_batch* b, int32_t* status);
 int fi_batch_destroy(fi_batch* b);
