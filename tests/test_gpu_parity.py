@@ -101,8 +101,9 @@ def ref_disc(name, n=31, dx=200e3, **over):
     return W.Workload(name=name, params=p, nx_ice=n, ny_ice=n, dx=dx, z_bed=np.full((n, n), 1e6), H_final=H)
 
 
-@pytest.mark.parametrize("name,over", [("test1d", {}), ("test1e", {}), ("test2c", {}), ("test3a", {}),
-                                       ("test3c", {}), ("test2c", {"lithosphere": 2})])
+@pytest.mark.parametrize("name,over", [("test1d", {}), ("test1e", {}), ("test2a", {}), ("test2b", {}), ("test2c", {}),
+                                       ("test3a", {}), ("test3b", {}), ("test3c", {}), ("test3d", {}),
+                                       ("test2c", {"lithosphere": 2})])
 def test_reference_experiments_tsit54(name, over):
     """Reference experiments (par/*.nml) with the reference's own integrator
     semantics (frozen RHS, transposed Tsit5 tableau).  test2c with a
