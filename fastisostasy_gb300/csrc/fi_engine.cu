@@ -366,26 +366,37 @@ __global__ void __launch_bounds__(512, 2) k_engine_rk4(EngineArgs g)
     const size_t n = (size_t)nx * ny;
     const int na = (ny + RA - 1) / RA, nb = (g.p.h + 1 + g.CB - 1) / g.CB, nc = (ny + RC - 1) / RC;
     Ctl* ctl = g.ctl;
-    __shared__ double s_h;
-    const bool tr = g.trace && blockIdx.x == 0 && threadIdx.x == 0;
+    // The step control is replicated in every block (the same arithmetic on
+    // the same inputs, so every block decides alike) instead of broadcast
+    // through a grid barrier; block 0 keeps the control block up to date.
+    __shared__ double s_t, s_tf, s_dt;
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        s_t = ctl->t;
+        s_tf = ctl->tf;
+        s_dt = ctl->dt;
+        s_ok = ctl->status == ST_OK;
+    }
+    __syncthreads();
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    const bool tr = g.trace && lead;
     int tk = 0;
 #define TRACE() do { if (tr && step == 0 && tk < 64) g.trace[tk++] = gtimer(); } while (0)
     for (int step = 0; step < g.nsteps; ++step) {
         TRACE();
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            // step_rk4: h = min(dt, tf - t) (src/integrators.f90:62-63)
-            if (ctl->status == ST_OK && ctl->t < ctl->tf) {
-                ctl->h = fmin(ctl->dt, ctl->tf - ctl->t);
-                ctl->done = 0;
-            } else {
-                ctl->done = 1;
-            }
+        const double t = s_t;
+        if (!(s_ok && t < s_tf)) {   // uniform over the grid
+            if (lead) ctl->done = 1;
+            return;
         }
-        grid.sync();
-        if (threadIdx.x == 0) s_h = ((volatile Ctl*)ctl)->done ? -1.0 : ((volatile Ctl*)ctl)->h;
-        __syncthreads();
-        const double h = s_h;
-        if (h < 0.0) return;   // uniform over the grid
+        // step_rk4: h = min(dt, tf - t) (src/integrators.f90:62-63)
+        const double h = fmin(s_dt, s_tf - t);
+        if (lead) {
+            ctl->h = h;
+            ctl->done = 0;
+        }
+        // now%w is read by nothing inside the engine: written in the last step only
+        const bool last = step + 1 == g.nsteps || !(t + h < s_tf);
         TRACE();
         for (int stage = 0; stage < 4; ++stage) {
             for (int it = blockIdx.x; it < na; it += gridDim.x) phase_a<T>(g, it * RA, stage, h, smem);
@@ -421,7 +432,7 @@ __global__ void __launch_bounds__(512, 2) k_engine_rk4(EngineArgs g)
                 const float inc = k * scf;
                 const double v = g.x[e] + (double)inc;   // the FP64 state update
                 g.x[e] = v;
-                g.w[e] = v;
+                if (last) g.w[e] = v;
                 // the float pair of x takes the same increment by an FP32 two-sum
                 const float hi = g.xhi[e], lo = g.xlo[e];
                 const float sm = hi + inc, bb = sm - hi;
@@ -435,11 +446,12 @@ __global__ void __launch_bounds__(512, 2) k_engine_rk4(EngineArgs g)
                 const double k3 = ((double)r3[e] - s_c[3]) * g.spy, k4 = ((double)r4[e] - s_c[4]) * g.spy;
                 const double v = g.x[e] + s_c[0] * (((k1 + 2 * k2) + 2 * k3) + k4);
                 g.x[e] = v;
-                g.w[e] = v;
+                if (last) g.w[e] = v;
             }
         }
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            ctl->t = ctl->t + h;
+        if (threadIdx.x == 0) s_t = t + h;   // read after the grid barrier below
+        if (lead) {
+            ctl->t = t + h;
             ctl->n_accept++;
         }
         TRACE();
