@@ -471,11 +471,20 @@ int upload_static(fi_handle* h)
 int kernel_spectrum(fi_handle* h, const std::vector<double>& ker, int which)
 {
     const size_t hs = (size_t)h->pconv.ny * h->pconv.sp;
-    double* tmp;
-    double2* S64;
+    double* tmp = nullptr;
+    double2* S64 = nullptr;
     int rc;
-    if ((rc = dalloc(h, &tmp, h->n * sizeof(double))) || (rc = dalloc(h, &S64, hs * sizeof(double2)))) return rc;
-    if ((rc = upload(h, tmp, ker.data(), h->n * sizeof(double)))) return rc;
+    // stream-ordered temporaries: no device-wide synchronisation at set-up
+    if (cudaMallocAsync((void**)&tmp, h->n * sizeof(double), h->s) != cudaSuccess) return fail(h, FI_E_OOM, "spectrum");
+    if (cudaMallocAsync((void**)&S64, hs * sizeof(double2), h->s) != cudaSuccess) {
+        cudaFreeAsync(tmp, h->s);
+        return fail(h, FI_E_OOM, "spectrum");
+    }
+    if ((rc = upload(h, tmp, ker.data(), h->n * sizeof(double)))) {
+        cudaFreeAsync(tmp, h->s);
+        cudaFreeAsync(S64, h->s);
+        return rc;
+    }
     launch_rows_fwd<double>(tmp, h->nx, h->nx, h->ny, S64, h->pconv, h->s);
     launch_cols_fwd<double>(S64, h->ny, h->pconv, h->s);
     CK(cudaGetLastError());
@@ -484,13 +493,9 @@ int kernel_spectrum(fi_handle* h, const std::vector<double>& ker, int which)
     } else {
         CK(cudaMemcpyAsync(h->KS[which], S64, hs * sizeof(double2), cudaMemcpyDeviceToDevice, h->s));
     }
+    cudaFreeAsync(tmp, h->s);
+    cudaFreeAsync(S64, h->s);
     CK(cudaStreamSynchronize(h->s));
-    // release the temporaries
-    for (void* p : {(void*)tmp, (void*)S64}) {
-        for (size_t i = 0; i < h->allocs.size(); ++i)
-            if (h->allocs[i] == p) { h->allocs.erase(h->allocs.begin() + i); break; }
-        cudaFree(p);
-    }
     return FI_OK;
 }
 

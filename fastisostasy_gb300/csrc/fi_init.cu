@@ -60,7 +60,8 @@ int init_fields_device(int nx, int ny, double dx, double dy, double pi_lit, doub
 {
     const size_t n = (size_t)nx * ny;
     double* buf = nullptr;
-    if (cudaMalloc(&buf, 3 * n * sizeof(double)) != cudaSuccess) return 1;
+    // stream-ordered: set-up of one handle never waits for other handles' work
+    if (cudaMallocAsync((void**)&buf, 3 * n * sizeof(double), s) != cudaSuccess) return 1;
     int rc = 0;
     if (cudaMemcpyToSymbolAsync(c_ge_rn, ge_rn, 42 * sizeof(float), 0, cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyToSymbolAsync(c_ge_v, ge_v, 42 * sizeof(float), 0, cudaMemcpyHostToDevice, s) != cudaSuccess)
@@ -78,7 +79,7 @@ int init_fields_device(int nx, int ny, double dx, double dy, double pi_lit, doub
             cudaStreamSynchronize(s) != cudaSuccess)
             rc = 1;
     }
-    cudaFree(buf);
+    cudaFreeAsync(buf, s);
     if (!rc) kappa[0] = (kappa[nx] + kappa[1]) / 2.0;   // kappa(1,1), src/lv_elva.f90:478
     return rc;
 }
@@ -338,16 +339,21 @@ __global__ void k_smooth_pass(double* __restrict__ out, const double* __restrict
 
 namespace {
 
+// Scratch of one set-up call, stream-ordered (cudaMallocAsync /
+// cudaFreeAsync on the handle's stream): no device-wide synchronisation, so
+// handles created while others run (serving) do not stall them.
 struct DevBuf {
+    cudaStream_t s;
     std::vector<void*> p;
+    explicit DevBuf(cudaStream_t st) : s(st) {}
     ~DevBuf()
     {
-        for (void* q : p) cudaFree(q);
+        for (void* q : p) cudaFreeAsync(q, s);
     }
     template <typename T> T* get(size_t count)
     {
         void* q = nullptr;
-        if (cudaMalloc(&q, count * sizeof(T) + 16) != cudaSuccess) return nullptr;
+        if (cudaMallocAsync(&q, count * sizeof(T) + 16, s) != cudaSuccess) return nullptr;
         p.push_back(q);
         return (T*)q;
     }
@@ -396,7 +402,7 @@ int rheology_device(const RheoParams& P, const double* xc, const double* yc, dou
     const int nx = P.nx, ny = P.ny;
     const size_t n = (size_t)nx * ny;
     const int G = grid_of(n);
-    DevBuf B;
+    DevBuf B(s);
     double *dxc = B.get<double>(nx), *dyc = B.get<double>(ny), *He = B.get<double>(n), *D = B.get<double>(n);
     double *eta = B.get<double>(n), *R = B.get<double>(n), *tmp = B.get<double>(n);
     unsigned long long* ext = B.get<unsigned long long>(1);
