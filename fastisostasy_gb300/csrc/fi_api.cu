@@ -231,10 +231,12 @@ template <typename P> int dalloc(fi_handle* h, P** out, size_t bytes)
 {
     void* p = nullptr;
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(&p, bytes);
+    // stream-ordered on the handle's stream: creating and destroying handles
+    // (a serving loop) never synchronises the device under other requests
+    cudaError_t e = cudaMallocAsync(&p, bytes, h->s);
     if (e != cudaSuccess) {
         *out = nullptr;
-        return fail(h, e == cudaErrorMemoryAllocation ? FI_E_OOM : FI_E_CUDA, "cudaMalloc(%zu): %s", bytes,
+        return fail(h, e == cudaErrorMemoryAllocation ? FI_E_OOM : FI_E_CUDA, "cudaMallocAsync(%zu): %s", bytes,
                     cudaGetErrorString(e));
     }
     h->allocs.push_back(p);
@@ -1240,8 +1242,13 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
 int fi_destroy(fi_handle* h)
 {
     if (!h) return FI_OK;
-    if (h->s) cudaStreamSynchronize(h->s);
-    for (void* p : h->allocs) cudaFree(p);
+    if (h->s_out) cudaStreamSynchronize(h->s_out);
+    if (h->s) {
+        for (void* p : h->allocs) cudaFreeAsync(p, h->s);
+        cudaStreamSynchronize(h->s);
+    } else {
+        for (void* p : h->allocs) cudaFree(p);
+    }
     if (h->hpin) cudaFreeHost(h->hpin);
     for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
