@@ -6,12 +6,14 @@
 // the device kernels in the order of isos_update
 // (src/fastisostasy.f90:731-872).  There is no CPU compute path: every
 // per-cell operation of init_state/update runs on the device.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/fi_gpu.h"
@@ -1478,15 +1480,33 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
     rc = read_status(h, &hc);
     bsl->bsl_now = hc.bsl;
     if (out) {
+        // the staged fields into the caller's arrays: one host thread per
+        // slice of fields (a single core copies a few GB/s; the fields are
+        // ~100 B per cell)
         double* dst[8] = {out->z_bed, out->z_ss, out->dz_ss, out->w, out->we, out->dwdt, out->canom_full, out->Hice};
-        for (int f = 0; f < 8; ++f)
-            if (dst[f]) memcpy(dst[f], h->hpin + (size_t)f * ni, ni * 8);
         uint8_t* mdst[3] = {out->maskocean, out->maskgrounded, out->maskcontinent};
-        for (int f = 0; f < 3; ++f)
-            if (mdst[f]) {
-                const double* src = h->hpin + (size_t)(8 + f) * ni;
-                for (size_t e = 0; e < ni; ++e) mdst[f][e] = src[e] != 0.0;
+        auto copy_field = [&](int f) {
+            if (f < 8) {
+                if (dst[f]) memcpy(dst[f], h->hpin + (size_t)f * ni, ni * 8);
+            } else if (mdst[f - 8]) {
+                const double* src = h->hpin + (size_t)f * ni;
+                uint8_t* m = mdst[f - 8];
+                for (size_t e = 0; e < ni; ++e) m[e] = src[e] != 0.0;
             }
+        };
+        const unsigned hw = std::thread::hardware_concurrency();
+        const int nthr = ni < (1u << 16) ? 1 : (int)std::min<unsigned>(hw > 1 ? hw : 1, 11u);
+        if (nthr <= 1) {
+            for (int f = 0; f < 11; ++f) copy_field(f);
+        } else {
+            std::vector<std::thread> pool;
+            for (int t = 1; t < nthr; ++t)
+                pool.emplace_back([&, t] {
+                    for (int f = t; f < 11; f += nthr) copy_field(f);
+                });
+            for (int f = 0; f < 11; f += nthr) copy_field(f);
+            for (auto& th : pool) th.join();
+        }
     }
     return rc;
 }
