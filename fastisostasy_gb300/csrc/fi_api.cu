@@ -13,6 +13,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <functional>
+#include <mutex>
+#include <condition_variable>
 #include <thread>
 #include <vector>
 
@@ -26,6 +29,104 @@
 using namespace fi;
 
 namespace {
+
+// A small persistent pool of host threads for the copies between the
+// caller's arrays and the page-locked staging buffer (a single core copies a
+// few GB/s; the isos%out fields are ~100 B per cell).  run(n, fn) calls
+// fn(0..n-1) on the workers and the calling thread and returns when all are
+// done; one job at a time.
+class HostPool {
+public:
+    static HostPool& get()
+    {
+        static HostPool p;
+        return p;
+    }
+    void run(int ntasks, const std::function<void(int)>& fn)
+    {
+        if (ntasks <= 1 || workers_.empty()) {
+            for (int i = 0; i < ntasks; ++i) fn(i);
+            return;
+        }
+        std::lock_guard<std::mutex> job(job_mu_);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            fn_ = &fn;
+            ntasks_ = ntasks;
+            next_ = 0;
+            pending_ = ntasks;
+            ++gen_;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&] { return pending_ == 0; });
+        fn_ = nullptr;
+    }
+
+private:
+    HostPool()
+    {
+        unsigned hw = std::thread::hardware_concurrency();
+        const int nw = (int)std::min<unsigned>(hw > 1 ? hw - 1 : 0, 7u);
+        for (int i = 0; i < nw; ++i)
+            workers_.emplace_back([this] {
+                unsigned long long seen = 0;
+                for (;;) {
+                    {
+                        std::unique_lock<std::mutex> lk(mu_);
+                        cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                        if (stop_) return;
+                        seen = gen_;
+                    }
+                    work();
+                }
+            });
+    }
+    ~HostPool()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : workers_) t.join();
+    }
+    void work()
+    {
+        for (;;) {
+            int i;
+            const std::function<void(int)>* f;
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                if (!fn_ || next_ >= ntasks_) return;
+                i = next_++;
+                f = fn_;
+            }
+            (*f)(i);
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--pending_ == 0) done_cv_.notify_all();
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex mu_, job_mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(int)>* fn_ = nullptr;
+    int ntasks_ = 0, next_ = 0, pending_ = 0;
+    unsigned long long gen_ = 0;
+    bool stop_ = false;
+};
+
+// dst <- src in `parts` slices on the pool
+void pool_copy(void* dst, const void* src, size_t bytes, int parts)
+{
+    const size_t chunk = (bytes + parts - 1) / parts;
+    HostPool::get().run(parts, [&](int i) {
+        const size_t a = (size_t)i * chunk;
+        if (a < bytes) memcpy((char*)dst + a, (const char*)src + a, std::min(chunk, bytes - a));
+    });
+}
+
 
 const double PI_LIT = (double)3.14159265359f;   // src/isostasy_defs.f90:8 (default-real literal)
 inline double sp(double x) { return (double)(float)x; }
@@ -1468,7 +1569,8 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
     if (!h->state_ready) return fail(h, FI_E_STATE, "fi_update before fi_init_state");
     const size_t ni = (size_t)h->nx_ice * h->ny_ice;
     int rc;
-    memcpy(h->hpin, H_ice, ni * 8);
+    if (ni < (1u << 16)) memcpy(h->hpin, H_ice, ni * 8);
+    else pool_copy(h->hpin, H_ice, ni * 8, 4);
     CK(cudaMemcpyAsync(h->dH, h->hpin, ni * 8, cudaMemcpyHostToDevice, h->s));
     enqueue_args(h, time, bsl, true);
     if ((rc = update_any(h, h->dH, time, true))) return rc;
@@ -1494,18 +1596,10 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
                 for (size_t e = 0; e < ni; ++e) m[e] = src[e] != 0.0;
             }
         };
-        const unsigned hw = std::thread::hardware_concurrency();
-        const int nthr = ni < (1u << 16) ? 1 : (int)std::min<unsigned>(hw > 1 ? hw : 1, 11u);
-        if (nthr <= 1) {
+        if (ni < (1u << 16)) {
             for (int f = 0; f < 11; ++f) copy_field(f);
         } else {
-            std::vector<std::thread> pool;
-            for (int t = 1; t < nthr; ++t)
-                pool.emplace_back([&, t] {
-                    for (int f = t; f < 11; f += nthr) copy_field(f);
-                });
-            for (int f = 0; f < 11; f += nthr) copy_field(f);
-            for (auto& th : pool) th.join();
+            HostPool::get().run(11, copy_field);
         }
     }
     return rc;
