@@ -197,9 +197,13 @@ def test_mixed_precision_error_bound():
     a.close(); b.close()
 
 
-def test_outputs_and_restart_roundtrip():
-    wl = W.config2(n=32, L=3000e3 * 32 / 256, dt=1.0, stage_mode=1)
-    pair = Pair(wl)
+@pytest.mark.parametrize("precision,n", [(0, 32), (1, 64)])
+def test_outputs_and_restart_roundtrip(precision, n):
+    """isos%out of fi_update equals the fields; a restart (state export,
+    further updates, import) repeats an update bit for bit — in the mixed
+    form through the step engine, whose row flags restart with the state."""
+    wl = W.config2(n=n, L=3000e3 * n / 256, dt=1.0, stage_mode=1)
+    pair = Pair(wl, precision=precision)
     pair.init()
     pair.step(3)
     dom = pair.dom
@@ -212,6 +216,7 @@ def test_outputs_and_restart_roundtrip():
     assert np.array_equal(out["w"], dom.crop(dom.field("w")))
     assert np.array_equal(out["z_bed"], dom.crop(dom.field("z_bed")))
     w1 = dom.field("w")
+    dom.update(wl.H_at(t + wl.dtt), t + wl.dtt, pair.bg)   # advance further before the restart
     dom.state_import(buf)
     dom.update(wl.H_at(t), t, pair.bg)
     assert np.array_equal(dom.field("w"), w1)
