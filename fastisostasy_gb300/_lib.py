@@ -33,7 +33,7 @@ EXPORTS = ["fi_create", "fi_destroy", "fi_dims", "fi_set_fields", "fi_set_kernel
            "fi_serve_result", "fi_serve_clock", "fi_serve_destroy", "fi_batch_update", "fi_batch_synchronize",
            "fi_batch_create", "fi_batch_step", "fi_batch_wait", "fi_batch_destroy", "fi_elva_disk",
            "fi_batch_set_priority", "fi_set_rheology", "fi_output_bytes", "fi_output_async",
-           "fi_output_wait", "fi_batch_autotune"]
+           "fi_output_wait", "fi_batch_autotune", "fi_set_stream"]
 
 PROFILE_KERNELS = ["flexure", "rows_fwd", "cols_hartley", "rows_inv", "conv_rows_fwd", "conv_cols",
                    "conv_rows_inv", "rk_stage", "rk_final", "upd_begin", "upd_masks", "upd_litho",
@@ -167,6 +167,7 @@ def load(build_if_missing: bool = True):
     L.fi_batch_step.argtypes = [H, C.c_double, C.POINTER(FiBsl)]
     L.fi_batch_set_priority.argtypes = [H, C.c_int]
     L.fi_batch_autotune.argtypes = [H, C.POINTER(C.c_int32)]
+    L.fi_set_stream.argtypes = [H, C.c_void_p]
     L.fi_batch_wait.argtypes = [H, C.POINTER(C.c_int32)]
     L.fi_batch_destroy.argtypes = [H]
     L.fi_elva_disk.argtypes = [C.c_int, C.c_int] + [C.c_double] * 9 + [_dp]

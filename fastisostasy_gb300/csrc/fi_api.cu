@@ -217,7 +217,8 @@ struct fi_handle {
     size_t prof_used = 0;
     double prof_ms[32] = {0};
     long long prof_cnt[32] = {0};
-    cudaStream_t s = nullptr;
+    cudaStream_t s = nullptr;            // work of this handle (its own, or the caller's: fi_set_stream)
+    cudaStream_t s_own = nullptr;        // the handle's own stream while the caller's is in use
     cudaStream_t s_body = nullptr;       // captures the body of the device Tsit5 loop
     std::vector<void*> allocs;
     std::string err;
@@ -1039,6 +1040,16 @@ int fi_version(void) { return 1; }
 
 void* fi_stream(fi_handle* h) { return h ? (void*)h->s : nullptr; }
 
+int fi_set_stream(fi_handle* h, void* stream)
+{
+    if (!h) return FI_E_ARG;
+    if (h->s_out) CK(cudaStreamSynchronize(h->s_out));
+    CK(cudaStreamSynchronize(h->s));
+    if (!h->s_own) h->s_own = h->s;   // the stream the handle created, destroyed with it
+    h->s = stream ? (cudaStream_t)stream : h->s_own;
+    return FI_OK;
+}
+
 long long fi_launch_count(const fi_handle* h) { return h ? h->launches : -1; }
 
 int fi_engine_trace(fi_handle* h, unsigned long long* out, int n)
@@ -1361,7 +1372,8 @@ int fi_destroy(fi_handle* h)
     }
     if (h->ev_snap) cudaEventDestroy(h->ev_snap);
     if (h->ev_out) cudaEventDestroy(h->ev_out);
-    if (h->s) cudaStreamDestroy(h->s);
+    if (h->s_own) cudaStreamDestroy(h->s_own);   // h->s is the caller's then
+    else if (h->s) cudaStreamDestroy(h->s);
     if (h->s_body) cudaStreamDestroy(h->s_body);
     delete h;
     return FI_OK;

@@ -318,6 +318,11 @@ int fi_state_import(fi_handle* h, const double* buf);
 
 /* The handle's CUDA stream (cudaStream_t) for event timing by the caller. */
 void* fi_stream(fi_handle* h);
+/* Run the handle's work on the caller's stream (cudaStream_t; NULL returns
+ * to the handle's own), after the work already enqueued has finished.  The
+ * caller keeps the stream alive while the handle uses it.  (The reference
+ * has no streams; its FFTW plans are the handle's own state likewise.) */
+int fi_set_stream(fi_handle* h, void* stream);
 /* Number of kernels this handle has enqueued so far. */
 long long fi_launch_count(const fi_handle* h);
 /* Per-kernel CUDA-event timing of this handle's launches: enable = 1 on,

@@ -477,3 +477,27 @@ def test_async_output_snapshots_match_synchronous_outputs():
         for m in OUT_MASKS:
             assert np.array_equal(got[m], w_out[m].astype(bool)), m
     b.close()
+
+
+def test_caller_stream():
+    """fi_set_stream: the same updates on a stream the caller owns give the
+    same bits as on the handle's own stream."""
+    import torch
+    wl = W.config2(n=48, L=3000e3 * 48 / 256, dt=1.0, stage_mode=1)
+    res = []
+    for use_caller in (False, True):
+        dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=1)
+        dom.set_fields(**wl.padded_fields(dom.nx, dom.ny))
+        b = gpu_bsl()
+        dom.init_state(wl.z_bed, wl.H_at(0.0), 0.0, b)
+        st = torch.cuda.Stream() if use_caller else None
+        if st is not None:
+            assert dom.L.fi_set_stream(dom.h, st.cuda_stream) == 0
+            assert dom.L.fi_stream(dom.h) == st.cuda_stream
+        for t in (10.0, 20.0, 30.0):
+            dom.update(wl.H_at(t), t, b)
+        res.append(dom.field("w"))
+        if st is not None:
+            assert dom.L.fi_set_stream(dom.h, None) == 0
+        dom.close()
+    assert np.array_equal(res[0], res[1])
