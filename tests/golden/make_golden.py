@@ -2,8 +2,9 @@
 
 1. params_<test>.json: the reference's experiment namelists
    (par/test_isostasy_<test>.nml of the reference project) parsed with
-   fastisostasy_gb300.params, and kei_reference.npz: the reference's
-   Kelvin-function table — both need the reference tree, so they are only
+   fastisostasy_gb300.params, kei_reference.npz: the reference's
+   Kelvin-function table, and ge_reference.npz: its elastic Green's-function
+   table — these need the reference tree, so they are only
    made where that tree is mounted (pass its path as argv[1]).
 2. oracle_golden.npz: outputs of the cases in tests/make_golden_cases.py.
 
@@ -39,6 +40,24 @@ def kei_reference(ref):
     return t[:, 0], t[:, 1]
 
 
+def ge_reference(ref):
+    """The reference's Farrell elastic Green's-function table
+    (calc_elastic_green, src/green_functions.f90: rn_vals, ge_vals), read
+    from its source: 42 radii [km] and values, default-real literals hence
+    single precision; the radii are scaled by 1.e3 in single precision."""
+    import re
+    with open(os.path.join(ref, "src", "green_functions.f90")) as fh:
+        src = fh.read()
+
+    def table(name):
+        blk = src[src.index(name):]
+        blk = blk[blk.index("[") + 1:blk.index("]")]
+        return np.array([float(x) for x in re.findall(r"[-+]?\d+\.\d*", blk)], dtype=np.float32)
+    rn = (table("rn_vals") * np.float32(1.e3)).astype(np.float64)
+    ge = table("ge_vals").astype(np.float64)
+    return rn, ge
+
+
 def main():
     if len(sys.argv) > 1:
         ref = sys.argv[1]
@@ -49,6 +68,9 @@ def main():
                 json.dump(p, fh, indent=1, sort_keys=True)
         rn, kei = kei_reference(ref)
         np.savez_compressed(os.path.join(HERE, "kei_reference.npz"), rn=rn, kei=kei)
+        rn, ge = ge_reference(ref)
+        assert len(rn) == 42 and len(ge) == 42
+        np.savez_compressed(os.path.join(HERE, "ge_reference.npz"), rn=rn, ge=ge)
     import make_golden_cases as MG
     out = {}
     for name, fn in MG.CASES.items():

@@ -182,3 +182,30 @@ def test_bilinear_array_nodes_and_flat_extension():
     assert np.allclose(got, z[3:-3, 3:-3].astype(np.float32), rtol=0, atol=2e-6)
     far = O.bilinear_array(xr, yr, z, np.array([-2e6, 2e6]), np.array([-2e6, 2e6]))
     assert far[0, 0] == np.float32(z[0, 0]) and far[1, 1] == np.float32(z[-1, -1])
+
+
+def test_elastic_green_uses_the_reference_table():
+    """The oracle's elastic Green's function equals calc_elastic_green
+    evaluated from the reference's own Farrell table (rn_vals, ge_vals of
+    src/green_functions.f90, extracted into ge_reference.npz), bit for bit."""
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "ge_reference.npz"))
+    rn, ge = ref["rn"], ref["ge"]
+    n, dx = 24, 75e3
+    got = O.elastic_green(n, n, dx)
+    mx = n // 2
+    f12, f981 = float(np.float32(1.e-12)), float(np.float32(9.81))
+    want = np.zeros((n, n))
+    for j in range(n):
+        for i in range(n):
+            x, y = (i - mx) * dx, (j - mx) * dx
+            r = np.sqrt(x * x + y * y)
+            if r > rn[41]:
+                g = 0.0
+            else:
+                k = 0
+                while k < 41 and not (rn[k] <= r < rn[k + 1]):
+                    k += 1
+                k = min(k, 40)
+                g = ge[k] + (r - rn[k]) / (rn[k + 1] - rn[k]) * (ge[k + 1] - ge[k])
+            want[j, i] = g * f12 * (dx * dx) / (f981 * max(r, dx))
+    assert np.array_equal(got, want)
