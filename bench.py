@@ -490,6 +490,82 @@ def serve_leg(lams=(10, 30, 100, 300, 1000, 2000), n_req=48, reserve_gb=8.0):
             "sequential_fp64_service_s": {str(k): {"setup": v[0], "per_update": v[1]} for k, v in cost.items()}}
 
 
+def scale_leg(sizes=(1024, 2048), n_updates=4):
+    """The headline workload (Gaussian lithosphere, disc, RK4 true stages,
+    dt = 1 yr, coupling 10 yr, elastic + geoid) on larger grids, where the
+    fields no longer fit the 129 MB L2: kyr/s and cell-steps/s of both forms,
+    the mixed form's per-kernel CUDA-event profile and the algorithmic GB/s
+    of each kernel against the measured HBM peak.  (At 2048^2 the step
+    engine's phase-A tiles exceed shared memory and the mixed form runs the
+    kernel sequence.)"""
+    import torch
+    from fastisostasy_gb300 import workloads as W
+    from fastisostasy_gb300.isostasy import Domain
+    from fastisostasy_gb300 import _lib
+    peak, peak_kind = peaks()
+    out = {}
+    for n in sizes:
+        wl = W.config2(n=n, L=n * DX, dt=DT, dtt=DTT, stage_mode=1)
+        res = {}
+        for prec in (0, 1):
+            d = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=prec)
+            d.set_fields(**wl.padded_fields(d.nx, d.ny))
+            b = _lib.FiBsl()
+            b.method, b.constant_ocean_surface, b.bsl_init, b.bsl_now = 0, 1, 0.0, 0.0
+            b.A_ocean_pd = b.A_ocean_now = 3.625e14
+            d.init_state(wl.z_bed, wl.H_at(0.0), 0.0, b)
+            H = torch.from_numpy(np.ascontiguousarray(wl.H_final)).to("cuda")
+            ext = torch.cuda.ExternalStream(d.L.fi_stream(d.h))
+            t = 0.0
+            for _ in range(2):
+                t += wl.dtt
+                d.update_async(H.data_ptr(), t, b)
+            d.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            for _ in range(n_updates):
+                t += wl.dtt
+                d.update_async(H.data_ptr(), t, b)
+            e1.record(ext)
+            d.synchronize()
+            ms = e0.elapsed_time(e1) / n_updates
+            entry = {"ms_per_update": ms, "kyr_s": DTT / 1000.0 / (ms / 1000.0),
+                     "cell_steps_per_s": d.nx * d.ny * (DTT / DT) / (ms / 1000.0)}
+            if prec == 1:
+                d.L.fi_profile(d.h, -1)
+                d.L.fi_profile(d.h, 1)
+                for _ in range(n_updates):
+                    t += wl.dtt
+                    d.update_async(H.data_ptr(), t, b)
+                d.synchronize()
+                import ctypes as C
+                nk = len(_lib.PROFILE_KERNELS)
+                msv = (C.c_double * nk)()
+                cnt = (C.c_longlong * nk)()
+                d.L.fi_profile_read(d.h, msv, cnt, nk)
+                d.L.fi_profile(d.h, 0)
+                kern = {}
+                tot = sum(msv[i] for i in range(nk))
+                for i, name in enumerate(_lib.PROFILE_KERNELS):
+                    if cnt[i] == 0:
+                        continue
+                    alg = algorithmic_bytes(name, d, 1, 1)
+                    us = 1000.0 * msv[i] / cnt[i]
+                    gbs = alg / (us * 1e-6) / 1e9 if alg else None
+                    kern[name] = {"share": round(msv[i] / tot, 4), "avg_launch_us": round(us, 2),
+                                  "alg_GBs": round(gbs, 1) if gbs else None,
+                                  "frac_of_peak": round(gbs / peak, 3) if gbs else None}
+                entry["kernels"] = kern
+                entry["step_engine"] = "engine" in kern
+            res["fp64" if prec == 0 else "mixed"] = entry
+            d.close()
+        res["mixed_over_fp64"] = res["fp64"]["ms_per_update"] / res["mixed"]["ms_per_update"]
+        out["%dx%d" % (n, n)] = res
+    out["peak"] = {"value": peak, "unit": "GB/s", "kind": peak_kind}
+    return out
+
+
 def configs_leg():
     """The other configurations as bounded samples: config 1 (128^2 uniform
     disc, reference-compatible Tsit5), config 2 (256^2 Gaussian lithosphere,
@@ -634,7 +710,7 @@ def main():
     ap.add_argument("--ensemble-members", type=int, default=256)
     ap.add_argument("--ensemble-updates", type=int, default=10)
     ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--only", choices=["ensemble", "serve", "configs"],
+    ap.add_argument("--only", choices=["ensemble", "serve", "configs", "scale"],
                     help="run one secondary leg alone and print its JSON (for profiling), not a bench line")
     ap.add_argument("--lean", action="store_true",
                     help="mixed form only, no profile / e2e / CPU legs (for ncu captures); prints the timing only")
@@ -671,6 +747,9 @@ def main():
         return 0
     if args.only == "configs":
         print(json.dumps({"configs": configs_leg()}))
+        return 0
+    if args.only == "scale":
+        print(json.dumps({"scale": scale_leg()}))
         return 0
     if args.lean:
         dom, wl, b = make_domain(1)

@@ -541,6 +541,12 @@ template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, siz
     // no more blocks than the largest phase has work items: a small domain
     // then leaves SMs free for other handles' work (serving, ensembles)
     const int na = (p.ny + RA - 1) / RA, nb = (p.h + 1 + cb - 1) / cb, nc = (p.ny + RC - 1) / RC;
+    // the stencil phase must fit one wave of resident blocks: beyond that
+    // (1024^2: 512 items on 152 one-block SMs) every barrier waits for
+    // several items in a row and the kernel sequence is faster (measured
+    // 5.4 ms per update in the engine against 13.4 / 4 ms per 1024^2-sized
+    // quarter of a 2048^2 update in the kernel sequence)
+    if (na > per_sm * nsm) return 0;
     int items = na > nb ? na : nb;
     if (nc > items) items = nc;
     *grid = per_sm * nsm < items ? per_sm * nsm : items;
