@@ -17,6 +17,7 @@
 // the DFT of DHT^-1(m H); when m is even in both indices this reduces to
 // F' = m F (flag `even`).
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 #include "fi_fft.cuh"
@@ -342,11 +343,17 @@ __device__ __forceinline__ int strip_tasks(int nx, int ny, int seg)
     return ((nx + SW - 1) / SW) * ((ny + seg - 1) / seg);
 }
 
+// PAIR: the state as a float pair (whi + wlo), no mantle term; else the
+// FP64 state y, its first differences taken in double and rounded (as
+// flexure_f32_body<false>), and with wref the mantle term
+// coef_mantle (y - wref) at masked cells.
+template <bool PAIR>
 __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, const float* __restrict__ wlo,
                                               const float* __restrict__ q0, const uint8_t* __restrict__ mask,
                                               const float* __restrict__ D, const float* __restrict__ inv2eta,
                                               float* __restrict__ f, int nx, int ny, const FlexCoefF& c, int seg,
-                                              int task)
+                                              int task, const double* __restrict__ y = nullptr,
+                                              const double* __restrict__ wref = nullptr)
 {
     const unsigned FULL = 0xffffffffu;
     const int ncg = (nx + SW - 1) / SW;
@@ -360,6 +367,7 @@ __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, con
     const int o0 = sg * seg, o1 = min(o0 + seg, ny);
     const int cc = cin ? col : 0;
     float hp = 0.f, lp = 0.f;                           // pair of row r - 1
+    double yp = 0.0;                                    // FP64 state of row r - 1 (!PAIR)
     float Wx1 = 0.f, Wx2 = 0.f, Wx3 = 0.f;              // Wx of rows r-1, r-2, r-3
     float wxx1 = 0.f, wxx2 = 0.f;                       // wxx of rows r-1, r-2
     float dY1 = 0.f, dY2 = 0.f, dY3 = 0.f, dY4 = 0.f;   // dY of rows r-1 .. r-4 (dY_j = y_{j+1} - y_j)
@@ -368,21 +376,28 @@ __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, con
     float mx0 = 0.f, mx1 = 0.f, mx2 = 0.f;                         // mx_xx of rows m .. m-2
     // the next row's loads are issued one iteration ahead
     int r = o0 - 4;
-    auto ld_pair = [&](int rr, float& h, float& l) {
+    auto ld_pair = [&](int rr, float& h, float& l, double& yy) {
         if (cin && rr >= 0 && rr < ny) {
             const size_t e = (size_t)rr * nx + cc;
-            h = __ldg(whi + e);
-            l = __ldg(wlo + e);
+            if constexpr (PAIR) {
+                h = __ldg(whi + e);
+                l = __ldg(wlo + e);
+            } else {
+                yy = __ldg(y + e);
+            }
         } else {
             h = 0.f;
             l = 0.f;
+            yy = 0.0;
         }
     };
-    float hn, ln;
-    ld_pair(r, hn, ln);
+    float hn = 0.f, ln = 0.f;
+    double yn = 0.0;
+    ld_pair(r, hn, ln, yn);
     for (; r < o1 + 4; ++r) {
         const float h = hn, l = ln;
-        ld_pair(r + 1, hn, ln);
+        const double yv = yn;
+        ld_pair(r + 1, hn, ln, yn);
         const int m = r - 2, o = r - 4;
         const bool mrow = cin && m >= 0 && m < ny;
         const float Dm = mrow ? __ldg(D + (size_t)m * nx + cc) : 0.f;
@@ -391,8 +406,14 @@ __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, con
         const uint8_t om = orow ? __ldg(mask + eo) : (uint8_t)0;
         const float oq = orow ? __ldg(q0 + eo) : 0.f, oie = orow ? __ldg(inv2eta + eo) : 0.f;
         // row r: first differences, Wx, wxx
-        const float hr = __shfl_down_sync(FULL, h, 1), lr = __shfl_down_sync(FULL, l, 1);
-        const float dX = (hr - h) + (lr - l);
+        float dX;
+        if constexpr (PAIR) {
+            const float hr = __shfl_down_sync(FULL, h, 1), lr = __shfl_down_sync(FULL, l, 1);
+            dX = (hr - h) + (lr - l);
+        } else {
+            const double yr = __shfl_down_sync(FULL, yv, 1);
+            dX = (float)(yr - yv);
+        }
         const float dXm = __shfl_up_sync(FULL, dX, 1);
         float Wx, wxx;
         if (edge) {
@@ -403,9 +424,12 @@ __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, con
             Wx = (dX + dXm) * c.inv_2dx;
             wxx = (dX - dXm) * c.inv_dx2;
         }
-        const float dYn = (h - hp) + (l - lp);   // dY of row r - 1
+        float dYn;   // dY of row r - 1
+        if constexpr (PAIR) dYn = (h - hp) + (l - lp);
+        else dYn = (float)(yv - yp);
         hp = h;
         lp = l;
+        yp = yv;
         dY4 = dY3; dY3 = dY2; dY2 = dY1; dY1 = dYn;
         // moments of row m = r - 2 (Wx1..3 are still those of rows r-1..r-3)
         float wxy, wyy;
@@ -455,7 +479,10 @@ __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, con
                 mxy_xy = (Mq1 - Mq3) * c.inv_2dy;
                 my_yy = ((My1 - 2.f * My2) + My3) * c.inv_dy2;
             }
-            const float p = om ? oq : 0.f;
+            float p = om ? oq : 0.f;
+            if constexpr (!PAIR) {
+                if (om && wref) p += c.coef_mantle * (float)(__ldg(y + eo) - __ldg(wref + eo));
+            }
             f[eo] = (((p + mx2) + 2.f * mxy_xy) + my_yy) * oie;
         }
     }
@@ -469,7 +496,18 @@ k_flexure_strip(const float* __restrict__ whi, const float* __restrict__ wlo, co
     if (gate && *gate == 0) return;
     const int task = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (task >= strip_tasks(nx, ny, seg)) return;   // whole warps
-    flexure_strip(whi, wlo, q0, mask, D, inv2eta, f, nx, ny, c, seg, task);
+    flexure_strip<true>(whi, wlo, q0, mask, D, inv2eta, f, nx, ny, c, seg, task);
+}
+
+__global__ void __launch_bounds__(256)
+k_flexure_strip_y(const double* __restrict__ y, const double* __restrict__ wref, const float* __restrict__ q0,
+                  const uint8_t* __restrict__ mask, const float* __restrict__ D, const float* __restrict__ inv2eta,
+                  float* __restrict__ f, int nx, int ny, FlexCoefF c, int seg, const int* __restrict__ gate)
+{
+    if (gate && *gate == 0) return;
+    const int task = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (task >= strip_tasks(nx, ny, seg)) return;   // whole warps
+    flexure_strip<false>(nullptr, nullptr, q0, mask, D, inv2eta, f, nx, ny, c, seg, task, y, wref);
 }
 
 // rows per warp task for a single domain: enough tasks to fill the GPU
@@ -513,6 +551,19 @@ void launch_flexure(const double* y, const double* wref, const T* q0, const uint
             const int tasks = ((nx + SW - 1) / SW) * ((ny + seg - 1) / seg);
             k_flexure_strip<<<(tasks + 7) / 8, 256, 0, s>>>(whi, wlo, (const float*)q0, mask, (const float*)D,
                                                             (const float*)inv2eta, (float*)f, nx, ny, cf, seg, gate);
+            return;
+        }
+        // the FP64 state by column strips (the shared-memory tile form is
+        // kept for FI_FLEXURE_TILES=1)
+        static const bool tiles = [] {
+            const char* e = getenv("FI_FLEXURE_TILES");
+            return e && e[0] == '1';
+        }();
+        if (!tiles) {
+            const int seg = strip_seg_single(nx, ny);
+            const int tasks = ((nx + SW - 1) / SW) * ((ny + seg - 1) / seg);
+            k_flexure_strip_y<<<(tasks + 7) / 8, 256, 0, s>>>(y, wref, (const float*)q0, mask, (const float*)D,
+                                                              (const float*)inv2eta, (float*)f, nx, ny, cf, seg, gate);
             return;
         }
         k_flexure_f32<<<g, b, 0, s>>>(y, wref, (const float*)q0, mask, (const float*)D, (const float*)inv2eta,
@@ -924,7 +975,7 @@ __global__ void __launch_bounds__(256) k_b_flexure(const BMember* __restrict__ M
             // pair: column strips, 8 warp tasks per virtual block
             const int task = local * 8 + (int)threadIdx.y;   // 32 x 8 block: warp = threadIdx.y
             if (task < strip_tasks(b.p.nx, b.p.ny, b.fseg))
-                flexure_strip(b.d.whi, b.d.wlo, (const float*)b.q0, b.mask, (const float*)b.D,
+                flexure_strip<true>(b.d.whi, b.d.wlo, (const float*)b.q0, b.mask, (const float*)b.D,
                               (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, b.fcf, b.fseg, task);
         } else {
             flexure_body<T>(b.y, nullptr, (const T*)b.q0, b.mask, (const T*)b.D, (const T*)b.inv2eta, (T*)b.f,
