@@ -574,6 +574,78 @@ int upload_static(fi_handle* h)
 
 // kernel spectrum: zero-padded r2c of a padded-grid kernel (precompute_kernel,
 // src/convolutions.f90:93-108), computed in double on the device.
+// Autotuner of the single-domain RHS transforms: rows per row-transform
+// block and spectrum columns per column-transform block, timed on the
+// handle's own buffers (RHS scratch, dead at set-up) and cached per grid
+// size and precision for the process.  The step engine has its own shapes.
+template <typename T> void tune_rhs_shapes(fi_handle* h)
+{
+    typedef typename vec2<T>::type C2;
+    struct Key {
+        int nx, ny, sz;
+        bool operator==(const Key& o) const { return nx == o.nx && ny == o.ny && sz == o.sz; }
+    };
+    static std::mutex mu;
+    static std::vector<std::pair<Key, std::pair<int, int>>> cache;
+    const Key key{h->nx, h->ny, (int)sizeof(T)};
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (auto& e : cache)
+            if (e.first == key) {
+                h->prhs.rb = e.second.first;
+                h->prhs.cb = e.second.second;
+                return;
+            }
+    }
+    int optin = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    Plan2D p = h->prhs;
+    auto time_it = [&](auto&& fn) {
+        float best = 1e30f;
+        for (int r = 0; r < 4; ++r) {
+            cudaEventRecord(e0, h->s);
+            fn();
+            cudaEventRecord(e1, h->s);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0 && ms < best) best = ms;
+        }
+        return best;
+    };
+    const double scale = 1.0 / (double)(float)((long long)h->nx * h->ny);
+    int best_rb = 0, best_cb = 0;
+    float tr = 1e30f, tc = 1e30f;
+    for (int rb : {1, 2, 4, 8}) {
+        if (2 * (size_t)rb * p.h * sizeof(C2) > (size_t)optin) continue;
+        p.rb = rb;
+        const float t = time_it([&] {
+            launch_rows_fwd<T>((const T*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, p, h->s);
+            launch_rows_inv<T>((const C2*)h->S, (T*)h->raw[0], p, scale, h->s);
+        });
+        if (t < tr) { tr = t; best_rb = rb; }
+    }
+    for (int cb : {1, 2, 4, 8}) {
+        if (2 * (size_t)cb * (p.ny + 1) * sizeof(C2) > (size_t)optin) continue;
+        p.cb = cb;
+        const float t = time_it([&] {
+            launch_cols_hartley<T>((C2*)h->S, (const T*)h->mA, (const T*)h->mB, h->even, p, h->s);
+        });
+        if (t < tc) { tc = t; best_cb = cb; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGetLastError();
+    h->prhs.rb = best_rb;
+    h->prhs.cb = best_cb;
+    std::lock_guard<std::mutex> lk(mu);
+    cache.push_back({key, {best_rb, best_cb}});
+}
+
 int kernel_spectrum(fi_handle* h, const std::vector<double>& ker, int which)
 {
     const size_t hs = (size_t)h->pconv.ny * h->pconv.sp;
@@ -1339,6 +1411,11 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
         }
     }
     if ((rc = upload_static(h))) return rc;
+    if (p.method == 3 && !h->engine_ok && !(getenv("FI_NO_TUNE") && getenv("FI_NO_TUNE")[0] == '1')) {
+        if (mixed(h)) tune_rhs_shapes<float>(h);
+        else tune_rhs_shapes<double>(h);
+        CK(cudaGetLastError());
+    }
     if ((rc = kernel_spectrum(h, h->GE, 0)) || (rc = kernel_spectrum(h, h->GN, 1))) return rc;
     if (p.method == 2 && (rc = kernel_spectrum(h, h->GV, 2))) return rc;
     // zero_init_state (src/fastisostasy.f90:505-548): z_bed background 1e6

@@ -649,7 +649,7 @@ void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, type
                      const Plan2D& p, cudaStream_t s, const int* gate)
 {
     typedef typename vec2<T>::type C2;
-    const int RB = rows_per_block(p.h);
+    const int RB = p.rb > 0 ? p.rb : rows_per_block(p.h);
     const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
     set_smem(k_rows_fwd<T>, sm);
     const int nblk = (nrows_in + RB - 1) / RB;
@@ -710,7 +710,7 @@ void launch_rows_inv(const typename vec2<T>::type* S, T* out, const Plan2D& p, d
                      const int* gate)
 {
     typedef typename vec2<T>::type C2;
-    const int RB = rows_per_block(p.h);
+    const int RB = p.rb > 0 ? p.rb : rows_per_block(p.h);
     const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
     set_smem(k_rows_inv<T>, sm);
     const int nblk = (p.ny + RB - 1) / RB;
@@ -819,7 +819,7 @@ void launch_cols_hartley(typename vec2<T>::type* S, const T* mA, const T* mB, in
                          cudaStream_t s, const int* gate)
 {
     typedef typename vec2<T>::type C2;
-    const int CB = cols_per_block<T>(p.ny);
+    const int CB = p.cb > 0 ? p.cb : cols_per_block<T>(p.ny);
     const size_t sm = 2 * (size_t)CB * col_stride(p.ny) * sizeof(C2);
     set_smem(k_cols_hartley<T>, sm);
     const int nblk = (p.h + 1 + CB - 1) / CB;
@@ -868,7 +868,7 @@ void launch_cols_conv(typename vec2<T>::type* S, const typename vec2<T>::type* K
                       int n_out, const Plan2D& p, cudaStream_t s)
 {
     typedef typename vec2<T>::type C2;
-    const int CB = cols_per_block<T>(p.ny);
+    const int CB = p.cb > 0 ? p.cb : cols_per_block<T>(p.ny);
     const size_t sm = 2 * (size_t)CB * col_stride(p.ny) * sizeof(C2);
     set_smem(k_cols_conv<T>, sm);
     const int nblk = (p.h + 1 + CB - 1) / CB;
@@ -879,7 +879,7 @@ template <typename T>
 void launch_cols_fwd(typename vec2<T>::type* S, int nrows_in, const Plan2D& p, cudaStream_t s)
 {
     typedef typename vec2<T>::type C2;
-    const int CB = cols_per_block<T>(p.ny);
+    const int CB = p.cb > 0 ? p.cb : cols_per_block<T>(p.ny);
     const size_t sm = 2 * (size_t)CB * col_stride(p.ny) * sizeof(C2);
     set_smem(k_cols_conv<T>, sm);
     const int nblk = (p.h + 1 + CB - 1) / CB;
@@ -946,7 +946,7 @@ void launch_conv_rows_inv(const typename vec2<T>::type* S, int n_out, double* ou
                           const Plan2D& p, double scale, cudaStream_t s)
 {
     typedef typename vec2<T>::type C2;
-    const int RB = rows_per_block(p.h);
+    const int RB = p.rb > 0 ? p.rb : rows_per_block(p.h);
     const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
     set_smem(k_conv_rows_inv<T>, sm);
     const int nblk = (n_out + RB - 1) / RB;
