@@ -709,6 +709,7 @@ def main():
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--ensemble-members", type=int, default=256)
     ap.add_argument("--ensemble-updates", type=int, default=10)
+    ap.add_argument("--scale-sizes", default="1024,2048", help="grid sizes of --only scale")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--only", choices=["ensemble", "serve", "configs", "scale"],
                     help="run one secondary leg alone and print its JSON (for profiling), not a bench line")
@@ -749,7 +750,7 @@ def main():
         print(json.dumps({"configs": configs_leg()}))
         return 0
     if args.only == "scale":
-        print(json.dumps({"scale": scale_leg()}))
+        print(json.dumps({"scale": scale_leg(tuple(int(v) for v in args.scale_sizes.split(",")))}))
         return 0
     if args.lean:
         dom, wl, b = make_domain(1)
