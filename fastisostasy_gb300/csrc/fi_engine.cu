@@ -46,7 +46,7 @@ __constant__ double c_rk4_a[4] = {0.0, 0.5, 0.5, 1.0};
 
 template <typename T> struct PhaseAMem {
     // level-0 differences on RA+4 rows, moments on RA+2 rows, all full width
-    static size_t bytes(int nx, int h)
+    __host__ __device__ static size_t bytes(int nx, int h)
     {
         typedef typename vec2<T>::type C2;
         const size_t rows = (RA + 4) + (RA + 3) + (RA + 4) + 4 * (RA + 2);
@@ -54,15 +54,64 @@ template <typename T> struct PhaseAMem {
     }
 };
 
+// Dynamic shared memory: the phase scratch (the largest of A, B, C), then
+// the twiddle tables of the row and column transforms and of the real-FFT
+// split, copied once per launch and resident for all its phases.
+template <typename T> __host__ __device__ inline size_t engine_tab_off(int nx, int h, int ny, int CB)
+{
+    typedef typename vec2<T>::type C2;
+    const size_t a = PhaseAMem<T>::bytes(nx, h);
+    const size_t b = 2 * (size_t)CB * ny * sizeof(C2);
+    const size_t c = 2 * (size_t)RC * h * sizeof(C2);
+    size_t m = a > b ? a : b;
+    m = m > c ? m : c;
+    return (m + 15) & ~(size_t)15;
+}
+template <typename T> __host__ __device__ inline size_t engine_tab_count(int h, int ny)
+{
+    return (size_t)h + (size_t)ny + (size_t)h + 1;   // row, column, real split
+}
+
 template <typename T> size_t engine_smem_bytes(const Plan2D& p, int CB)
 {
     typedef typename vec2<T>::type C2;
-    size_t a = PhaseAMem<T>::bytes(p.nx, p.h);
-    size_t b = 2 * (size_t)CB * p.ny * sizeof(C2);
-    size_t c = 2 * (size_t)RC * p.h * sizeof(C2);
-    size_t m = a > b ? a : b;
-    return (m > c ? m : c) + 64;
+    return engine_tab_off<T>(p.nx, p.h, p.ny, CB) + engine_tab_count<T>(p.h, p.ny) * sizeof(C2) + 64;
 }
+
+// (row, column) walk of a block's threads over a row-major strip of width w
+// in steps of the block size: the element index e = r*w + i advances by nt
+// without a per-element integer division (a runtime division is a long
+// instruction sequence and the strip loops of phase A are issue-bound).
+struct Walk {
+    int r0, i0, dr, di, w;
+    __device__ __forceinline__ void init(int width, int tid, int nt)
+    {
+        w = width;
+        r0 = tid / width;
+        i0 = tid - r0 * width;
+        dr = nt / width;
+        di = nt - dr * width;
+    }
+    __device__ __forceinline__ void next(int& r, int& i) const
+    {
+        i += di;
+        r += dr;
+        if (i >= w) {
+            i -= w;
+            ++r;
+        }
+    }
+};
+
+// per-launch constants of a block: resident twiddle tables and strip walks
+template <typename T> struct EngTw {
+    const typename vec2<T>::type* row;
+    const typename vec2<T>::type* col;
+    const typename vec2<T>::type* rtw;
+    Walk wx;    // width nx (phase A strips)
+    Walk wh;    // width h (phase C rows)
+    Walk wh1;   // width h+1 (half-spectrum rows)
+};
 
 template <typename T> __device__ __forceinline__ double corner_mean_dev(const T* a, int nx, int ny)
 {
@@ -73,11 +122,11 @@ template <typename T> __device__ __forceinline__ double corner_mean_dev(const T*
 // Phase A: one item = output rows j0, j0+1 (full width).
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsigned char* smem)
+__device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsigned char* smem, const EngTw<T>& tw)
 {
     typedef typename vec2<T>::type C2;
     const int nx = g.p.nx, ny = g.p.ny, hh = g.p.h;
-    const int tid = threadIdx.x, nt = blockDim.x;
+    const int tid = threadIdx.x;
     T* dX = reinterpret_cast<T*>(smem);
     T* dY = dX + (size_t)(RA + 4) * nx;
     T* Wx = dY + (size_t)(RA + 3) * nx;
@@ -89,21 +138,33 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
     C2* b1 = b0 + (size_t)RA * hh;
 
     const T* rprev = stage > 0 ? (const T*)g.raw[stage - 1] : nullptr;
-    __shared__ double s_sc[2];
-    if (tid == 0) {
-        // y = x + a h spy (raw - cm): the scale s and the corner mean cm
-        s_sc[0] = stage > 0 ? c_rk4_a[stage] * h * g.spy : 0.0;
-        s_sc[1] = stage > 0 ? corner_mean_of(rprev, nx, ny) : 0.0;
+    __shared__ double s_cm;
+    // y = x + a h spy (raw - cm): the scale s, the same arithmetic in every
+    // thread, and the corner mean cm of raw_{s-1}
+    const double sd = stage > 0 ? c_rk4_a[stage] * h * g.spy : 0.0;
+    // In the mixed form cm cancels in the level-0 differences and enters only
+    // the mantle term: thread 0 issues the four corner loads now and forms
+    // the mean after the level-0 loop, so their L2 latency hides behind it.
+    float cf[4] = {0.f, 0.f, 0.f, 0.f};
+    if constexpr (std::is_same<T, float>::value) {
+        if (tid == 0 && rprev) {
+            const size_t last = (size_t)(ny - 1) * nx;
+            const float* q[4] = {(const float*)rprev, (const float*)rprev + last + nx - 1,
+                                 (const float*)rprev + last, (const float*)rprev + nx - 1};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(cf[c]) : "l"(q[c]));
+        }
+    } else {
+        if (tid == 0) s_cm = stage > 0 ? corner_mean_of(rprev, nx, ny) : 0.0;
+        __syncthreads();
     }
-    __syncthreads();
-    const double sd = s_sc[0], cmd = s_sc[1];
+    const double cmd_early = std::is_same<T, float>::value ? 0.0 : s_cm;   // plain form only
     // float copies made once: every FP64 instruction (conversions included)
     // costs the mixed form 64 FP32 slots on this GPU
-    const float sdf = (float)sd, cmdf = (float)cmd, cmant = (float)g.fc.coef_mantle;
+    const float sdf = (float)sd, cmant = (float)g.fc.coef_mantle;
 
     // level 0: forward differences along x (dX) and y (dY)
-    for (int e = tid; e < (RA + 4) * nx; e += nt) {
-        const int r = e / nx, i = e - r * nx;
+    for (int r = tw.wx.r0, i = tw.wx.i0; r < RA + 4; tw.wx.next(r, i)) {
         const int gj = j0 - 2 + r;
         if (gj < 0 || gj >= ny) continue;
         const size_t c0 = (size_t)gj * nx + i;
@@ -114,7 +175,10 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
                 dX[(size_t)r * nx + i] = v;
             } else {
                 double y1 = g.x[c0 + 1], y0 = g.x[c0];
-                if (rprev) { y1 += sd * ((double)rprev[c0 + 1] - cmd); y0 += sd * ((double)rprev[c0] - cmd); }
+                if (rprev) {
+                    y1 += sd * ((double)rprev[c0 + 1] - cmd_early);
+                    y0 += sd * ((double)rprev[c0] - cmd_early);
+                }
                 dX[(size_t)r * nx + i] = y1 - y0;
             }
         }
@@ -126,16 +190,23 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
                 dY[(size_t)r * nx + i] = v;
             } else {
                 double y1 = g.x[c1], y0 = g.x[c0];
-                if (rprev) { y1 += sd * ((double)rprev[c1] - cmd); y0 += sd * ((double)rprev[c0] - cmd); }
+                if (rprev) {
+                    y1 += sd * ((double)rprev[c1] - cmd_early);
+                    y0 += sd * ((double)rprev[c0] - cmd_early);
+                }
                 dY[(size_t)r * nx + i] = y1 - y0;
             }
         }
     }
+    if constexpr (std::is_same<T, float>::value) {
+        if (tid == 0) s_cm = rprev ? corner_mean((double)cf[0], (double)cf[1], (double)cf[2], (double)cf[3]) : 0.0;
+    }
     __syncthreads();
+    const double cmd = s_cm;
+    const float cmdf = (float)cmd;
     const T inv_dx = (T)g.fc.inv_dx, inv_2dx = (T)g.fc.inv_2dx, inv_dx2 = (T)g.fc.inv_dx2;
     const T inv_dy = (T)g.fc.inv_dy, inv_2dy = (T)g.fc.inv_2dy, inv_dy2 = (T)g.fc.inv_dy2;
-    for (int e = tid; e < (RA + 4) * nx; e += nt) {
-        const int r = e / nx, i = e - r * nx;
+    for (int r = tw.wx.r0, i = tw.wx.i0; r < RA + 4; tw.wx.next(r, i)) {
         const int gj = j0 - 2 + r;
         if (gj < 0 || gj >= ny) continue;
         const T* d = dX + (size_t)r * nx;
@@ -147,8 +218,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
     }
     __syncthreads();
     const T nu = (T)g.fc.nu, omn = (T)g.fc.one_minus_nu;
-    for (int e = tid; e < (RA + 2) * nx; e += nt) {
-        const int m = e / nx, i = e - m * nx;
+    for (int m = tw.wx.r0, i = tw.wx.i0; m < RA + 2; tw.wx.next(m, i)) {
         const int r = m + 1;
         const int gj = j0 - 2 + r;
         if (gj < 0 || gj >= ny) continue;
@@ -171,8 +241,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         Mxy[mi] = (-Dl * omn) * wxy;
     }
     __syncthreads();
-    for (int e = tid; e < (RA + 2) * nx; e += nt) {
-        const int m = e / nx, i = e - m * nx;
+    for (int m = tw.wx.r0, i = tw.wx.i0; m < RA + 2; tw.wx.next(m, i)) {
         const int gj = j0 - 1 + m;
         if (gj < 0 || gj >= ny) continue;
         const T* M = Mxy + (size_t)m * nx;
@@ -185,8 +254,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
     __syncthreads();
     const T* q0 = g.q0_T<T>();
     const T* i2e = g.inv2eta_T<T>();
-    for (int e = tid; e < RA * nx; e += nt) {
-        const int o = e / nx, i = e - o * nx;
+    for (int o = tw.wx.r0, i = tw.wx.i0; o < RA; tw.wx.next(o, i)) {
         const int gj = j0 + o;
         T fv = (T)0;
         if (gj < ny) {
@@ -224,11 +292,10 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         bz[i] = fv;
     }
     __syncthreads();
-    C2* r = block_fft<T>(b0, b1, g.p.row.d, RA, hh, etw<T>(g.p.row), -1);
-    const C2* rtw = ertw<T>(g.p);
+    C2* r = block_fft<T, true>(b0, b1, g.p.row.d, RA, hh, tw.row, -1);
+    const C2* rtw = tw.rtw;
     C2* S = (C2*)g.S;
-    for (int e = tid; e < RA * (hh + 1); e += nt) {
-        const int o = e / (hh + 1), k = e - o * (hh + 1);
+    for (int o = tw.wh1.r0, k = tw.wh1.i0; o < RA; tw.wh1.next(o, k)) {
         const int gj = j0 + o;
         if (gj >= ny) continue;
         const C2 Zk = r[o * hh + (k == hh ? 0 : k)];
@@ -238,7 +305,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         E.y = (T)0.5 * (Zk.y - Zc.y);
         O.x = (T)0.5 * (Zk.y + Zc.y);
         O.y = (T)-0.5 * (Zk.x - Zc.x);
-        S[(size_t)gj * g.p.sp + k] = cadd(E, cmul(__ldg(rtw + k), O));
+        S[(size_t)gj * g.p.sp + k] = cadd(E, cmul(rtw[k], O));
     }
     __syncthreads();
 }
@@ -248,7 +315,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
 // inverse column FFT.
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem)
+__device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem, const EngTw<T>& tw)
 {
     typedef typename vec2<T>::type C2;
     const int ny = g.p.ny;
@@ -257,17 +324,17 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
     C2* S = (C2*)g.S;
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int e = tid; e < CB * ny; e += nt) {
-        const int c = e % CB, l = e / CB;
+        const int c = CB == 1 ? 0 : e % CB, l = CB == 1 ? e : e / CB;
         const int k = k0 + c;
         b0[c * ny + l] = (k <= g.p.h) ? S[(size_t)l * g.p.sp + k] : mk2<T>((T)0, (T)0);
     }
     __syncthreads();
-    C2* r = block_fft<T>(b0, b1, g.p.col.d, CB, ny, etw<T>(g.p.col), -1);
+    C2* r = block_fft<T, true>(b0, b1, g.p.col.d, CB, ny, tw.col, -1);
     const T* mA = g.mA_T<T>();
     const T* mB = g.mB_T<T>();
     const int half = ny / 2 + 1;
     for (int e = tid; e < CB * half; e += nt) {
-        const int c = e % CB, l = e / CB;
+        const int c = CB == 1 ? 0 : e % CB, l = CB == 1 ? e : e / CB;
         const int k = k0 + c;
         if (k > g.p.h) continue;
         const int lm = (ny - l) % ny;
@@ -297,9 +364,9 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
     }
     __syncthreads();
     C2* other = (r == b0) ? b1 : b0;
-    C2* q = block_fft<T>(r, other, g.p.col.d, CB, ny, etw<T>(g.p.col), +1);
+    C2* q = block_fft<T, true>(r, other, g.p.col.d, CB, ny, tw.col, +1);
     for (int e = tid; e < CB * ny; e += nt) {
-        const int c = e % CB, l = e / CB;
+        const int c = CB == 1 ? 0 : e % CB, l = CB == 1 ? e : e / CB;
         const int k = k0 + c;
         if (k <= g.p.h) S[(size_t)l * g.p.sp + k] = q[c * ny + l];
     }
@@ -310,17 +377,16 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
 // Phase C: inverse row real-FFT of rows j0 .. j0+RC-1 -> raw (scaled 1/(nx ny)).
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem)
+__device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem, const EngTw<T>& tw)
 {
     typedef typename vec2<T>::type C2;
     const int hh = g.p.h, ny = g.p.ny, nx = g.p.nx;
     C2* b0 = reinterpret_cast<C2*>(smem);
     C2* b1 = b0 + (size_t)RC * hh;
     const C2* S = (const C2*)g.S;
-    const C2* rtw = ertw<T>(g.p);
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int e = tid; e < RC * hh; e += nt) {
-        const int o = e / hh, k = e - o * hh;
+    const C2* rtw = tw.rtw;
+    for (int o = tw.wh.r0, k = tw.wh.i0; o < RC; tw.wh.next(o, k)) {
+        const int e = o * hh + k;
         const int j = j0 + o;
         C2 z = mk2<T>((T)0, (T)0);
         if (j < ny) {
@@ -328,20 +394,19 @@ __device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem
             C2 B = S[(size_t)j * g.p.sp + (hh - k)];
             B.y = -B.y;
             const C2 sum = cadd(A, B), dif = csub(A, B);
-            const C2 t = cmulc(dif, __ldg(rtw + k));
+            const C2 t = cmulc(dif, rtw[k]);
             z.x = sum.x - t.y;
             z.y = sum.y + t.x;
         }
         b0[e] = z;
     }
     __syncthreads();
-    C2* r = block_fft<T>(b0, b1, g.p.row.d, RC, hh, etw<T>(g.p.row), +1);
+    C2* r = block_fft<T, true>(b0, b1, g.p.row.d, RC, hh, tw.row, +1);
     const T scale = (T)g.norm_scale;
-    for (int e = tid; e < RC * hh; e += nt) {
-        const int o = e / hh, m = e - o * hh;
+    for (int o = tw.wh.r0, m = tw.wh.i0; o < RC; tw.wh.next(o, m)) {
         const int j = j0 + o;
         if (j >= ny) continue;
-        C2 v = r[e];
+        C2 v = r[o * hh + m];
         v.x *= scale;
         v.y *= scale;
         *reinterpret_cast<C2*>(out + (size_t)j * nx + 2 * m) = v;
@@ -377,6 +442,25 @@ __global__ void __launch_bounds__(512, 2) k_engine_rk4(EngineArgs g)
         s_dt = ctl->dt;
         s_ok = ctl->status == ST_OK;
     }
+    // resident twiddle tables (see engine_tab_off)
+    typedef typename vec2<T>::type C2;
+    EngTw<T> tw;
+    {
+        C2* tab = reinterpret_cast<C2*>(smem + engine_tab_off<T>(nx, g.p.h, ny, g.CB));
+        const C2* srow = etw<T>(g.p.row);
+        const C2* scol = etw<T>(g.p.col);
+        const C2* srtw = ertw<T>(g.p);
+        const int h = g.p.h;
+        for (int e = threadIdx.x; e < h; e += blockDim.x) tab[e] = srow[e];
+        for (int e = threadIdx.x; e < ny; e += blockDim.x) tab[h + e] = scol[e];
+        for (int e = threadIdx.x; e <= h; e += blockDim.x) tab[h + ny + e] = srtw[e];
+        tw.row = tab;
+        tw.col = tab + h;
+        tw.rtw = tab + h + ny;
+        tw.wx.init(nx, threadIdx.x, blockDim.x);
+        tw.wh.init(h, threadIdx.x, blockDim.x);
+        tw.wh1.init(h + 1, threadIdx.x, blockDim.x);
+    }
     __syncthreads();
     const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
     const bool tr = g.trace && lead;
@@ -399,15 +483,15 @@ __global__ void __launch_bounds__(512, 2) k_engine_rk4(EngineArgs g)
         const bool last = step + 1 == g.nsteps || !(t + h < s_tf);
         TRACE();
         for (int stage = 0; stage < 4; ++stage) {
-            for (int it = blockIdx.x; it < na; it += gridDim.x) phase_a<T>(g, it * RA, stage, h, smem);
+            for (int it = blockIdx.x; it < na; it += gridDim.x) phase_a<T>(g, it * RA, stage, h, smem, tw);
             TRACE();
             grid.sync();
             TRACE();
-            for (int it = blockIdx.x; it < nb; it += gridDim.x) phase_b<T>(g, it * g.CB, g.CB, smem);
+            for (int it = blockIdx.x; it < nb; it += gridDim.x) phase_b<T>(g, it * g.CB, g.CB, smem, tw);
             TRACE();
             grid.sync();
             TRACE();
-            for (int it = blockIdx.x; it < nc; it += gridDim.x) phase_c<T>(g, it * RC, (T*)g.raw[stage], smem);
+            for (int it = blockIdx.x; it < nc; it += gridDim.x) phase_c<T>(g, it * RC, (T*)g.raw[stage], smem, tw);
             TRACE();
             grid.sync();
             TRACE();

@@ -10,17 +10,19 @@
 //
 // Twiddles come from a per-length table tw[t] = exp(-2 pi i t / n) built on
 // the host in long double; sign = -1 is the forward transform, +1 the
-// unnormalised inverse.
+// unnormalised inverse.  SH = true reads the table from a shared-memory copy
+// (a persistent kernel keeps it resident instead of refetching it from L2
+// after the data it streams has pushed it out of L1).
 #pragma once
 
 #include "fi_common.cuh"
 
 namespace fi {
 
-template <typename T, typename C2>
+template <typename T, typename C2, bool SH = false>
 __device__ __forceinline__ C2 tw_load(const C2* __restrict__ tw, int t, int sign)
 {
-    C2 w = __ldg(tw + t);
+    C2 w = SH ? tw[t] : __ldg(tw + t);
     if (sign > 0) w.y = -w.y;
     return w;
 }
@@ -100,7 +102,7 @@ __device__ __forceinline__ void dft3(C2& a, C2& b, C2& c, int sign)
 
 // One line-parallel Stockham stage.  Specialised radices keep the R values
 // in registers; other radices use a direct sum over the table.
-template <typename T, int R>
+template <typename T, int R, bool SH = false>
 __device__ __forceinline__ void stage_fixed(const typename vec2<T>::type* __restrict__ src,
                                             typename vec2<T>::type* __restrict__ dst, int n, int nl,
                                             int ls, int Ns, const typename vec2<T>::type* __restrict__ tw,
@@ -121,7 +123,7 @@ __device__ __forceinline__ void stage_fixed(const typename vec2<T>::type* __rest
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             C2 a = x[j + r * NR];
-            if (r > 0 && jm > 0) a = cmul(a, tw_load<T, C2>(tw, jm * r * tstep, sign));
+            if (r > 0 && jm > 0) a = cmul(a, tw_load<T, C2, SH>(tw, jm * r * tstep, sign));
             v[r] = a;
         }
         if (R == 2) dft2<T, C2>(v[0], v[1]);
@@ -133,7 +135,7 @@ __device__ __forceinline__ void stage_fixed(const typename vec2<T>::type* __rest
     }
 }
 
-template <typename T>
+template <typename T, bool SH = false>
 __device__ void stage_generic(const typename vec2<T>::type* __restrict__ src,
                               typename vec2<T>::type* __restrict__ dst, int n, int nl, int ls, int R,
                               int Ns, const typename vec2<T>::type* __restrict__ tw, int sign, int tid,
@@ -156,9 +158,9 @@ __device__ void stage_generic(const typename vec2<T>::type* __restrict__ src,
         C2 acc = mk2<T>((T)0, (T)0);
         for (int r = 0; r < R; ++r) {
             C2 a = x[j + r * NR];
-            if (r > 0 && jm > 0) a = cmul(a, tw_load<T, C2>(tw, jm * r * tstep, sign));
+            if (r > 0 && jm > 0) a = cmul(a, tw_load<T, C2, SH>(tw, jm * r * tstep, sign));
             const int e = ((r * q) % R) * step;
-            acc = cadd(acc, cmul(a, tw_load<T, C2>(tw, e, sign)));
+            acc = cadd(acc, cmul(a, tw_load<T, C2, SH>(tw, e, sign)));
         }
         y[out0 + q * Ns] = acc;
     }
@@ -167,7 +169,7 @@ __device__ void stage_generic(const typename vec2<T>::type* __restrict__ src,
 // Runs all stages on nl lines held in buf0 (scratch buf1, same shape).
 // Returns the buffer holding the result.  Must be called by every thread of
 // the block (it synchronises internally); the caller synchronises before.
-template <typename T>
+template <typename T, bool SH = false>
 __device__ typename vec2<T>::type* block_fft(typename vec2<T>::type* buf0, typename vec2<T>::type* buf1,
                                              const FftDesc& d, int nl, int ls,
                                              const typename vec2<T>::type* __restrict__ tw, int sign)
@@ -181,11 +183,11 @@ __device__ typename vec2<T>::type* block_fft(typename vec2<T>::type* buf0, typen
     for (int s = 0; s < d.nf; ++s) {
         const int R = d.fac[s];
         switch (R) {
-        case 8: stage_fixed<T, 8>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        case 4: stage_fixed<T, 4>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        case 2: stage_fixed<T, 2>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        case 3: stage_fixed<T, 3>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        default: stage_generic<T>(src, dst, d.n, nl, ls, R, Ns, tw, sign, tid, nthr); break;
+        case 8: stage_fixed<T, 8, SH>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        case 4: stage_fixed<T, 4, SH>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        case 2: stage_fixed<T, 2, SH>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        case 3: stage_fixed<T, 3, SH>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        default: stage_generic<T, SH>(src, dst, d.n, nl, ls, R, Ns, tw, sign, tid, nthr); break;
         }
         __syncthreads();
         C2* t = src;
