@@ -240,6 +240,11 @@ struct fi_handle {
     void* S = nullptr;                   // RHS half spectrum (T complex)
     void* mA = nullptr;                  // 1/(kappa R) at (k, l) (T)
     void* mB = nullptr;                  // 1/(kappa R) at (-k, l) (T)
+    // step engine only: the half spectrum and the factors column-major
+    // (element (l, k) at k*ny + l), so a spectrum column is contiguous
+    void* ST = nullptr;
+    void* mAT = nullptr;
+    void* mBT = nullptr;
     void* S2 = nullptr;                  // convolution spectrum (T complex)
     void* KS[3] = {nullptr, nullptr, nullptr};   // elastic / geoid / LV-ELRA viscous kernel spectra (T complex)
     double* weq = nullptr;               // equilibrium displacement (methods 0-2)
@@ -567,6 +572,15 @@ int upload_static(fi_handle* h)
         for (int k = 0; k < nx; ++k)
             if (m(k, l) != m((nx - k) % nx, l) || m(k, l) != m(k, (ny - l) % ny)) { h->even = 0; break; }
     if ((rc = upload_T(h, h->mA, A)) || (rc = upload_T(h, h->mB, B))) return rc;
+    if (h->mAT) {
+        std::vector<double> AT((size_t)(hh + 1) * ny), BT((size_t)(hh + 1) * ny);
+        for (int k = 0; k <= hh; ++k)
+            for (int l = 0; l < ny; ++l) {
+                AT[(size_t)k * ny + l] = A[(size_t)l * spitch + k];
+                BT[(size_t)k * ny + l] = B[(size_t)l * spitch + k];
+            }
+        if ((rc = upload_T(h, h->mAT, AT)) || (rc = upload_T(h, h->mBT, BT))) return rc;
+    }
 
     if ((rc = upload(h, (void*)h->d.mactive, h->mact.data(), n))) return rc;
     return FI_OK;
@@ -792,8 +806,9 @@ template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
     g.q0 = h->q0;
     g.D = h->Dt;
     g.inv2eta = h->inv2eta;
-    g.mA = h->mA;
-    g.mB = h->mB;
+    g.mA = h->mAT;
+    g.mB = h->mBT;
+    g.ST = h->ST;
     g.even = h->even;
     g.mask = h->d.mactive;
     for (int i = 0; i < 4; ++i) g.raw[i] = h->raw[i];
@@ -1403,11 +1418,15 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
                               : engine_config<double>(h->prhs, &h->eng_grid, &h->eng_CB, &h->eng_smem);
             h->engine_ok = ok != 0;
             cudaGetLastError();
-            if (h->engine_ok && mixed(h)) {
 #define AL2(ptr, bytes) if ((rc = dalloc(h, &(ptr), (bytes)))) return rc
-                AL2(h->xhi, n * 4); AL2(h->xlo, n * 4); AL2(h->wrefhi, n * 4); AL2(h->wreflo, n * 4);
-#undef AL2
+            if (h->engine_ok) {
+                const size_t nk = (size_t)(h->prhs.h + 1) * h->ny;
+                AL2(h->ST, nk * c2); AL2(h->mAT, nk * tsz(h)); AL2(h->mBT, nk * tsz(h));
             }
+            if (h->engine_ok && mixed(h)) {
+                AL2(h->xhi, n * 4); AL2(h->xlo, n * 4); AL2(h->wrefhi, n * 4); AL2(h->wreflo, n * 4);
+            }
+#undef AL2
         }
     }
     if ((rc = upload_static(h))) return rc;

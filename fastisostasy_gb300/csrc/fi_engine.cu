@@ -294,7 +294,9 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
     __syncthreads();
     C2* r = block_fft<T, true>(b0, b1, g.p.row.d, RA, hh, tw.row, -1);
     const C2* rtw = tw.rtw;
-    C2* S = (C2*)g.S;
+    // column-major: the strided stores do not hold the block up, and phase B
+    // then reads each spectrum column contiguously
+    C2* ST = (C2*)g.ST;
     for (int o = tw.wh1.r0, k = tw.wh1.i0; o < RA; tw.wh1.next(o, k)) {
         const int gj = j0 + o;
         if (gj >= ny) continue;
@@ -305,14 +307,15 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         E.y = (T)0.5 * (Zk.y - Zc.y);
         O.x = (T)0.5 * (Zk.y + Zc.y);
         O.y = (T)-0.5 * (Zk.x - Zc.x);
-        S[(size_t)gj * g.p.sp + k] = cadd(E, cmul(rtw[k], O));
+        ST[(size_t)k * ny + gj] = cadd(E, cmul(rtw[k], O));
     }
     __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
 // Phase B: CB spectrum columns: forward column FFT, Hartley-basis multiply,
-// inverse column FFT.
+// inverse column FFT.  Columns come contiguous from the column-major copy
+// phase A wrote; the result goes back row-major for the row passes of C.
 // ---------------------------------------------------------------------------
 template <typename T>
 __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem, const EngTw<T>& tw)
@@ -326,7 +329,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
     for (int e = tid; e < CB * ny; e += nt) {
         const int c = CB == 1 ? 0 : e % CB, l = CB == 1 ? e : e / CB;
         const int k = k0 + c;
-        b0[c * ny + l] = (k <= g.p.h) ? S[(size_t)l * g.p.sp + k] : mk2<T>((T)0, (T)0);
+        b0[c * ny + l] = (k <= g.p.h) ? ((const C2*)g.ST)[(size_t)k * ny + l] : mk2<T>((T)0, (T)0);
     }
     __syncthreads();
     C2* r = block_fft<T, true>(b0, b1, g.p.col.d, CB, ny, tw.col, -1);
@@ -339,7 +342,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
         if (k > g.p.h) continue;
         const int lm = (ny - l) % ny;
         C2* col = r + (size_t)c * ny;
-        const size_t ia = (size_t)l * g.p.sp + k, ib = (size_t)lm * g.p.sp + k;
+        const size_t ia = (size_t)k * ny + l, ib = (size_t)k * ny + lm;   // column-major factors
         const C2 Fa = col[l], Fb = col[lm];
         if (g.even) {
             const T ma = mA[ia], mb = mA[ib];

@@ -22,12 +22,13 @@ struct EngineArgs {
     const void* q0;                  // RHS load term, field type
     const void* D;
     const void* inv2eta;
-    const void* mA;
+    const void* mA;                  // 1/(kappa R) factors, column-major (k*ny + l)
     const void* mB;
     int even;
     const uint8_t* mask;
     void* raw[4];                    // stage outputs, field type
-    void* S;                         // half spectrum, field type complex
+    void* S;                         // half spectrum, field type complex, row-major (pitch p.sp)
+    void* ST;                        // the same, column-major (k*ny + l): phase A -> phase B
     Ctl* ctl;
     int nsteps;
     int CB;                          // spectrum columns per phase-B item
