@@ -222,6 +222,7 @@ struct fi_handle {
     cudaStream_t s_body = nullptr;       // captures the body of the device Tsit5 loop
     std::vector<void*> allocs;
     std::string err;
+    cudaError_t launch_err = cudaSuccess;   // a launch whose status the enqueue path cannot return
     // host copies of the static fields
     std::vector<double> K, kappa, R, D, He, eta_eff, GE, GN, GV, xc, yc;
     std::vector<uint8_t> mact;
@@ -819,7 +820,9 @@ template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
     g.spy = h->spy;
     g.norm_scale = 1.0 / (double)(float)((long long)h->nx * h->ny);
     g.trace = h->trace;
-    PROF(h, K_ENGINE, engine_launch<T>(g, h->eng_grid, h->eng_smem, h->s));
+    cudaError_t le = cudaSuccess;
+    PROF(h, K_ENGINE, le = engine_launch<T>(g, h->eng_grid, h->eng_smem, h->s));
+    if (le != cudaSuccess && h->launch_err == cudaSuccess) h->launch_err = le;
     h->launches += 1;
     return (T*)h->raw[3];
 }
@@ -1037,9 +1040,20 @@ template <typename T> int update_T(fi_handle* h, const double* dH, double time, 
         enqueue_post<T>(h, (T*)h->raw[0], -1);
         return FI_OK;
     };
+    // the status of the engine's cooperative launch, which the enqueue path
+    // records instead of returning: a refused launch fails this update, also
+    // inside a stream capture, instead of leaving a step sequence that did
+    // nothing
+    auto launch_status = [&]() -> int {
+        const cudaError_t le = h->launch_err;
+        h->launch_err = cudaSuccess;
+        if (le != cudaSuccess) return fail(h, FI_E_CUDA, "engine launch: %s", cudaGetErrorString(le));
+        return FI_OK;
+    };
     if (!h->use_graphs || h->prof_on || (tsit && !h->tsit_graph_ok)) {
         const int rc = enqueue();
         if (rc) return rc;
+        if (const int lrc = launch_status()) return lrc;
         CK(cudaGetLastError());
         return FI_OK;
     }
@@ -1056,6 +1070,7 @@ template <typename T> int update_T(fi_handle* h, const double* dH, double time, 
         h->graph_seen.push_back(key);
         const int rc = enqueue();
         if (rc) return rc;
+        if (const int lrc = launch_status()) return lrc;
         CK(cudaGetLastError());
         return FI_OK;
     }
@@ -1064,9 +1079,15 @@ template <typename T> int update_T(fi_handle* h, const double* dH, double time, 
     const int rc = enqueue_captured();
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(h->s, &graph);
+    if (e == cudaSuccess && h->launch_err != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return launch_status();
+    }
     if (rc || e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         cudaGetLastError();
+        h->launch_err = cudaSuccess;
         if (tsit && rc != FI_E_CONFIG && !h->require_tsit_graph) {
             // no conditional graph nodes here: keep deciding Tsit5 attempts on the host
             h->tsit_graph_ok = false;
@@ -1074,6 +1095,7 @@ template <typename T> int update_T(fi_handle* h, const double* dH, double time, 
             h->launches = l0;
             const int rc2 = enqueue();
             if (rc2) return rc2;
+            if (const int lrc = launch_status()) return lrc;
             CK(cudaGetLastError());
             return FI_OK;
         }
@@ -2009,8 +2031,11 @@ int batch_shape(fi_batch* b, int RB, int CB, int fseg, int waves)
     if (b->rows_smem > 200 * 1024 || b->cols_smem > 200 * 1024) return 2;   // shape does not fit
     for (int k = 0; k < 4; ++k) b->nblk[k] = off[k * (n + 1) + n];
     b->hoff = off;
-    if (cudaMemcpy(b->dM, b->hM.data(), n * sizeof(BMember), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(b->doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+    // on the batch stream that reads them (a plain cudaMemcpy from pageable
+    // memory is not ordered before work on a non-blocking stream)
+    if (cudaMemcpyAsync(b->dM, b->hM.data(), n * sizeof(BMember), cudaMemcpyHostToDevice, b->s) != cudaSuccess ||
+        cudaMemcpyAsync(b->doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, b->s) != cudaSuccess ||
+        cudaStreamSynchronize(b->s) != cudaSuccess)
         return 1;
     int res[4];
     if (b->mixed) {
@@ -2306,7 +2331,10 @@ int batch_all_lists(fi_batch* b)
         const int src = k < 3 ? k : (k == 3 ? 3 : k - 4);
         for (int i = 0; i <= n; ++i) cl[2 + 2 * n + k * (n + 1) + i] = b->hoff[src * (n + 1) + i];
     }
-    return cudaMemcpy(b->dcl, cl.data(), cl.size() * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess ? 0 : 1;
+    return (cudaMemcpyAsync(b->dcl, cl.data(), cl.size() * sizeof(int), cudaMemcpyHostToDevice, b->s) == cudaSuccess &&
+            cudaStreamSynchronize(b->s) == cudaSuccess)
+               ? 0
+               : 1;
 }
 
 // Device time [ms] of the first RHS of an attempt over all members: part 1

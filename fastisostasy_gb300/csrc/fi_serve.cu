@@ -21,6 +21,7 @@
 // A request's arithmetic does not depend on what else runs: every handle has
 // its own buffers and stream and every reduction is deterministic, so a
 // result is bit-identical alone and in a mix.
+#include <cmath>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -98,7 +99,7 @@ namespace {
 
 void finish(fi_server* s, Req* r, int state, int status)
 {
-    if (state == 3) {
+    if (state == 3 && !r->info.error[0]) {
         const char* m = r->h ? fi_last_error(r->h) : "";
         snprintf(r->info.error, sizeof(r->info.error), "%s", (m && m[0]) ? m : "solve failed");
     }
@@ -145,7 +146,13 @@ int start(fi_server* s, Req* r)
     if ((rc = fi_init_state(r->h, r->z_bed.data(), r->Href.data(), r->t0, &r->b))) return rc;
     const size_t hb = r->H.size() * sizeof(double);
     if (cudaMalloc(&r->dH, hb) != cudaSuccess) return FI_E_OOM;
-    if (cudaMemcpy(r->dH, r->H.data(), hb, cudaMemcpyHostToDevice) != cudaSuccess) return FI_E_CUDA;
+    // On the handle's stream: a plain cudaMemcpy from pageable memory may
+    // return before its DMA lands, and the handle's non-blocking stream, which
+    // reads the load first thing in the first update, is not ordered after it.
+    cudaStream_t hs = (cudaStream_t)fi_stream(r->h);
+    if (cudaMemcpyAsync(r->dH, r->H.data(), hb, cudaMemcpyHostToDevice, hs) != cudaSuccess ||
+        cudaStreamSynchronize(hs) != cudaSuccess)
+        return FI_E_CUDA;
     for (auto& e : r->ev)
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return FI_E_CUDA;
     size_t free1 = 0;
@@ -186,6 +193,17 @@ void collect(fi_server* s, Req* r)
         return;
     }
     int st = fi_synchronize(r->h);
+    if (st == FI_OK && r->nsteps > 0) {
+        // the model clock must have reached t_end: a request whose solve did
+        // not advance is an error, never a result
+        double sc[16];
+        if ((st = fi_get_scalars(r->h, sc)) == FI_OK &&
+            !(fabs(sc[0] - r->t_end) <= 1e-9 * fmax(1.0, fabs(r->t_end)))) {
+            snprintf(r->info.error, sizeof(r->info.error), "model clock %.9g short of t_end %.9g (dt %.3g, %d steps)",
+                     sc[0], r->t_end, sc[1], (int)sc[9]);
+            st = FI_E_STATE;
+        }
+    }
     if (st == FI_OK) {
         const int nx = r->pd[0];
         std::vector<double> pad((size_t)r->pd[0] * r->pd[1]);

@@ -153,7 +153,10 @@ int fi_init_state(fi_handle* h, const double* z_bed, const double* H_ice, double
 int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_out* out);
 /* Asynchronous isos_update for device-resident inputs: d_H_ice is a DEVICE
  * pointer to the ice-grid thickness (NULL keeps the previous one).  Valid for
- * bsl methods const and file; returns before the work completes. */
+ * bsl methods const and file; returns before the work completes.  The read of
+ * d_H_ice is ordered on the handle's stream (fi_stream / fi_set_stream): work
+ * that fills it on another stream, including a plain cudaMemcpy from pageable
+ * memory, must have completed or be ordered before that stream. */
 int fi_update_async(fi_handle* h, const double* d_H_ice, double time, fi_bsl* bsl);
 /* Waits for the handle's stream; returns the device status (FI_E_NAN, ...). */
 int fi_synchronize(fi_handle* h);

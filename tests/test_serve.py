@@ -91,6 +91,37 @@ def test_alone_and_in_a_mix_are_identical(precision):
 
 
 @pytest.mark.gpu
+def test_every_request_of_a_repeated_mix_matches_its_solve_alone():
+    """Regression for a load upload that was not ordered before the handle's
+    stream: run the same mix of mixed-form step-engine requests (and FP64
+    Tsit5 ones beside them) several times and compare every request, not one,
+    with its solve alone."""
+    sizes = (32, 48, 96, 128, 40, 80, 64)
+    srv = Server(max_inflight=1, reserve_gb=1.0)
+    alone = {}
+    for n in sizes:
+        rid = srv.submit(small_rk4(n), precision=1)
+        srv.wait(rid, 120.0)
+        alone[n] = srv.result(rid)
+    srv.close()
+    for _ in range(12):
+        srv = Server(max_inflight=16, reserve_gb=1.0)
+        ids = []
+        for i, n in enumerate(sizes[:6]):
+            ids.append((n, srv.submit(small_rk4(n), precision=1)))
+            if i == 2:
+                ids.append((64, srv.submit(small_rk4(64), precision=1)))
+            ids.append((None, srv.submit(small_tsit(32 + 8 * (i % 3)), precision=0)))
+        for n, rid in ids:
+            info = srv.wait(rid, 300.0)
+            assert info["status"] == 0, info
+            w, zb = srv.result(rid)
+            if n is not None:
+                assert np.array_equal(w, alone[n][0]) and np.array_equal(zb, alone[n][1]), n
+        srv.close()
+
+
+@pytest.mark.gpu
 def test_inflight_cap_and_drain():
     srv = Server(max_inflight=2, reserve_gb=0.5)
     ids = [srv.submit(small_rk4(48)) for _ in range(5)]
