@@ -5,7 +5,7 @@
 // calc_lvelva, src/lv_elva.f90:31-126, at every stage state).  The grid
 // walks through phases separated by grid-wide barriers:
 //
-//   A  stencil + row real-FFT   (work item = 2 grid rows, full width)
+//   A  stencil + row real-FFT   (work item = 4 grid rows, full width)
 //   B  column FFT, multiply by 1/(kappa R) in the Hartley basis, inverse
 //   C  inverse row real-FFT -> raw_s (stage output before corner BC / sec_per_year)
 //   D  x += h/6 (k1 + 2 k2 + 2 k3 + k4), w = x
@@ -38,8 +38,12 @@ template <typename T> __device__ __forceinline__ const typename vec2<T>::type* e
 template <> __device__ __forceinline__ const double2* ertw<double>(const Plan2D& p) { return p.rtw64; }
 template <> __device__ __forceinline__ const float2* ertw<float>(const Plan2D& p) { return p.rtw32; }
 
-constexpr int RA = 2;   // rows per phase-A item (must be even: see the y-boundary stencils)
-constexpr int RC = 2;   // rows per phase-C item
+// Rows per phase-A item (even: see the y-boundary stencils).  Four rows on
+// one 1024-thread block per SM read 8 state rows for 4 output rows; two-row
+// items on two 512-thread blocks per SM read 12 (measured 1.198 against
+// 1.251 ms per 512^2 update).
+constexpr int RA = 4;
+constexpr int RC = 4;   // rows per phase-C item
 
 // stage coefficients of RK4: y_s = x + a_s h k_{s-1}
 __constant__ double c_rk4_a[4] = {0.0, 0.5, 0.5, 1.0};
@@ -119,7 +123,7 @@ template <typename T> __device__ __forceinline__ double corner_mean_dev(const T*
 }
 
 // ---------------------------------------------------------------------------
-// Phase A: one item = output rows j0, j0+1 (full width).
+// Phase A: one item = output rows j0 .. j0+RA-1 (full width).
 // ---------------------------------------------------------------------------
 template <typename T>
 __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsigned char* smem, const EngTw<T>& tw)
@@ -426,7 +430,7 @@ __device__ __forceinline__ unsigned long long gtimer()
 }
 
 template <typename T>
-__global__ void __launch_bounds__(512, 2) k_engine_rk4(EngineArgs g)
+__global__ void __launch_bounds__(1024, 1) k_engine_rk4(EngineArgs g)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     cg::grid_group grid = cg::this_grid();
@@ -567,16 +571,16 @@ void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s)
     k_split<<<b, 256, 0, s>>>(x, hi, lo, n);
 }
 
-// threads per engine block: 512 (two blocks, 1024 threads per SM at 64
-// registers); FI_ENGINE_THREADS=256 for tuning
+// threads per engine block: 1024 (one block per SM, the whole register
+// file at 64 registers); FI_ENGINE_THREADS=256 or 512 for tuning
 int engine_threads()
 {
     static int t = [] {
         if (const char* ev = getenv("FI_ENGINE_THREADS")) {
             const int v = atoi(ev);
-            if (v == 256 || v == 512) return v;
+            if (v == 256 || v == 512 || v == 1024) return v;
         }
-        return 512;
+        return 1024;
     }();
     return t;
 }
@@ -586,9 +590,9 @@ template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, siz
     // The plain FP64 form is FP64-throughput bound; it runs faster as the
     // multi-kernel graph (full occupancy) than in the one-grid engine.
     if (sizeof(T) == 8) return 0;
-    // one spectrum column per phase-B item: twice the items of two, so all
-    // resident blocks share phase B (measured faster at 512^2 than 16-byte rows)
-    int cb = 1;
+    // two spectrum columns per phase-B item, one per half of the 1024-thread
+    // block: 129 items at 512^2, one for each resident block
+    int cb = 2;
     // FI_ENGINE_CB: spectrum columns per phase-B item (tuning)
     if (const char* ev = getenv("FI_ENGINE_CB")) {
         const int v = atoi(ev);
@@ -619,7 +623,7 @@ template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, siz
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T>, engine_threads(), *smem) != cudaSuccess || per_sm < 1)
         return 0;
-    int cap = 2;   // FI_ENGINE_PER_SM: resident blocks per SM, at most (tuning)
+    int cap = 1;   // FI_ENGINE_PER_SM: resident blocks per SM, at most (tuning)
     if (const char* ev = getenv("FI_ENGINE_PER_SM")) {
         const int v = atoi(ev);
         if (v >= 1 && v <= 8) cap = v;
