@@ -38,17 +38,22 @@ template <typename T> __device__ __forceinline__ const typename vec2<T>::type* e
 template <> __device__ __forceinline__ const double2* ertw<double>(const Plan2D& p) { return p.rtw64; }
 template <> __device__ __forceinline__ const float2* ertw<float>(const Plan2D& p) { return p.rtw32; }
 
-// Rows per phase-A item (even: see the y-boundary stencils).  Four rows on
-// one 1024-thread block per SM read 8 state rows for 4 output rows; two-row
-// items on two 512-thread blocks per SM read 12 (measured 1.198 against
-// 1.251 ms per 512^2 update).
-constexpr int RA = 4;
-constexpr int RC = 4;   // rows per phase-C item
+// Rows per phase-A and phase-C item, a template parameter of the kernel
+// (even: see the y-boundary stencils).  RA = 4 on one 1024-thread block per
+// SM reads 8 state rows for 4 output rows; RA = 2 on two 512-thread blocks
+// per SM reads 12, but has twice the items.  The 4-row shape is taken when
+// its items occupy most SMs (512^2: 1.198 against 1.251 ms per update), the
+// 2-row shape below that (256^2: 128 two-row items against 64 four-row ones).
+template <int RA> struct EngShape {
+    static constexpr int threads = RA == 4 ? 1024 : 512;
+    static constexpr int per_sm = RA == 4 ? 1 : 2;   // resident blocks per SM
+    static constexpr int cb = RA == 4 ? 2 : 1;       // spectrum columns per phase-B item
+};
 
 // stage coefficients of RK4: y_s = x + a_s h k_{s-1}
 __constant__ double c_rk4_a[4] = {0.0, 0.5, 0.5, 1.0};
 
-template <typename T> struct PhaseAMem {
+template <typename T, int RA> struct PhaseAMem {
     // level-0 differences on RA+4 rows, moments on RA+2 rows, all full width
     __host__ __device__ static size_t bytes(int nx, int h)
     {
@@ -61,10 +66,11 @@ template <typename T> struct PhaseAMem {
 // Dynamic shared memory: the phase scratch (the largest of A, B, C), then
 // the twiddle tables of the row and column transforms and of the real-FFT
 // split, copied once per launch and resident for all its phases.
-template <typename T> __host__ __device__ inline size_t engine_tab_off(int nx, int h, int ny, int CB)
+template <typename T, int RA> __host__ __device__ inline size_t engine_tab_off(int nx, int h, int ny, int CB)
 {
     typedef typename vec2<T>::type C2;
-    const size_t a = PhaseAMem<T>::bytes(nx, h);
+    constexpr int RC = RA;
+    const size_t a = PhaseAMem<T, RA>::bytes(nx, h);
     const size_t b = 2 * (size_t)CB * ny * sizeof(C2);
     const size_t c = 2 * (size_t)RC * h * sizeof(C2);
     size_t m = a > b ? a : b;
@@ -76,10 +82,10 @@ template <typename T> __host__ __device__ inline size_t engine_tab_count(int h, 
     return (size_t)h + (size_t)ny + (size_t)h + 1;   // row, column, real split
 }
 
-template <typename T> size_t engine_smem_bytes(const Plan2D& p, int CB)
+template <typename T, int RA> size_t engine_smem_bytes(const Plan2D& p, int CB)
 {
     typedef typename vec2<T>::type C2;
-    return engine_tab_off<T>(p.nx, p.h, p.ny, CB) + engine_tab_count<T>(p.h, p.ny) * sizeof(C2) + 64;
+    return engine_tab_off<T, RA>(p.nx, p.h, p.ny, CB) + engine_tab_count<T>(p.h, p.ny) * sizeof(C2) + 64;
 }
 
 // (row, column) walk of a block's threads over a row-major strip of width w
@@ -125,7 +131,7 @@ template <typename T> __device__ __forceinline__ double corner_mean_dev(const T*
 // ---------------------------------------------------------------------------
 // Phase A: one item = output rows j0 .. j0+RA-1 (full width).
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, int RA>
 __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsigned char* smem, const EngTw<T>& tw)
 {
     typedef typename vec2<T>::type C2;
@@ -383,7 +389,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
 // ---------------------------------------------------------------------------
 // Phase C: inverse row real-FFT of rows j0 .. j0+RC-1 -> raw (scaled 1/(nx ny)).
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, int RC>
 __device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem, const EngTw<T>& tw)
 {
     typedef typename vec2<T>::type C2;
@@ -429,9 +435,10 @@ __device__ __forceinline__ unsigned long long gtimer()
     return t;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(1024, 1) k_engine_rk4(EngineArgs g)
+template <typename T, int RA>
+__global__ void __launch_bounds__(EngShape<RA>::threads, EngShape<RA>::per_sm) k_engine_rk4(EngineArgs g)
 {
+    constexpr int RC = RA;
     extern __shared__ __align__(16) unsigned char smem[];
     cg::grid_group grid = cg::this_grid();
     const int nx = g.p.nx, ny = g.p.ny;
@@ -453,7 +460,7 @@ __global__ void __launch_bounds__(1024, 1) k_engine_rk4(EngineArgs g)
     typedef typename vec2<T>::type C2;
     EngTw<T> tw;
     {
-        C2* tab = reinterpret_cast<C2*>(smem + engine_tab_off<T>(nx, g.p.h, ny, g.CB));
+        C2* tab = reinterpret_cast<C2*>(smem + engine_tab_off<T, RA>(nx, g.p.h, ny, g.CB));
         const C2* srow = etw<T>(g.p.row);
         const C2* scol = etw<T>(g.p.col);
         const C2* srtw = ertw<T>(g.p);
@@ -490,7 +497,7 @@ __global__ void __launch_bounds__(1024, 1) k_engine_rk4(EngineArgs g)
         const bool last = step + 1 == g.nsteps || !(t + h < s_tf);
         TRACE();
         for (int stage = 0; stage < 4; ++stage) {
-            for (int it = blockIdx.x; it < na; it += gridDim.x) phase_a<T>(g, it * RA, stage, h, smem, tw);
+            for (int it = blockIdx.x; it < na; it += gridDim.x) phase_a<T, RA>(g, it * RA, stage, h, smem, tw);
             TRACE();
             grid.sync();
             TRACE();
@@ -498,7 +505,7 @@ __global__ void __launch_bounds__(1024, 1) k_engine_rk4(EngineArgs g)
             TRACE();
             grid.sync();
             TRACE();
-            for (int it = blockIdx.x; it < nc; it += gridDim.x) phase_c<T>(g, it * RC, (T*)g.raw[stage], smem, tw);
+            for (int it = blockIdx.x; it < nc; it += gridDim.x) phase_c<T, RC>(g, it * RC, (T*)g.raw[stage], smem, tw);
             TRACE();
             grid.sync();
             TRACE();
@@ -571,40 +578,12 @@ void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s)
     k_split<<<b, 256, 0, s>>>(x, hi, lo, n);
 }
 
-// threads per engine block: 1024 (one block per SM, the whole register
-// file at 64 registers); FI_ENGINE_THREADS=256 or 512 for tuning
-int engine_threads()
+template <typename T, int RA> int engine_config_shape(const Plan2D& p, int nsm, int optin, int* grid, int* CB,
+                                                     size_t* smem)
 {
-    static int t = [] {
-        if (const char* ev = getenv("FI_ENGINE_THREADS")) {
-            const int v = atoi(ev);
-            if (v == 256 || v == 512 || v == 1024) return v;
-        }
-        return 1024;
-    }();
-    return t;
-}
-
-template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem)
-{
-    // The plain FP64 form is FP64-throughput bound; it runs faster as the
-    // multi-kernel graph (full occupancy) than in the one-grid engine.
-    if (sizeof(T) == 8) return 0;
-    // two spectrum columns per phase-B item, one per half of the 1024-thread
-    // block: 129 items at 512^2, one for each resident block
-    int cb = 2;
-    // FI_ENGINE_CB: spectrum columns per phase-B item (tuning)
-    if (const char* ev = getenv("FI_ENGINE_CB")) {
-        const int v = atoi(ev);
-        if (v >= 1 && v <= 8) cb = v;
-    }
-    if (cb < 1) cb = 1;
+    const int cb = EngShape<RA>::cb;
     *CB = cb;
-    *smem = engine_smem_bytes<T>(p, cb);
-    int dev = 0, nsm = 0, optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    *smem = engine_smem_bytes<T, RA>(p, cb);
     if (*smem > (size_t)optin) return 0;
     {
         // the limit is a property of the kernel, shared by every handle:
@@ -614,29 +593,26 @@ template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, siz
         static size_t cur = 0;
         std::lock_guard<std::mutex> lk(mu);
         if (*smem > cur) {
-            if (cudaFuncSetAttribute(k_engine_rk4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) !=
+            if (cudaFuncSetAttribute(k_engine_rk4<T, RA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) !=
                 cudaSuccess)
                 return 0;
             cur = *smem;
         }
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T>, engine_threads(), *smem) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T, RA>, EngShape<RA>::threads, *smem) !=
+            cudaSuccess ||
+        per_sm < 1)
         return 0;
-    int cap = 1;   // FI_ENGINE_PER_SM: resident blocks per SM, at most (tuning)
-    if (const char* ev = getenv("FI_ENGINE_PER_SM")) {
-        const int v = atoi(ev);
-        if (v >= 1 && v <= 8) cap = v;
-    }
-    if (per_sm > cap) per_sm = cap;
+    if (per_sm > EngShape<RA>::per_sm) per_sm = EngShape<RA>::per_sm;
     // no more blocks than the largest phase has work items: a small domain
     // then leaves SMs free for other handles' work (serving, ensembles)
-    const int na = (p.ny + RA - 1) / RA, nb = (p.h + 1 + cb - 1) / cb, nc = (p.ny + RC - 1) / RC;
+    const int na = (p.ny + RA - 1) / RA, nb = (p.h + 1 + cb - 1) / cb, nc = na;
     // the stencil phase must fit one wave of resident blocks: beyond that
-    // (1024^2: 512 items on 152 one-block SMs) every barrier waits for
-    // several items in a row and the kernel sequence is faster (measured
-    // 5.4 ms per update in the engine against 13.4 / 4 ms per 1024^2-sized
-    // quarter of a 2048^2 update in the kernel sequence)
+    // (1024^2) every barrier waits for several items in a row and the kernel
+    // sequence is faster (measured 5.4 ms per update in the engine against
+    // 13.4 / 4 ms per 1024^2-sized quarter of a 2048^2 update in the kernel
+    // sequence)
     if (na > per_sm * nsm) return 0;
     int items = na > nb ? na : nb;
     if (nc > items) items = nc;
@@ -644,25 +620,54 @@ template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, siz
     return 1;
 }
 
-template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, size_t smem, cudaStream_t s)
+template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem, int* RA)
 {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(engine_threads());
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_engine_rk4<T>, g);
+    // The plain FP64 form is FP64-throughput bound; it runs faster as the
+    // multi-kernel graph (full occupancy) than in the one-grid engine.
+    if (sizeof(T) == 8) return 0;
+    int dev = 0, nsm = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    // four-row items when there are enough of them for three quarters of the SMs
+    int ra = (p.ny + 3) / 4 >= (3 * nsm + 3) / 4 ? 4 : 2;
+    // FI_ENGINE_RA: rows per stencil item, 2 or 4 (tuning)
+    if (const char* ev = getenv("FI_ENGINE_RA")) {
+        const int v = atoi(ev);
+        if (v == 2 || v == 4) ra = v;
+    }
+    if constexpr (sizeof(T) == 4) {
+        if (ra == 4 && engine_config_shape<T, 4>(p, nsm, optin, grid, CB, smem)) {
+            *RA = 4;
+            return 1;
+        }
+        *RA = 2;
+        return engine_config_shape<T, 2>(p, nsm, optin, grid, CB, smem);
+    }
+    return 0;
 }
 
-template size_t engine_smem_bytes<float>(const Plan2D&, int);
-template size_t engine_smem_bytes<double>(const Plan2D&, int);
-template int engine_config<float>(const Plan2D&, int*, int*, size_t*);
-template int engine_config<double>(const Plan2D&, int*, int*, size_t*);
+template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, size_t smem, cudaStream_t s)
+{
+    if constexpr (sizeof(T) == 8) {
+        return cudaErrorNotSupported;   // engine_config never selects the plain form
+    } else {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(g.ra == 4 ? EngShape<4>::threads : EngShape<2>::threads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return g.ra == 4 ? cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 4>, g) : cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 2>, g);
+    }
+}
+
+template int engine_config<float>(const Plan2D&, int*, int*, size_t*, int*);
+template int engine_config<double>(const Plan2D&, int*, int*, size_t*, int*);
 template cudaError_t engine_launch<float>(const EngineArgs&, int, size_t, cudaStream_t);
 template cudaError_t engine_launch<double>(const EngineArgs&, int, size_t, cudaStream_t);
 

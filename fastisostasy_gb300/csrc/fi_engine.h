@@ -32,6 +32,7 @@ struct EngineArgs {
     Ctl* ctl;
     int nsteps;
     int CB;                          // spectrum columns per phase-B item
+    int ra;                          // rows per stencil item (kernel shape: 2 or 4)
     double spy;
     double norm_scale;               // 1 / (nx*ny*1.) as the reference normalises
     unsigned long long* trace;       // optional: %globaltimer at phase boundaries of the first step
@@ -43,9 +44,10 @@ struct EngineArgs {
     template <typename T> __device__ __forceinline__ const T* mB_T() const { return (const T*)mB; }
 };
 
-// Grid size (co-resident blocks), phase-B column count and dynamic shared
-// memory of the engine for this transform plan; 0 if it cannot run.
-template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem);
+// Grid size (co-resident blocks), phase-B column count, dynamic shared
+// memory and rows per stencil item of the engine for this transform plan;
+// 0 if it cannot run.
+template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem, int* RA);
 template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, size_t smem, cudaStream_t s);
 void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s);
 
