@@ -302,7 +302,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         bz[i] = fv;
     }
     __syncthreads();
-    C2* r = block_fft<T, true>(b0, b1, g.p.row.d, RA, hh, tw.row, -1);
+    C2* r = block_fft<T, true, false>(b0, b1, g.p.row.d, RA, hh, tw.row, -1);
     const C2* rtw = tw.rtw;
     // column-major: the strided stores do not hold the block up, and phase B
     // then reads each spectrum column contiguously
@@ -342,7 +342,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
         b0[c * ny + l] = (k <= g.p.h) ? ((const C2*)g.ST)[(size_t)k * ny + l] : mk2<T>((T)0, (T)0);
     }
     __syncthreads();
-    C2* r = block_fft<T, true>(b0, b1, g.p.col.d, CB, ny, tw.col, -1);
+    C2* r = block_fft<T, true, false>(b0, b1, g.p.col.d, CB, ny, tw.col, -1);
     const T* mA = g.mA_T<T>();
     const T* mB = g.mB_T<T>();
     const int half = ny / 2 + 1;
@@ -377,7 +377,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
     }
     __syncthreads();
     C2* other = (r == b0) ? b1 : b0;
-    C2* q = block_fft<T, true>(r, other, g.p.col.d, CB, ny, tw.col, +1);
+    C2* q = block_fft<T, true, false>(r, other, g.p.col.d, CB, ny, tw.col, +1);
     for (int e = tid; e < CB * ny; e += nt) {
         const int c = CB == 1 ? 0 : e % CB, l = CB == 1 ? e : e / CB;
         const int k = k0 + c;
@@ -414,7 +414,7 @@ __device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem
         b0[e] = z;
     }
     __syncthreads();
-    C2* r = block_fft<T, true>(b0, b1, g.p.row.d, RC, hh, tw.row, +1);
+    C2* r = block_fft<T, true, false>(b0, b1, g.p.row.d, RC, hh, tw.row, +1);
     const T scale = (T)g.norm_scale;
     for (int o = tw.wh.r0, m = tw.wh.i0; o < RC; tw.wh.next(o, m)) {
         const int j = j0 + o;

@@ -102,7 +102,7 @@ __device__ __forceinline__ void dft3(C2& a, C2& b, C2& c, int sign)
 
 // One line-parallel Stockham stage.  Specialised radices keep the R values
 // in registers; other radices use a direct sum over the table.
-template <typename T, int R, bool SH = false>
+template <typename T, int R, bool SH = false, bool P2 = true>
 __device__ __forceinline__ void stage_fixed(const typename vec2<T>::type* __restrict__ src,
                                             typename vec2<T>::type* __restrict__ dst, int n, int nl,
                                             int ls, int Ns, const typename vec2<T>::type* __restrict__ tw,
@@ -112,13 +112,9 @@ __device__ __forceinline__ void stage_fixed(const typename vec2<T>::type* __rest
     const int NR = n / R;
     const int tstep = n / (Ns * R);
     const int items = nl * NR;
-    for (int it = tid; it < items; it += nthr) {
-        const int line = it / NR;
-        const int j = it - line * NR;
+    auto butterfly = [&](int line, int j, int jm, int out0) {
         const C2* x = src + (size_t)line * ls;
         C2* y = dst + (size_t)line * ls;
-        const int jm = j % Ns;
-        const int out0 = (j / Ns) * Ns * R + jm;
         C2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -132,6 +128,26 @@ __device__ __forceinline__ void stage_fixed(const typename vec2<T>::type* __rest
         else if (R == 3) dft3<T, C2>(v[0], v[1], v[2], sign);
 #pragma unroll
         for (int r = 0; r < R; ++r) y[out0 + r * Ns] = v[r];
+    };
+    if (P2 && (n & (n - 1)) == 0 && (R & (R - 1)) == 0) {
+        // power-of-two length: NR and Ns are powers of two, so the butterfly
+        // index splits by shifts and masks instead of three runtime integer
+        // divisions per butterfly (long instruction sequences on the
+        // critical path of a stage that only a few warps execute)
+        const int lnr = __ffs(NR) - 1, lns = __ffs(Ns) - 1, lr = __ffs(R) - 1;
+        for (int it = tid; it < items; it += nthr) {
+            const int line = it >> lnr;
+            const int j = it & (NR - 1);
+            const int jm = j & (Ns - 1);
+            butterfly(line, j, jm, ((j >> lns) << (lns + lr)) + jm);
+        }
+        return;
+    }
+    for (int it = tid; it < items; it += nthr) {
+        const int line = it / NR;
+        const int j = it - line * NR;
+        const int jm = j % Ns;
+        butterfly(line, j, jm, (j / Ns) * Ns * R + jm);
     }
 }
 
@@ -169,7 +185,11 @@ __device__ void stage_generic(const typename vec2<T>::type* __restrict__ src,
 // Runs all stages on nl lines held in buf0 (scratch buf1, same shape).
 // Returns the buffer holding the result.  Must be called by every thread of
 // the block (it synchronises internally); the caller synchronises before.
-template <typename T, bool SH = false>
+// P2 = false leaves out the power-of-two index path: the persistent step
+// engine inlines four transforms, and the second loop variant in each made
+// it slower (1.20 -> 1.24 ms per 512^2 update) where the per-launch
+// transform kernels gained up to 5 %.
+template <typename T, bool SH = false, bool P2 = true>
 __device__ typename vec2<T>::type* block_fft(typename vec2<T>::type* buf0, typename vec2<T>::type* buf1,
                                              const FftDesc& d, int nl, int ls,
                                              const typename vec2<T>::type* __restrict__ tw, int sign)
@@ -183,10 +203,10 @@ __device__ typename vec2<T>::type* block_fft(typename vec2<T>::type* buf0, typen
     for (int s = 0; s < d.nf; ++s) {
         const int R = d.fac[s];
         switch (R) {
-        case 8: stage_fixed<T, 8, SH>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        case 4: stage_fixed<T, 4, SH>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        case 2: stage_fixed<T, 2, SH>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        case 3: stage_fixed<T, 3, SH>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        case 8: stage_fixed<T, 8, SH, P2>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        case 4: stage_fixed<T, 4, SH, P2>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        case 2: stage_fixed<T, 2, SH, P2>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        case 3: stage_fixed<T, 3, SH, P2>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
         default: stage_generic<T, SH>(src, dst, d.n, nl, ls, R, Ns, tw, sign, tid, nthr); break;
         }
         __syncthreads();
