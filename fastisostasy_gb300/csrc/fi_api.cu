@@ -206,7 +206,7 @@ struct fi_handle {
     bool require_tsit_graph = false;   // FI_REQUIRE_TSIT_GRAPH=1: no host-loop fallback (tests)
     // persistent cooperative RK4 engine (true stages, uniform spacing)
     bool engine_ok = false;
-    int eng_grid = 0, eng_CB = 1, eng_RA = 2;
+    int eng_grid = 0, eng_CB = 1, eng_RA = 2, eng_P2 = 0;
     size_t eng_smem = 0;
     float *xhi = nullptr, *xlo = nullptr, *wrefhi = nullptr, *wreflo = nullptr;
     unsigned long long* trace = nullptr;   // engine phase timestamps (fi_engine_trace)
@@ -818,6 +818,7 @@ template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
     g.nsteps = nsteps;
     g.CB = h->eng_CB;
     g.ra = h->eng_RA;
+    g.p2 = h->eng_P2;
     g.spy = h->spy;
     g.norm_scale = 1.0 / (double)(float)((long long)h->nx * h->ny);
     g.trace = h->trace;
@@ -1437,8 +1438,10 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
         const bool want = p.method == 3 && p.stage_mode == 1 && p.dt_method == 1 && h->uniform &&
                           !(ev && ev[0] == '1');
         if (want) {
-            int ok = mixed(h) ? engine_config<float>(h->prhs, &h->eng_grid, &h->eng_CB, &h->eng_smem, &h->eng_RA)
-                              : engine_config<double>(h->prhs, &h->eng_grid, &h->eng_CB, &h->eng_smem, &h->eng_RA);
+            int ok = mixed(h) ? engine_config<float>(h->prhs, &h->eng_grid, &h->eng_CB, &h->eng_smem, &h->eng_RA,
+                                                  &h->eng_P2)
+                              : engine_config<double>(h->prhs, &h->eng_grid, &h->eng_CB, &h->eng_smem, &h->eng_RA,
+                                                      &h->eng_P2);
             h->engine_ok = ok != 0;
             cudaGetLastError();
 #define AL2(ptr, bytes) if ((rc = dalloc(h, &(ptr), (bytes)))) return rc

@@ -131,7 +131,7 @@ template <typename T> __device__ __forceinline__ double corner_mean_dev(const T*
 // ---------------------------------------------------------------------------
 // Phase A: one item = output rows j0 .. j0+RA-1 (full width).
 // ---------------------------------------------------------------------------
-template <typename T, int RA>
+template <typename T, int RA, int FM>
 __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsigned char* smem, const EngTw<T>& tw)
 {
     typedef typename vec2<T>::type C2;
@@ -302,7 +302,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         bz[i] = fv;
     }
     __syncthreads();
-    C2* r = block_fft<T, true, false>(b0, b1, g.p.row.d, RA, hh, tw.row, -1);
+    C2* r = block_fft<T, true, FM>(b0, b1, g.p.row.d, RA, hh, tw.row, -1);
     const C2* rtw = tw.rtw;
     // column-major: the strided stores do not hold the block up, and phase B
     // then reads each spectrum column contiguously
@@ -327,7 +327,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
 // inverse column FFT.  Columns come contiguous from the column-major copy
 // phase A wrote; the result goes back row-major for the row passes of C.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, int FM>
 __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem, const EngTw<T>& tw)
 {
     typedef typename vec2<T>::type C2;
@@ -342,7 +342,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
         b0[c * ny + l] = (k <= g.p.h) ? ((const C2*)g.ST)[(size_t)k * ny + l] : mk2<T>((T)0, (T)0);
     }
     __syncthreads();
-    C2* r = block_fft<T, true, false>(b0, b1, g.p.col.d, CB, ny, tw.col, -1);
+    C2* r = block_fft<T, true, FM>(b0, b1, g.p.col.d, CB, ny, tw.col, -1);
     const T* mA = g.mA_T<T>();
     const T* mB = g.mB_T<T>();
     const int half = ny / 2 + 1;
@@ -377,7 +377,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
     }
     __syncthreads();
     C2* other = (r == b0) ? b1 : b0;
-    C2* q = block_fft<T, true, false>(r, other, g.p.col.d, CB, ny, tw.col, +1);
+    C2* q = block_fft<T, true, FM>(r, other, g.p.col.d, CB, ny, tw.col, +1);
     for (int e = tid; e < CB * ny; e += nt) {
         const int c = CB == 1 ? 0 : e % CB, l = CB == 1 ? e : e / CB;
         const int k = k0 + c;
@@ -389,7 +389,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
 // ---------------------------------------------------------------------------
 // Phase C: inverse row real-FFT of rows j0 .. j0+RC-1 -> raw (scaled 1/(nx ny)).
 // ---------------------------------------------------------------------------
-template <typename T, int RC>
+template <typename T, int RC, int FM>
 __device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem, const EngTw<T>& tw)
 {
     typedef typename vec2<T>::type C2;
@@ -414,7 +414,7 @@ __device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem
         b0[e] = z;
     }
     __syncthreads();
-    C2* r = block_fft<T, true, false>(b0, b1, g.p.row.d, RC, hh, tw.row, +1);
+    C2* r = block_fft<T, true, FM>(b0, b1, g.p.row.d, RC, hh, tw.row, +1);
     const T scale = (T)g.norm_scale;
     for (int o = tw.wh.r0, m = tw.wh.i0; o < RC; tw.wh.next(o, m)) {
         const int j = j0 + o;
@@ -435,7 +435,9 @@ __device__ __forceinline__ unsigned long long gtimer()
     return t;
 }
 
-template <typename T, int RA>
+// FM: the block-FFT index mode, FFT_POW2 when both transform lengths are
+// powers of two, else FFT_ANY
+template <typename T, int RA, int FM>
 __global__ void __launch_bounds__(EngShape<RA>::threads, EngShape<RA>::per_sm) k_engine_rk4(EngineArgs g)
 {
     constexpr int RC = RA;
@@ -497,15 +499,15 @@ __global__ void __launch_bounds__(EngShape<RA>::threads, EngShape<RA>::per_sm) k
         const bool last = step + 1 == g.nsteps || !(t + h < s_tf);
         TRACE();
         for (int stage = 0; stage < 4; ++stage) {
-            for (int it = blockIdx.x; it < na; it += gridDim.x) phase_a<T, RA>(g, it * RA, stage, h, smem, tw);
+            for (int it = blockIdx.x; it < na; it += gridDim.x) phase_a<T, RA, FM>(g, it * RA, stage, h, smem, tw);
             TRACE();
             grid.sync();
             TRACE();
-            for (int it = blockIdx.x; it < nb; it += gridDim.x) phase_b<T>(g, it * g.CB, g.CB, smem, tw);
+            for (int it = blockIdx.x; it < nb; it += gridDim.x) phase_b<T, FM>(g, it * g.CB, g.CB, smem, tw);
             TRACE();
             grid.sync();
             TRACE();
-            for (int it = blockIdx.x; it < nc; it += gridDim.x) phase_c<T, RC>(g, it * RC, (T*)g.raw[stage], smem, tw);
+            for (int it = blockIdx.x; it < nc; it += gridDim.x) phase_c<T, RC, FM>(g, it * RC, (T*)g.raw[stage], smem, tw);
             TRACE();
             grid.sync();
             TRACE();
@@ -578,7 +580,7 @@ void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s)
     k_split<<<b, 256, 0, s>>>(x, hi, lo, n);
 }
 
-template <typename T, int RA> int engine_config_shape(const Plan2D& p, int nsm, int optin, int* grid, int* CB,
+template <typename T, int RA, int FM> int engine_config_shape(const Plan2D& p, int nsm, int optin, int* grid, int* CB,
                                                      size_t* smem)
 {
     const int cb = EngShape<RA>::cb;
@@ -593,14 +595,14 @@ template <typename T, int RA> int engine_config_shape(const Plan2D& p, int nsm, 
         static size_t cur = 0;
         std::lock_guard<std::mutex> lk(mu);
         if (*smem > cur) {
-            if (cudaFuncSetAttribute(k_engine_rk4<T, RA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) !=
+            if (cudaFuncSetAttribute(k_engine_rk4<T, RA, FM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) !=
                 cudaSuccess)
                 return 0;
             cur = *smem;
         }
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T, RA>, EngShape<RA>::threads, *smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_engine_rk4<T, RA, FM>, EngShape<RA>::threads, *smem) !=
             cudaSuccess ||
         per_sm < 1)
         return 0;
@@ -620,7 +622,7 @@ template <typename T, int RA> int engine_config_shape(const Plan2D& p, int nsm, 
     return 1;
 }
 
-template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem, int* RA)
+template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem, int* RA, int* P2)
 {
     // The plain FP64 form is FP64-throughput bound; it runs faster as the
     // multi-kernel graph (full occupancy) than in the one-grid engine.
@@ -636,13 +638,21 @@ template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, siz
         const int v = atoi(ev);
         if (v == 2 || v == 4) ra = v;
     }
+    const int p2 = ((p.h & (p.h - 1)) == 0 && (p.ny & (p.ny - 1)) == 0) ? 1 : 0;
+    *P2 = p2;
     if constexpr (sizeof(T) == 4) {
-        if (ra == 4 && engine_config_shape<T, 4>(p, nsm, optin, grid, CB, smem)) {
+        auto shape = [&](int r) {
+            if (r == 4) return p2 ? engine_config_shape<T, 4, FFT_POW2>(p, nsm, optin, grid, CB, smem)
+                                  : engine_config_shape<T, 4, FFT_ANY>(p, nsm, optin, grid, CB, smem);
+            return p2 ? engine_config_shape<T, 2, FFT_POW2>(p, nsm, optin, grid, CB, smem)
+                      : engine_config_shape<T, 2, FFT_ANY>(p, nsm, optin, grid, CB, smem);
+        };
+        if (ra == 4 && shape(4)) {
             *RA = 4;
             return 1;
         }
         *RA = 2;
-        return engine_config_shape<T, 2>(p, nsm, optin, grid, CB, smem);
+        return shape(2);
     }
     return 0;
 }
@@ -662,12 +672,15 @@ template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, s
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        return g.ra == 4 ? cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 4>, g) : cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 2>, g);
+        if (g.ra == 4) return g.p2 ? cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 4, FFT_POW2>, g)
+                                   : cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 4, FFT_ANY>, g);
+        return g.p2 ? cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 2, FFT_POW2>, g)
+                    : cudaLaunchKernelEx(&cfg, k_engine_rk4<T, 2, FFT_ANY>, g);
     }
 }
 
-template int engine_config<float>(const Plan2D&, int*, int*, size_t*, int*);
-template int engine_config<double>(const Plan2D&, int*, int*, size_t*, int*);
+template int engine_config<float>(const Plan2D&, int*, int*, size_t*, int*, int*);
+template int engine_config<double>(const Plan2D&, int*, int*, size_t*, int*, int*);
 template cudaError_t engine_launch<float>(const EngineArgs&, int, size_t, cudaStream_t);
 template cudaError_t engine_launch<double>(const EngineArgs&, int, size_t, cudaStream_t);
 

@@ -33,6 +33,7 @@ struct EngineArgs {
     int nsteps;
     int CB;                          // spectrum columns per phase-B item
     int ra;                          // rows per stencil item (kernel shape: 2 or 4)
+    int p2;                          // both transform lengths are powers of two
     double spy;
     double norm_scale;               // 1 / (nx*ny*1.) as the reference normalises
     unsigned long long* trace;       // optional: %globaltimer at phase boundaries of the first step
@@ -45,9 +46,9 @@ struct EngineArgs {
 };
 
 // Grid size (co-resident blocks), phase-B column count, dynamic shared
-// memory and rows per stencil item of the engine for this transform plan;
-// 0 if it cannot run.
-template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem, int* RA);
+// memory, rows per stencil item and transform index mode of the engine for
+// this transform plan; 0 if it cannot run.
+template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem, int* RA, int* P2);
 template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, size_t smem, cudaStream_t s);
 void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s);
 

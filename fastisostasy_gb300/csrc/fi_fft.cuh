@@ -102,7 +102,13 @@ __device__ __forceinline__ void dft3(C2& a, C2& b, C2& c, int sign)
 
 // One line-parallel Stockham stage.  Specialised radices keep the R values
 // in registers; other radices use a direct sum over the table.
-template <typename T, int R, bool SH = false, bool P2 = true>
+// Index modes of a stage: FFT_ANY divides by the stage's runtime sizes,
+// FFT_AUTO takes shifts and masks when the length is a power of two and
+// divides otherwise, FFT_POW2 handles power-of-two lengths only (one loop,
+// radices 8, 4, 2: the smallest code, for the persistent step engine).
+enum { FFT_ANY = 0, FFT_AUTO = 1, FFT_POW2 = 2 };
+
+template <typename T, int R, bool SH = false, int MODE = FFT_AUTO>
 __device__ __forceinline__ void stage_fixed(const typename vec2<T>::type* __restrict__ src,
                                             typename vec2<T>::type* __restrict__ dst, int n, int nl,
                                             int ls, int Ns, const typename vec2<T>::type* __restrict__ tw,
@@ -129,7 +135,7 @@ __device__ __forceinline__ void stage_fixed(const typename vec2<T>::type* __rest
 #pragma unroll
         for (int r = 0; r < R; ++r) y[out0 + r * Ns] = v[r];
     };
-    if (P2 && (n & (n - 1)) == 0 && (R & (R - 1)) == 0) {
+    if (MODE == FFT_POW2 || (MODE == FFT_AUTO && (n & (n - 1)) == 0 && (R & (R - 1)) == 0)) {
         // power-of-two length: NR and Ns are powers of two, so the butterfly
         // index splits by shifts and masks instead of three runtime integer
         // divisions per butterfly (long instruction sequences on the
@@ -143,11 +149,13 @@ __device__ __forceinline__ void stage_fixed(const typename vec2<T>::type* __rest
         }
         return;
     }
-    for (int it = tid; it < items; it += nthr) {
-        const int line = it / NR;
-        const int j = it - line * NR;
-        const int jm = j % Ns;
-        butterfly(line, j, jm, (j / Ns) * Ns * R + jm);
+    if constexpr (MODE != FFT_POW2) {
+        for (int it = tid; it < items; it += nthr) {
+            const int line = it / NR;
+            const int j = it - line * NR;
+            const int jm = j % Ns;
+            butterfly(line, j, jm, (j / Ns) * Ns * R + jm);
+        }
     }
 }
 
@@ -185,11 +193,11 @@ __device__ void stage_generic(const typename vec2<T>::type* __restrict__ src,
 // Runs all stages on nl lines held in buf0 (scratch buf1, same shape).
 // Returns the buffer holding the result.  Must be called by every thread of
 // the block (it synchronises internally); the caller synchronises before.
-// P2 = false leaves out the power-of-two index path: the persistent step
-// engine inlines four transforms, and the second loop variant in each made
-// it slower (1.20 -> 1.24 ms per 512^2 update) where the per-launch
-// transform kernels gained up to 5 %.
-template <typename T, bool SH = false, bool P2 = true>
+// MODE: see stage_fixed.  The persistent step engine inlines four
+// transforms; carrying both loop forms in each made it slower (1.20 -> 1.24
+// ms per 512^2 update) where the per-launch transform kernels gained up to
+// 5 %, so the engine takes FFT_POW2 or FFT_ANY by its plan.
+template <typename T, bool SH = false, int MODE = FFT_AUTO>
 __device__ typename vec2<T>::type* block_fft(typename vec2<T>::type* buf0, typename vec2<T>::type* buf1,
                                              const FftDesc& d, int nl, int ls,
                                              const typename vec2<T>::type* __restrict__ tw, int sign)
@@ -203,11 +211,15 @@ __device__ typename vec2<T>::type* block_fft(typename vec2<T>::type* buf0, typen
     for (int s = 0; s < d.nf; ++s) {
         const int R = d.fac[s];
         switch (R) {
-        case 8: stage_fixed<T, 8, SH, P2>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        case 4: stage_fixed<T, 4, SH, P2>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        case 2: stage_fixed<T, 2, SH, P2>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        case 3: stage_fixed<T, 3, SH, P2>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
-        default: stage_generic<T, SH>(src, dst, d.n, nl, ls, R, Ns, tw, sign, tid, nthr); break;
+        case 8: stage_fixed<T, 8, SH, MODE>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        case 4: stage_fixed<T, 4, SH, MODE>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        case 2: stage_fixed<T, 2, SH, MODE>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr); break;
+        case 3:
+            if constexpr (MODE != FFT_POW2) stage_fixed<T, 3, SH, MODE>(src, dst, d.n, nl, ls, Ns, tw, sign, tid, nthr);
+            break;
+        default:
+            if constexpr (MODE != FFT_POW2) stage_generic<T, SH>(src, dst, d.n, nl, ls, R, Ns, tw, sign, tid, nthr);
+            break;
         }
         __syncthreads();
         C2* t = src;
