@@ -296,6 +296,38 @@ def test_step_engine_matches_kernel_sequence(precision, n, monkeypatch):
     assert rel(res[1], res[0]) <= (1e-12 if precision == 0 else 1e-6)
 
 
+def test_step_engine_shapes_agree_bit_for_bit(monkeypatch):
+    """512^2 mixed: the four-row engine shape (one 1024-thread block per SM,
+    power-of-two transforms) and the two-row shape run the same arithmetic
+    per cell, so they agree bit for bit; both match the kernel sequence
+    within the mixed-form bound."""
+    wl = W.config2(n=512, L=3000e3 * 2, dt=1.0, stage_mode=1)
+    res = {}
+    for key, env in (("ra4", {}), ("ra2", {"FI_ENGINE_RA": "2"}), ("seq", {"FI_NO_ENGINE": "1"})):
+        monkeypatch.delenv("FI_ENGINE_RA", raising=False)
+        monkeypatch.delenv("FI_NO_ENGINE", raising=False)
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=1)
+        assert dom.ny <= 600, "the step engine runs only where its stencil phase fits one wave"
+        f = wl.padded_fields(dom.nx, dom.ny)
+        if f:
+            dom.set_fields(**f)
+        m = wl.bsl.get("method", 0)
+        bg = gpu_bsl(m, wl.bsl.get("bsl_init", 0.0), wl.bsl.get("A_ocean_pd", 3.625e14))
+        dom.init_state(wl.z_bed, wl.H_at(0.0), 0.0, bg)
+        t = 0.0
+        for _ in range(3):
+            t += wl.dtt
+            _lib.load().fi_bsl_update(bg, t)
+            dom.update(wl.H_at(t), t, bg)
+        res[key] = dom.field("w")
+        dom.close()
+    assert np.abs(res["ra4"]).max() > 0
+    assert np.array_equal(res["ra4"], res["ra2"])
+    assert rel(res["ra4"], res["seq"]) <= 1e-6
+
+
 def test_device_analytical_disk():
     """fi_elva_disk (the analytical ELVA disc evaluated on the device) against
     the oracle's evaluation of the same integral, then used as the validator
