@@ -34,18 +34,6 @@ template <typename T> __device__ __forceinline__ const typename vec2<T>::type* r
 template <> __device__ __forceinline__ const double2* rtwp<double>(const Plan2D& p) { return p.rtw64; }
 template <> __device__ __forceinline__ const float2* rtwp<float>(const Plan2D& p) { return p.rtw32; }
 
-static int g_smem_optin = -1;
-static int smem_optin()
-{
-    if (g_smem_optin < 0) {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        g_smem_optin = v;
-    }
-    return g_smem_optin;
-}
-
 // Raise a kernel's dynamic shared-memory limit when a larger launch needs it
 // (the limit belongs to the kernel and is shared by every handle, so it only
 // ever grows).
