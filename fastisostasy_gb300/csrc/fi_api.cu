@@ -68,7 +68,7 @@ private:
     HostPool()
     {
         unsigned hw = std::thread::hardware_concurrency();
-        const int nw = (int)std::min<unsigned>(hw > 1 ? hw - 1 : 0, 7u);
+        const int nw = (int)std::min<unsigned>(hw > 1 ? hw - 1 : 0, 15u);
         for (int i = 0; i < nw; ++i)
             workers_.emplace_back([this] {
                 unsigned long long seen = 0;
@@ -1704,7 +1704,7 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
     const size_t ni = (size_t)h->nx_ice * h->ny_ice;
     int rc;
     if (ni < (1u << 16)) memcpy(h->hpin, H_ice, ni * 8);
-    else pool_copy(h->hpin, H_ice, ni * 8, 4);
+    else pool_copy(h->hpin, H_ice, ni * 8, 8);
     CK(cudaMemcpyAsync(h->dH, h->hpin, ni * 8, cudaMemcpyHostToDevice, h->s));
     enqueue_args(h, time, bsl, true);
     if ((rc = update_any(h, h->dH, time, true))) return rc;
@@ -1716,24 +1716,30 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
     rc = read_status(h, &hc);
     bsl->bsl_now = hc.bsl;
     if (out) {
-        // the staged fields into the caller's arrays: one host thread per
-        // slice of fields (a single core copies a few GB/s; the fields are
-        // ~100 B per cell)
+        // the staged fields into the caller's arrays, each field in kParts
+        // slices spread over the host pool (a single core copies a few GB/s;
+        // the fields are ~100 B per cell, and 11 whole-field tasks left the
+        // pool's threads waiting on the last few)
+        constexpr int kParts = 4;
         double* dst[8] = {out->z_bed, out->z_ss, out->dz_ss, out->w, out->we, out->dwdt, out->canom_full, out->Hice};
         uint8_t* mdst[3] = {out->maskocean, out->maskgrounded, out->maskcontinent};
-        auto copy_field = [&](int f) {
+        const size_t chunk = (ni + kParts - 1) / kParts;
+        auto copy_part = [&](int t) {
+            const int f = t / kParts;
+            const size_t a = (size_t)(t % kParts) * chunk, b = std::min(ni, a + chunk);
+            if (a >= b) return;
             if (f < 8) {
-                if (dst[f]) memcpy(dst[f], h->hpin + (size_t)f * ni, ni * 8);
+                if (dst[f]) memcpy(dst[f] + a, h->hpin + (size_t)f * ni + a, (b - a) * 8);
             } else if (mdst[f - 8]) {
                 const double* src = h->hpin + (size_t)f * ni;
                 uint8_t* m = mdst[f - 8];
-                for (size_t e = 0; e < ni; ++e) m[e] = src[e] != 0.0;
+                for (size_t e = a; e < b; ++e) m[e] = src[e] != 0.0;
             }
         };
         if (ni < (1u << 16)) {
-            for (int f = 0; f < 11; ++f) copy_field(f);
+            for (int t = 0; t < 11 * kParts; ++t) copy_part(t);
         } else {
-            HostPool::get().run(11, copy_field);
+            HostPool::get().run(11 * kParts, copy_part);
         }
     }
     return rc;
