@@ -223,6 +223,11 @@ struct fi_handle {
     std::vector<void*> allocs;
     std::string err;
     cudaError_t launch_err = cudaSuccess;   // a launch whose status the enqueue path cannot return
+    // fi_update's output path: one event per staged field and a page-locked
+    // copy of the control block, so the host unpacks a field while the
+    // later ones are still being copied
+    std::vector<cudaEvent_t> ev_field;
+    Ctl* hctl = nullptr;
     // host copies of the static fields
     std::vector<double> K, kappa, R, D, He, eta_eff, GE, GN, GV, xc, yc;
     std::vector<uint8_t> mact;
@@ -1128,10 +1133,8 @@ void enqueue_args(fi_handle* h, double tf, const fi_bsl* b, bool write_bsl)
     h->launches += 1;
 }
 
-int read_status(fi_handle* h, Ctl* hc)
+int decode_status(fi_handle* h, const Ctl* hc)
 {
-    CK(cudaMemcpyAsync(hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
-    CK(cudaStreamSynchronize(h->s));
     switch (hc->status) {
     case ST_OK: return FI_OK;
     case ST_NAN: return fail(h, FI_E_NAN, "isos_update: NaNs detected");
@@ -1140,6 +1143,13 @@ int read_status(fi_handle* h, Ctl* hc)
     case ST_STEP: return fail(h, FI_E_STEP, "adaptive step rejected too often");
     default: return fail(h, FI_E_CUDA, "unknown device status %d", hc->status);
     }
+}
+
+int read_status(fi_handle* h, Ctl* hc)
+{
+    CK(cudaMemcpyAsync(hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return decode_status(h, hc);
 }
 
 }  // namespace
@@ -1486,6 +1496,9 @@ int fi_destroy(fi_handle* h)
         for (void* p : h->allocs) cudaFree(p);
     }
     if (h->hpin) cudaFreeHost(h->hpin);
+    if (h->hctl) cudaFreeHost(h->hctl);
+    for (cudaEvent_t e : h->ev_field)
+        if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : h->prof_ev) cudaEventDestroy(e);
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
     if (h->s_out) {
@@ -1708,13 +1721,34 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
     CK(cudaMemcpyAsync(h->dH, h->hpin, ni * 8, cudaMemcpyHostToDevice, h->s));
     enqueue_args(h, time, bsl, true);
     if ((rc = update_any(h, h->dH, time, true))) return rc;
+    const bool piped = out && ni >= (1u << 16);
+    if (piped && h->ev_field.empty()) {
+        h->ev_field.resize(11, nullptr);
+        for (auto& e : h->ev_field) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    if (piped && !h->hctl) CK(cudaMallocHost(&h->hctl, sizeof(Ctl)));
     if (out) {
         gather(h->gsrc, h->gmsrc, 8, 3, h->d, h->dpack, h->s);
-        CK(cudaMemcpyAsync(h->hpin, h->dpack, ni * 11 * 8, cudaMemcpyDeviceToHost, h->s));
+        if (piped) {
+            // one copy per field, each followed by its event
+            for (int f = 0; f < 11; ++f) {
+                CK(cudaMemcpyAsync(h->hpin + (size_t)f * ni, h->dpack + (size_t)f * ni, ni * 8,
+                                   cudaMemcpyDeviceToHost, h->s));
+                CK(cudaEventRecord(h->ev_field[f], h->s));
+            }
+        } else {
+            CK(cudaMemcpyAsync(h->hpin, h->dpack, ni * 11 * 8, cudaMemcpyDeviceToHost, h->s));
+        }
     }
     Ctl hc;
-    rc = read_status(h, &hc);
-    bsl->bsl_now = hc.bsl;
+    if (piped) {
+        // the control block last, into page-locked memory: the call does not
+        // wait here, and the unpack below follows the field copies
+        CK(cudaMemcpyAsync(h->hctl, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+    } else {
+        rc = read_status(h, &hc);
+        bsl->bsl_now = hc.bsl;
+    }
     if (out) {
         // the staged fields into the caller's arrays, each field in kParts
         // slices spread over the host pool (a single core copies a few GB/s;
@@ -1728,6 +1762,7 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
             const int f = t / kParts;
             const size_t a = (size_t)(t % kParts) * chunk, b = std::min(ni, a + chunk);
             if (a >= b) return;
+            if (piped) cudaEventSynchronize(h->ev_field[f]);
             if (f < 8) {
                 if (dst[f]) memcpy(dst[f] + a, h->hpin + (size_t)f * ni + a, (b - a) * 8);
             } else if (mdst[f - 8]) {
@@ -1741,6 +1776,12 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
         } else {
             HostPool::get().run(11 * kParts, copy_part);
         }
+    }
+    if (piped) {
+        CK(cudaStreamSynchronize(h->s));
+        hc = *h->hctl;
+        rc = decode_status(h, &hc);
+        bsl->bsl_now = hc.bsl;
     }
     return rc;
 }
