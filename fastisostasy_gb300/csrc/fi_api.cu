@@ -1727,16 +1727,24 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
         for (auto& e : h->ev_field) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     if (piped && !h->hctl) CK(cudaMallocHost(&h->hctl, sizeof(Ctl)));
+    // piped: the 8 double fields, then the 3 masks as bytes
+    uint8_t* const dmask = (uint8_t*)(h->dpack + (size_t)8 * ni);
+    uint8_t* const hmask = (uint8_t*)(h->hpin + (size_t)8 * ni);
     if (out) {
-        gather(h->gsrc, h->gmsrc, 8, 3, h->d, h->dpack, h->s);
         if (piped) {
+            gather_bytes(h->gsrc, h->gmsrc, 8, 3, h->d, h->dpack, dmask, h->s);
             // one copy per field, each followed by its event
             for (int f = 0; f < 11; ++f) {
-                CK(cudaMemcpyAsync(h->hpin + (size_t)f * ni, h->dpack + (size_t)f * ni, ni * 8,
-                                   cudaMemcpyDeviceToHost, h->s));
+                if (f < 8)
+                    CK(cudaMemcpyAsync(h->hpin + (size_t)f * ni, h->dpack + (size_t)f * ni, ni * 8,
+                                       cudaMemcpyDeviceToHost, h->s));
+                else
+                    CK(cudaMemcpyAsync(hmask + (size_t)(f - 8) * ni, dmask + (size_t)(f - 8) * ni, ni,
+                                       cudaMemcpyDeviceToHost, h->s));
                 CK(cudaEventRecord(h->ev_field[f], h->s));
             }
         } else {
+            gather(h->gsrc, h->gmsrc, 8, 3, h->d, h->dpack, h->s);
             CK(cudaMemcpyAsync(h->hpin, h->dpack, ni * 11 * 8, cudaMemcpyDeviceToHost, h->s));
         }
     }
@@ -1766,9 +1774,13 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
             if (f < 8) {
                 if (dst[f]) memcpy(dst[f] + a, h->hpin + (size_t)f * ni + a, (b - a) * 8);
             } else if (mdst[f - 8]) {
-                const double* src = h->hpin + (size_t)f * ni;
-                uint8_t* m = mdst[f - 8];
-                for (size_t e = a; e < b; ++e) m[e] = src[e] != 0.0;
+                if (piped) {
+                    memcpy(mdst[f - 8] + a, hmask + (size_t)(f - 8) * ni + a, b - a);
+                } else {
+                    const double* src = h->hpin + (size_t)f * ni;
+                    uint8_t* m = mdst[f - 8];
+                    for (size_t e = a; e < b; ++e) m[e] = src[e] != 0.0;
+                }
             }
         };
         if (ni < (1u << 16)) {

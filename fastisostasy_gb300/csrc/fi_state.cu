@@ -923,6 +923,24 @@ k_gather(const double* const* __restrict__ src, const uint8_t* const* __restrict
     }
 }
 
+// The same crop with the masks kept as bytes: nf double fields into out, nm
+// byte masks into mout (fi_update's host copy, a quarter fewer bytes).
+__global__ void __launch_bounds__(NT)
+k_gather_bytes(const double* const* __restrict__ src, const uint8_t* const* __restrict__ msrc, int nf, int nm, Dom d,
+               double* __restrict__ out, uint8_t* __restrict__ mout)
+{
+    const size_t nc = (size_t)d.nxi * d.nyi;
+    const size_t tot = nc * (nf + nm);
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < tot; e += (size_t)gridDim.x * NT) {
+        const int f = (int)(e / nc);
+        const size_t r = e - (size_t)f * nc;
+        const int i = (int)(r % d.nxi), j = (int)(r / d.nxi);
+        const size_t g = (size_t)(j + d.j0) * d.nx + (i + d.i0);
+        if (f < nf) out[e] = src[f][g];
+        else mout[(size_t)(f - nf) * nc + r] = msrc[f - nf][g];
+    }
+}
+
 // Scatter an ice-grid field into the padded grid: background outside the crop.
 __global__ void __launch_bounds__(NT)
 k_out2in(double* __restrict__ dst, const double* __restrict__ src, Dom d, double background, int keep_outside)
@@ -1403,6 +1421,11 @@ void gather(const double* const* src, const uint8_t* const* msrc, int nf, int nm
             cudaStream_t s)
 {
     k_gather<<<grid_for((size_t)d.nxi * d.nyi * (nf + nm)), NT, 0, s>>>(src, msrc, nf, nm, d, out);
+}
+void gather_bytes(const double* const* src, const uint8_t* const* msrc, int nf, int nm, const Dom& d, double* out,
+                  uint8_t* mout, cudaStream_t s)
+{
+    k_gather_bytes<<<grid_for((size_t)d.nxi * d.nyi * (nf + nm)), NT, 0, s>>>(src, msrc, nf, nm, d, out, mout);
 }
 void out2in(double* dst, const double* src, const Dom& d, double background, int keep_outside, cudaStream_t s)
 {

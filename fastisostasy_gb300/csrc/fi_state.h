@@ -79,6 +79,9 @@ void ts_commit_pair(const Dom& d, const float* raw, cudaStream_t s);
 template <typename T> void upd_end(const Dom& d, const T* raw_last, int have_rhs, cudaStream_t s);
 void gather(const double* const* src, const uint8_t* const* msrc, int nf, int nm, const Dom& d, double* out,
             cudaStream_t s);
+// the same with the masks as bytes into mout (nm * nxi * nyi bytes)
+void gather_bytes(const double* const* src, const uint8_t* const* msrc, int nf, int nm, const Dom& d, double* out,
+                  uint8_t* mout, cudaStream_t s);
 void out2in(double* dst, const double* src, const Dom& d, double background, int keep_outside, cudaStream_t s);
 void state_diag(double* z_ss, const double* zss_base, const double* dz_ss, double bsl, const double* z_bed,
                 const double* Hice, double* Haf, uint8_t* mo, uint8_t* mg, uint8_t* mc, size_t n,
