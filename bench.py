@@ -15,8 +15,8 @@ Workload (one "step" = one coupling step, i.e. one isos_update call):
 device; `e2e` times the public fi_update call with host arrays (ice load in,
 every isos%out field back).  L2 is flushed (256 MiB write) between timed
 steps, outside the timed events.  `--impl reference` times the CPU
-restatement of the reference (reference integrator semantics) on all host
-cores instead.
+restatement of the reference (the oracle) on the same workload and
+integrator (RK4 with true stages) on all host cores instead.
 """
 import argparse
 import json
@@ -270,10 +270,43 @@ def run_e2e(dom, wl, b, steps, warmup, flush, t0):
     return secs, h2d, d2h
 
 
+def cpu_model():
+    """The host CPU's model name and core count (lscpu, else /proc/cpuinfo)."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                name = line.split(":", 1)[1].strip()
+                break
+        if name is None:
+            for line in out.splitlines():
+                if line.lower().startswith("vendor id"):
+                    name = line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    if name is None:
+        try:
+            with open("/proc/cpuinfo") as fh:
+                for line in fh:
+                    if line.lower().startswith(("model name", "cpu part")):
+                        name = line.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    import platform
+    return {"model": name or "unknown", "arch": platform.machine(), "host_cores": os.cpu_count()}
+
+
 def cpu_baseline(samples=8, threads=1, stage_mode=1):
-    """The oracle (C restatement) on the same workload, `samples` coupling steps."""
+    """The oracle (C restatement) on the same workload, `samples` coupling
+    steps, convolving at the smallest 2/3/5/7-smooth size >= 2n-1 (1024 for
+    the reference's 1023 = 3*11*31: the same linear convolution at the cost
+    of an optimised FFT library, where this file's FFT would evaluate the
+    radix-11 and radix-31 stages as direct sums)."""
     from oracle import oracle as O
     O.set_threads(threads)
+    O.set_smooth_convolution(True)
     wl = workload(stage_mode)
     m = O.Model(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
     m.set_fields(**wl.padded_fields(m.nx, m.ny))
@@ -290,7 +323,76 @@ def cpu_baseline(samples=8, threads=1, stage_mode=1):
             raise RuntimeError("oracle update failed %d" % rc)
     secs = time.perf_counter() - a
     m.close()
+    O.set_smooth_convolution(False)
     return samples * wl.dtt / 1000.0 / secs, secs
+
+
+def oracle_leg(headline_updates=3):
+    """err_vs_oracle: both GPU forms against the FP64 oracle (all host
+    cores) from the same start, on the headline workload (512^2, RK4 true
+    stages, `headline_updates` coupling steps) and on configuration 3
+    (512 x 1024, interactive sea level, reference-compatible Tsit5, one
+    coupling step of a few hundred attempts).  max and RMS of |u_gpu -
+    u_oracle| / max|u_oracle| for the displacement w, and the count of mask
+    cells that differ."""
+    from fastisostasy_gb300 import workloads as W
+    from fastisostasy_gb300.isostasy import Domain
+    from fastisostasy_gb300 import _lib
+    from oracle import oracle as O
+    O.set_threads(os.cpu_count() or 1)
+    O.set_reuse_frozen(True)   # bit-identical: the frozen RHS evaluated once per attempt
+    masks = ("maskocean", "maskgrounded", "maskcontinent")
+
+    def run(wl, n_up):
+        o = O.Model(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
+        f = wl.padded_fields(o.nx, o.ny)
+        if f:
+            o.set_fields(**f)
+        bo = O.make_bsl()
+        o.init_state(wl.z_bed, wl.H_at(0.0), 0.0, bo)
+        a = time.perf_counter()
+        t = 0.0
+        for _ in range(n_up):
+            t += wl.dtt
+            rc = o.update(wl.H_at(t), t, bo)
+            if rc:
+                raise RuntimeError("oracle update failed %d" % rc)
+        o_secs = time.perf_counter() - a
+        ref = {k: o.field(k) for k in ("w",) + masks}
+        sc_o = o.scalars()
+        o.close()
+        out = {"oracle_s": o_secs, "updates": n_up}
+        for prec, key in ((0, "fp64"), (1, "mixed")):
+            d = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=prec)
+            if f:
+                d.set_fields(**f)
+            b = _lib.FiBsl()
+            b.method, b.constant_ocean_surface = 0, 1
+            b.A_ocean_pd = b.A_ocean_now = 3.625e14
+            d.init_state(wl.z_bed, wl.H_at(0.0), 0.0, b)
+            t = 0.0
+            for _ in range(n_up):
+                t += wl.dtt
+                d.update(wl.H_at(t), t, b)
+            w = d.field("w")
+            sc = d.scalars()
+            wmax = max(np.abs(ref["w"]).max(), 1e-300)
+            out[key] = {"max_rel": float(np.abs(w - ref["w"]).max() / wmax),
+                        "rms_rel": float(np.sqrt(np.mean((w - ref["w"]) ** 2)) / wmax),
+                        "mask_mismatch": int(sum(np.sum(d.field(m) != ref[m]) for m in masks)),
+                        "same_step_sequence": bool(sc["n_accept"] == sc_o["n_accept"]
+                                                   and sc["n_reject"] == sc_o["n_reject"])}
+            d.close()
+        out["attempts"] = {"accept": sc_o["n_accept"], "reject": sc_o["n_reject"]}
+        return out
+
+    try:
+        res = {"headline": run(workload(1), headline_updates), "config3": run(W.config3(), 1)}
+    finally:
+        O.set_reuse_frozen(False)
+    res["note"] = ("FP64 oracle on %d host threads; w after the stated coupling steps from the same start"
+                   % (os.cpu_count() or 1))
+    return res
 
 
 def ensemble_leg(n_members=256, n_updates=10):
@@ -669,7 +771,8 @@ def reference_arm(args):
     threads = os.cpu_count() or 1
     from oracle import oracle as O
     O.set_threads(threads)
-    wl = workload(stage_mode=0)
+    O.set_smooth_convolution(True)
+    wl = workload(stage_mode=1)
     m = O.Model(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
     m.set_fields(**wl.padded_fields(m.nx, m.ny))
     bo = O.make_bsl()
@@ -688,10 +791,10 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": val, "unit": "kyr/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "l2": "n/a (CPU)", "integrator": "reference semantics (frozen RHS, 4 RHS/RK4 step)"},
-        "cpu_baseline": {"value": val, "unit": "kyr/s", "cores": threads, "kind": "port",
-                         "sample": "%d coupling steps (%d x 40 RHS + 2 convolutions at 1023^2), OpenMP %d threads"
-                                   % (args.steps, args.steps, threads)},
+        "config": {"workload": WORKLOAD, "form": "FP64", "stage_mode": "true stages", "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": val, "unit": "kyr/s", "cores": threads, "kind": "port", "cpu": cpu_model(),
+                         "sample": "%d coupling steps (%d x 40 RHS + 2 convolutions at 1024^2, the smallest "
+                                   "smooth size >= 2n-1), OpenMP %d threads" % (args.steps, args.steps, threads)},
         "e2e": {"value": val, "unit": "kyr/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -709,11 +812,12 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
+    ap.add_argument("--no-oracle", action="store_true", help="skip the err_vs_oracle leg")
     ap.add_argument("--ensemble-members", type=int, default=256)
     ap.add_argument("--ensemble-updates", type=int, default=10)
     ap.add_argument("--scale-sizes", default="1024,2048", help="grid sizes of --only scale")
     ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--only", choices=["ensemble", "serve", "configs", "scale"],
+    ap.add_argument("--only", choices=["ensemble", "serve", "configs", "scale", "oracle"],
                     help="run one secondary leg alone and print its JSON (for profiling), not a bench line")
     ap.add_argument("--lean", action="store_true",
                     help="mixed form only, no profile / e2e / CPU legs (for ncu captures); prints the timing only")
@@ -747,6 +851,9 @@ def main():
         return 0
     if args.only == "serve":
         print(json.dumps({"serve": serve_leg(n_req=args.serve_requests)}))
+        return 0
+    if args.only == "oracle":
+        print(json.dumps({"err_vs_oracle": oracle_leg()}))
         return 0
     if args.only == "configs":
         print(json.dumps({"configs": configs_leg()}))
@@ -798,11 +905,14 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, secs = cpu_baseline(args.cpu_samples, threads=1, stage_mode=1)
-        cpu = {"value": v, "unit": "kyr/s", "cores": 1, "kind": "port",
-               "sample": "%d coupling steps of the same workload (%d x 40 RHS + 2 convolutions at 1023^2), "
-                         "%.1f s, 1 thread (the reference is serial)" % (args.cpu_samples, args.cpu_samples, secs)}
+        cpu = {"value": v, "unit": "kyr/s", "cores": 1, "kind": "port", "cpu": cpu_model(),
+               "sample": "%d coupling steps of the same workload (%d x 40 RHS + 2 convolutions at 1024^2, the "
+                         "smallest smooth size >= 2n-1), %.1f s, 1 thread (the reference is serial)"
+                         % (args.cpu_samples, args.cpu_samples, secs)}
 
-    ens = serve = cfgs = None
+    ens = serve = cfgs = orc = None
+    if rank == 0 and not args.no_oracle:
+        orc = oracle_leg()
     if not args.no_configs:
         cfgs = configs_leg()
     if not args.no_ensemble:
@@ -821,6 +931,7 @@ def main():
             "mixed_over_fp64": r64["ms"] / r32["ms"],
             "err_vs_fp64": {"max_rel": err_max, "rms_rel": err_rms,
                             "after_steps": args.warmup + args.steps},
+            "err_vs_oracle": orc,
             "cell_steps_per_s": ws * N_CELLS * N_CELLS * (DTT / DT) / (r32["ms"] / 1000.0),
             "e2e": {"value": kyr(1000.0 * e2e_secs / args.steps), "unit": "kyr/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

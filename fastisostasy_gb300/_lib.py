@@ -9,12 +9,12 @@ import os
 from . import build as _build
 
 FI_OK, FI_E_NAN, FI_E_LARGE, FI_E_STEP, FI_E_OOM, FI_E_CONFIG, FI_E_CUDA, FI_E_TIMEOUT, FI_E_ARG, FI_E_STATE, \
-    FI_E_SIZE = range(11)
+    FI_E_SIZE, FI_E_CANCELLED = range(12)
 FI_STATIC_MAX_N = 256
 FI_PREC_FP64, FI_PREC_MIXED = 0, 1
 
 ERRORS = {1: "FI_E_NAN", 2: "FI_E_LARGE", 3: "FI_E_STEP", 4: "FI_E_OOM", 5: "FI_E_CONFIG", 6: "FI_E_CUDA",
-          7: "FI_E_TIMEOUT", 8: "FI_E_ARG", 9: "FI_E_STATE", 10: "FI_E_SIZE"}
+          7: "FI_E_TIMEOUT", 8: "FI_E_ARG", 9: "FI_E_STATE", 10: "FI_E_SIZE", 11: "FI_E_CANCELLED"}
 
 FIELDS = {
     "z_bed": 0, "dwdt": 1, "w": 2, "we": 3, "Haf": 4, "Hice": 5, "z_ss": 6, "dz_ss": 7,
@@ -33,7 +33,7 @@ EXPORTS = ["fi_create", "fi_destroy", "fi_dims", "fi_set_fields", "fi_set_kernel
            "fi_serve_result", "fi_serve_clock", "fi_serve_destroy", "fi_batch_update", "fi_batch_synchronize",
            "fi_batch_create", "fi_batch_step", "fi_batch_wait", "fi_batch_destroy", "fi_elva_disk",
            "fi_batch_set_priority", "fi_set_rheology", "fi_output_bytes", "fi_output_async",
-           "fi_output_wait", "fi_batch_autotune", "fi_set_stream"]
+           "fi_output_wait", "fi_batch_autotune", "fi_set_stream", "fi_set_max_rejections", "fi_serve_cancel"]
 
 PROFILE_KERNELS = ["flexure", "rows_fwd", "cols_hartley", "rows_inv", "conv_rows_fwd", "conv_cols",
                    "conv_rows_inv", "rk_stage", "rk_final", "upd_begin", "upd_masks", "upd_litho",
@@ -132,14 +132,15 @@ def load(build_if_missing: bool = True):
     L.fi_update.argtypes = [H, _dp, C.c_double, C.POINTER(FiBsl), C.POINTER(FiOut)]
     L.fi_update_async.argtypes = [H, C.c_void_p, C.c_double, C.POINTER(FiBsl)]
     L.fi_synchronize.argtypes = [H]
+    L.fi_set_max_rejections.argtypes = [H, C.c_int64]
     L.fi_bsl_update.argtypes = [C.POINTER(FiBsl), C.c_double]
     L.fi_get_field.argtypes = [H, C.c_int, _dp]
     L.fi_get_scalars.argtypes = [H, _dp]
     L.fi_lvelva.argtypes = [H, _dp, _dp, _dp]
     L.fi_convolve.argtypes = [H, C.c_int, _dp, _dp]
     _v = C.c_void_p
-    L.fi_lvelva_static.argtypes = [_v, _v, _v, _v, _v, _v, _v, C.c_int, C.c_int, C.c_double, C.c_double,
-                                   C.c_double, C.c_double, C.c_double, _v, _v]
+    L.fi_lvelva_static.argtypes = [_v, _v, _v, _v, _v, _v, _v, _v, _v, C.c_int, C.c_int, C.c_double,
+                                   C.c_double, C.c_double, C.c_double, C.c_double, _v, _v]
     L.fi_state_size.argtypes = [H]
     L.fi_state_size.restype = C.c_size_t
     L.fi_state_export.argtypes = [H, _dp]
@@ -161,6 +162,7 @@ def load(build_if_missing: bool = True):
     L.fi_serve_clock.argtypes = [H]
     L.fi_serve_clock.restype = C.c_double
     L.fi_serve_destroy.argtypes = [H]
+    L.fi_serve_cancel.argtypes = [H, C.c_uint64]
     L.fi_batch_update.argtypes = [C.POINTER(H), C.c_int, C.c_double, C.POINTER(FiBsl)]
     L.fi_batch_synchronize.argtypes = [C.POINTER(H), C.c_int, C.POINTER(C.c_int32)]
     L.fi_batch_create.argtypes = [C.POINTER(H), C.c_int, C.POINTER(H)]

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -835,6 +836,7 @@ template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
 }
 
 const int kMaxAttempts = 10000000;
+const long long kDefaultMaxReject = 1000000;   // rejections per update (fi_set_max_rejections)
 
 // One attempt of Tsitouras 5(4) with true stages (the Dormand-Prince 5(4)
 // pair, FSAL), decided on the device: k_0 = f(x) unless an accepted attempt
@@ -854,7 +856,7 @@ template <typename T> void tsit_true_attempt(fi_handle* h, cudaGraphConditionalH
         rhs<T>(h, y, h->w_ref, (T*)h->raw[i], &h->ctl->active);
     }
     PROF(h, K_TS, dp_err<T>(h->d, R, p.atol, p.rtol, h->s));
-    PROF(h, K_TS, ts_err<T>(h->d, (const T*)h->raw[0], p.q, p.dt_max, 100000, h->s));
+    PROF(h, K_TS, ts_err<T>(h->d, (const T*)h->raw[0], p.q, p.dt_max, h->s));
     PROF(h, K_TS, ts_commit<T>(h->d, (const T*)h->raw[0], h->s));
     PROF(h, K_TS, fsal_copy<T>(h->ctl, (T*)h->raw[0], (const T*)h->raw[6], h->n, h->s));
     ts_attempt_end(h->ctl, loop, h->s, 1, more_out);
@@ -893,12 +895,12 @@ template <typename T> int integrate_tsit(fi_handle* h, double tf, int* have_rhs,
         PROF(h, K_CONTROL, step_begin(h->ctl, 2, h->s));
         if (need_rhs) { rhs<T>(h, h->d.w, nullptr, r0, nullptr, h->d.whi, h->d.wlo); *have_rhs = 1; }
         if (sizeof(T) == 4 && h->d.whi) {
-            PROF(h, K_TS, ts_fused(h->d, (const float*)r0, p.atol, p.rtol, p.q, p.dt_max, 100000, h->s));
+            PROF(h, K_TS, ts_fused(h->d, (const float*)r0, p.atol, p.rtol, p.q, p.dt_max, h->s));
             PROF(h, K_TS, ts_commit_pair(h->d, (const float*)r0, h->s));
             h->launches += 3;
         } else {
             PROF(h, K_TS, ts_max<T>(h->d, r0, p.atol, p.rtol, h->s));
-            PROF(h, K_TS, ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s));
+            PROF(h, K_TS, ts_err<T>(h->d, r0, p.q, p.dt_max, h->s));
             PROF(h, K_TS, ts_commit<T>(h->d, r0, h->s));
             h->launches += 4;
         }
@@ -948,12 +950,12 @@ template <typename T> int enqueue_tsit_loop(fi_handle* h)
         ts_attempt_begin(h->ctl, kMaxAttempts, h->s);
         rhs<T>(h, h->d.w, nullptr, r0, &h->ctl->need_rhs, h->d.whi, h->d.wlo);
         if (sizeof(T) == 4 && h->d.whi) {
-            ts_fused(h->d, (const float*)r0, p.atol, p.rtol, p.q, p.dt_max, 100000, h->s);
+            ts_fused(h->d, (const float*)r0, p.atol, p.rtol, p.q, p.dt_max, h->s);
             ts_commit_pair(h->d, (const float*)r0, h->s);
             h->launches -= 1;
         } else {
             ts_max<T>(h->d, r0, p.atol, p.rtol, h->s);
-            ts_err<T>(h->d, r0, p.q, p.dt_max, 100000, h->s);
+            ts_err<T>(h->d, r0, p.q, p.dt_max, h->s);
             ts_commit<T>(h->d, r0, h->s);
         }
         ts_attempt_end(h->ctl, loop, h->s);
@@ -1347,13 +1349,6 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     AL(d.m_ocean, n); AL(d.m_grounded, n); AL(d.m_cont, n);
     AL(h->ctl, sizeof(Ctl));
     d.ctl = h->ctl;
-    if (p.method != 3) {
-        // methods 0-2 produce the rate itself: no corner mean, no sec/yr
-        Ctl c0;
-        memset(&c0, 0, sizeof(c0));
-        c0.plain = 1;
-        if ((rc = upload(h, h->ctl, &c0, sizeof(Ctl)))) return rc;
-    }
     AL(d.partials, (size_t)reduce_blocks(n) * 4 * sizeof(double));
     if (p.dt_method == 2) {
         AL(d.ts_x2, n * sizeof(double));
@@ -1479,6 +1474,10 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
         if ((rc = upload(h, d.z_bed, bg.data(), n * 8)) || (rc = upload(h, h->z_bed_ref, bg.data(), n * 8))) return rc;
         Ctl c0;
         memset(&c0, 0, sizeof(c0));
+        // methods 0-2 produce the rate itself: no corner mean, no sec/yr
+        c0.plain = p.method != 3 ? 1 : 0;
+        c0.dt_min = p.dt_min;
+        c0.max_reject = kDefaultMaxReject;
         if ((rc = upload(h, h->ctl, &c0, sizeof(c0)))) return rc;
     }
     CK(cudaStreamSynchronize(h->s));
@@ -1701,6 +1700,16 @@ int fi_update_async(fi_handle* h, const double* d_H_ice, double time, fi_bsl* bs
         CK(cudaMemcpyAsync(h->dH, d_H_ice, (size_t)h->nx_ice * h->ny_ice * 8, cudaMemcpyDeviceToDevice, h->s));
     }
     return update_any(h, h->dH, time, true);
+}
+
+int fi_set_max_rejections(fi_handle* h, int64_t max_per_update)
+{
+    if (!h || max_per_update < 0) return FI_E_ARG;
+    const long long v = max_per_update ? (long long)max_per_update : kDefaultMaxReject;
+    // in stream order: updates already enqueued keep the limit they saw
+    CK(cudaMemcpyAsync((char*)h->ctl + offsetof(Ctl, max_reject), &v, sizeof(v), cudaMemcpyHostToDevice, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return FI_OK;
 }
 
 int fi_synchronize(fi_handle* h)
@@ -2150,7 +2159,7 @@ template <typename T> void batch_attempt(fi_batch* b, cudaStream_t s, cudaGraphC
             batch_rows_inv<T>(b->dM, LR6, b->grid[1], b->rows_threads, b->rows_smem, s, i);
         }
         batch_dp_err<T>(b->dM, LT, b->grid[3], s);
-        batch_ts_err<T>(b->dM, LT, b->grid[3], 100000, s);
+        batch_ts_err<T>(b->dM, LT, b->grid[3], s);
         batch_ts_commit<T>(b->dM, LT, b->grid[3], s);
         batch_fsal<T>(b->dM, LT, b->grid[3], s);
         batch_attempt_end(b->dM, nm, loop, s, more_out, 1);
@@ -2163,12 +2172,12 @@ template <typename T> void batch_attempt(fi_batch* b, cudaStream_t s, cudaGraphC
     batch_rows_inv<T>(b->dM, LR, b->grid[1], b->rows_threads, b->rows_smem, s);
     if (sizeof(T) == 4) {
         // mixed members always carry now%w's float pair
-        batch_ts_fused(b->dM, LT, b->grid[3], 100000, s);
+        batch_ts_fused(b->dM, LT, b->grid[3], s);
         batch_ts_commit_pair(b->dM, LT, b->grid[3], s);
         b->launches += 9;
     } else {
         batch_ts_max<T>(b->dM, LT, b->grid[3], s);
-        batch_ts_err<T>(b->dM, LT, b->grid[3], 100000, s);
+        batch_ts_err<T>(b->dM, LT, b->grid[3], s);
         batch_ts_commit<T>(b->dM, LT, b->grid[3], s);
         b->launches += 10;
     }

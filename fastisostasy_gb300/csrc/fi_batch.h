@@ -102,7 +102,7 @@ template <typename T>
 void batch_rows_inv(const BMember* M, BList L, int nblk, int threads, size_t smem, cudaStream_t s, int stage = 0);
 template <typename T> void batch_ts_max(const BMember* M, BList L, int nblk, cudaStream_t s);
 template <typename T>
-void batch_ts_err(const BMember* M, BList L, int nblk, int max_reject, cudaStream_t s);
+void batch_ts_err(const BMember* M, BList L, int nblk, cudaStream_t s);
 template <typename T> void batch_ts_commit(const BMember* M, BList L, int nblk, cudaStream_t s);
 // true stages (Dormand-Prince 5(4) with FSAL) per member
 template <typename T> void batch_dp_stage(const BMember* M, BList L, int nblk, int i, cudaStream_t s);
@@ -110,7 +110,7 @@ template <typename T> void batch_dp_err(const BMember* M, BList L, int nblk, cud
 template <typename T> void batch_fsal(const BMember* M, BList L, int nblk, cudaStream_t s);
 template <typename T> void batch_flexure_y(const BMember* M, BList L, int nblk, int stage, cudaStream_t s);
 // mixed form with the float pair of now%w: ts_fused / ts_commit_pair per member
-void batch_ts_fused(const BMember* M, BList L, int nblk, int max_reject, cudaStream_t s);
+void batch_ts_fused(const BMember* M, BList L, int nblk, cudaStream_t s);
 void batch_ts_commit_pair(const BMember* M, BList L, int nblk, cudaStream_t s);
 void batch_loop_begin(const BMember* M, int nm, cudaStream_t s);
 // attempt_begin of every member, then the compacted lists (cl, blist_ints(nm)

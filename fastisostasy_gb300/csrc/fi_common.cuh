@@ -66,6 +66,11 @@ struct Ctl {
     int active;                // device Tsit5 loop: this attempt runs (gate of the stage RHS)
     int plain;                 // methods 0-2: stage outputs are the rate itself (no corner mean, no sec/yr)
     long long n_accept, n_reject, n_rhs, n_attempt;
+    // step-control limits (adaptive methods): a rejection that halves dt
+    // below dt_min, or more than max_reject rejections within one update,
+    // fails the update with ST_STEP; rej0 = n_reject when the update began
+    double dt_min;
+    long long max_reject, rej0;
     unsigned int counter[8];   // last-block arrival counters of grid reductions
 };
 

@@ -17,15 +17,20 @@
 // Nothing in the scratch has to start at zero: every word a kernel reads was
 // written earlier in the same call.
 //
-// Host code cannot use the array's name as a device address, so the first
-// call on each device (with that device current) looks the address up with
-// cudaGetSymbolAddress and caches it; make that first call before capturing
-// any stream.  All calls on one device share the one array: calls whose work
-// can overlap on the GPU (different streams, or different host threads) race
-// on it and must be serialised by the caller.
+// Host code cannot use the array's name as a device address, so every call
+// looks the address up on the current device with cudaGetSymbolAddress (a
+// lookup that allocates nothing once the library's device code is loaded,
+// and that stays valid after a cudaDeviceReset, which a cached pointer would
+// not).  The first call on a device loads that code; make it before
+// capturing any stream.  All calls on one device share the one array: calls
+// whose work can overlap on the GPU (different streams, or different host
+// threads) race on it and must be serialised by the caller.
+//
+// Spacing: dx, dy for a uniform grid, or the per-cell dx*K and dy*K fields
+// of a distorted projection (src/fastisostasy.f90:152-155), which
+// calc_lvelva's finite differences use cell by cell (src/lv_elva.f90:31).
 #include <cmath>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/fi_gpu.h"
 #include "fi_kernels.h"
@@ -55,9 +60,6 @@ constexpr size_t NA_BYTES = OFF_RTW + (size_t)(NA_N / 2 + 1) * 16;
 static_assert(NA_BYTES == 3219472, "scratch size stated in the header comment");
 
 static __device__ __align__(256) unsigned char g_fi_static_scratch[NA_BYTES];
-
-std::mutex g_na_mutex;
-unsigned char* g_na_ptr[64] = {nullptr};
 
 // exp(-2 pi i t / n) for t < n, and exp(-2 pi i k / nx) for k <= nx/2
 __global__ void k_na_twiddles(double2* twr, int nr, double2* twc, int nc, double2* rtw, int nx)
@@ -111,27 +113,20 @@ FftDesc na_factorize(int n)
 
 extern "C" int fi_lvelva_static(const double* d_w, const double* d_canom_full, const uint8_t* d_maskactive,
                                 const double* d_D_lith, const double* d_eta_eff, const double* d_kappa,
-                                const double* d_R, int nx, int ny, double dx, double dy, double g, double nu,
-                                double sec_per_year, double* d_dwdt, void* stream)
+                                const double* d_R, const double* d_dx_matrix, const double* d_dy_matrix, int nx,
+                                int ny, double dx, double dy, double g, double nu, double sec_per_year,
+                                double* d_dwdt, void* stream)
 {
     if (!d_w || !d_canom_full || !d_maskactive || !d_D_lith || !d_eta_eff || !d_kappa || !d_R || !d_dwdt)
         return FI_E_ARG;
     if (!(dx > 0.0) || !(dy > 0.0)) return FI_E_ARG;
+    if ((d_dx_matrix == nullptr) != (d_dy_matrix == nullptr)) return FI_E_ARG;   // both or neither
     // grids the static scratch cannot hold are refused, not truncated
     if (nx < 4 || ny < 4 || nx > NA_N || ny > NA_N || (nx & 1) || (ny & 1)) return FI_E_SIZE;
     cudaStream_t s = (cudaStream_t)stream;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FI_E_CUDA;
-    unsigned char* base;
-    {
-        std::lock_guard<std::mutex> lk(g_na_mutex);
-        if (!g_na_ptr[dev]) {
-            void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_fi_static_scratch) != cudaSuccess || !p) return FI_E_CUDA;
-            g_na_ptr[dev] = static_cast<unsigned char*>(p);
-        }
-        base = g_na_ptr[dev];
-    }
+    void* sym = nullptr;
+    if (cudaGetSymbolAddress(&sym, g_fi_static_scratch) != cudaSuccess || !sym) return FI_E_CUDA;
+    unsigned char* const base = static_cast<unsigned char*>(sym);
     double* q0 = reinterpret_cast<double*>(base + OFF_Q0);
     double* i2e = reinterpret_cast<double*>(base + OFF_I2E);
     double* f = reinterpret_cast<double*>(base + OFF_F);
@@ -169,6 +164,8 @@ extern "C" int fi_lvelva_static(const double* d_w, const double* d_canom_full, c
     c.inv_dy = 1.0 / dy;
     c.inv_2dy = 1.0 / (2 * dy);
     c.inv_dy2 = 1.0 / (dy * dy);
+    c.dxm = d_dx_matrix;   // null: uniform spacing from dx, dy
+    c.dym = d_dy_matrix;
     launch_flexure<double>(d_w, nullptr, q0, d_maskactive, d_D_lith, i2e, f, nx, ny, c, s);
     launch_rows_fwd<double>(f, nx, nx, ny, S, p, s);
     launch_cols_hartley<double>(S, mA, mB, 0, p, s);

@@ -58,6 +58,7 @@ struct Req {
     double* dH = nullptr;          // the load on the device, handed to the first update
     int nout = 0, head = 0;
     int fail_rc = 0;               // stepping failed with this status
+    std::atomic<bool> cancel{false};   // fi_serve_cancel: stop issuing, retire when idle
     cudaEvent_t ev[kDepth] = {nullptr, nullptr};
     int32_t pd[6] = {0, 0, 0, 0, 0, 0};
     size_t mem_key = 0;
@@ -71,6 +72,7 @@ struct fi_server {
     int device = 0;
     int max_inflight = 1;
     size_t reserve = 0;
+    size_t device_total = 0;           // bytes of device memory (admission bound)
     std::chrono::steady_clock::time_point t0;
     std::mutex mu;
     std::condition_variable cv;        // wakes the scheduler
@@ -188,6 +190,11 @@ bool can_admit(fi_server* s, size_t* est)
 
 void collect(fi_server* s, Req* r)
 {
+    if (r->fail_rc == FI_E_CANCELLED || (r->cancel.load() && !r->fail_rc)) {
+        // the request's stream is idle (no update in flight): drop the handle
+        finish(s, r, 4, FI_E_CANCELLED);
+        return;
+    }
     if (r->fail_rc) {
         finish(s, r, 3, r->fail_rc);
         return;
@@ -238,6 +245,20 @@ void worker(fi_server* s)
             continue;
         }
         size_t est = 0;
+        if (!s->queue.empty() && s->device_total &&
+            estimate(s, s->queue.front()) + s->reserve > s->device_total) {
+            // admission can never succeed: the request's estimated footprint
+            // plus the reserve exceeds the device's memory
+            Req* r = s->queue.front();
+            s->queue.pop_front();
+            snprintf(r->info.error, sizeof(r->info.error),
+                     "needs about %.2f GB + reserve %.2f GB, device has %.2f GB",
+                     estimate(s, r) / 1e9, s->reserve / 1e9, s->device_total / 1e9);
+            lk.unlock();
+            finish(s, r, 3, FI_E_OOM);
+            lk.lock();
+            continue;
+        }
         if (can_admit(s, &est)) {
             Req* r = s->queue.front();
             s->queue.pop_front();
@@ -286,7 +307,8 @@ void run(fi_server* s)
                 work = true;
             }
             int rc = FI_OK;
-            while (r->nout < kDepth && r->k < r->nsteps) {
+            const bool cancelled = r->cancel.load();
+            while (!cancelled && r->nout < kDepth && r->k < r->nsteps) {
                 // the same time sequence as a caller stepping by dtt, clipped at t_end
                 double tn = r->t0 + (double)(r->k + 1) * r->dtt;
                 if (r->k + 1 == r->nsteps || tn > r->t_end) tn = r->t_end;
@@ -296,8 +318,8 @@ void run(fi_server* s)
                 r->k++;
                 work = true;
             }
-            if (rc || (r->k >= r->nsteps && r->nout == 0)) {
-                r->fail_rc = rc;
+            if (rc || (r->nout == 0 && (cancelled || r->k >= r->nsteps))) {
+                r->fail_rc = rc ? rc : (cancelled ? FI_E_CANCELLED : 0);
                 out.push_back(r);
                 s->active.erase(s->active.begin() + a);
                 work = true;
@@ -338,7 +360,11 @@ int fi_serve_create(int max_inflight, double reserve_gb, fi_server** out)
     fi_server* s = new fi_server();
     s->device = dev;
     s->max_inflight = max_inflight;
-    s->reserve = (size_t)(reserve_gb * 1e9);
+    s->reserve = (size_t)fmin(reserve_gb * 1e9, 1.8e19);
+    {
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) s->device_total = tot;
+    }
     s->t0 = std::chrono::steady_clock::now();
     s->th = std::thread(run, s);
     for (int i = 0; i < kWorkers; ++i) s->workers.emplace_back(worker, s);
@@ -424,13 +450,39 @@ int fi_serve_result(fi_server* s, uint64_t id, double* w_ice, double* z_bed_ice)
         if (r->info.state < 2) return FI_E_STATE;
         s->all.erase(it);
     }
-    int rc = r->info.state == 2 ? FI_OK : (r->info.status ? r->info.status : FI_E_CUDA);
+    int rc = r->info.state == 2 ? FI_OK : (r->info.status ? r->info.status : FI_E_CUDA);   // 4: FI_E_CANCELLED
     if (rc == FI_OK) {
         if (w_ice) memcpy(w_ice, r->w_out.data(), r->w_out.size() * sizeof(double));
         if (z_bed_ice) memcpy(z_bed_ice, r->zb_out.data(), r->zb_out.size() * sizeof(double));
     }
     delete r;
     return rc;
+}
+
+int fi_serve_cancel(fi_server* s, uint64_t id)
+{
+    if (!s) return FI_E_ARG;
+    Req* queued = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->all.find(id);
+        if (it == s->all.end()) return FI_E_ARG;
+        Req* r = it->second;
+        if (r->info.state >= 2) return FI_E_STATE;
+        for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
+            if (*q == r) {
+                s->queue.erase(q);
+                queued = r;
+                break;
+            }
+        // admitted: the scheduler stops issuing its updates and retires it
+        // once the ones in flight have finished
+        r->cancel.store(true);
+    }
+    if (queued) finish(s, queued, 4, FI_E_CANCELLED);
+    s->cv.notify_all();
+    s->work_cv.notify_all();
+    return FI_OK;
 }
 
 double fi_serve_clock(fi_server* s) { return s ? s->now() : 0.0; }

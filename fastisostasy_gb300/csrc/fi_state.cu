@@ -327,6 +327,7 @@ __device__ __forceinline__ void set_args_one(Ctl* c, double tf, double bsl, doub
                                              int write_bsl)
 {
     c->tf = tf;
+    c->rej0 = c->n_reject;
     if (write_bsl) c->bsl = bsl;
     c->A_ocean = A_ocean;
     c->bsl_method = method;
@@ -467,8 +468,11 @@ __device__ __forceinline__ void ts_x12(double x, double k, double dt, double& x1
 }
 
 // Accept or reject an attempt from its error norm, adapt dt
-// (src/integrators.f90, tsit54 step control).
-__device__ __forceinline__ void ts_decide(Ctl* c, double err, double dt, double q, double dt_max, int max_reject)
+// (src/integrators.f90:186-199, tsit54 step control).  The reference halves
+// dt without a floor and never reads dt_min; here a rejection that takes dt
+// below dt_min, or one past the per-update rejection limit, ends the update
+// with ST_STEP (FI_E_STEP on the host).
+__device__ __forceinline__ void ts_decide(Ctl* c, double err, double dt, double q, double dt_max)
 {
     c->err = err;
     c->n_attempt++;
@@ -481,7 +485,7 @@ __device__ __forceinline__ void ts_decide(Ctl* c, double err, double dt, double 
         c->accepted = 0;
         c->dt = dt * 0.5;
         c->n_reject++;
-        if (c->n_reject > max_reject) { c->status = ST_STEP; c->done = 1; }
+        if (c->n_reject - c->rej0 > c->max_reject || c->dt < c->dt_min) { c->status = ST_STEP; c->done = 1; }
     }
 }
 
@@ -536,7 +540,7 @@ __global__ void __launch_bounds__(NT) k_ts_max(Dom d, const T* __restrict__ raw,
 }
 
 template <typename T>
-__device__ __forceinline__ void ts_err_body(Dom d, const T* __restrict__ raw, double q, double dt_max, int max_reject, int bid, int nblk)
+__device__ __forceinline__ void ts_err_body(Dom d, const T* __restrict__ raw, double q, double dt_max, int bid, int nblk)
 {
     Ctl* c = d.ctl;
     if (c->done) return;
@@ -558,13 +562,13 @@ __device__ __forceinline__ void ts_err_body(Dom d, const T* __restrict__ raw, do
         }
     }
     double tot[1];
-    if (grid_finish<1>(v, mx, d.partials, &c->counter[2], tot, bid, nblk)) ts_decide(c, sqrt(tot[0] / (double)d.n), dt, q, dt_max, max_reject);
+    if (grid_finish<1>(v, mx, d.partials, &c->counter[2], tot, bid, nblk)) ts_decide(c, sqrt(tot[0] / (double)d.n), dt, q, dt_max);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NT) k_ts_err(Dom d, const T* __restrict__ raw, double q, double dt_max, int max_reject)
+__global__ void __launch_bounds__(NT) k_ts_err(Dom d, const T* __restrict__ raw, double q, double dt_max)
 {
-    ts_err_body<T>(d, raw, q, dt_max, max_reject, (int)blockIdx.x, (int)gridDim.x);
+    ts_err_body<T>(d, raw, q, dt_max, (int)blockIdx.x, (int)gridDim.x);
 }
 
 // Mixed form with now%w as a float pair (whi + wlo), one pass per attempt:
@@ -576,7 +580,7 @@ __global__ void __launch_bounds__(NT) k_ts_err(Dom d, const T* __restrict__ raw,
 // per cell here: the FP64 state update moves to ts_commit_pair_body, which
 // runs for accepted attempts only.
 __device__ __forceinline__ void ts_fused_body(Dom d, const float* __restrict__ raw, double atol, double rtol, double q,
-                                              double dt_max, int max_reject, int bid, int nblk)
+                                              double dt_max, int bid, int nblk)
 {
     Ctl* c = d.ctl;
     if (c->done) return;
@@ -602,7 +606,7 @@ __device__ __forceinline__ void ts_fused_body(Dom d, const float* __restrict__ r
     if (grid_finish_f<3>(v, mx, d.partials, &c->counter[1], tot, bid, nblk)) {
         const double tol = atol + rtol * fmax(tot[0], tot[1]);
         c->tol = tol;
-        ts_decide(c, sqrt(tot[2] / (double)d.n) / tol, dt, q, dt_max, max_reject);
+        ts_decide(c, sqrt(tot[2] / (double)d.n) / tol, dt, q, dt_max);
     }
 }
 
@@ -635,9 +639,9 @@ __device__ __forceinline__ void ts_commit_pair_body(Dom d, const float* __restri
 }
 
 __global__ void __launch_bounds__(NT) k_ts_fused(Dom d, const float* __restrict__ raw, double atol, double rtol,
-                                                 double q, double dt_max, int max_reject)
+                                                 double q, double dt_max)
 {
-    ts_fused_body(d, raw, atol, rtol, q, dt_max, max_reject, (int)blockIdx.x, (int)gridDim.x);
+    ts_fused_body(d, raw, atol, rtol, q, dt_max, (int)blockIdx.x, (int)gridDim.x);
 }
 
 __global__ void __launch_bounds__(NT) k_ts_commit_pair(Dom d, const float* __restrict__ raw)
@@ -1078,11 +1082,11 @@ __global__ void __launch_bounds__(NT) k_b_ts_max(const BMember* __restrict__ M, 
 
 template <typename T>
 __global__ void __launch_bounds__(NT)
-k_b_ts_err(const BMember* __restrict__ M, BList L, int max_reject)
+k_b_ts_err(const BMember* __restrict__ M, BList L)
 {
     batch_walk(L, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
         const BMember& b = M[m];
-        ts_err_body<T>(b.d, (const T*)b.raw, b.q, b.dt_max, max_reject, local, b.red_nblk);
+        ts_err_body<T>(b.d, (const T*)b.raw, b.q, b.dt_max, local, b.red_nblk);
         __syncthreads();
     });
 }
@@ -1098,11 +1102,11 @@ __global__ void __launch_bounds__(NT) k_b_ts_commit(const BMember* __restrict__ 
 }
 
 __global__ void __launch_bounds__(NT)
-k_b_ts_fused(const BMember* __restrict__ M, BList L, int max_reject)
+k_b_ts_fused(const BMember* __restrict__ M, BList L)
 {
     batch_walk(L, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
         const BMember& b = M[m];
-        ts_fused_body(b.d, (const float*)b.raw, b.atol, b.rtol, b.q, b.dt_max, max_reject, local, b.red_nblk);
+        ts_fused_body(b.d, (const float*)b.raw, b.atol, b.rtol, b.q, b.dt_max, local, b.red_nblk);
         __syncthreads();
     });
 }
@@ -1285,13 +1289,13 @@ template <typename T> void batch_ts_max(const BMember* M, BList L, int nblk, cud
     k_b_ts_max<T><<<nblk, NT, 0, s>>>(M, L);
 }
 template <typename T>
-void batch_ts_err(const BMember* M, BList L, int nblk, int max_reject, cudaStream_t s)
+void batch_ts_err(const BMember* M, BList L, int nblk, cudaStream_t s)
 {
-    k_b_ts_err<T><<<nblk, NT, 0, s>>>(M, L, max_reject);
+    k_b_ts_err<T><<<nblk, NT, 0, s>>>(M, L);
 }
-void batch_ts_fused(const BMember* M, BList L, int nblk, int max_reject, cudaStream_t s)
+void batch_ts_fused(const BMember* M, BList L, int nblk, cudaStream_t s)
 {
-    k_b_ts_fused<<<nblk, NT, 0, s>>>(M, L, max_reject);
+    k_b_ts_fused<<<nblk, NT, 0, s>>>(M, L);
 }
 void batch_ts_commit_pair(const BMember* M, BList L, int nblk, cudaStream_t s)
 {
@@ -1314,8 +1318,8 @@ void batch_attempt_end(const BMember* M, int nm, cudaGraphConditionalHandle loop
 void batch_set_args(const BArgs* a, int nm, cudaStream_t s) { k_b_set_args<<<(nm + 127) / 128, 128, 0, s>>>(a, nm); }
 template void batch_ts_max<float>(const BMember*, BList, int, cudaStream_t);
 template void batch_ts_max<double>(const BMember*, BList, int, cudaStream_t);
-template void batch_ts_err<float>(const BMember*, BList, int, int, cudaStream_t);
-template void batch_ts_err<double>(const BMember*, BList, int, int, cudaStream_t);
+template void batch_ts_err<float>(const BMember*, BList, int, cudaStream_t);
+template void batch_ts_err<double>(const BMember*, BList, int, cudaStream_t);
 template void batch_ts_commit<float>(const BMember*, BList, int, cudaStream_t);
 template void batch_ts_commit<double>(const BMember*, BList, int, cudaStream_t);
 
@@ -1395,18 +1399,18 @@ template <typename T> void ts_max(const Dom& d, const T* raw, double atol, doubl
 {
     k_ts_max<T><<<ts_grid(d.n), NT, 0, s>>>(d, raw, atol, rtol);
 }
-template <typename T> void ts_err(const Dom& d, const T* raw, double q, double dt_max, int max_reject, cudaStream_t s)
+template <typename T> void ts_err(const Dom& d, const T* raw, double q, double dt_max, cudaStream_t s)
 {
-    k_ts_err<T><<<ts_grid(d.n), NT, 0, s>>>(d, raw, q, dt_max, max_reject);
+    k_ts_err<T><<<ts_grid(d.n), NT, 0, s>>>(d, raw, q, dt_max);
 }
 template <typename T> void ts_commit(const Dom& d, const T* raw, cudaStream_t s)
 {
     k_ts_commit<T><<<ts_grid(d.n), NT, 0, s>>>(d, raw);
 }
-void ts_fused(const Dom& d, const float* raw, double atol, double rtol, double q, double dt_max, int max_reject,
+void ts_fused(const Dom& d, const float* raw, double atol, double rtol, double q, double dt_max,
               cudaStream_t s)
 {
-    k_ts_fused<<<ts_grid(d.n), NT, 0, s>>>(d, raw, atol, rtol, q, dt_max, max_reject);
+    k_ts_fused<<<ts_grid(d.n), NT, 0, s>>>(d, raw, atol, rtol, q, dt_max);
 }
 void ts_commit_pair(const Dom& d, const float* raw, cudaStream_t s)
 {
@@ -1498,7 +1502,7 @@ template <typename T> void q0_from_cf(T* q0, const double* cf, const uint8_t* ma
                                cudaStream_t);                                                                 \
     template void euler_final<T>(const Ctl*, double*, double*, const T*, int, int, double, cudaStream_t);     \
     template void ts_max<T>(const Dom&, const T*, double, double, cudaStream_t);                              \
-    template void ts_err<T>(const Dom&, const T*, double, double, int, cudaStream_t);                         \
+    template void ts_err<T>(const Dom&, const T*, double, double, cudaStream_t);                              \
     template void ts_commit<T>(const Dom&, const T*, cudaStream_t);                                           \
     template void upd_end<T>(const Dom&, const T*, int, cudaStream_t);                                       \
     template void rhs_finish<T>(double*, const T*, int, int, double, cudaStream_t);                          \

@@ -68,11 +68,11 @@ template <typename T>
 void euler_final(const Ctl* c, double* x, double* w, const T* r1, int nx, int ny, double spy, cudaStream_t s);
 template <typename T> void ts_max(const Dom& d, const T* raw, double atol, double rtol, cudaStream_t s);
 template <typename T>
-void ts_err(const Dom& d, const T* raw, double q, double dt_max, int max_reject, cudaStream_t s);
+void ts_err(const Dom& d, const T* raw, double q, double dt_max, cudaStream_t s);
 template <typename T> void ts_commit(const Dom& d, const T* raw, cudaStream_t s);
 // Mixed form with now%w's float pair (d.whi/d.wlo): tolerance, error norm
 // and decision in one pass, then the commit of an accepted attempt.
-void ts_fused(const Dom& d, const float* raw, double atol, double rtol, double q, double dt_max, int max_reject,
+void ts_fused(const Dom& d, const float* raw, double atol, double rtol, double q, double dt_max,
               cudaStream_t s);
 void ts_commit_pair(const Dom& d, const float* raw, cudaStream_t s);
 // have_rhs < 0: read it from the control block (device Tsit5 loop)

@@ -13,7 +13,7 @@ import numpy as np
 from . import _lib
 from .isostasy import FiError, _f64, make_params
 
-STATE = {0: "queued", 1: "running", 2: "done", 3: "failed"}
+STATE = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "cancelled"}
 
 
 def padded_dims(params: dict, nx_ice: int, ny_ice: int, dx: float, dy: Optional[float] = None, precision=0):
@@ -115,6 +115,12 @@ class Server:
         if rc:
             raise FiError(rc, "fi_serve_result")
         return w, zb
+
+    def cancel(self, rid: int) -> None:
+        """Cancel a queued or running request (fi_serve_cancel)."""
+        rc = self.L.fi_serve_cancel(self.h, C.c_uint64(rid))
+        if rc:
+            raise FiError(rc, "fi_serve_cancel")
 
     def clock(self) -> float:
         return self.L.fi_serve_clock(self.h)

@@ -6,7 +6,7 @@
  * point replaces one reference routine of module `fastisostasy`
  * (src/fastisostasy.f90) or `barysealevel` (src/barysealevel.f90); the
  * Fortran caller keeps its isos_class / bsl_class and binds these functions
- * through iso_c_binding.
+ * through iso_c_binding (module fastisostasy_gpu, fastisostasy_gpu.f90).
  *
  * Conventions
  *   - Arrays are plain host pointers in the reference's Fortran layout:
@@ -37,14 +37,15 @@ enum {
     FI_OK = 0,
     FI_E_NAN = 1,      /* NaN in z_bed (src/fastisostasy.f90:864-869) */
     FI_E_LARGE = 2,    /* |w|,|we| > 1e5 or |dz_ss| > 1e3 (check_isos_instabilities :874-899) */
-    FI_E_STEP = 3,     /* adaptive step rejected too often (the reference loops forever) */
+    FI_E_STEP = 3,     /* adaptive step below dt_min or rejected too often (fi_set_max_rejections) */
     FI_E_OOM = 4,      /* device allocation failed */
     FI_E_CONFIG = 5,   /* unsupported configuration (the reference's `stop`s in isos_init) */
     FI_E_CUDA = 6,     /* CUDA runtime error */
     FI_E_TIMEOUT = 7,  /* a bounded device wait expired */
     FI_E_ARG = 8,      /* invalid argument */
     FI_E_STATE = 9,    /* call out of order (e.g. update before init_state) */
-    FI_E_SIZE = 10     /* grid larger than fi_lvelva_static's scratch (or odd-sized) */
+    FI_E_SIZE = 10,    /* grid larger than fi_lvelva_static's scratch (or odd-sized) */
+    FI_E_CANCELLED = 11  /* solve request cancelled (fi_serve_cancel) */
 };
 
 enum { FI_PREC_FP64 = 0, FI_PREC_MIXED = 1 };
@@ -160,6 +161,13 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
 int fi_update_async(fi_handle* h, const double* d_H_ice, double time, fi_bsl* bsl);
 /* Waits for the handle's stream; returns the device status (FI_E_NAN, ...). */
 int fi_synchronize(fi_handle* h);
+/* Step-control safety of the adaptive method (tsit54).  The reference
+ * halves dt after a rejection without any floor (src/integrators.f90:196-198)
+ * and reads dt_min (src/fastisostasy.f90:1008) without using it.  Here an
+ * update fails with FI_E_STEP when a rejection would take dt below
+ * fi_params.dt_min, or when more than max_per_update attempts are rejected
+ * within one update (default 1e6; 0 restores it). */
+int fi_set_max_rejections(fi_handle* h, int64_t max_per_update);
 /* Replaces bsl_update (src/barysealevel.f90:195-252). */
 int fi_bsl_update(fi_bsl* b, double year_bp);
 
@@ -201,22 +209,27 @@ int fi_lvelva(fi_handle* h, const double* w, const double* canom_full, double* d
 int fi_convolve(fi_handle* h, int kernel, const double* in_padded, double* out_padded);
 
 /* fi_lvelva_static has no counterpart in the reference: calc_lvelva
- * (src/lv_elva.f90:31-126) for callers that may not allocate device memory.
- * All arrays are DEVICE pointers of the caller, (nx, ny) with x fastest,
- * double except the 0/1 mask; d_kappa and d_R are the cell-layout fields of
- * calc_kappa / the viscous response (FI_FIELD_KAPPA, FI_FIELD_R).  The FP64
- * work is queued on `stream` (a cudaStream_t, NULL = legacy default stream)
- * and the call returns without waiting.  No device memory is allocated: the
- * scratch is one static device array sized for nx, ny <= FI_STATIC_MAX_N
- * (even, >= 4); other sizes return FI_E_SIZE.  The first call on a device
- * (which must be current) looks up the array's address; make it before
- * capturing any stream.  Calls that can overlap on one device race on the
- * shared scratch and must be serialised by the caller. */
+ * (src/lv_elva.f90:31-126) for callers that may not allocate device memory
+ * once running (a coupled model that splits HBM among its components at
+ * start-up; a loop that cannot afford cudaFree's device-wide sync).  All
+ * arrays are DEVICE pointers of the caller, (nx, ny) with x fastest, double
+ * except the 0/1 mask; d_kappa and d_R are the cell-layout fields of
+ * calc_kappa / the viscous response (FI_FIELD_KAPPA, FI_FIELD_R).  Spacing
+ * is uniform (dx, dy) when d_dx_matrix and d_dy_matrix are both NULL, else
+ * they are the per-cell dx*K and dy*K of a distorted grid (both or neither).
+ * The FP64 work is queued on `stream` (a cudaStream_t, NULL = legacy default
+ * stream) and the call returns without waiting.  No device memory is
+ * allocated: the scratch is one static device array sized for
+ * nx, ny <= FI_STATIC_MAX_N (even, >= 4); other sizes return FI_E_SIZE.
+ * The first call on a device (which must be current) loads the library's
+ * device code; make it before capturing any stream.  Calls that can overlap
+ * on one device race on the shared scratch and must be serialised by the
+ * caller. */
 #define FI_STATIC_MAX_N 256
 int fi_lvelva_static(const double* d_w, const double* d_canom_full, const uint8_t* d_maskactive,
                      const double* d_D_lith, const double* d_eta_eff, const double* d_kappa, const double* d_R,
-                     int nx, int ny, double dx, double dy, double g, double nu, double sec_per_year,
-                     double* d_dwdt, void* stream);
+                     const double* d_dx_matrix, const double* d_dy_matrix, int nx, int ny, double dx, double dy,
+                     double g, double nu, double sec_per_year, double* d_dwdt, void* stream);
 
 /* ---- Solve server: continuous batching of independent solves ----------
  * No counterpart in the reference (a caller there runs one isos_class at a
@@ -244,13 +257,18 @@ typedef struct {
     double bsl;                   /* barystatic sea level [m] */
 } fi_request;
 typedef struct {
-    int32_t state;                /* 0 queued, 1 running, 2 done, 3 failed */
+    int32_t state;                /* 0 queued, 1 running, 2 done, 3 failed, 4 cancelled */
     int32_t status;               /* FI_* status of the solve */
     int64_t updates;              /* isos_update calls issued */
     double t_submit, t_admit, t_done;   /* seconds on the server clock */
     char error[128];              /* message of a failed solve */
 } fi_request_info;
-/* The server drives the device that is current when it is created. */
+/* The server drives the device that is current when it is created.  A
+ * request whose estimated device footprint plus reserve_gb exceeds the
+ * device's memory is never admitted: it fails at once with FI_E_OOM.  One
+ * that fits is admitted when free memory (less the reserve) allows, or when
+ * nothing else runs; a device allocation that fails then fails it with
+ * FI_E_OOM, and the server goes on with the others. */
 int fi_serve_create(int max_inflight, double reserve_gb, fi_server** out);
 /* Copies the request's arrays; returns at once. */
 int fi_serve_submit(fi_server* s, const fi_request* r, uint64_t* id);
@@ -261,6 +279,11 @@ int fi_serve_wait(fi_server* s, uint64_t id, double timeout_s, fi_request_info* 
  * releases the request's record. */
 int fi_serve_result(fi_server* s, uint64_t id, double* w_ice, double* z_bed_ice);
 double fi_serve_clock(fi_server* s);
+/* Cancels a request: a queued one at once; a running one stops issuing
+ * updates and is retired (its handle freed) once those in flight finish,
+ * without disturbing the other requests.  Its state becomes 4 and
+ * fi_serve_result returns FI_E_CANCELLED.  FI_E_STATE if it already ended. */
+int fi_serve_cancel(fi_server* s, uint64_t id);
 /* Finishes every submitted request, then stops the scheduler. */
 int fi_serve_destroy(fi_server* s);
 

@@ -33,6 +33,44 @@ void orc_set_threads(int n)
 #endif
 }
 
+/* Reference-compatible stages evaluate get_dwdt at now%w for every stage
+ * (src/fastisostasy.f90:677-729 ignores its state argument), so the six
+ * Tsit5 / four RK4 evaluations of one attempt are the same computation on
+ * the same inputs.  With reuse on, the first evaluation is copied into the
+ * other stages: bit-identical results, a sixth of the transforms (the test
+ * suite's setting).  Off (the default) repeats them as the reference does. */
+static int g_reuse_frozen = 0;
+void orc_set_reuse_frozen(int on) { g_reuse_frozen = on ? 1 : 0; }
+
+/* Step-control limits.  The reference halves dt without bound and never
+ * reads dt_min (src/integrators.f90:196-198; dt_min is parsed at
+ * src/fastisostasy.f90:1008 and documented as the minimum dt of the
+ * adaptive methods).  Here a rejection that would take dt below dt_min,
+ * or more than g_max_reject rejections within one isos_update, ends the
+ * update with status 3 (FI_E_STEP), the same rule as the GPU library. */
+static long g_max_reject = 1000000;
+
+/* Convolution transform size.  Off (the default): the reference's (2n-1)^2,
+ * e.g. 1023 = 3 * 11 * 31 at n = 512, whose radix-11 and radix-31 stages
+ * this file's FFT evaluates as direct sums.  On: the smallest size >= 2n-1
+ * with factors 2, 3, 5, 7 only (1024 at n = 512), which gives the same
+ * linear convolution to rounding at the cost an optimised FFT library
+ * would have; the timed CPU baselines use it. */
+static int g_conv_smooth = 0;
+void orc_set_smooth_convolution(int on) { g_conv_smooth = on ? 1 : 0; }
+static int smooth_size(int n)
+{
+    for (;; n++) {
+        int m = n;
+        while (m % 2 == 0) m /= 2;
+        while (m % 3 == 0) m /= 3;
+        while (m % 5 == 0) m /= 5;
+        while (m % 7 == 0) m /= 7;
+        if (m == 1) return n;
+    }
+}
+void orc_set_max_rejections(long n) { g_max_reject = n > 0 ? n : 1000000; }
+
 /* ======================================================================
  * 1-D complex FFT: self-sorting Stockham, mixed radix, any length.
  * Stage with radix R over sub-transform size Ns: butterfly j loads
@@ -331,10 +369,16 @@ static void zerobc_corners(double *x, int nx, int ny)
 }
 
 /* precomputed_fftconvolution, src/convolutions.f90:59-91, with the crop of
- * calc_convolution_indices (:29-55) for even nx, ny (offset 0). */
+ * calc_convolution_indices (:29-55) for even nx, ny (offset 0).  M is the
+ * transform size: the reference's 2 max(nx, ny) - 1, or any larger size (the
+ * circular convolution of the zero-padded arrays is the linear one for
+ * every M >= 2n - 1).  The corners whose mean the reference subtracts are
+ * those of its (2n-1)^2 buffer, i.e. the linear-convolution lags 0 and
+ * 2n - 2, whatever M is. */
 void orc_conv(double *out, int nx, int ny, int M, const double *spec_re, const double *spec_im,
               const double *in)
 {
+    const int Mc = 2 * (nx > ny ? nx : ny) - 1;
     const int H = M / 2 + 1;
     double *ext = (double *)calloc((size_t)M * M, sizeof(double));
     double *sr = (double *)malloc(sizeof(double) * (size_t)M * H);
@@ -355,10 +399,18 @@ void orc_conv(double *out, int nx, int ny, int M, const double *spec_re, const d
         const double norm = (double)M * (double)M;   /* nx*ny*1._wp, isos_utils.f90:214 */
         for (e = 0; e < (size_t)M * M; e++) ext[e] = ext[e] / norm;
     }
-    zerobc_corners(ext, M, M);
-    for (j = 0; j < ny; j++)
-        for (i = 0; i < nx; i++)
-            out[(size_t)j * nx + i] = ext[(size_t)(j1 - 1 + j) * M + (i1 - 1 + i)];
+    if (M == Mc) {
+        zerobc_corners(ext, M, M);
+        for (j = 0; j < ny; j++)
+            for (i = 0; i < nx; i++)
+                out[(size_t)j * nx + i] = ext[(size_t)(j1 - 1 + j) * M + (i1 - 1 + i)];
+    } else {
+        const size_t last = (size_t)(Mc - 1) * M;
+        const double c = 0.25 * (((ext[0] + ext[last + Mc - 1]) + ext[last]) + ext[Mc - 1]);
+        for (j = 0; j < ny; j++)
+            for (i = 0; i < nx; i++)
+                out[(size_t)j * nx + i] = ext[(size_t)(j1 - 1 + j) * M + (i1 - 1 + i)] - c;
+    }
     free(ext); free(sr); free(si);
 }
 
@@ -737,6 +789,7 @@ orc_model *orc_create(const orc_params *p, int nx_ice, int ny_ice, double dx, do
     m->icrop1 += npx; m->icrop2 = m->nx - npx;
     m->jcrop1 += npy; m->jcrop2 = m->ny - npy;
     m->M = 2 * (m->nx > m->ny ? m->nx : m->ny) - 1;
+    if (g_conv_smooth) m->M = smooth_size(m->M);
     n = (size_t)m->nx * m->ny;
     {
         const int nx = m->nx, ny = m->ny;
@@ -1129,7 +1182,10 @@ static int step_rk4(orc_model *m, double tf)
             /* get_dwdt ignores its argument: all four stages see now%w */
             int s;
             rhs_eval(m, m->now.w, m->k[0]);
-            for (s = 1; s < 4; s++) { rhs_eval(m, m->now.w, m->k[s]); }
+            for (s = 1; s < 4; s++) {
+                if (g_reuse_frozen) { memcpy(m->k[s], m->k[0], n * sizeof(double)); m->n_rhs++; }
+                else rhs_eval(m, m->now.w, m->k[s]);
+            }
         } else {
             double *yy = m->x1;
             rhs_eval(m, m->x, m->k[0]);
@@ -1166,7 +1222,10 @@ static int step_tsit54(orc_model *m, double tf)
         m->dt = fmin(m->dt, tf - m->t);
         if (m->p.stage_mode == 0) {
             int st;
-            for (st = 0; st < 6; st++) rhs_eval(m, m->now.w, m->k[st]);
+            for (st = 0; st < 6; st++) {
+                if (st > 0 && g_reuse_frozen) { memcpy(m->k[st], m->k[0], n * sizeof(double)); m->n_rhs++; }
+                else rhs_eval(m, m->now.w, m->k[st]);
+            }
             for (e = 0; e < n; e++) {
                 double a1 = m->x[e], a2 = m->x[e];
                 for (st = 0; st < 6; st++) {
@@ -1217,7 +1276,8 @@ static int step_tsit54(orc_model *m, double tf)
         } else {
             m->dt = m->dt * 0.5;
             m->n_reject++;
-            if (++rejects > 200) return 3;   /* reference loops forever here (no dt_min floor) */
+            /* the reference keeps halving (no floor): see g_max_reject */
+            if (++rejects > g_max_reject || m->dt < m->p.dt_min) return 3;
         }
     }
     return 0;

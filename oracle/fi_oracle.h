@@ -105,6 +105,9 @@ int  orc_get_field(const orc_model *m, int which, double *out);   /* padded grid
 int  orc_get_scalars(const orc_model *m, double *out16);
 void orc_rhs_now(orc_model *m, double *dwdt);   /* get_dwdt at the current state */
 void orc_set_threads(int n);
+void orc_set_reuse_frozen(int on);          /* bit-identical reuse of the frozen RHS */
+void orc_set_max_rejections(long n);        /* per isos_update; 0 = default 1e6 */
+void orc_set_smooth_convolution(int on);    /* 2/3/5/7-smooth convolution size (timed baselines) */
 
 /* The Kelvin-function table of LV-ELRA (1001 entries each). */
 void orc_kei_table(double *rn, double *kei);

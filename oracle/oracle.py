@@ -84,6 +84,9 @@ def lib():
         L.orc_get_scalars.argtypes = [C.c_void_p, dp]
         L.orc_rhs_now.argtypes = [C.c_void_p, dp]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_set_reuse_frozen.argtypes = [C.c_int]
+        L.orc_set_max_rejections.argtypes = [C.c_long]
+        L.orc_set_smooth_convolution.argtypes = [C.c_int]
         L.orc_bilinear_array.argtypes = [dp, C.c_int, dp, C.c_int, dp, dp, C.c_int, dp, C.c_int, dp]
         L.orc_interp_0d.argtypes = [dp, dp, C.c_int, C.c_double]
         L.orc_interp_0d.restype = C.c_double
@@ -104,6 +107,26 @@ def _f64(a):
 
 def set_threads(n: int) -> None:
     lib().orc_set_threads(int(n))
+
+
+def set_reuse_frozen(on: bool) -> None:
+    """Evaluate the frozen (reference-compatible) RHS once per attempt and
+    copy it into the other stages: bit-identical, six times fewer
+    transforms for Tsit5."""
+    lib().orc_set_reuse_frozen(1 if on else 0)
+
+
+def set_smooth_convolution(on: bool) -> None:
+    """Convolve at the smallest 2/3/5/7-smooth size >= 2n-1 instead of the
+    reference's 2n-1 (same linear convolution to rounding, the cost of an
+    optimised FFT library); models created afterwards use it."""
+    lib().orc_set_smooth_convolution(1 if on else 0)
+
+
+def set_max_rejections(n: int) -> None:
+    """Rejected Tsit5 attempts allowed within one update before it fails
+    with status 3 (0 restores the default, 1e6)."""
+    lib().orc_set_max_rejections(int(n))
 
 
 def cfft(x: np.ndarray, sign: int = -1) -> np.ndarray:

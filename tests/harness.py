@@ -60,3 +60,26 @@ class Pair:
         if self.dom is not None:
             self.dom.close()
         self.orc.close()
+
+
+def oracle_solve(wl: W.Workload, times, stage_mode=None):
+    """w on the padded grid after isos_update at each of `times`, from no
+    ice at t = 0 under the workload's final load (the serve / ensemble
+    solve), by the oracle on every host core."""
+    import os
+    O.set_threads(os.cpu_count() or 1)
+    p = dict(wl.params)
+    if stage_mode is not None:
+        p["stage_mode"] = stage_mode
+    m = O.Model(p, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
+    f = wl.padded_fields(m.nx, m.ny)
+    if f:
+        m.set_fields(**f)
+    b = O.make_bsl()
+    m.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+    for t in times:
+        rc = m.update(wl.H_final, t, b)
+        assert rc == 0, "oracle update failed with %d at t=%g" % (rc, t)
+    w = m.field("w")
+    m.close()
+    return w

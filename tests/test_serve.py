@@ -6,7 +6,8 @@ import pytest
 from fastisostasy_gb300 import workloads as W
 from fastisostasy_gb300.isostasy import Domain
 from fastisostasy_gb300.serve import Server, padded_dims
-from harness import gpu_bsl
+from harness import gpu_bsl, oracle_solve, rel
+from fastisostasy_gb300 import _lib
 from oracle import oracle as O
 
 
@@ -122,6 +123,96 @@ def test_every_request_of_a_repeated_mix_matches_its_solve_alone():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_served_requests_match_oracle(precision):
+    """Two requests of different sizes and integrators served side by side,
+    each against the oracle: FP64 within 1e-10, mixed within 1e-5."""
+    wls = [small_rk4(48), small_tsit(40)]
+    srv = Server(max_inflight=4, reserve_gb=1.0)
+    ids = [srv.submit(wl, precision=precision) for wl in wls]
+    res = []
+    for rid in ids:
+        info = srv.wait(rid, 120.0)
+        assert info["status"] == 0, info
+        res.append(srv.result(rid)[0])
+    srv.close()
+    for wl, w in zip(wls, res):
+        times = [min(wl.dtt * (k + 1), wl.t_end) for k in range(int(np.ceil(wl.t_end / wl.dtt)))]
+        wo = oracle_solve(wl, times)
+        dom_pd = padded_dims(wl.params, wl.nx_ice, wl.ny_ice, wl.dx)
+        i1, i2, j1, j2 = dom_pd[2:]
+        wo = wo[j1 - 1:j2, i1 - 1:i2]
+        assert rel(w, wo) <= (1e-10 if precision == 0 else 1e-5)
+
+
+@pytest.mark.gpu
+def test_cancel_running_and_queued_requests():
+    """fi_serve_cancel: a running request stops issuing updates and is
+    retired; a queued one never starts; the requests beside them finish with
+    the bits they get alone."""
+    long_wl = small_rk4(96)
+    long_wl.t_end = 20000.0           # 2000 updates: still running when cancelled
+    nb = [small_rk4(48), small_tsit(40)]
+    want = [direct(wl) for wl in nb]
+    srv = Server(max_inflight=8, reserve_gb=1.0)
+    rl = srv.submit(long_wl)
+    ids = [srv.submit(wl) for wl in nb]
+    import time
+    t0 = time.time()
+    while srv.info(rl)["updates"] < 4:
+        assert time.time() - t0 < 60.0
+        time.sleep(0.002)
+    srv.cancel(rl)
+    info = srv.wait(rl, 60.0)
+    assert info["state"] == "cancelled" and info["status"] == _lib.FI_E_CANCELLED
+    assert 4 <= info["updates"] < 2000
+    with pytest.raises(_lib.FiError) as e:
+        srv.result(rl)
+    assert e.value.code == _lib.FI_E_CANCELLED
+    for rid, (w_ref, zb_ref) in zip(ids, want):
+        assert srv.wait(rid, 120.0)["state"] == "done"
+        w, zb = srv.result(rid)
+        assert np.array_equal(w, w_ref) and np.array_equal(zb, zb_ref)
+    with pytest.raises(_lib.FiError) as e:
+        srv.cancel(rl)               # released
+    srv.close()
+    # a queued request: one slot, held by a long solve
+    srv = Server(max_inflight=1, reserve_gb=1.0)
+    ra = srv.submit(long_wl)
+    rb = srv.submit(small_rk4(48))
+    assert srv.info(rb)["state"] == "queued"
+    srv.cancel(rb)
+    ib = srv.wait(rb, 10.0)
+    assert ib["state"] == "cancelled" and ib["updates"] == 0
+    srv.cancel(ra)
+    assert srv.wait(ra, 60.0)["state"] == "cancelled"
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_request_that_cannot_fit_fails_with_oom():
+    """Admission by device memory: with a reserve larger than the device, no
+    request can ever be admitted, and each fails at once with FI_E_OOM
+    instead of waiting; a server with room still solves the same request."""
+    wl = small_rk4(48)
+    srv = Server(max_inflight=4, reserve_gb=1e6)
+    ids = [srv.submit(wl) for _ in range(2)]
+    for rid in ids:
+        info = srv.wait(rid, 30.0)
+        assert info["state"] == "failed" and info["status"] == _lib.FI_E_OOM, info
+        assert "device has" in info["error"]
+        with pytest.raises(_lib.FiError):
+            srv.result(rid)
+    srv.close()
+    srv = Server(max_inflight=4, reserve_gb=1.0)
+    rid = srv.submit(wl)
+    assert srv.wait(rid, 120.0)["state"] == "done"
+    w, _ = srv.result(rid)
+    srv.close()
+    assert np.array_equal(w, direct(wl)[0])
+
+
+@pytest.mark.gpu
 def test_inflight_cap_and_drain():
     srv = Server(max_inflight=2, reserve_gb=0.5)
     ids = [srv.submit(small_rk4(48)) for _ in range(5)]
@@ -189,6 +280,10 @@ def test_ensemble_lockstep_matches_members_alone(precision, mode):
             dom.update(wl.H_final, t, b)
         w = dom.field("w")
         dom.close()
+        if mode == "graph" and wl.name.startswith("member_"):
+            # the batched member against the oracle as well
+            wo = oracle_solve(wl, (10.0, 20.0, 30.0, 40.0, 50.0, 60.0))
+            assert rel(g, wo) <= (1e-10 if precision == 0 else 1e-5), (wl.name, rel(g, wo))
         if mode == "graph" and precision == 1:
             # the batched launches are other kernels built from the same
             # code; the compiler may fuse FP32 multiply-adds differently in
