@@ -57,6 +57,38 @@ static long g_max_reject = 1000000;
  * linear convolution to rounding at the cost an optimised FFT library
  * would have; the timed CPU baselines use it. */
 static int g_conv_smooth = 0;
+
+/* Conditioning probe (tests only): white noise of relative size eps times
+ * max|k| added to every right-hand side evaluation, a stand-in for the
+ * rounding of a lower-precision RHS (eps = 1e-7 for FP32).  Seeded,
+ * deterministic; off (eps = 0) by default. */
+static double g_rhs_noise = 0.0;
+static unsigned long long g_noise_state = 0x9E3779B97F4A7C15ULL;
+void orc_set_rhs_noise(double eps, unsigned long long seed)
+{
+    g_rhs_noise = eps;
+    g_noise_state = seed ? seed : 0x9E3779B97F4A7C15ULL;
+}
+static double noise_uniform(void)
+{
+    /* xorshift64*: uniform in (0, 1) */
+    g_noise_state ^= g_noise_state >> 12;
+    g_noise_state ^= g_noise_state << 25;
+    g_noise_state ^= g_noise_state >> 27;
+    return ((double)((g_noise_state * 2685821657736338717ULL) >> 11) + 0.5) / 9007199254740992.0;
+}
+static void add_rhs_noise(double *k, size_t n)
+{
+    double mx = 0.0;
+    size_t e;
+    for (e = 0; e < n; e++) mx = fmax(mx, fabs(k[e]));
+    for (e = 0; e < n; e += 2) {
+        /* Box-Muller: two normal deviates per pair of cells */
+        const double r = sqrt(-2.0 * log(noise_uniform())), a = 2.0 * PI_LIT * noise_uniform();
+        k[e] += g_rhs_noise * mx * r * cos(a);
+        if (e + 1 < n) k[e + 1] += g_rhs_noise * mx * r * sin(a);
+    }
+}
 void orc_set_smooth_convolution(int on) { g_conv_smooth = on ? 1 : 0; }
 static int smooth_size(int n)
 {
@@ -1143,6 +1175,10 @@ static void rhs_eval(orc_model *m, const double *state, double *dwdt)
         memcpy(m->now.dwdt, dwdt, n * sizeof(double));
     }
     if (cf != m->y) free(cf);
+    if (g_rhs_noise > 0.0) {
+        add_rhs_noise(dwdt, n);
+        if (dwdt != m->now.dwdt) memcpy(m->now.dwdt, dwdt, n * sizeof(double));
+    }
     m->n_rhs++;
 }
 

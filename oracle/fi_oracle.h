@@ -108,6 +108,7 @@ void orc_set_threads(int n);
 void orc_set_reuse_frozen(int on);          /* bit-identical reuse of the frozen RHS */
 void orc_set_max_rejections(long n);        /* per isos_update; 0 = default 1e6 */
 void orc_set_smooth_convolution(int on);    /* 2/3/5/7-smooth convolution size (timed baselines) */
+void orc_set_rhs_noise(double eps, unsigned long long seed);   /* conditioning probe, tests only */
 
 /* The Kelvin-function table of LV-ELRA (1001 entries each). */
 void orc_kei_table(double *rn, double *kei);

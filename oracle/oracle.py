@@ -87,6 +87,7 @@ def lib():
         L.orc_set_reuse_frozen.argtypes = [C.c_int]
         L.orc_set_max_rejections.argtypes = [C.c_long]
         L.orc_set_smooth_convolution.argtypes = [C.c_int]
+        L.orc_set_rhs_noise.argtypes = [C.c_double, C.c_ulonglong]
         L.orc_bilinear_array.argtypes = [dp, C.c_int, dp, C.c_int, dp, dp, C.c_int, dp, C.c_int, dp]
         L.orc_interp_0d.argtypes = [dp, dp, C.c_int, C.c_double]
         L.orc_interp_0d.restype = C.c_double
@@ -121,6 +122,13 @@ def set_smooth_convolution(on: bool) -> None:
     reference's 2n-1 (same linear convolution to rounding, the cost of an
     optimised FFT library); models created afterwards use it."""
     lib().orc_set_smooth_convolution(1 if on else 0)
+
+
+def set_rhs_noise(eps: float, seed: int = 1) -> None:
+    """Add seeded white noise of relative size eps * max|k| to every RHS
+    evaluation (a conditioning probe: eps = 1e-7 stands in for the rounding
+    of an FP32 right-hand side); 0 turns it off."""
+    lib().orc_set_rhs_noise(float(eps), int(seed))
 
 
 def set_max_rejections(n: int) -> None:

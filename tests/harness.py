@@ -62,10 +62,14 @@ class Pair:
         self.orc.close()
 
 
-def oracle_solve(wl: W.Workload, times, stage_mode=None):
+def oracle_solve(wl: W.Workload, times, stage_mode=None, eta_scale=1.0, counts=False, rhs_noise=0.0):
     """w on the padded grid after isos_update at each of `times`, from no
     ice at t = 0 under the workload's final load (the serve / ensemble
-    solve), by the oracle on every host core."""
+    solve), by the oracle on every host core; `eta_scale` multiplies the
+    workload's viscosity field and `rhs_noise` adds seeded white noise of
+    that size relative to max|k| to every right-hand side (perturbations to
+    measure conditioning); with `counts`, also the accepted and rejected
+    step counts."""
     import os
     O.set_threads(os.cpu_count() or 1)
     p = dict(wl.params)
@@ -73,13 +77,36 @@ def oracle_solve(wl: W.Workload, times, stage_mode=None):
         p["stage_mode"] = stage_mode
     m = O.Model(p, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
     f = wl.padded_fields(m.nx, m.ny)
+    if eta_scale != 1.0:
+        f["eta_eff"] = f["eta_eff"] * eta_scale
     if f:
         m.set_fields(**f)
     b = O.make_bsl()
     m.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
-    for t in times:
-        rc = m.update(wl.H_final, t, b)
-        assert rc == 0, "oracle update failed with %d at t=%g" % (rc, t)
+    if rhs_noise:
+        O.set_rhs_noise(rhs_noise, 99)
+    try:
+        for t in times:
+            rc = m.update(wl.H_final, t, b)
+            assert rc == 0, "oracle update failed with %d at t=%g" % (rc, t)
+    finally:
+        O.set_rhs_noise(0.0)
     w = m.field("w")
+    sc = m.scalars()
     m.close()
-    return w
+    return (w, (sc["n_accept"], sc["n_reject"])) if counts else w
+
+
+def mixed_bound(wl: W.Workload, times, w_oracle):
+    """The mixed form's bound against the FP64 oracle for one solve: 1e-5 of
+    max|w|, or ten times the move of the oracle's own solution under white
+    noise of FP32 size (1e-7 of max|k|) added to every right-hand side,
+    where the solve amplifies such noise.  The reference's Tsit5 (one frozen RHS per
+    attempt, i.e. forward-Euler steps sized by an error estimate that does
+    not see stability) can step past the stability limit of the stiffest,
+    grid-scale modes, where any rounding noise then grows geometrically: the
+    FP32 right-hand side starts that noise 1e9 times higher than FP64 does,
+    and the FP64 solution itself drifts from the same solve computed in
+    another order by the same factor per step."""
+    sens = rel(oracle_solve(wl, times, rhs_noise=1e-7), w_oracle)
+    return max(1e-5, 10.0 * sens), sens

@@ -44,14 +44,29 @@ def headline(stage_mode=1):
     return W.config2(n=512, L=512 * 11.71875e3, dt=1.0, dtt=10.0, stage_mode=stage_mode)
 
 
+def check_masks(pair):
+    """Masks bit-exact, except at ties: cells where the bed and the sea
+    surface agree to rounding (|z_bed - z_ss| at 1e-10 of the deflection
+    scale), whose comparison z_bed > z_ss (src/sealevel.f90:147-187) any
+    rounding decides.  Configuration 1 has such a grid: a flat bed at 0 m
+    under a sea surface at 0 m, so its corner cells, where the corner
+    boundary condition leaves w at rounding level, are ties."""
+    zb, zs = pair.orc.field("z_bed"), pair.orc.field("z_ss")
+    scale = max(np.abs(pair.orc.field("w")).max(), np.abs(zb - zb.mean()).max(), 1.0)
+    tie = np.abs(zb - zs) <= 1e-10 * scale
+    for m in MASKS:
+        diff = pair.dom.field(m) != pair.orc.field(m)
+        assert not (diff & ~tie).any(), (m, int((diff & ~tie).sum()))
+    return int(tie.sum())
+
+
 def check_fp64(pair):
     worst = {}
     for f in FIELDS:
         a, b = pair.dom.field(f), pair.orc.field(f)
         worst[f] = rel(a, b) if np.abs(b).max() > 0 else float(np.abs(a).max())
         assert worst[f] <= TOL64, (f, worst[f])
-    for m in MASKS:
-        assert np.array_equal(pair.dom.field(m), pair.orc.field(m)), m
+    check_masks(pair)
     return worst
 
 
@@ -145,16 +160,45 @@ def test_config2_256_rk4_matches_oracle(precision):
 
 def test_config3_512x1024_fp64_matches_oracle():
     """Configuration 3 at its full size (336 x 560 ice grid padded to
-    512 x 1024): interactive sea level with bit-exact masks, two-layer
-    freqdomain mantle (general Hartley multiply), elastic + geoid, and the
-    reference's Tsit5 with the same accept/reject sequence over one coupling
-    step of a few hundred attempts."""
-    pair = Pair(W.config3(), precision=0)
+    512 x 1024): interactive sea level, two-layer freqdomain mantle (general
+    Hartley multiply), elastic + geoid, the reference's Tsit5.
+
+    That integrator rides the explicit stability edge here (frozen RHS: each
+    attempt is a forward-Euler step whose error estimate does not see
+    stability), so rounding-level differences grow by about 1e4 per model
+    year: a 1e-13 change of the upper-mantle viscosity moves the oracle's
+    own solution by ~2e-9 of max|w| at t = 2 yr and by ~0.3 at t = 4 yr, with
+    a different accept/reject sequence (test_oracle.py pins this on the
+    CPU).  The comparison therefore runs over the first two model years
+    (about 45 attempts): the same accept/reject sequence, masks bit-exact,
+    every field within 1e-10 at t = 1 yr, and at t = 2 yr w closer to the
+    oracle than the oracle is to itself under that 1e-13 change."""
+    wl = W.config3()
+    pair = Pair(wl, precision=0)
     assert (pair.dom.nx, pair.dom.ny) == (512, 1024)
     pair.init()
-    pair.step(1)
-    check_counts(pair)
-    assert pair.orc.scalars()["n_reject"] > 0
+    for t in (0.5, 1.0):
+        pair.wl.dtt = t - pair.t
+        pair.step(1)
+        check_counts(pair)
     check_fp64(pair)
+    assert check_masks(pair) == 0   # a fractal bed: no ties
     assert pair.dom.field("maskocean").any() and pair.dom.field("maskcontinent").any()
+    pair.wl.dtt = 1.0
+    pair.step(1)                    # t = 2 yr
+    check_counts(pair)
+    assert pair.orc.scalars()["n_reject"] > 10
+    assert check_masks(pair) == 0
+    w_g, w_o = pair.dom.field("w"), pair.orc.field("w")
     pair.close()
+    wp = W.config3()
+    wp.params["viscosities"] = [1e20 * (1 + 1e-13), 1e21]
+    m = O.Model(wp.params, wp.nx_ice, wp.ny_ice, wp.dx, wp.dx)
+    b = O.make_bsl()
+    m.init_state(wp.z_bed, wp.H_at(0.0), 0.0, b)
+    for t in (0.5, 1.0, 2.0):
+        assert m.update(wp.H_at(t), t, b) == 0
+    sens = rel(m.field("w"), w_o)
+    m.close()
+    assert 1e-12 < sens < 1e-6, sens
+    assert rel(w_g, w_o) <= sens, (rel(w_g, w_o), sens)

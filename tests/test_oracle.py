@@ -9,6 +9,7 @@ import pytest
 
 import np_restatement as R
 from oracle import analytical as A
+from fastisostasy_gb300 import workloads as W
 from oracle import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -209,3 +210,35 @@ def test_elastic_green_uses_the_reference_table():
                 g = ge[k] + (r - rn[k]) / (rn[k + 1] - rn[k]) * (ge[k + 1] - ge[k])
             want[j, i] = g * f12 * (dx * dx) / (f981 * max(r, dx))
     assert np.array_equal(got, want)
+
+
+def test_config3_reference_tsit54_is_ill_conditioned():
+    """Configuration 3 (512 x 1024, a 1e20 Pa s layer at 5 km spacing) under
+    the reference's Tsit5 (frozen RHS: every attempt is a forward-Euler step,
+    src/integrators.f90:131-203, src/fastisostasy.f90:677-729): a 1e-13
+    relative change of the upper-mantle viscosity, far below any FP64
+    implementation difference, moves w by more than 1e-3 of max|w| within
+    five model years (the accept/reject counts may still coincide).  No build of
+    the reference (another compiler, another CPU, FFTW) can reproduce its
+    step sequence over a 10-yr coupling step; GPU parity at this size is
+    therefore checked over the first two years (test_gpu_full_size.py)."""
+    O.set_threads(os.cpu_count() or 1)
+    O.set_reuse_frozen(True)
+    try:
+        out = []
+        for pert in (0.0, 1e-13):
+            wl = W.config3()
+            wl.params["viscosities"] = [1e20 * (1 + pert), 1e21]
+            m = O.Model(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
+            b = O.make_bsl()
+            m.init_state(wl.z_bed, wl.H_at(0.0), 0.0, b)
+            for t in (1.0, 2.0, 3.0, 4.0, 5.0):
+                assert m.update(wl.H_at(t), t, b) == 0
+            s = m.scalars()
+            out.append((s["n_accept"], s["n_reject"], m.field("w")))
+            m.close()
+    finally:
+        O.set_reuse_frozen(False)
+    (a0, r0, w0), (a1, r1, w1) = out
+    assert a0 + r0 > 100
+    assert np.abs(w1 - w0).max() > 1e-3 * np.abs(w0).max()
