@@ -262,3 +262,53 @@ def test_reference_api_driver_loop(tmp_path, precision):
         assert np.array_equal(isos.out[m].astype(bool), dom.crop(orc.field(m)).astype(bool)), m
     I.isos_end(isos)
     orc.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_c_driver_replays_reference_loop(tmp_path, precision):
+    """The C driver (tests/driver/fi_test_isostasy.c) runs the reference's
+    test loop for its disc experiment test1d through the C ABI: bsl_update
+    then isos_update every dtt, isos%out read back every dt_out.  Its
+    outputs against the oracle driven through the same sequence."""
+    import subprocess
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "driver"))
+    import build_driver
+    exe = build_driver.build()
+    n, dx, nt, dtt, dt_out = 41, 100e3, 31, 10.0, 100.0
+    out = os.path.join(str(tmp_path), "out.bin")
+    r = subprocess.run([exe, out, str(precision), str(n), repr(dx), str(nt), repr(dtt), repr(dt_out)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    rec = np.fromfile(out, dtype=np.float64).reshape(-1, 1 + 4 * n * n)
+    assert list(rec[:, 0]) == [0.0, 100.0, 200.0, 300.0]
+    p = dict(P.DEFAULTS)            # the test1d values the driver sets
+    orc = O.Model(p, n, n, dx, dx)
+    xc = (np.arange(n) - (n - 1) / 2.0) * dx
+    H1 = np.where(xc[None, :] ** 2 + xc[:, None] ** 2 <= (1000e3) ** 2, 1000.0, 0.0)
+    H0 = np.zeros_like(H1)
+    z_bed = np.full((n, n), 1e6)
+    bo = O.make_bsl()
+    O.lib().orc_bsl_update(bo, 0.0)
+    orc.init_state(z_bed, H0, 0.0, bo)
+    i1, i2, j1, j2 = orc.icrop1, orc.icrop2, orc.jcrop1, orc.jcrop2
+    k_out = 0
+    tol = TOL64 if precision == 0 else 1e-5
+    for k in range(1, nt + 1):
+        t = (k - 1) * dtt
+        O.lib().orc_bsl_update(bo, t)
+        assert orc.update(H1 if t > 0 else H0, t, bo) == 0
+        if t % dt_out == 0.0:
+            got = rec[k_out, 1:].reshape(4, n, n)
+            crop = lambda f: orc.field(f)[j1 - 1:j2, i1 - 1:i2]
+            for i, f in enumerate(("z_bed", "w", "we")):
+                ref = crop(f)
+                if np.abs(ref).max() > 0 and f != "z_bed":
+                    assert rel(got[i], ref) <= tol, (t, f, rel(got[i], ref))
+                elif f == "z_bed":
+                    assert np.abs(got[i] - ref).max() <= tol * max(np.abs(crop("w")).max(), 1.0), (t, f)
+            assert np.array_equal(got[3] != 0.0, crop("maskocean") != 0), t
+            k_out += 1
+    assert k_out == 4
+    assert np.abs(rec[-1, 1 + n * n:1 + 2 * n * n]).max() > 1.0   # the disc has depressed the bed
+    orc.close()

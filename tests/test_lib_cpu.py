@@ -75,3 +75,69 @@ def test_workloads_are_seeded():
     f1 = m1.padded_fields(m1.nx_ice, m1.ny_ice)["eta_eff"]
     assert np.array_equal(f0, f1)
     assert abs(np.log10(f0).mean() - 21.0) < 1e-9
+
+
+def _header_functions():
+    """{name: number of parameters} of every function fi_gpu.h declares."""
+    text = open(os.path.join(ROOT, "include", "fi_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(fi_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def _fortran_interfaces():
+    """{C name: number of dummy arguments} of the interface blocks in
+    include/fastisostasy_gpu.f90, and the components of its bind(C) types."""
+    text = open(os.path.join(ROOT, "include", "fastisostasy_gpu.f90")).read()
+    text = re.sub(r"!.*", "", text).replace("&\n", " ")
+    funcs = {}
+    for m in re.finditer(r"function[ \t]+(\w+)[ \t]*\(([^)]*)\)[^\n]*bind\(C,\s*name=\"(\w+)\"\)", text, re.I):
+        args = [a for a in m.group(2).replace(" ", "").split(",") if a]
+        assert m.group(1) == m.group(3)
+        funcs[m.group(3)] = len(args)
+    types = {}
+    for m in re.finditer(r"type,\s*bind\(C\)\s*::\s*(\w+)(.*?)end type", text, re.S | re.I):
+        comps = []
+        for line in m.group(2).splitlines():
+            if "::" in line:
+                for c in line.split("::", 1)[1].split(","):
+                    c = re.sub(r"\(.*", "", c.strip())
+                    if c:
+                        comps.append(c.lower())
+        types[m.group(1)] = comps
+    return funcs, types
+
+
+def test_fortran_module_binds_every_entry_point():
+    """No Fortran compiler exists here: the interface module is checked
+    against the header instead.  Every function of fi_gpu.h has an
+    interface of the same name and arity, and the bind(C) types list the
+    C structs' fields in the same order as the ctypes mirror (whose layout
+    the gcc test above checks)."""
+    from fastisostasy_gb300 import _lib as L
+    hdr = _header_functions()
+    funcs, types = _fortran_interfaces()
+    assert set(funcs) == set(hdr), (set(hdr) ^ set(funcs))
+    for name, n in hdr.items():
+        assert funcs[name] == n, (name, funcs[name], n)
+    for ftype, ctype in (("fi_params", L.FiParams), ("fi_bsl", L.FiBsl), ("fi_out", L.FiOut),
+                         ("fi_rheology", L.FiRheology), ("fi_request", L.FiRequest),
+                         ("fi_request_info", L.FiRequestInfo)):
+        assert types[ftype] == [f[0].lower() for f in ctype._fields_], ftype
+
+
+def test_c_driver_builds_and_fails_loudly_without_a_gpu(tmp_path):
+    """The C driver that replays the reference's test loop compiles and
+    links against libfigpu.so; without a GPU its isos_init fails with
+    FI_E_CUDA (there is no CPU path)."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "driver"))
+    import build_driver
+    exe = build_driver.build()
+    r = subprocess.run([exe, str(tmp_path / "o.bin"), "0", "33", "100e3", "3", "10", "10"], capture_output=True,
+                       text=True)
+    assert r.returncode == 6, (r.returncode, r.stderr)
+    assert "isos_init" in r.stderr
