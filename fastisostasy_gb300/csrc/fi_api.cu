@@ -607,14 +607,19 @@ template <typename T> void tune_rhs_shapes(fi_handle* h)
         bool operator==(const Key& o) const { return nx == o.nx && ny == o.ny && sz == o.sz; }
     };
     static std::mutex mu;
-    static std::vector<std::pair<Key, std::pair<int, int>>> cache;
+    struct Shape {
+        int rb, rt, cb, ct;
+    };
+    static std::vector<std::pair<Key, Shape>> cache;
     const Key key{h->nx, h->ny, (int)sizeof(T)};
     {
         std::lock_guard<std::mutex> lk(mu);
         for (auto& e : cache)
             if (e.first == key) {
-                h->prhs.rb = e.second.first;
-                h->prhs.cb = e.second.second;
+                h->prhs.rb = e.second.rb;
+                h->prhs.rt = e.second.rt;
+                h->prhs.cb = e.second.cb;
+                h->prhs.ct = e.second.ct;
                 return;
             }
     }
@@ -639,32 +644,47 @@ template <typename T> void tune_rhs_shapes(fi_handle* h)
         return best;
     };
     const double scale = 1.0 / (double)(float)((long long)h->nx * h->ny);
-    int best_rb = 0, best_cb = 0;
+    // rows (columns) per block x threads per block: more threads per
+    // block keep more warps resident on long rows, where one block per
+    // row of 1024 points at 256 threads left most warp slots empty
+    int best_rb = 0, best_cb = 0, best_rt = 0, best_ct = 0;
     float tr = 1e30f, tc = 1e30f;
     for (int rb : {1, 2, 4, 8}) {
         if (2 * (size_t)rb * p.h * sizeof(C2) > (size_t)optin) continue;
-        p.rb = rb;
-        const float t = time_it([&] {
-            launch_rows_fwd<T>((const T*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, p, h->s);
-            launch_rows_inv<T>((const C2*)h->S, (T*)h->raw[0], p, scale, h->s);
-        });
-        if (t < tr) { tr = t; best_rb = rb; }
+        for (int rt : {128, 256, 512, 1024}) {
+            if (rt > 128 && rt > rb * p.h / 2) continue;   // at most one element pair per thread
+            p.rb = rb;
+            p.rt = rt;
+            const float t = time_it([&] {
+                launch_rows_fwd<T>((const T*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, p, h->s);
+                launch_rows_inv<T>((const C2*)h->S, (T*)h->raw[0], p, scale, h->s);
+            });
+            if (cudaGetLastError() != cudaSuccess) continue;   // a shape the device refuses
+            if (t < tr) { tr = t; best_rb = rb; best_rt = rt; }
+        }
     }
     for (int cb : {1, 2, 4, 8}) {
         if (2 * (size_t)cb * (p.ny + 1) * sizeof(C2) > (size_t)optin) continue;
-        p.cb = cb;
-        const float t = time_it([&] {
-            launch_cols_hartley<T>((C2*)h->S, (const T*)h->mA, (const T*)h->mB, h->even, p, h->s);
-        });
-        if (t < tc) { tc = t; best_cb = cb; }
+        for (int ct : {128, 256, 512, 1024}) {
+            if (ct > 128 && ct > cb * p.ny / 2) continue;
+            p.cb = cb;
+            p.ct = ct;
+            const float t = time_it([&] {
+                launch_cols_hartley<T>((C2*)h->S, (const T*)h->mA, (const T*)h->mB, h->even, p, h->s);
+            });
+            if (cudaGetLastError() != cudaSuccess) continue;
+            if (t < tc) { tc = t; best_cb = cb; best_ct = ct; }
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaGetLastError();
     h->prhs.rb = best_rb;
+    h->prhs.rt = best_rt;
     h->prhs.cb = best_cb;
+    h->prhs.ct = best_ct;
     std::lock_guard<std::mutex> lk(mu);
-    cache.push_back({key, {best_rb, best_cb}});
+    cache.push_back({key, Shape{best_rb, best_rt, best_cb, best_ct}});
 }
 
 int kernel_spectrum(fi_handle* h, const std::vector<double>& ker, int which)

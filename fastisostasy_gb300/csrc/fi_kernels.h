@@ -52,6 +52,7 @@ struct Plan2D {
     const double2* rtw64;   // exp(-2 pi i k / nx), k <= h
     const float2* rtw32;
     int rb = 0, cb = 0;     // rows per row-transform block, columns per column-transform block (0: default)
+    int rt = 0, ct = 0;     // threads per row- / column-transform block (0: default)
 };
 
 // The RHS launchers take an optional device flag: when it points at 0 every

@@ -641,7 +641,8 @@ void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, type
     const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
     set_smem(k_rows_fwd<T>, sm);
     const int nblk = (nrows_in + RB - 1) / RB;
-    k_rows_fwd<T><<<nblk, threads_for(RB * p.h / 4), sm, s>>>(in, in_pitch, in_width, nrows_in, S, p, RB, gate);
+    const int nt = p.rt > 0 ? p.rt : threads_for(RB * p.h / 4);
+    k_rows_fwd<T><<<nblk, nt, sm, s>>>(in, in_pitch, in_width, nrows_in, S, p, RB, gate);
 }
 
 template <typename T>
@@ -702,7 +703,8 @@ void launch_rows_inv(const typename vec2<T>::type* S, T* out, const Plan2D& p, d
     const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
     set_smem(k_rows_inv<T>, sm);
     const int nblk = (p.ny + RB - 1) / RB;
-    k_rows_inv<T><<<nblk, threads_for(RB * p.h / 4), sm, s>>>(S, p.ny, out, p.nx, p, RB, (T)scale, gate);
+    const int nt = p.rt > 0 ? p.rt : threads_for(RB * p.h / 4);
+    k_rows_inv<T><<<nblk, nt, sm, s>>>(S, p.ny, out, p.nx, p, RB, (T)scale, gate);
 }
 
 // ---------------------------------------------------------------------------
@@ -811,7 +813,8 @@ void launch_cols_hartley(typename vec2<T>::type* S, const T* mA, const T* mB, in
     const size_t sm = 2 * (size_t)CB * col_stride(p.ny) * sizeof(C2);
     set_smem(k_cols_hartley<T>, sm);
     const int nblk = (p.h + 1 + CB - 1) / CB;
-    k_cols_hartley<T><<<nblk, threads_for(CB * p.ny / 4), sm, s>>>(S, mA, mB, even, p, CB, gate);
+    const int nt = p.ct > 0 ? p.ct : threads_for(CB * p.ny / 4);
+    k_cols_hartley<T><<<nblk, nt, sm, s>>>(S, mA, mB, even, p, CB, gate);
 }
 
 template <typename T>
