@@ -479,7 +479,35 @@ def ensemble_leg(n_members=256, n_updates=10):
         d.close()
         cond.append({"member": i, "n": wl.nx_ice, "mixed_vs_fp64": float(errs[i]),
                      "fp64_eta_1e-7_vs_fp64": float(np.abs(wp - w64[i]).max() / max(np.abs(w64[i]).max(), 1e-300))})
+    # one member over the stated 10 kyr horizon (1000 coupling steps), alone
+    # in each form: the smallest grid, so that the horizon fits the run
+    hm = min(range(n_members), key=lambda i: (wls[i].nx_ice, i))
+    horizon = {}
+    for prec, key in ((1, "mixed"), (0, "fp64")):
+        wl = wls[hm]
+        d = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=prec)
+        f = wl.padded_fields(d.nx, d.ny)
+        if f:
+            d.set_fields(**f)
+        b = _lib.FiBsl()
+        b.method, b.constant_ocean_surface = 0, 1
+        b.A_ocean_pd = b.A_ocean_now = 3.625e14
+        d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+        d.update(wl.H_final, 10.0, b)
+        a = time.perf_counter()
+        for k in range(2, 1001):
+            d.update_async(0, 10.0 * k, b)
+        d.synchronize()
+        secs = time.perf_counter() - a
+        sc = d.scalars()
+        horizon[key] = {"kyr_s": 9.99 / secs, "t_end_yr": sc["t"], "accepted": sc["n_accept"],
+                        "rejected": sc["n_reject"], "w": d.field("w")}
+        d.close()
+    wm, wd = horizon["mixed"].pop("w"), horizon["fp64"].pop("w")
+    horizon.update({"member": hm, "n": wls[hm].nx_ice, "horizon_kyr": 10.0,
+                    "err_mixed_vs_fp64": float(np.abs(wm - wd).max() / max(np.abs(wd).max(), 1e-300))})
     return {
+        "horizon_member": horizon,
         "workload": "ensemble: %d members, n in {128,192,256,384,512} (%s), dx 10-30 km, log10 eta Gaussian random "
                     "field (mean 21, std 0.5, 500 km), He 50-150 km, disc 300-1200 km / 500-3000 m; "
                     "reference-compatible Tsit5; %d coupling steps of 10 yr per member (the 10 kyr horizon "
@@ -505,19 +533,62 @@ def ensemble_leg(n_members=256, n_updates=10):
     }
 
 
-def serve_leg(lams=(10, 30, 100, 300, 1000, 2000), n_req=48, reserve_gb=8.0):
-    """Continuous batching: Poisson arrivals at rate lam of n_req solve
-    requests (sizes 64^2..1024^2 weighted 0.3/0.3/0.2/0.15/0.05, random-field
-    rheology, disc or dome load, horizon log-uniform 1-100 kyr scaled by
-    1/100), mixed form, through the solve server; latency = completion -
-    submission on the server clock.  The sequential plain-FP64 comparison
-    replays the same arrivals through one FIFO server whose service times
-    are measured per size (set-up + updates x time per update, FP64)."""
-    from fastisostasy_gb300 import workloads as W
+def _fp64_solve(wl, n):
+    """One request solved alone in the plain FP64 form: handle set-up, then
+    isos_update every dtt to t_end (the served solve's sequence)."""
     from fastisostasy_gb300.isostasy import Domain
-    from fastisostasy_gb300.serve import Server
     from fastisostasy_gb300 import _lib
-    wls = [W.serve_request(i) for i in range(n_req)]
+    d = Domain(wl.params, n, n, wl.dx, precision=0)
+    f = wl.padded_fields(d.nx, d.ny)
+    if f:
+        d.set_fields(**f)
+    b = _lib.FiBsl()
+    b.method, b.constant_ocean_surface = 0, 1
+    b.A_ocean_pd = b.A_ocean_now = 3.625e14
+    d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+    t = 0.0
+    while t < wl.t_end:
+        t = min(t + wl.dtt, wl.t_end)
+        d.update(wl.H_final, t, b)
+    w = d.crop(d.field("w"))
+    d.close()
+    return w
+
+
+def _sequential_fp64(wls, arrivals):
+    """A single FIFO worker that solves each request in FP64 as it arrives
+    (real time): latency = completion - arrival."""
+    t0 = time.perf_counter()
+    lat = []
+    for wl, a in zip(wls, arrivals):
+        now = time.perf_counter() - t0
+        if now < a:
+            time.sleep(a - now)
+        _fp64_solve(wl, wl.nx_ice)
+        lat.append(time.perf_counter() - t0 - a)
+    span = time.perf_counter() - t0 - arrivals[0]
+    lat = np.array(lat) * 1e3
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "throughput_req_per_s": len(wls) / span}
+
+
+def serve_leg(lams=(10, 30, 100, 300, 1000, 2000), n_req=48, reserve_gb=8.0, n_long=6):
+    """Continuous batching (configuration 5): Poisson arrivals at rate lam of
+    n_req solve requests whose sizes 64^2..1024^2 come in the weights
+    0.3/0.3/0.2/0.15/0.05 by quota (so a stream of 48 holds three 1024^2
+    requests), random-field rheology, disc or dome load, horizon
+    log-uniform 1-100 kyr scaled by 1/100, mixed form, through the solve
+    server; latency = completion - submission on the server clock.  Beside
+    each rate, the same arrivals served by one FIFO worker that solves every
+    request in the plain FP64 form as it arrives, actually run.  A second
+    stream of n_long requests (64^2..256^2) keeps the unscaled 1-100 kyr
+    horizons: served together, against the same requests solved one after
+    another in FP64, with each served result's difference from its FP64
+    solve."""
+    from fastisostasy_gb300 import workloads as W
+    from fastisostasy_gb300.serve import Server
+    sizes = W.serve_sizes(n_req)
+    wls = [W.serve_request(i, n=sizes[i]) for i in range(n_req)]
     srv = Server(max_inflight=64, reserve_gb=reserve_gb)
     preps = [srv.prepare(wl, precision=1) for wl in wls]
     # warm-up: one short request per size (kernel attributes, first captures)
@@ -549,49 +620,35 @@ def serve_leg(lams=(10, 30, 100, 300, 1000, 2000), n_req=48, reserve_gb=8.0):
         levels.append({"lambda_per_s": lam, "p50_ms": float(np.percentile(lat, 50)),
                        "p99_ms": float(np.percentile(lat, 99)), "throughput_req_per_s": n_req / span,
                        "arrivals": arr})
+    # the unscaled-horizon stream, served together (a burst)
+    long_sizes = [64, 128, 256, 64, 128, 256][:n_long]
+    lwls = [W.serve_request(1000 + i, horizon_scale=1.0, n=long_sizes[i]) for i in range(n_long)]
+    t0 = srv.clock()
+    lids = [srv.submit(wl, precision=1) for wl in lwls]
+    linfo = [srv.wait(i, 1200.0) for i in lids]
+    lres = [srv.result(i)[0] for i in lids]
+    served_span = max(f["t_done"] for f in linfo) - t0
     srv.close()
-    # sequential plain FP64: measured service time per size
-    cost = {}
-    for wl in wls:
-        n = wl.nx_ice
-        if n in cost:
-            continue
-        a = time.perf_counter()
-        d = Domain(wl.params, n, n, wl.dx, precision=0)
-        f = wl.padded_fields(d.nx, d.ny)
-        if f:
-            d.set_fields(**f)
-        b = _lib.FiBsl()
-        b.method, b.constant_ocean_surface = 0, 1
-        b.A_ocean_pd = b.A_ocean_now = 3.625e14
-        d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
-        setup = time.perf_counter() - a
-        for k in range(2):
-            d.update(wl.H_final, 10.0 * (k + 1), b)
-        a = time.perf_counter()
-        for k in range(4):
-            d.update(wl.H_final, 30.0 + 10.0 * k, b)
-        cost[n] = (setup, (time.perf_counter() - a) / 4)
-        d.close()
-    service = np.array([cost[wl.nx_ice][0] + np.ceil(wl.t_end / wl.dtt) * cost[wl.nx_ice][1] for wl in wls])
+    # sequential plain FP64, actually run: the same arrivals, one FIFO worker
     for lv in levels:
         arr = lv.pop("arrivals")
-        t_free, lat = 0.0, []
-        for a_k, s_k in zip(arr, service):
-            start = max(a_k, t_free)
-            t_free = start + s_k
-            lat.append(t_free - a_k)
-        lat = np.array(lat) * 1e3
-        lv["sequential_fp64"] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                                 "throughput_req_per_s": n_req / (t_free - arr[0])}
-    sizes = {}
-    for wl in wls:
-        sizes[wl.nx_ice] = sizes.get(wl.nx_ice, 0) + 1
-    return {"workload": "serve stream: %d requests per rate, sizes %s, mixed form, RK4 true stages dt=1 yr, "
+        lv["sequential_fp64"] = _sequential_fp64(wls, arr - arr[0])
+    a = time.perf_counter()
+    lerr = []
+    for wl, w32 in zip(lwls, lres):
+        w64 = _fp64_solve(wl, wl.nx_ice)
+        lerr.append(float(np.abs(w32 - w64).max() / max(np.abs(w64).max(), 1e-300)))
+    seq_span = time.perf_counter() - a
+    count = {n: sizes.count(n) for n in sorted(set(sizes))}
+    return {"workload": "serve stream: %d requests per rate, sizes %s by quota, mixed form, RK4 true stages dt=1 yr, "
                         "coupling 10 yr, horizon log-uniform 1-100 kyr x 1/100 (mean %.0f yr)"
-                        % (n_req, sizes, float(np.mean([w.t_end for w in wls]))),
+                        % (n_req, count, float(np.mean([w.t_end for w in wls]))),
             "levels": levels,
-            "sequential_fp64_service_s": {str(k): {"setup": v[0], "per_update": v[1]} for k, v in cost.items()}}
+            "unscaled_horizons": {
+                "requests": [{"n": wl.nx_ice, "horizon_yr": wl.t_end, "latency_ms": 1e3 * (f["t_done"] - f["t_submit"]),
+                              "err_mixed_vs_fp64": e} for wl, f, e in zip(lwls, linfo, lerr)],
+                "served_together_s": served_span, "sequential_fp64_s": seq_span,
+                "speedup": seq_span / served_span}}
 
 
 def scale_leg(sizes=(1024, 2048), n_updates=4):

@@ -847,6 +847,8 @@ template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
     g.p2 = h->eng_P2;
     g.spy = h->spy;
     g.norm_scale = 1.0 / (double)(float)((long long)h->nx * h->ny);
+    g.norm_scale_f = (float)g.norm_scale;
+    g.fcf = flex_coef_f32(h->fc);
     g.trace = h->trace;
     cudaError_t le = cudaSuccess;
     PROF(h, K_ENGINE, le = engine_launch<T>(g, h->eng_grid, h->eng_smem, h->s));
@@ -1200,13 +1202,14 @@ int fi_engine_trace(fi_handle* h, unsigned long long* out, int n)
     if (!h) return FI_E_ARG;
     if (!h->trace) {
         int rc;
-        if ((rc = dalloc(h, &h->trace, 64 * sizeof(unsigned long long)))) return rc;
+        if ((rc = dalloc(h, &h->trace, 256 * sizeof(unsigned long long)))) return rc;
+        CK(cudaMemsetAsync(h->trace, 0, 256 * sizeof(unsigned long long), h->s));
         CK(cudaStreamSynchronize(h->s));
         return FI_OK;
     }
     if (!out) return FI_OK;
     CK(cudaStreamSynchronize(h->s));
-    CK(cudaMemcpy(out, h->trace, (n < 64 ? n : 64) * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out, h->trace, (n < 256 ? n : 256) * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
     return FI_OK;
 }
 

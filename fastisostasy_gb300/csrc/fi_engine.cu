@@ -128,12 +128,29 @@ template <typename T> __device__ __forceinline__ double corner_mean_dev(const T*
     return corner_mean_of(a, nx, ny);
 }
 
+// Phase tracing (fi_engine_trace): block 0 stamps %globaltimer at phase and
+// sub-phase boundaries of the first RK4 step; s_trk < 0 when not tracing.
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__shared__ int s_trk;
+constexpr int kTraceLen = 256;
+__device__ __forceinline__ void tmark(unsigned long long* tr)
+{
+    if (threadIdx.x == 0 && s_trk >= 0 && s_trk < kTraceLen) tr[s_trk++] = gtimer();
+}
+
 // ---------------------------------------------------------------------------
 // Phase A: one item = output rows j0 .. j0+RA-1 (full width).
 // ---------------------------------------------------------------------------
 template <typename T, int RA, int FM>
-__device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsigned char* smem, const EngTw<T>& tw)
+__device__ void phase_a(const EngineArgs& g, int j0, int stage, float sdf_in, unsigned char* smem,
+                        const EngTw<T>& tw)
 {
+    static_assert(std::is_same<T, float>::value, "the step engine runs the mixed form only");
     typedef typename vec2<T>::type C2;
     const int nx = g.p.nx, ny = g.p.ny, hh = g.p.h;
     const int tid = threadIdx.x;
@@ -147,31 +164,24 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
     C2* b0 = reinterpret_cast<C2*>(Mxyx + (size_t)(RA + 2) * nx);
     C2* b1 = b0 + (size_t)RA * hh;
 
-    const T* rprev = stage > 0 ? (const T*)g.raw[stage - 1] : nullptr;
-    __shared__ double s_cm;
-    // y = x + a h spy (raw - cm): the scale s, the same arithmetic in every
-    // thread, and the corner mean cm of raw_{s-1}
-    const double sd = stage > 0 ? c_rk4_a[stage] * h * g.spy : 0.0;
-    // In the mixed form cm cancels in the level-0 differences and enters only
-    // the mantle term: thread 0 issues the four corner loads now and forms
-    // the mean after the level-0 loop, so their L2 latency hides behind it.
+    const float* rprev = stage > 0 ? (const float*)g.raw[stage - 1] : nullptr;
+    __shared__ float s_cmf;
+    // y = x + a h spy (raw - cm): the float scale sdf_in = a h spy and the
+    // corner mean cm of raw_{s-1}.  GB300 runs FP64 instructions
+    // (conversions included) at 1/64 of the FP32 rate, so no thread but
+    // thread 0 executes any here: the scale and the coefficients come in as
+    // floats (sdf_in, g.fcf).  cm cancels in the level-0 differences and
+    // enters only the mantle term: thread 0 issues the four corner loads now
+    // and forms the mean after the level-0 loop, so their L2 latency hides
+    // behind it.
     float cf[4] = {0.f, 0.f, 0.f, 0.f};
-    if constexpr (std::is_same<T, float>::value) {
-        if (tid == 0 && rprev) {
-            const size_t last = (size_t)(ny - 1) * nx;
-            const float* q[4] = {(const float*)rprev, (const float*)rprev + last + nx - 1,
-                                 (const float*)rprev + last, (const float*)rprev + nx - 1};
+    if (tid == 0 && rprev) {
+        const size_t last = (size_t)(ny - 1) * nx;
+        const float* q[4] = {rprev, rprev + last + nx - 1, rprev + last, rprev + nx - 1};
 #pragma unroll
-            for (int c = 0; c < 4; ++c) asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(cf[c]) : "l"(q[c]));
-        }
-    } else {
-        if (tid == 0) s_cm = stage > 0 ? corner_mean_of(rprev, nx, ny) : 0.0;
-        __syncthreads();
+        for (int c = 0; c < 4; ++c) asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(cf[c]) : "l"(q[c]));
     }
-    const double cmd_early = std::is_same<T, float>::value ? 0.0 : s_cm;   // plain form only
-    // float copies made once: every FP64 instruction (conversions included)
-    // costs the mixed form 64 FP32 slots on this GPU
-    const float sdf = (float)sd, cmant = (float)g.fc.coef_mantle;
+    const float sdf = sdf_in, cmant = g.fcf.coef_mantle;
 
     // level 0: forward differences along x (dX) and y (dY)
     for (int r = tw.wx.r0, i = tw.wx.i0; r < RA + 4; tw.wx.next(r, i)) {
@@ -179,55 +189,36 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         if (gj < 0 || gj >= ny) continue;
         const size_t c0 = (size_t)gj * nx + i;
         if (i < nx - 1) {
-            if constexpr (std::is_same<T, float>::value) {
-                float v = (g.xhi[c0 + 1] - g.xhi[c0]) + (g.xlo[c0 + 1] - g.xlo[c0]);
-                if (rprev) v += sdf * (rprev[c0 + 1] - rprev[c0]);
-                dX[(size_t)r * nx + i] = v;
-            } else {
-                double y1 = g.x[c0 + 1], y0 = g.x[c0];
-                if (rprev) {
-                    y1 += sd * ((double)rprev[c0 + 1] - cmd_early);
-                    y0 += sd * ((double)rprev[c0] - cmd_early);
-                }
-                dX[(size_t)r * nx + i] = y1 - y0;
-            }
+            float v = (g.xhi[c0 + 1] - g.xhi[c0]) + (g.xlo[c0 + 1] - g.xlo[c0]);
+            if (rprev) v += sdf * (rprev[c0 + 1] - rprev[c0]);
+            dX[(size_t)r * nx + i] = v;
         }
         if (r < RA + 3 && gj + 1 < ny) {
             const size_t c1 = c0 + nx;
-            if constexpr (std::is_same<T, float>::value) {
-                float v = (g.xhi[c1] - g.xhi[c0]) + (g.xlo[c1] - g.xlo[c0]);
-                if (rprev) v += sdf * (rprev[c1] - rprev[c0]);
-                dY[(size_t)r * nx + i] = v;
-            } else {
-                double y1 = g.x[c1], y0 = g.x[c0];
-                if (rprev) {
-                    y1 += sd * ((double)rprev[c1] - cmd_early);
-                    y0 += sd * ((double)rprev[c0] - cmd_early);
-                }
-                dY[(size_t)r * nx + i] = y1 - y0;
-            }
+            float v = (g.xhi[c1] - g.xhi[c0]) + (g.xlo[c1] - g.xlo[c0]);
+            if (rprev) v += sdf * (rprev[c1] - rprev[c0]);
+            dY[(size_t)r * nx + i] = v;
         }
     }
-    if constexpr (std::is_same<T, float>::value) {
-        if (tid == 0) s_cm = rprev ? corner_mean((double)cf[0], (double)cf[1], (double)cf[2], (double)cf[3]) : 0.0;
-    }
+    if (tid == 0) s_cmf = rprev ? (float)corner_mean((double)cf[0], (double)cf[1], (double)cf[2], (double)cf[3]) : 0.f;
     __syncthreads();
-    const double cmd = s_cm;
-    const float cmdf = (float)cmd;
-    const T inv_dx = (T)g.fc.inv_dx, inv_2dx = (T)g.fc.inv_2dx, inv_dx2 = (T)g.fc.inv_dx2;
-    const T inv_dy = (T)g.fc.inv_dy, inv_2dy = (T)g.fc.inv_2dy, inv_dy2 = (T)g.fc.inv_dy2;
+    tmark(g.trace);
+    const float inv_dx = g.fcf.inv_dx, inv_2dx = g.fcf.inv_2dx, inv_dx2 = g.fcf.inv_dx2;
+    const float inv_dy = g.fcf.inv_dy, inv_2dy = g.fcf.inv_2dy, inv_dy2 = g.fcf.inv_dy2;
+    const float cmdf = s_cmf;
     for (int r = tw.wx.r0, i = tw.wx.i0; r < RA + 4; tw.wx.next(r, i)) {
         const int gj = j0 - 2 + r;
         if (gj < 0 || gj >= ny) continue;
-        const T* d = dX + (size_t)r * nx;
-        T v;
+        const float* d = dX + (size_t)r * nx;
+        float v;
         if (i == 0) v = d[0] * inv_dx;
         else if (i == nx - 1) v = d[nx - 2] * inv_dx;
         else v = (d[i] + d[i - 1]) * inv_2dx;
         Wx[(size_t)r * nx + i] = v;
     }
     __syncthreads();
-    const T nu = (T)g.fc.nu, omn = (T)g.fc.one_minus_nu;
+    tmark(g.trace);
+    const float nu = g.fcf.nu, omn = g.fcf.one_minus_nu;
     for (int m = tw.wx.r0, i = tw.wx.i0; m < RA + 2; tw.wx.next(m, i)) {
         const int r = m + 1;
         const int gj = j0 - 2 + r;
@@ -244,13 +235,14 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         if (gj == 0) wyy = (dY[ri + nx] - dY[ri]) * inv_dy2;
         else if (gj == ny - 1) wyy = (dY[ri - nx] - dY[ri - 2 * nx]) * inv_dy2;
         else wyy = (dY[ri] - dY[ri - nx]) * inv_dy2;
-        const T Dl = g.D_T<T>()[(size_t)gj * nx + i];
         const size_t mi = (size_t)m * nx + i;
+        const float Dl = ((const float*)g.D)[(size_t)gj * nx + i];
         Mxx[mi] = -Dl * (wxx + nu * wyy);
         Myy[mi] = -Dl * (wyy + nu * wxx);
         Mxy[mi] = (-Dl * omn) * wxy;
     }
     __syncthreads();
+    tmark(g.trace);
     for (int m = tw.wx.r0, i = tw.wx.i0; m < RA + 2; tw.wx.next(m, i)) {
         const int gj = j0 - 1 + m;
         if (gj < 0 || gj >= ny) continue;
@@ -262,8 +254,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         Mxyx[(size_t)m * nx + i] = v;
     }
     __syncthreads();
-    const T* q0 = g.q0_T<T>();
-    const T* i2e = g.inv2eta_T<T>();
+    tmark(g.trace);
     for (int o = tw.wx.r0, i = tw.wx.i0; o < RA; tw.wx.next(o, i)) {
         const int gj = j0 + o;
         T fv = (T)0;
@@ -282,26 +273,21 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
             else if (gj == ny - 1) my_yy = ((Myy[mi] - (T)2 * Myy[mi - nx]) + Myy[mi - 2 * nx]) * inv_dy2;
             else my_yy = ((Myy[mi + nx] - (T)2 * Myy[mi]) + Myy[mi - nx]) * inv_dy2;
             const size_t c = (size_t)gj * nx + i;
-            T p = (T)0;
+            float p = 0.f;
             if (g.mask[c]) {
                 // q0 + (-g rho_m) (y - w_ref) with y the stage state
-                if constexpr (std::is_same<T, float>::value) {
-                    float dy = (g.xhi[c] - g.wrefhi[c]) + (g.xlo[c] - g.wreflo[c]);
-                    if (rprev) dy += sdf * (rprev[c] - cmdf);
-                    p = q0[c] + cmant * dy;
-                } else {
-                    double y = g.x[c];
-                    if (rprev) y += sd * ((double)rprev[c] - cmd);
-                    p = (double)q0[c] + g.fc.coef_mantle * (y - g.wref[c]);
-                }
+                float dy = (g.xhi[c] - g.wrefhi[c]) + (g.xlo[c] - g.wreflo[c]);
+                if (rprev) dy += sdf * (rprev[c] - cmdf);
+                p = ((const float*)g.q0)[c] + cmant * dy;
             }
-            fv = (((p + mx_xx) + (T)2 * mxy_xy) + my_yy) * i2e[c];
+            fv = (((p + mx_xx) + 2.f * mxy_xy) + my_yy) * ((const float*)g.inv2eta)[c];
         }
         // pack the real row as complex pairs for the half-length FFT
         T* bz = reinterpret_cast<T*>(b0 + (size_t)o * hh);
         bz[i] = fv;
     }
     __syncthreads();
+    tmark(g.trace);
     C2* r = block_fft<T, true, FM>(b0, b1, g.p.row.d, RA, hh, tw.row, -1);
     const C2* rtw = tw.rtw;
     // column-major: the strided stores do not hold the block up, and phase B
@@ -320,6 +306,7 @@ __device__ void phase_a(const EngineArgs& g, int j0, int stage, double h, unsign
         ST[(size_t)k * ny + gj] = cadd(E, cmul(rtw[k], O));
     }
     __syncthreads();
+    tmark(g.trace);
 }
 
 // ---------------------------------------------------------------------------
@@ -342,6 +329,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
         b0[c * ny + l] = (k <= g.p.h) ? ((const C2*)g.ST)[(size_t)k * ny + l] : mk2<T>((T)0, (T)0);
     }
     __syncthreads();
+    tmark(g.trace);
     C2* r = block_fft<T, true, FM>(b0, b1, g.p.col.d, CB, ny, tw.col, -1);
     const T* mA = g.mA_T<T>();
     const T* mB = g.mB_T<T>();
@@ -376,6 +364,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
         }
     }
     __syncthreads();
+    tmark(g.trace);
     C2* other = (r == b0) ? b1 : b0;
     C2* q = block_fft<T, true, FM>(r, other, g.p.col.d, CB, ny, tw.col, +1);
     for (int e = tid; e < CB * ny; e += nt) {
@@ -384,6 +373,7 @@ __device__ void phase_b(const EngineArgs& g, int k0, int CB, unsigned char* smem
         if (k <= g.p.h) S[(size_t)l * g.p.sp + k] = q[c * ny + l];
     }
     __syncthreads();
+    tmark(g.trace);
 }
 
 // ---------------------------------------------------------------------------
@@ -414,8 +404,11 @@ __device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem
         b0[e] = z;
     }
     __syncthreads();
+    tmark(g.trace);
     C2* r = block_fft<T, true, FM>(b0, b1, g.p.row.d, RC, hh, tw.row, +1);
-    const T scale = (T)g.norm_scale;
+    T scale;
+    if constexpr (std::is_same<T, float>::value) scale = g.norm_scale_f;
+    else scale = g.norm_scale;
     for (int o = tw.wh.r0, m = tw.wh.i0; o < RC; tw.wh.next(o, m)) {
         const int j = j0 + o;
         if (j >= ny) continue;
@@ -425,15 +418,10 @@ __device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem
         *reinterpret_cast<C2*>(out + (size_t)j * nx + 2 * m) = v;
     }
     __syncthreads();
+    tmark(g.trace);
 }
 
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned long long gtimer()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 // FM: the block-FFT index mode, FFT_POW2 when both transform lengths are
 // powers of two, else FFT_ANY
@@ -479,27 +467,42 @@ __global__ void __launch_bounds__(EngShape<RA>::threads, EngShape<RA>::per_sm) k
     }
     __syncthreads();
     const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
-    const bool tr = g.trace && lead;
-    int tk = 0;
-#define TRACE() do { if (tr && step == 0 && tk < 64) g.trace[tk++] = gtimer(); } while (0)
+    if (threadIdx.x == 0) s_trk = (g.trace && blockIdx.x == 0) ? 0 : -1;
+    __syncthreads();
+#define TRACE() tmark(g.trace)
+    // per-step scalars, computed by thread 0 (the only thread of the mixed
+    // form that executes FP64 instructions outside the state update)
+    __shared__ int s_go, s_last;
+    __shared__ double s_h;
+    __shared__ float s_sdf[4];   // float stage scales a_s h spy
+    __shared__ float s_cf[5];    // phase D: corner means of raw_1..4 and h/6 spy
     for (int step = 0; step < g.nsteps; ++step) {
         TRACE();
-        const double t = s_t;
-        if (!(s_ok && t < s_tf)) {   // uniform over the grid
+        if (threadIdx.x == 0) {
+            const double t = s_t;
+            s_go = s_ok && t < s_tf;
+            // step_rk4: h = min(dt, tf - t) (src/integrators.f90:62-63)
+            const double hh = fmin(s_dt, s_tf - t);
+            s_h = hh;
+            // now%w is read by nothing inside the engine: written in the last step only
+            s_last = step + 1 == g.nsteps || !(t + hh < s_tf);
+            for (int st = 0; st < 4; ++st) s_sdf[st] = st > 0 ? (float)(c_rk4_a[st] * hh * g.spy) : 0.f;
+        }
+        __syncthreads();
+        if (!s_go) {   // uniform over the grid
             if (lead) ctl->done = 1;
             return;
         }
-        // step_rk4: h = min(dt, tf - t) (src/integrators.f90:62-63)
-        const double h = fmin(s_dt, s_tf - t);
+        const double h = s_h;
         if (lead) {
             ctl->h = h;
             ctl->done = 0;
         }
-        // now%w is read by nothing inside the engine: written in the last step only
-        const bool last = step + 1 == g.nsteps || !(t + h < s_tf);
+        const bool last = s_last != 0;
         TRACE();
         for (int stage = 0; stage < 4; ++stage) {
-            for (int it = blockIdx.x; it < na; it += gridDim.x) phase_a<T, RA, FM>(g, it * RA, stage, h, smem, tw);
+            for (int it = blockIdx.x; it < na; it += gridDim.x)
+                phase_a<T, RA, FM>(g, it * RA, stage, s_sdf[stage], smem, tw);
             TRACE();
             grid.sync();
             TRACE();
@@ -517,10 +520,12 @@ __global__ void __launch_bounds__(EngShape<RA>::threads, EngShape<RA>::per_sm) k
         if (threadIdx.x == 0) {
             s_c[0] = h / 6;
             for (int s = 0; s < 4; ++s) s_c[1 + s] = corner_mean_of((const T*)g.raw[s], nx, ny);
+            for (int s = 0; s < 4; ++s) s_cf[s] = (float)s_c[1 + s];
+            s_cf[4] = (float)(s_c[0] * g.spy);
         }
         __syncthreads();
-        const float c1f = (float)s_c[1], c2f = (float)s_c[2], c3f = (float)s_c[3], c4f = (float)s_c[4];
-        const float scf = (float)(s_c[0] * g.spy);
+        const float c1f = s_cf[0], c2f = s_cf[1], c3f = s_cf[2], c4f = s_cf[3];
+        const float scf = s_cf[4];
         const T* r1 = (const T*)g.raw[0];
         const T* r2 = (const T*)g.raw[1];
         const T* r3 = (const T*)g.raw[2];
@@ -549,14 +554,18 @@ __global__ void __launch_bounds__(EngShape<RA>::threads, EngShape<RA>::per_sm) k
                 if (last) g.w[e] = v;
             }
         }
-        if (threadIdx.x == 0) s_t = t + h;   // read after the grid barrier below
-        if (lead) {
-            ctl->t = t + h;
-            ctl->n_accept++;
+        if (threadIdx.x == 0) {
+            const double tn = s_t + h;
+            s_t = tn;   // read after the grid barrier below
+            if (lead) {
+                ctl->t = tn;
+                ctl->n_accept++;
+            }
         }
         TRACE();
         grid.sync();
         TRACE();
+        if (threadIdx.x == 0 && step == 0) s_trk = -1;   // trace the first step only
     }
 #undef TRACE
 }

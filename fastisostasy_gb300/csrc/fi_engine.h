@@ -12,6 +12,7 @@ namespace fi {
 struct EngineArgs {
     Plan2D p;
     FlexCoef fc;                     // uniform spacing only
+    FlexCoefF fcf;                   // the same in float (mixed form: no per-thread conversions)
     double* x;                       // integrator state (double)
     double* w;                       // now%w
     float* xhi;                      // mixed form: x = xhi + xlo
@@ -36,6 +37,7 @@ struct EngineArgs {
     int p2;                          // both transform lengths are powers of two
     double spy;
     double norm_scale;               // 1 / (nx*ny*1.) as the reference normalises
+    float norm_scale_f;              // the same in float
     unsigned long long* trace;       // optional: %globaltimer at phase boundaries of the first step
 
     template <typename T> __device__ __forceinline__ const T* q0_T() const { return (const T*)q0; }

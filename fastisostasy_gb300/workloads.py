@@ -184,17 +184,33 @@ SERVE_SIZES = (64, 128, 256, 512, 1024)
 SERVE_WEIGHTS = (0.3, 0.3, 0.2, 0.15, 0.05)
 
 
-def serve_request(i: int, horizon_scale: float = 0.01, dx: float = 25e3) -> Workload:
+def serve_sizes(n_req: int, seed: int = 77) -> list:
+    """Grid sizes of a stream of n_req requests in SERVE_WEIGHTS proportions
+    by quota (largest remainders), in a seeded random order: every size
+    appears at its weight even in a short stream (a draw of 48 can miss the
+    5 % of 1024^2 requests entirely)."""
+    quota = [w * n_req for w in SERVE_WEIGHTS]
+    counts = [int(q) for q in quota]
+    for k in sorted(range(len(quota)), key=lambda k: counts[k] - quota[k])[: n_req - sum(counts)]:
+        counts[k] += 1
+    sizes = [n for n, c in zip(SERVE_SIZES, counts) for _ in range(c)]
+    np.random.default_rng(seed).shuffle(sizes)
+    return [int(v) for v in sizes]
+
+
+def serve_request(i: int, horizon_scale: float = 0.01, dx: float = 25e3, n: Optional[int] = None) -> Workload:
     """Request i of the serving stream: n drawn from SERVE_SIZES with
     SERVE_WEIGHTS, seeded random-field mantle viscosity (log10 eta: mean 21,
     std 0.25, correlation 500 km) and lithosphere thickness (mean 85 km, std
     15 km, clipped to 50-120 km, mapped to rigidity with E = 66 GPa,
     nu = 0.28), a disc or a parabolic dome load, horizon log-uniform in
-    1-100 kyr times `horizon_scale`.  RK4 with true stages at dt = 1 yr,
+    1-100 kyr times `horizon_scale` (`n` overrides the drawn size, for
+    quota-sized streams).  RK4 with true stages at dt = 1 yr,
     coupling every 10 yr; the spacing keeps dt = 1 yr inside RK4's stability
     region for every draw."""
     rng = np.random.default_rng(5000 + i)
-    n = int(rng.choice(SERVE_SIZES, p=SERVE_WEIGHTS))
+    drawn = int(rng.choice(SERVE_SIZES, p=SERVE_WEIGHTS))
+    n = drawn if n is None else int(n)
     horizon = float(np.exp(rng.uniform(np.log(1e3), np.log(1e5)))) * horizon_scale
     horizon = max(10.0, 10.0 * np.ceil(horizon / 10.0))
     L = n * dx

@@ -359,8 +359,10 @@ long long fi_launch_count(const fi_handle* h);
  * 12 upd_load, 13 upd_end. */
 int fi_profile(fi_handle* h, int enable);
 /* Step-engine phase timestamps (%globaltimer, ns) of the first RK4 step of
- * the last update: the first call enables tracing, later calls copy up to n
- * timestamps into `out`. */
+ * the last update, taken by block 0 at every phase and sub-phase boundary
+ * (up to 256): the first call enables tracing (for updates launched after
+ * it: a CUDA graph captured earlier keeps running untraced), later calls
+ * copy up to n timestamps into `out`. */
 int fi_engine_trace(fi_handle* h, unsigned long long* out, int n);
 int fi_profile_read(fi_handle* h, double* ms, long long* counts, int n);
 
