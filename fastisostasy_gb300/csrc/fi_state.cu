@@ -180,6 +180,24 @@ template <typename T> __device__ __forceinline__ double block_corner_mean(const 
     return s_cm;
 }
 
+// Per-block scalars of the mixed-form update kernels.  GB300 executes FP64
+// instructions, conversions included, at 1/64 of the FP32 rate: a preamble
+// of ten FP64 operations in every thread costs more than the few cells each
+// thread then updates.  Thread 0 evaluates the scalars (in FP64, as before)
+// and the block reads the float results from shared memory.
+struct BlockScal {
+    float f[6];
+    double d;
+};
+template <typename F> __device__ __forceinline__ BlockScal block_scalars(F&& eval)
+{
+    __shared__ BlockScal s_bs;
+    __syncthreads();
+    if (threadIdx.x == 0) s_bs = eval();
+    __syncthreads();
+    return s_bs;
+}
+
 __device__ __forceinline__ bool in_crop(const Dom& d, int i, int j)
 {
     return i >= d.i0 && i < d.i0 + d.nxi && j >= d.j0 && j < d.j0 + d.nyi;
@@ -360,16 +378,22 @@ k_rk_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __re
            double a, int nx, int ny, double spy)
 {
     if (c->done) return;
-    const double cm = c->plain ? 0.0 : block_corner_mean(raw, nx, ny);
-    const double ah = a * c->h;
     const size_t n = (size_t)nx * ny;
     if (sizeof(T) == 8) {
+        const double cm = c->plain ? 0.0 : block_corner_mean(raw, nx, ny);
+        const double ah = a * c->h;
         for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
             const double k = ((double)raw[e] - cm) * spy;
             y[e] = x[e] + ah * k;
         }
     } else {
-        const float cmf = (float)cm, sc = (float)(ah * spy);
+        const BlockScal bs = block_scalars([&] {
+            BlockScal r;
+            r.f[0] = c->plain ? 0.f : (float)corner_mean_of(raw, nx, ny);
+            r.f[1] = (float)((a * c->h) * spy);
+            return r;
+        });
+        const float cmf = bs.f[0], sc = bs.f[1];
         for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
             y[e] = x[e] + (double)(((float)raw[e] - cmf) * sc);
     }
@@ -406,7 +430,13 @@ k_rk4_final(Ctl* c, double* __restrict__ x, double* __restrict__ w, const T* __r
             w[e] = v;
         }
     } else {
-        const float f1 = (float)c1, f2 = (float)c2, f3 = (float)c3, f4 = (float)c4, sc = (float)(h6 * spy);
+        const BlockScal bs = block_scalars([&] {
+            BlockScal r;
+            r.f[0] = (float)c1; r.f[1] = (float)c2; r.f[2] = (float)c3; r.f[3] = (float)c4;
+            r.f[4] = (float)(h6 * spy);
+            return r;
+        });
+        const float f1 = bs.f[0], f2 = bs.f[1], f3 = bs.f[2], f4 = bs.f[3], sc = bs.f[4];
         for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
             const float k = ((((float)r1[e] - f1) + 2.f * ((float)r2[e] - f2)) + 2.f * ((float)r3[e] - f3)) +
                             ((float)r4[e] - f4);
@@ -431,17 +461,23 @@ k_euler_final(const Ctl* __restrict__ c, double* __restrict__ x, double* __restr
               int nx, int ny, double spy)
 {
     if (c->done) return;
-    const double c1 = c->plain ? 0.0 : block_corner_mean(r1, nx, ny);
-    const double h = c->h;
     const size_t n = (size_t)nx * ny;
     if (sizeof(T) == 8) {
+        const double c1 = c->plain ? 0.0 : block_corner_mean(r1, nx, ny);
+        const double h = c->h;
         for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
             const double v = x[e] + h * (((double)r1[e] - c1) * spy);
             x[e] = v;
             w[e] = v;
         }
     } else {
-        const float f1 = (float)c1, sc = (float)(h * spy);
+        const BlockScal bs = block_scalars([&] {
+            BlockScal r;
+            r.f[0] = c->plain ? 0.f : (float)corner_mean_of(r1, nx, ny);
+            r.f[1] = (float)(c->h * spy);
+            return r;
+        });
+        const float f1 = bs.f[0], sc = bs.f[1];
         for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
             const double v = x[e] + (double)(((float)r1[e] - f1) * sc);
             x[e] = v;
@@ -585,10 +621,15 @@ __device__ __forceinline__ void ts_fused_body(Dom d, const float* __restrict__ r
     Ctl* c = d.ctl;
     if (c->done) return;
     const double dt = c->h;
-    const double cm = c->plain ? 0.0 : block_corner_mean(raw, d.nx, d.ny);
-    const float cxf = (float)(((dt * c_ts_b[0] + dt * c_ts_b[3]) + dt * c_ts_b[4]) + dt * c_ts_b[5]);
-    const float ce = (float)(dt * c_ts_b[5] - dt * c_ts_bh[5]);
-    const float cmf = (float)cm, spyf = (float)d.spy;
+    const BlockScal bs = block_scalars([&] {
+        BlockScal r;
+        r.f[0] = (float)(((dt * c_ts_b[0] + dt * c_ts_b[3]) + dt * c_ts_b[4]) + dt * c_ts_b[5]);
+        r.f[1] = (float)(dt * c_ts_b[5] - dt * c_ts_bh[5]);
+        r.f[2] = c->plain ? 0.f : (float)corner_mean_of(raw, d.nx, d.ny);
+        r.f[3] = (float)d.spy;
+        return r;
+    });
+    const float cxf = bs.f[0], ce = bs.f[1], cmf = bs.f[2], spyf = bs.f[3];
     float m1 = 0.f, m2 = 0.f, s2 = 0.f;
     // unrolled so that several cells' loads are in flight per thread
 #pragma unroll 4
@@ -617,10 +658,17 @@ __device__ __forceinline__ void ts_commit_pair_body(Dom d, const float* __restri
 {
     const Ctl* c = d.ctl;
     if (c->done || !c->accepted) return;
-    const double dt = c->h;
-    const double cx = ((dt * c_ts_b[0] + dt * c_ts_b[3]) + dt * c_ts_b[4]) + dt * c_ts_b[5];
-    const float cxf = (float)cx;
-    const float cmf = c->plain ? 0.f : (float)block_corner_mean(raw, d.nx, d.ny), spyf = (float)d.spy;
+    const BlockScal bs = block_scalars([&] {
+        const double dt = c->h;
+        BlockScal r;
+        r.d = ((dt * c_ts_b[0] + dt * c_ts_b[3]) + dt * c_ts_b[4]) + dt * c_ts_b[5];
+        r.f[0] = (float)r.d;
+        r.f[1] = c->plain ? 0.f : (float)corner_mean_of(raw, d.nx, d.ny);
+        r.f[2] = (float)d.spy;
+        return r;
+    });
+    const double cx = bs.d;
+    const float cxf = bs.f[0], cmf = bs.f[1], spyf = bs.f[2];
 #pragma unroll 4
     for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
         const float k = (raw[e] - cmf) * spyf;
