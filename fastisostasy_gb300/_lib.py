@@ -33,7 +33,8 @@ EXPORTS = ["fi_create", "fi_destroy", "fi_dims", "fi_set_fields", "fi_set_kernel
            "fi_serve_result", "fi_serve_clock", "fi_serve_destroy", "fi_batch_update", "fi_batch_synchronize",
            "fi_batch_create", "fi_batch_step", "fi_batch_wait", "fi_batch_destroy", "fi_elva_disk",
            "fi_batch_set_priority", "fi_set_rheology", "fi_output_bytes", "fi_output_async",
-           "fi_output_wait", "fi_batch_autotune", "fi_set_stream", "fi_set_max_rejections", "fi_serve_cancel"]
+           "fi_output_wait", "fi_batch_autotune", "fi_set_stream", "fi_set_max_rejections", "fi_serve_cancel",
+           "fi_metrics_json"]
 
 PROFILE_KERNELS = ["flexure", "rows_fwd", "cols_hartley", "rows_inv", "conv_rows_fwd", "conv_cols",
                    "conv_rows_inv", "rk_stage", "rk_final", "upd_begin", "upd_masks", "upd_litho",
@@ -133,6 +134,7 @@ def load(build_if_missing: bool = True):
     L.fi_update_async.argtypes = [H, C.c_void_p, C.c_double, C.POINTER(FiBsl)]
     L.fi_synchronize.argtypes = [H]
     L.fi_set_max_rejections.argtypes = [H, C.c_int64]
+    L.fi_metrics_json.argtypes = [H, C.c_char_p, C.c_size_t]
     L.fi_bsl_update.argtypes = [C.POINTER(FiBsl), C.c_double]
     L.fi_get_field.argtypes = [H, C.c_int, _dp]
     L.fi_get_scalars.argtypes = [H, _dp]

@@ -7,6 +7,7 @@
 // (src/fastisostasy.f90:731-872).  There is no CPU compute path: every
 // per-cell operation of init_state/update runs on the device.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstddef>
@@ -20,6 +21,8 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/fi_gpu.h"
 #include "fi_engine.h"
 #include "fi_init.h"
@@ -28,6 +31,23 @@
 #include "fi_state.h"
 
 using namespace fi;
+
+namespace {
+
+// Host API ranges for timeline tools (NVTX: inert unless a tool is attached)
+// and the host-time accounting of the update calls.
+struct ApiRange {
+    explicit ApiRange(const char* name) { nvtxRangePushA(name); }
+    ~ApiRange() { nvtxRangePop(); }
+};
+struct UpdateClock {
+    fi_handle* h;
+    std::chrono::steady_clock::time_point t0;
+    explicit UpdateClock(fi_handle* hh);
+    ~UpdateClock();
+};
+
+}  // namespace
 
 namespace {
 
@@ -194,6 +214,8 @@ struct fi_handle {
     int Px = 0, Py = 0;
     int even = 1, uniform = 1;
     long long launches = 0;            // kernels enqueued by this handle
+    long long updates = 0;             // isos_update calls (fi_update, fi_update_async)
+    double host_update_s = 0.0;        // host time spent inside them (enqueue + copies + waits)
     // CUDA graphs of whole updates, keyed by (step count, diagnostics, ...)
     struct GraphEntry {
         long long key;
@@ -1285,6 +1307,7 @@ int fi_padded_dims(const fi_params* p, int nx_ice, int ny_ice, double dx, double
 int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy, const double* K_or_null,
               fi_handle** out)
 {
+    ApiRange nr("fi_create");
     if (!pin || !out) return FI_E_ARG;
     *out = nullptr;
     const fi_params& p = *pin;
@@ -1509,7 +1532,23 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
 
 int fi_destroy(fi_handle* h)
 {
+    ApiRange nr("fi_destroy");
     if (!h) return FI_OK;
+    // per-run metrics sink: one JSON line per handle, appended to the file
+    // FI_METRICS_FILE names
+    if (const char* path = getenv("FI_METRICS_FILE")) {
+        if (path[0]) {
+            char line[1024];
+            if (fi_metrics_json(h, line, sizeof(line)) == FI_OK) {
+                static std::mutex mu;
+                std::lock_guard<std::mutex> lk(mu);
+                if (FILE* f = fopen(path, "a")) {
+                    fprintf(f, "%s\n", line);
+                    fclose(f);
+                }
+            }
+        }
+    }
     if (h->s_out) cudaStreamSynchronize(h->s_out);
     if (h->s) {
         for (void* p : h->allocs) cudaFreeAsync(p, h->s);
@@ -1664,6 +1703,7 @@ int fi_init_ref(fi_handle* h, const double* z_bed, const double* H_ice, double b
 
 int fi_init_state(fi_handle* h, const double* z_bed, const double* H_ice, double time, fi_bsl* bsl)
 {
+    ApiRange nr("fi_init_state");
     // isos_init_state, src/fastisostasy.f90:596-660 (no restart file)
     if (!h || !z_bed || !H_ice || !bsl) return FI_E_ARG;
     const size_t ni = (size_t)h->nx_ice * h->ny_ice;
@@ -1714,9 +1754,20 @@ int fi_init_state(fi_handle* h, const double* z_bed, const double* H_ice, double
     return read_status(h, &st);
 }
 
+namespace {
+UpdateClock::UpdateClock(fi_handle* hh) : h(hh), t0(std::chrono::steady_clock::now()) {}
+UpdateClock::~UpdateClock()
+{
+    h->updates++;
+    h->host_update_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+}  // namespace
+
 int fi_update_async(fi_handle* h, const double* d_H_ice, double time, fi_bsl* bsl)
 {
+    ApiRange nr("fi_update_async");
     if (!h || !bsl) return FI_E_ARG;
+    UpdateClock uc(h);
     if (!h->state_ready) return fail(h, FI_E_STATE, "fi_update before fi_init_state");
     enqueue_args(h, time, bsl, bsl->method == 0 || bsl->method == 1);
     if (d_H_ice) {
@@ -1735,6 +1786,26 @@ int fi_set_max_rejections(fi_handle* h, int64_t max_per_update)
     return FI_OK;
 }
 
+int fi_metrics_json(fi_handle* h, char* buf, size_t len)
+{
+    if (!h || !buf || len == 0) return FI_E_ARG;
+    Ctl hc;
+    CK(cudaMemcpyAsync(&hc, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    const fi_params& p = h->p;
+    const int n = snprintf(buf, len,
+                           "{\"nx\": %d, \"ny\": %d, \"nx_ice\": %d, \"ny_ice\": %d, \"precision\": \"%s\", "
+                           "\"method\": %d, \"dt_method\": %d, \"stage_mode\": %d, \"step_engine\": %s, "
+                           "\"updates\": %lld, \"t\": %.17g, \"dt\": %.17g, \"n_accept\": %lld, \"n_reject\": %lld, "
+                           "\"n_attempt\": %lld, \"kernels_enqueued\": %lld, \"graphs_captured\": %d, "
+                           "\"host_update_ms\": %.6f, \"status\": %d}",
+                           h->nx, h->ny, h->nx_ice, h->ny_ice, mixed(h) ? "mixed" : "fp64", p.method, p.dt_method,
+                           p.stage_mode, h->engine_ok ? "true" : "false", h->updates, hc.t, hc.dt, hc.n_accept,
+                           hc.n_reject, hc.n_attempt, h->launches, (int)h->graphs.size(), 1e3 * h->host_update_s,
+                           hc.status);
+    return (n < 0 || (size_t)n >= len) ? FI_E_SIZE : FI_OK;
+}
+
 int fi_synchronize(fi_handle* h)
 {
     if (!h) return FI_E_ARG;
@@ -1744,7 +1815,9 @@ int fi_synchronize(fi_handle* h)
 
 int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_out* out)
 {
+    ApiRange nr("fi_update");
     if (!h || !H_ice || !bsl) return FI_E_ARG;
+    UpdateClock uc(h);
     if (!h->state_ready) return fail(h, FI_E_STATE, "fi_update before fi_init_state");
     const size_t ni = (size_t)h->nx_ice * h->ny_ice;
     int rc;
@@ -2528,6 +2601,7 @@ int fi_batch_set_priority(fi_batch* b, int level)
 
 int fi_batch_step(fi_batch* b, double time, fi_bsl* bsl)
 {
+    ApiRange nr("fi_batch_step");
     if (!b || !bsl) return FI_E_ARG;
     fi_handle* h0 = b->hs[0];
     const bool diag = time - h0->time_diag >= sp(1e-3);   // the same for every member (lockstep)

@@ -223,6 +223,13 @@ class Domain:
         self._check(self.L.fi_convolve(self.h, int(kernel), _dp(x), _dp(out)))
         return out
 
+    def metrics(self) -> dict:
+        """Run metrics of the handle (fi_metrics_json)."""
+        import json
+        buf = C.create_string_buffer(1024)
+        self._check(self.L.fi_metrics_json(self.h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
     def state_export(self) -> np.ndarray:
         buf = np.zeros(self.L.fi_state_size(self.h))
         self._check(self.L.fi_state_export(self.h, _dp(buf)))

@@ -170,6 +170,12 @@ module fastisostasy_gpu
             type(c_ptr), value :: h
             integer(c_int64_t), value :: max_per_update
         end function
+        integer(c_int) function fi_metrics_json(h, buf, len) bind(C, name="fi_metrics_json")
+            import
+            type(c_ptr), value :: h
+            character(kind=c_char), intent(out) :: buf(*)   ! NUL-terminated JSON line
+            integer(c_size_t), value :: len
+        end function
 
         ! ---- bsl_update (src/barysealevel.f90:195-252)
         integer(c_int) function fi_bsl_update(bsl, year_bp) bind(C, name="fi_bsl_update")

@@ -161,6 +161,16 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
 int fi_update_async(fi_handle* h, const double* d_H_ice, double time, fi_bsl* bsl);
 /* Waits for the handle's stream; returns the device status (FI_E_NAN, ...). */
 int fi_synchronize(fi_handle* h);
+/* Run metrics of a handle (no reference counterpart; the reference has no
+ * instrumentation beyond gprof): one JSON object, NUL-terminated, in buf —
+ * grid, form, integrator, updates made, model time and step, accepted and
+ * rejected steps, adaptive attempts (tsit54), kernels enqueued, CUDA graphs
+ * captured, host time inside the update calls, device status.  Waits for
+ * the handle's stream.  FI_E_SIZE when len is too small (1 KiB suffices).
+ * With the environment variable FI_METRICS_FILE set, fi_destroy appends
+ * this line to that file (a per-run metrics sink).  The host API calls
+ * also open NVTX ranges (fi_create, fi_update, ...) for timeline tools. */
+int fi_metrics_json(fi_handle* h, char* buf, size_t len);
 /* Step-control safety of the adaptive method (tsit54).  The reference
  * halves dt after a rejection without any floor (src/integrators.f90:196-198)
  * and reads dt_min (src/fastisostasy.f90:1008) without using it.  Here an

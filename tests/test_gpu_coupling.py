@@ -312,3 +312,30 @@ def test_c_driver_replays_reference_loop(tmp_path, precision):
     assert k_out == 4
     assert np.abs(rec[-1, 1 + n * n:1 + 2 * n * n]).max() > 1.0   # the disc has depressed the bed
     orc.close()
+
+
+def test_metrics_json_and_sink(tmp_path, monkeypatch):
+    """fi_metrics_json reports the handle's run (updates, accepted and
+    rejected steps, adaptive attempts, kernels, device status) as the
+    scalars give them (attempts = accepted + rejected); with FI_METRICS_FILE set, fi_destroy appends that
+    line to the file."""
+    import json
+    path = os.path.join(str(tmp_path), "metrics.jsonl")
+    monkeypatch.setenv("FI_METRICS_FILE", path)
+    wl = W.config1(48)
+    wl.params["stage_mode"] = 0
+    dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=1)
+    b = gpu_bsl()
+    dom.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+    for k in range(1, 5):
+        dom.update(wl.H_final, 10.0 * k, b)
+    m, sc = dom.metrics(), dom.scalars()
+    assert m["updates"] == 4 and m["t"] == sc["t"] == 40.0
+    assert m["n_accept"] == sc["n_accept"] > 0 and m["n_reject"] == sc["n_reject"]
+    assert m["n_attempt"] == m["n_accept"] + m["n_reject"]
+    assert m["kernels_enqueued"] > 0 and m["status"] == 0
+    assert m["precision"] == "mixed" and (m["nx"], m["ny"]) == (dom.nx, dom.ny)
+    dom.close()
+    with open(path) as fh:
+        lines = [json.loads(v) for v in fh.read().splitlines()]
+    assert lines[-1]["updates"] == 4 and lines[-1]["n_accept"] == m["n_accept"]
