@@ -593,6 +593,64 @@ def _sequential_fp64(wls, arrivals):
             "throughput_req_per_s": len(wls) / span}
 
 
+def ensemble_true_leg(n_members=64, n_updates=4, groups=2, mode="graph"):
+    """Configuration 4's members in Tsit5 with true stages (Dormand-Prince
+    5(4) with FSAL, the RHS at every stage state; no reference counterpart)
+    as one batched graph per coupling step, mixed form, against the same
+    members solved one after another in FP64: member-kyr/s, speed-up and the
+    per-member difference.  Members start at t = 30 yr after three untimed
+    updates, then n_updates coupling steps of 10 yr are timed."""
+    import torch
+    from fastisostasy_gb300 import workloads as W
+    from fastisostasy_gb300.isostasy import Domain
+    from fastisostasy_gb300.serve import Ensemble
+    from fastisostasy_gb300 import _lib
+    wls = [W.ensemble_member(i, stage_mode=1) for i in range(n_members)]
+    ens = Ensemble(wls, precision=1, mode=mode, groups=groups if mode == "graph" else 1)
+    ens.first_update(10.0)
+    ens.update(20.0)
+    ens.update(30.0)
+    ens.synchronize()
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    for k in range(n_updates):
+        ens.update(40.0 + 10.0 * k)
+    ens.synchronize()
+    batched_s = time.perf_counter() - a
+    w_mixed = [d.field("w") for d in ens.doms]
+    attempts = [d.scalars()["n_accept"] + d.scalars()["n_reject"] for d in ens.doms]
+    ens.close()
+    seq_s, w64 = 0.0, []
+    for wl in wls:
+        d = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=0)
+        f = wl.padded_fields(d.nx, d.ny)
+        if f:
+            d.set_fields(**f)
+        b = _lib.FiBsl()
+        b.method, b.constant_ocean_surface = 0, 1
+        b.A_ocean_pd = b.A_ocean_now = 3.625e14
+        d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+        for t in (10.0, 20.0, 30.0):
+            d.update(wl.H_final, t, b)
+        a = time.perf_counter()
+        for k in range(n_updates):
+            d.update(wl.H_final, 40.0 + 10.0 * k, b)
+        seq_s += time.perf_counter() - a
+        w64.append(d.field("w"))
+        d.close()
+    errs = np.array([float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300)) for x, y in zip(w_mixed, w64)])
+    mkyr = n_members * n_updates * 10.0 / 1000.0
+    return {"workload": "%d ensemble members (configuration 4 draws), Tsit5 with true stages, mixed, %s, "
+                        "%d coupling steps of 10 yr after three untimed"
+                        % (n_members, "batched graphs in %d stiffness groups" % groups if mode == "graph"
+                           else "per-member streams", n_updates),
+            "unit": "member-kyr/s", "batched_mixed": mkyr / batched_s, "sequential_fp64": mkyr / seq_s,
+            "speedup": seq_s / batched_s, "attempts_per_member": {"mean": float(np.mean(attempts)),
+                                                                  "max": float(np.max(attempts))},
+            "err_vs_fp64": {"members_within_1e-5": int(np.sum(errs <= 1e-5)), "median_rel": float(np.median(errs)),
+                            "max_rel": float(errs.max())}}
+
+
 def serve_leg(lams=(10, 30, 100, 300, 1000, 2000), n_req=48, reserve_gb=8.0, n_long=6):
     """Continuous batching (configuration 5): Poisson arrivals at rate lam of
     n_req solve requests whose sizes 64^2..1024^2 come in the weights
@@ -931,9 +989,13 @@ def main():
     ap.add_argument("--no-oracle", action="store_true", help="skip the err_vs_oracle leg")
     ap.add_argument("--ensemble-members", type=int, default=256)
     ap.add_argument("--ensemble-updates", type=int, default=10)
+    ap.add_argument("--groups", type=int, default=2, help="stiffness groups of --only ensemble-true")
+    ap.add_argument("--ensemble-mode", default="graph", choices=["graph", "streams"],
+                    help="batched graphs or per-member streams for --only ensemble-true")
     ap.add_argument("--scale-sizes", default="1024,2048", help="grid sizes of --only scale")
     ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--only", choices=["ensemble", "serve", "configs", "scale", "oracle", "engine-trace"],
+    ap.add_argument("--only", choices=["ensemble", "ensemble-true", "serve", "configs", "scale", "oracle",
+                                       "engine-trace"],
                     help="run one secondary leg alone and print its JSON (for profiling), not a bench line")
     ap.add_argument("--lean", action="store_true",
                     help="mixed form only, no profile / e2e / CPU legs (for ncu captures); prints the timing only")
@@ -967,6 +1029,9 @@ def main():
         return 0
     if args.only == "serve":
         print(json.dumps({"serve": serve_leg(n_req=args.serve_requests)}))
+        return 0
+    if args.only == "ensemble-true":
+        print(json.dumps({"ensemble_true": ensemble_true_leg(groups=args.groups, mode=args.ensemble_mode)}))
         return 0
     if args.only == "engine-trace":
         print(json.dumps({"engine_trace": engine_trace_leg()}))

@@ -2430,6 +2430,8 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         m.p = h->prhs;
         m.fc = h->fc;
         m.fcf = flex_coef_f32(h->fc);
+        m.norm_scale = 1.0 / (double)(float)((long long)h->prhs.nx * h->prhs.ny);   // nx*ny*1. (default real)
+        m.norm_scale_f = (float)m.norm_scale;
         m.y = h->d.w;
         m.q0 = h->q0;
         m.mask = h->d.mactive;

@@ -39,6 +39,8 @@ struct BMember {
     int fgx;                  // flexure blocks along x (FP64 tiles)
     int fseg;                 // output rows per flexure warp task (mixed column strips)
     int red_nblk;             // blocks of the reduction kernels
+    double norm_scale;        // 1 / (nx*ny*1.) as the reference normalises
+    float norm_scale_f;       // the same in float: no FP64 division per thread
     Dom d;
     double atol, rtol, q, dt_max;
 };

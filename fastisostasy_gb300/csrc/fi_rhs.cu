@@ -1004,8 +1004,10 @@ __global__ void k_b_rows_inv(const BMember* __restrict__ M, BList L, int stage)
     typedef typename vec2<T>::type C2;
     batch_walk(L, [&](int m) { return true; }, [&](int m, int local) {
         const BMember& b = M[m];
-        const double norm = (double)(float)((long long)b.p.nx * b.p.ny);   // nx*ny*1. (default real)
-        rows_inv_body<T>((const C2*)b.S, b.p.ny, (T*)b.raw7[stage], b.p.nx, b.p, b.RB, (T)(1.0 / norm), local, 0);
+        T scale;   // 1/(nx*ny*1.), converted on the host
+        if constexpr (sizeof(T) == 4) scale = b.norm_scale_f;
+        else scale = b.norm_scale;
+        rows_inv_body<T>((const C2*)b.S, b.p.ny, (T*)b.raw7[stage], b.p.nx, b.p, b.RB, scale, local, 0);
         __syncthreads();
     });
 }

@@ -795,8 +795,13 @@ __device__ __forceinline__ void dp_stage_body(const Ctl* __restrict__ c, double*
             y[e] = x[e] + h * a;
         }
     } else {
-        float af[6], cmf[6];
-        for (int q = 0; q < i; ++q) { af[q] = (float)(c_dp_a[i][q] * h * spy); cmf[q] = (float)cm[q]; }
+        // the float coefficients, one thread each (no FP64 preamble in every thread)
+        __shared__ float af[6], cmf[6];
+        if (threadIdx.x < (unsigned)i) {
+            af[threadIdx.x] = (float)(c_dp_a[i][threadIdx.x] * h * spy);
+            cmf[threadIdx.x] = (float)cm[threadIdx.x];
+        }
+        __syncthreads();
         for (size_t e = (size_t)bid * NT + threadIdx.x; e < n; e += (size_t)nblk * NT) {
             float a = 0.f;
             for (int q = 0; q < i; ++q) a += af[q] * ((float)r.p[q][e] - cmf[q]);
@@ -835,12 +840,15 @@ __device__ __forceinline__ void dp_err_body(Dom d, const DPRaw<T>& r, double ato
             v[1] = fmax(v[1], fabs(x2));
         }
     } else {
-        // x2 - x1 = h sum_r (a_{6 r} - bs_r) k_r in FP32
-        float ce[7], cmf[7];
-        for (int q = 0; q < 7; ++q) {
+        // x2 - x1 = h sum_r (a_{6 r} - bs_r) k_r in FP32; the float
+        // coefficients one thread each
+        __shared__ float ce[7], cmf[7];
+        if (threadIdx.x < 7u) {
+            const int q = (int)threadIdx.x;
             ce[q] = (float)(((q < 6 ? c_dp_a[6][q] : 0.0) - c_dp_bs[q]) * h * d.spy);
             cmf[q] = (float)cm[q];
         }
+        __syncthreads();
         float m1 = 0.f, m2 = 0.f;
         for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
             float dx = 0.f;
