@@ -232,6 +232,7 @@ struct fi_handle {
     int eng_grid = 0, eng_CB = 1, eng_RA = 2, eng_P2 = 0;
     size_t eng_smem = 0;
     float *xhi = nullptr, *xlo = nullptr, *wrefhi = nullptr, *wreflo = nullptr;
+    float* dxw = nullptr;   // (xhi - wrefhi) + (xlo - wreflo): the kernel sequence's mixed RK4 stages
     unsigned long long* trace = nullptr;   // engine phase timestamps (fi_engine_trace)
     // optional per-kernel CUDA-event timing (fi_profile)
     bool prof_on = false;
@@ -768,6 +769,22 @@ void rhs(fi_handle* h, const double* y, const double* wref, T* raw_out, const in
     h->launches += 4;
 }
 
+// One mixed RK4 stage RHS from the float pair of x (rprev: the previous
+// stage's raw RHS, null at the first stage; a: its tableau weight).
+void rhs_pair_stage(fi_handle* h, const float* rprev, double a, float* raw_out)
+{
+    typedef vec2<float>::type C2;
+    PROF(h, K_FLEX, launch_flexure_stage(h->xhi, h->xlo, rprev, h->dxw, (const float*)h->q0, h->d.mactive,
+                                         (const float*)h->Dt, (const float*)h->inv2eta, (float*)h->f, h->nx, h->ny,
+                                         h->fc, h->ctl, a, h->rate_scale, h->s));
+    PROF(h, K_ROWS_FWD, launch_rows_fwd<float>((const float*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, h->prhs, h->s));
+    PROF(h, K_COLS_HARTLEY,
+         launch_cols_hartley<float>((C2*)h->S, (const float*)h->mA, (const float*)h->mB, h->even, h->prhs, h->s));
+    const double norm = (double)(float)((long long)h->nx * h->ny);   // nx*ny*1. (default real)
+    PROF(h, K_ROWS_INV, launch_rows_inv<float>((const C2*)h->S, raw_out, h->prhs, 1.0 / norm, h->s));
+    h->launches += 4;
+}
+
 template <typename T> void conv(fi_handle* h, int which, double* out_raw, double* corners)
 {
     typedef typename vec2<T>::type C2;
@@ -805,10 +822,27 @@ template <typename T> T* enqueue_steps(fi_handle* h, int nsteps)
     T *r0 = (T*)h->raw[0], *r1 = (T*)h->raw[1], *r2 = (T*)h->raw[2], *r3 = (T*)h->raw[3];
     const bool truem = p.stage_mode == 1;
     const double* wref = truem ? h->w_ref : nullptr;
+    // mixed true-stage RK4 on a uniform grid: stage states from the float
+    // pair of x, as the step engine forms them (no FP64 stage state)
+    const bool pairs = sizeof(T) == 4 && truem && p.dt_method == 1 && p.method == 3 && h->dxw != nullptr;
+    if (pairs && nsteps > 0) {
+        PROF(h, K_STAGE, split_hilo_dxw(h->d.x, h->xhi, h->xlo, h->wrefhi, h->wreflo, h->dxw, h->n, h->s));
+        h->launches += 1;
+    }
     T* last = r0;
     for (int st = 0; st < nsteps; ++st) {
         PROF(h, K_CONTROL, step_begin(h->ctl, p.dt_method == 1 ? 1 : 0, h->s));
-        if (p.dt_method == 1 && truem) {
+        if (pairs) {
+            rhs_pair_stage(h, nullptr, 0.0, (float*)r0);
+            rhs_pair_stage(h, (const float*)r0, 0.5, (float*)r1);
+            rhs_pair_stage(h, (const float*)r1, 0.5, (float*)r2);
+            rhs_pair_stage(h, (const float*)r2, 1.0, (float*)r3);
+            PROF(h, K_RK_FINAL, rk4_final_pair(h->ctl, h->d.x, h->d.w, h->xhi, h->xlo, h->wrefhi, h->wreflo, h->dxw,
+                                               (const float*)r0, (const float*)r1, (const float*)r2,
+                                               (const float*)r3, h->nx, h->ny, spy, h->s));
+            h->launches += 1;
+            last = r3;
+        } else if (p.dt_method == 1 && truem) {
             rhs<T>(h, h->d.x, wref, r0);
             PROF(h, K_STAGE, rk_stage<T>(h->ctl, h->y, h->d.x, r0, 0.5, h->nx, h->ny, spy, h->s));
             rhs<T>(h, h->y, wref, r1);
@@ -1483,11 +1517,14 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
         }
     }
 #undef AL
-    // cooperative step engine for true-stage RK4 on uniform grids
+    // cooperative step engine for true-stage RK4 on uniform grids; where it
+    // does not fit (or FI_NO_ENGINE=1) the mixed form's kernel sequence forms
+    // the same stage states from the float pairs
     {
         const char* ev = getenv("FI_NO_ENGINE");
-        const bool want = p.method == 3 && p.stage_mode == 1 && p.dt_method == 1 && h->uniform &&
-                          !(ev && ev[0] == '1');
+        const bool rk4_true = p.method == 3 && p.stage_mode == 1 && p.dt_method == 1 && h->uniform;
+        const bool want = rk4_true && !(ev && ev[0] == '1');
+#define AL2(ptr, bytes) if ((rc = dalloc(h, &(ptr), (bytes)))) return rc
         if (want) {
             int ok = mixed(h) ? engine_config<float>(h->prhs, &h->eng_grid, &h->eng_CB, &h->eng_smem, &h->eng_RA,
                                                   &h->eng_P2)
@@ -1495,16 +1532,17 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
                                                       &h->eng_P2);
             h->engine_ok = ok != 0;
             cudaGetLastError();
-#define AL2(ptr, bytes) if ((rc = dalloc(h, &(ptr), (bytes)))) return rc
             if (h->engine_ok) {
                 const size_t nk = (size_t)(h->prhs.h + 1) * h->ny;
                 AL2(h->ST, nk * c2); AL2(h->mAT, nk * tsz(h)); AL2(h->mBT, nk * tsz(h));
             }
-            if (h->engine_ok && mixed(h)) {
-                AL2(h->xhi, n * 4); AL2(h->xlo, n * 4); AL2(h->wrefhi, n * 4); AL2(h->wreflo, n * 4);
-            }
-#undef AL2
         }
+        if (rk4_true && mixed(h)) {
+            // the float pairs of x and w_ref (the stage states of either path)
+            AL2(h->xhi, n * 4); AL2(h->xlo, n * 4); AL2(h->wrefhi, n * 4); AL2(h->wreflo, n * 4);
+            if (!h->engine_ok) AL2(h->dxw, n * 4);
+        }
+#undef AL2
     }
     if ((rc = upload_static(h))) return rc;
     if (p.method == 3 && !h->engine_ok && !(getenv("FI_NO_TUNE") && getenv("FI_NO_TUNE")[0] == '1')) {

@@ -589,6 +589,31 @@ void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s)
     k_split<<<b, 256, 0, s>>>(x, hi, lo, n);
 }
 
+// The same split for the kernel sequence's stage states, which also keeps
+// dxw = (xhi - w_ref,hi) + (xlo - w_ref,lo), the state part of the mantle
+// term, in the order the step engine's phase A forms it.
+__global__ void k_split_dxw(const double* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo,
+                            const float* __restrict__ wrhi, const float* __restrict__ wrlo, float* __restrict__ dxw,
+                            size_t n)
+{
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+        const double v = x[e];
+        const float a = (float)v;
+        const float b = (float)(v - (double)a);
+        hi[e] = a;
+        lo[e] = b;
+        dxw[e] = (a - wrhi[e]) + (b - wrlo[e]);
+    }
+}
+
+void split_hilo_dxw(const double* x, float* hi, float* lo, const float* wrhi, const float* wrlo, float* dxw, size_t n,
+                    cudaStream_t s)
+{
+    int b = (int)((n + 255) / 256);
+    if (b > 1216) b = 1216;
+    k_split_dxw<<<b, 256, 0, s>>>(x, hi, lo, wrhi, wrlo, dxw, n);
+}
+
 template <typename T, int RA, int FM> int engine_config_shape(const Plan2D& p, int nsm, int optin, int* grid, int* CB,
                                                      size_t* smem)
 {

@@ -53,5 +53,8 @@ struct EngineArgs {
 template <typename T> int engine_config(const Plan2D& p, int* grid, int* CB, size_t* smem, int* RA, int* P2);
 template <typename T> cudaError_t engine_launch(const EngineArgs& g, int grid, size_t smem, cudaStream_t s);
 void split_hilo(const double* x, float* hi, float* lo, size_t n, cudaStream_t s);
+// split plus dxw = (hi - wrhi) + (lo - wrlo) (the kernel sequence's mixed RK4 stages)
+void split_hilo_dxw(const double* x, float* hi, float* lo, const float* wrhi, const float* wrlo, float* dxw, size_t n,
+                    cudaStream_t s);
 
 }  // namespace fi

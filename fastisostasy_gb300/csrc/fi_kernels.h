@@ -64,6 +64,15 @@ void launch_flexure(const double* y, const double* wref, const T* q0, const uint
                     const T* inv2eta, T* f, int nx, int ny, const FlexCoef& c, cudaStream_t s,
                     const int* gate = nullptr, const float* whi = nullptr, const float* wlo = nullptr);
 
+// Mixed-form RK4 stage RHS (uniform spacing, true stages): the stage state
+// x + (a h spy) (rprev - corner mean) from the float pair of x and the raw
+// RHS of the previous stage (null at the first stage); the mantle term takes
+// dxw = (xhi - w_ref,hi) + (xlo - w_ref,lo) per cell; h is read from the
+// control block.
+void launch_flexure_stage(const float* whi, const float* wlo, const float* rprev, const float* dxw, const float* q0,
+                          const uint8_t* mask, const float* D, const float* inv2eta, float* f, int nx, int ny,
+                          const FlexCoef& c, const Ctl* ctl, double a, double spy, cudaStream_t s);
+
 template <typename T>
 void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, typename vec2<T>::type* S,
                      const Plan2D& p, cudaStream_t s, const int* gate = nullptr);

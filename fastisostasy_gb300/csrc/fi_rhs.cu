@@ -335,14 +335,26 @@ __device__ __forceinline__ int strip_tasks(int nx, int ny, int seg)
 // FP64 state y, its first differences taken in double and rounded (as
 // flexure_f32_body<false>), and with wref the mantle term
 // coef_mantle (y - wref) at masked cells.
-template <bool PAIR>
+// STG (with PAIR): an RK stage state y = x + sdf (rprev - cm) formed on the
+// fly from the pair x = whi + wlo and the previous stage's raw RHS rprev
+// (null at the first stage), with the mantle term
+// coef_mantle (dxw + sdf (rprev - cm)) at masked cells, where
+// dxw = (whi - w_ref,hi) + (wlo - w_ref,lo) is kept per cell beside the pair:
+// the arithmetic of the step engine's phase A, term by term, and no FP64
+// instruction.  (Loading every field one row ahead, as the state already is,
+// takes 78 registers instead of 64 and ran 35 % slower at 2048^2: the walk
+// is bound by warps in flight, not by the distance of each warp's loads.)
+template <bool PAIR, bool STG = false>
 __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, const float* __restrict__ wlo,
                                               const float* __restrict__ q0, const uint8_t* __restrict__ mask,
                                               const float* __restrict__ D, const float* __restrict__ inv2eta,
                                               float* __restrict__ f, int nx, int ny, const FlexCoefF& c, int seg,
                                               int task, const double* __restrict__ y = nullptr,
-                                              const double* __restrict__ wref = nullptr)
+                                              const double* __restrict__ wref = nullptr,
+                                              const float* __restrict__ rprev = nullptr, float sdf = 0.f,
+                                              float cmdf = 0.f, const float* __restrict__ dxw = nullptr)
 {
+    static_assert(PAIR || !STG, "stage states are formed from the float pair");
     const unsigned FULL = 0xffffffffu;
     const int ncg = (nx + SW - 1) / SW;
     const int g = task % ncg, sg = task / ncg;
@@ -355,6 +367,7 @@ __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, con
     const int o0 = sg * seg, o1 = min(o0 + seg, ny);
     const int cc = cin ? col : 0;
     float hp = 0.f, lp = 0.f;                           // pair of row r - 1
+    float rp = 0.f;                                     // rprev of row r - 1 (STG)
     double yp = 0.0;                                    // FP64 state of row r - 1 (!PAIR)
     float Wx1 = 0.f, Wx2 = 0.f, Wx3 = 0.f;              // Wx of rows r-1, r-2, r-3
     float wxx1 = 0.f, wxx2 = 0.f;                       // wxx of rows r-1, r-2
@@ -364,12 +377,14 @@ __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, con
     float mx0 = 0.f, mx1 = 0.f, mx2 = 0.f;                         // mx_xx of rows m .. m-2
     // the next row's loads are issued one iteration ahead
     int r = o0 - 4;
-    auto ld_pair = [&](int rr, float& h, float& l, double& yy) {
+    const bool stg = STG && rprev != nullptr;   // uniform
+    auto ld_pair = [&](int rr, float& h, float& l, double& yy, float& rv) {
         if (cin && rr >= 0 && rr < ny) {
             const size_t e = (size_t)rr * nx + cc;
             if constexpr (PAIR) {
                 h = __ldg(whi + e);
                 l = __ldg(wlo + e);
+                if (stg) rv = __ldg(rprev + e);
             } else {
                 yy = __ldg(y + e);
             }
@@ -377,27 +392,55 @@ __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, con
             h = 0.f;
             l = 0.f;
             yy = 0.0;
+            rv = 0.f;
         }
     };
-    float hn = 0.f, ln = 0.f;
+    float hn = 0.f, ln = 0.f, rn = 0.f;
     double yn = 0.0;
-    ld_pair(r, hn, ln, yn);
+    ld_pair(r, hn, ln, yn, rn);
+    // the fields of input row rr that are used at rows m = rr - 2 (D) and
+    // o = rr - 4 (mask, load, 1/(2 eta), and with STG dxw and rprev)
+    auto ld_rest = [&](int rr, float& Dv, uint32_t& mv, float& qv, float& iev, float& dv, float& rov) {
+        const int mm = rr - 2, oo = rr - 4;
+        const bool mr = cin && mm >= 0 && mm < ny;
+        Dv = mr ? __ldg(D + (size_t)mm * nx + cc) : 0.f;
+        const bool orr = outl && oo >= o0 && oo < o1;
+        const size_t ee = orr ? (size_t)oo * nx + cc : 0;
+        mv = orr ? (uint32_t)__ldg(mask + ee) : 0u;
+        qv = orr ? __ldg(q0 + ee) : 0.f;
+        iev = orr ? __ldg(inv2eta + ee) : 0.f;
+        if constexpr (STG) {
+            dv = orr ? __ldg(dxw + ee) : 0.f;
+            rov = (orr && stg) ? __ldg(rprev + ee) : 0.f;
+        }
+    };
     for (; r < o1 + 4; ++r) {
-        const float h = hn, l = ln;
+        const float h = hn, l = ln, rv = rn;
         const double yv = yn;
-        ld_pair(r + 1, hn, ln, yn);
+        ld_pair(r + 1, hn, ln, yn, rn);
         const int m = r - 2, o = r - 4;
-        const bool mrow = cin && m >= 0 && m < ny;
-        const float Dm = mrow ? __ldg(D + (size_t)m * nx + cc) : 0.f;
         const bool orow = outl && o >= o0 && o < o1;
         const size_t eo = orow ? (size_t)o * nx + cc : 0;
-        const uint8_t om = orow ? __ldg(mask + eo) : (uint8_t)0;
-        const float oq = orow ? __ldg(q0 + eo) : 0.f, oie = orow ? __ldg(inv2eta + eo) : 0.f;
+        float Dm, oq, oie, od = 0.f, orv = 0.f;
+        uint32_t om;
+        if constexpr (STG) {
+            ld_rest(r, Dm, om, oq, oie, od, orv);
+        } else {
+            const bool mrow = cin && m >= 0 && m < ny;
+            Dm = mrow ? __ldg(D + (size_t)m * nx + cc) : 0.f;
+            om = orow ? __ldg(mask + eo) : (uint8_t)0;
+            oq = orow ? __ldg(q0 + eo) : 0.f;
+            oie = orow ? __ldg(inv2eta + eo) : 0.f;
+        }
         // row r: first differences, Wx, wxx
         float dX;
         if constexpr (PAIR) {
             const float hr = __shfl_down_sync(FULL, h, 1), lr = __shfl_down_sync(FULL, l, 1);
             dX = (hr - h) + (lr - l);
+            if constexpr (STG) {
+                const float rr = __shfl_down_sync(FULL, rv, 1);
+                if (stg) dX += sdf * (rr - rv);
+            }
         } else {
             const double yr = __shfl_down_sync(FULL, yv, 1);
             dX = (float)(yr - yv);
@@ -413,8 +456,15 @@ __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, con
             wxx = (dX - dXm) * c.inv_dx2;
         }
         float dYn;   // dY of row r - 1
-        if constexpr (PAIR) dYn = (h - hp) + (l - lp);
-        else dYn = (float)(yv - yp);
+        if constexpr (PAIR) {
+            dYn = (h - hp) + (l - lp);
+            if constexpr (STG) {
+                if (stg) dYn += sdf * (rv - rp);
+                rp = rv;
+            }
+        } else {
+            dYn = (float)(yv - yp);
+        }
         hp = h;
         lp = l;
         yp = yv;
@@ -471,6 +521,13 @@ __device__ __forceinline__ void flexure_strip(const float* __restrict__ whi, con
             if constexpr (!PAIR) {
                 if (om && wref) p += c.coef_mantle * (float)(__ldg(y + eo) - __ldg(wref + eo));
             }
+            if constexpr (STG) {
+                if (om) {
+                    float dy = od;
+                    if (stg) dy += sdf * (orv - cmdf);
+                    p = oq + c.coef_mantle * dy;
+                }
+            }
             f[eo] = (((p + mx2) + 2.f * mxy_xy) + my_yy) * oie;
         }
     }
@@ -496,6 +553,27 @@ k_flexure_strip_y(const double* __restrict__ y, const double* __restrict__ wref,
     const int task = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (task >= strip_tasks(nx, ny, seg)) return;   // whole warps
     flexure_strip<false>(nullptr, nullptr, q0, mask, D, inv2eta, f, nx, ny, c, seg, task, y, wref);
+}
+
+// RK4 stage RHS from the float pair of x: stage scale sdf = (a h) spy with h
+// the step size in the control block, cm the corner mean of rprev; thread 0
+// forms both (the only FP64 instructions of the kernel).
+__global__ void __launch_bounds__(256)
+k_flexure_strip_stage(const float* __restrict__ whi, const float* __restrict__ wlo, const float* __restrict__ rprev,
+                      const float* __restrict__ dxw, const float* __restrict__ q0, const uint8_t* __restrict__ mask,
+                      const float* __restrict__ D, const float* __restrict__ inv2eta, float* __restrict__ f, int nx,
+                      int ny, FlexCoefF c, int seg, const Ctl* __restrict__ ctl, double a, double spy)
+{
+    __shared__ float s_sc[2];
+    if (threadIdx.x == 0) {
+        s_sc[0] = rprev ? (float)(a * ctl->h * spy) : 0.f;
+        s_sc[1] = rprev ? (float)corner_mean_of(rprev, nx, ny) : 0.f;
+    }
+    __syncthreads();
+    const int task = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (task >= strip_tasks(nx, ny, seg)) return;   // whole warps
+    flexure_strip<true, true>(whi, wlo, q0, mask, D, inv2eta, f, nx, ny, c, seg, task, nullptr, nullptr, rprev,
+                              s_sc[0], s_sc[1], dxw);
 }
 
 // rows per warp task for a single domain: enough tasks to fill the GPU
@@ -559,6 +637,17 @@ void launch_flexure(const double* y, const double* wref, const T* q0, const uint
         return;
     }
     k_flexure<T><<<g, b, 0, s>>>(y, wref, q0, mask, D, inv2eta, f, nx, ny, c, gate);
+}
+
+void launch_flexure_stage(const float* whi, const float* wlo, const float* rprev, const float* dxw, const float* q0,
+                          const uint8_t* mask, const float* D, const float* inv2eta, float* f, int nx, int ny,
+                          const FlexCoef& c, const Ctl* ctl, double a, double spy, cudaStream_t s)
+{
+    const FlexCoefF cf = flex_coef_f32(c);
+    const int seg = strip_seg_single(nx, ny);
+    const int tasks = ((nx + SW - 1) / SW) * ((ny + seg - 1) / seg);
+    k_flexure_strip_stage<<<(tasks + 7) / 8, 256, 0, s>>>(whi, wlo, rprev, dxw, q0, mask, D, inv2eta, f, nx, ny, cf,
+                                                          seg, ctl, a, spy);
 }
 
 // ---------------------------------------------------------------------------

@@ -447,6 +447,48 @@ k_rk4_final(Ctl* c, double* __restrict__ x, double* __restrict__ w, const T* __r
     }
 }
 
+// Mixed RK4 combination that also carries the float pair of x (the stage
+// RHS of the next step reads x as xhi + xlo): the FP64 state takes the float
+// increment, the pair the same increment by an FP32 two-sum, as in the step
+// engine's state update; dxw = (xhi - w_ref,hi) + (xlo - w_ref,lo) of the new
+// pair feeds the mantle term of the next step's stages.
+__global__ void __launch_bounds__(NT)
+k_rk4_final_pair(Ctl* c, double* __restrict__ x, double* __restrict__ w, float* __restrict__ xhi,
+                 float* __restrict__ xlo, const float* __restrict__ wrhi, const float* __restrict__ wrlo,
+                 float* __restrict__ dxw, const float* __restrict__ r1, const float* __restrict__ r2,
+                 const float* __restrict__ r3, const float* __restrict__ r4, int nx, int ny, double spy)
+{
+    if (c->done) return;
+    const BlockScal bs = block_scalars([&] {
+        BlockScal r;
+        r.f[0] = (float)corner_mean_of(r1, nx, ny);
+        r.f[1] = (float)corner_mean_of(r2, nx, ny);
+        r.f[2] = (float)corner_mean_of(r3, nx, ny);
+        r.f[3] = (float)corner_mean_of(r4, nx, ny);
+        r.f[4] = (float)((c->h / 6) * spy);
+        return r;
+    });
+    const float f1 = bs.f[0], f2 = bs.f[1], f3 = bs.f[2], f4 = bs.f[3], sc = bs.f[4];
+    const size_t n = (size_t)nx * ny;
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+        const float k = ((((float)r1[e] - f1) + 2.f * ((float)r2[e] - f2)) + 2.f * ((float)r3[e] - f3)) +
+                        ((float)r4[e] - f4);
+        const float inc = k * sc;
+        const double v = x[e] + (double)inc;
+        x[e] = v;
+        w[e] = v;
+        const float hi = xhi[e], lo = xlo[e];
+        const float sm = hi + inc, bb = sm - hi;
+        const float er = (hi - (sm - bb)) + (inc - bb);
+        const float l2 = lo + er;
+        const float h2 = sm + l2;
+        const float lo2 = l2 - (h2 - sm);
+        xhi[e] = h2;
+        xlo[e] = lo2;
+        dxw[e] = (h2 - wrhi[e]) + (lo2 - wrlo[e]);
+    }
+}
+
 __global__ void k_step_end(Ctl* c)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0 || c->done) return;
@@ -1445,6 +1487,13 @@ void rk4_final(Ctl* c, double* x, double* w, const T* r1, const T* r2, const T* 
                double spy, cudaStream_t s)
 {
     k_rk4_final<T><<<grid_for((size_t)nx * ny), NT, 0, s>>>(c, x, w, r1, r2, r3, r4, nx, ny, spy);
+}
+void rk4_final_pair(Ctl* c, double* x, double* w, float* xhi, float* xlo, const float* wrhi, const float* wrlo,
+                    float* dxw, const float* r1, const float* r2, const float* r3, const float* r4, int nx, int ny,
+                    double spy, cudaStream_t s)
+{
+    k_rk4_final_pair<<<grid_for((size_t)nx * ny), NT, 0, s>>>(c, x, w, xhi, xlo, wrhi, wrlo, dxw, r1, r2, r3, r4, nx,
+                                                              ny, spy);
 }
 template <typename T>
 void euler_final(const Ctl* c, double* x, double* w, const T* r1, int nx, int ny, double spy, cudaStream_t s)

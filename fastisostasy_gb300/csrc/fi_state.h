@@ -64,6 +64,11 @@ void rk_stage(const Ctl* c, double* y, const double* x, const T* raw, double a, 
 template <typename T>
 void rk4_final(Ctl* c, double* x, double* w, const T* r1, const T* r2, const T* r3, const T* r4, int nx, int ny,
                double spy, cudaStream_t s);
+// mixed RK4 combination that also advances the float pair xhi + xlo of x and
+// dxw = (xhi - wrhi) + (xlo - wrlo)
+void rk4_final_pair(Ctl* c, double* x, double* w, float* xhi, float* xlo, const float* wrhi, const float* wrlo,
+                    float* dxw, const float* r1, const float* r2, const float* r3, const float* r4, int nx, int ny,
+                    double spy, cudaStream_t s);
 template <typename T>
 void euler_final(const Ctl* c, double* x, double* w, const T* r1, int nx, int ny, double spy, cudaStream_t s);
 template <typename T> void ts_max(const Dom& d, const T* raw, double atol, double rtol, cudaStream_t s);

@@ -2,8 +2,9 @@
 
 The 512^2 headline workload that bench.py times, in both forms: the FP64
 kernel-sequence graph (every floating field within 1e-10 of max|value|,
-masks bit-exact) and the mixed form through the production step engine
-(displacement within 1e-5 of max|u| of the FP64 oracle); configuration 1 at
+masks bit-exact) and the mixed form through the production step engine and
+through the kernel sequence that replaces it on larger grids (displacement
+within 1e-5 of max|u| of the FP64 oracle); configuration 1 at
 128^2 (reference-compatible Tsit5), configuration 2 at 256^2 (RK4, true
 stages) and configuration 3 at 512 x 1024 (interactive sea level, two-layer
 freqdomain mantle, reference-compatible Tsit5: the same accept/reject
@@ -20,7 +21,8 @@ import pytest
 
 from fastisostasy_gb300 import _lib
 from fastisostasy_gb300 import workloads as W
-from harness import Pair, rel
+from fastisostasy_gb300.isostasy import Domain
+from harness import Pair, gpu_bsl, rel
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -123,6 +125,46 @@ def test_headline_512_mixed_engine_matches_oracle():
     check_counts(pair)
     assert "engine" in used_kernels(pair.dom, pair.t + 10.0, pair.wl, pair.bg)
     pair.close()
+
+
+def test_headline_512_mixed_kernel_sequence_matches_oracle(monkeypatch):
+    """The mixed form through the kernel sequence that runs where the step
+    engine does not fit (1024^2 and up): stage states formed from the float
+    pair of x inside the column-strip stencil, the pair advanced with the
+    FP64 state.  Against the FP64 oracle within 1e-5, and against the
+    engine within the mixed-form bound."""
+    monkeypatch.setenv("FI_NO_ENGINE", "1")
+    pair = Pair(headline(), precision=1)
+    pair.init()
+    pair.step(3)
+    w_g, w_o = pair.dom.field("w"), pair.orc.field("w")
+    e = rel(w_g, w_o)
+    assert e <= TOLMIX, e
+    assert rel(pair.dom.field("z_bed"), pair.orc.field("z_bed")) <= TOLMIX
+    for m in MASKS:
+        assert np.array_equal(pair.dom.field(m), pair.orc.field(m)), m
+    check_counts(pair)
+    used = used_kernels(pair.dom, pair.t + 10.0, pair.wl, pair.bg)
+    assert "engine" not in used and "flexure" in used and "rk_final" in used
+    w_seq = pair.dom.field("w")
+    t_end = pair.t + 10.0
+    pair.close()
+    monkeypatch.delenv("FI_NO_ENGINE")
+    wl = headline()
+    dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=1)
+    f = wl.padded_fields(dom.nx, dom.ny)
+    if f:
+        dom.set_fields(**f)
+    bg = gpu_bsl(wl.bsl.get("method", 0), wl.bsl.get("bsl_init", 0.0), wl.bsl.get("A_ocean_pd", 3.625e14))
+    dom.init_state(wl.z_bed, wl.H_at(0.0), 0.0, bg)
+    t = 0.0
+    for _ in range(4):
+        t += wl.dtt
+        _lib.load().fi_bsl_update(bg, t)
+        dom.update(wl.H_at(t), t, bg)
+    assert t == t_end
+    assert rel(dom.field("w"), w_seq) <= 1e-6
+    dom.close()
 
 
 @pytest.mark.parametrize("precision", [0, 1])
