@@ -259,6 +259,7 @@ struct fi_handle {
     Dom d;
     Ctl* ctl = nullptr;
     Plan2D prhs, pconv;
+    Plan2D pconv_run;   // pconv with the transform shapes tuned for the update's precision
     FlexCoef fc;
     double* y = nullptr;                 // stage state
     void* q0 = nullptr;                  // RHS load term (T)
@@ -741,6 +742,100 @@ int kernel_spectrum(fi_handle* h, const std::vector<double>& ker, int which)
     return FI_OK;
 }
 
+// The convolution transforms (2n-padded grid) by the same search: rows
+// (rows per block x threads) over the forward rows and the cropped inverse
+// rows, columns (columns per block x threads) over the column pass with the
+// kernel multiply.  The shapes go to pconv_run, which only the update's
+// convolutions use (the set-up transforms of the kernels keep pconv).
+template <typename T> void tune_conv_shapes(fi_handle* h)
+{
+    typedef typename vec2<T>::type C2;
+    struct Key {
+        int px, py, sz;
+        bool operator==(const Key& o) const { return px == o.px && py == o.py && sz == o.sz; }
+    };
+    struct Shape {
+        int rb, rt, cb, ct;
+    };
+    static std::mutex mu;
+    static std::vector<std::pair<Key, Shape>> cache;
+    const Key key{h->Px, h->Py, (int)sizeof(T)};
+    h->pconv_run = h->pconv;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (auto& e : cache)
+            if (e.first == key) {
+                h->pconv_run.rb = e.second.rb;
+                h->pconv_run.rt = e.second.rt;
+                h->pconv_run.cb = e.second.cb;
+                h->pconv_run.ct = e.second.ct;
+                return;
+            }
+    }
+    int optin = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    Plan2D p = h->pconv;
+    auto time_it = [&](auto&& fn) {
+        float best = 1e30f;
+        for (int r = 0; r < 4; ++r) {
+            cudaEventRecord(e0, h->s);
+            fn();
+            cudaEventRecord(e1, h->s);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0 && ms < best) best = ms;
+        }
+        return best;
+    };
+    const double scale = 1.0 / ((double)h->Px * (double)h->Py);
+    int best_rb = 0, best_cb = 0, best_rt = 0, best_ct = 0;
+    float tr = 1e30f, tc = 1e30f;
+    for (int rb : {1, 2, 4}) {
+        if (2 * (size_t)rb * p.h * sizeof(C2) > (size_t)optin) continue;
+        for (int rt : {128, 256, 512, 1024}) {
+            if (rt > 128 && rt > rb * p.h / 2) continue;   // at most one element pair per thread
+            p.rb = rb;
+            p.rt = rt;
+            const float t = time_it([&] {
+                launch_rows_fwd<T>((const T*)h->conv_in, h->nx, h->nx, h->ny, (C2*)h->S2, p, h->s);
+                launch_conv_rows_inv<T>((const C2*)h->S2, h->ny + 2, h->we_raw, h->nx, h->ny, h->nx / 2 - 1,
+                                        h->corners, 0, 0, 2 * h->nx - 2, p, scale, h->s);
+            });
+            if (cudaGetLastError() != cudaSuccess) continue;   // a shape the device refuses
+            if (t < tr) { tr = t; best_rb = rb; best_rt = rt; }
+        }
+    }
+    p.rb = best_rb;
+    p.rt = best_rt;
+    for (int cb : {1, 2, 4}) {
+        if (2 * (size_t)cb * (p.ny + 1) * sizeof(C2) > (size_t)optin) continue;
+        for (int ct : {128, 256, 512, 1024}) {
+            if (ct > 128 && ct > cb * p.ny / 2) continue;
+            p.cb = cb;
+            p.ct = ct;
+            const float t = time_it([&] {
+                launch_cols_conv<T>((C2*)h->S2, (const C2*)h->KS[0], h->ny, h->out_rows, h->ny + 2, p, h->s);
+            });
+            if (cudaGetLastError() != cudaSuccess) continue;
+            if (t < tc) { tc = t; best_cb = cb; best_ct = ct; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGetLastError();
+    h->pconv_run.rb = best_rb;
+    h->pconv_run.rt = best_rt;
+    h->pconv_run.cb = best_cb;
+    h->pconv_run.ct = best_ct;
+    std::lock_guard<std::mutex> lk(mu);
+    cache.push_back({key, Shape{best_rb, best_rt, best_cb, best_ct}});
+}
+
 // ---- device pipelines ------------------------------------------------------
 template <typename T> struct TT {
     typedef typename vec2<T>::type C2;
@@ -788,11 +883,12 @@ void rhs_pair_stage(fi_handle* h, const float* rprev, double a, float* raw_out)
 template <typename T> void conv(fi_handle* h, int which, double* out_raw, double* corners)
 {
     typedef typename vec2<T>::type C2;
-    PROF(h, K_CONV_ROWS_FWD, launch_rows_fwd<T>((const T*)h->conv_in, h->nx, h->nx, h->ny, (C2*)h->S2, h->pconv, h->s));
-    PROF(h, K_CONV_COLS, launch_cols_conv<T>((C2*)h->S2, (const C2*)h->KS[which], h->ny, h->out_rows, h->ny + 2, h->pconv,
-                                             h->s));
+    PROF(h, K_CONV_ROWS_FWD,
+         launch_rows_fwd<T>((const T*)h->conv_in, h->nx, h->nx, h->ny, (C2*)h->S2, h->pconv_run, h->s));
+    PROF(h, K_CONV_COLS, launch_cols_conv<T>((C2*)h->S2, (const C2*)h->KS[which], h->ny, h->out_rows, h->ny + 2,
+                                             h->pconv_run, h->s));
     PROF(h, K_CONV_ROWS_INV, launch_conv_rows_inv<T>((const C2*)h->S2, h->ny + 2, out_raw, h->nx, h->ny, h->nx / 2 - 1,
-                                                     corners, 0, 0, 2 * h->nx - 2, h->pconv,
+                                                     corners, 0, 0, 2 * h->nx - 2, h->pconv_run,
                                                      1.0 / ((double)h->Px * (double)h->Py), h->s));
     h->launches += 3;
 }
@@ -1545,6 +1641,11 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
 #undef AL2
     }
     if ((rc = upload_static(h))) return rc;
+    h->pconv_run = h->pconv;
+    if ((p.include_elastic || p.heterogeneous_ssh) && !(getenv("FI_NO_TUNE") && getenv("FI_NO_TUNE")[0] == '1')) {
+        if (mixed(h)) tune_conv_shapes<float>(h);
+        else tune_conv_shapes<double>(h);
+    }
     if (p.method == 3 && !h->engine_ok && !(getenv("FI_NO_TUNE") && getenv("FI_NO_TUNE")[0] == '1')) {
         if (mixed(h)) tune_rhs_shapes<float>(h);
         else tune_rhs_shapes<double>(h);

@@ -952,7 +952,8 @@ void launch_cols_conv(typename vec2<T>::type* S, const typename vec2<T>::type* K
     const size_t sm = 2 * (size_t)CB * col_stride(p.ny) * sizeof(C2);
     set_smem(k_cols_conv<T>, sm);
     const int nblk = (p.h + 1 + CB - 1) / CB;
-    k_cols_conv<T><<<nblk, threads_for(CB * p.ny / 4), sm, s>>>(S, K, nrows_in, out_rows, n_out, p, CB, 1);
+    const int nt = p.ct > 0 ? p.ct : threads_for(CB * p.ny / 4);
+    k_cols_conv<T><<<nblk, nt, sm, s>>>(S, K, nrows_in, out_rows, n_out, p, CB, 1);
 }
 
 template <typename T>
@@ -1030,8 +1031,8 @@ void launch_conv_rows_inv(const typename vec2<T>::type* S, int n_out, double* ou
     const size_t sm = 2 * (size_t)RB * p.h * sizeof(C2);
     set_smem(k_conv_rows_inv<T>, sm);
     const int nblk = (n_out + RB - 1) / RB;
-    k_conv_rows_inv<T><<<nblk, threads_for(RB * p.h / 4), sm, s>>>(S, n_out, out, nx, ny, i_off, corners,
-                                                                   corner_col1, p, RB, (T)scale);
+    const int nt = p.rt > 0 ? p.rt : threads_for(RB * p.h / 4);
+    k_conv_rows_inv<T><<<nblk, nt, sm, s>>>(S, n_out, out, nx, ny, i_off, corners, corner_col1, p, RB, (T)scale);
 }
 
 // ---------------------------------------------------------------------------
