@@ -114,20 +114,23 @@ def algorithmic_bytes(kernel, dom, precision, stage_mode, rk_steps=int(round(DTT
     cspec_in = ny * (px // 2 + 1) * 2 * f
     cspec_k = py * (px // 2 + 1) * 2 * f
     cspec_out = (ny + 2) * (px // 2 + 1) * 2 * f
-    # the mixed true-stage kernel sequence reads x and w_ref as float pairs
-    # and the previous stage output (3 stages of 4), splits x once per
-    # update (rk_stage) and advances the pair in the final combination
+    # the mixed true-stage kernel sequence reads x as a float pair, the
+    # previous stage output (3 stages of 4) and dxw = (x - w_ref) of the
+    # pairs; it splits x once per update (rk_stage: x and the w_ref pair in,
+    # the x pair and dxw out) and advances the pair and dxw in the final
+    # combination
     pairs = precision == 1 and stage_mode == 1
+    state = (8 + 3 + 4) if pairs else 8 + (8 if stage_mode == 1 else 0)
     table = {
-        "flexure": n * ((8 + 3 + 8) if pairs else (8 + (8 if stage_mode == 1 else 0)) + 3 * f + 1 + f),
+        "flexure": n * (state + 3 * f + 1 + f),
         "rows_fwd": n * f + spec,
         "cols_hartley": 2 * spec + spec // 2,
         "rows_inv": spec + n * f,
         "conv_rows_fwd": n * f + cspec_in,
         "conv_cols": cspec_in + cspec_k + cspec_out,
         "conv_rows_inv": cspec_out + n * 8,
-        "rk_stage": n * (8 + 8) if pairs else n * (8 + f + 8),
-        "rk_final": n * (8 + 4 * f + 16 + (16 if pairs else 0)),
+        "rk_stage": n * (8 + 8 + 12) if pairs else n * (8 + f + 8),
+        "rk_final": n * (8 + 4 * f + 16 + (28 if pairs else 0)),
         "engine": n * rk_steps * (6 * 8 + 27 * f) if stage_mode == 1 else None,
     }
     return table.get(kernel)
