@@ -139,6 +139,20 @@ private:
 };
 
 // dst <- src in `parts` slices on the pool
+// A caller buffer in page-locked host memory (cudaHostAlloc, or a range
+// registered with cudaHostRegister) is copied to and from the device
+// directly; pageable memory goes through the handle's staging buffer.
+bool host_pinned(const void* p)
+{
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 void pool_copy(void* dst, const void* src, size_t bytes, int parts)
 {
     const size_t chunk = (bytes + parts - 1) / parts;
@@ -1960,12 +1974,29 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
     if (!h->state_ready) return fail(h, FI_E_STATE, "fi_update before fi_init_state");
     const size_t ni = (size_t)h->nx_ice * h->ny_ice;
     int rc;
-    if (ni < (1u << 16)) memcpy(h->hpin, H_ice, ni * 8);
-    else pool_copy(h->hpin, H_ice, ni * 8, 8);
-    CK(cudaMemcpyAsync(h->dH, h->hpin, ni * 8, cudaMemcpyHostToDevice, h->s));
+    if (ni >= (1u << 16) && host_pinned(H_ice)) {
+        CK(cudaMemcpyAsync(h->dH, H_ice, ni * 8, cudaMemcpyHostToDevice, h->s));
+    } else {
+        if (ni < (1u << 16)) memcpy(h->hpin, H_ice, ni * 8);
+        else pool_copy(h->hpin, H_ice, ni * 8, 8);
+        CK(cudaMemcpyAsync(h->dH, h->hpin, ni * 8, cudaMemcpyHostToDevice, h->s));
+    }
     enqueue_args(h, time, bsl, true);
     if ((rc = update_any(h, h->dH, time, true))) return rc;
     const bool piped = out && ni >= (1u << 16);
+    double* dst[8] = {nullptr};
+    uint8_t* mdst[3] = {nullptr};
+    bool direct[11] = {false};   // piped fields copied straight into a page-locked caller array
+    if (out) {
+        double* d8[8] = {out->z_bed, out->z_ss, out->dz_ss, out->w, out->we, out->dwdt, out->canom_full, out->Hice};
+        uint8_t* m3[3] = {out->maskocean, out->maskgrounded, out->maskcontinent};
+        for (int f = 0; f < 8; ++f) dst[f] = d8[f];
+        for (int f = 0; f < 3; ++f) mdst[f] = m3[f];
+        if (piped) {
+            for (int f = 0; f < 8; ++f) direct[f] = host_pinned(dst[f]);
+            for (int f = 0; f < 3; ++f) direct[8 + f] = host_pinned(mdst[f]);
+        }
+    }
     if (piped && h->ev_field.empty()) {
         h->ev_field.resize(11, nullptr);
         for (auto& e : h->ev_field) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1979,12 +2010,15 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
             gather_bytes(h->gsrc, h->gmsrc, 8, 3, h->d, h->dpack, dmask, h->s);
             // one copy per field, each followed by its event
             for (int f = 0; f < 11; ++f) {
-                if (f < 8)
-                    CK(cudaMemcpyAsync(h->hpin + (size_t)f * ni, h->dpack + (size_t)f * ni, ni * 8,
-                                       cudaMemcpyDeviceToHost, h->s));
-                else
-                    CK(cudaMemcpyAsync(hmask + (size_t)(f - 8) * ni, dmask + (size_t)(f - 8) * ni, ni,
-                                       cudaMemcpyDeviceToHost, h->s));
+                if (f < 8) {
+                    if (!dst[f]) continue;
+                    CK(cudaMemcpyAsync(direct[f] ? dst[f] : h->hpin + (size_t)f * ni, h->dpack + (size_t)f * ni,
+                                       ni * 8, cudaMemcpyDeviceToHost, h->s));
+                } else {
+                    if (!mdst[f - 8]) continue;
+                    CK(cudaMemcpyAsync(direct[f] ? mdst[f - 8] : hmask + (size_t)(f - 8) * ni,
+                                       dmask + (size_t)(f - 8) * ni, ni, cudaMemcpyDeviceToHost, h->s));
+                }
                 CK(cudaEventRecord(h->ev_field[f], h->s));
             }
         } else {
@@ -2007,13 +2041,12 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
         // the fields are ~100 B per cell, and 11 whole-field tasks left the
         // pool's threads waiting on the last few)
         constexpr int kParts = 4;
-        double* dst[8] = {out->z_bed, out->z_ss, out->dz_ss, out->w, out->we, out->dwdt, out->canom_full, out->Hice};
-        uint8_t* mdst[3] = {out->maskocean, out->maskgrounded, out->maskcontinent};
         const size_t chunk = (ni + kParts - 1) / kParts;
         auto copy_part = [&](int t) {
             const int f = t / kParts;
             const size_t a = (size_t)(t % kParts) * chunk, b = std::min(ni, a + chunk);
-            if (a >= b) return;
+            if (a >= b || direct[f]) return;
+            if (f < 8 ? !dst[f] : !mdst[f - 8]) return;
             if (piped) cudaEventSynchronize(h->ev_field[f]);
             if (f < 8) {
                 if (dst[f]) memcpy(dst[f] + a, h->hpin + (size_t)f * ni + a, (b - a) * 8);

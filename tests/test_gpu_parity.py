@@ -223,6 +223,47 @@ def test_outputs_and_restart_roundtrip(precision, n):
     pair.close()
 
 
+def test_page_locked_and_pageable_host_arrays_agree():
+    """fi_update on a grid above 65536 ice cells (one copy per field):
+    outputs into page-locked arrays go straight from the device, pageable
+    ones through the staging buffer, absent ones are skipped; a page-locked
+    ice load is uploaded directly.  Every output equals the field, and the
+    two input forms give the same state bit for bit."""
+    import torch
+    wl = W.config2(n=512, L=512 * 11.71875e3, dt=1.0, stage_mode=1)
+    ni = (wl.ny_ice, wl.nx_ice)
+    res = []
+    for pin in (False, True):
+        dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=1)
+        dom.set_fields(**wl.padded_fields(dom.nx, dom.ny))
+        bg = gpu_bsl()
+        dom.init_state(wl.z_bed, wl.H_at(0.0), 0.0, bg)
+
+        def arr(dtype, locked):
+            if locked:
+                return torch.zeros(ni, dtype=dtype, pin_memory=True).numpy()
+            return np.zeros(ni, dtype=np.float64 if dtype == torch.float64 else np.uint8)
+
+        # page-locked and pageable outputs side by side; dwdt and Hice absent
+        out = {"w": arr(torch.float64, pin), "we": arr(torch.float64, not pin),
+               "z_bed": arr(torch.float64, pin), "z_ss": arr(torch.float64, True),
+               "dz_ss": arr(torch.float64, False), "canom_full": arr(torch.float64, pin),
+               "maskocean": arr(torch.uint8, pin), "maskgrounded": arr(torch.uint8, not pin),
+               "maskcontinent": arr(torch.uint8, True)}
+        H = arr(torch.float64, pin)
+        for t in (10.0, 20.0):
+            H[...] = wl.H_at(t)
+            dom.update(H, t, bg, out=out)
+        for k in ("w", "we", "z_bed", "z_ss", "dz_ss", "canom_full"):
+            assert np.array_equal(out[k], dom.crop(dom.field(k))), k
+        for k in ("maskocean", "maskgrounded", "maskcontinent"):
+            assert np.array_equal(out[k], dom.crop(dom.field(k)).astype(np.uint8)), k
+        res.append(dom.field("w"))
+        dom.close()
+    assert np.abs(res[0]).max() > 0
+    assert np.array_equal(res[0], res[1])
+
+
 def test_error_status_codes():
     wl = W.config2(n=32, L=3000e3 * 32 / 256, dt=1.0, stage_mode=1)
     dom = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx)
