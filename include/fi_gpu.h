@@ -150,7 +150,11 @@ int fi_init_ref(fi_handle* h, const double* z_bed, const double* H_ice, double b
 /* Replaces isos_init_state (src/fastisostasy.f90:596-660), without restart. */
 int fi_init_state(fi_handle* h, const double* z_bed, const double* H_ice, double time, fi_bsl* bsl);
 /* Replaces isos_update (src/fastisostasy.f90:731-872).  H_ice is ice grid;
- * outputs are copied to `out` (may be NULL).  Synchronous. */
+ * outputs are copied to `out` (may be NULL; so may each of its arrays).
+ * Synchronous.  On ice grids of 65536 cells and more, arrays in page-locked
+ * host memory (cudaHostAlloc, or ranges registered with cudaHostRegister)
+ * are copied to and from the device directly; pageable arrays go through a
+ * page-locked staging buffer of the handle. */
 int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_out* out);
 /* Asynchronous isos_update for device-resident inputs: d_H_ice is a DEVICE
  * pointer to the ice-grid thickness (NULL keeps the previous one).  Valid for
