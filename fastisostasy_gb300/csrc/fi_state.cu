@@ -19,6 +19,19 @@ namespace fi {
 
 constexpr int NT = 256;
 
+// |x| as the bit pattern of a double (sign cleared); above kInfBits it is a NaN
+constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
+__device__ __forceinline__ unsigned long long abs_bits(double x)
+{
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+// m = max(m, |x|) on the bit patterns, NaN ignored as fmax ignores it
+__device__ __forceinline__ void absmax_bits(unsigned long long& m, double x)
+{
+    const unsigned long long b = abs_bits(x);
+    if (b <= kInfBits && b > m) m = b;
+}
+
 __device__ __forceinline__ double warp_sum(double v)
 {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -209,7 +222,11 @@ __global__ void __launch_bounds__(NT) k_upd_begin(Dom d, const double* __restric
     double v[2] = {0.0, 0.0};
     const bool mx[2] = {false, false};
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
-        const int i = (int)(e % d.nx), j = (int)(e / d.nx);
+        // 32-bit index arithmetic (a 64-bit division is a long instruction
+        // sequence; a padded grid has far fewer than 2^32 cells)
+        const unsigned eu = (unsigned)e, nxu = (unsigned)d.nx;
+        const unsigned ju = eu / nxu;
+        const int j = (int)ju, i = (int)(eu - ju * nxu);
         double H = 0.0;
         if (H_ice && in_crop(d, i, j)) H = H_ice[(size_t)(j - d.j0) * d.nxi + (i - d.i0)];
         else if (!H_ice) H = d.Hice[e];
@@ -976,20 +993,27 @@ __global__ void __launch_bounds__(NT) k_upd_end(Dom d, const T* __restrict__ raw
     }
     __syncthreads();
     const double cw = s_c[0], cr = s_c[1];
-    double v[4] = {0.0, 0.0, 0.0, 0.0};
-    const bool mx[4] = {true, true, true, true};
+    // max |w|, |we|, |dz_ss| over the non-NaN cells, on the bit patterns
+    // (for non-negative doubles the IEEE order is the integer order of the
+    // bits; the FP64 unit is left to the arithmetic), and a NaN flag of z_bed
+    unsigned long long m[3] = {0ull, 0ull, 0ull};
+    bool nan = false;
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < d.n; e += (size_t)gridDim.x * NT) {
         const double w = d.w[e] - cw;
         d.wout[e] = w;
         d.c_mantle[e] = 0.0 + d.rho_m * (w - d.w_ref[e]);
-        const double zb = (d.z_bed_ref[e] + w) + d.we[e];
+        const double we = d.we[e];
+        const double zb = (d.z_bed_ref[e] + w) + we;
         d.z_bed[e] = zb;
         if (have_rhs) d.dwdt[e] = ((double)raw_last[e] - cr) * d.spy;
-        v[0] = fmax(v[0], fabs(w));
-        v[1] = fmax(v[1], fabs(d.we[e]));
-        v[2] = fmax(v[2], fabs(d.dz_ss[e]));
-        if (zb != zb) v[3] = 1.0;
+        absmax_bits(m[0], w);
+        absmax_bits(m[1], we);
+        absmax_bits(m[2], d.dz_ss[e]);
+        nan |= abs_bits(zb) > kInfBits;
     }
+    double v[4] = {__longlong_as_double((long long)m[0]), __longlong_as_double((long long)m[1]),
+                   __longlong_as_double((long long)m[2]), nan ? 1.0 : 0.0};
+    const bool mx[4] = {true, true, true, true};
     double tot[4];
     if (grid_finish<4>(v, mx, d.partials, &d.ctl->counter[3], tot)) {
         Ctl* c = d.ctl;
@@ -1423,9 +1447,18 @@ template void batch_ts_commit<double>(const BMember*, BList, int, cudaStream_t);
 
 int reduce_blocks(size_t n) { return grid_for(n); }
 
+// Kernels ending in a grid reduction: two blocks of NT per SM, each thread
+// looping over several cells, so the per-thread shuffle tree of the block
+// reduction is paid once per several cells (at most reduce_blocks blocks).
+static int red_grid(size_t n)
+{
+    const int g = grid_for(n);
+    return g < 152 * 2 ? g : 152 * 2;
+}
+
 void upd_begin(const Dom& d, const double* H_ice, cudaStream_t s)
 {
-    k_upd_begin<<<grid_for(d.n), NT, 0, s>>>(d, H_ice);
+    k_upd_begin<<<red_grid(d.n), NT, 0, s>>>(d, H_ice);
 }
 template <typename T> void upd_masks(const Dom& d, T* conv_in, cudaStream_t s)
 {
@@ -1523,7 +1556,7 @@ void ts_commit_pair(const Dom& d, const float* raw, cudaStream_t s)
 }
 template <typename T> void upd_end(const Dom& d, const T* raw_last, int have_rhs, cudaStream_t s)
 {
-    k_upd_end<T><<<grid_for(d.n), NT, 0, s>>>(d, raw_last, have_rhs);
+    k_upd_end<T><<<red_grid(d.n), NT, 0, s>>>(d, raw_last, have_rhs);
     k_copy<<<grid_for(d.n), NT, 0, s>>>(d.w, d.wout, d.n);
 }
 void gather(const double* const* src, const uint8_t* const* msrc, int nf, int nm, const Dom& d, double* out,
