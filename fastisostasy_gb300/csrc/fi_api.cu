@@ -247,6 +247,8 @@ struct fi_handle {
     size_t eng_smem = 0;
     float *xhi = nullptr, *xlo = nullptr, *wrefhi = nullptr, *wreflo = nullptr;
     float* dxw = nullptr;   // (xhi - wrefhi) + (xlo - wreflo): the kernel sequence's mixed RK4 stages
+    // true-stage Tsit5, mixed form: the stage state as a float pair and its dxw
+    float *yhi = nullptr, *ylo = nullptr, *ydw = nullptr;
     unsigned long long* trace = nullptr;   // engine phase timestamps (fi_engine_trace)
     // optional per-kernel CUDA-event timing (fi_profile)
     bool prof_on = false;
@@ -894,6 +896,23 @@ void rhs_pair_stage(fi_handle* h, const float* rprev, double a, float* raw_out)
     h->launches += 4;
 }
 
+// One RHS of the mixed true-stage Tsit5 at a stage state given as a float
+// pair with its dxw (rhs with the column-strip stencil in stage mode).
+void rhs_tpair(fi_handle* h, const float* hi, const float* lo, const float* dw, float* raw_out, const int* gate)
+{
+    typedef vec2<float>::type C2;
+    PROF(h, K_FLEX, launch_flexure_stage(hi, lo, nullptr, dw, (const float*)h->q0, h->d.mactive, (const float*)h->Dt,
+                                         (const float*)h->inv2eta, (float*)h->f, h->nx, h->ny, h->fc, h->ctl, 0.0,
+                                         h->rate_scale, h->s, gate));
+    PROF(h, K_ROWS_FWD,
+         launch_rows_fwd<float>((const float*)h->f, h->nx, h->nx, h->ny, (C2*)h->S, h->prhs, h->s, gate));
+    PROF(h, K_COLS_HARTLEY, launch_cols_hartley<float>((C2*)h->S, (const float*)h->mA, (const float*)h->mB, h->even,
+                                                       h->prhs, h->s, gate));
+    const double norm = (double)(float)((long long)h->nx * h->ny);   // nx*ny*1. (default real)
+    PROF(h, K_ROWS_INV, launch_rows_inv<float>((const C2*)h->S, raw_out, h->prhs, 1.0 / norm, h->s, gate));
+    h->launches += 4;
+}
+
 template <typename T> void conv(fi_handle* h, int which, double* out_raw, double* corners)
 {
     typedef typename vec2<T>::type C2;
@@ -1037,6 +1056,25 @@ template <typename T> void tsit_true_attempt(fi_handle* h, cudaGraphConditionalH
     DPRaw<T> R;
     for (int i = 0; i < 7; ++i) R.p[i] = (const T*)h->raw[i];
     ts_attempt_begin(h->ctl, kMaxAttempts, h->s);
+    if (sizeof(T) == 4 && h->yhi) {
+        // mixed form: stage states as float pairs (no FP64 stage state but x2)
+        DPRaw<float> Rf;
+        for (int i = 0; i < 7; ++i) Rf.p[i] = (const float*)h->raw[i];
+        rhs_tpair(h, h->xhi, h->xlo, h->dxw, (float*)h->raw[0], &h->ctl->need_rhs);
+        for (int i = 1; i <= 6; ++i) {
+            PROF(h, K_STAGE, dp_stage_pair(h->ctl, h->xhi, h->xlo, h->wrefhi, h->wreflo, h->yhi, h->ylo, h->ydw,
+                                           i == 6 ? h->d.ts_x2 : nullptr, h->d.x, Rf, i, h->nx, h->ny,
+                                           h->rate_scale, h->s));
+            rhs_tpair(h, h->yhi, h->ylo, h->ydw, (float*)h->raw[i], &h->ctl->active);
+        }
+        PROF(h, K_TS, dp_err<T>(h->d, R, p.atol, p.rtol, h->s));
+        PROF(h, K_TS, ts_err<T>(h->d, (const T*)h->raw[0], p.q, p.dt_max, h->s));
+        PROF(h, K_TS, ts_commit_tpair(h->d, h->xhi, h->xlo, h->dxw, h->yhi, h->ylo, h->ydw, h->s));
+        PROF(h, K_TS, fsal_copy<T>(h->ctl, (T*)h->raw[0], (const T*)h->raw[6], h->n, h->s));
+        ts_attempt_end(h->ctl, loop, h->s, 1, more_out);
+        h->launches += 12;
+        return;
+    }
     rhs<T>(h, h->d.x, h->w_ref, (T*)h->raw[0], &h->ctl->need_rhs);
     for (int i = 1; i <= 6; ++i) {
         double* y = i == 6 ? h->d.ts_x2 : h->y;
@@ -1062,6 +1100,7 @@ template <typename T> int integrate_tsit(fi_handle* h, double tf, int* have_rhs,
     *raw_last = r0;
     if (p.stage_mode == 1) {
         ts_loop_begin(h->ctl, h->s);
+        if (h->yhi) split_hilo_dxw(h->d.x, h->xhi, h->xlo, h->wrefhi, h->wreflo, h->dxw, h->n, h->s);
         for (long long it = 0;; ++it) {
             tsit_true_attempt<T>(h, 0, h->dmore);
             int more = 0;
@@ -1111,6 +1150,10 @@ template <typename T> int enqueue_tsit_loop(fi_handle* h)
     h->launches += 1;
     if (h->d.whi) {
         split_hilo(h->d.w, h->d.whi, h->d.wlo, h->n, h->s);
+        h->launches += 1;
+    }
+    if (h->yhi) {
+        split_hilo_dxw(h->d.x, h->xhi, h->xlo, h->wrefhi, h->wreflo, h->dxw, h->n, h->s);
         h->launches += 1;
     }
     cudaStreamCaptureStatus st;
@@ -1633,6 +1676,7 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
     {
         const char* ev = getenv("FI_NO_ENGINE");
         const bool rk4_true = p.method == 3 && p.stage_mode == 1 && p.dt_method == 1 && h->uniform;
+        const bool tsit_true = p.method == 3 && p.stage_mode == 1 && p.dt_method == 2 && h->uniform;
         const bool want = rk4_true && !(ev && ev[0] == '1');
 #define AL2(ptr, bytes) if ((rc = dalloc(h, &(ptr), (bytes)))) return rc
         if (want) {
@@ -1647,11 +1691,12 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
                 AL2(h->ST, nk * c2); AL2(h->mAT, nk * tsz(h)); AL2(h->mBT, nk * tsz(h));
             }
         }
-        if (rk4_true && mixed(h)) {
-            // the float pairs of x and w_ref (the stage states of either path)
+        if ((rk4_true || tsit_true) && mixed(h)) {
+            // the float pairs of x and w_ref (the stage states of every path)
             AL2(h->xhi, n * 4); AL2(h->xlo, n * 4); AL2(h->wrefhi, n * 4); AL2(h->wreflo, n * 4);
             if (!h->engine_ok) AL2(h->dxw, n * 4);
         }
+        if (tsit_true && mixed(h)) { AL2(h->yhi, n * 4); AL2(h->ylo, n * 4); AL2(h->ydw, n * 4); }
 #undef AL2
     }
     if ((rc = upload_static(h))) return rc;
@@ -2353,8 +2398,8 @@ int batch_shape(fi_batch* b, int RB, int CB, int fseg, int waves)
         m.RB = RB > 0 ? RB : rhs_rows_per_block(m.p.h);
         m.CB = CB > 0 ? CB : (b->mixed ? rhs_cols_per_block<float>(m.p.ny) : rhs_cols_per_block<double>(m.p.ny));
         m.fseg = fseg;
-        const int fblk = (b->mixed && !b->true_stages) ? batch_flexure_blocks(m.p.nx, m.p.ny, m.fseg)
-                                                       : m.fgx * ((m.p.ny + 7) / 8);
+        const int fblk = (b->mixed && (!b->true_stages || m.yhi)) ? batch_flexure_blocks(m.p.nx, m.p.ny, m.fseg)
+                                                                  : m.fgx * ((m.p.ny + 7) / 8);
         const int rblk = (m.p.ny + m.RB - 1) / m.RB;
         const int cblk = (m.p.h + 1 + m.CB - 1) / m.CB;
         off[i + 1] = off[i] + fblk;
@@ -2470,6 +2515,7 @@ template <typename T> int batch_eager(fi_batch* b, bool diag)
     int rc = fork_join([&](fi_handle* h) {
         enqueue_pre<T>(h, h->dH, diag, true);
         if (h->d.whi) split_hilo(h->d.w, h->d.whi, h->d.wlo, h->n, h->s);
+        if (h->yhi) split_hilo_dxw(h->d.x, h->xhi, h->xlo, h->wrefhi, h->wreflo, h->dxw, h->n, h->s);
     });
     if (rc) return rc;
     batch_loop_begin(b->dM, b->nm, b->s);
@@ -2506,6 +2552,7 @@ template <typename T> int batch_capture(fi_batch* b, bool diag, cudaGraph_t* out
     rc = join_members([&](fi_handle* h) {
         enqueue_pre<T>(h, h->dH, diag, true);
         if (h->d.whi) split_hilo(h->d.w, h->d.whi, h->d.wlo, h->n, h->s);
+        if (h->yhi) split_hilo_dxw(h->d.x, h->xhi, h->xlo, h->wrefhi, h->wreflo, h->dxw, h->n, h->s);
     });
     if (!rc) {
         batch_loop_begin(b->dM, b->nm, b->s);
@@ -2617,6 +2664,11 @@ int fi_batch_create(fi_handle* const* hs, int n, fi_batch** out)
         for (int q = 0; q < 7; ++q) m.raw7[q] = h->raw[q];
         m.yst = h->y;
         m.wref = h->w_ref;
+        if (h->yhi) {
+            m.xhi = h->xhi; m.xlo = h->xlo; m.xdw = h->dxw;
+            m.yhi = h->yhi; m.ylo = h->ylo; m.ydw = h->ydw;
+            m.wrhi = h->wrefhi; m.wrlo = h->wreflo;
+        }
         m.even = h->even;
         m.fgx = (m.p.nx + 31) / 32;
         m.red_nblk = ts_grid(h->n);
@@ -2719,8 +2771,10 @@ int fi_batch_autotune(fi_batch* b, int32_t* chosen4)
     for (fi_handle* h : b->hs)
         if (cudaStreamSynchronize(h->s) != cudaSuccess) return FI_E_CUDA;
     // the stencil of the reference stages reads now%w's float pair
-    for (fi_handle* h : b->hs)
+    for (fi_handle* h : b->hs) {
         if (h->d.whi) split_hilo(h->d.w, h->d.whi, h->d.wlo, h->n, b->s);
+        if (h->yhi) split_hilo_dxw(h->d.x, h->xhi, h->xlo, h->wrefhi, h->wreflo, h->dxw, h->n, b->s);
+    }
     auto time_of = [&](int part) { return b->mixed ? batch_time_rhs<float>(b, part, 3) : batch_time_rhs<double>(b, part, 3); };
     int sh[4] = {b->shape[0], b->shape[1], b->shape[2], b->shape[3]};
     auto try_shape = [&](const int* c, int part, float* t) -> int {

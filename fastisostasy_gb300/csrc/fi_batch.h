@@ -34,6 +34,11 @@ struct BMember {
     void* raw7[7];            // true stages: the seven stage outputs (T); raw7[0] = raw
     double* yst;              // true stages: stage state buffer (stages 1-5; stage 6 is d.ts_x2)
     const double* wref;       // true stages: w_ref of the mantle term
+    // true stages, mixed form (null otherwise): the float pair of x with
+    // dxw = (x - w_ref) of the pairs, the stage state's pair and dxw, and
+    // the pair of w_ref
+    float *xhi, *xlo, *xdw, *yhi, *ylo, *ydw;
+    const float *wrhi, *wrlo;
     int even;
     int RB, CB;               // rows per row block, columns per column block
     int fgx;                  // flexure blocks along x (FP64 tiles)

@@ -68,10 +68,11 @@ void launch_flexure(const double* y, const double* wref, const T* q0, const uint
 // x + (a h spy) (rprev - corner mean) from the float pair of x and the raw
 // RHS of the previous stage (null at the first stage); the mantle term takes
 // dxw = (xhi - w_ref,hi) + (xlo - w_ref,lo) per cell; h is read from the
-// control block.
+// control block.  With a gate, every block returns at once when it is 0.
 void launch_flexure_stage(const float* whi, const float* wlo, const float* rprev, const float* dxw, const float* q0,
                           const uint8_t* mask, const float* D, const float* inv2eta, float* f, int nx, int ny,
-                          const FlexCoef& c, const Ctl* ctl, double a, double spy, cudaStream_t s);
+                          const FlexCoef& c, const Ctl* ctl, double a, double spy, cudaStream_t s,
+                          const int* gate = nullptr);
 
 template <typename T>
 void launch_rows_fwd(const T* in, int in_pitch, int in_width, int nrows_in, typename vec2<T>::type* S,

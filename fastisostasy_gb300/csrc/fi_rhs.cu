@@ -562,8 +562,10 @@ __global__ void __launch_bounds__(256)
 k_flexure_strip_stage(const float* __restrict__ whi, const float* __restrict__ wlo, const float* __restrict__ rprev,
                       const float* __restrict__ dxw, const float* __restrict__ q0, const uint8_t* __restrict__ mask,
                       const float* __restrict__ D, const float* __restrict__ inv2eta, float* __restrict__ f, int nx,
-                      int ny, FlexCoefF c, int seg, const Ctl* __restrict__ ctl, double a, double spy)
+                      int ny, FlexCoefF c, int seg, const Ctl* __restrict__ ctl, double a, double spy,
+                      const int* __restrict__ gate)
 {
+    if (gate && *gate == 0) return;
     __shared__ float s_sc[2];
     if (threadIdx.x == 0) {
         s_sc[0] = rprev ? (float)(a * ctl->h * spy) : 0.f;
@@ -641,13 +643,14 @@ void launch_flexure(const double* y, const double* wref, const T* q0, const uint
 
 void launch_flexure_stage(const float* whi, const float* wlo, const float* rprev, const float* dxw, const float* q0,
                           const uint8_t* mask, const float* D, const float* inv2eta, float* f, int nx, int ny,
-                          const FlexCoef& c, const Ctl* ctl, double a, double spy, cudaStream_t s)
+                          const FlexCoef& c, const Ctl* ctl, double a, double spy, cudaStream_t s,
+                          const int* gate)
 {
     const FlexCoefF cf = flex_coef_f32(c);
     const int seg = strip_seg_single(nx, ny);
     const int tasks = ((nx + SW - 1) / SW) * ((ny + seg - 1) / seg);
     k_flexure_strip_stage<<<(tasks + 7) / 8, 256, 0, s>>>(whi, wlo, rprev, dxw, q0, mask, D, inv2eta, f, nx, ny, cf,
-                                                          seg, ctl, a, spy);
+                                                          seg, ctl, a, spy, gate);
 }
 
 // ---------------------------------------------------------------------------
@@ -1147,7 +1150,9 @@ void batch_rows_inv(const BMember* M, BList L, int nblk, int threads, size_t sme
 }
 
 // True stages: the RHS at stage state y (stage 0: x, 1-5: the stage buffer,
-// 6: x2) with the mantle term at that state, by shared-memory tiles.
+// 6: x2) with the mantle term at that state: mixed members by column strips
+// over the float pair of the stage state (stage 0: of x) and its dxw, FP64
+// members (and mixed ones without the pairs) by shared-memory tiles.
 template <typename T>
 __global__ void __launch_bounds__(256) k_b_flexure_y(const BMember* __restrict__ M, BList L, int stage)
 {
@@ -1156,8 +1161,19 @@ __global__ void __launch_bounds__(256) k_b_flexure_y(const BMember* __restrict__
         const int bx = local % b.fgx, by = local / b.fgx;
         const double* y = stage == 0 ? b.d.x : (stage == 6 ? b.d.ts_x2 : b.yst);
         if constexpr (sizeof(T) == 4) {
-            flexure_f32_body<false>(y, b.wref, (const float*)b.q0, b.mask, (const float*)b.D,
-                                    (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, b.fcf, bx, by);
+            if (b.yhi) {
+                const int task = local * 8 + (int)threadIdx.y;   // 32 x 8 block: warp = threadIdx.y
+                if (task < strip_tasks(b.p.nx, b.p.ny, b.fseg)) {
+                    const bool s0 = stage == 0;
+                    flexure_strip<true, true>(s0 ? b.xhi : b.yhi, s0 ? b.xlo : b.ylo, (const float*)b.q0, b.mask,
+                                              (const float*)b.D, (const float*)b.inv2eta, (float*)b.f, b.p.nx,
+                                              b.p.ny, b.fcf, b.fseg, task, nullptr, nullptr, nullptr, 0.f, 0.f,
+                                              s0 ? b.xdw : b.ydw);
+                }
+            } else {
+                flexure_f32_body<false>(y, b.wref, (const float*)b.q0, b.mask, (const float*)b.D,
+                                        (const float*)b.inv2eta, (float*)b.f, b.p.nx, b.p.ny, b.fcf, bx, by);
+            }
         } else {
             flexure_body<T>(y, b.wref, (const T*)b.q0, b.mask, (const T*)b.D, (const T*)b.inv2eta, (T*)b.f, b.p.nx,
                             b.p.ny, b.fc, bx, by);

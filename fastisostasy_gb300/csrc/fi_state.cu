@@ -869,6 +869,57 @@ __device__ __forceinline__ void dp_stage_body(const Ctl* __restrict__ c, double*
     }
 }
 
+// The same stage state in the mixed form as a float pair: the FP32
+// increment a of dp_stage_body added to the pair of x by an FP32 two-sum,
+// and dxw = (yhi - w_ref,hi) + (ylo - w_ref,lo), the state part of the
+// mantle term, so that the stencil takes no FP64 stage state; stage 6 (x2)
+// also in FP64 (x2 non-null) for the error estimate and the commit, the
+// same value dp_stage_body writes.
+__device__ __forceinline__ void dp_stage_pair_body(const Ctl* __restrict__ c, const float* __restrict__ xhi,
+                                                   const float* __restrict__ xlo, const float* __restrict__ wrhi,
+                                                   const float* __restrict__ wrlo, float* __restrict__ yhi,
+                                                   float* __restrict__ ylo, float* __restrict__ ydw,
+                                                   double* __restrict__ x2, const double* __restrict__ x,
+                                                   const DPRaw<float>& r, int i, int nx, int ny, double spy, int bid,
+                                                   int nblk)
+{
+    if (c->done) return;
+    __shared__ double cm[7];
+    dp_corner_means(c, r, i, nx, ny, cm);
+    const double h = c->h;
+    __shared__ float af[6], cmf[6];
+    if (threadIdx.x < (unsigned)i) {
+        af[threadIdx.x] = (float)(c_dp_a[i][threadIdx.x] * h * spy);
+        cmf[threadIdx.x] = (float)cm[threadIdx.x];
+    }
+    __syncthreads();
+    const size_t n = (size_t)nx * ny;
+    for (size_t e = (size_t)bid * NT + threadIdx.x; e < n; e += (size_t)nblk * NT) {
+        float a = 0.f;
+        for (int q = 0; q < i; ++q) a += af[q] * (r.p[q][e] - cmf[q]);
+        if (x2) x2[e] = x[e] + (double)a;
+        const float hi = xhi[e], lo = xlo[e];
+        const float sm = hi + a, bb = sm - hi;
+        const float er = (hi - (sm - bb)) + (a - bb);
+        const float l2 = lo + er;
+        const float h2 = sm + l2;
+        const float lo2 = l2 - (h2 - sm);
+        yhi[e] = h2;
+        ylo[e] = lo2;
+        ydw[e] = (h2 - wrhi[e]) + (lo2 - wrlo[e]);
+    }
+}
+
+__global__ void __launch_bounds__(NT)
+k_dp_stage_pair(const Ctl* __restrict__ c, const float* __restrict__ xhi, const float* __restrict__ xlo,
+                const float* __restrict__ wrhi, const float* __restrict__ wrlo, float* __restrict__ yhi,
+                float* __restrict__ ylo, float* __restrict__ ydw, double* __restrict__ x2,
+                const double* __restrict__ x, DPRaw<float> r, int i, int nx, int ny, double spy)
+{
+    dp_stage_pair_body(c, xhi, xlo, wrhi, wrlo, yhi, ylo, ydw, x2, x, r, i, nx, ny, spy, (int)blockIdx.x,
+                       (int)gridDim.x);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NT)
 k_dp_stage(const Ctl* __restrict__ c, double* __restrict__ y, const double* __restrict__ x, DPRaw<T> r, int i, int nx,
@@ -970,6 +1021,33 @@ __device__ __forceinline__ void ts_commit_body(Dom d, const T* __restrict__ raw,
         d.x[e] = x2;
         d.w[e] = x2;
     }
+}
+
+// Accepted attempt of the true-stage Tsit5 in the mixed form: x = x2 (FP64),
+// now%w = x, and the float pair of x with its dxw take those of the stage-6
+// state (the pair buffers still hold them).
+__device__ __forceinline__ void ts_commit_tpair_body(Dom d, float* __restrict__ xhi, float* __restrict__ xlo,
+                                                     float* __restrict__ xdw, const float* __restrict__ yhi,
+                                                     const float* __restrict__ ylo, const float* __restrict__ ydw,
+                                                     int bid, int nblk)
+{
+    const Ctl* c = d.ctl;
+    if (c->done || !c->accepted) return;
+    for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
+        const double x2 = d.ts_x2[e];
+        d.x[e] = x2;
+        d.w[e] = x2;
+        xhi[e] = yhi[e];
+        xlo[e] = ylo[e];
+        xdw[e] = ydw[e];
+    }
+}
+
+__global__ void __launch_bounds__(NT)
+k_ts_commit_tpair(Dom d, float* __restrict__ xhi, float* __restrict__ xlo, float* __restrict__ xdw,
+                  const float* __restrict__ yhi, const float* __restrict__ ylo, const float* __restrict__ ydw)
+{
+    ts_commit_tpair_body(d, xhi, xlo, xdw, yhi, ylo, ydw, (int)blockIdx.x, (int)gridDim.x);
 }
 
 template <typename T>
@@ -1219,7 +1297,8 @@ __global__ void __launch_bounds__(NT) k_b_ts_commit(const BMember* __restrict__ 
     batch_walk(L, [&](int m) { const Ctl* c = M[m].d.ctl; return c->done == 0 && c->accepted != 0; },
                [&](int m, int local) {
                    const BMember& b = M[m];
-                   ts_commit_body<T>(b.d, (const T*)b.raw, local, b.red_nblk);
+                   if (b.yhi) ts_commit_tpair_body(b.d, b.xhi, b.xlo, b.xdw, b.yhi, b.ylo, b.ydw, local, b.red_nblk);
+                   else ts_commit_body<T>(b.d, (const T*)b.raw, local, b.red_nblk);
                });
 }
 
@@ -1255,6 +1334,15 @@ __global__ void __launch_bounds__(NT) k_b_dp_stage(const BMember* __restrict__ M
 {
     batch_walk(L, [&](int m) { return M[m].d.ctl->done == 0; }, [&](int m, int local) {
         const BMember& b = M[m];
+        if constexpr (sizeof(T) == 4) {
+            if (b.yhi) {   // mixed members: the stage state as a float pair
+                dp_stage_pair_body(b.d.ctl, b.xhi, b.xlo, b.wrhi, b.wrlo, b.yhi, b.ylo, b.ydw,
+                                   i == 6 ? b.d.ts_x2 : nullptr, b.d.x, member_raw<T>(b), i, b.p.nx, b.p.ny, b.d.spy,
+                                   local, b.red_nblk);
+                __syncthreads();
+                return;
+            }
+        }
         dp_stage_body<T>(b.d.ctl, i == 6 ? b.d.ts_x2 : b.yst, b.d.x, member_raw<T>(b), i, b.p.nx, b.p.ny, b.d.spy,
                          local, b.red_nblk);
         __syncthreads();
@@ -1520,6 +1608,18 @@ void rk4_final(Ctl* c, double* x, double* w, const T* r1, const T* r2, const T* 
                double spy, cudaStream_t s)
 {
     k_rk4_final<T><<<grid_for((size_t)nx * ny), NT, 0, s>>>(c, x, w, r1, r2, r3, r4, nx, ny, spy);
+}
+void dp_stage_pair(const Ctl* c, const float* xhi, const float* xlo, const float* wrhi, const float* wrlo, float* yhi,
+                   float* ylo, float* ydw, double* x2, const double* x, const DPRaw<float>& r, int i, int nx, int ny,
+                   double spy, cudaStream_t s)
+{
+    k_dp_stage_pair<<<grid_for((size_t)nx * ny), NT, 0, s>>>(c, xhi, xlo, wrhi, wrlo, yhi, ylo, ydw, x2, x, r, i, nx,
+                                                             ny, spy);
+}
+void ts_commit_tpair(const Dom& d, float* xhi, float* xlo, float* xdw, const float* yhi, const float* ylo,
+                     const float* ydw, cudaStream_t s)
+{
+    k_ts_commit_tpair<<<ts_grid(d.n), NT, 0, s>>>(d, xhi, xlo, xdw, yhi, ylo, ydw);
 }
 void rk4_final_pair(Ctl* c, double* x, double* w, float* xhi, float* xlo, const float* wrhi, const float* wrlo,
                     float* dxw, const float* r1, const float* r2, const float* r3, const float* r4, int nx, int ny,

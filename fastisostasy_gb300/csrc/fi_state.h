@@ -64,6 +64,14 @@ void rk_stage(const Ctl* c, double* y, const double* x, const T* raw, double a, 
 template <typename T>
 void rk4_final(Ctl* c, double* x, double* w, const T* r1, const T* r2, const T* r3, const T* r4, int nx, int ny,
                double spy, cudaStream_t s);
+// true-stage Tsit5, mixed form: stage state i as a float pair (yhi, ylo) with
+// its dxw, x2 in FP64 at stage 6 (x2 non-null); the commit takes the
+// stage-6 pair into the pair of x
+void dp_stage_pair(const Ctl* c, const float* xhi, const float* xlo, const float* wrhi, const float* wrlo, float* yhi,
+                   float* ylo, float* ydw, double* x2, const double* x, const DPRaw<float>& r, int i, int nx, int ny,
+                   double spy, cudaStream_t s);
+void ts_commit_tpair(const Dom& d, float* xhi, float* xlo, float* xdw, const float* yhi, const float* ylo,
+                     const float* ydw, cudaStream_t s);
 // mixed RK4 combination that also advances the float pair xhi + xlo of x and
 // dxw = (xhi - wrhi) + (xlo - wrlo)
 void rk4_final_pair(Ctl* c, double* x, double* w, float* xhi, float* xlo, const float* wrhi, const float* wrlo,
