@@ -894,11 +894,15 @@ __device__ __forceinline__ void dp_stage_pair_body(const Ctl* __restrict__ c, co
     }
     __syncthreads();
     const size_t n = (size_t)nx * ny;
+    // read-only loads (the stage outputs come through a pointer array the
+    // compiler cannot tell apart from the stores) and several cells per
+    // thread in flight
+#pragma unroll 4
     for (size_t e = (size_t)bid * NT + threadIdx.x; e < n; e += (size_t)nblk * NT) {
         float a = 0.f;
-        for (int q = 0; q < i; ++q) a += af[q] * (r.p[q][e] - cmf[q]);
-        if (x2) x2[e] = x[e] + (double)a;
-        const float hi = xhi[e], lo = xlo[e];
+        for (int q = 0; q < i; ++q) a += af[q] * (__ldg(r.p[q] + e) - cmf[q]);
+        if (x2) x2[e] = __ldg(x + e) + (double)a;
+        const float hi = __ldg(xhi + e), lo = __ldg(xlo + e);
         const float sm = hi + a, bb = sm - hi;
         const float er = (hi - (sm - bb)) + (a - bb);
         const float l2 = lo + er;
@@ -906,7 +910,7 @@ __device__ __forceinline__ void dp_stage_pair_body(const Ctl* __restrict__ c, co
         const float lo2 = l2 - (h2 - sm);
         yhi[e] = h2;
         ylo[e] = lo2;
-        ydw[e] = (h2 - wrhi[e]) + (lo2 - wrlo[e]);
+        ydw[e] = (h2 - __ldg(wrhi + e)) + (lo2 - __ldg(wrlo + e));
     }
 }
 
@@ -960,11 +964,12 @@ __device__ __forceinline__ void dp_err_body(Dom d, const DPRaw<T>& r, double ato
         }
         __syncthreads();
         float m1 = 0.f, m2 = 0.f;
+#pragma unroll 4
         for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
             float dx = 0.f;
-            for (int q = 0; q < 7; ++q) dx += ce[q] * ((float)r.p[q][e] - cmf[q]);
+            for (int q = 0; q < 7; ++q) dx += ce[q] * ((float)__ldg(r.p[q] + e) - cmf[q]);
             ((float*)d.ts_dx)[e] = dx;
-            const float x2f = (float)d.ts_x2[e];
+            const float x2f = (float)__ldg(d.ts_x2 + e);
             m1 = fmaxf(m1, fabsf(x2f - dx));
             m2 = fmaxf(m2, fabsf(x2f));
         }
@@ -1033,13 +1038,14 @@ __device__ __forceinline__ void ts_commit_tpair_body(Dom d, float* __restrict__ 
 {
     const Ctl* c = d.ctl;
     if (c->done || !c->accepted) return;
+#pragma unroll 4
     for (size_t e = (size_t)bid * NT + threadIdx.x; e < d.n; e += (size_t)nblk * NT) {
-        const double x2 = d.ts_x2[e];
+        const double x2 = __ldg(d.ts_x2 + e);
         d.x[e] = x2;
         d.w[e] = x2;
-        xhi[e] = yhi[e];
-        xlo[e] = ylo[e];
-        xdw[e] = ydw[e];
+        xhi[e] = __ldg(yhi + e);
+        xlo[e] = __ldg(ylo + e);
+        xdw[e] = __ldg(ydw + e);
     }
 }
 
