@@ -145,19 +145,36 @@ def update_bytes(dom, precision, rk_steps=int(round(DTT / DT))):
     return dom.nx * dom.ny * (rk_steps * (6 * 8 + 27 * f) + 12 * f + 15 * f + 3)
 
 
-def ncu_traffic(kernel):
-    """DRAM bytes per launch of `kernel` (dram__bytes_read.sum +
-    dram__bytes_write.sum) from the committed ncu summaries in profiles/,
-    or None when no capture of it is committed."""
+def ncu_value(name, kernel):
+    """A figure `name[kernel] = value` of the committed ncu summaries in
+    profiles/, or None when no capture of it is committed."""
     import glob
     import re
-    pat = re.compile(r"traffic_per_launch\[%s\]\s*=\s*([0-9.eE+]+)" % re.escape(kernel))
+    pat = re.compile(r"%s\[%s\]\s*=\s*([0-9.eE+]+)" % (re.escape(name), re.escape(kernel)))
     for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
         with open(path) as fh:
             m = pat.search(fh.read())
         if m:
             return float(m.group(1))
     return None
+
+
+def l2_line(kernel, launch_us):
+    """The dominant kernel against the L2 instead of HBM: L2 bytes per launch
+    (lts__t_sectors.sum x 32 B) from the committed capture over this run's
+    launch time, and the capture's lts__throughput fraction of the L2 peak."""
+    b = ncu_value("l2_bytes_per_launch", kernel)
+    if not b or not launch_us:
+        return None
+    return {"bytes_per_launch": b, "achieved_gbs": b / (launch_us * 1e-6) / 1e9,
+            "frac_of_l2_peak_ncu": ncu_value("l2_throughput_frac", kernel),
+            "source": "lts__t_sectors.sum x 32 B and lts__throughput of the committed ncu capture"}
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` (dram__bytes_read.sum +
+    dram__bytes_write.sum) from the committed ncu summaries."""
+    return ncu_value("traffic_per_launch", kernel)
 
 
 def make_domain(precision, stage_mode=1):
@@ -1140,7 +1157,8 @@ def main():
                          "avg_launch_us": 1000.0 * tot_ms / cnt, "kernel_time_shares": shares,
                          "whole_update": {"algorithmic_bytes": upd,
                                           "achieved": upd / (r32["ms"] / 1000.0) / 1e9,
-                                          "frac": upd / (r32["ms"] / 1000.0) / 1e9 / peak}},
+                                          "frac": upd / (r32["ms"] / 1000.0) / 1e9 / peak},
+                         "l2": l2_line(dominant, 1000.0 * tot_ms / cnt)},
             "output_async": outp,
             "cpu_baseline": cpu,
             "configs": cfgs,
