@@ -963,6 +963,92 @@ def configs_leg():
     return res
 
 
+def horizons_leg(oracle_threads=None):
+    """Configurations 1-3 to their stated end times in both forms on the
+    GPU: configuration 1 (128^2, reference-compatible Tsit5) to 50 kyr with
+    the output every 1 kyr, configuration 2 (256^2, RK4 true stages, dt =
+    1 yr) to 20 kyr, configuration 3 (512 x 1024, interactive sea level,
+    reference-compatible Tsit5) to 10 kyr.  Wall time and simulated kyr/s
+    of each form, the mixed form's difference from the FP64 form at the end
+    (configuration 1: at every output), mask mismatches, and configuration
+    1 at 50 kyr against the oracle (every host core; the frozen RHS of the
+    reference's stages evaluated once per attempt, bit-identical)."""
+    from fastisostasy_gb300 import workloads as W
+    from fastisostasy_gb300.isostasy import Domain
+    from fastisostasy_gb300 import _lib
+
+    def run(wl, prec, stage_mode, t_end, out_every):
+        p = dict(wl.params)
+        if stage_mode is not None:
+            p["stage_mode"] = stage_mode
+        d = Domain(p, wl.nx_ice, wl.ny_ice, wl.dx, precision=prec)
+        f = wl.padded_fields(d.nx, d.ny)
+        if f:
+            d.set_fields(**f)
+        b = _lib.FiBsl()
+        b.method, b.constant_ocean_surface = 0, 1
+        b.A_ocean_pd = b.A_ocean_now = 3.625e14
+        d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+        a = time.perf_counter()
+        t = wl.dtt
+        d.update(wl.H_final, t, b)
+        outs = []
+        n = int(round(t_end / wl.dtt))
+        for k in range(2, n + 1):
+            t = k * wl.dtt
+            d.update_async(0, t, b)
+            if out_every and (k * wl.dtt) % out_every == 0:
+                outs.append(d.field("w"))   # waits for the update
+        d.synchronize()
+        secs = time.perf_counter() - a
+        sc = d.scalars()
+        res = {k: d.field(k) for k in ("w", "maskocean", "maskgrounded", "maskcontinent")}
+        d.close()
+        return secs, res, outs, sc
+
+    out = {}
+    cases = [("config1", W.config1(128), 0, 50e3, 1000.0), ("config2", W.config2(n=256), None, 20e3, None),
+             ("config3", W.config3(), None, 10e3, None)]
+    for name, wl, sm, t_end, every in cases:
+        s64, r64, o64, sc64 = run(wl, 0, sm, t_end, every)
+        s32, r32, o32, sc32 = run(wl, 1, sm, t_end, every)
+        wmax = max(np.abs(r64["w"]).max(), 1e-300)
+        e = {"t_end_yr": t_end, "fp64_s": s64, "mixed_s": s32, "fp64_kyr_s": t_end / 1e3 / s64,
+             "mixed_kyr_s": t_end / 1e3 / s32,
+             "err_mixed_vs_fp64_end": {"max_rel": float(np.abs(r32["w"] - r64["w"]).max() / wmax),
+                                       "rms_rel": float(np.sqrt(np.mean((r32["w"] - r64["w"]) ** 2)) / wmax)},
+             "mask_mismatch_end": {m: int(np.sum(r32[m] != r64[m]))
+                                   for m in ("maskocean", "maskgrounded", "maskcontinent")},
+             "steps": {"fp64": [sc64["n_accept"], sc64["n_reject"]], "mixed": [sc32["n_accept"], sc32["n_reject"]]}}
+        if o64:
+            e["err_mixed_vs_fp64_outputs_max"] = max(float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+                                                     for a, b in zip(o32, o64))
+        if name == "config1":
+            from oracle import oracle as O
+            O.set_threads(oracle_threads or os.cpu_count() or 1)
+            O.set_reuse_frozen(True)
+            m = O.Model(dict(wl.params, stage_mode=0), wl.nx_ice, wl.ny_ice, wl.dx, wl.dx)
+            f = wl.padded_fields(m.nx, m.ny)
+            if f:
+                m.set_fields(**f)
+            bo = O.make_bsl()
+            m.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, bo)
+            a = time.perf_counter()
+            for k in range(1, int(round(t_end / wl.dtt)) + 1):
+                rc = m.update(wl.H_final, k * wl.dtt, bo)
+                if rc:
+                    break
+            so = m.scalars()
+            wo = m.field("w")
+            e["oracle"] = {"s": time.perf_counter() - a, "rc": int(rc), "steps": [so["n_accept"], so["n_reject"]],
+                           "fp64_vs_oracle_max_rel": float(np.abs(r64["w"] - wo).max() / max(np.abs(wo).max(), 1e-300)),
+                           "mixed_vs_oracle_max_rel": float(np.abs(r32["w"] - wo).max() / max(np.abs(wo).max(), 1e-300))}
+            m.close()
+            O.set_reuse_frozen(False)
+        out[name] = e
+    return {"horizons": out}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -1026,7 +1112,7 @@ def main():
                     help="batched graphs or per-member streams for --only ensemble-true")
     ap.add_argument("--scale-sizes", default="1024,2048", help="grid sizes of --only scale")
     ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--only", choices=["ensemble", "ensemble-true", "serve", "configs", "scale", "oracle",
+    ap.add_argument("--only", choices=["ensemble", "ensemble-true", "serve", "configs", "horizons", "scale", "oracle",
                                        "engine-trace"],
                     help="run one secondary leg alone and print its JSON (for profiling), not a bench line")
     ap.add_argument("--lean", action="store_true",
@@ -1073,6 +1159,9 @@ def main():
         return 0
     if args.only == "configs":
         print(json.dumps({"configs": configs_leg()}))
+        return 0
+    if args.only == "horizons":
+        print(json.dumps(horizons_leg()))
         return 0
     if args.only == "scale":
         print(json.dumps({"scale": scale_leg(tuple(int(v) for v in args.scale_sizes.split(",")))}))
