@@ -625,6 +625,72 @@ def _sequential_fp64(wls, arrivals):
             "throughput_req_per_s": len(wls) / span}
 
 
+def ensemble_full_leg(n_members=256, horizon=10e3, n_seq=8):
+    """Configuration 4 at its stated extent: every member of the 256-member
+    ensemble (reference-compatible Tsit5, mixed form, batched graphs in two
+    stiffness groups) integrated to 10 kyr from no ice, handle set-up
+    excluded; beside it a sample of n_seq members (every 256/n_seq-th)
+    solved one after another in FP64 to the same horizon, with their
+    difference from the batched mixed result at the end.  The sequential
+    time of the whole ensemble is estimated from the sample (labelled as
+    such)."""
+    import torch
+    from fastisostasy_gb300 import workloads as W
+    from fastisostasy_gb300.isostasy import Domain
+    from fastisostasy_gb300.serve import Ensemble
+    from fastisostasy_gb300 import _lib
+    wls = [W.ensemble_member(i, stage_mode=0) for i in range(n_members)]
+    ens = Ensemble(wls, precision=1, mode="graph", groups=2)
+    torch.cuda.synchronize()
+    n = int(round(horizon / 10.0))
+    a = time.perf_counter()
+    err = None
+    try:
+        ens.first_update(10.0)
+        for k in range(2, n + 1):
+            ens.update(10.0 * k)
+        ens.synchronize()
+    except Exception as exc:   # a member that fails its update: reported, not raised
+        err = str(exc)
+    batched_s = time.perf_counter() - a
+    w_mixed = [d.field("w") for d in ens.doms]
+    sc = [d.scalars() for d in ens.doms]
+    ens.close()
+    idx = list(range(0, n_members, max(1, n_members // n_seq)))[:n_seq]
+    seq = []
+    for i in idx:
+        wl = wls[i]
+        d = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=0)
+        f = wl.padded_fields(d.nx, d.ny)
+        if f:
+            d.set_fields(**f)
+        b = _lib.FiBsl()
+        b.method, b.constant_ocean_surface = 0, 1
+        b.A_ocean_pd = b.A_ocean_now = 3.625e14
+        d.init_state(wl.z_bed, np.zeros_like(wl.H_final), 0.0, b)
+        a = time.perf_counter()
+        for k in range(1, n + 1):
+            d.update(wl.H_final, 10.0 * k, b)
+        secs = time.perf_counter() - a
+        w64 = d.field("w")
+        s64 = d.scalars()
+        d.close()
+        seq.append({"member": i, "n": wl.nx_ice, "fp64_s": secs,
+                    "err_mixed_vs_fp64": float(np.abs(w_mixed[i] - w64).max() / max(np.abs(w64).max(), 1e-300)),
+                    "attempts_fp64": s64["n_accept"] + s64["n_reject"],
+                    "attempts_mixed": sc[i]["n_accept"] + sc[i]["n_reject"]})
+    seq_est = sum(r["fp64_s"] for r in seq) * n_members / len(seq)
+    mkyr = n_members * horizon / 1000.0
+    return {"workload": "configuration 4 at its stated extent: %d members, reference-compatible Tsit5, mixed, "
+                        "batched graphs in 2 stiffness groups, 10 kyr each from no ice" % n_members,
+            "unit": "member-kyr/s", "batched_s": batched_s, "batched_mixed": mkyr / batched_s,
+            "t_end_yr": sc[0]["t"] if sc else None, "error": err,
+            "attempts": {"mean": float(np.mean([x["n_accept"] + x["n_reject"] for x in sc])),
+                         "max": float(np.max([x["n_accept"] + x["n_reject"] for x in sc]))},
+            "sequential_fp64_sample": seq,
+            "sequential_fp64_estimate_s": seq_est, "speedup_estimate": seq_est / batched_s}
+
+
 def ensemble_true_leg(n_members=64, n_updates=4, groups=2, mode="graph"):
     """Configuration 4's members in Tsit5 with true stages (Dormand-Prince
     5(4) with FSAL, the RHS at every stage state; no reference counterpart)
@@ -1112,7 +1178,8 @@ def main():
                     help="batched graphs or per-member streams for --only ensemble-true")
     ap.add_argument("--scale-sizes", default="1024,2048", help="grid sizes of --only scale")
     ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--only", choices=["ensemble", "ensemble-true", "serve", "configs", "horizons", "scale", "oracle",
+    ap.add_argument("--only", choices=["ensemble", "ensemble-true", "ensemble-full", "serve", "configs", "horizons",
+                                       "scale", "oracle",
                                        "engine-trace"],
                     help="run one secondary leg alone and print its JSON (for profiling), not a bench line")
     ap.add_argument("--lean", action="store_true",
@@ -1147,6 +1214,9 @@ def main():
         return 0
     if args.only == "serve":
         print(json.dumps({"serve": serve_leg(n_req=args.serve_requests)}))
+        return 0
+    if args.only == "ensemble-full":
+        print(json.dumps({"ensemble_full": ensemble_full_leg()}))
         return 0
     if args.only == "ensemble-true":
         print(json.dumps({"ensemble_true": ensemble_true_leg(groups=args.groups, mode=args.ensemble_mode)}))
