@@ -290,6 +290,7 @@ struct fi_handle {
     // step engine only: the half spectrum and the factors column-major
     // (element (l, k) at k*ny + l), so a spectrum column is contiguous
     void* ST = nullptr;
+    unsigned* eng_bar = nullptr;   // the step engine's grid-barrier counter
     void* mAT = nullptr;
     void* mBT = nullptr;
     void* S2 = nullptr;                  // convolution spectrum (T complex)
@@ -1035,7 +1036,9 @@ template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
     g.norm_scale_f = (float)g.norm_scale;
     g.fcf = flex_coef_f32(h->fc);
     g.trace = h->trace;
-    cudaError_t le = cudaSuccess;
+    g.bar = h->eng_bar;
+    cudaError_t le = cudaMemsetAsync(h->eng_bar, 0, sizeof(unsigned), h->s);
+    if (le != cudaSuccess && h->launch_err == cudaSuccess) h->launch_err = le;
     PROF(h, K_ENGINE, le = engine_launch<T>(g, h->eng_grid, h->eng_smem, h->s));
     if (le != cudaSuccess && h->launch_err == cudaSuccess) h->launch_err = le;
     h->launches += 1;
@@ -1374,6 +1377,7 @@ int decode_status(fi_handle* h, const Ctl* hc)
     case ST_LARGE: return fail(h, FI_E_LARGE, "large_check: large values detected (|w| %.3g, |we| %.3g, |dz_ss| %.3g)",
                                 hc->red[0], hc->red[1], hc->red[2]);
     case ST_STEP: return fail(h, FI_E_STEP, "adaptive step rejected too often");
+    case ST_TIMEOUT: return fail(h, FI_E_TIMEOUT, "step engine: a grid barrier wait expired");
     default: return fail(h, FI_E_CUDA, "unknown device status %d", hc->status);
     }
 }
@@ -1689,6 +1693,7 @@ int fi_create(const fi_params* pin, int nx_ice, int ny_ice, double dx, double dy
             if (h->engine_ok) {
                 const size_t nk = (size_t)(h->prhs.h + 1) * h->ny;
                 AL2(h->ST, nk * c2); AL2(h->mAT, nk * tsz(h)); AL2(h->mBT, nk * tsz(h));
+                AL2(h->eng_bar, sizeof(unsigned));
             }
         }
         if ((rk4_true || tsit_true) && mixed(h)) {

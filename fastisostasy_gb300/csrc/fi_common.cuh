@@ -75,7 +75,7 @@ struct Ctl {
 };
 
 // status codes (mirrors include/fi_gpu.h)
-enum { ST_OK = 0, ST_NAN = 1, ST_LARGE = 2, ST_STEP = 3 };
+enum { ST_OK = 0, ST_NAN = 1, ST_LARGE = 2, ST_STEP = 3, ST_TIMEOUT = 4 };
 
 __device__ __forceinline__ double corner_mean(const double c00, const double cnn, const double c0n,
                                               const double cn0)

@@ -423,6 +423,40 @@ __device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem
 
 // ---------------------------------------------------------------------------
 
+// Grid barrier of the cooperative launch (every block is resident): after
+// the block's barrier, thread 0 arrives with a release add on the launch's
+// counter and polls it with acquire loads until all blocks of this barrier
+// have arrived (the target grows by gridDim.x per barrier; the counter is
+// zeroed before the launch), then releases its block.  The release makes
+// the block's writes before the barrier visible at GPU scope to every
+// block whose acquire sees the count.  The wait is bounded: past kBarPolls
+// polls the block records ST_TIMEOUT and the kernel returns; the blocks
+// still waiting then run out of polls as well.
+constexpr long long kBarPolls = 1ll << 22;
+__device__ __forceinline__ bool grid_barrier(const EngineArgs& g, unsigned& target)
+{
+    __shared__ int s_bar_ok;
+    __syncthreads();
+    target += gridDim.x;
+    if (threadIdx.x == 0) {
+        asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(g.bar), "r"(1u) : "memory");
+        int ok = 1;
+        for (long long polls = 0;; ++polls) {
+            unsigned v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(g.bar) : "memory");
+            if (v >= target) break;
+            if (polls > kBarPolls) {
+                ok = 0;
+                g.ctl->status = ST_TIMEOUT;
+                break;
+            }
+        }
+        s_bar_ok = ok;
+    }
+    __syncthreads();
+    return s_bar_ok != 0;
+}
+
 // FM: the block-FFT index mode, FFT_POW2 when both transform lengths are
 // powers of two, else FFT_ANY
 template <typename T, int RA, int FM>
@@ -430,7 +464,7 @@ __global__ void __launch_bounds__(EngShape<RA>::threads, EngShape<RA>::per_sm) k
 {
     constexpr int RC = RA;
     extern __shared__ __align__(16) unsigned char smem[];
-    cg::grid_group grid = cg::this_grid();
+    unsigned bar_target = 0;   // arrivals expected at the next grid barrier
     const int nx = g.p.nx, ny = g.p.ny;
     const size_t n = (size_t)nx * ny;
     const int na = (ny + RA - 1) / RA, nb = (g.p.h + 1 + g.CB - 1) / g.CB, nc = (ny + RC - 1) / RC;
@@ -504,15 +538,15 @@ __global__ void __launch_bounds__(EngShape<RA>::threads, EngShape<RA>::per_sm) k
             for (int it = blockIdx.x; it < na; it += gridDim.x)
                 phase_a<T, RA, FM>(g, it * RA, stage, s_sdf[stage], smem, tw);
             TRACE();
-            grid.sync();
+            if (!grid_barrier(g, bar_target)) return;
             TRACE();
             for (int it = blockIdx.x; it < nb; it += gridDim.x) phase_b<T, FM>(g, it * g.CB, g.CB, smem, tw);
             TRACE();
-            grid.sync();
+            if (!grid_barrier(g, bar_target)) return;
             TRACE();
             for (int it = blockIdx.x; it < nc; it += gridDim.x) phase_c<T, RC, FM>(g, it * RC, (T*)g.raw[stage], smem, tw);
             TRACE();
-            grid.sync();
+            if (!grid_barrier(g, bar_target)) return;
             TRACE();
         }
         // phase D: x += h/6 (k1 + 2 k2 + 2 k3 + k4), w = x (+ hi/lo copy)
@@ -563,7 +597,7 @@ __global__ void __launch_bounds__(EngShape<RA>::threads, EngShape<RA>::per_sm) k
             }
         }
         TRACE();
-        grid.sync();
+        if (!grid_barrier(g, bar_target)) return;
         TRACE();
         if (threadIdx.x == 0 && step == 0) s_trk = -1;   // trace the first step only
     }

@@ -39,6 +39,7 @@ struct EngineArgs {
     double norm_scale;               // 1 / (nx*ny*1.) as the reference normalises
     float norm_scale_f;              // the same in float
     unsigned long long* trace;       // optional: %globaltimer at phase boundaries of the first step
+    unsigned* bar;                   // grid-barrier arrival counter, zeroed before the launch
 
     template <typename T> __device__ __forceinline__ const T* q0_T() const { return (const T*)q0; }
     template <typename T> __device__ __forceinline__ const T* D_T() const { return (const T*)D; }
