@@ -1037,6 +1037,12 @@ template <typename T> T* enqueue_engine(fi_handle* h, int nsteps)
     g.fcf = flex_coef_f32(h->fc);
     g.trace = h->trace;
     g.bar = h->eng_bar;
+    {
+        // test only: FI_ENGINE_BARRIER_PHANTOM=1 expects one arrival more than
+        // the grid has, so every barrier wait runs out (FI_E_TIMEOUT)
+        const char* e = getenv("FI_ENGINE_BARRIER_PHANTOM");
+        g.bar_phantom = (e && e[0] == '1') ? 1 : 0;
+    }
     cudaError_t le = cudaMemsetAsync(h->eng_bar, 0, sizeof(unsigned), h->s);
     if (le != cudaSuccess && h->launch_err == cudaSuccess) h->launch_err = le;
     PROF(h, K_ENGINE, le = engine_launch<T>(g, h->eng_grid, h->eng_smem, h->s));

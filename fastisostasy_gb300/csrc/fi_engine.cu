@@ -431,13 +431,14 @@ __device__ void phase_c(const EngineArgs& g, int j0, T* out, unsigned char* smem
 // the block's writes before the barrier visible at GPU scope to every
 // block whose acquire sees the count.  The wait is bounded: past kBarPolls
 // polls the block records ST_TIMEOUT and the kernel returns; the blocks
-// still waiting then run out of polls as well.
+// still waiting then run out of polls as well (bar_phantom > 0 makes every
+// wait expire so, for the test of this bound).
 constexpr long long kBarPolls = 1ll << 22;
 __device__ __forceinline__ bool grid_barrier(const EngineArgs& g, unsigned& target)
 {
     __shared__ int s_bar_ok;
     __syncthreads();
-    target += gridDim.x;
+    target += gridDim.x + (unsigned)g.bar_phantom;
     if (threadIdx.x == 0) {
         asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(g.bar), "r"(1u) : "memory");
         int ok = 1;

@@ -40,6 +40,7 @@ struct EngineArgs {
     float norm_scale_f;              // the same in float
     unsigned long long* trace;       // optional: %globaltimer at phase boundaries of the first step
     unsigned* bar;                   // grid-barrier arrival counter, zeroed before the launch
+    int bar_phantom;                 // test only: arrivals expected beyond the grid (a wait that expires)
 
     template <typename T> __device__ __forceinline__ const T* q0_T() const { return (const T*)q0; }
     template <typename T> __device__ __forceinline__ const T* D_T() const { return (const T*)D; }

@@ -170,6 +170,37 @@ def test_rejection_limit_returns_fi_e_step(precision):
     assert so["n_reject"] == 5
 
 
+def test_engine_barrier_wait_is_bounded(monkeypatch):
+    """The step engine's grid barrier polls a bounded number of times: with
+    one arrival that never comes (FI_ENGINE_BARRIER_PHANTOM, a test-only
+    phantom block), every block gives up at its first barrier, the update
+    fails with FI_E_TIMEOUT instead of hanging, and the device stays
+    usable: a new handle then integrates normally."""
+    import time
+    wl = W.config2(n=128, L=3000e3 * 128 / 256, dt=1.0, stage_mode=1)
+
+    def domain():
+        d = Domain(wl.params, wl.nx_ice, wl.ny_ice, wl.dx, precision=1)
+        d.set_fields(**wl.padded_fields(d.nx, d.ny))
+        b = gpu_bsl()
+        d.init_state(wl.z_bed, wl.H_at(0.0), 0.0, b)
+        return d, b
+
+    monkeypatch.setenv("FI_ENGINE_BARRIER_PHANTOM", "1")
+    d, b = domain()
+    a = time.perf_counter()
+    with pytest.raises(_lib.FiError) as e:
+        d.update(wl.H_at(10.0), 10.0, b)
+    assert e.value.code == _lib.FI_E_TIMEOUT
+    assert time.perf_counter() - a < 60.0
+    d.close()
+    monkeypatch.delenv("FI_ENGINE_BARRIER_PHANTOM")
+    d, b = domain()
+    d.update(wl.H_at(10.0), 10.0, b)
+    assert np.abs(d.field("w")).max() > 0
+    d.close()
+
+
 @pytest.mark.parametrize("dt_method", [2, 1, 0])
 def test_llra_load_at_the_corners(dt_method):
     """LLRA (test1b's method) under a load covering the whole domain: the
