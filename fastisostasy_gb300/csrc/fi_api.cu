@@ -291,6 +291,14 @@ struct fi_handle {
     // (element (l, k) at k*ny + l), so a spectrum column is contiguous
     void* ST = nullptr;
     unsigned* eng_bar = nullptr;   // the step engine's grid-barrier counter
+    // page-locked status of the caller's host arrays seen by fi_update (the
+    // same arrays come back every step; a stale entry only costs speed:
+    // cudaMemcpyAsync from pageable memory is still correct)
+    struct PinSeen {
+        const void* p;
+        bool pinned;
+    } pin_seen[16] = {};
+    int pin_next = 0;
     void* mAT = nullptr;
     void* mBT = nullptr;
     void* S2 = nullptr;                  // convolution spectrum (T complex)
@@ -2030,7 +2038,16 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
     if (!h->state_ready) return fail(h, FI_E_STATE, "fi_update before fi_init_state");
     const size_t ni = (size_t)h->nx_ice * h->ny_ice;
     int rc;
-    if (ni >= (1u << 16) && host_pinned(H_ice)) {
+    auto pinned = [&](const void* ptr) {
+        if (!ptr) return false;
+        for (const auto& e : h->pin_seen)
+            if (e.p == ptr) return e.pinned;
+        const bool pl = host_pinned(ptr);
+        h->pin_seen[h->pin_next] = {ptr, pl};
+        h->pin_next = (h->pin_next + 1) % 16;
+        return pl;
+    };
+    if (ni >= (1u << 16) && pinned(H_ice)) {
         CK(cudaMemcpyAsync(h->dH, H_ice, ni * 8, cudaMemcpyHostToDevice, h->s));
     } else {
         if (ni < (1u << 16)) memcpy(h->hpin, H_ice, ni * 8);
@@ -2049,8 +2066,8 @@ int fi_update(fi_handle* h, const double* H_ice, double time, fi_bsl* bsl, fi_ou
         for (int f = 0; f < 8; ++f) dst[f] = d8[f];
         for (int f = 0; f < 3; ++f) mdst[f] = m3[f];
         if (piped) {
-            for (int f = 0; f < 8; ++f) direct[f] = host_pinned(dst[f]);
-            for (int f = 0; f < 3; ++f) direct[8 + f] = host_pinned(mdst[f]);
+            for (int f = 0; f < 8; ++f) direct[f] = pinned(dst[f]);
+            for (int f = 0; f < 3; ++f) direct[8 + f] = pinned(mdst[f]);
         }
     }
     if (piped && h->ev_field.empty()) {
